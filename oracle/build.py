@@ -1,0 +1,65 @@
+"""Builds the oracle (test infrastructure only).
+
+* ``liboracle.so`` from rpd_oracle.c -- the CPU restatement of the reference's
+  RPD path, compiled with -ffp-contract=off so every float/double operation
+  is one IEEE-rounded step, as the reference's sources state them.
+* ``_ref/libref.so`` -- the reference's own clipping kernel
+  (src/rpd3d/convex_cell.cu) compiled for the CPU through ref_shim/, built
+  only when the reference sources are present (they are not on the GPU
+  machines; the tests that need it skip there).
+"""
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_ROOT = os.environ.get("RPD_REFERENCE_ROOT", "/root/reference")
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
+
+
+def _stale(out, srcs):
+    if not os.path.exists(out):
+        return True
+    t = os.path.getmtime(out)
+    return any(os.path.getmtime(s) > t for s in srcs)
+
+
+def build_oracle(force=False):
+    src = os.path.join(HERE, "rpd_oracle.c")
+    hdr = os.path.join(HERE, "rpd_oracle.h")
+    out = os.path.join(HERE, "liboracle.so")
+    if force or _stale(out, [src, hdr]):
+        _run(["gcc", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
+              "-std=gnu11", "-o", out, src, "-lm"])
+    return out
+
+
+def build_ref(force=False):
+    """Returns the path of _ref/libref.so, or None without reference sources."""
+    kernel = os.path.join(REF_ROOT, "src", "rpd3d", "convex_cell.cu")
+    if not os.path.exists(kernel):
+        return None
+    outdir = os.path.join(HERE, "_ref")
+    os.makedirs(outdir, exist_ok=True)
+    out = os.path.join(outdir, "libref.so")
+    drv = os.path.join(HERE, "ref_driver.cpp")
+    shim = os.path.join(HERE, "ref_shim", "cuda_runtime.h")
+    if force or _stale(out, [drv, shim, kernel]):
+        _run(["g++", "-O2", "-fPIC", "-shared", "-std=c++17", "-DNDEBUG",
+              "-ffp-contract=off", "-w", "-pthread",
+              "-I" + os.path.join(HERE, "ref_shim"),
+              "-I" + os.path.join(REF_ROOT, "include"),
+              "-I" + os.path.join(REF_ROOT, "src", "rpd3d"),
+              "-I" + os.path.join(REF_ROOT, "src", "rpd3d_base"),
+              "-x", "c++", drv, "-o", out])
+    return out
+
+
+if __name__ == "__main__":
+    print(build_oracle(force="-f" in sys.argv))
+    print(build_ref(force="-f" in sys.argv))

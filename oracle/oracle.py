@@ -1,0 +1,229 @@
+"""ctypes bindings of the oracle (test infrastructure only).
+
+Only tests/, the smoke check and bench.py's CPU-baseline leg import this
+module.  It wraps liboracle.so (the CPU restatement of libmat's RPD path) and,
+where the reference sources were present at build time, _ref/libref.so (the
+reference's own clipping kernel compiled for the CPU).
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+HEADER_DTYPE = np.dtype([
+    ("tet_id", "<i4"), ("site_id", "<i4"), ("status", "<i4"),
+    ("nb_v", "u1"), ("nb_p", "u1"), ("nb_e", "u1"), ("flags", "u1"),
+    ("offset", "<u8"), ("volume", "<f8"),
+])
+assert HEADER_DTYPE.itemsize == 32
+
+SUCCESS = 4
+
+_lib = None
+_ref = None
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build_oracle()
+        L = ctypes.CDLL(path)
+        vp, i32, i64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64
+        L.orc_payload_bytes.restype = ctypes.c_size_t
+        L.orc_payload_bytes.argtypes = [i32, i32, i32]
+        L.orc_mesh_adjacency.restype = i32
+        L.orc_mesh_adjacency.argtypes = [i32, i32, vp, vp, vp, vp, vp, vp]
+        L.orc_dense_e_adjs_size.restype = i64
+        L.orc_dense_e_adjs_size.argtypes = [i32]
+        L.orc_dense_e_adjs.restype = None
+        L.orc_dense_e_adjs.argtypes = [i32, i32, vp, vp, vp]
+        L.orc_knn.restype = None
+        L.orc_knn.argtypes = [i32, vp, i32, vp, vp, i32]
+        L.orc_candidate_pairs.restype = i64
+        L.orc_candidate_pairs.argtypes = [i32, vp, i32, vp, i32, vp, vp, vp,
+                                          i32, vp, vp, i64, i32]
+        L.orc_clip_cells.restype = i64
+        L.orc_clip_cells.argtypes = [i32, vp, vp, i32, vp, vp, vp, vp, vp, i32,
+                                     vp, vp, vp, i32, vp, vp, i32, vp, vp, i64,
+                                     vp, i32]
+        L.orc_det4x4_ref.restype = ctypes.c_double
+        L.orc_det4x4_ref.argtypes = [vp, vp, vp, vp]
+        L.orc_filter_sign.restype = i32
+        L.orc_filter_sign.argtypes = [vp, vp, vp, vp]
+        L.orc_bisector_key.restype = ctypes.c_float
+        L.orc_bisector_key.argtypes = [vp, vp]
+        _lib = L
+    return _lib
+
+
+def ref_lib():
+    """The reference's own clipper on the CPU, or None when unavailable."""
+    global _ref
+    if _ref is None:
+        path = _build.build_ref()
+        if path is None:
+            return None
+        L = ctypes.CDLL(path)
+        vp, i32, i64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64
+        L.ref_clip_cells.restype = i64
+        L.ref_clip_cells.argtypes = [i32, vp, i32, vp, vp, vp, vp, vp, i32, vp,
+                                     vp, vp, vp, i32, vp, i32, vp, vp, vp, i64,
+                                     i32]
+        _ref = L
+    return _ref
+
+
+def nthreads():
+    return max(1, os.cpu_count() or 1)
+
+
+def payload_bytes(nb_v, nb_p, nb_e):
+    return int(lib().orc_payload_bytes(int(nb_v), int(nb_p), int(nb_e)))
+
+
+def mesh_adjacency(n_vert, tets):
+    tets = np.ascontiguousarray(tets, dtype=np.int32)
+    n_tet = tets.shape[0]
+    v_adjs = np.zeros(n_vert, np.int32)
+    e_adj6 = np.zeros((n_tet, 6), np.uint8)
+    f_adjs = np.zeros((n_tet, 4), np.int32)
+    f_ids = np.zeros((n_tet, 4), np.int32)
+    nb = np.zeros(1, np.int32)
+    rc = lib().orc_mesh_adjacency(n_vert, n_tet, _p(tets), _p(v_adjs), _p(e_adj6),
+                                  _p(f_adjs), _p(f_ids), _p(nb))
+    if rc != 0:
+        raise ValueError("mesh adjacency failed (%d)" % rc)
+    return dict(v_adjs=v_adjs, e_adj6=e_adj6, f_adjs=f_adjs, f_ids=f_ids,
+                n_boundary_faces=int(nb[0]))
+
+
+def dense_e_adjs(n_vert, tets, e_adj6):
+    tets = np.ascontiguousarray(tets, dtype=np.int32)
+    n = int(lib().orc_dense_e_adjs_size(n_vert))
+    out = np.empty(n, np.int32)
+    lib().orc_dense_e_adjs(n_vert, tets.shape[0], _p(tets),
+                           _p(np.ascontiguousarray(e_adj6, np.uint8)), _p(out))
+    return out
+
+
+def knn(site4f, k, n_threads=None):
+    site4f = np.ascontiguousarray(site4f, dtype=np.float32)
+    n = site4f.shape[0]
+    nbr = np.empty((n, k), np.int32)
+    keys = np.empty((n, k), np.float32)
+    lib().orc_knn(n, _p(site4f), k, _p(nbr), _p(keys), n_threads or nthreads())
+    return nbr, keys
+
+
+def candidate_pairs(vert3f, tets, site4f, flags, nbr, n_threads=None):
+    vert3f = np.ascontiguousarray(vert3f, np.float32)
+    tets = np.ascontiguousarray(tets, np.int32)
+    site4f = np.ascontiguousarray(site4f, np.float32)
+    flags = np.ascontiguousarray(flags, np.uint32)
+    nbr = np.ascontiguousarray(nbr, np.int32)
+    n_tet = tets.shape[0]
+    offs = np.zeros(n_tet + 1, np.int32)
+    cap = max(16, 64 * n_tet)
+    while True:
+        sites = np.empty(cap, np.int32)
+        n = lib().orc_candidate_pairs(vert3f.shape[0], _p(vert3f), n_tet, _p(tets),
+                                      site4f.shape[0], _p(site4f), _p(flags),
+                                      _p(nbr), nbr.shape[1], _p(offs), _p(sites),
+                                      cap, n_threads or nthreads())
+        if n >= 0:
+            return offs, sites[:n].copy()
+        cap = int(offs[-1]) + 16
+
+
+def clip_cells(mesh, sites, nbr, offs, pair_sites, pred_mode=0, n_threads=None):
+    """mesh: dict(vert3d, tets, v_adjs, e_adj6, f_adjs, f_ids);
+    sites: float64 [n, 4] (x, y, z, w).  Returns (headers, payload, stats)."""
+    vert3d = np.ascontiguousarray(mesh["vert3d"], np.float64)
+    vert3f = vert3d.astype(np.float32)
+    site4d = np.ascontiguousarray(sites, np.float64)
+    site4f = site4d.astype(np.float32)
+    tets = np.ascontiguousarray(mesh["tets"], np.int32)
+    nbr = np.ascontiguousarray(nbr, np.int32)
+    offs = np.ascontiguousarray(offs, np.int32)
+    pair_sites = np.ascontiguousarray(pair_sites, np.int32)
+    n_pairs = int(offs[-1])
+    headers = np.zeros(max(n_pairs, 1), HEADER_DTYPE)
+    stats = np.zeros(2, np.int64)
+    cap = max(4096, 1024 * n_pairs)
+    for _ in range(3):
+        payload = np.zeros(cap, np.uint8)
+        used = lib().orc_clip_cells(
+            vert3d.shape[0], _p(vert3f), _p(vert3d), tets.shape[0], _p(tets),
+            _p(np.ascontiguousarray(mesh["v_adjs"], np.int32)),
+            _p(np.ascontiguousarray(mesh["e_adj6"], np.uint8)),
+            _p(np.ascontiguousarray(mesh["f_adjs"], np.int32)),
+            _p(np.ascontiguousarray(mesh["f_ids"], np.int32)),
+            site4d.shape[0], _p(site4f), _p(site4d), _p(nbr), nbr.shape[1],
+            _p(offs), _p(pair_sites), pred_mode, _p(headers), _p(payload), cap,
+            _p(stats), n_threads or nthreads())
+        if used >= 0:
+            return headers[:n_pairs], payload[:used], stats
+        last = headers[n_pairs - 1]
+        cap = int(last["offset"]) + payload_bytes(last["nb_v"], last["nb_p"], last["nb_e"]) + 16
+    raise RuntimeError("oracle payload sizing failed")
+
+
+def ref_clip_cells(mesh, sites, flags, nbr, offs, pair_sites, n_threads=None):
+    """Runs the reference's own kernel code (CPU build) on the same pairs.
+    Returns (headers, payload, thread_ids) or None without the reference."""
+    L = ref_lib()
+    if L is None:
+        return None
+    vert3f = np.ascontiguousarray(mesh["vert3d"], np.float64).astype(np.float32)
+    tets = np.ascontiguousarray(mesh["tets"], np.int32)
+    n_vert, n_tet = vert3f.shape[0], tets.shape[0]
+    site4f = np.ascontiguousarray(sites, np.float64).astype(np.float32)
+    n_site = site4f.shape[0]
+    vert_soa = np.ascontiguousarray(vert3f.T)
+    idx_soa = np.ascontiguousarray(tets.T)
+    site_soa = np.ascontiguousarray(site4f[:, :3].T)
+    site_w = np.ascontiguousarray(site4f[:, 3])
+    k = nbr.shape[1]
+    site_knn = np.full((k + 1, n_site), -1, np.int32)
+    site_knn[:k] = np.asarray(nbr, np.int32).T
+    counts = np.diff(offs)
+    tet_k = int(counts.max()) if n_tet else 0
+    tet_knn = np.full((max(tet_k, 1), n_tet), -1, np.int32)
+    for t in range(n_tet):
+        c = counts[t]
+        tet_knn[:c, t] = pair_sites[offs[t]:offs[t + 1]]
+    e_adjs = dense_e_adjs(n_vert, tets, mesh["e_adj6"])
+    n_pairs = int(offs[-1])
+    headers = np.zeros(max(n_pairs, 1), HEADER_DTYPE)
+    tids = np.zeros(max(n_pairs, 1), np.int32)
+    cap = max(4096, 1024 * n_pairs)
+    payload = np.zeros(cap, np.uint8)
+    used = L.ref_clip_cells(
+        n_vert, _p(vert_soa), n_tet, _p(idx_soa),
+        _p(np.ascontiguousarray(mesh["v_adjs"], np.int32)), _p(e_adjs),
+        _p(np.ascontiguousarray(mesh["f_adjs"], np.int32)),
+        _p(np.ascontiguousarray(mesh["f_ids"], np.int32)), n_site, _p(site_soa),
+        _p(site_w), _p(np.ascontiguousarray(flags, np.uint32)), _p(site_knn), k,
+        _p(tet_knn), tet_k, _p(headers), _p(tids), _p(payload), cap,
+        n_threads or nthreads())
+    if used < 0:
+        raise RuntimeError("reference payload capacity too small")
+    return headers[:n_pairs], payload[:used], tids[:n_pairs]
+
+
+def det4x4_ref(p1, p2, p3, e):
+    a = [np.ascontiguousarray(x, np.float32) for x in (p1, p2, p3, e)]
+    return float(lib().orc_det4x4_ref(*[_p(x) for x in a]))
+
+
+def filter_sign(p1, p2, p3, e):
+    a = [np.ascontiguousarray(x, np.float32) for x in (p1, p2, p3, e)]
+    return int(lib().orc_filter_sign(*[_p(x) for x in a]))

@@ -1,0 +1,882 @@
+/*
+ * rpd_oracle.c -- CPU restatement of libmat's RPD hot path (test
+ * infrastructure only; see rpd_oracle.h for the list of reference sources
+ * each part follows).  Build with -ffp-contract=off: the reference's float
+ * and double formulas are evaluated one IEEE-rounded operation at a time.
+ */
+#include "rpd_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define END ORC_END_OF_LIST
+
+/* ------------------------------------------------------------------ */
+/* payload layout                                                     */
+/* ------------------------------------------------------------------ */
+static size_t al16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+size_t orc_payload_bytes(int nb_v, int nb_p, int nb_e) {
+  size_t b = 0;
+  b += (size_t)16 * nb_p;          /* planes */
+  b += al16((size_t)8 * nb_p);     /* id2 */
+  b += al16((size_t)4 * nb_v);     /* ver */
+  b += al16((size_t)4 * nb_e);     /* edges */
+  b += al16((size_t)nb_p);         /* h */
+  b += al16((size_t)24 * nb_v);    /* xyz (double) */
+  return b;
+}
+
+/* ------------------------------------------------------------------ */
+/* mesh adjacency (io.cxx:238-335)                                    */
+/* ------------------------------------------------------------------ */
+/* local faces of a tet, as the reference's tet_faces_lvid
+ * (convex_cell.h:25-26): face i is opposite vertex i */
+static const int kFaceLv[4][3] = {{2, 1, 3}, {0, 2, 3}, {1, 0, 3}, {0, 1, 2}};
+/* local edges in the order the reference's cell constructor visits them
+ * (convex_cell.cu:193-211): (0,1) (0,2) (0,3) (1,2) (1,3) (2,3) */
+static const int kEdgeLv[6][2] = {{0, 1}, {0, 2}, {0, 3},
+                                  {1, 2}, {1, 3}, {2, 3}};
+/* the two tet faces meeting at each of those edges */
+static const int kEdgeFaces[6][2] = {{2, 3}, {1, 3}, {1, 2},
+                                     {0, 3}, {0, 2}, {0, 1}};
+
+typedef struct {
+  int32_t a, b, c;
+  int32_t idx;
+} key3;
+
+static int cmp_key3(const void* x, const void* y) {
+  const key3* p = (const key3*)x;
+  const key3* q = (const key3*)y;
+  if (p->a != q->a) return p->a < q->a ? -1 : 1;
+  if (p->b != q->b) return p->b < q->b ? -1 : 1;
+  if (p->c != q->c) return p->c < q->c ? -1 : 1;
+  return p->idx < q->idx ? -1 : (p->idx > q->idx);
+}
+
+static void sort3(int32_t* v) {
+  int32_t t;
+  if (v[0] > v[1]) { t = v[0]; v[0] = v[1]; v[1] = t; }
+  if (v[1] > v[2]) { t = v[1]; v[1] = v[2]; v[2] = t; }
+  if (v[0] > v[1]) { t = v[0]; v[0] = v[1]; v[1] = t; }
+}
+
+int orc_mesh_adjacency(int n_vert, int n_tet, const int32_t* tets,
+                       int32_t* v_adjs, uint8_t* e_adj6, int32_t* f_adjs,
+                       int32_t* f_ids, int32_t* n_boundary_faces) {
+  /* #tets per vertex */
+  for (int v = 0; v < n_vert; ++v) v_adjs[v] = 0;
+  for (int64_t i = 0; i < (int64_t)n_tet * 4; ++i) {
+    int v = tets[i];
+    if (v < 0 || v >= n_vert) return -1;
+    v_adjs[v]++;
+  }
+  /* #tets per edge: group the 6 edges of every tet */
+  int64_t ne = (int64_t)n_tet * 6;
+  key3* ek = (key3*)malloc(sizeof(key3) * (size_t)(ne > 0 ? ne : 1));
+  for (int t = 0; t < n_tet; ++t)
+    for (int e = 0; e < 6; ++e) {
+      int32_t a = tets[4 * t + kEdgeLv[e][0]], b = tets[4 * t + kEdgeLv[e][1]];
+      key3* k = &ek[(int64_t)t * 6 + e];
+      k->a = a < b ? a : b;
+      k->b = a < b ? b : a;
+      k->c = 0;
+      k->idx = t * 6 + e;
+    }
+  qsort(ek, (size_t)ne, sizeof(key3), cmp_key3);
+  for (int64_t s = 0; s < ne;) {
+    int64_t r = s;
+    while (r < ne && ek[r].a == ek[s].a && ek[r].b == ek[s].b) ++r;
+    for (int64_t q = s; q < r; ++q) e_adj6[ek[q].idx] = (uint8_t)(r - s);
+    s = r;
+  }
+  free(ek);
+  /* faces: count and ids */
+  int64_t nf = (int64_t)n_tet * 4;
+  key3* fk = (key3*)malloc(sizeof(key3) * (size_t)(nf > 0 ? nf : 1));
+  for (int t = 0; t < n_tet; ++t)
+    for (int f = 0; f < 4; ++f) {
+      int32_t v[3] = {tets[4 * t + kFaceLv[f][0]], tets[4 * t + kFaceLv[f][1]],
+                      tets[4 * t + kFaceLv[f][2]]};
+      sort3(v);
+      key3* k = &fk[(int64_t)t * 4 + f];
+      k->a = v[0];
+      k->b = v[1];
+      k->c = v[2];
+      k->idx = t * 4 + f;
+    }
+  qsort(fk, (size_t)nf, sizeof(key3), cmp_key3);
+  /* partner[i] = the other face slot sharing the face, -1 on the boundary */
+  int32_t* partner = (int32_t*)malloc(sizeof(int32_t) * (size_t)(nf > 0 ? nf : 1));
+  int bad = 0;
+  for (int64_t s = 0; s < nf;) {
+    int64_t r = s;
+    while (r < nf && fk[r].a == fk[s].a && fk[r].b == fk[s].b &&
+           fk[r].c == fk[s].c)
+      ++r;
+    if (r - s > 2) bad = 1;
+    for (int64_t q = s; q < r; ++q) {
+      f_adjs[fk[q].idx] = (int32_t)(r - s);
+      partner[fk[q].idx] = (r - s == 2) ? fk[q == s ? s + 1 : s].idx : -1;
+    }
+    s = r;
+  }
+  free(fk);
+  int32_t nb = 0;
+  for (int64_t i = 0; i < nf; ++i)
+    if (partner[i] < 0) f_ids[i] = nb++;
+  int32_t next = nb;
+  for (int64_t i = 0; i < nf; ++i) {
+    if (partner[i] < 0) continue;
+    if (partner[i] > i) f_ids[i] = next++;
+    else f_ids[i] = f_ids[partner[i]];
+  }
+  free(partner);
+  if (n_boundary_faces) *n_boundary_faces = nb;
+  return bad ? -2 : 0;
+}
+
+int64_t orc_dense_e_adjs_size(int n_vert) {
+  return (int64_t)n_vert * (1 + n_vert) / 2 + 1;
+}
+
+/* index of edge (v1, v2) in the dense triangular table, closed form of the
+ * reference's loop (convex_cell.h:46-59) */
+static int64_t dense_edge_idx(int64_t v1, int64_t v2, int64_t n) {
+  int64_t lo = v1 < v2 ? v1 : v2, hi = v1 < v2 ? v2 : v1;
+  return (lo + 1) * n - lo * (lo + 1) / 2 - (n - hi);
+}
+
+void orc_dense_e_adjs(int n_vert, int n_tet, const int32_t* tets,
+                      const uint8_t* e_adj6, int32_t* e_adjs) {
+  int64_t n = orc_dense_e_adjs_size(n_vert);
+  for (int64_t i = 0; i < n; ++i) e_adjs[i] = -1;
+  for (int t = 0; t < n_tet; ++t)
+    for (int e = 0; e < 6; ++e)
+      e_adjs[dense_edge_idx(tets[4 * t + kEdgeLv[e][0]],
+                            tets[4 * t + kEdgeLv[e][1]], n_vert)] =
+          e_adj6[6 * t + e];
+}
+
+/* ------------------------------------------------------------------ */
+/* neighbour lists                                                    */
+/* ------------------------------------------------------------------ */
+float orc_bisector_key(const float* si, const float* sj) {
+  float dx = sj[0] - si[0], dy = sj[1] - si[1], dz = sj[2] - si[2];
+  float d2 = dx * dx + dy * dy + dz * dz;
+  if (d2 == 0.0f) return sj[3] > si[3] ? -INFINITY : INFINITY;
+  float num = (d2 - sj[3]) + si[3];
+  float den = 2.0f * sqrtf(d2);
+  return num / den;
+}
+
+typedef struct {
+  float key;
+  int32_t id;
+} kv;
+
+static int cmp_kv(const void* x, const void* y) {
+  const kv* p = (const kv*)x;
+  const kv* q = (const kv*)y;
+  if (p->key < q->key) return -1;
+  if (p->key > q->key) return 1;
+  return p->id < q->id ? -1 : (p->id > q->id);
+}
+
+void orc_knn(int n_site, const float* site4, int k, int32_t* nbr, float* keys,
+             int n_threads) {
+#ifdef _OPENMP
+  if (n_threads > 0) omp_set_num_threads(n_threads);
+#pragma omp parallel
+#endif
+  {
+    kv* buf = (kv*)malloc(sizeof(kv) * (size_t)(n_site > 0 ? n_site : 1));
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 64)
+#endif
+    for (int i = 0; i < n_site; ++i) {
+      int m = 0;
+      for (int j = 0; j < n_site; ++j) {
+        if (j == i) continue;
+        buf[m].key = orc_bisector_key(site4 + 4 * (int64_t)i, site4 + 4 * (int64_t)j);
+        buf[m].id = j;
+        ++m;
+      }
+      qsort(buf, (size_t)m, sizeof(kv), cmp_kv);
+      for (int r = 0; r < k; ++r) {
+        nbr[(int64_t)i * k + r] = r < m ? buf[r].id : -1;
+        if (keys) keys[(int64_t)i * k + r] = r < m ? buf[r].key : INFINITY;
+      }
+    }
+    free(buf);
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* candidate pairs: voronoi.cu:154-193, knncuda.cu:21-94 + :130-160   */
+/* ------------------------------------------------------------------ */
+/* power distance of mesh vertex v to site s, in the reference's order:
+ * ((0 + t0^2) + t1^2) + t2^2, then minus the weight */
+static float pow_dist(const float* s, const float* v) {
+  float ssd = 0.0f, t;
+  t = s[0] - v[0];
+  ssd = ssd + t * t;
+  t = s[1] - v[1];
+  ssd = ssd + t * t;
+  t = s[2] - v[2];
+  ssd = ssd + t * t;
+  return ssd - s[3];
+}
+
+int64_t orc_candidate_pairs(int n_vert, const float* vert3, int n_tet,
+                            const int32_t* tets, int n_site,
+                            const float* site4, const uint32_t* flags,
+                            const int32_t* nbr, int k, int32_t* tet_offsets,
+                            int32_t* pair_sites, int64_t capacity,
+                            int n_threads) {
+  (void)n_vert;
+  int32_t* cnt = (int32_t*)calloc((size_t)n_tet + 1, sizeof(int32_t));
+  uint8_t* rel = NULL;
+  /* first pass: counts; second pass: fill (same deterministic test) */
+  for (int pass = 0; pass < 2; ++pass) {
+#ifdef _OPENMP
+    if (n_threads > 0) omp_set_num_threads(n_threads);
+#pragma omp parallel for schedule(dynamic, 64)
+#endif
+    for (int t = 0; t < n_tet; ++t) {
+      const float* tv[4];
+      for (int q = 0; q < 4; ++q) tv[q] = vert3 + 3 * (int64_t)tets[4 * t + q];
+      int32_t c = 0;
+      int32_t base = pass ? tet_offsets[t] : 0;
+      for (int i = 0; i < n_site; ++i) {
+        if (flags[i] != 1u) continue;
+        float pdi[4];
+        for (int q = 0; q < 4; ++q) pdi[q] = pow_dist(site4 + 4 * (int64_t)i, tv[q]);
+        int ok = 1;
+        for (int r = 0; r < k && ok; ++r) {
+          int m = nbr[(int64_t)i * k + r];
+          if (m == -1) continue; /* voronoi.cu:171 skips, does not stop */
+          int hit = 0;
+          for (int q = 0; q < 4 && !hit; ++q)
+            if (pow_dist(site4 + 4 * (int64_t)m, tv[q]) > pdi[q]) hit = 1;
+          ok = hit;
+        }
+        if (ok) {
+          if (pass && base + c < capacity) pair_sites[base + c] = i;
+          ++c;
+        }
+      }
+      if (!pass) cnt[t] = c;
+    }
+    if (!pass) {
+      tet_offsets[0] = 0;
+      for (int t = 0; t < n_tet; ++t) tet_offsets[t + 1] = tet_offsets[t] + cnt[t];
+      if (tet_offsets[n_tet] > capacity) {
+        free(cnt);
+        return -1;
+      }
+    }
+  }
+  (void)rel;
+  free(cnt);
+  return tet_offsets[n_tet];
+}
+
+/* ------------------------------------------------------------------ */
+/* the convex cell (convex_cell.h:117-185, convex_cell.cu:116-774)    */
+/* ------------------------------------------------------------------ */
+typedef struct {
+  float pl[ORC_MAX_P][4];
+  int32_t id2[ORC_MAX_P][2];
+  uint8_t h[ORC_MAX_P];
+  uint8_t ver[ORC_MAX_T][4];
+  uint8_t edge[ORC_MAX_E][3];
+  uint8_t bnext[ORC_MAX_P];
+  int nb_v, nb_p, nb_e, nb_r;
+  int first;
+  int status;
+  float seed[4];
+  int seed_id;
+  int pred_mode;
+  int64_t n_pred, n_esc;
+} cell_t;
+
+/* include/common_cuda.h:195-213 in double */
+static double det4x4d(double a11, double a12, double a13, double a14,
+                      double a21, double a22, double a23, double a24,
+                      double a31, double a32, double a33, double a34,
+                      double a41, double a42, double a43, double a44) {
+  double m12 = a21 * a12 - a11 * a22;
+  double m13 = a31 * a12 - a11 * a32;
+  double m14 = a41 * a12 - a11 * a42;
+  double m23 = a31 * a22 - a21 * a32;
+  double m24 = a41 * a22 - a21 * a42;
+  double m34 = a41 * a32 - a31 * a42;
+  double m123 = m23 * a13 - m13 * a23 + m12 * a33;
+  double m124 = m24 * a13 - m14 * a23 + m12 * a43;
+  double m134 = m34 * a13 - m14 * a33 + m13 * a43;
+  double m234 = m34 * a23 - m24 * a33 + m23 * a43;
+  return (m234 * a14 - m134 * a24 + m124 * a34 - m123 * a44);
+}
+
+double orc_det4x4_ref(const float* p1, const float* p2, const float* p3,
+                      const float* e) {
+  return det4x4d(p1[0], p2[0], p3[0], e[0], p1[1], p2[1], p3[1], e[1], p1[2],
+                 p2[2], p3[2], e[2], p1[3], p2[3], p3[3], e[3]);
+}
+
+/* include/common_cuda.h:153-166 in float */
+static float det2x2f(float a11, float a12, float a21, float a22) {
+  return a11 * a22 - a12 * a21;
+}
+static float det3x3f(float a11, float a12, float a13, float a21, float a22,
+                     float a23, float a31, float a32, float a33) {
+  return a11 * det2x2f(a22, a23, a32, a33) - a21 * det2x2f(a12, a13, a32, a33) +
+         a31 * det2x2f(a12, a13, a22, a23);
+}
+
+/* FP32 static filter.  det4x4(p1,p2,p3,e) = sum_r e_r K_r where K_r are the
+ * signed 3x3 minors of the three vertex planes.  K_r is evaluated in FP32
+ * with FMA (error <= gamma_5 * permanent), the dot with e adds gamma_4.  The
+ * bound also covers the reference's own FP64 evaluation error (gamma_9 of
+ * double precision times the 4x4 permanent), so a decided sign equals the
+ * sign the reference's FP64 determinant returns. */
+static void minor3(float a1, float b1, float c1, float a2, float b2, float c2,
+                   float a3, float b3, float c3, float* det, float* perm) {
+  float u1 = fmaf(b2, c3, -(b3 * c2));
+  float u2 = fmaf(a2, c3, -(a3 * c2));
+  float u3 = fmaf(a2, b3, -(a3 * b2));
+  *det = fmaf(a1, u1, fmaf(-b1, u2, c1 * u3));
+  float v1 = fmaf(fabsf(b2), fabsf(c3), fabsf(b3) * fabsf(c2));
+  float v2 = fmaf(fabsf(a2), fabsf(c3), fabsf(a3) * fabsf(c2));
+  float v3 = fmaf(fabsf(a2), fabsf(b3), fabsf(a3) * fabsf(b2));
+  *perm = fmaf(fabsf(a1), v1, fmaf(fabsf(b1), v2, fabsf(c1) * v3));
+}
+
+/* cofactors K[4] and the largest 3x3 permanent M of the vertex (p1,p2,p3) */
+static void vertex_cofactors(const float* p1, const float* p2, const float* p3,
+                             float* K, float* M) {
+  float d, pm, mx = 0.0f;
+  /* rows y z w */
+  minor3(p1[1], p1[2], p1[3], p2[1], p2[2], p2[3], p3[1], p3[2], p3[3], &d, &pm);
+  K[0] = -d;
+  mx = fmaxf(mx, pm);
+  /* rows x z w */
+  minor3(p1[0], p1[2], p1[3], p2[0], p2[2], p2[3], p3[0], p3[2], p3[3], &d, &pm);
+  K[1] = d;
+  mx = fmaxf(mx, pm);
+  /* rows x y w */
+  minor3(p1[0], p1[1], p1[3], p2[0], p2[1], p2[3], p3[0], p3[1], p3[3], &d, &pm);
+  K[2] = -d;
+  mx = fmaxf(mx, pm);
+  /* rows x y z */
+  minor3(p1[0], p1[1], p1[2], p2[0], p2[1], p2[2], p3[0], p3[1], p3[2], &d, &pm);
+  K[3] = d;
+  mx = fmaxf(mx, pm);
+  *M = mx;
+}
+
+/* filter constants: 5u for the dot, 6u for the cofactor and FP64 terms,
+ * u = 2^-24; absolute floor for underflow */
+#define FILT_C1 (5.0f * 5.9604645e-08f)
+#define FILT_C2 (6.0f * 5.9604645e-08f)
+#define FILT_ABS 1e-30f
+
+static int filter_sign_k(const float* K, float M, const float* e) {
+  float s = fmaf(e[3], K[3], fmaf(e[2], K[2], fmaf(e[1], K[1], e[0] * K[0])));
+  float t = fmaf(fabsf(e[3]), fabsf(K[3]),
+                 fmaf(fabsf(e[2]), fabsf(K[2]),
+                      fmaf(fabsf(e[1]), fabsf(K[1]), fabsf(e[0]) * fabsf(K[0]))));
+  float se = (fabsf(e[0]) + fabsf(e[1])) + (fabsf(e[2]) + fabsf(e[3]));
+  float b = fmaf(FILT_C1, t, FILT_C2 * (M * se)) + FILT_ABS;
+  if (s > b) return 1;
+  if (s < -b) return -1;
+  return 0;
+}
+
+int orc_filter_sign(const float* p1, const float* p2, const float* p3,
+                    const float* e) {
+  float K[4], M;
+  vertex_cofactors(p1, p2, p3, K, &M);
+  return filter_sign_k(K, M, e);
+}
+
+static int plane_eq(const float* a, const float* b) {
+  return a[0] == b[0] && a[1] == b[1] && a[2] == b[2] && a[3] == b[3];
+}
+
+/* convex_cell.cu:437-500 (cc_vertex_is_in_conflict_double) */
+static int in_conflict(cell_t* c, const uint8_t* v, const float* e) {
+  const float* p1 = c->pl[v[0]];
+  const float* p2 = c->pl[v[1]];
+  const float* p3 = c->pl[v[2]];
+  if (plane_eq(e, p1) || plane_eq(e, p2) || plane_eq(e, p3)) return 0;
+  c->n_pred++;
+  if (c->pred_mode == 1) {
+    int s = orc_filter_sign(p1, p2, p3, e);
+    if (s != 0) return s > 0;
+    c->n_esc++;
+  }
+  double det = orc_det4x4_ref(p1, p2, p3, e);
+  return det > 0.0;
+}
+
+/* tri2plane (common_cuda.h:248-254) on the face vertices */
+static void tri2plane_f(const float* v0, const float* v1, const float* v2,
+                        float* out) {
+  float ax = v1[0] - v0[0], ay = v1[1] - v0[1], az = v1[2] - v0[2];
+  float bx = v2[0] - v0[0], by = v2[1] - v0[1], bz = v2[2] - v0[2];
+  float nx = ay * bz - az * by;
+  float ny = az * bx - ax * bz;
+  float nz = ax * by - ay * bx;
+  out[0] = nx;
+  out[1] = ny;
+  out[2] = nz;
+  out[3] = -(v0[0] * nx + v0[1] * ny + v0[2] * nz);
+}
+
+/* new_plane (convex_cell.cu:561-592): bisector of seed S and site B, normal
+ * towards S, weights added for the power diagram */
+static void bisector_f(const float* S, const float* B, float* out) {
+  float dx = S[0] - B[0], dy = S[1] - B[1], dz = S[2] - B[2];
+  float ax = S[0] + B[0], ay = S[1] + B[1], az = S[2] + B[2];
+  float dot = (ax * dx + ay * dy + az * dz) + (B[3] - S[3]);
+  out[0] = dx;
+  out[1] = dy;
+  out[2] = dz;
+  out[3] = -dot / 2.f;
+}
+
+static void cell_init(cell_t* c, const float* vert3, const int32_t* tv,
+                      const int32_t* v_adjs, const uint8_t* e6,
+                      const int32_t* fa, const int32_t* fi) {
+  c->first = END;
+  memset(c->bnext, END, sizeof(c->bnext));
+  c->status = ORC_SUCCESS;
+  for (int i = 0; i < 4; ++i) {
+    tri2plane_f(vert3 + 3 * (int64_t)tv[kFaceLv[i][0]],
+                vert3 + 3 * (int64_t)tv[kFaceLv[i][1]],
+                vert3 + 3 * (int64_t)tv[kFaceLv[i][2]], c->pl[i]);
+    c->h[i] = (uint8_t)fa[i];
+    c->id2[i][0] = fi[i];
+    c->id2[i][1] = -1;
+  }
+  c->nb_p = 4;
+  static const uint8_t tri[4][3] = {{1, 3, 2}, {0, 2, 3}, {0, 3, 1}, {0, 1, 2}};
+  for (int i = 0; i < 4; ++i) {
+    c->ver[i][0] = tri[i][0];
+    c->ver[i][1] = tri[i][1];
+    c->ver[i][2] = tri[i][2];
+    c->ver[i][3] = (uint8_t)v_adjs[tv[i]];
+  }
+  c->nb_v = 4;
+  for (int e = 0; e < 6; ++e) {
+    c->edge[e][0] = (uint8_t)kEdgeFaces[e][0];
+    c->edge[e][1] = (uint8_t)kEdgeFaces[e][1];
+    c->edge[e][2] = e6[e];
+  }
+  c->nb_e = 6;
+}
+
+static int find_edge(const cell_t* c, int p1, int p2) {
+  int lo = p1 < p2 ? p1 : p2, hi = p1 < p2 ? p2 : p1;
+  for (int e = 0; e < c->nb_e; ++e)
+    if (c->edge[e][0] == lo && c->edge[e][1] == hi) return e;
+  return -1;
+}
+
+static void swap_ver(cell_t* c, int a, int b) {
+  uint8_t t[4];
+  memcpy(t, c->ver[a], 4);
+  memcpy(c->ver[a], c->ver[b], 4);
+  memcpy(c->ver[b], t, 4);
+}
+
+/* convex_cell.cu:618-678 */
+static void compute_boundary(cell_t* c) {
+  memset(c->bnext, END, sizeof(c->bnext));
+  c->first = END;
+  int nb_iter = 0;
+  int t = c->nb_v;
+  while (c->nb_r > 0) {
+    if (nb_iter++ > 65535) {
+      c->status = ORC_INCONSISTENT_BOUNDARY;
+      return;
+    }
+    const uint8_t* tr = c->ver[t];
+    int in_border[3], opp[3];
+    for (int e = 0; e < 3; ++e) in_border[e] = c->bnext[tr[e]] != END;
+    for (int e = 0; e < 3; ++e) opp[e] = c->bnext[tr[(e + 1) % 3]] == tr[e];
+    int simple = 1;
+    for (int e = 0; e < 3; ++e)
+      if (!opp[e] && !opp[(e + 1) % 3] && in_border[(e + 1) % 3]) simple = 0;
+    if (!opp[0] && !opp[1] && !opp[2]) {
+      if (c->first == END) {
+        for (int e = 0; e < 3; ++e) c->bnext[tr[e]] = tr[(e + 1) % 3];
+        c->first = tr[0];
+      } else {
+        simple = 0;
+      }
+    }
+    if (!simple) {
+      t++;
+      if (t == c->nb_v + c->nb_r) t = c->nb_v;
+      continue;
+    }
+    for (int e = 0; e < 3; ++e)
+      if (!opp[e]) c->bnext[tr[e]] = tr[(e + 1) % 3];
+    for (int e = 0; e < 3; ++e)
+      if (opp[e] && opp[(e + 1) % 3]) {
+        if (c->first == tr[(e + 1) % 3]) c->first = c->bnext[tr[(e + 1) % 3]];
+        c->bnext[tr[(e + 1) % 3]] = END;
+      }
+    swap_ver(c, t, c->nb_v + c->nb_r - 1);
+    t = c->nb_v;
+    c->nb_r--;
+  }
+}
+
+/* convex_cell.cu:274-316: a new vertex whose three planes have a zero
+ * float 3x3 determinant cannot be represented */
+static void check_perturb(cell_t* c, int i, int j, int k) {
+  const float* a = c->pl[i];
+  const float* b = c->pl[j];
+  const float* d = c->pl[k];
+  float w = det3x3f(a[0], a[1], a[2], b[0], b[1], b[2], d[0], d[1], d[2]);
+  if (w == 0.f) c->status = ORC_NEEDS_PERTURB;
+}
+
+/* convex_cell.cu:680-774 */
+static void clip_by_site(cell_t* c, const float* site4, int nid) {
+  if (c->nb_p >= ORC_MAX_P) {
+    c->status = ORC_VERTEX_OVERFLOW;
+    return;
+  }
+  int cur = c->nb_p;
+  const float* B = site4 + 4 * (int64_t)nid;
+  bisector_f(c->seed, B, c->pl[cur]);
+  c->h[cur] = 1;
+  c->id2[cur][0] = c->seed_id < nid ? c->seed_id : nid;
+  c->id2[cur][1] = c->seed_id < nid ? nid : c->seed_id;
+  c->nb_p++;
+  const float* e = c->pl[cur];
+  c->nb_r = 0;
+  int i = 0;
+  while (i < c->nb_v) {
+    if (in_conflict(c, c->ver[i], e)) {
+      c->nb_v--;
+      swap_ver(c, i, c->nb_v);
+      c->nb_r++;
+    } else {
+      i++;
+    }
+  }
+  if (c->nb_r == 0) {
+    c->nb_p--;
+    return;
+  }
+  if (c->nb_v == 0) {
+    c->status = ORC_NO_INTERSECTION;
+    return;
+  }
+  compute_boundary(c);
+  if (c->status != ORC_SUCCESS) return;
+  if (c->first == END) return;
+  int cir = c->first;
+  do {
+    if (c->nb_e >= ORC_MAX_E) {
+      c->status = ORC_EDGE_OVERFLOW;
+      return;
+    }
+    int lo = cur < cir ? cur : cir, hi = cur < cir ? cir : cur;
+    uint8_t ha = c->h[cur], hb = c->h[cir];
+    c->edge[c->nb_e][0] = (uint8_t)lo;
+    c->edge[c->nb_e][1] = (uint8_t)hi;
+    c->edge[c->nb_e][2] = ha > hb ? ha : hb;
+    c->nb_e++;
+    cir = c->bnext[cir];
+  } while (cir != c->first);
+  cir = c->first;
+  do {
+    int nx = c->bnext[cir];
+    if (c->nb_v + 1 >= ORC_MAX_T) {
+      c->status = ORC_TRIANGLE_OVERFLOW;
+    } else {
+      int e1 = find_edge(c, cur, cir), e2 = find_edge(c, cur, nx),
+          e3 = find_edge(c, cir, nx);
+      if (e1 < 0 || e2 < 0 || e3 < 0) {
+        /* the reference reads out of bounds here (assert compiled out);
+         * treat as an inconsistent cell */
+        c->status = ORC_INCONSISTENT_BOUNDARY;
+        return;
+      }
+      uint8_t adj = c->edge[e1][2];
+      if (c->edge[e2][2] > adj) adj = c->edge[e2][2];
+      if (c->edge[e3][2] > adj) adj = c->edge[e3][2];
+      c->ver[c->nb_v][0] = (uint8_t)cur;
+      c->ver[c->nb_v][1] = (uint8_t)cir;
+      c->ver[c->nb_v][2] = (uint8_t)nx;
+      c->ver[c->nb_v][3] = adj;
+      c->nb_v++;
+    }
+    check_perturb(c, cur, cir, nx);
+    if (c->status != ORC_SUCCESS) return;
+    cir = nx;
+  } while (cir != c->first);
+}
+
+/* ------------------------------------------------------------------ */
+/* FP64 reconstruction                                                */
+/* ------------------------------------------------------------------ */
+static void tri2plane_d(const double* v0, const double* v1, const double* v2,
+                        double* out) {
+  double ax = v1[0] - v0[0], ay = v1[1] - v0[1], az = v1[2] - v0[2];
+  double bx = v2[0] - v0[0], by = v2[1] - v0[1], bz = v2[2] - v0[2];
+  double nx = ay * bz - az * by;
+  double ny = az * bx - ax * bz;
+  double nz = ax * by - ay * bx;
+  out[0] = nx;
+  out[1] = ny;
+  out[2] = nz;
+  out[3] = -(v0[0] * nx + v0[1] * ny + v0[2] * nz);
+}
+
+static void bisector_d(const double* S, const double* B, double* out) {
+  double dx = S[0] - B[0], dy = S[1] - B[1], dz = S[2] - B[2];
+  double ax = S[0] + B[0], ay = S[1] + B[1], az = S[2] + B[2];
+  double dot = (ax * dx + ay * dy + az * dz) + (B[3] - S[3]);
+  out[0] = dx;
+  out[1] = dy;
+  out[2] = dz;
+  out[3] = -dot * 0.5;
+}
+
+static double det3d(double a11, double a12, double a13, double a21, double a22,
+                    double a23, double a31, double a32, double a33) {
+  return a11 * (a22 * a33 - a23 * a32) - a21 * (a12 * a33 - a13 * a32) +
+         a31 * (a12 * a23 - a13 * a22);
+}
+
+/* intersection of three planes (homogeneous Cramer, as the reference's
+ * compute_vertex_coordinates, convex_cell.cu:319-351) */
+static void vertex_d(const double* a, const double* b, const double* c,
+                     double* out) {
+  double x = -det3d(a[3], a[1], a[2], b[3], b[1], b[2], c[3], c[1], c[2]);
+  double y = -det3d(a[0], a[3], a[2], b[0], b[3], b[2], c[0], c[3], c[2]);
+  double z = -det3d(a[0], a[1], a[3], b[0], b[1], b[3], c[0], c[1], c[3]);
+  double w = det3d(a[0], a[1], a[2], b[0], b[1], b[2], c[0], c[1], c[2]);
+  out[0] = x / w;
+  out[1] = y / w;
+  out[2] = z / w;
+}
+
+static void project_d(const double* P, const double* pl, double* out) {
+  double n2 = pl[0] * pl[0] + pl[1] * pl[1] + pl[2] * pl[2];
+  double lam =
+      n2 > 0.0 ? (pl[0] * P[0] + pl[1] * P[1] + pl[2] * P[2] + pl[3]) / n2 : 0.0;
+  out[0] = P[0] - lam * pl[0];
+  out[1] = P[1] - lam * pl[1];
+  out[2] = P[2] - lam * pl[2];
+}
+
+/* signed volume of one vertex's 6 flag tets (convex_cell.cu:986-1069):
+ * C = seed, A = vertex, P[2i] = foot of C on face i, P[2i+1] = foot of C on
+ * the edge line between faces i and i+1 */
+static double vertex_volume_d(const double* C, const double* A,
+                              const double* f0, const double* f1,
+                              const double* f2) {
+  const double* f[3] = {f0, f1, f2};
+  double P[6][3];
+  for (int i = 0; i < 3; ++i) project_d(C, f[i], P[2 * i]);
+  for (int i = 0; i < 3; ++i) {
+    /* the edge between faces i and i+1 runs along n_i x n_(i+1); the foot of
+     * C on that line is the projection of A onto the plane through C with
+     * that normal */
+    const double* u = f[i];
+    const double* v = f[(i + 1) % 3];
+    double n[4] = {u[1] * v[2] - u[2] * v[1], u[2] * v[0] - u[0] * v[2],
+                   u[0] * v[1] - u[1] * v[0], 0.0};
+    n[3] = -(C[0] * n[0] + C[1] * n[1] + C[2] * n[2]);
+    project_d(A, n, P[2 * i + 1]);
+  }
+  double vol = 0.0;
+  for (int i = 0; i < 6; ++i) {
+    const double* p = P[i];
+    const double* q = P[(i + 1) % 6];
+    double a0 = p[0] - A[0], a1 = p[1] - A[1], a2 = p[2] - A[2];
+    double b0 = q[0] - A[0], b1 = q[1] - A[1], b2 = q[2] - A[2];
+    double c0 = C[0] - A[0], c1 = C[1] - A[1], c2 = C[2] - A[2];
+    vol += -det3d(a0, a1, a2, b0, b1, b2, c0, c1, c2) / 6.0;
+  }
+  return vol;
+}
+
+/* ------------------------------------------------------------------ */
+/* per-pair driver (convex_cell.cu:1166-1337)                         */
+/* ------------------------------------------------------------------ */
+static int64_t emit_payload(const cell_t* c, const double* vert3d,
+                            const int32_t* tv, const double* site4d,
+                            uint8_t* out, double* volume) {
+  int np = c->nb_p, nv = c->nb_v, ne = c->nb_e;
+  uint8_t* p = out;
+  memcpy(p, c->pl, (size_t)16 * np);
+  p += 16 * np;
+  memset(p, 0, al16((size_t)8 * np));
+  memcpy(p, c->id2, (size_t)8 * np);
+  p += al16((size_t)8 * np);
+  memset(p, 0, al16((size_t)4 * nv));
+  memcpy(p, c->ver, (size_t)4 * nv);
+  p += al16((size_t)4 * nv);
+  memset(p, 0, al16((size_t)4 * ne));
+  for (int e = 0; e < ne; ++e) {
+    p[4 * e + 0] = c->edge[e][0];
+    p[4 * e + 1] = c->edge[e][1];
+    p[4 * e + 2] = c->edge[e][2];
+    p[4 * e + 3] = 0;
+  }
+  p += al16((size_t)4 * ne);
+  memset(p, 0, al16((size_t)np));
+  memcpy(p, c->h, (size_t)np);
+  p += al16((size_t)np);
+  /* FP64 planes from FP64 inputs */
+  double pd[ORC_MAX_P][4];
+  for (int i = 0; i < 4 && i < np; ++i)
+    tri2plane_d(vert3d + 3 * (int64_t)tv[kFaceLv[i][0]],
+                vert3d + 3 * (int64_t)tv[kFaceLv[i][1]],
+                vert3d + 3 * (int64_t)tv[kFaceLv[i][2]], pd[i]);
+  const double* S = site4d + 4 * (int64_t)c->seed_id;
+  for (int i = 4; i < np; ++i) {
+    int other = c->id2[i][0] == c->seed_id ? c->id2[i][1] : c->id2[i][0];
+    bisector_d(S, site4d + 4 * (int64_t)other, pd[i]);
+  }
+  double* xyz = (double*)p;
+  double vol = 0.0;
+  for (int v = 0; v < nv; ++v) {
+    const uint8_t* t = c->ver[v];
+    vertex_d(pd[t[0]], pd[t[1]], pd[t[2]], xyz + 3 * v);
+    vol += vertex_volume_d(S, xyz + 3 * v, pd[t[0]], pd[t[1]], pd[t[2]]);
+  }
+  p += al16((size_t)24 * nv);
+  *volume = vol;
+  return (int64_t)(p - out);
+}
+
+typedef struct {
+  uint8_t* buf;
+  int64_t size, cap;
+} tbuf_t;
+
+static uint8_t* tbuf_reserve(tbuf_t* b, int64_t n) {
+  if (b->size + n > b->cap) {
+    int64_t nc = b->cap ? b->cap * 2 : (1 << 20);
+    while (nc < b->size + n) nc *= 2;
+    b->buf = (uint8_t*)realloc(b->buf, (size_t)nc);
+    b->cap = nc;
+  }
+  return b->buf + b->size;
+}
+
+int64_t orc_clip_cells(int n_vert, const float* vert3, const double* vert3d,
+                       int n_tet, const int32_t* tets, const int32_t* v_adjs,
+                       const uint8_t* e_adj6, const int32_t* f_adjs,
+                       const int32_t* f_ids, int n_site, const float* site4,
+                       const double* site4d, const int32_t* nbr, int k,
+                       const int32_t* tet_offsets, const int32_t* pair_sites,
+                       int pred_mode, orc_cell_header* headers,
+                       uint8_t* payload, int64_t payload_capacity,
+                       int64_t* stats, int n_threads) {
+  (void)n_vert;
+  (void)n_site;
+  int64_t n_pairs = tet_offsets[n_tet];
+  int nthr = 1;
+#ifdef _OPENMP
+  if (n_threads > 0) omp_set_num_threads(n_threads);
+  nthr = omp_get_max_threads();
+#endif
+  tbuf_t* tb = (tbuf_t*)calloc((size_t)nthr, sizeof(tbuf_t));
+  /* per pair: owning thread and offset in that thread's buffer */
+  int32_t* own = (int32_t*)malloc(sizeof(int32_t) * (size_t)(n_pairs > 0 ? n_pairs : 1));
+  int64_t* loff = (int64_t*)malloc(sizeof(int64_t) * (size_t)(n_pairs > 0 ? n_pairs : 1));
+  int64_t tot_pred = 0, tot_esc = 0;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 16) reduction(+ : tot_pred, tot_esc)
+#endif
+  for (int t = 0; t < n_tet; ++t) {
+    int me = 0;
+#ifdef _OPENMP
+    me = omp_get_thread_num();
+#endif
+    cell_t c;
+    for (int32_t q = tet_offsets[t]; q < tet_offsets[t + 1]; ++q) {
+      int s = pair_sites[q];
+      c.pred_mode = pred_mode;
+      c.n_pred = c.n_esc = 0;
+      c.seed_id = s;
+      memcpy(c.seed, site4 + 4 * (int64_t)s, sizeof(float) * 4);
+      cell_init(&c, vert3, tets + 4 * (int64_t)t, v_adjs, e_adj6 + 6 * (int64_t)t,
+                f_adjs + 4 * (int64_t)t, f_ids + 4 * (int64_t)t);
+      for (int r = 0; r < k; ++r) {
+        int nid = nbr[(int64_t)s * k + r];
+        if (nid == -1) break;
+        clip_by_site(&c, site4, nid);
+        if (c.status != ORC_SUCCESS) break;
+      }
+      tot_pred += c.n_pred;
+      tot_esc += c.n_esc;
+      orc_cell_header* h = &headers[q];
+      h->tet_id = t;
+      h->site_id = s;
+      h->status = c.status;
+      h->flags = 0;
+      h->offset = 0;
+      h->volume = 0.0;
+      h->nb_v = h->nb_p = h->nb_e = 0;
+      own[q] = me;
+      loff[q] = -1;
+      if (c.status == ORC_SUCCESS) {
+        h->nb_v = (uint8_t)c.nb_v;
+        h->nb_p = (uint8_t)c.nb_p;
+        h->nb_e = (uint8_t)c.nb_e;
+        int64_t need = (int64_t)orc_payload_bytes(c.nb_v, c.nb_p, c.nb_e);
+        uint8_t* dst = tbuf_reserve(&tb[me], need);
+        double vol = 0.0;
+        emit_payload(&c, vert3d, tets + 4 * (int64_t)t, site4d, dst, &vol);
+        h->volume = vol;
+        loff[q] = tb[me].size;
+        tb[me].size += need;
+      }
+    }
+  }
+  int64_t off = 0;
+  for (int64_t q = 0; q < n_pairs; ++q) {
+    headers[q].offset = (uint64_t)off;
+    if (headers[q].status == ORC_SUCCESS)
+      off += (int64_t)orc_payload_bytes(headers[q].nb_v, headers[q].nb_p,
+                                        headers[q].nb_e);
+  }
+  if (stats) {
+    stats[0] = tot_pred;
+    stats[1] = tot_esc;
+  }
+  if (off <= payload_capacity && payload) {
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+    for (int64_t q = 0; q < n_pairs; ++q) {
+      if (headers[q].status != ORC_SUCCESS) continue;
+      memcpy(payload + headers[q].offset, tb[own[q]].buf + loff[q],
+             orc_payload_bytes(headers[q].nb_v, headers[q].nb_p,
+                               headers[q].nb_e));
+    }
+  }
+  for (int i = 0; i < nthr; ++i) free(tb[i].buf);
+  free(tb);
+  free(own);
+  free(loff);
+  return off <= payload_capacity ? off : -1;
+}

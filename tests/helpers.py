@@ -1,0 +1,58 @@
+"""Shared helpers for the tests: golden-case unpacking and cell comparison."""
+import numpy as np
+
+from oracle import oracle as O
+
+SUCCESS = 4
+
+
+def mesh_of(case):
+    return dict(vert3d=case["vert3d"], tets=case["tets"], v_adjs=case["v_adjs"],
+                e_adj6=case["e_adj6"], f_adjs=case["f_adjs"], f_ids=case["f_ids"])
+
+
+def ref_headers(case):
+    return case["ref_headers"].reshape(-1).view(O.HEADER_DTYPE)
+
+
+def section_sizes(nb_v, nb_p, nb_e):
+    a = lambda x: (x + 15) // 16 * 16  # noqa: E731
+    return dict(plane=16 * nb_p, id2=a(8 * nb_p), ver=a(4 * nb_v), edge=a(4 * nb_e),
+                h=a(nb_p), xyz=a(24 * nb_v))
+
+
+def topo_bytes(payload, off, nb_v, nb_p, nb_e):
+    s = section_sizes(int(nb_v), int(nb_p), int(nb_e))
+    n = s["plane"] + s["id2"] + s["ver"] + s["edge"] + s["h"]
+    return payload[int(off):int(off) + n]
+
+
+def xyz_of(payload, off, nb_v, nb_p, nb_e):
+    s = section_sizes(int(nb_v), int(nb_p), int(nb_e))
+    start = int(off) + s["plane"] + s["id2"] + s["ver"] + s["edge"] + s["h"]
+    return payload[start:start + 24 * int(nb_v)].view(np.float64).reshape(-1, 3)
+
+
+def compare_cells(h1, p1, h2, p2):
+    """Bit-exact comparison of two packed cell sets over the same pairs:
+    statuses, counts and the topology/plane bytes of every emitted cell.
+    Returns the number of differing pairs."""
+    assert len(h1) == len(h2)
+    bad = 0
+    for f in ("tet_id", "site_id", "status", "nb_v", "nb_p", "nb_e"):
+        bad += int((h1[f] != h2[f]).sum())
+    if bad:
+        return bad
+    ok = np.flatnonzero(h1["status"] == SUCCESS)
+    for q in ok:
+        a = topo_bytes(p1, h1["offset"][q], h1["nb_v"][q], h1["nb_p"][q], h1["nb_e"][q])
+        b = topo_bytes(p2, h2["offset"][q], h2["nb_v"][q], h2["nb_p"][q], h2["nb_e"][q])
+        if not np.array_equal(a, b):
+            bad += 1
+    return bad
+
+
+def tet_volumes(vert, tets):
+    a = vert[tets[:, 0]]
+    return np.abs(np.einsum("ij,ij->i", np.cross(vert[tets[:, 1]] - a, vert[tets[:, 2]] - a),
+                            vert[tets[:, 3]] - a)) / 6.0
