@@ -1,0 +1,194 @@
+/*
+ * rpd_gb300.h -- C ABI of the GB300-native restricted power diagram (RPD)
+ * engine (librpd_gb300.so).
+ *
+ * It replaces the reference's GPU RPD entry point
+ *   compute_clipped_voro_diagram_GPU(...)      src/rpd3d/voronoi.h:52-61
+ * (host driver src/rpd3d/voronoi.cu:455-795, hot kernel
+ *  clipped_voro_cell_test_GPU_param_tet, src/rpd3d/convex_cell.cu:1166-1337)
+ * with a context object, plain pointers and sizes, and status codes.  The
+ * C++ signature of the reference (returning std::vector<ConvexCellHost>) is
+ * kept as a thin shim in rpd_gb300_compat.hpp on top of this ABI.
+ *
+ * Ownership: the caller owns every input buffer (they are copied into the
+ * context's device memory); the context owns its device buffers and one
+ * CUDA stream.  Views returned by rpd_get_cells stay valid until the next
+ * rpd_compute or rpd_destroy.  No function calls exit(); every failure is a
+ * status code, with a message in rpd_last_error().  One context per host
+ * thread at a time.
+ */
+#ifndef RPD_GB300_H
+#define RPD_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RPD_GB300_ABI_VERSION 1
+
+typedef enum rpd_status {
+  RPD_OK = 0,
+  RPD_ERR_INVALID_ARGUMENT = 1,
+  RPD_ERR_CUDA = 2,
+  RPD_ERR_OUT_OF_MEMORY = 3,
+  RPD_ERR_NOT_READY = 4,  /* compute before mesh / sites / neighbours set */
+  RPD_ERR_CAPACITY = 5,   /* a size limit of the call was exceeded */
+  RPD_ERR_NO_DEVICE = 6
+} rpd_status;
+
+/* How each conflict predicate sign is obtained.  The predicate is the
+ * reference's: sign of det4x4 of the vertex's three float planes and the new
+ * float plane, evaluated in FP64 (convex_cell.cu:437-500), tie = no
+ * conflict. */
+typedef enum rpd_predicate_mode {
+  RPD_PRED_FP64 = 0,        /* FP64 determinant for every predicate */
+  RPD_PRED_FP32_FILTER = 1  /* FP32 cofactor filter with a proven error
+                               bound; FP64 determinant only when the filter
+                               cannot decide.  Same signs as RPD_PRED_FP64. */
+} rpd_predicate_mode;
+
+/* Where the per-site neighbour lists come from. */
+typedef enum rpd_neighbor_source {
+  RPD_NEIGH_USER = 0, /* rpd_set_neighbors (e.g. libmat's RT neighbours) */
+  RPD_NEIGH_KNN = 1   /* built on the GPU: k smallest power-bisector
+                         distances, uniform-grid search */
+} rpd_neighbor_source;
+
+/* Clipping order inside a GPU-built list. */
+typedef enum rpd_clip_order {
+  RPD_ORDER_SITE_ID = 0,  /* ascending site id, as the reference's sorted
+                             std::set lists (triangulation.cxx:324-352) */
+  RPD_ORDER_DISTANCE = 1  /* ascending bisector distance */
+} rpd_clip_order;
+
+typedef struct rpd_config {
+  int device;            /* CUDA device ordinal */
+  int predicate_mode;    /* rpd_predicate_mode */
+  int neighbor_source;   /* rpd_neighbor_source */
+  int knn_k;             /* list length for RPD_NEIGH_KNN, 1..128 */
+  int clip_order;        /* rpd_clip_order (RPD_NEIGH_KNN only) */
+  int compute_geometry;  /* 1: FP64 vertex coordinates and cell volumes */
+  int warps_per_block;   /* clip kernel block size in warps, 0 = default */
+  int blocks_per_sm;     /* persistent grid: blocks per SM, 0 = default */
+  int reserved[8];
+} rpd_config;
+
+/* One record per candidate (tet, site) pair; 32 bytes. */
+typedef struct rpd_cell_header {
+  int32_t tet_id;
+  int32_t site_id;
+  int32_t status;      /* reference Status value; 4 = success (emitted) */
+  uint8_t nb_v, nb_p, nb_e, flags;
+  uint64_t offset;     /* payload byte offset (emitted cells) */
+  double volume;       /* FP64 cell volume (compute_geometry) */
+} rpd_cell_header;
+
+/* Payload of an emitted cell at `offset`, sections 16-byte aligned:
+ *   float  plane[nb_p][4]  (a, b, c, d) of a*x+b*y+c*z+d >= 0 (inside)
+ *   int32  id2[nb_p][2]    (face id, -1) for tet faces, (min, max) site ids
+ *                          for bisectors -- ConvexCellHost::clip_id2_data_trans
+ *   uint8  ver[nb_v][4]    (plane, plane, plane, #adjacent cells)
+ *   uint8  edge[nb_e][4]   (plane_min, plane_max, #adjacent cells, 0)
+ *   uint8  h[nb_p]         #adjacent cells of each face
+ *   double xyz[nb_v][3]    FP64 vertex coordinates (compute_geometry) */
+size_t rpd_payload_bytes(int nb_v, int nb_p, int nb_e);
+
+typedef struct rpd_stats {
+  int64_t n_pairs;            /* candidate (tet, site) pairs clipped */
+  int64_t n_cells;            /* emitted cells (status success) */
+  int64_t status_counts[10];  /* per reference status value 0..8, [9] other */
+  int64_t n_predicates;       /* conflict predicates evaluated */
+  int64_t n_escalated;        /* of those, decided by the FP64 determinant */
+  int64_t payload_bytes;      /* payload bytes written */
+  int32_t tet_k;              /* max pairs of one tet (reference's tet_k) */
+  int32_t knn_k;              /* neighbour list length used */
+  float ms_total;             /* device time of rpd_compute, CUDA events */
+  float ms_knn, ms_pairs, ms_clip, ms_compact;
+} rpd_stats;
+
+typedef struct rpd_cells_view {
+  int64_t n_cells;                 /* emitted cells, (tet, site) ascending */
+  const rpd_cell_header* headers;  /* device pointer, n_cells records */
+  const uint8_t* payload;          /* device pointer */
+  int64_t payload_bytes;
+  int64_t n_pairs;                 /* all pairs, including dropped ones */
+  const rpd_cell_header* pair_headers; /* device pointer, n_pairs records */
+} rpd_cells_view;
+
+const char* rpd_status_string(rpd_status s);
+void rpd_config_default(rpd_config* cfg);
+
+rpd_status rpd_create(const rpd_config* cfg, struct rpd_ctx** out);
+void rpd_destroy(struct rpd_ctx* ctx);
+const char* rpd_last_error(const struct rpd_ctx* ctx);
+
+/* Tet mesh (replaces copy_tet_data + load_num_adjacent_cells_and_ids,
+ * voronoi.cu:324-415).  xyz: n_vert x 3 doubles; tets: n_tet x 4 vertex
+ * ids, positively oriented; v_adjs: #tets per vertex; e_adj6: #tets per
+ * tet edge, edges (0,1)(0,2)(0,3)(1,2)(1,3)(2,3) -- the per-tet form of the
+ * reference's dense e_adjs table (io.cxx:264-281); f_adjs, f_ids: per tet
+ * face (face i opposite vertex i), as load_tet_adj_info (io.cxx:238-335). */
+rpd_status rpd_set_mesh(struct rpd_ctx* ctx, const double* xyz, int n_vert,
+                        const int32_t* tets, int n_tet, const int32_t* v_adjs,
+                        const uint8_t* e_adj6, const int32_t* f_adjs,
+                        const int32_t* f_ids);
+
+/* Sites: xyzw = n_site x 4 doubles (centre, weight = squared radius);
+ * flags: 1 = compute this site's cells (SiteFlag::is_selected,
+ * voronoi_common.h:7), 0 = neighbour only.  flags may be NULL (all 1). */
+rpd_status rpd_set_sites(struct rpd_ctx* ctx, const double* xyzw, int n_site,
+                         const uint32_t* flags);
+
+/* User neighbour lists.  layout 0: row-major n_site x k, -1 padded;
+ * layout 1: the reference's site_knn, (k + 1) rows x n_site
+ * (triangulation.cxx:324-352).  Each list is clipped in its given order up
+ * to its first -1 (convex_cell.cu:1255-1259). */
+rpd_status rpd_set_neighbors(struct rpd_ctx* ctx, const int32_t* nbr, int k,
+                             int layout);
+
+/* Runs the whole path on the device: neighbour lists (RPD_NEIGH_KNN),
+ * candidate pairs (the reference's rule, voronoi.cu:154-193), clipping,
+ * compaction.  Blocks until done.  stats may be NULL. */
+rpd_status rpd_compute(struct rpd_ctx* ctx, rpd_stats* stats);
+
+rpd_status rpd_get_cells(struct rpd_ctx* ctx, rpd_cells_view* view);
+
+/* Copies the emitted cells to host memory.  Pass NULL buffers to query the
+ * sizes first. */
+rpd_status rpd_copy_cells_to_host(struct rpd_ctx* ctx, rpd_cell_header* headers,
+                                  int64_t max_cells, void* payload,
+                                  int64_t payload_capacity, int64_t* n_cells,
+                                  int64_t* payload_bytes);
+
+/* The headers of every candidate pair of the last rpd_compute (dropped
+ * cells included, with their failure status), in (tet, site) order. */
+rpd_status rpd_copy_pair_headers_to_host(struct rpd_ctx* ctx, rpd_cell_header* headers,
+                                         int64_t capacity, int64_t* n_pairs);
+
+/* The neighbour lists used by the last rpd_compute (n_site x k, -1 padded),
+ * copied to the host.  k_out receives k. */
+rpd_status rpd_copy_neighbors_to_host(struct rpd_ctx* ctx, int32_t* nbr,
+                                      int64_t capacity, int* k_out);
+
+/* The candidate pairs of the last rpd_compute as a per-tet CSR (host). */
+rpd_status rpd_copy_pairs_to_host(struct rpd_ctx* ctx, int32_t* tet_offsets,
+                                  int32_t* pair_sites, int64_t capacity,
+                                  int64_t* n_pairs);
+
+/* Host helper: mesh adjacency counts and face ids with the semantics of
+ * load_tet_adj_info (io.cxx:238-335); boundary faces are numbered first in
+ * scan order (the surface facets), interior faces from n_boundary_faces up.
+ * Returns RPD_ERR_INVALID_ARGUMENT for out-of-range ids or faces shared by
+ * more than two tets. */
+rpd_status rpd_build_mesh_adjacency(int n_vert, const int32_t* tets, int n_tet,
+                                    int32_t* v_adjs, uint8_t* e_adj6,
+                                    int32_t* f_adjs, int32_t* f_ids,
+                                    int32_t* n_boundary_faces);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,676 @@
+// rpd_api.cpp -- the C ABI of include/rpd_gb300.h: context, device buffers,
+// one CUDA stream, and the orchestration of the kernels.
+//
+// Replaces the host driver compute_clipped_voro_diagram_GPU
+// (src/rpd3d/voronoi.cu:455-795): instead of pitched AoS->SoA copies, dense
+// n_site x n_tet relation matrices, a host gather loop and a copy of every
+// 3.4 KB thread slot back to the host, everything stays on the device --
+// neighbour lists, candidate pairs (per-tet CSR), cells (compact records) --
+// and only emitted cells are copied out on request.  Errors are returned,
+// never exit()ed (the reference exits on CUDA errors, voronoi.cu:31-37).
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/rpd_gb300.h"
+#include "rpd_common.cuh"
+#include "rpd_kernels.cuh"
+
+using namespace rpd;
+
+namespace {
+
+template <class T>
+struct DevBuf {
+  T* ptr = nullptr;
+  size_t cap = 0;  // elements
+  cudaError_t ensure(size_t n) {
+    if (n <= cap && ptr) return cudaSuccess;
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+    size_t want = std::max<size_t>(n, 1);
+    cudaError_t e = cudaMalloc((void**)&ptr, want * sizeof(T));
+    if (e == cudaSuccess) cap = want;
+    return e;
+  }
+  void release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+  }
+};
+
+enum Ev { kEvStart, kEvKnn, kEvPairs, kEvClip, kEvEnd, kEvCount };
+
+}  // namespace
+
+struct rpd_ctx {
+  rpd_config cfg;
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[kEvCount] = {};
+  std::string err;
+
+  // mesh
+  int n_vert = 0, n_tet = 0;
+  DevBuf<float> vert3f;
+  DevBuf<double> vert3d;
+  DevBuf<int4> tets;
+  DevBuf<int32_t> v_adjs, f_adjs, f_ids;
+  DevBuf<uint8_t> e_adj6;
+  double mesh_lo[3] = {0, 0, 0}, mesh_hi[3] = {0, 0, 0};
+  double tet_radius = 0.0;
+  bool has_mesh = false;
+
+  // sites
+  int n_site = 0;
+  DevBuf<float4> site4f;
+  DevBuf<double> site4d;
+  DevBuf<uint32_t> flags;
+  double site_lo[3] = {0, 0, 0}, site_hi[3] = {0, 0, 0};
+  float w_max = 0.f;
+  bool has_sites = false;
+
+  // neighbour lists
+  int k = 0;
+  DevBuf<int32_t> nbr, nbr_ref_tmp, knn_status;
+  DevBuf<float> nbr_keys;
+  bool has_user_nbr = false;
+
+  // grids
+  DevBuf<int32_t> s_cell_of, s_cell_count, s_cell_start, s_cell_fill, s_cell_items;
+  DevBuf<int32_t> t_cell_of, t_cell_count, t_cell_start, t_cell_fill, t_cell_items;
+  DevBuf<float4> centroid, site_box;
+  DevBuf<int32_t> scan_tmp;
+
+  // pairs
+  DevBuf<int2> pair_buf;
+  DevBuf<int32_t> tet_count, tet_offsets, tet_fill, pair_site, pair_tet;
+  long long pair_cap_hint = 0;
+
+  // cells
+  DevBuf<rpd_cell_header> pair_headers, cells;
+  DevBuf<uint8_t> payload;
+  DevBuf<int32_t> flag_tmp, pos_tmp;
+  DevBuf<unsigned long long> scratch;  // [0] payload cursor [1] work [2..3] counters
+                                       // [4] pair cursor [8..18] status hist
+  DevBuf<long long> n_out;
+  long long payload_cap_hint = 0;
+
+  // results of the last compute
+  long long n_pairs = 0, n_cells = 0, payload_bytes = 0;
+  int tet_k = 0;
+  bool has_result = false;
+};
+
+namespace {
+
+rpd_status fail(rpd_ctx* c, rpd_status s, const std::string& msg) {
+  if (c) c->err = msg;
+  return s;
+}
+
+rpd_status cuda_fail(rpd_ctx* c, cudaError_t e, const char* where) {
+  cudaGetLastError();  // clear non-sticky errors
+  return fail(c, e == cudaErrorMemoryAllocation ? RPD_ERR_OUT_OF_MEMORY : RPD_ERR_CUDA,
+              std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(expr, where)                          \
+  do {                                           \
+    cudaError_t _e = (expr);                     \
+    if (_e != cudaSuccess) return cuda_fail(c, _e, where); \
+  } while (0)
+
+Grid make_grid(const double* lo, const double* hi, long long n_items, double per_cell) {
+  Grid g;
+  double ext[3], vol = 1.0;
+  for (int a = 0; a < 3; ++a) {
+    ext[a] = std::max(hi[a] - lo[a], 1e-9);
+    vol *= ext[a];
+  }
+  double cell = std::cbrt(vol * per_cell / (double)std::max<long long>(n_items, 1));
+  double maxe = std::max(ext[0], std::max(ext[1], ext[2]));
+  cell = std::max(cell, maxe / 512.0);
+  int n[3];
+  for (int a = 0; a < 3; ++a) n[a] = std::max(1, (int)std::ceil(ext[a] / cell));
+  while ((long long)n[0] * n[1] * n[2] > (1ll << 26)) {
+    cell *= 1.25;
+    for (int a = 0; a < 3; ++a) n[a] = std::max(1, (int)std::ceil(ext[a] / cell));
+  }
+  g.lo = make_float3((float)lo[0], (float)lo[1], (float)lo[2]);
+  g.cell = (float)cell;
+  g.inv_cell = (float)(1.0 / cell);
+  g.nx = n[0];
+  g.ny = n[1];
+  g.nz = n[2];
+  return g;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* rpd_status_string(rpd_status s) {
+  switch (s) {
+    case RPD_OK: return "ok";
+    case RPD_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case RPD_ERR_CUDA: return "CUDA error";
+    case RPD_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case RPD_ERR_NOT_READY: return "inputs not set";
+    case RPD_ERR_CAPACITY: return "capacity exceeded";
+    case RPD_ERR_NO_DEVICE: return "no CUDA device";
+  }
+  return "unknown status";
+}
+
+size_t rpd_payload_bytes(int nb_v, int nb_p, int nb_e) {
+  return PayloadLayout(nb_v, nb_p, nb_e).total;
+}
+
+void rpd_config_default(rpd_config* cfg) {
+  if (!cfg) return;
+  std::memset(cfg, 0, sizeof(*cfg));
+  cfg->device = 0;
+  cfg->predicate_mode = RPD_PRED_FP32_FILTER;
+  cfg->neighbor_source = RPD_NEIGH_KNN;
+  cfg->knn_k = 64;
+  cfg->clip_order = RPD_ORDER_SITE_ID;
+  cfg->compute_geometry = 1;
+  cfg->warps_per_block = 0;
+  cfg->blocks_per_sm = 0;
+}
+
+rpd_status rpd_create(const rpd_config* cfg, rpd_ctx** out) {
+  if (!out) return RPD_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  rpd_config c0;
+  rpd_config_default(&c0);
+  if (cfg) c0 = *cfg;
+  if (c0.predicate_mode != RPD_PRED_FP64 && c0.predicate_mode != RPD_PRED_FP32_FILTER)
+    return RPD_ERR_INVALID_ARGUMENT;
+  if (c0.neighbor_source != RPD_NEIGH_USER && c0.neighbor_source != RPD_NEIGH_KNN)
+    return RPD_ERR_INVALID_ARGUMENT;
+  if (c0.neighbor_source == RPD_NEIGH_KNN && (c0.knn_k < 1 || c0.knn_k > 128))
+    return RPD_ERR_INVALID_ARGUMENT;
+  if (c0.warps_per_block < 0 || c0.warps_per_block > kClipMaxThreads / 32 || c0.blocks_per_sm < 0)
+    return RPD_ERR_INVALID_ARGUMENT;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
+    cudaGetLastError();
+    return RPD_ERR_NO_DEVICE;
+  }
+  if (c0.device < 0 || c0.device >= ndev) return RPD_ERR_INVALID_ARGUMENT;
+  rpd_ctx* c = new rpd_ctx();
+  c->cfg = c0;
+  c->device = c0.device;
+  if (cudaSetDevice(c->device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    delete c;
+    return RPD_ERR_CUDA;
+  }
+  for (int i = 0; i < kEvCount; ++i) cudaEventCreate(&c->ev[i]);
+  cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device);
+  *out = c;
+  return RPD_OK;
+}
+
+void rpd_destroy(rpd_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  c->vert3f.release(); c->vert3d.release(); c->tets.release(); c->v_adjs.release();
+  c->f_adjs.release(); c->f_ids.release(); c->e_adj6.release();
+  c->site4f.release(); c->site4d.release(); c->flags.release();
+  c->nbr.release(); c->nbr_ref_tmp.release(); c->knn_status.release(); c->nbr_keys.release();
+  c->s_cell_of.release(); c->s_cell_count.release(); c->s_cell_start.release();
+  c->s_cell_fill.release(); c->s_cell_items.release();
+  c->t_cell_of.release(); c->t_cell_count.release(); c->t_cell_start.release();
+  c->t_cell_fill.release(); c->t_cell_items.release();
+  c->centroid.release(); c->site_box.release(); c->scan_tmp.release();
+  c->pair_buf.release(); c->tet_count.release(); c->tet_offsets.release();
+  c->tet_fill.release(); c->pair_site.release(); c->pair_tet.release();
+  c->pair_headers.release(); c->cells.release(); c->payload.release();
+  c->flag_tmp.release(); c->pos_tmp.release(); c->scratch.release(); c->n_out.release();
+  for (int i = 0; i < kEvCount; ++i)
+    if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+const char* rpd_last_error(const rpd_ctx* c) { return c ? c->err.c_str() : "no context"; }
+
+rpd_status rpd_set_mesh(rpd_ctx* c, const double* xyz, int n_vert, const int32_t* tets, int n_tet,
+                        const int32_t* v_adjs, const uint8_t* e_adj6, const int32_t* f_adjs,
+                        const int32_t* f_ids) {
+  if (!c) return RPD_ERR_INVALID_ARGUMENT;
+  if (n_vert <= 0 || n_tet <= 0 || !xyz || !tets || !v_adjs || !e_adj6 || !f_adjs || !f_ids)
+    return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_set_mesh: empty mesh or null buffer");
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  // validate ids and compute the box and the largest tet radius on the host
+  double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  std::vector<float> vf((size_t)n_vert * 3);
+  for (long long i = 0; i < (long long)n_vert * 3; ++i) {
+    if (!std::isfinite(xyz[i])) return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_set_mesh: non-finite vertex");
+    vf[i] = (float)xyz[i];
+    lo[i % 3] = std::min(lo[i % 3], xyz[i]);
+    hi[i % 3] = std::max(hi[i % 3], xyz[i]);
+  }
+  double rmax = 0.0;
+  for (long long t = 0; t < n_tet; ++t) {
+    double cen[3] = {0, 0, 0};
+    for (int q = 0; q < 4; ++q) {
+      int v = tets[4 * t + q];
+      if (v < 0 || v >= n_vert) return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_set_mesh: vertex id out of range");
+      for (int a = 0; a < 3; ++a) cen[a] += 0.25 * xyz[3 * (long long)v + a];
+    }
+    for (int q = 0; q < 4; ++q) {
+      int v = tets[4 * t + q];
+      double d2 = 0;
+      for (int a = 0; a < 3; ++a) {
+        double d = xyz[3 * (long long)v + a] - cen[a];
+        d2 += d * d;
+      }
+      rmax = std::max(rmax, std::sqrt(d2));
+    }
+  }
+  CK(c->vert3f.ensure((size_t)n_vert * 3), "alloc vert3f");
+  CK(c->vert3d.ensure((size_t)n_vert * 3), "alloc vert3d");
+  CK(c->tets.ensure(n_tet), "alloc tets");
+  CK(c->v_adjs.ensure(n_vert), "alloc v_adjs");
+  CK(c->e_adj6.ensure((size_t)n_tet * 6), "alloc e_adj6");
+  CK(c->f_adjs.ensure((size_t)n_tet * 4), "alloc f_adjs");
+  CK(c->f_ids.ensure((size_t)n_tet * 4), "alloc f_ids");
+  cudaStream_t st = c->stream;
+  CK(cudaMemcpyAsync(c->vert3f.ptr, vf.data(), vf.size() * 4, cudaMemcpyHostToDevice, st), "H2D vert");
+  CK(cudaMemcpyAsync(c->vert3d.ptr, xyz, (size_t)n_vert * 24, cudaMemcpyHostToDevice, st), "H2D vert");
+  CK(cudaMemcpyAsync(c->tets.ptr, tets, (size_t)n_tet * 16, cudaMemcpyHostToDevice, st), "H2D tets");
+  CK(cudaMemcpyAsync(c->v_adjs.ptr, v_adjs, (size_t)n_vert * 4, cudaMemcpyHostToDevice, st), "H2D v_adjs");
+  CK(cudaMemcpyAsync(c->e_adj6.ptr, e_adj6, (size_t)n_tet * 6, cudaMemcpyHostToDevice, st), "H2D e_adj6");
+  CK(cudaMemcpyAsync(c->f_adjs.ptr, f_adjs, (size_t)n_tet * 16, cudaMemcpyHostToDevice, st), "H2D f_adjs");
+  CK(cudaMemcpyAsync(c->f_ids.ptr, f_ids, (size_t)n_tet * 16, cudaMemcpyHostToDevice, st), "H2D f_ids");
+  CK(cudaStreamSynchronize(st), "set_mesh sync");
+  c->n_vert = n_vert;
+  c->n_tet = n_tet;
+  for (int a = 0; a < 3; ++a) {
+    c->mesh_lo[a] = lo[a];
+    c->mesh_hi[a] = hi[a];
+  }
+  c->tet_radius = rmax;
+  c->has_mesh = true;
+  c->has_result = false;
+  return RPD_OK;
+}
+
+rpd_status rpd_set_sites(rpd_ctx* c, const double* xyzw, int n_site, const uint32_t* flags) {
+  if (!c) return RPD_ERR_INVALID_ARGUMENT;
+  if (n_site <= 0 || !xyzw) return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_set_sites: no sites");
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  std::vector<float> sf((size_t)n_site * 4);
+  std::vector<uint32_t> fl((size_t)n_site, 1u);
+  double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  float wmax = -INFINITY;
+  for (long long i = 0; i < n_site; ++i) {
+    for (int a = 0; a < 4; ++a) {
+      double v = xyzw[4 * i + a];
+      if (!std::isfinite(v)) return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_set_sites: non-finite site");
+      sf[4 * i + a] = (float)v;
+    }
+    for (int a = 0; a < 3; ++a) {
+      lo[a] = std::min(lo[a], xyzw[4 * i + a]);
+      hi[a] = std::max(hi[a], xyzw[4 * i + a]);
+    }
+    wmax = std::max(wmax, sf[4 * i + 3]);
+    if (flags) fl[i] = flags[i];
+  }
+  CK(c->site4f.ensure(n_site), "alloc sites");
+  CK(c->site4d.ensure((size_t)n_site * 4), "alloc sites");
+  CK(c->flags.ensure(n_site), "alloc flags");
+  cudaStream_t st = c->stream;
+  CK(cudaMemcpyAsync(c->site4f.ptr, sf.data(), sf.size() * 4, cudaMemcpyHostToDevice, st), "H2D sites");
+  CK(cudaMemcpyAsync(c->site4d.ptr, xyzw, (size_t)n_site * 32, cudaMemcpyHostToDevice, st), "H2D sites");
+  CK(cudaMemcpyAsync(c->flags.ptr, fl.data(), (size_t)n_site * 4, cudaMemcpyHostToDevice, st), "H2D flags");
+  CK(cudaStreamSynchronize(st), "set_sites sync");
+  if (c->n_site != n_site) c->has_user_nbr = false;
+  c->n_site = n_site;
+  for (int a = 0; a < 3; ++a) {
+    c->site_lo[a] = lo[a];
+    c->site_hi[a] = hi[a];
+  }
+  c->w_max = wmax;
+  c->has_sites = true;
+  c->has_result = false;
+  return RPD_OK;
+}
+
+rpd_status rpd_set_neighbors(rpd_ctx* c, const int32_t* nbr, int k, int layout) {
+  if (!c) return RPD_ERR_INVALID_ARGUMENT;
+  if (!c->has_sites) return fail(c, RPD_ERR_NOT_READY, "rpd_set_neighbors: set the sites first");
+  if (!nbr || k < 0 || (layout != 0 && layout != 1))
+    return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_set_neighbors: bad arguments");
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  long long n = (long long)c->n_site * k;
+  long long n_in = layout == 1 ? (long long)c->n_site * (k + 1) : n;
+  for (long long i = 0; i < n_in; ++i)
+    if (nbr[i] < -1 || nbr[i] >= c->n_site)
+      return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_set_neighbors: site id out of range");
+  int kk = std::max(k, 1);
+  CK(c->nbr.ensure((size_t)c->n_site * kk), "alloc nbr");
+  cudaStream_t st = c->stream;
+  if (k == 0) {
+    CK(cudaMemsetAsync(c->nbr.ptr, 0xff, sizeof(int32_t) * (size_t)c->n_site, st), "memset nbr");
+  } else if (layout == 0) {
+    CK(cudaMemcpyAsync(c->nbr.ptr, nbr, sizeof(int32_t) * (size_t)n, cudaMemcpyHostToDevice, st), "H2D nbr");
+  } else {
+    CK(c->nbr_ref_tmp.ensure((size_t)n_in), "alloc nbr");
+    CK(cudaMemcpyAsync(c->nbr_ref_tmp.ptr, nbr, sizeof(int32_t) * (size_t)n_in, cudaMemcpyHostToDevice, st), "H2D nbr");
+    CK(neighbors_from_reference(c->nbr_ref_tmp.ptr, k, c->n_site, c->nbr.ptr, st), "nbr transpose");
+  }
+  CK(cudaStreamSynchronize(st), "set_neighbors sync");
+  c->k = kk;
+  c->has_user_nbr = true;
+  c->has_result = false;
+  return RPD_OK;
+}
+
+rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
+  if (!c) return RPD_ERR_INVALID_ARGUMENT;
+  if (!c->has_mesh || !c->has_sites) return fail(c, RPD_ERR_NOT_READY, "rpd_compute: mesh and sites required");
+  const bool knn = c->cfg.neighbor_source == RPD_NEIGH_KNN;
+  if (!knn && !c->has_user_nbr)
+    return fail(c, RPD_ERR_NOT_READY, "rpd_compute: neighbour lists required (rpd_set_neighbors)");
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  cudaStream_t st = c->stream;
+  const int n_site = c->n_site, n_tet = c->n_tet;
+  CK(c->scratch.ensure(32), "alloc scratch");
+  CK(cudaMemsetAsync(c->scratch.ptr, 0, 32 * sizeof(unsigned long long), st), "memset");
+  CK(cudaEventRecord(c->ev[kEvStart], st), "event");
+
+  // ---- neighbour lists
+  if (knn) {
+    c->k = c->cfg.knn_k;
+    Grid g = make_grid(c->site_lo, c->site_hi, n_site, 2.0);
+    long long nc = (long long)g.nx * g.ny * g.nz;
+    CK(c->s_cell_of.ensure(n_site), "alloc");
+    CK(c->s_cell_count.ensure(nc), "alloc");
+    CK(c->s_cell_start.ensure(nc + 1), "alloc");
+    CK(c->s_cell_fill.ensure(nc), "alloc");
+    CK(c->s_cell_items.ensure(n_site), "alloc");
+    CK(c->scan_tmp.ensure(scan_temp_ints(std::max<long long>(nc, n_tet)) + 16), "alloc");
+    CK(c->nbr.ensure((size_t)n_site * c->k), "alloc nbr");
+    CK(c->nbr_keys.ensure((size_t)n_site * c->k), "alloc nbr");
+    CK(c->knn_status.ensure(n_site), "alloc");
+    CK(grid_build_sites(c->site4f.ptr, n_site, g, c->s_cell_of.ptr, c->s_cell_count.ptr,
+                        c->s_cell_start.ptr, c->s_cell_fill.ptr, c->s_cell_items.ptr,
+                        c->scan_tmp.ptr, st), "site grid");
+    CK(launch_knn(c->site4f.ptr, n_site, g, c->s_cell_start.ptr, c->s_cell_items.ptr, c->k,
+                  c->w_max, c->cfg.clip_order == RPD_ORDER_SITE_ID ? 1 : 0, c->nbr.ptr,
+                  c->nbr_keys.ptr, c->knn_status.ptr, st), "knn");
+  }
+  CK(cudaEventRecord(c->ev[kEvKnn], st), "event");
+
+  // ---- candidate pairs
+  {
+    Grid tg = make_grid(c->mesh_lo, c->mesh_hi, n_tet, 4.0);
+    long long nc = (long long)tg.nx * tg.ny * tg.nz;
+    CK(c->centroid.ensure(n_tet), "alloc");
+    CK(c->t_cell_of.ensure(n_tet), "alloc");
+    CK(c->t_cell_count.ensure(nc), "alloc");
+    CK(c->t_cell_start.ensure(nc + 1), "alloc");
+    CK(c->t_cell_fill.ensure(nc), "alloc");
+    CK(c->t_cell_items.ensure(n_tet), "alloc");
+    CK(c->scan_tmp.ensure(scan_temp_ints(std::max<long long>(nc, n_tet)) + 16), "alloc");
+    CK(grid_build_tets(c->vert3f.ptr, c->tets.ptr, n_tet, tg, c->centroid.ptr, c->t_cell_of.ptr,
+                       c->t_cell_count.ptr, c->t_cell_start.ptr, c->t_cell_fill.ptr,
+                       c->t_cell_items.ptr, c->scan_tmp.ptr, st), "tet grid");
+    // per-site boxes
+    double diag2 = 0.0, cs = 0.0;
+    for (int a = 0; a < 3; ++a) {
+      double l = std::min(c->mesh_lo[a], c->site_lo[a]), h = std::max(c->mesh_hi[a], c->site_hi[a]);
+      diag2 += (h - l) * (h - l);
+      cs = std::max(cs, std::max(std::fabs(l), std::fabs(h)));
+    }
+    const double u = std::ldexp(1.0, -24);
+    const double R = c->tet_radius * (1.0 + 1e-5) + 1e-6 * cs;
+    double ext = 0.0;
+    for (int a = 0; a < 3; ++a) ext = std::max(ext, c->mesh_hi[a] - c->mesh_lo[a]);
+    const double margin = 1e-4 * ext + 1e-6 * cs;
+    BoxParams bp;
+    bp.site4f = c->site4f.ptr;
+    bp.flags = c->flags.ptr;
+    bp.nbr = c->nbr.ptr;
+    bp.k = c->k;
+    bp.n_site = n_site;
+    bp.box_lo = make_float4((float)(c->mesh_lo[0] - margin), (float)(c->mesh_lo[1] - margin),
+                            (float)(c->mesh_lo[2] - margin), 0.f);
+    bp.box_hi = make_float4((float)(c->mesh_hi[0] + margin), (float)(c->mesh_hi[1] + margin),
+                            (float)(c->mesh_hi[2] + margin), 0.f);
+    bp.offset_r = (float)R;
+    bp.offset_e = (float)(48.0 * u * (diag2 + std::fabs((double)c->w_max)));
+    bp.coord_scale = (float)cs;
+    bp.abs_margin = (float)margin;
+    CK(c->site_box.ensure((size_t)n_site * 2), "alloc");
+    bp.site_box = c->site_box.ptr;
+    bp.counters = nullptr;
+    int bw = 4;
+    int bblocks = std::max(1, std::min((n_site + bw - 1) / bw, c->num_sms * box_blocks_per_sm(bw)));
+    CK(launch_site_box(bp, bblocks, bw, st), "site boxes");
+
+    CK(c->tet_count.ensure(n_tet), "alloc");
+    CK(c->tet_offsets.ensure((size_t)n_tet + 1), "alloc");
+    CK(c->tet_fill.ensure(n_tet), "alloc");
+    long long cap = c->pair_cap_hint > 0 ? c->pair_cap_hint : std::max<long long>(1 << 20, 16ll * n_tet);
+    for (int attempt = 0; attempt < 3; ++attempt) {
+      CK(c->pair_buf.ensure((size_t)cap), "alloc pairs");
+      CK(cudaMemsetAsync(c->tet_count.ptr, 0, sizeof(int32_t) * (size_t)n_tet, st), "memset");
+      CK(cudaMemsetAsync(c->scratch.ptr + 4, 0, sizeof(unsigned long long), st), "memset");
+      PairParams pp;
+      pp.vert3f = c->vert3f.ptr;
+      pp.tets = c->tets.ptr;
+      pp.centroid = c->centroid.ptr;
+      pp.tg = tg;
+      pp.tcell_start = c->t_cell_start.ptr;
+      pp.tcell_items = c->t_cell_items.ptr;
+      pp.site4f = c->site4f.ptr;
+      pp.flags = c->flags.ptr;
+      pp.nbr = c->nbr.ptr;
+      pp.k = c->k;
+      pp.n_site = n_site;
+      pp.site_box = c->site_box.ptr;
+      pp.pair_buf = c->pair_buf.ptr;
+      pp.pair_cursor = c->scratch.ptr + 4;
+      pp.pair_cap = (long long)c->pair_buf.cap;
+      pp.tet_count = c->tet_count.ptr;
+      CK(launch_pairs(pp, st), "pairs");
+      unsigned long long np = 0;
+      CK(cudaMemcpyAsync(&np, c->scratch.ptr + 4, sizeof(np), cudaMemcpyDeviceToHost, st), "D2H");
+      CK(cudaStreamSynchronize(st), "pairs sync");
+      c->n_pairs = (long long)np;
+      if ((long long)np <= (long long)c->pair_buf.cap) break;
+      cap = (long long)np + (long long)np / 8 + 1024;
+      if (attempt == 2) return fail(c, RPD_ERR_CAPACITY, "rpd_compute: pair buffer");
+    }
+    if (c->n_pairs > INT32_MAX) return fail(c, RPD_ERR_CAPACITY, "rpd_compute: more than 2^31 pairs");
+    c->pair_cap_hint = std::max<long long>(c->pair_cap_hint, c->n_pairs + c->n_pairs / 8 + 1024);
+    CK(scan_exclusive(c->tet_count.ptr, c->tet_offsets.ptr, n_tet, c->scan_tmp.ptr, st), "scan");
+    CK(c->pair_site.ensure((size_t)c->n_pairs), "alloc");
+    CK(c->pair_tet.ensure((size_t)c->n_pairs), "alloc");
+    CK(pairs_to_csr(c->pair_buf.ptr, c->n_pairs, n_tet, c->tet_offsets.ptr, c->tet_fill.ptr,
+                    c->pair_site.ptr, c->pair_tet.ptr,
+                    reinterpret_cast<int32_t*>(c->scratch.ptr + 5), st), "csr");
+  }
+  CK(cudaEventRecord(c->ev[kEvPairs], st), "event");
+
+  // ---- clipping
+  const long long n_pairs = c->n_pairs;
+  CK(c->pair_headers.ensure((size_t)std::max<long long>(n_pairs, 1)), "alloc headers");
+  long long pcap = c->payload_cap_hint > 0 ? c->payload_cap_hint
+                                           : std::max<long long>(1 << 24, 640ll * n_pairs);
+  const int warps = c->cfg.warps_per_block > 0 ? c->cfg.warps_per_block : 4;
+  int bps = c->cfg.blocks_per_sm;
+  if (bps <= 0) bps = clip_blocks_per_sm(c->cfg.predicate_mode, warps);
+  int blocks = std::max(1, c->num_sms * bps);
+  for (int attempt = 0; attempt < 3; ++attempt) {
+    CK(c->payload.ensure((size_t)pcap), "alloc payload");
+    CK(cudaMemsetAsync(c->scratch.ptr, 0, 4 * sizeof(unsigned long long), st), "memset");
+    ClipParams p;
+    p.vert3f = c->vert3f.ptr;
+    p.vert3d = c->vert3d.ptr;
+    p.tets = c->tets.ptr;
+    p.v_adjs = c->v_adjs.ptr;
+    p.e_adj6 = c->e_adj6.ptr;
+    p.f_adjs = c->f_adjs.ptr;
+    p.f_ids = c->f_ids.ptr;
+    p.site4f = c->site4f.ptr;
+    p.site4d = c->site4d.ptr;
+    p.nbr = c->nbr.ptr;
+    p.k = c->k;
+    p.pair_tet = c->pair_tet.ptr;
+    p.pair_site = c->pair_site.ptr;
+    p.n_pairs = n_pairs;
+    p.headers = c->pair_headers.ptr;
+    p.payload = c->payload.ptr;
+    p.payload_cursor = c->scratch.ptr + 0;
+    p.payload_cap = (unsigned long long)c->payload.cap;
+    p.work = c->scratch.ptr + 1;
+    p.counters = c->scratch.ptr + 2;
+    p.geometry = c->cfg.compute_geometry;
+    if (n_pairs > 0) CK(launch_clip_cells(p, c->cfg.predicate_mode, blocks, warps, st), "clip");
+    unsigned long long cur = 0;
+    CK(cudaMemcpyAsync(&cur, c->scratch.ptr, sizeof(cur), cudaMemcpyDeviceToHost, st), "D2H");
+    CK(cudaStreamSynchronize(st), "clip sync");
+    c->payload_bytes = (long long)cur;
+    if ((long long)cur <= (long long)c->payload.cap) break;
+    pcap = (long long)cur + (long long)cur / 8 + (1 << 20);
+    if (attempt == 2) return fail(c, RPD_ERR_CAPACITY, "rpd_compute: payload buffer");
+  }
+  c->payload_cap_hint = std::max<long long>(c->payload_cap_hint, c->payload_bytes + c->payload_bytes / 8 + (1 << 20));
+  CK(cudaEventRecord(c->ev[kEvClip], st), "event");
+
+  // ---- compaction
+  CK(c->cells.ensure((size_t)std::max<long long>(n_pairs, 1)), "alloc cells");
+  CK(c->flag_tmp.ensure((size_t)n_pairs + 1), "alloc");
+  CK(c->pos_tmp.ensure((size_t)n_pairs + 1), "alloc");
+  CK(c->scan_tmp.ensure(scan_temp_ints(std::max<long long>(n_pairs, n_tet)) + 16), "alloc");
+  CK(c->n_out.ensure(1), "alloc");
+  CK(compact_cells(c->pair_headers.ptr, n_pairs, c->flag_tmp.ptr, c->pos_tmp.ptr, c->scan_tmp.ptr,
+                   c->cells.ptr, c->n_out.ptr, c->scratch.ptr + 8, st), "compact");
+  CK(cudaEventRecord(c->ev[kEvEnd], st), "event");
+  unsigned long long host_scratch[32];
+  long long n_cells = 0;
+  CK(cudaMemcpyAsync(host_scratch, c->scratch.ptr, sizeof(host_scratch), cudaMemcpyDeviceToHost, st), "D2H");
+  CK(cudaMemcpyAsync(&n_cells, c->n_out.ptr, sizeof(n_cells), cudaMemcpyDeviceToHost, st), "D2H");
+  CK(cudaStreamSynchronize(st), "compute sync");
+  c->n_cells = n_cells;
+  c->tet_k = (int)reinterpret_cast<int32_t*>(host_scratch + 5)[0];
+  c->has_result = true;
+  if (host_scratch[8 + 10] != 0)
+    return fail(c, RPD_ERR_CAPACITY, "rpd_compute: cells lost to a full payload buffer");
+  if (stats) {
+    std::memset(stats, 0, sizeof(*stats));
+    stats->n_pairs = n_pairs;
+    stats->n_cells = n_cells;
+    for (int i = 0; i < 10; ++i) stats->status_counts[i] = (int64_t)host_scratch[8 + i];
+    stats->n_predicates = (int64_t)host_scratch[2];
+    stats->n_escalated = (int64_t)host_scratch[3];
+    stats->payload_bytes = c->payload_bytes;
+    stats->tet_k = c->tet_k;
+    stats->knn_k = c->k;
+    cudaEventElapsedTime(&stats->ms_total, c->ev[kEvStart], c->ev[kEvEnd]);
+    cudaEventElapsedTime(&stats->ms_knn, c->ev[kEvStart], c->ev[kEvKnn]);
+    cudaEventElapsedTime(&stats->ms_pairs, c->ev[kEvKnn], c->ev[kEvPairs]);
+    cudaEventElapsedTime(&stats->ms_clip, c->ev[kEvPairs], c->ev[kEvClip]);
+    cudaEventElapsedTime(&stats->ms_compact, c->ev[kEvClip], c->ev[kEvEnd]);
+  }
+  return RPD_OK;
+}
+
+rpd_status rpd_get_cells(rpd_ctx* c, rpd_cells_view* v) {
+  if (!c || !v) return RPD_ERR_INVALID_ARGUMENT;
+  if (!c->has_result) return fail(c, RPD_ERR_NOT_READY, "rpd_get_cells: no result");
+  v->n_cells = c->n_cells;
+  v->headers = c->cells.ptr;
+  v->payload = c->payload.ptr;
+  v->payload_bytes = c->payload_bytes;
+  v->n_pairs = c->n_pairs;
+  v->pair_headers = c->pair_headers.ptr;
+  return RPD_OK;
+}
+
+rpd_status rpd_copy_cells_to_host(rpd_ctx* c, rpd_cell_header* headers, int64_t max_cells,
+                                  void* payload, int64_t payload_capacity, int64_t* n_cells,
+                                  int64_t* payload_bytes) {
+  if (!c) return RPD_ERR_INVALID_ARGUMENT;
+  if (!c->has_result) return fail(c, RPD_ERR_NOT_READY, "rpd_copy_cells_to_host: no result");
+  if (n_cells) *n_cells = c->n_cells;
+  if (payload_bytes) *payload_bytes = c->payload_bytes;
+  if (!headers && !payload) return RPD_OK;
+  if ((headers && max_cells < c->n_cells) || (payload && payload_capacity < c->payload_bytes))
+    return fail(c, RPD_ERR_CAPACITY, "rpd_copy_cells_to_host: buffers too small");
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  cudaStream_t st = c->stream;
+  if (headers && c->n_cells > 0)
+    CK(cudaMemcpyAsync(headers, c->cells.ptr, sizeof(rpd_cell_header) * (size_t)c->n_cells,
+                       cudaMemcpyDeviceToHost, st), "D2H cells");
+  if (payload && c->payload_bytes > 0)
+    CK(cudaMemcpyAsync(payload, c->payload.ptr, (size_t)c->payload_bytes, cudaMemcpyDeviceToHost, st),
+       "D2H payload");
+  CK(cudaStreamSynchronize(st), "copy sync");
+  return RPD_OK;
+}
+
+rpd_status rpd_copy_pair_headers_to_host(rpd_ctx* c, rpd_cell_header* headers, int64_t capacity,
+                                         int64_t* n_pairs) {
+  if (!c) return RPD_ERR_INVALID_ARGUMENT;
+  if (!c->has_result) return fail(c, RPD_ERR_NOT_READY, "rpd_copy_pair_headers_to_host: no result");
+  if (n_pairs) *n_pairs = c->n_pairs;
+  if (!headers) return RPD_OK;
+  if (capacity < c->n_pairs) return fail(c, RPD_ERR_CAPACITY, "rpd_copy_pair_headers_to_host: buffer too small");
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  if (c->n_pairs > 0)
+    CK(cudaMemcpyAsync(headers, c->pair_headers.ptr, sizeof(rpd_cell_header) * (size_t)c->n_pairs,
+                       cudaMemcpyDeviceToHost, c->stream), "D2H");
+  CK(cudaStreamSynchronize(c->stream), "sync");
+  return RPD_OK;
+}
+
+rpd_status rpd_copy_neighbors_to_host(rpd_ctx* c, int32_t* nbr, int64_t capacity, int* k_out) {
+  if (!c) return RPD_ERR_INVALID_ARGUMENT;
+  if (k_out) *k_out = c->k;
+  if (!nbr) return RPD_OK;
+  long long n = (long long)c->n_site * c->k;
+  if (capacity < n) return fail(c, RPD_ERR_CAPACITY, "rpd_copy_neighbors_to_host: buffer too small");
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  CK(cudaMemcpyAsync(nbr, c->nbr.ptr, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost, c->stream), "D2H");
+  CK(cudaStreamSynchronize(c->stream), "sync");
+  return RPD_OK;
+}
+
+rpd_status rpd_copy_pairs_to_host(rpd_ctx* c, int32_t* tet_offsets, int32_t* pair_sites,
+                                  int64_t capacity, int64_t* n_pairs) {
+  if (!c) return RPD_ERR_INVALID_ARGUMENT;
+  if (!c->has_result) return fail(c, RPD_ERR_NOT_READY, "rpd_copy_pairs_to_host: no result");
+  if (n_pairs) *n_pairs = c->n_pairs;
+  if (!tet_offsets && !pair_sites) return RPD_OK;
+  if (pair_sites && capacity < c->n_pairs) return fail(c, RPD_ERR_CAPACITY, "rpd_copy_pairs_to_host: buffer too small");
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  if (tet_offsets)
+    CK(cudaMemcpyAsync(tet_offsets, c->tet_offsets.ptr, sizeof(int32_t) * ((size_t)c->n_tet + 1),
+                       cudaMemcpyDeviceToHost, c->stream), "D2H");
+  if (pair_sites && c->n_pairs > 0)
+    CK(cudaMemcpyAsync(pair_sites, c->pair_site.ptr, sizeof(int32_t) * (size_t)c->n_pairs,
+                       cudaMemcpyDeviceToHost, c->stream), "D2H");
+  CK(cudaStreamSynchronize(c->stream), "sync");
+  return RPD_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,883 @@
+// rpd_clip.cu -- warp-cooperative convex-cell clipping on sm_103a.
+//
+// One warp owns one cell: the tet (or a box) clipped by the power bisectors
+// of one site's neighbour list, in list order.  The cell's planes, dual
+// triangles (vertices), edges and boundary links live in shared memory in
+// the reference's representation (convex_cell.h:73-115, :117-185), so the
+// records it emits are the reference's ConvexCell contents.
+//
+// Semantics follow src/rpd3d/convex_cell.cu exactly:
+//   cell = tet                         :116-214
+//   bisector plane (FP32)              :561-592
+//   conflict predicate, tie = none     :437-500 (FP64 det4x4 of float planes)
+//   conflict partition (swap to tail)  :706-721
+//   cavity boundary walk               :618-678
+//   new edges / vertices / perturb     :524-554, :604-616, :274-316
+//   per-list driver and drop rules     :1166-1337
+// What is GB300-specific is the execution: the plane coefficients of 32
+// neighbours are built by 32 lanes at once; while the cell has <= 16
+// vertices each predicate step tests several consecutive planes against all
+// vertices in one ballot and jumps to the first plane that clips anything
+// (planes that clip nothing leave the cell unchanged, so skipping them is
+// exact); predicate signs come from an FP32 cofactor filter with a proven
+// error bound and fall back to the reference's FP64 determinant only when
+// undecided; the topology update of a clipping plane runs on lane 0 while
+// the vertex cofactors of the new vertices are rebuilt in parallel.
+//
+// This translation unit is compiled with -fmad=false: every float/double
+// expression below that restates a reference formula is evaluated one IEEE
+// rounding at a time, as in the reference's source.  FMA is used only where
+// written explicitly (the filter).
+
+#include <cuda_runtime.h>
+
+#include "rpd_common.cuh"
+#include "rpd_kernels.cuh"
+
+namespace rpd {
+
+// ------------------------------------------------------------------------
+// shared-memory cell
+// ------------------------------------------------------------------------
+struct __align__(16) WarpCell {
+  float4 pl[kMaxP];  // plane (a, b, c, d), inside: a x + b y + c z + d >= 0
+  union {
+    struct {
+      float4 K[kMaxT];  // cofactors of each vertex (filter)
+      float M[kMaxT];   // largest 3x3 permanent of each vertex (filter)
+    } f;
+    double pd[kMaxP][4];  // FP64 planes (geometry pass)
+  } u;
+  int2 id2[kMaxP];
+  uchar4 ver[kMaxT];
+  uchar4 edge[kMaxE];
+  uint8_t h[kMaxP];
+  uint8_t bnext[kMaxP];
+};
+
+struct CellState {
+  int nb_v, nb_p, nb_e;
+  int status;
+};
+
+// local faces / edges of a tet (convex_cell.h:25-29, convex_cell.cu:193-211)
+__constant__ int8_t cFaceLv[4][3] = {{2, 1, 3}, {0, 2, 3}, {1, 0, 3}, {0, 1, 2}};
+__constant__ int8_t cEdgeFaces[6][2] = {{2, 3}, {1, 3}, {1, 2}, {0, 3}, {0, 2}, {0, 1}};
+__constant__ int8_t cTetTri[4][3] = {{1, 3, 2}, {0, 2, 3}, {0, 3, 1}, {0, 1, 2}};
+
+// ------------------------------------------------------------------------
+// reference arithmetic (no contraction in this TU)
+// ------------------------------------------------------------------------
+__device__ __forceinline__ float4 tri2plane_f(float3 v0, float3 v1, float3 v2) {
+  float ax = v1.x - v0.x, ay = v1.y - v0.y, az = v1.z - v0.z;
+  float bx = v2.x - v0.x, by = v2.y - v0.y, bz = v2.z - v0.z;
+  float nx = ay * bz - az * by;
+  float ny = az * bx - ax * bz;
+  float nz = ax * by - ay * bx;
+  return make_float4(nx, ny, nz, -(v0.x * nx + v0.y * ny + v0.z * nz));
+}
+
+__device__ __forceinline__ float4 bisector_f(float4 S, float4 B) {
+  float dx = S.x - B.x, dy = S.y - B.y, dz = S.z - B.z;
+  float ax = S.x + B.x, ay = S.y + B.y, az = S.z + B.z;
+  float dot = (ax * dx + ay * dy + az * dz) + (B.w - S.w);
+  return make_float4(dx, dy, dz, -dot / 2.f);
+}
+
+__device__ __forceinline__ double det4x4_ref(float4 p1, float4 p2, float4 p3,
+                                             float4 e) {
+  double a11 = p1.x, a12 = p2.x, a13 = p3.x, a14 = e.x;
+  double a21 = p1.y, a22 = p2.y, a23 = p3.y, a24 = e.y;
+  double a31 = p1.z, a32 = p2.z, a33 = p3.z, a34 = e.z;
+  double a41 = p1.w, a42 = p2.w, a43 = p3.w, a44 = e.w;
+  double m12 = a21 * a12 - a11 * a22;
+  double m13 = a31 * a12 - a11 * a32;
+  double m14 = a41 * a12 - a11 * a42;
+  double m23 = a31 * a22 - a21 * a32;
+  double m24 = a41 * a22 - a21 * a42;
+  double m34 = a41 * a32 - a31 * a42;
+  double m123 = m23 * a13 - m13 * a23 + m12 * a33;
+  double m124 = m24 * a13 - m14 * a23 + m12 * a43;
+  double m134 = m34 * a13 - m14 * a33 + m13 * a43;
+  double m234 = m34 * a23 - m24 * a33 + m23 * a43;
+  return (m234 * a14 - m134 * a24 + m124 * a34 - m123 * a44);
+}
+
+// float det3x3 of the three plane normals (convex_cell.cu:274-316, the w
+// of the homogeneous vertex); zero means the vertex needs a perturbation
+__device__ __forceinline__ float det3x3_f(float4 a, float4 b, float4 c) {
+  float t1 = b.y * c.z - b.z * c.y;
+  float t2 = a.y * c.z - a.z * c.y;
+  float t3 = a.y * b.z - a.z * b.y;
+  return a.x * t1 - b.x * t2 + c.x * t3;
+}
+
+// ------------------------------------------------------------------------
+// FP32 filter: det4x4(p1,p2,p3,e) = sum_r e_r K_r, K_r the signed 3x3
+// minors of the vertex planes.  |fl(K_r) - K_r| <= gamma_5 M_r (M_r the 3x3
+// permanent), the FMA dot adds gamma_4 sum|e_r K_r|; the bound also covers
+// the reference's FP64 evaluation (gamma_9 in double times the 4x4
+// permanent), so a decided sign is the sign of the reference's FP64 det.
+// ------------------------------------------------------------------------
+__device__ __forceinline__ void minor3(float a1, float b1, float c1, float a2,
+                                       float b2, float c2, float a3, float b3,
+                                       float c3, float& det, float& perm) {
+  float u1 = __fmaf_rn(b2, c3, -(b3 * c2));
+  float u2 = __fmaf_rn(a2, c3, -(a3 * c2));
+  float u3 = __fmaf_rn(a2, b3, -(a3 * b2));
+  det = __fmaf_rn(a1, u1, __fmaf_rn(-b1, u2, c1 * u3));
+  float v1 = __fmaf_rn(fabsf(b2), fabsf(c3), fabsf(b3) * fabsf(c2));
+  float v2 = __fmaf_rn(fabsf(a2), fabsf(c3), fabsf(a3) * fabsf(c2));
+  float v3 = __fmaf_rn(fabsf(a2), fabsf(b3), fabsf(a3) * fabsf(b2));
+  perm = __fmaf_rn(fabsf(a1), v1, __fmaf_rn(fabsf(b1), v2, fabsf(c1) * v3));
+}
+
+__device__ __forceinline__ void vertex_cofactors(float4 p1, float4 p2, float4 p3,
+                                                 float4& K, float& M) {
+  float d, pm, mx;
+  minor3(p1.y, p1.z, p1.w, p2.y, p2.z, p2.w, p3.y, p3.z, p3.w, d, pm);
+  K.x = -d;
+  mx = pm;
+  minor3(p1.x, p1.z, p1.w, p2.x, p2.z, p2.w, p3.x, p3.z, p3.w, d, pm);
+  K.y = d;
+  mx = fmaxf(mx, pm);
+  minor3(p1.x, p1.y, p1.w, p2.x, p2.y, p2.w, p3.x, p3.y, p3.w, d, pm);
+  K.z = -d;
+  mx = fmaxf(mx, pm);
+  minor3(p1.x, p1.y, p1.z, p2.x, p2.y, p2.z, p3.x, p3.y, p3.z, d, pm);
+  K.w = d;
+  mx = fmaxf(mx, pm);
+  M = mx;
+}
+
+constexpr float kFiltC1 = 5.0f * 5.9604645e-08f;
+constexpr float kFiltC2 = 6.0f * 5.9604645e-08f;
+constexpr float kFiltAbs = 1e-30f;
+
+// +1 / -1 decided, 0 undecided
+__device__ __forceinline__ int filter_sign(float4 K, float M, float4 e, float se) {
+  float s = __fmaf_rn(e.w, K.w, __fmaf_rn(e.z, K.z, __fmaf_rn(e.y, K.y, e.x * K.x)));
+  float t = __fmaf_rn(fabsf(e.w), fabsf(K.w),
+                      __fmaf_rn(fabsf(e.z), fabsf(K.z),
+                                __fmaf_rn(fabsf(e.y), fabsf(K.y), fabsf(e.x) * fabsf(K.x))));
+  float b = __fmaf_rn(kFiltC1, t, kFiltC2 * (M * se)) + kFiltAbs;
+  return s > b ? 1 : (s < -b ? -1 : 0);
+}
+
+__device__ __forceinline__ bool plane_eq(float4 a, float4 b) {
+  return a.x == b.x && a.y == b.y && a.z == b.z && a.w == b.w;
+}
+
+__device__ __forceinline__ float plane_abs_sum(float4 e) {
+  return (fabsf(e.x) + fabsf(e.y)) + (fabsf(e.z) + fabsf(e.w));
+}
+
+// conflict of the vertex in slot vi with plane e; dup = planes identical to e
+template <int PRED>
+__device__ __forceinline__ bool in_conflict(const WarpCell& c, int vi, float4 e,
+                                            float se, uint64_t dup,
+                                            uint32_t& n_pred, uint32_t& n_esc) {
+  uchar4 v = c.ver[vi];
+  uint64_t vm = (1ull << v.x) | (1ull << v.y) | (1ull << v.z);
+  if (dup & vm) return false;
+  ++n_pred;
+  if (PRED == RPD_PRED_FP32_FILTER) {
+    int s = filter_sign(c.u.f.K[vi], c.u.f.M[vi], e, se);
+    if (s != 0) return s > 0;
+    ++n_esc;
+  }
+  return det4x4_ref(c.pl[v.x], c.pl[v.y], c.pl[v.z], e) > 0.0;
+}
+
+// ------------------------------------------------------------------------
+// sequential topology update, run by lane 0 (convex_cell.cu:618-774)
+// ------------------------------------------------------------------------
+__device__ __forceinline__ bool getbit(const uint32_t* m, int i) {
+  return (m[i >> 5] >> (i & 31)) & 1u;
+}
+__device__ __forceinline__ void putbit(uint32_t* m, int i, bool b) {
+  uint32_t bit = 1u << (i & 31);
+  m[i >> 5] = b ? (m[i >> 5] | bit) : (m[i >> 5] & ~bit);
+}
+
+template <bool FULL>
+__device__ __forceinline__ void swap_slots(WarpCell& c, int a, int b) {
+  uchar4 t = c.ver[a];
+  c.ver[a] = c.ver[b];
+  c.ver[b] = t;
+  float4 k = c.u.f.K[a];
+  c.u.f.K[a] = c.u.f.K[b];
+  c.u.f.K[b] = k;
+  float m = c.u.f.M[a];
+  c.u.f.M[a] = c.u.f.M[b];
+  c.u.f.M[b] = m;
+}
+
+__device__ __forceinline__ uint8_t tri_plane(const uchar4& t, int e) {
+  return e == 0 ? t.x : (e == 1 ? t.y : t.z);
+}
+
+// cavity boundary as a circular list over plane ids (convex_cell.cu:618-678)
+__device__ void compute_boundary(WarpCell& c, int nb_v, int& nb_r, int& first,
+                                 int& status) {
+  for (int i = 0; i < kMaxP; ++i) c.bnext[i] = kEnd;
+  first = kEnd;
+  int nb_iter = 0;
+  int t = nb_v;
+  while (nb_r > 0) {
+    if (nb_iter++ > 65535) {
+      status = kInconsistentBoundary;
+      return;
+    }
+    uchar4 tr = c.ver[t];
+    uint8_t p[3] = {tr.x, tr.y, tr.z};
+    bool in_border[3], opp[3];
+    for (int e = 0; e < 3; ++e) in_border[e] = c.bnext[p[e]] != kEnd;
+    for (int e = 0; e < 3; ++e) opp[e] = c.bnext[p[(e + 1) % 3]] == p[e];
+    bool simple = true;
+    for (int e = 0; e < 3; ++e)
+      if (!opp[e] && !opp[(e + 1) % 3] && in_border[(e + 1) % 3]) simple = false;
+    if (!opp[0] && !opp[1] && !opp[2]) {
+      if (first == kEnd) {
+        for (int e = 0; e < 3; ++e) c.bnext[p[e]] = p[(e + 1) % 3];
+        first = p[0];
+      } else {
+        simple = false;
+      }
+    }
+    if (!simple) {
+      t++;
+      if (t == nb_v + nb_r) t = nb_v;
+      continue;
+    }
+    for (int e = 0; e < 3; ++e)
+      if (!opp[e]) c.bnext[p[e]] = p[(e + 1) % 3];
+    for (int e = 0; e < 3; ++e)
+      if (opp[e] && opp[(e + 1) % 3]) {
+        if (first == p[(e + 1) % 3]) first = c.bnext[p[(e + 1) % 3]];
+        c.bnext[p[(e + 1) % 3]] = kEnd;
+      }
+    int last = nb_v + nb_r - 1;
+    uchar4 tmp = c.ver[t];
+    c.ver[t] = c.ver[last];
+    c.ver[last] = tmp;
+    t = nb_v;
+    nb_r--;
+  }
+}
+
+__device__ __forceinline__ int find_edge(const WarpCell& c, int nb_e, int p1, int p2) {
+  int lo = p1 < p2 ? p1 : p2, hi = p1 < p2 ? p2 : p1;
+  for (int e = 0; e < nb_e; ++e) {
+    uchar4 ed = c.edge[e];
+    if (ed.x == lo && ed.y == hi) return e;
+  }
+  return -1;
+}
+
+// Adds plane e (already written to slot nb_p by the caller) and applies the
+// clip whose conflicting vertex slots are in mask[3].  Lane 0 only.
+// FULL: reference bookkeeping (edges, adjacency counts, perturb check);
+// otherwise only the polytope (box clipping for the candidate filter).
+template <bool FULL>
+__device__ void apply_clip(WarpCell& c, CellState& s, const uint32_t* mask_in) {
+  uint32_t m[3] = {mask_in[0], mask_in[1], mask_in[2]};
+  const int cur = s.nb_p;
+  s.nb_p++;
+  // conflict partition, exactly the reference's swap-to-tail loop
+  int nb_v = s.nb_v, nb_r = 0, i = 0;
+  while (i < nb_v) {
+    if (getbit(m, i)) {
+      nb_v--;
+      swap_slots<FULL>(c, i, nb_v);
+      bool bi = getbit(m, i), bn = getbit(m, nb_v);
+      putbit(m, i, bn);
+      putbit(m, nb_v, bi);
+      nb_r++;
+    } else {
+      i++;
+    }
+  }
+  s.nb_v = nb_v;
+  if (nb_v == 0) {
+    s.status = kNoIntersection;
+    return;
+  }
+  int first;
+  compute_boundary(c, nb_v, nb_r, first, s.status);
+  if (s.status != kSuccess) return;
+  if (first == kEnd) return;
+  if (FULL) {
+    int cir = first;
+    do {
+      if (s.nb_e >= kMaxE) {
+        s.status = kEdgeOverflow;
+        return;
+      }
+      uint8_t ha = c.h[cur], hb = c.h[cir];
+      c.edge[s.nb_e] = make_uchar4((uint8_t)(cur < cir ? cur : cir),
+                                   (uint8_t)(cur < cir ? cir : cur), ha > hb ? ha : hb, 0);
+      s.nb_e++;
+      cir = c.bnext[cir];
+    } while (cir != first);
+  }
+  int cir = first;
+  do {
+    int nx = c.bnext[cir];
+    if (s.nb_v + 1 >= kMaxT) {
+      s.status = kTriangleOverflow;
+    } else {
+      uint8_t adj = 0;
+      if (FULL) {
+        int e1 = find_edge(c, s.nb_e, cur, cir), e2 = find_edge(c, s.nb_e, cur, nx),
+            e3 = find_edge(c, s.nb_e, cir, nx);
+        if (e1 < 0 || e2 < 0 || e3 < 0) {
+          // the reference reads out of bounds here; reported as inconsistent
+          s.status = kInconsistentBoundary;
+          return;
+        }
+        adj = c.edge[e1].z;
+        if (c.edge[e2].z > adj) adj = c.edge[e2].z;
+        if (c.edge[e3].z > adj) adj = c.edge[e3].z;
+      }
+      c.ver[s.nb_v] = make_uchar4((uint8_t)cur, (uint8_t)cir, (uint8_t)nx, adj);
+      s.nb_v++;
+    }
+    if (FULL && det3x3_f(c.pl[cur], c.pl[cir], c.pl[nx]) == 0.f) s.status = kNeedsPerturb;
+    if (s.status != kSuccess) return;
+    cir = nx;
+  } while (cir != first);
+}
+
+__device__ __forceinline__ void broadcast_state(CellState& s) {
+  s.nb_v = __shfl_sync(0xffffffffu, s.nb_v, 0);
+  s.nb_p = __shfl_sync(0xffffffffu, s.nb_p, 0);
+  s.nb_e = __shfl_sync(0xffffffffu, s.nb_e, 0);
+  s.status = __shfl_sync(0xffffffffu, s.status, 0);
+}
+
+__device__ __forceinline__ float4 shfl4(float4 v, int src) {
+  v.x = __shfl_sync(0xffffffffu, v.x, src);
+  v.y = __shfl_sync(0xffffffffu, v.y, src);
+  v.z = __shfl_sync(0xffffffffu, v.z, src);
+  v.w = __shfl_sync(0xffffffffu, v.w, src);
+  return v;
+}
+
+__device__ __forceinline__ uint64_t shfl64(uint64_t v, int src) {
+  uint32_t lo = __shfl_sync(0xffffffffu, (uint32_t)v, src);
+  uint32_t hi = __shfl_sync(0xffffffffu, (uint32_t)(v >> 32), src);
+  return ((uint64_t)hi << 32) | lo;
+}
+
+// recompute the filter cofactors of vertex slots [from, to)
+__device__ __forceinline__ void refresh_cofactors(WarpCell& c, int from, int to, int lane) {
+  for (int v = from + lane; v < to; v += 32) {
+    uchar4 t = c.ver[v];
+    float4 K;
+    float M;
+    vertex_cofactors(c.pl[t.x], c.pl[t.y], c.pl[t.z], K, M);
+    c.u.f.K[v] = K;
+    c.u.f.M[v] = M;
+  }
+}
+
+// ------------------------------------------------------------------------
+// the neighbour loop shared by the cell kernel and the box kernel
+// ------------------------------------------------------------------------
+// make_plane(j) builds the plane of list entry j (bisector, or offset
+// bisector for the box kernel).
+template <int PRED, bool FULL, class MakePlane>
+__device__ void clip_list(WarpCell& c, CellState& s, const int32_t* list, int k,
+                          int seed_id, MakePlane make_plane, int lane,
+                          uint32_t& n_pred, uint32_t& n_esc) {
+  for (int base = 0; base < k && s.status == kSuccess; base += 32) {
+    int j = (base + lane < k) ? __ldg(list + base + lane) : -1;
+    uint32_t valid = __ballot_sync(0xffffffffu, j != -1);
+    int count = (~valid == 0u) ? 32 : (__ffs(~valid) - 1);  // up to first -1
+    float4 e_mine = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (lane < count) e_mine = make_plane(j);
+    float se_mine = plane_abs_sum(e_mine);
+    // planes already in the cell that equal this lane's plane
+    uint64_t dup_mine = 0;
+    for (int p = 0; p < s.nb_p; ++p)
+      if (plane_eq(e_mine, c.pl[p])) dup_mine |= 1ull << p;
+    int r = 0;
+    while (r < count) {
+      if (s.nb_p >= kMaxP) {  // new_plane fails before any evaluation
+        s.status = kVertexOverflow;
+        break;
+      }
+      uint32_t mask[3] = {0u, 0u, 0u};
+      int hit = -1;
+      if (s.nb_v <= 32) {
+        int lgV = s.nb_v <= 4 ? 2 : (s.nb_v <= 8 ? 3 : (s.nb_v <= 16 ? 4 : 5));
+        int V = 1 << lgV;
+        int pi = lane >> lgV, vi = lane & (V - 1);
+        int pidx = r + pi;
+        float4 e = shfl4(e_mine, pidx & 31);
+        float se = __shfl_sync(0xffffffffu, se_mine, pidx & 31);
+        uint64_t dup = shfl64(dup_mine, pidx & 31);
+        bool cf = false;
+        if (pidx < count && vi < s.nb_v) cf = in_conflict<PRED>(c, vi, e, se, dup, n_pred, n_esc);
+        uint32_t m = __ballot_sync(0xffffffffu, cf);
+        if (m == 0u) {
+          r += 32 >> lgV;
+          continue;
+        }
+        int pf = (__ffs(m) - 1) >> lgV;
+        mask[0] = (V == 32) ? m : ((m >> (pf << lgV)) & ((1u << V) - 1u));
+        hit = r + pf;
+      } else {
+        float4 e = shfl4(e_mine, r);
+        float se = __shfl_sync(0xffffffffu, se_mine, r);
+        uint64_t dup = shfl64(dup_mine, r);
+        bool any = false;
+        for (int w = 0; w < 3; ++w) {
+          int vi = lane + 32 * w;
+          bool cf = false;
+          if (vi < s.nb_v) cf = in_conflict<PRED>(c, vi, e, se, dup, n_pred, n_esc);
+          mask[w] = __ballot_sync(0xffffffffu, cf);
+          any |= mask[w] != 0u;
+        }
+        if (!any) {
+          r += 1;
+          continue;
+        }
+        hit = r;
+      }
+      // the plane of list entry `hit` clips: write it and update topology
+      float4 e = shfl4(e_mine, hit);
+      int jn = __shfl_sync(0xffffffffu, j, hit);
+      if (lane == 0) {
+        const int cur = s.nb_p;
+        c.pl[cur] = e;
+        c.h[cur] = 1;
+        c.id2[cur] = make_int2(seed_id < jn ? seed_id : jn, seed_id < jn ? jn : seed_id);
+        apply_clip<FULL>(c, s, mask);
+      }
+      __syncwarp();
+      broadcast_state(s);
+      // new vertices sit at the end; the surviving ones keep their
+      // cofactors (moved by the partition), so rebuild from the first new
+      if (s.status == kSuccess) {
+        // the vertices created by this clip are the last ones; their count
+        // is at most nb_v, so recompute slots whose planes include the new
+        // plane index (they are exactly the new ones)
+        const int cur = s.nb_p - 1;
+        for (int v = lane; v < s.nb_v; v += 32) {
+          uchar4 t = c.ver[v];
+          if (t.x == cur) {
+            float4 K;
+            float M;
+            vertex_cofactors(c.pl[t.x], c.pl[t.y], c.pl[t.z], K, M);
+            c.u.f.K[v] = K;
+            c.u.f.M[v] = M;
+          }
+        }
+      }
+      __syncwarp();
+      // later planes of this chunk identical to the new one
+      if (plane_eq(e_mine, e)) dup_mine |= 1ull << (s.nb_p - 1);
+      if (s.status != kSuccess) break;
+      r = hit + 1;
+    }
+    if (count < 32) break;  // the list ended (-1) inside this chunk
+  }
+}
+
+// ------------------------------------------------------------------------
+// cell kernel
+// ------------------------------------------------------------------------
+__device__ __forceinline__ void tri2plane_d(const double* v0, const double* v1,
+                                            const double* v2, double* out) {
+  double ax = v1[0] - v0[0], ay = v1[1] - v0[1], az = v1[2] - v0[2];
+  double bx = v2[0] - v0[0], by = v2[1] - v0[1], bz = v2[2] - v0[2];
+  double nx = ay * bz - az * by;
+  double ny = az * bx - ax * bz;
+  double nz = ax * by - ay * bx;
+  out[0] = nx;
+  out[1] = ny;
+  out[2] = nz;
+  out[3] = -(v0[0] * nx + v0[1] * ny + v0[2] * nz);
+}
+
+__device__ __forceinline__ void bisector_d(const double* S, const double* B, double* out) {
+  double dx = S[0] - B[0], dy = S[1] - B[1], dz = S[2] - B[2];
+  double ax = S[0] + B[0], ay = S[1] + B[1], az = S[2] + B[2];
+  double dot = (ax * dx + ay * dy + az * dz) + (B[3] - S[3]);
+  out[0] = dx;
+  out[1] = dy;
+  out[2] = dz;
+  out[3] = -dot * 0.5;
+}
+
+__device__ __forceinline__ double det3d(double a11, double a12, double a13, double a21,
+                                        double a22, double a23, double a31, double a32,
+                                        double a33) {
+  return a11 * (a22 * a33 - a23 * a32) - a21 * (a12 * a33 - a13 * a32) +
+         a31 * (a12 * a23 - a13 * a22);
+}
+
+__device__ __forceinline__ void vertex_d(const double* a, const double* b, const double* c,
+                                         double* out) {
+  double x = -det3d(a[3], a[1], a[2], b[3], b[1], b[2], c[3], c[1], c[2]);
+  double y = -det3d(a[0], a[3], a[2], b[0], b[3], b[2], c[0], c[3], c[2]);
+  double z = -det3d(a[0], a[1], a[3], b[0], b[1], b[3], c[0], c[1], c[3]);
+  double w = det3d(a[0], a[1], a[2], b[0], b[1], b[2], c[0], c[1], c[2]);
+  out[0] = x / w;
+  out[1] = y / w;
+  out[2] = z / w;
+}
+
+__device__ __forceinline__ void project_d(const double* P, const double* pl, double* out) {
+  double n2 = pl[0] * pl[0] + pl[1] * pl[1] + pl[2] * pl[2];
+  double lam = n2 > 0.0 ? (pl[0] * P[0] + pl[1] * P[1] + pl[2] * P[2] + pl[3]) / n2 : 0.0;
+  out[0] = P[0] - lam * pl[0];
+  out[1] = P[1] - lam * pl[1];
+  out[2] = P[2] - lam * pl[2];
+}
+
+// signed volume of the 6 flag tets of one vertex (the decomposition of
+// convex_cell.cu:986-1069, in FP64): C seed, A vertex, feet of C on the 3
+// faces and on the 3 edge lines through A
+__device__ double vertex_volume_d(const double* C, const double* A, const double* f0,
+                                  const double* f1, const double* f2) {
+  const double* f[3] = {f0, f1, f2};
+  double P[6][3];
+  for (int i = 0; i < 3; ++i) project_d(C, f[i], P[2 * i]);
+  for (int i = 0; i < 3; ++i) {
+    const double* u = f[i];
+    const double* v = f[(i + 1) % 3];
+    double n[4] = {u[1] * v[2] - u[2] * v[1], u[2] * v[0] - u[0] * v[2],
+                   u[0] * v[1] - u[1] * v[0], 0.0};
+    n[3] = -(C[0] * n[0] + C[1] * n[1] + C[2] * n[2]);
+    project_d(A, n, P[2 * i + 1]);
+  }
+  double vol = 0.0;
+  for (int i = 0; i < 6; ++i) {
+    const double* p = P[i];
+    const double* q = P[(i + 1) % 6];
+    double a0 = p[0] - A[0], a1 = p[1] - A[1], a2 = p[2] - A[2];
+    double b0 = q[0] - A[0], b1 = q[1] - A[1], b2 = q[2] - A[2];
+    double c0 = C[0] - A[0], c1 = C[1] - A[1], c2 = C[2] - A[2];
+    vol += -det3d(a0, a1, a2, b0, b1, b2, c0, c1, c2) / 6.0;
+  }
+  return vol;
+}
+
+template <int PRED>
+__global__ void __launch_bounds__(kClipMaxThreads) clip_cells_kernel(ClipParams p) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31;
+  const int wid = threadIdx.x >> 5;
+  WarpCell& c = reinterpret_cast<WarpCell*>(smem_raw)[wid];
+  uint32_t n_pred = 0, n_esc = 0;
+
+  for (;;) {
+    long long q = 0;
+    if (lane == 0) q = (long long)atomicAdd(p.work, 1ull);
+    q = __shfl_sync(0xffffffffu, q, 0);
+    if (q >= p.n_pairs) break;
+    const int t = __ldg(p.pair_tet + q);
+    const int sid = __ldg(p.pair_site + q);
+    const float4 seed = __ldg(p.site4f + sid);
+
+    // ---- cell = tet (convex_cell.cu:116-214)
+    const int4 tv = __ldg(p.tets + t);
+    const int tvs[4] = {tv.x, tv.y, tv.z, tv.w};
+    if (lane < 4) {
+      int a = tvs[cFaceLv[lane][0]], b = tvs[cFaceLv[lane][1]], d = tvs[cFaceLv[lane][2]];
+      float3 v0 = make_float3(p.vert3f[3 * a], p.vert3f[3 * a + 1], p.vert3f[3 * a + 2]);
+      float3 v1 = make_float3(p.vert3f[3 * b], p.vert3f[3 * b + 1], p.vert3f[3 * b + 2]);
+      float3 v2 = make_float3(p.vert3f[3 * d], p.vert3f[3 * d + 1], p.vert3f[3 * d + 2]);
+      c.pl[lane] = tri2plane_f(v0, v1, v2);
+      c.h[lane] = (uint8_t)__ldg(p.f_adjs + 4 * t + lane);
+      c.id2[lane] = make_int2(__ldg(p.f_ids + 4 * t + lane), -1);
+    } else if (lane < 8) {
+      int i = lane - 4;
+      c.ver[i] = make_uchar4((uint8_t)cTetTri[i][0], (uint8_t)cTetTri[i][1],
+                             (uint8_t)cTetTri[i][2], (uint8_t)__ldg(p.v_adjs + tvs[i]));
+    } else if (lane < 14) {
+      int e = lane - 8;
+      c.edge[e] = make_uchar4((uint8_t)cEdgeFaces[e][0], (uint8_t)cEdgeFaces[e][1],
+                              __ldg(p.e_adj6 + 6 * (long long)t + e), 0);
+    }
+    __syncwarp();
+    CellState s;
+    s.nb_v = 4;
+    s.nb_p = 4;
+    s.nb_e = 6;
+    s.status = kSuccess;
+    if (PRED == RPD_PRED_FP32_FILTER) {
+      refresh_cofactors(c, 0, 4, lane);
+      __syncwarp();
+    }
+
+    // ---- clip by the site's neighbour list
+    const float4* site4f = p.site4f;
+    auto make_plane = [&](int j) { return bisector_f(seed, __ldg(site4f + j)); };
+    clip_list<PRED, true>(c, s, p.nbr + (long long)sid * p.k, p.k, sid, make_plane, lane,
+                          n_pred, n_esc);
+
+    // ---- emit
+    rpd_cell_header hd;
+    hd.tet_id = t;
+    hd.site_id = sid;
+    hd.status = s.status;
+    hd.nb_v = hd.nb_p = hd.nb_e = 0;
+    hd.flags = 0;
+    hd.offset = 0;
+    hd.volume = 0.0;
+    if (s.status == kSuccess) {
+      PayloadLayout L(s.nb_v, s.nb_p, s.nb_e);
+      unsigned long long off = 0;
+      if (lane == 0) off = atomicAdd(p.payload_cursor, (unsigned long long)L.total);
+      off = __shfl_sync(0xffffffffu, off, 0);
+      if (off + L.total > p.payload_cap) {
+        hd.status = kPayloadFull;
+      } else {
+        uint8_t* dst = p.payload + off;
+        for (int i = lane; i < s.nb_p; i += 32) {
+          reinterpret_cast<float4*>(dst + L.plane)[i] = c.pl[i];
+          reinterpret_cast<int2*>(dst + L.id2)[i] = c.id2[i];
+        }
+        for (int i = lane; i < s.nb_v; i += 32)
+          reinterpret_cast<uchar4*>(dst + L.ver)[i] = c.ver[i];
+        for (int i = lane; i < s.nb_e; i += 32)
+          reinterpret_cast<uchar4*>(dst + L.edge)[i] = c.edge[i];
+        for (int i = lane; i < (int)al16(s.nb_p); i += 32)
+          dst[L.h + i] = i < s.nb_p ? c.h[i] : 0;
+        // pad bytes of the id2 / ver / edge sections
+        for (int i = 2 * s.nb_p + lane; i < (int)(al16(8u * s.nb_p) / 4); i += 32)
+          reinterpret_cast<int32_t*>(dst + L.id2)[i] = 0;
+        for (int i = s.nb_v + lane; i < (int)(al16(4u * s.nb_v) / 4); i += 32)
+          reinterpret_cast<uint32_t*>(dst + L.ver)[i] = 0u;
+        for (int i = s.nb_e + lane; i < (int)(al16(4u * s.nb_e) / 4); i += 32)
+          reinterpret_cast<uint32_t*>(dst + L.edge)[i] = 0u;
+        double* xyz = reinterpret_cast<double*>(dst + L.xyz);
+        double vol = 0.0;
+        if (p.geometry) {
+          __syncwarp();
+          // FP64 planes from FP64 inputs (cofactor storage is dead now)
+          const double* S = p.site4d + 4 * (long long)sid;
+          for (int i = lane; i < s.nb_p; i += 32) {
+            double* out = c.u.pd[i];
+            if (i < 4) {
+              int a = tvs[cFaceLv[i][0]], b = tvs[cFaceLv[i][1]], d = tvs[cFaceLv[i][2]];
+              tri2plane_d(p.vert3d + 3 * (long long)a, p.vert3d + 3 * (long long)b,
+                          p.vert3d + 3 * (long long)d, out);
+            } else {
+              int2 id = c.id2[i];
+              int other = id.x == sid ? id.y : id.x;
+              bisector_d(S, p.site4d + 4 * (long long)other, out);
+            }
+          }
+          __syncwarp();
+          for (int v = lane; v < s.nb_v; v += 32) {
+            uchar4 tr = c.ver[v];
+            double A[3];
+            vertex_d(c.u.pd[tr.x], c.u.pd[tr.y], c.u.pd[tr.z], A);
+            xyz[3 * v] = A[0];
+            xyz[3 * v + 1] = A[1];
+            xyz[3 * v + 2] = A[2];
+            vol += vertex_volume_d(S, A, c.u.pd[tr.x], c.u.pd[tr.y], c.u.pd[tr.z]);
+          }
+          for (int o = 16; o > 0; o >>= 1) vol += __shfl_xor_sync(0xffffffffu, vol, o);
+        } else {
+          for (int i = lane; i < 3 * s.nb_v; i += 32) xyz[i] = 0.0;
+        }
+        hd.nb_v = (uint8_t)s.nb_v;
+        hd.nb_p = (uint8_t)s.nb_p;
+        hd.nb_e = (uint8_t)s.nb_e;
+        hd.offset = off;
+        hd.volume = vol;
+      }
+    }
+    if (lane == 0) p.headers[q] = hd;
+    __syncwarp();
+  }
+  // statistics
+  for (int o = 16; o > 0; o >>= 1) {
+    n_pred += __shfl_xor_sync(0xffffffffu, n_pred, o);
+    n_esc += __shfl_xor_sync(0xffffffffu, n_esc, o);
+  }
+  if (lane == 0) {
+    atomicAdd(p.counters + 0, (unsigned long long)n_pred);
+    atomicAdd(p.counters + 1, (unsigned long long)n_esc);
+  }
+}
+
+// ------------------------------------------------------------------------
+// box kernel: bounding box of a site's cell grown by an offset, used to
+// enumerate candidate tets (see rpd_pairs.cu)
+// ------------------------------------------------------------------------
+__global__ void __launch_bounds__(kClipMaxThreads) site_box_kernel(BoxParams p) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31;
+  const int wid = threadIdx.x >> 5;
+  WarpCell& c = reinterpret_cast<WarpCell*>(smem_raw)[wid];
+  uint32_t n_pred = 0, n_esc = 0;
+  const int warps_total = (gridDim.x * blockDim.x) >> 5;
+  for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < p.n_site; i += warps_total) {
+    float lo[3] = {p.box_lo.x, p.box_lo.y, p.box_lo.z};
+    float hi[3] = {p.box_hi.x, p.box_hi.y, p.box_hi.z};
+    if (p.flags[i] != 1u) {
+      if (lane == 0) {
+        p.site_box[2 * i] = make_float4(1.f, 1.f, 1.f, 0.f);  // empty box
+        p.site_box[2 * i + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+      continue;
+    }
+    const float4 seed = p.site4f[i];
+    // box planes x>=lo, x<=hi, y>=lo, y<=hi, z>=lo, z<=hi
+    if (lane < 6) {
+      int ax = lane >> 1;
+      float4 pl = make_float4(0.f, 0.f, 0.f, 0.f);
+      float* q = reinterpret_cast<float*>(&pl);
+      if ((lane & 1) == 0) {
+        q[ax] = 1.f;
+        pl.w = -lo[ax];
+      } else {
+        q[ax] = -1.f;
+        pl.w = hi[ax];
+      }
+      c.pl[lane] = pl;
+    } else if (lane < 14) {
+      // corner (sx, sy, sz): planes X = sx, Y = 2 + sy, Z = 4 + sz, ordered
+      // (X, Z, Y) for even parity and (X, Y, Z) for odd parity: the eight
+      // dual triangles are then consistently oriented with the same sign as
+      // the tet's (det4x4 of the triangle's planes with (0,0,0,1) < 0), so
+      // "det > 0" means "outside" for both
+      int v = lane - 6;
+      int sx = v & 1, sy = (v >> 1) & 1, sz = (v >> 2) & 1;
+      uint8_t X = (uint8_t)sx, Y = (uint8_t)(2 + sy), Z = (uint8_t)(4 + sz);
+      c.ver[v] = ((sx + sy + sz) & 1) == 0 ? make_uchar4(X, Z, Y, 0) : make_uchar4(X, Y, Z, 0);
+    }
+    __syncwarp();
+    CellState s;
+    s.nb_v = 8;
+    s.nb_p = 6;
+    s.nb_e = 0;
+    s.status = kSuccess;
+    refresh_cofactors(c, 0, 8, lane);
+    __syncwarp();
+    const float4* site4f = p.site4f;
+    const float R = p.offset_r, E = p.offset_e;
+    auto make_plane = [&](int j) {
+      float4 b = __ldg(site4f + j);
+      float4 e = bisector_f(seed, b);
+      float D = sqrtf(e.x * e.x + e.y * e.y + e.z * e.z);
+      // push the plane outwards by R plus the float error of the rule's
+      // power distances (E / 2D) plus a relative slack
+      float slack = 1e-5f * (fabsf(e.w) + D * p.coord_scale);
+      float d = e.w + R * D + 0.5f * E + slack;
+      if (!(D > 0.f) || !(d < 3.0e38f)) return make_float4(0.f, 0.f, 0.f, 1.f);  // no constraint
+      return make_float4(e.x, e.y, e.z, d);
+    };
+    clip_list<RPD_PRED_FP32_FILTER, false>(c, s, p.nbr + (long long)i * p.k, p.k, i, make_plane,
+                                           lane, n_pred, n_esc);
+    float bl[3], bh[3];
+    if (s.status == kSuccess) {
+      bl[0] = bl[1] = bl[2] = 3.0e38f;
+      bh[0] = bh[1] = bh[2] = -3.0e38f;
+      for (int v = lane; v < s.nb_v; v += 32) {
+        uchar4 tr = c.ver[v];
+        double a[4], b[4], d[4], X[3];
+        float4 fa = c.pl[tr.x], fb = c.pl[tr.y], fd = c.pl[tr.z];
+        a[0] = fa.x; a[1] = fa.y; a[2] = fa.z; a[3] = fa.w;
+        b[0] = fb.x; b[1] = fb.y; b[2] = fb.z; b[3] = fb.w;
+        d[0] = fd.x; d[1] = fd.y; d[2] = fd.z; d[3] = fd.w;
+        vertex_d(a, b, d, X);
+        for (int k = 0; k < 3; ++k) {
+          float xl = __double2float_rd(X[k]), xh = __double2float_ru(X[k]);
+          if (!(X[k] == X[k])) { xl = lo[k]; xh = hi[k]; }
+          bl[k] = fminf(bl[k], xl);
+          bh[k] = fmaxf(bh[k], xh);
+        }
+      }
+      for (int o = 16; o > 0; o >>= 1)
+        for (int k = 0; k < 3; ++k) {
+          bl[k] = fminf(bl[k], __shfl_xor_sync(0xffffffffu, bl[k], o));
+          bh[k] = fmaxf(bh[k], __shfl_xor_sync(0xffffffffu, bh[k], o));
+        }
+      for (int k = 0; k < 3; ++k) {
+        float m = 1e-3f * (bh[k] - bl[k]) + p.abs_margin;
+        bl[k] = fmaxf(bl[k] - m, lo[k]);
+        bh[k] = fminf(bh[k] + m, hi[k]);
+      }
+    } else if (s.status == kNoIntersection) {
+      bl[0] = bl[1] = bl[2] = 1.f;
+      bh[0] = bh[1] = bh[2] = 0.f;
+    } else {
+      for (int k = 0; k < 3; ++k) {
+        bl[k] = lo[k];
+        bh[k] = hi[k];
+      }
+    }
+    if (lane == 0) {
+      p.site_box[2 * i] = make_float4(bl[0], bl[1], bl[2], (float)s.status);
+      p.site_box[2 * i + 1] = make_float4(bh[0], bh[1], bh[2], 0.f);
+    }
+    __syncwarp();
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    n_pred += __shfl_xor_sync(0xffffffffu, n_pred, o);
+    n_esc += __shfl_xor_sync(0xffffffffu, n_esc, o);
+  }
+  if (lane == 0 && p.counters) {
+    atomicAdd(p.counters + 0, (unsigned long long)n_pred);
+    atomicAdd(p.counters + 1, (unsigned long long)n_esc);
+  }
+}
+
+size_t clip_smem_per_warp() { return sizeof(WarpCell); }
+
+int clip_blocks_per_sm(int pred_mode, int warps) {
+  size_t smem = sizeof(WarpCell) * warps;
+  int n = 0;
+  if (pred_mode == RPD_PRED_FP32_FILTER) {
+    cudaFuncSetAttribute(clip_cells_kernel<RPD_PRED_FP32_FILTER>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, clip_cells_kernel<RPD_PRED_FP32_FILTER>,
+                                                  warps * 32, smem);
+  } else {
+    cudaFuncSetAttribute(clip_cells_kernel<RPD_PRED_FP64>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, clip_cells_kernel<RPD_PRED_FP64>,
+                                                  warps * 32, smem);
+  }
+  return n > 0 ? n : 1;
+}
+
+int box_blocks_per_sm(int warps) {
+  size_t smem = sizeof(WarpCell) * warps;
+  int n = 0;
+  cudaFuncSetAttribute(site_box_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, site_box_kernel, warps * 32, smem);
+  return n > 0 ? n : 1;
+}
+
+cudaError_t launch_clip_cells(const ClipParams& p, int pred_mode, int blocks, int warps,
+                              cudaStream_t st) {
+  size_t smem = sizeof(WarpCell) * warps;
+  if (pred_mode == RPD_PRED_FP32_FILTER) {
+    cudaFuncSetAttribute(clip_cells_kernel<RPD_PRED_FP32_FILTER>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    clip_cells_kernel<RPD_PRED_FP32_FILTER><<<blocks, warps * 32, smem, st>>>(p);
+  } else {
+    cudaFuncSetAttribute(clip_cells_kernel<RPD_PRED_FP64>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    clip_cells_kernel<RPD_PRED_FP64><<<blocks, warps * 32, smem, st>>>(p);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_site_box(const BoxParams& p, int blocks, int warps, cudaStream_t st) {
+  size_t smem = sizeof(WarpCell) * warps;
+  cudaFuncSetAttribute(site_box_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  site_box_kernel<<<blocks, warps * 32, smem, st>>>(p);
+  return cudaGetLastError();
+}
+
+}  // namespace rpd

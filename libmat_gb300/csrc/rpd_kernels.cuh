@@ -1,0 +1,129 @@
+// rpd_kernels.cuh -- kernel parameter blocks and launchers (host-callable).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+#include "../../include/rpd_gb300.h"
+
+namespace rpd {
+
+constexpr int kClipMaxThreads = 512;
+
+struct ClipParams {
+  const float* vert3f;   // n_vert x 3, float copies of the mesh vertices
+  const double* vert3d;  // n_vert x 3
+  const int4* tets;
+  const int32_t* v_adjs;
+  const uint8_t* e_adj6;  // n_tet x 6
+  const int32_t* f_adjs;  // n_tet x 4
+  const int32_t* f_ids;   // n_tet x 4
+  const float4* site4f;   // n_site, (x, y, z, w) float
+  const double* site4d;   // n_site x 4
+  const int32_t* nbr;     // n_site x k, -1 padded
+  int k;
+  const int32_t* pair_tet;
+  const int32_t* pair_site;
+  long long n_pairs;
+  rpd_cell_header* headers;  // n_pairs
+  uint8_t* payload;
+  unsigned long long* payload_cursor;
+  unsigned long long payload_cap;
+  unsigned long long* work;      // work-queue counter, zeroed before launch
+  unsigned long long* counters;  // [0] predicates, [1] escalated
+  int geometry;
+};
+
+struct BoxParams {
+  const float4* site4f;
+  const uint32_t* flags;
+  const int32_t* nbr;
+  int k;
+  int n_site;
+  float4 box_lo, box_hi;  // mesh box grown by offset_r
+  float offset_r;         // largest distance of a tet vertex to its centroid
+  float offset_e;         // bound on the float error of a power distance
+  float coord_scale;      // largest coordinate magnitude
+  float abs_margin;
+  float4* site_box;       // n_site x 2: (lo, status), (hi, 0)
+  unsigned long long* counters;
+};
+
+size_t clip_smem_per_warp();
+int clip_blocks_per_sm(int pred_mode, int warps);
+int box_blocks_per_sm(int warps);
+cudaError_t launch_clip_cells(const ClipParams& p, int pred_mode, int blocks, int warps,
+                              cudaStream_t st);
+cudaError_t launch_site_box(const BoxParams& p, int blocks, int warps, cudaStream_t st);
+
+// ---- uniform grids, kNN, candidate pairs, scans (rpd_pairs.cu)
+struct Grid {
+  float3 lo;
+  float inv_cell;  // 1 / cell size
+  float cell;
+  int nx, ny, nz;
+};
+
+// exclusive scan of n int32 counts into out (n + 1 entries, out[n] = total);
+// temp must hold scan_temp_ints(n) ints
+size_t scan_temp_ints(long long n);
+cudaError_t scan_exclusive(const int32_t* in, int32_t* out, long long n, int32_t* temp,
+                           cudaStream_t st);
+
+// bins points into grid cells: cell_of[n], cell_start[n_cells + 1],
+// cell_items[n] (ascending item id within a cell)
+cudaError_t grid_build_sites(const float4* pts, int n, const Grid& g, int32_t* cell_of,
+                             int32_t* cell_count, int32_t* cell_start, int32_t* cell_fill,
+                             int32_t* cell_items, int32_t* scan_tmp, cudaStream_t st);
+cudaError_t grid_build_tets(const float* vert3f, const int4* tets, int n_tet, const Grid& g,
+                            float4* centroid, int32_t* cell_of, int32_t* cell_count,
+                            int32_t* cell_start, int32_t* cell_fill, int32_t* cell_items,
+                            int32_t* scan_tmp, cudaStream_t st);
+
+// k smallest power-bisector distances per site (ties by id); lists in
+// distance order or sorted by id
+cudaError_t launch_knn(const float4* site4f, int n_site, const Grid& g,
+                       const int32_t* cell_start, const int32_t* cell_items, int k,
+                       float w_max, int order_by_id, int32_t* nbr, float* keys,
+                       int32_t* status, cudaStream_t st);
+
+// candidate pairs: per site, tets whose centroid lies in the site's box and
+// that pass the reference rule; appends (tet, site) and counts per tet
+struct PairParams {
+  const float* vert3f;
+  const int4* tets;
+  const float4* centroid;
+  Grid tg;
+  const int32_t* tcell_start;
+  const int32_t* tcell_items;
+  const float4* site4f;
+  const uint32_t* flags;
+  const int32_t* nbr;
+  int k;
+  int n_site;
+  const float4* site_box;
+  int2* pair_buf;            // (tet, site)
+  unsigned long long* pair_cursor;
+  long long pair_cap;
+  int32_t* tet_count;
+};
+cudaError_t launch_pairs(const PairParams& p, cudaStream_t st);
+
+// scatter the pair buffer into per-tet CSR and sort sites in each tet
+cudaError_t pairs_to_csr(const int2* pair_buf, long long n_pairs, int n_tet,
+                         const int32_t* tet_offsets, int32_t* tet_fill, int32_t* pair_site,
+                         int32_t* pair_tet, int32_t* tet_k_out, cudaStream_t st);
+
+// compaction of emitted cells (status success) in pair order
+cudaError_t compact_cells(const rpd_cell_header* pair_headers, long long n_pairs,
+                          int32_t* flag_tmp, int32_t* pos_tmp, int32_t* scan_tmp,
+                          rpd_cell_header* out, long long* n_out_dev,
+                          unsigned long long* status_hist, cudaStream_t st);
+
+// reference site_knn layout -> row-major lists; validation of ids
+cudaError_t neighbors_from_reference(const int32_t* ref, int k, int n_site, int32_t* nbr,
+                                     cudaStream_t st);
+
+}  // namespace rpd

@@ -1,0 +1,597 @@
+// rpd_pairs.cu -- everything around the clip kernel: uniform grids, the
+// k-nearest-power-neighbour build, candidate (tet, site) pairs, scans and
+// compaction.
+//
+// Reference counterparts:
+//   * neighbour lists: libmat takes each site's regular-triangulation
+//     neighbours from CGAL on the CPU (src/rpd3d_base/triangulation.cxx:
+//     62-144, :442-558); here the lists are the k smallest power-bisector
+//     distances, found by a ring search over a uniform grid of sites.
+//   * candidate pairs: libmat tests every (tet, site) with the rule of
+//     tet_sphere_relations_dev (src/rpd3d/voronoi.cu:154-193) -- tet t is a
+//     candidate of flagged site i iff for every listed neighbour m some tet
+//     vertex v has pd_m(v) > pd_i(v), power distances computed as in
+//     src/rpd3d/kNN-CUDA/knncuda.cu:21-94 + :130-160 -- on dense n_site x
+//     n_vert and n_site x n_tet matrices, then gathers them on the host
+//     (:265-317).  Here the same rule is applied only to tets whose centroid
+//     lies in a per-site box that provably contains every tet passing it
+//     (see site_box_kernel), and the pairs are written as a per-tet CSR with
+//     sites ascending, the reference's tet_knn order.
+// Compiled with -fmad=false: the power distances and bisector keys are the
+// reference's / oracle's float expressions evaluated without contraction.
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "rpd_common.cuh"
+#include "rpd_kernels.cuh"
+
+namespace rpd {
+
+// ------------------------------------------------------------------------
+// scan
+// ------------------------------------------------------------------------
+constexpr int kScanBlock = 1024;
+
+size_t scan_temp_ints(long long n) { return (size_t)((n + kScanBlock - 1) / kScanBlock) + 1; }
+
+__device__ __forceinline__ int warp_incl_scan(int v, int lane) {
+  for (int o = 1; o < 32; o <<= 1) {
+    int t = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += t;
+  }
+  return v;
+}
+
+// block-wide exclusive scan of one value per thread; returns the exclusive
+// prefix and writes the block total to *total
+__device__ int block_excl_scan(int v, int* total) {
+  __shared__ int wsum[32];
+  __shared__ int wtot;
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int incl = warp_incl_scan(v, lane);
+  if (lane == 31) wsum[wid] = incl;
+  __syncthreads();
+  if (wid == 0) {
+    int nw = blockDim.x >> 5;
+    int x = lane < nw ? wsum[lane] : 0;
+    int xi = warp_incl_scan(x, lane);
+    if (lane < nw) wsum[lane] = xi - x;
+    if (lane == 31) wtot = xi;
+  }
+  __syncthreads();
+  int res = incl - v + wsum[wid];
+  if (total) *total = wtot;
+  __syncthreads();
+  return res;
+}
+
+__global__ void scan_reduce_kernel(const int32_t* in, long long n, int32_t* block_sums) {
+  long long i = (long long)blockIdx.x * kScanBlock + threadIdx.x;
+  int v = i < n ? in[i] : 0;
+  int tot;
+  block_excl_scan(v, &tot);
+  if (threadIdx.x == 0) block_sums[blockIdx.x] = tot;
+}
+
+__global__ void scan_blocksums_kernel(int32_t* sums, int nb) {
+  int carry = 0;
+  for (int base = 0; base < nb; base += kScanBlock) {
+    int i = base + threadIdx.x;
+    int v = i < nb ? sums[i] : 0;
+    int tot;
+    int ex = block_excl_scan(v, &tot);
+    if (i < nb) sums[i] = ex + carry;
+    carry += tot;
+  }
+  if (threadIdx.x == 0) sums[nb] = carry;
+}
+
+__global__ void scan_apply_kernel(const int32_t* in, long long n, const int32_t* block_sums,
+                                  int nb, int32_t* out) {
+  long long i = (long long)blockIdx.x * kScanBlock + threadIdx.x;
+  int v = i < n ? in[i] : 0;
+  int ex = block_excl_scan(v, nullptr);
+  if (i < n) out[i] = ex + block_sums[blockIdx.x];
+  if (blockIdx.x == 0 && threadIdx.x == 0) out[n] = block_sums[nb];
+}
+
+cudaError_t scan_exclusive(const int32_t* in, int32_t* out, long long n, int32_t* temp,
+                           cudaStream_t st) {
+  int nb = (int)((n + kScanBlock - 1) / kScanBlock);
+  if (nb == 0) {
+    return cudaMemsetAsync(out, 0, sizeof(int32_t), st);
+  }
+  scan_reduce_kernel<<<nb, kScanBlock, 0, st>>>(in, n, temp);
+  scan_blocksums_kernel<<<1, kScanBlock, 0, st>>>(temp, nb);
+  scan_apply_kernel<<<nb, kScanBlock, 0, st>>>(in, n, temp, nb, out);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------------
+// uniform grids
+// ------------------------------------------------------------------------
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+__device__ __forceinline__ int cell_index(const Grid& g, float x, float y, float z) {
+  int ix = clampi((int)floorf((x - g.lo.x) * g.inv_cell), 0, g.nx - 1);
+  int iy = clampi((int)floorf((y - g.lo.y) * g.inv_cell), 0, g.ny - 1);
+  int iz = clampi((int)floorf((z - g.lo.z) * g.inv_cell), 0, g.nz - 1);
+  return ix + g.nx * (iy + g.ny * iz);
+}
+
+__global__ void bin_points_kernel(const float4* pts, int n, Grid g, int32_t* cell_of,
+                                  int32_t* cell_count) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float4 p = pts[i];
+  int c = cell_index(g, p.x, p.y, p.z);
+  cell_of[i] = c;
+  atomicAdd(cell_count + c, 1);
+}
+
+__global__ void fill_cells_kernel(int n, const int32_t* cell_of, const int32_t* cell_start,
+                                  int32_t* cell_fill, int32_t* cell_items) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int c = cell_of[i];
+  int slot = atomicAdd(cell_fill + c, 1);
+  cell_items[cell_start[c] + slot] = i;
+}
+
+// insertion sort of each cell's item list (short lists): deterministic order
+__global__ void sort_cells_kernel(int n_cells, const int32_t* cell_start, int32_t* items) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n_cells) return;
+  int b = cell_start[c], e = cell_start[c + 1];
+  for (int i = b + 1; i < e; ++i) {
+    int v = items[i];
+    int j = i - 1;
+    while (j >= b && items[j] > v) {
+      items[j + 1] = items[j];
+      --j;
+    }
+    items[j + 1] = v;
+  }
+}
+
+static cudaError_t grid_finish(int n, const Grid& g, const int32_t* cell_of, int32_t* cell_count,
+                               int32_t* cell_start, int32_t* cell_fill, int32_t* cell_items,
+                               int32_t* scan_tmp, cudaStream_t st) {
+  long long n_cells = (long long)g.nx * g.ny * g.nz;
+  cudaError_t err = scan_exclusive(cell_count, cell_start, n_cells, scan_tmp, st);
+  if (err != cudaSuccess) return err;
+  cudaMemsetAsync(cell_fill, 0, sizeof(int32_t) * n_cells, st);
+  fill_cells_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, cell_of, cell_start, cell_fill, cell_items);
+  sort_cells_kernel<<<(int)((n_cells + 255) / 256), 256, 0, st>>>((int)n_cells, cell_start,
+                                                                 cell_items);
+  return cudaGetLastError();
+}
+
+cudaError_t grid_build_sites(const float4* pts, int n, const Grid& g, int32_t* cell_of,
+                             int32_t* cell_count, int32_t* cell_start, int32_t* cell_fill,
+                             int32_t* cell_items, int32_t* scan_tmp, cudaStream_t st) {
+  long long n_cells = (long long)g.nx * g.ny * g.nz;
+  cudaMemsetAsync(cell_count, 0, sizeof(int32_t) * n_cells, st);
+  if (n > 0) bin_points_kernel<<<(n + 255) / 256, 256, 0, st>>>(pts, n, g, cell_of, cell_count);
+  return grid_finish(n, g, cell_of, cell_count, cell_start, cell_fill, cell_items, scan_tmp, st);
+}
+
+// centroid and radius (largest vertex distance) of every tet
+__global__ void tet_centroid_kernel(const float* v, const int4* tets, int n_tet, float4* out) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_tet) return;
+  int4 q = tets[t];
+  int id[4] = {q.x, q.y, q.z, q.w};
+  float cx = 0.f, cy = 0.f, cz = 0.f;
+  for (int k = 0; k < 4; ++k) {
+    cx += v[3 * id[k]];
+    cy += v[3 * id[k] + 1];
+    cz += v[3 * id[k] + 2];
+  }
+  cx *= 0.25f;
+  cy *= 0.25f;
+  cz *= 0.25f;
+  float r2 = 0.f;
+  for (int k = 0; k < 4; ++k) {
+    float dx = v[3 * id[k]] - cx, dy = v[3 * id[k] + 1] - cy, dz = v[3 * id[k] + 2] - cz;
+    r2 = fmaxf(r2, dx * dx + dy * dy + dz * dz);
+  }
+  out[t] = make_float4(cx, cy, cz, sqrtf(r2));
+}
+
+cudaError_t grid_build_tets(const float* vert3f, const int4* tets, int n_tet, const Grid& g,
+                            float4* centroid, int32_t* cell_of, int32_t* cell_count,
+                            int32_t* cell_start, int32_t* cell_fill, int32_t* cell_items,
+                            int32_t* scan_tmp, cudaStream_t st) {
+  if (n_tet > 0)
+    tet_centroid_kernel<<<(n_tet + 255) / 256, 256, 0, st>>>(vert3f, tets, n_tet, centroid);
+  long long n_cells = (long long)g.nx * g.ny * g.nz;
+  cudaMemsetAsync(cell_count, 0, sizeof(int32_t) * n_cells, st);
+  if (n_tet > 0)
+    bin_points_kernel<<<(n_tet + 255) / 256, 256, 0, st>>>(centroid, n_tet, g, cell_of, cell_count);
+  return grid_finish(n_tet, g, cell_of, cell_count, cell_start, cell_fill, cell_items, scan_tmp,
+                     st);
+}
+
+// ------------------------------------------------------------------------
+// warp helper: iterate the items of a set of grid cells, 32 at a time
+// ------------------------------------------------------------------------
+// cells are enumerated by `cell_at(idx)` for idx in [0, n_cells_iter), which
+// returns a cell id or -1; fn(item, valid) is called warp-uniformly for
+// batches of 32 items (valid = false for padding lanes).
+template <class CellAt, class Fn>
+__device__ void for_items(int n_cells_iter, CellAt cell_at, const int32_t* cell_start,
+                          const int32_t* cell_items, int lane, Fn fn) {
+  for (int cb = 0; cb < n_cells_iter; cb += 32) {
+    int ci = cb + lane;
+    int cell = ci < n_cells_iter ? cell_at(ci) : -1;
+    int b = 0, cnt = 0;
+    if (cell >= 0) {
+      b = cell_start[cell];
+      cnt = cell_start[cell + 1] - b;
+    }
+    int incl = warp_incl_scan(cnt, lane);
+    int total = __shfl_sync(0xffffffffu, incl, 31);
+    int excl = incl - cnt;
+    for (int ib = 0; ib < total; ib += 32) {
+      int g = ib + lane;
+      // owner lane: the last lane whose exclusive prefix is <= g
+      int owner = 0;
+      for (int o = 16; o > 0; o >>= 1) {
+        int cand = owner + o;
+        int ex = __shfl_sync(0xffffffffu, excl, cand);
+        if (ex <= g) owner = cand;
+      }
+      int ob = __shfl_sync(0xffffffffu, b, owner);
+      int oe = __shfl_sync(0xffffffffu, excl, owner);
+      bool valid = g < total;
+      int item = valid ? cell_items[ob + (g - oe)] : -1;
+      fn(item, valid);
+    }
+  }
+}
+
+// ------------------------------------------------------------------------
+// k nearest power neighbours
+// ------------------------------------------------------------------------
+constexpr int kKnnBuf = 1024;
+constexpr int kKnnWarps = 4;
+
+__device__ __forceinline__ uint32_t order_key(float f) {
+  uint32_t u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float key_value(uint32_t u) {
+  return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+// power-bisector distance of site j from site i (same expression as the
+// oracle): ((|cj - ci|^2 - wj) + wi) / (2 |cj - ci|)
+__device__ __forceinline__ float bisector_key(float4 si, float4 sj) {
+  float dx = sj.x - si.x, dy = sj.y - si.y, dz = sj.z - si.z;
+  float d2 = dx * dx + dy * dy + dz * dz;
+  if (d2 == 0.0f) return sj.w > si.w ? -INFINITY : INFINITY;
+  float num = (d2 - sj.w) + si.w;
+  float den = 2.0f * sqrtf(d2);
+  return num / den;
+}
+
+// bitonic sort of buf[0..n) (n power of two) by one warp, ascending
+__device__ void warp_bitonic_sort(unsigned long long* buf, int n, int lane) {
+  for (int k = 2; k <= n; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = lane; i < n; i += 32) {
+        int l = i ^ j;
+        if (l > i) {
+          unsigned long long a = buf[i], b = buf[l];
+          bool up = (i & k) == 0;
+          if ((a > b) == up) {
+            buf[i] = b;
+            buf[l] = a;
+          }
+        }
+      }
+      __syncwarp();
+    }
+  }
+}
+
+__device__ __forceinline__ int next_pow2(int x) {
+  int p = 32;
+  while (p < x) p <<= 1;
+  return p;
+}
+
+__global__ void __launch_bounds__(kKnnWarps * 32) knn_kernel(
+    const float4* site4f, int n_site, Grid g, const int32_t* cell_start,
+    const int32_t* cell_items, int k, float w_max, int order_by_id, int32_t* nbr, float* keys,
+    int32_t* status) {
+  __shared__ unsigned long long sbuf[kKnnWarps][kKnnBuf];
+  __shared__ int scnt[kKnnWarps];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  unsigned long long* buf = sbuf[wid];
+  const int i = blockIdx.x * kKnnWarps + wid;
+  if (i >= n_site) return;
+  const float4 si = site4f[i];
+  const int cx = clampi((int)floorf((si.x - g.lo.x) * g.inv_cell), 0, g.nx - 1);
+  const int cy = clampi((int)floorf((si.y - g.lo.y) * g.inv_cell), 0, g.ny - 1);
+  const int cz = clampi((int)floorf((si.z - g.lo.z) * g.inv_cell), 0, g.nz - 1);
+  const int rmax = max(max(max(cx, g.nx - 1 - cx), max(cy, g.ny - 1 - cy)), max(cz, g.nz - 1 - cz));
+  if (lane == 0) scnt[wid] = 0;
+  __syncwarp();
+  unsigned long long kth = ~0ull;  // packed k-th best so far (after a sort)
+  int done = 0;
+  for (int r = 0; r <= rmax && !done; ++r) {
+    const int side = 2 * r + 1;
+    const int n_cube = side * side * side;
+    auto cell_at = [&](int idx) -> int {
+      int dx = idx % side - r, dy = (idx / side) % side - r, dz = idx / (side * side) - r;
+      if (max(max(abs(dx), abs(dy)), abs(dz)) != r) return -1;
+      int x = cx + dx, y = cy + dy, z = cz + dz;
+      if (x < 0 || y < 0 || z < 0 || x >= g.nx || y >= g.ny || z >= g.nz) return -1;
+      return x + g.nx * (y + g.ny * z);
+    };
+    for_items(n_cube, cell_at, cell_start, cell_items, lane, [&](int j, bool valid) {
+      bool take = false;
+      unsigned long long packed = 0;
+      if (valid && j != i) {
+        float key = bisector_key(si, site4f[j]);
+        packed = ((unsigned long long)order_key(key) << 32) | (uint32_t)j;
+        take = packed < kth;
+      }
+      uint32_t m = __ballot_sync(0xffffffffu, take);
+      int base = scnt[wid];
+      if (take) buf[base + __popc(m & ((1u << lane) - 1u))] = packed;
+      __syncwarp();
+      int cnt = base + __popc(m);
+      if (cnt > kKnnBuf - 32) {
+        // sort and keep the best k
+        for (int q = cnt + lane; q < kKnnBuf; q += 32) buf[q] = ~0ull;
+        __syncwarp();
+        warp_bitonic_sort(buf, kKnnBuf, lane);
+        cnt = min(cnt, k);
+        if (cnt >= k) kth = buf[k - 1];
+      }
+      if (lane == 0) scnt[wid] = cnt;
+      __syncwarp();
+    });
+    int cnt = scnt[wid];
+    int n = next_pow2(max(cnt, 1));
+    for (int q = cnt + lane; q < n; q += 32) buf[q] = ~0ull;
+    __syncwarp();
+    warp_bitonic_sort(buf, n, lane);
+    cnt = min(cnt, k);
+    if (lane == 0) scnt[wid] = cnt;
+    if (cnt >= k) {
+      kth = buf[k - 1];
+      // keys of sites outside the searched block are >= f(D) with
+      // D >= r * cell, f(D) = (D^2 + wi - wmax) / (2D) increasing in D
+      float D = (float)r * g.cell;
+      if (D > 0.f) {
+        float lb = (D * D + si.w - w_max) / (2.f * D);
+        float kv = key_value((uint32_t)(kth >> 32));
+        if (kv < lb - 1e-4f * (fabsf(lb) + D)) done = 1;
+      }
+    }
+    __syncwarp();
+  }
+  int cnt = scnt[wid];
+  if (status && lane == 0) status[i] = done ? 0 : 1;  // 1: exhausted grid
+  // outputs in distance order
+  for (int q = lane; q < k; q += 32) {
+    if (q < cnt) {
+      if (keys) keys[(long long)i * k + q] = key_value((uint32_t)(buf[q] >> 32));
+      if (!order_by_id) nbr[(long long)i * k + q] = (int32_t)(uint32_t)buf[q];
+    } else {
+      if (keys) keys[(long long)i * k + q] = INFINITY;
+      if (!order_by_id) nbr[(long long)i * k + q] = -1;
+    }
+  }
+  if (order_by_id) {
+    __syncwarp();
+    int n = next_pow2(max(k, 1));
+    // reuse the buffer: ids as 64-bit values, padding at the end
+    for (int q = lane; q < n; q += 32) {
+      unsigned long long v = ~0ull;
+      if (q < cnt) v = (unsigned long long)(uint32_t)buf[q];
+      __syncwarp();
+      buf[q] = v;
+    }
+    __syncwarp();
+    warp_bitonic_sort(buf, n, lane);
+    for (int q = lane; q < k; q += 32)
+      nbr[(long long)i * k + q] = q < cnt ? (int32_t)buf[q] : -1;
+  }
+}
+
+cudaError_t launch_knn(const float4* site4f, int n_site, const Grid& g, const int32_t* cell_start,
+                       const int32_t* cell_items, int k, float w_max, int order_by_id,
+                       int32_t* nbr, float* keys, int32_t* status, cudaStream_t st) {
+  if (n_site <= 0) return cudaSuccess;
+  int blocks = (n_site + kKnnWarps - 1) / kKnnWarps;
+  knn_kernel<<<blocks, kKnnWarps * 32, 0, st>>>(site4f, n_site, g, cell_start, cell_items, k,
+                                               w_max, order_by_id, nbr, keys, status);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------------
+// candidate pairs
+// ------------------------------------------------------------------------
+// power distance of a mesh vertex to a site, the reference's float order
+__device__ __forceinline__ float pow_dist(float4 s, float3 v) {
+  float t0 = s.x - v.x, t1 = s.y - v.y, t2 = s.z - v.z;
+  float ssd = t0 * t0;
+  ssd = ssd + t1 * t1;
+  ssd = ssd + t2 * t2;
+  return ssd - s.w;
+}
+
+constexpr int kPairWarps = 4;
+
+__global__ void __launch_bounds__(kPairWarps * 32) pairs_kernel(PairParams p) {
+  const int lane = threadIdx.x & 31;
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (i >= p.n_site) return;
+  if (p.flags[i] != 1u) return;
+  const float4 blo = p.site_box[2 * i], bhi = p.site_box[2 * i + 1];
+  if (!(blo.x <= bhi.x && blo.y <= bhi.y && blo.z <= bhi.z)) return;
+  const float4 si = p.site4f[i];
+  const Grid& g = p.tg;
+  const int x0 = clampi((int)floorf((blo.x - g.lo.x) * g.inv_cell), 0, g.nx - 1);
+  const int y0 = clampi((int)floorf((blo.y - g.lo.y) * g.inv_cell), 0, g.ny - 1);
+  const int z0 = clampi((int)floorf((blo.z - g.lo.z) * g.inv_cell), 0, g.nz - 1);
+  const int x1 = clampi((int)floorf((bhi.x - g.lo.x) * g.inv_cell), 0, g.nx - 1);
+  const int y1 = clampi((int)floorf((bhi.y - g.lo.y) * g.inv_cell), 0, g.ny - 1);
+  const int z1 = clampi((int)floorf((bhi.z - g.lo.z) * g.inv_cell), 0, g.nz - 1);
+  const int sx = x1 - x0 + 1, sy = y1 - y0 + 1, sz = z1 - z0 + 1;
+  const int n_iter = sx * sy * sz;
+  const int32_t* L = p.nbr + (long long)i * p.k;
+  auto cell_at = [&](int idx) -> int {
+    int x = x0 + idx % sx, y = y0 + (idx / sx) % sy, z = z0 + idx / (sx * sy);
+    return x + g.nx * (y + g.ny * z);
+  };
+  for_items(n_iter, cell_at, p.tcell_start, p.tcell_items, lane, [&](int t, bool valid) {
+    bool pass = false;
+    if (valid) {
+      float4 c = p.centroid[t];
+      if (c.x >= blo.x && c.x <= bhi.x && c.y >= blo.y && c.y <= bhi.y && c.z >= blo.z &&
+          c.z <= bhi.z) {
+        int4 q = p.tets[t];
+        float3 v[4];
+        int id[4] = {q.x, q.y, q.z, q.w};
+        float pdi[4];
+        for (int a = 0; a < 4; ++a) {
+          v[a] = make_float3(p.vert3f[3 * id[a]], p.vert3f[3 * id[a] + 1], p.vert3f[3 * id[a] + 2]);
+          pdi[a] = pow_dist(si, v[a]);
+        }
+        pass = true;
+        for (int r = 0; r < p.k && pass; ++r) {
+          int m = __ldg(L + r);
+          if (m == -1) continue;  // voronoi.cu:171 skips holes
+          float4 sm = __ldg(p.site4f + m);
+          bool hit = false;
+          for (int a = 0; a < 4; ++a) hit |= pow_dist(sm, v[a]) > pdi[a];
+          pass = hit;
+        }
+      }
+    }
+    uint32_t msk = __ballot_sync(0xffffffffu, pass);
+    if (msk) {
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(p.pair_cursor, (unsigned long long)__popc(msk));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (pass) {
+        unsigned long long slot = base + __popc(msk & ((1u << lane) - 1u));
+        if ((long long)slot < p.pair_cap) p.pair_buf[slot] = make_int2(t, i);
+        atomicAdd(p.tet_count + t, 1);
+      }
+    }
+  });
+}
+
+cudaError_t launch_pairs(const PairParams& p, cudaStream_t st) {
+  if (p.n_site <= 0) return cudaSuccess;
+  int blocks = (p.n_site + kPairWarps - 1) / kPairWarps;
+  pairs_kernel<<<blocks, kPairWarps * 32, 0, st>>>(p);
+  return cudaGetLastError();
+}
+
+__global__ void scatter_pairs_kernel(const int2* buf, long long n, const int32_t* offs,
+                                     int32_t* fill, int32_t* pair_site) {
+  long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  int2 pr = buf[q];
+  int slot = atomicAdd(fill + pr.x, 1);
+  pair_site[offs[pr.x] + slot] = pr.y;
+}
+
+__global__ void sort_tet_pairs_kernel(int n_tet, const int32_t* offs, int32_t* pair_site,
+                                      int32_t* pair_tet, int32_t* tet_k) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_tet) return;
+  int b = offs[t], e = offs[t + 1];
+  for (int i = b + 1; i < e; ++i) {
+    int v = pair_site[i];
+    int j = i - 1;
+    while (j >= b && pair_site[j] > v) {
+      pair_site[j + 1] = pair_site[j];
+      --j;
+    }
+    pair_site[j + 1] = v;
+  }
+  for (int i = b; i < e; ++i) pair_tet[i] = t;
+  if (e > b) atomicMax(tet_k, e - b);
+}
+
+cudaError_t pairs_to_csr(const int2* pair_buf, long long n_pairs, int n_tet,
+                         const int32_t* tet_offsets, int32_t* tet_fill, int32_t* pair_site,
+                         int32_t* pair_tet, int32_t* tet_k_out, cudaStream_t st) {
+  cudaMemsetAsync(tet_fill, 0, sizeof(int32_t) * (size_t)n_tet, st);
+  cudaMemsetAsync(tet_k_out, 0, sizeof(int32_t), st);
+  if (n_pairs > 0)
+    scatter_pairs_kernel<<<(int)((n_pairs + 255) / 256), 256, 0, st>>>(pair_buf, n_pairs,
+                                                                      tet_offsets, tet_fill,
+                                                                      pair_site);
+  if (n_tet > 0)
+    sort_tet_pairs_kernel<<<(n_tet + 255) / 256, 256, 0, st>>>(n_tet, tet_offsets, pair_site,
+                                                              pair_tet, tet_k_out);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------------
+// compaction
+// ------------------------------------------------------------------------
+__global__ void flag_cells_kernel(const rpd_cell_header* h, long long n, int32_t* flag,
+                                  unsigned long long* hist) {
+  __shared__ unsigned int sh[11];
+  if (threadIdx.x < 11) sh[threadIdx.x] = 0;
+  __syncthreads();
+  long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < n) {
+    int s = h[q].status;
+    flag[q] = s == kSuccess ? 1 : 0;
+    int b = (s >= 0 && s <= 8) ? s : (s == kPayloadFull ? 10 : 9);
+    atomicAdd(sh + b, 1u);
+  }
+  __syncthreads();
+  if (threadIdx.x < 11 && sh[threadIdx.x]) atomicAdd(hist + threadIdx.x, (unsigned long long)sh[threadIdx.x]);
+}
+
+__global__ void gather_cells_kernel(const rpd_cell_header* h, long long n, const int32_t* pos,
+                                    rpd_cell_header* out, long long* n_out) {
+  long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < n && h[q].status == kSuccess) out[pos[q]] = h[q];
+  if (q == 0) *n_out = pos[n];
+}
+
+cudaError_t compact_cells(const rpd_cell_header* pair_headers, long long n_pairs, int32_t* flag_tmp,
+                          int32_t* pos_tmp, int32_t* scan_tmp, rpd_cell_header* out,
+                          long long* n_out_dev, unsigned long long* status_hist, cudaStream_t st) {
+  int nb = (int)((n_pairs + 255) / 256);
+  if (n_pairs > 0) flag_cells_kernel<<<nb, 256, 0, st>>>(pair_headers, n_pairs, flag_tmp, status_hist);
+  cudaError_t err = scan_exclusive(flag_tmp, pos_tmp, n_pairs, scan_tmp, st);
+  if (err != cudaSuccess) return err;
+  gather_cells_kernel<<<nb > 0 ? nb : 1, 256, 0, st>>>(pair_headers, n_pairs, pos_tmp, out, n_out_dev);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------------
+// reference site_knn layout ((k+1) rows x n_site) -> row-major lists
+// ------------------------------------------------------------------------
+__global__ void ref_lists_kernel(const int32_t* ref, int k, int n_site, int32_t* nbr) {
+  long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= (long long)n_site * k) return;
+  int i = (int)(q / k), r = (int)(q % k);
+  nbr[q] = ref[(long long)r * n_site + i];
+}
+
+cudaError_t neighbors_from_reference(const int32_t* ref, int k, int n_site, int32_t* nbr,
+                                     cudaStream_t st) {
+  long long n = (long long)n_site * k;
+  if (n > 0) ref_lists_kernel<<<(int)((n + 255) / 256), 256, 0, st>>>(ref, k, n_site, nbr);
+  return cudaGetLastError();
+}
+
+}  // namespace rpd

@@ -1,0 +1,266 @@
+"""Python host bindings of librpd_gb300.so (ctypes over the C ABI of
+include/rpd_gb300.h).
+
+The library is the product; this module only marshals numpy arrays.  It
+raises if the library is missing or cannot be loaded -- there is no CPU
+fallback anywhere in the package.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "librpd_gb300.so")
+
+PRED_FP64 = 0
+PRED_FP32_FILTER = 1
+NEIGH_USER = 0
+NEIGH_KNN = 1
+ORDER_SITE_ID = 0
+ORDER_DISTANCE = 1
+
+STATUS_NAMES = ["triangle_overflow", "vertex_overflow", "inconsistent_boundary",
+                "security_radius_not_reached", "success", "needs_exact_predicates",
+                "no_intersection", "edge_overflow", "needs_perturb", "other"]
+SUCCESS = 4
+
+HEADER_DTYPE = np.dtype([
+    ("tet_id", "<i4"), ("site_id", "<i4"), ("status", "<i4"),
+    ("nb_v", "u1"), ("nb_p", "u1"), ("nb_e", "u1"), ("flags", "u1"),
+    ("offset", "<u8"), ("volume", "<f8"),
+])
+
+# every symbol declared in include/rpd_gb300.h
+EXPORTS = [
+    "rpd_status_string", "rpd_config_default", "rpd_payload_bytes", "rpd_create",
+    "rpd_destroy", "rpd_last_error", "rpd_set_mesh", "rpd_set_sites", "rpd_set_neighbors",
+    "rpd_compute", "rpd_get_cells", "rpd_copy_cells_to_host", "rpd_copy_neighbors_to_host",
+    "rpd_copy_pairs_to_host", "rpd_copy_pair_headers_to_host", "rpd_build_mesh_adjacency",
+]
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("predicate_mode", ctypes.c_int),
+                ("neighbor_source", ctypes.c_int), ("knn_k", ctypes.c_int),
+                ("clip_order", ctypes.c_int), ("compute_geometry", ctypes.c_int),
+                ("warps_per_block", ctypes.c_int), ("blocks_per_sm", ctypes.c_int),
+                ("reserved", ctypes.c_int * 8)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("n_pairs", ctypes.c_int64), ("n_cells", ctypes.c_int64),
+                ("status_counts", ctypes.c_int64 * 10), ("n_predicates", ctypes.c_int64),
+                ("n_escalated", ctypes.c_int64), ("payload_bytes", ctypes.c_int64),
+                ("tet_k", ctypes.c_int32), ("knn_k", ctypes.c_int32),
+                ("ms_total", ctypes.c_float), ("ms_knn", ctypes.c_float),
+                ("ms_pairs", ctypes.c_float), ("ms_clip", ctypes.c_float),
+                ("ms_compact", ctypes.c_float)]
+
+    def as_dict(self):
+        d = {f: getattr(self, f) for f, _ in self._fields_ if f != "status_counts"}
+        d["status_counts"] = {STATUS_NAMES[i]: int(self.status_counts[i]) for i in range(10)}
+        return d
+
+
+class CellsView(ctypes.Structure):
+    _fields_ = [("n_cells", ctypes.c_int64), ("headers", ctypes.c_void_p),
+                ("payload", ctypes.c_void_p), ("payload_bytes", ctypes.c_int64),
+                ("n_pairs", ctypes.c_int64), ("pair_headers", ctypes.c_void_p)]
+
+
+_lib = None
+
+
+def load(path=LIB_PATH):
+    """Loads librpd_gb300.so; raises if it was not built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError("librpd_gb300.so not built (run __graft_entry__.build())")
+    L = ctypes.CDLL(path)
+    vp, i32, i64, c = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes
+    L.rpd_status_string.restype = c.c_char_p
+    L.rpd_status_string.argtypes = [i32]
+    L.rpd_config_default.restype = None
+    L.rpd_config_default.argtypes = [c.POINTER(Config)]
+    L.rpd_payload_bytes.restype = c.c_size_t
+    L.rpd_payload_bytes.argtypes = [i32, i32, i32]
+    L.rpd_create.restype = i32
+    L.rpd_create.argtypes = [c.POINTER(Config), c.POINTER(vp)]
+    L.rpd_destroy.restype = None
+    L.rpd_destroy.argtypes = [vp]
+    L.rpd_last_error.restype = c.c_char_p
+    L.rpd_last_error.argtypes = [vp]
+    L.rpd_set_mesh.restype = i32
+    L.rpd_set_mesh.argtypes = [vp, vp, i32, vp, i32, vp, vp, vp, vp]
+    L.rpd_set_sites.restype = i32
+    L.rpd_set_sites.argtypes = [vp, vp, i32, vp]
+    L.rpd_set_neighbors.restype = i32
+    L.rpd_set_neighbors.argtypes = [vp, vp, i32, i32]
+    L.rpd_compute.restype = i32
+    L.rpd_compute.argtypes = [vp, c.POINTER(Stats)]
+    L.rpd_get_cells.restype = i32
+    L.rpd_get_cells.argtypes = [vp, c.POINTER(CellsView)]
+    L.rpd_copy_cells_to_host.restype = i32
+    L.rpd_copy_cells_to_host.argtypes = [vp, vp, i64, vp, i64, c.POINTER(i64), c.POINTER(i64)]
+    L.rpd_copy_neighbors_to_host.restype = i32
+    L.rpd_copy_neighbors_to_host.argtypes = [vp, vp, i64, c.POINTER(i32)]
+    L.rpd_copy_pairs_to_host.restype = i32
+    L.rpd_copy_pairs_to_host.argtypes = [vp, vp, vp, i64, c.POINTER(i64)]
+    L.rpd_copy_pair_headers_to_host.restype = i32
+    L.rpd_copy_pair_headers_to_host.argtypes = [vp, vp, i64, c.POINTER(i64)]
+    L.rpd_build_mesh_adjacency.restype = i32
+    L.rpd_build_mesh_adjacency.argtypes = [i32, vp, i32, vp, vp, vp, vp, vp]
+    _lib = L
+    return L
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+class RPDError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s: %s" % (status, msg))
+        self.status = status
+
+
+def mesh_adjacency(n_vert, tets):
+    """v_adjs, e_adj6, f_adjs, f_ids, n_boundary_faces (load_tet_adj_info)."""
+    L = load()
+    tets = np.ascontiguousarray(tets, np.int32)
+    n_tet = tets.shape[0]
+    v = np.zeros(n_vert, np.int32)
+    e6 = np.zeros((n_tet, 6), np.uint8)
+    fa = np.zeros((n_tet, 4), np.int32)
+    fi = np.zeros((n_tet, 4), np.int32)
+    nb = np.zeros(1, np.int32)
+    s = L.rpd_build_mesh_adjacency(n_vert, _p(tets), n_tet, _p(v), _p(e6), _p(fa), _p(fi), _p(nb))
+    if s != 0:
+        raise RPDError(s, "rpd_build_mesh_adjacency failed")
+    return dict(v_adjs=v, e_adj6=e6, f_adjs=fa, f_ids=fi, n_boundary_faces=int(nb[0]))
+
+
+def payload_bytes(nb_v, nb_p, nb_e):
+    return int(load().rpd_payload_bytes(int(nb_v), int(nb_p), int(nb_e)))
+
+
+class RPD:
+    """One engine context (one GPU, one stream)."""
+
+    def __init__(self, device=0, predicate_mode=PRED_FP32_FILTER, neighbor_source=NEIGH_KNN,
+                 knn_k=64, clip_order=ORDER_SITE_ID, compute_geometry=True,
+                 warps_per_block=0, blocks_per_sm=0):
+        L = load()
+        cfg = Config()
+        L.rpd_config_default(ctypes.byref(cfg))
+        cfg.device = device
+        cfg.predicate_mode = predicate_mode
+        cfg.neighbor_source = neighbor_source
+        cfg.knn_k = knn_k
+        cfg.clip_order = clip_order
+        cfg.compute_geometry = 1 if compute_geometry else 0
+        cfg.warps_per_block = warps_per_block
+        cfg.blocks_per_sm = blocks_per_sm
+        h = ctypes.c_void_p()
+        s = L.rpd_create(ctypes.byref(cfg), ctypes.byref(h))
+        if s != 0:
+            raise RPDError(s, L.rpd_status_string(s).decode())
+        self._L = L
+        self._h = h
+        self._keep = []
+
+    def close(self):
+        if self._h:
+            self._L.rpd_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, s):
+        if s != 0:
+            raise RPDError(s, self._L.rpd_last_error(self._h).decode())
+
+    def set_mesh(self, vert3d, tets, v_adjs, e_adj6, f_adjs, f_ids):
+        v = np.ascontiguousarray(vert3d, np.float64)
+        t = np.ascontiguousarray(tets, np.int32)
+        self._check(self._L.rpd_set_mesh(
+            self._h, _p(v), v.shape[0], _p(t), t.shape[0],
+            _p(np.ascontiguousarray(v_adjs, np.int32)),
+            _p(np.ascontiguousarray(e_adj6, np.uint8)),
+            _p(np.ascontiguousarray(f_adjs, np.int32)),
+            _p(np.ascontiguousarray(f_ids, np.int32))))
+
+    def set_sites(self, xyzw, flags=None):
+        s = np.ascontiguousarray(xyzw, np.float64)
+        f = None if flags is None else np.ascontiguousarray(flags, np.uint32)
+        self._check(self._L.rpd_set_sites(self._h, _p(s), s.shape[0], _p(f)))
+
+    def set_neighbors(self, nbr, layout=0):
+        n = np.ascontiguousarray(nbr, np.int32)
+        k = n.shape[1] if layout == 0 else n.shape[0] - 1
+        self._check(self._L.rpd_set_neighbors(self._h, _p(n), k, layout))
+
+    def compute(self):
+        st = Stats()
+        self._check(self._L.rpd_compute(self._h, ctypes.byref(st)))
+        return st
+
+    def view(self):
+        v = CellsView()
+        self._check(self._L.rpd_get_cells(self._h, ctypes.byref(v)))
+        return v
+
+    def cells(self, headers_out=None, payload_out=None):
+        """Emitted cells copied to the host: (headers, payload)."""
+        n = ctypes.c_int64()
+        b = ctypes.c_int64()
+        self._check(self._L.rpd_copy_cells_to_host(self._h, None, 0, None, 0,
+                                                   ctypes.byref(n), ctypes.byref(b)))
+        h = headers_out if headers_out is not None else np.zeros(n.value, HEADER_DTYPE)
+        p = payload_out if payload_out is not None else np.zeros(max(b.value, 1), np.uint8)
+        self._check(self._L.rpd_copy_cells_to_host(self._h, _p(h), h.shape[0], _p(p), p.nbytes,
+                                                   ctypes.byref(n), ctypes.byref(b)))
+        return h[:n.value], p[:b.value]
+
+    def pair_headers(self):
+        """Headers of all candidate pairs (dropped ones included)."""
+        n = ctypes.c_int64()
+        self._check(self._L.rpd_copy_pair_headers_to_host(self._h, None, 0, ctypes.byref(n)))
+        out = np.zeros(n.value, HEADER_DTYPE)
+        self._check(self._L.rpd_copy_pair_headers_to_host(self._h, _p(out), out.shape[0],
+                                                          ctypes.byref(n)))
+        return out
+
+    def neighbors(self):
+        k = ctypes.c_int()
+        self._check(self._L.rpd_copy_neighbors_to_host(self._h, None, 0, ctypes.byref(k)))
+        return k.value
+
+    def neighbor_lists(self, n_site):
+        k = self.neighbors()
+        out = np.zeros((n_site, k), np.int32)
+        kk = ctypes.c_int()
+        self._check(self._L.rpd_copy_neighbors_to_host(self._h, _p(out), out.size, ctypes.byref(kk)))
+        return out
+
+    def pairs(self, n_tet):
+        n = ctypes.c_int64()
+        self._check(self._L.rpd_copy_pairs_to_host(self._h, None, None, 0, ctypes.byref(n)))
+        offs = np.zeros(n_tet + 1, np.int32)
+        sites = np.zeros(max(n.value, 1), np.int32)
+        self._check(self._L.rpd_copy_pairs_to_host(self._h, _p(offs), _p(sites), sites.size,
+                                                   ctypes.byref(n)))
+        return offs, sites[:n.value]
