@@ -1,0 +1,451 @@
+"""Benchmark of the RPD hot path on one GB300 (or N replicas).
+
+Metric: RPD cells/sec -- one cell is one emitted (tet, site) restricted
+convex cell, the unit of libmat's ConvexCellHost -- on the 1M-tet ellipsoid
+workload (jittered-grid Delaunay ellipsoid, semi-axes 1.0/0.6/0.4, ~1M tets;
+50,000 sites, 70% near the surface, radii lognormal(ln 0.01, 0.5)), seeded
+synthetic data generated here.  One step = one rpd_compute: GPU kNN (k = 64),
+candidate pairs by the reference's rule, clipping, compaction, from
+device-resident mesh and sites to device-resident compact cells.
+
+  value   fast path: FP32 filter + FP64 fallback predicates (reference signs)
+  plain   the plain FP64 path: FP64 determinant on every predicate
+  e2e     the fast path through the C ABI with host buffers: mesh + sites
+          host->device, compute, every cell device->host, per step
+  cpu_baseline / --impl reference: the oracle (CPU restatement of the
+          reference's clipper and candidate rule, all host cores) on a
+          bounded sample of the same workload's tets
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "RPD cells/sec at 1M tets (learned-k + FP32 filter vs plain FP64), exact topology"
+UNIT = "cells/s"
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def make_workload(args):
+    from libmat_gb300 import workloads as W
+
+    t0 = time.time()
+    if args.config == "small":
+        cfg = W.config_small_cube()
+        name = "cube_20x20x20x6_48k_tets_2k_sites"
+    else:
+        cfg = W.config_ellipsoid(target_tets=args.tets, n_site=args.sites, seed=2)
+        name = "ellipsoid_%dk_tets_%dk_sites" % (round(args.tets / 1000), round(args.sites / 1000))
+    return cfg, name, time.time() - t0
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def flush_l2():
+    """Writes 256 MB (> 129 MB L2) on the device between timed steps."""
+    import torch
+
+    if not hasattr(flush_l2, "buf"):
+        flush_l2.buf = torch.empty(64 << 20, dtype=torch.int32, device="cuda")
+    flush_l2.buf.fill_(1)
+    torch.cuda.synchronize()
+
+
+def clip_algorithmic_bytes(cfg, n_pairs, k, payload_bytes):
+    """Bytes the clip kernel must move at least once per launch: the mesh
+    (float and double vertices, tets, face counts/ids, edge counts, vertex
+    counts), the sites (float + double), the neighbour lists, the pair list,
+    the per-pair headers and the emitted payload."""
+    nv, nt, ns = cfg["vert3d"].shape[0], cfg["tets"].shape[0], cfg["sites"].shape[0]
+    mesh = 12 * nv + 24 * nv + 16 * nt + 32 * nt + 6 * nt + 4 * nv
+    sites = 16 * ns + 32 * ns
+    return mesh + sites + 4 * k * ns + 8 * n_pairs + 32 * n_pairs + payload_bytes
+
+
+def cpu_sample_run(cfg, adj, nbr, n_tets, seed=0, n_threads=None):
+    """The oracle on n_tets random tets: the reference's candidate rule over
+    all sites (brute force, as the reference) + clipping with FP64
+    predicates.  Returns (cells, seconds, pairs)."""
+    from oracle import oracle as O
+
+    rng = np.random.default_rng(seed)
+    sub = np.sort(rng.choice(cfg["tets"].shape[0], size=min(n_tets, cfg["tets"].shape[0]),
+                             replace=False))
+    tets = cfg["tets"][sub]
+    mesh = dict(vert3d=cfg["vert3d"], tets=tets, v_adjs=adj["v_adjs"],
+                e_adj6=adj["e_adj6"][sub], f_adjs=adj["f_adjs"][sub], f_ids=adj["f_ids"][sub])
+    t0 = time.perf_counter()
+    offs, ps = O.candidate_pairs(cfg["vert3d"].astype(np.float32), tets,
+                                 cfg["sites"].astype(np.float32), cfg["flags"], nbr,
+                                 n_threads=n_threads)
+    h, p, _ = O.clip_cells(mesh, cfg["sites"], nbr, offs, ps, pred_mode=0, n_threads=n_threads)
+    dt = time.perf_counter() - t0
+    return int((h["status"] == 4).sum()), dt, int(offs[-1])
+
+
+def run_reference(args):
+    """--impl reference: the reference's CPU path restated (oracle port; the
+    reference's own clipper builds only where its sources are, not on the GPU
+    machines), all host threads, bounded sample per step."""
+    from libmat_gb300 import workloads as W  # noqa: F401
+    from oracle import oracle as O
+
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cfg, name, gen_s = make_workload(args)
+    adj = O.mesh_adjacency(cfg["vert3d"].shape[0], cfg["tets"])
+    nbr, _ = O.knn(cfg["sites"].astype(np.float32), args.k)
+    nbr = np.sort(nbr, axis=1)
+    cores = O.nthreads()
+    sample = args.ref_sample
+    for w in range(args.warmup):
+        cpu_sample_run(cfg, adj, nbr, max(sample // 8, 100), seed=100 + w)
+    cells = 0
+    secs = 0.0
+    for s in range(args.steps):
+        c, dt, _ = cpu_sample_run(cfg, adj, nbr, sample, seed=s)
+        cells += c
+        secs += dt
+    v = cells / secs
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * secs / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32+fp64",
+        "data": "synthetic (seeded)",
+        "config": {"workload": name, "n_tet": int(cfg["tets"].shape[0]),
+                   "n_site": int(cfg["sites"].shape[0]), "knn_k": args.k},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": "%d random tets per step: reference candidate rule over all "
+                                   "sites + clipping (FP64 predicates)" % sample},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    from libmat_gb300 import rpd
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as tdist
+
+        torch.cuda.set_device(local)
+        tdist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        dist = tdist
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    cfg, name, gen_s = make_workload(args)
+    adj = rpd.mesh_adjacency(cfg["vert3d"].shape[0], cfg["tets"])
+    nt, nv, ns = cfg["tets"].shape[0], cfg["vert3d"].shape[0], cfg["sites"].shape[0]
+
+    def engine(pred):
+        r = rpd.RPD(device=local if world > 1 else 0, predicate_mode=pred,
+                    neighbor_source=rpd.NEIGH_KNN, knn_k=args.k, clip_order=rpd.ORDER_SITE_ID)
+        r.set_mesh(cfg["vert3d"], cfg["tets"], adj["v_adjs"], adj["e_adj6"], adj["f_adjs"],
+                   adj["f_ids"])
+        r.set_sites(cfg["sites"], cfg["flags"])
+        return r
+
+    def timed(r, steps, warmup):
+        for _ in range(warmup):
+            r.compute()
+        ms, cells, st_last = [], 0, None
+        for _ in range(steps):
+            flush_l2()
+            barrier()
+            st = r.compute()
+            ms.append(st.ms_total)
+            cells += st.n_cells
+            st_last = st
+        return ms, cells, st_last
+
+    # ---- fast path (the metric)
+    fast = engine(rpd.PRED_FP32_FILTER)
+    barrier()
+    with ClockSampler(local) as clk:
+        ms, cells, st = timed(fast, args.steps, args.warmup)
+    total_ms = sum(ms)
+    if dist is not None:
+        import torch
+
+        t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = cells * world / (total_ms / 1000.0)
+    fast_ph = fast.pair_headers()
+    fast_h, fast_p = fast.cells()
+
+    # ---- plain FP64 path
+    plain = engine(rpd.PRED_FP64)
+    pms, pcells, pst = timed(plain, max(1, args.steps // 2), 1)
+    plain_value = pcells / (sum(pms) / 1000.0)
+    plain_ph = plain.pair_headers()
+    plain_h, plain_p = plain.cells()
+    plain.close()
+    same_headers = all(np.array_equal(fast_ph[f], plain_ph[f])
+                       for f in ("tet_id", "site_id", "status", "nb_v", "nb_p", "nb_e"))
+    topo_ok = same_headers and _sample_topology_equal(fast_ph, fast_p, plain_ph, plain_p)
+
+    # ---- end to end through the C ABI with host buffers
+    e2e = _e2e(args, cfg, adj, rpd)
+
+    # ---- roofline of the clip kernel
+    peak, peak_src = load_peaks()
+    alg = clip_algorithmic_bytes(cfg, st.n_pairs, st.knn_k, st.payload_bytes)
+    achieved = alg / (st.ms_clip_kernel / 1000.0) / 1e9
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "clip_traffic.json")
+    if os.path.exists(tfile):
+        tj = json.load(open(tfile))
+        traffic = tj.get("bytes_per_pair", 0) * st.n_pairs or None
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        from oracle import oracle as O
+
+        nbr = fast.neighbor_lists(ns)
+        c, dt, _ = cpu_sample_run(cfg, adj, nbr, args.cpu_sample)
+        cpu = {"value": c / dt, "unit": UNIT, "cores": O.nthreads(), "kind": "port",
+               "sample": "%d random tets: reference candidate rule over all sites + clipping "
+                         "(FP64 predicates), oracle on all host threads" % args.cpu_sample}
+    fast.close()
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32+fp64",
+        "data": "synthetic (seeded jittered-grid Delaunay ellipsoid and sites; no dataset)",
+        "config": {"workload": name, "n_tet": nt, "n_vert": nv, "n_site": ns, "knn_k": st.knn_k,
+                   "n_pairs": st.n_pairs, "n_cells": st.n_cells,
+                   "predicates": "fp32 filter, fp64 det when undecided",
+                   "neighbours": "gpu kNN, k smallest power-bisector distances, id order",
+                   "learned_k": False, "l2": "flushed between steps (256 MB write)",
+                   "parallelism": "replicas" if world > 1 else "single gpu",
+                   "generation_s": round(gen_s, 2)},
+        "plain": {"value": plain_value, "ms_per_step": sum(pms) / len(pms),
+                  "speedup_fast_over_plain": value / world / plain_value,
+                  "topology_bit_exact": bool(topo_ok)},
+        "stage_ms": {"knn": st.ms_knn, "pairs": st.ms_pairs, "clip": st.ms_clip,
+                     "clip_kernel": st.ms_clip_kernel, "compact": st.ms_compact},
+        "predicates": {"evaluated": st.n_predicates, "escalated_fp64": st.n_escalated,
+                       "escalation_rate": st.n_escalated / max(st.n_predicates, 1)},
+        "status_counts": {rpd.STATUS_NAMES[i]: int(st.status_counts[i]) for i in range(10)
+                          if st.status_counts[i]},
+        "e2e": e2e,
+        "gpu_launches": int(st.n_launches) * args.steps,
+        "roofline": {"bound": "hbm", "kernel": "clip_cells_kernel", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                     "peak_source": peak_src,
+                     "algorithmic_bytes": alg},
+        "cpu_baseline": cpu,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
+
+
+def run_fast_only(args):
+    """Set-up plus warmup + steps computes of the fast path, nothing else:
+    the command profiled by ncu (launch lists and kernel captures)."""
+    from libmat_gb300 import rpd
+
+    cfg, name, _ = make_workload(args)
+    adj = rpd.mesh_adjacency(cfg["vert3d"].shape[0], cfg["tets"])
+    r = rpd.RPD(predicate_mode=rpd.PRED_FP32_FILTER, neighbor_source=rpd.NEIGH_KNN,
+                knn_k=args.k, clip_order=rpd.ORDER_SITE_ID)
+    r.set_mesh(cfg["vert3d"], cfg["tets"], adj["v_adjs"], adj["e_adj6"], adj["f_adjs"],
+               adj["f_ids"])
+    r.set_sites(cfg["sites"], cfg["flags"])
+    out = []
+    for i in range(args.warmup + args.steps):
+        st = r.compute()
+        out.append(st.as_dict())
+    r.close()
+    print(json.dumps({"workload": name, "last": out[-1]}))
+
+
+def _sample_topology_equal(h1, p1, h2, p2, n=20000):
+    from libmat_gb300 import rpd
+
+    ok = np.flatnonzero(h1["status"] == rpd.SUCCESS)
+    if len(ok) == 0:
+        return True
+    rng = np.random.default_rng(0)
+    pick = rng.choice(ok, size=min(n, len(ok)), replace=False)
+    for q in pick:
+        nv, np_, ne = int(h1["nb_v"][q]), int(h1["nb_p"][q]), int(h1["nb_e"][q])
+        sz = rpd.payload_bytes(nv, np_, ne) - ((24 * nv + 15) // 16) * 16
+        a = p1[int(h1["offset"][q]):int(h1["offset"][q]) + sz]
+        b = p2[int(h2["offset"][q]):int(h2["offset"][q]) + sz]
+        if not np.array_equal(a, b):
+            return False
+    return True
+
+
+def _e2e(args, cfg, adj, rpd):
+    """The same metric through the C ABI with host buffers (page-locked):
+    per step rpd_set_mesh + rpd_set_sites (host->device), rpd_compute, and
+    rpd_copy_cells_to_host (device->host of every cell)."""
+    nt, nv, ns = cfg["tets"].shape[0], cfg["vert3d"].shape[0], cfg["sites"].shape[0]
+    pins = {}
+
+    def pin(name, a):
+        pa = rpd.PinnedArray(a.shape, a.dtype)
+        pa.array[...] = a
+        pins[name] = pa
+        return pa.array
+
+    v = pin("v", cfg["vert3d"])
+    t = pin("t", cfg["tets"])
+    va = pin("va", adj["v_adjs"])
+    e6 = pin("e6", adj["e_adj6"])
+    fa = pin("fa", adj["f_adjs"])
+    fi = pin("fi", adj["f_ids"])
+    s = pin("s", cfg["sites"])
+    fl = pin("fl", cfg["flags"])
+    r = rpd.RPD(predicate_mode=rpd.PRED_FP32_FILTER, neighbor_source=rpd.NEIGH_KNN,
+                knn_k=args.k, clip_order=rpd.ORDER_SITE_ID)
+    r.set_mesh(v, t, va, e6, fa, fi)
+    r.set_sites(s, fl)
+    st = r.compute()
+    hbuf = rpd.PinnedArray((int(st.n_cells * 1.1) + 1024,), rpd.HEADER_DTYPE)
+    pbuf = rpd.PinnedArray((int(st.payload_bytes * 1.1) + (1 << 20),), np.uint8)
+    h2d = (v.nbytes + t.nbytes + va.nbytes + e6.nbytes + fa.nbytes + fi.nbytes + s.nbytes +
+           fl.nbytes)
+    for _ in range(args.warmup):
+        r.set_mesh(v, t, va, e6, fa, fi)
+        r.set_sites(s, fl)
+        r.compute()
+        r.cells(hbuf.array, pbuf.array)
+    cells, d2h, secs = 0, 0, 0.0
+    for _ in range(args.steps):
+        flush_l2()
+        t0 = time.perf_counter()
+        r.set_mesh(v, t, va, e6, fa, fi)
+        r.set_sites(s, fl)
+        st = r.compute()
+        h, p = r.cells(hbuf.array, pbuf.array)
+        secs += time.perf_counter() - t0
+        cells += st.n_cells
+        d2h += h.nbytes + p.nbytes
+    r.close()
+    for pa in pins.values():
+        pa.free()
+    hbuf.free()
+    pbuf.free()
+    return {"value": cells / secs, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+            "d2h_bytes_per_step": int(d2h // args.steps),
+            "ms_per_step": 1000 * secs / args.steps}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="ellipsoid", choices=["ellipsoid", "small"])
+    ap.add_argument("--tets", type=int, default=1_000_000)
+    ap.add_argument("--sites", type=int, default=50_000)
+    ap.add_argument("--k", type=int, default=64)
+    ap.add_argument("--cpu-sample", type=int, default=20000)
+    ap.add_argument("--ref-sample", type=int, default=20000)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--fast-only", action="store_true",
+                    help="only the timed fast path (for profiler launch lists)")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    elif args.fast_only:
+        from __graft_entry__ import build
+
+        build()
+        run_fast_only(args)
+    else:
+        from __graft_entry__ import build
+
+        build()
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

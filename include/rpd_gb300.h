@@ -107,6 +107,8 @@ typedef struct rpd_stats {
   int32_t knn_k;              /* neighbour list length used */
   float ms_total;             /* device time of rpd_compute, CUDA events */
   float ms_knn, ms_pairs, ms_clip, ms_compact;
+  float ms_clip_kernel;       /* the clip kernel alone (events around it) */
+  int32_t n_launches;         /* kernels launched by this rpd_compute */
 } rpd_stats;
 
 typedef struct rpd_cells_view {
@@ -177,6 +179,11 @@ rpd_status rpd_copy_neighbors_to_host(struct rpd_ctx* ctx, int32_t* nbr,
 rpd_status rpd_copy_pairs_to_host(struct rpd_ctx* ctx, int32_t* tet_offsets,
                                   int32_t* pair_sites, int64_t capacity,
                                   int64_t* n_pairs);
+
+/* Page-locked host buffers for fast host<->device copies (cudaMallocHost);
+ * NULL on failure. */
+void* rpd_host_alloc(size_t bytes);
+void rpd_host_free(void* p);
 
 /* Host helper: mesh adjacency counts and face ids with the semantics of
  * load_tet_adj_info (io.cxx:238-335); boundary faces are numbered first in

@@ -47,7 +47,7 @@ struct DevBuf {
   }
 };
 
-enum Ev { kEvStart, kEvKnn, kEvPairs, kEvClip, kEvEnd, kEvCount };
+enum Ev { kEvStart, kEvKnn, kEvPairs, kEvClipK0, kEvClipK1, kEvClip, kEvEnd, kEvCount };
 
 }  // namespace
 
@@ -68,6 +68,12 @@ struct rpd_ctx {
   DevBuf<uint8_t> e_adj6;
   double mesh_lo[3] = {0, 0, 0}, mesh_hi[3] = {0, 0, 0};
   double tet_radius = 0.0;
+  // tets grouped by radius (largest vertex distance to the centroid): the
+  // candidate search offsets each site's cell by its class's largest radius
+  static constexpr int kClasses = 8;
+  DevBuf<uint8_t> tet_class;
+  int class_count[kClasses] = {0};
+  double class_radius[kClasses] = {0};
   bool has_mesh = false;
 
   // sites
@@ -81,14 +87,15 @@ struct rpd_ctx {
 
   // neighbour lists
   int k = 0;
-  DevBuf<int32_t> nbr, nbr_ref_tmp, knn_status;
+  DevBuf<int32_t> nbr, nbr_dist, nbr_ref_tmp, knn_status;
   DevBuf<float> nbr_keys;
   bool has_user_nbr = false;
 
   // grids
   DevBuf<int32_t> s_cell_of, s_cell_count, s_cell_start, s_cell_fill, s_cell_items;
   DevBuf<int32_t> t_cell_of, t_cell_count, t_cell_start, t_cell_fill, t_cell_items;
-  DevBuf<float4> centroid, site_box;
+  DevBuf<float4> centroid, site_box, site_planes;
+  DevBuf<int32_t> site_nplanes;
   DevBuf<int32_t> scan_tmp;
 
   // pairs
@@ -229,14 +236,15 @@ void rpd_destroy(rpd_ctx* c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   c->vert3f.release(); c->vert3d.release(); c->tets.release(); c->v_adjs.release();
-  c->f_adjs.release(); c->f_ids.release(); c->e_adj6.release();
+  c->f_adjs.release(); c->f_ids.release(); c->e_adj6.release(); c->tet_class.release();
   c->site4f.release(); c->site4d.release(); c->flags.release();
-  c->nbr.release(); c->nbr_ref_tmp.release(); c->knn_status.release(); c->nbr_keys.release();
+  c->nbr.release(); c->nbr_dist.release(); c->nbr_ref_tmp.release(); c->knn_status.release(); c->nbr_keys.release();
   c->s_cell_of.release(); c->s_cell_count.release(); c->s_cell_start.release();
   c->s_cell_fill.release(); c->s_cell_items.release();
   c->t_cell_of.release(); c->t_cell_count.release(); c->t_cell_start.release();
   c->t_cell_fill.release(); c->t_cell_items.release();
-  c->centroid.release(); c->site_box.release(); c->scan_tmp.release();
+  c->centroid.release(); c->site_box.release(); c->site_planes.release();
+  c->site_nplanes.release(); c->scan_tmp.release();
   c->pair_buf.release(); c->tet_count.release(); c->tet_offsets.release();
   c->tet_fill.release(); c->pair_site.release(); c->pair_tet.release();
   c->pair_headers.release(); c->cells.release(); c->payload.release();
@@ -265,6 +273,7 @@ rpd_status rpd_set_mesh(rpd_ctx* c, const double* xyz, int n_vert, const int32_t
     lo[i % 3] = std::min(lo[i % 3], xyz[i]);
     hi[i % 3] = std::max(hi[i % 3], xyz[i]);
   }
+  std::vector<double> rad((size_t)n_tet);
   double rmax = 0.0;
   for (long long t = 0; t < n_tet; ++t) {
     double cen[3] = {0, 0, 0};
@@ -273,6 +282,7 @@ rpd_status rpd_set_mesh(rpd_ctx* c, const double* xyz, int n_vert, const int32_t
       if (v < 0 || v >= n_vert) return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_set_mesh: vertex id out of range");
       for (int a = 0; a < 3; ++a) cen[a] += 0.25 * xyz[3 * (long long)v + a];
     }
+    double r = 0.0;
     for (int q = 0; q < 4; ++q) {
       int v = tets[4 * t + q];
       double d2 = 0;
@@ -280,7 +290,29 @@ rpd_status rpd_set_mesh(rpd_ctx* c, const double* xyz, int n_vert, const int32_t
         double d = xyz[3 * (long long)v + a] - cen[a];
         d2 += d * d;
       }
-      rmax = std::max(rmax, std::sqrt(d2));
+      r = std::max(r, std::sqrt(d2));
+    }
+    rad[t] = r;
+    rmax = std::max(rmax, r);
+  }
+  // radius classes: class 0 up to 1.5 x the median radius, then doubling
+  std::vector<uint8_t> cls((size_t)n_tet);
+  int ccount[rpd_ctx::kClasses] = {0};
+  double crad[rpd_ctx::kClasses] = {0};
+  {
+    std::vector<double> tmp(rad);
+    std::nth_element(tmp.begin(), tmp.begin() + tmp.size() / 2, tmp.end());
+    double r0 = std::max(1.5 * tmp[tmp.size() / 2], 1e-300);
+    for (long long t = 0; t < n_tet; ++t) {
+      int k = 0;
+      double lim = r0;
+      while (rad[t] > lim && k < rpd_ctx::kClasses - 1) {
+        lim *= 2.0;
+        ++k;
+      }
+      cls[t] = (uint8_t)k;
+      ccount[k]++;
+      crad[k] = std::max(crad[k], rad[t]);
     }
   }
   CK(c->vert3f.ensure((size_t)n_vert * 3), "alloc vert3f");
@@ -290,6 +322,7 @@ rpd_status rpd_set_mesh(rpd_ctx* c, const double* xyz, int n_vert, const int32_t
   CK(c->e_adj6.ensure((size_t)n_tet * 6), "alloc e_adj6");
   CK(c->f_adjs.ensure((size_t)n_tet * 4), "alloc f_adjs");
   CK(c->f_ids.ensure((size_t)n_tet * 4), "alloc f_ids");
+  CK(c->tet_class.ensure(n_tet), "alloc classes");
   cudaStream_t st = c->stream;
   CK(cudaMemcpyAsync(c->vert3f.ptr, vf.data(), vf.size() * 4, cudaMemcpyHostToDevice, st), "H2D vert");
   CK(cudaMemcpyAsync(c->vert3d.ptr, xyz, (size_t)n_vert * 24, cudaMemcpyHostToDevice, st), "H2D vert");
@@ -298,7 +331,12 @@ rpd_status rpd_set_mesh(rpd_ctx* c, const double* xyz, int n_vert, const int32_t
   CK(cudaMemcpyAsync(c->e_adj6.ptr, e_adj6, (size_t)n_tet * 6, cudaMemcpyHostToDevice, st), "H2D e_adj6");
   CK(cudaMemcpyAsync(c->f_adjs.ptr, f_adjs, (size_t)n_tet * 16, cudaMemcpyHostToDevice, st), "H2D f_adjs");
   CK(cudaMemcpyAsync(c->f_ids.ptr, f_ids, (size_t)n_tet * 16, cudaMemcpyHostToDevice, st), "H2D f_ids");
+  CK(cudaMemcpyAsync(c->tet_class.ptr, cls.data(), (size_t)n_tet, cudaMemcpyHostToDevice, st), "H2D classes");
   CK(cudaStreamSynchronize(st), "set_mesh sync");
+  for (int k = 0; k < rpd_ctx::kClasses; ++k) {
+    c->class_count[k] = ccount[k];
+    c->class_radius[k] = crad[k];
+  }
   c->n_vert = n_vert;
   c->n_tet = n_tet;
   for (int a = 0; a < 3; ++a) {
@@ -393,6 +431,7 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
   const int n_site = c->n_site, n_tet = c->n_tet;
   CK(c->scratch.ensure(32), "alloc scratch");
   CK(cudaMemsetAsync(c->scratch.ptr, 0, 32 * sizeof(unsigned long long), st), "memset");
+  take_launches();
   CK(cudaEventRecord(c->ev[kEvStart], st), "event");
 
   // ---- neighbour lists
@@ -408,31 +447,23 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
     CK(c->scan_tmp.ensure(scan_temp_ints(std::max<long long>(nc, n_tet)) + 16), "alloc");
     CK(c->nbr.ensure((size_t)n_site * c->k), "alloc nbr");
     CK(c->nbr_keys.ensure((size_t)n_site * c->k), "alloc nbr");
+    CK(c->nbr_dist.ensure((size_t)n_site * c->k), "alloc nbr");
     CK(c->knn_status.ensure(n_site), "alloc");
     CK(grid_build_sites(c->site4f.ptr, n_site, g, c->s_cell_of.ptr, c->s_cell_count.ptr,
                         c->s_cell_start.ptr, c->s_cell_fill.ptr, c->s_cell_items.ptr,
                         c->scan_tmp.ptr, st), "site grid");
     CK(launch_knn(c->site4f.ptr, n_site, g, c->s_cell_start.ptr, c->s_cell_items.ptr, c->k,
                   c->w_max, c->cfg.clip_order == RPD_ORDER_SITE_ID ? 1 : 0, c->nbr.ptr,
-                  c->nbr_keys.ptr, c->knn_status.ptr, st), "knn");
+                  c->nbr_keys.ptr, c->nbr_dist.ptr, c->knn_status.ptr, st), "knn");
   }
   CK(cudaEventRecord(c->ev[kEvKnn], st), "event");
 
   // ---- candidate pairs
   {
-    Grid tg = make_grid(c->mesh_lo, c->mesh_hi, n_tet, 4.0);
-    long long nc = (long long)tg.nx * tg.ny * tg.nz;
     CK(c->centroid.ensure(n_tet), "alloc");
     CK(c->t_cell_of.ensure(n_tet), "alloc");
-    CK(c->t_cell_count.ensure(nc), "alloc");
-    CK(c->t_cell_start.ensure(nc + 1), "alloc");
-    CK(c->t_cell_fill.ensure(nc), "alloc");
     CK(c->t_cell_items.ensure(n_tet), "alloc");
-    CK(c->scan_tmp.ensure(scan_temp_ints(std::max<long long>(nc, n_tet)) + 16), "alloc");
-    CK(grid_build_tets(c->vert3f.ptr, c->tets.ptr, n_tet, tg, c->centroid.ptr, c->t_cell_of.ptr,
-                       c->t_cell_count.ptr, c->t_cell_start.ptr, c->t_cell_fill.ptr,
-                       c->t_cell_items.ptr, c->scan_tmp.ptr, st), "tet grid");
-    // per-site boxes
+    CK(tet_centroids(c->vert3f.ptr, c->tets.ptr, n_tet, c->centroid.ptr, st), "centroids");
     double diag2 = 0.0, cs = 0.0;
     for (int a = 0; a < 3; ++a) {
       double l = std::min(c->mesh_lo[a], c->site_lo[a]), h = std::max(c->mesh_hi[a], c->site_hi[a]);
@@ -440,31 +471,16 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
       cs = std::max(cs, std::max(std::fabs(l), std::fabs(h)));
     }
     const double u = std::ldexp(1.0, -24);
-    const double R = c->tet_radius * (1.0 + 1e-5) + 1e-6 * cs;
     double ext = 0.0;
     for (int a = 0; a < 3; ++a) ext = std::max(ext, c->mesh_hi[a] - c->mesh_lo[a]);
     const double margin = 1e-4 * ext + 1e-6 * cs;
-    BoxParams bp;
-    bp.site4f = c->site4f.ptr;
-    bp.flags = c->flags.ptr;
-    bp.nbr = c->nbr.ptr;
-    bp.k = c->k;
-    bp.n_site = n_site;
-    bp.box_lo = make_float4((float)(c->mesh_lo[0] - margin), (float)(c->mesh_lo[1] - margin),
-                            (float)(c->mesh_lo[2] - margin), 0.f);
-    bp.box_hi = make_float4((float)(c->mesh_hi[0] + margin), (float)(c->mesh_hi[1] + margin),
-                            (float)(c->mesh_hi[2] + margin), 0.f);
-    bp.offset_r = (float)R;
-    bp.offset_e = (float)(48.0 * u * (diag2 + std::fabs((double)c->w_max)));
-    bp.coord_scale = (float)cs;
-    bp.abs_margin = (float)margin;
+    // the nearest bisectors bound each cell; with a GPU-built list the
+    // distance-ordered copy gives them first, a user list is used whole
+    const int32_t* box_list = knn ? c->nbr_dist.ptr : c->nbr.ptr;
+    const int k_box = knn ? std::min(c->k, 32) : c->k;
     CK(c->site_box.ensure((size_t)n_site * 2), "alloc");
-    bp.site_box = c->site_box.ptr;
-    bp.counters = nullptr;
-    int bw = 4;
-    int bblocks = std::max(1, std::min((n_site + bw - 1) / bw, c->num_sms * box_blocks_per_sm(bw)));
-    CK(launch_site_box(bp, bblocks, bw, st), "site boxes");
-
+    CK(c->site_planes.ensure((size_t)n_site * kBoxPlanes), "alloc");
+    CK(c->site_nplanes.ensure((size_t)n_site), "alloc");
     CK(c->tet_count.ensure(n_tet), "alloc");
     CK(c->tet_offsets.ensure((size_t)n_tet + 1), "alloc");
     CK(c->tet_fill.ensure(n_tet), "alloc");
@@ -473,24 +489,64 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
       CK(c->pair_buf.ensure((size_t)cap), "alloc pairs");
       CK(cudaMemsetAsync(c->tet_count.ptr, 0, sizeof(int32_t) * (size_t)n_tet, st), "memset");
       CK(cudaMemsetAsync(c->scratch.ptr + 4, 0, sizeof(unsigned long long), st), "memset");
-      PairParams pp;
-      pp.vert3f = c->vert3f.ptr;
-      pp.tets = c->tets.ptr;
-      pp.centroid = c->centroid.ptr;
-      pp.tg = tg;
-      pp.tcell_start = c->t_cell_start.ptr;
-      pp.tcell_items = c->t_cell_items.ptr;
-      pp.site4f = c->site4f.ptr;
-      pp.flags = c->flags.ptr;
-      pp.nbr = c->nbr.ptr;
-      pp.k = c->k;
-      pp.n_site = n_site;
-      pp.site_box = c->site_box.ptr;
-      pp.pair_buf = c->pair_buf.ptr;
-      pp.pair_cursor = c->scratch.ptr + 4;
-      pp.pair_cap = (long long)c->pair_buf.cap;
-      pp.tet_count = c->tet_count.ptr;
-      CK(launch_pairs(pp, st), "pairs");
+      for (int cl = 0; cl < rpd_ctx::kClasses; ++cl) {
+        if (c->class_count[cl] == 0) continue;
+        Grid tg = make_grid(c->mesh_lo, c->mesh_hi, c->class_count[cl], 4.0);
+        long long nc = (long long)tg.nx * tg.ny * tg.nz;
+        CK(c->t_cell_count.ensure(nc), "alloc");
+        CK(c->t_cell_start.ensure(nc + 1), "alloc");
+        CK(c->t_cell_fill.ensure(nc), "alloc");
+        CK(c->scan_tmp.ensure(scan_temp_ints(std::max<long long>(nc, n_tet)) + 16), "alloc");
+        CK(grid_build_tets(c->centroid.ptr, n_tet, c->tet_class.ptr, cl, tg, c->t_cell_of.ptr,
+                           c->t_cell_count.ptr, c->t_cell_start.ptr, c->t_cell_fill.ptr,
+                           c->t_cell_items.ptr, c->scan_tmp.ptr, st), "tet grid");
+        // per-site boxes: every tet of this class that passes the rule has
+        // its centroid in the site's cell pushed out by the class radius
+        const double R = c->class_radius[cl] * (1.0 + 1e-5) + 1e-6 * cs;
+        BoxParams bp;
+        bp.site4f = c->site4f.ptr;
+        bp.flags = c->flags.ptr;
+        bp.nbr = box_list;
+        bp.k = c->k;
+        bp.k_box = k_box;
+        bp.n_site = n_site;
+        bp.box_lo = make_float4((float)(c->mesh_lo[0] - margin), (float)(c->mesh_lo[1] - margin),
+                                (float)(c->mesh_lo[2] - margin), 0.f);
+        bp.box_hi = make_float4((float)(c->mesh_hi[0] + margin), (float)(c->mesh_hi[1] + margin),
+                                (float)(c->mesh_hi[2] + margin), 0.f);
+        bp.offset_r = (float)R;
+        bp.offset_e = (float)(48.0 * u * (diag2 + std::fabs((double)c->w_max)));
+        bp.coord_scale = (float)cs;
+        bp.abs_margin = (float)margin;
+        bp.site_box = c->site_box.ptr;
+        bp.site_planes = c->site_planes.ptr;
+        bp.site_nplanes = c->site_nplanes.ptr;
+        bp.counters = nullptr;
+        int bw = 4;
+        int bblocks = std::max(1, std::min((n_site + bw - 1) / bw, c->num_sms * box_blocks_per_sm(bw)));
+        CK(launch_site_box(bp, bblocks, bw, st), "site boxes");
+        PairParams pp;
+        pp.vert3f = c->vert3f.ptr;
+        pp.tets = c->tets.ptr;
+        pp.centroid = c->centroid.ptr;
+        pp.tg = tg;
+        pp.tcell_start = c->t_cell_start.ptr;
+        pp.tcell_items = c->t_cell_items.ptr;
+        pp.site4f = c->site4f.ptr;
+        pp.flags = c->flags.ptr;
+        pp.nbr = c->nbr.ptr;
+        pp.k = c->k;
+        pp.n_site = n_site;
+        pp.site_box = c->site_box.ptr;
+        pp.site_planes = c->site_planes.ptr;
+        pp.site_nplanes = c->site_nplanes.ptr;
+        pp.coord_scale = (float)cs;
+        pp.pair_buf = c->pair_buf.ptr;
+        pp.pair_cursor = c->scratch.ptr + 4;
+        pp.pair_cap = (long long)c->pair_buf.cap;
+        pp.tet_count = c->tet_count.ptr;
+        CK(launch_pairs(pp, st), "pairs");
+      }
       unsigned long long np = 0;
       CK(cudaMemcpyAsync(&np, c->scratch.ptr + 4, sizeof(np), cudaMemcpyDeviceToHost, st), "D2H");
       CK(cudaStreamSynchronize(st), "pairs sync");
@@ -544,7 +600,9 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
     p.work = c->scratch.ptr + 1;
     p.counters = c->scratch.ptr + 2;
     p.geometry = c->cfg.compute_geometry;
+    CK(cudaEventRecord(c->ev[kEvClipK0], st), "event");
     if (n_pairs > 0) CK(launch_clip_cells(p, c->cfg.predicate_mode, blocks, warps, st), "clip");
+    CK(cudaEventRecord(c->ev[kEvClipK1], st), "event");
     unsigned long long cur = 0;
     CK(cudaMemcpyAsync(&cur, c->scratch.ptr, sizeof(cur), cudaMemcpyDeviceToHost, st), "D2H");
     CK(cudaStreamSynchronize(st), "clip sync");
@@ -590,6 +648,8 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
     cudaEventElapsedTime(&stats->ms_pairs, c->ev[kEvKnn], c->ev[kEvPairs]);
     cudaEventElapsedTime(&stats->ms_clip, c->ev[kEvPairs], c->ev[kEvClip]);
     cudaEventElapsedTime(&stats->ms_compact, c->ev[kEvClip], c->ev[kEvEnd]);
+    cudaEventElapsedTime(&stats->ms_clip_kernel, c->ev[kEvClipK0], c->ev[kEvClipK1]);
+    stats->n_launches = take_launches();
   }
   return RPD_OK;
 }
@@ -671,6 +731,19 @@ rpd_status rpd_copy_pairs_to_host(rpd_ctx* c, int32_t* tet_offsets, int32_t* pai
                        cudaMemcpyDeviceToHost, c->stream), "D2H");
   CK(cudaStreamSynchronize(c->stream), "sync");
   return RPD_OK;
+}
+
+void* rpd_host_alloc(size_t bytes) {
+  void* p = nullptr;
+  if (cudaMallocHost(&p, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return p;
+}
+
+void rpd_host_free(void* p) {
+  if (p) cudaFreeHost(p);
 }
 
 }  // extern "C"

@@ -32,6 +32,7 @@
 #include <cuda_runtime.h>
 
 #include "rpd_common.cuh"
+#include "rpd_df64.cuh"
 #include "rpd_kernels.cuh"
 
 namespace rpd {
@@ -44,9 +45,13 @@ struct __align__(16) WarpCell {
   union {
     struct {
       float4 K[kMaxT];  // cofactors of each vertex (filter)
-      float M[kMaxT];   // largest 3x3 permanent of each vertex (filter)
+      float4 M[kMaxT];  // 3x3 permanents matching each cofactor (filter)
     } f;
-    double pd[kMaxP][4];  // FP64 planes (geometry pass)
+    struct {
+      df n[kMaxP][3];   // plane normal, seed frame, double-float (geometry)
+      df d[kMaxP];      // plane offset, seed frame
+      float dl[kMaxP];  // plane offset in the frame of the tet centroid
+    } g;
   } u;
   int2 id2[kMaxP];
   uchar4 ver[kMaxT];
@@ -64,6 +69,8 @@ struct CellState {
 __constant__ int8_t cFaceLv[4][3] = {{2, 1, 3}, {0, 2, 3}, {1, 0, 3}, {0, 1, 2}};
 __constant__ int8_t cEdgeFaces[6][2] = {{2, 3}, {1, 3}, {1, 2}, {0, 3}, {0, 2}, {0, 1}};
 __constant__ int8_t cTetTri[4][3] = {{1, 3, 2}, {0, 2, 3}, {0, 3, 1}, {0, 1, 2}};
+// slot of the initial edge between tet faces (lo, hi), lo < hi < 4
+__constant__ int8_t cTetEdgeSlot[4][4] = {{-1, 5, 4, 3}, {5, -1, 2, 1}, {4, 2, -1, 0}, {3, 1, 0, -1}};
 
 // ------------------------------------------------------------------------
 // reference arithmetic (no contraction in this TU)
@@ -133,34 +140,34 @@ __device__ __forceinline__ void minor3(float a1, float b1, float c1, float a2,
 }
 
 __device__ __forceinline__ void vertex_cofactors(float4 p1, float4 p2, float4 p3,
-                                                 float4& K, float& M) {
-  float d, pm, mx;
-  minor3(p1.y, p1.z, p1.w, p2.y, p2.z, p2.w, p3.y, p3.z, p3.w, d, pm);
+                                                 float4& K, float4& M) {
+  float d;
+  minor3(p1.y, p1.z, p1.w, p2.y, p2.z, p2.w, p3.y, p3.z, p3.w, d, M.x);
   K.x = -d;
-  mx = pm;
-  minor3(p1.x, p1.z, p1.w, p2.x, p2.z, p2.w, p3.x, p3.z, p3.w, d, pm);
+  minor3(p1.x, p1.z, p1.w, p2.x, p2.z, p2.w, p3.x, p3.z, p3.w, d, M.y);
   K.y = d;
-  mx = fmaxf(mx, pm);
-  minor3(p1.x, p1.y, p1.w, p2.x, p2.y, p2.w, p3.x, p3.y, p3.w, d, pm);
+  minor3(p1.x, p1.y, p1.w, p2.x, p2.y, p2.w, p3.x, p3.y, p3.w, d, M.z);
   K.z = -d;
-  mx = fmaxf(mx, pm);
-  minor3(p1.x, p1.y, p1.z, p2.x, p2.y, p2.z, p3.x, p3.y, p3.z, d, pm);
+  minor3(p1.x, p1.y, p1.z, p2.x, p2.y, p2.z, p3.x, p3.y, p3.z, d, M.w);
   K.w = d;
-  mx = fmaxf(mx, pm);
-  M = mx;
 }
 
 constexpr float kFiltC1 = 5.0f * 5.9604645e-08f;
 constexpr float kFiltC2 = 6.0f * 5.9604645e-08f;
 constexpr float kFiltAbs = 1e-30f;
 
-// +1 / -1 decided, 0 undecided
-__device__ __forceinline__ int filter_sign(float4 K, float M, float4 e, float se) {
+// +1 / -1 decided, 0 undecided.  Bound: c1 sum|e_r K_r| (rounding of the
+// dot) + c2 sum|e_r| M_r (rounding of the cofactors, and of the reference's
+// own FP64 evaluation, both proportional to the 4x4 permanent
+// sum_r |e_r| M_r)
+__device__ __forceinline__ int filter_sign(float4 K, float4 M, float4 e) {
   float s = __fmaf_rn(e.w, K.w, __fmaf_rn(e.z, K.z, __fmaf_rn(e.y, K.y, e.x * K.x)));
   float t = __fmaf_rn(fabsf(e.w), fabsf(K.w),
                       __fmaf_rn(fabsf(e.z), fabsf(K.z),
                                 __fmaf_rn(fabsf(e.y), fabsf(K.y), fabsf(e.x) * fabsf(K.x))));
-  float b = __fmaf_rn(kFiltC1, t, kFiltC2 * (M * se)) + kFiltAbs;
+  float pm = __fmaf_rn(fabsf(e.w), M.w,
+                       __fmaf_rn(fabsf(e.z), M.z, __fmaf_rn(fabsf(e.y), M.y, fabsf(e.x) * M.x)));
+  float b = __fmaf_rn(kFiltC1, t, kFiltC2 * pm) + kFiltAbs;
   return s > b ? 1 : (s < -b ? -1 : 0);
 }
 
@@ -168,21 +175,17 @@ __device__ __forceinline__ bool plane_eq(float4 a, float4 b) {
   return a.x == b.x && a.y == b.y && a.z == b.z && a.w == b.w;
 }
 
-__device__ __forceinline__ float plane_abs_sum(float4 e) {
-  return (fabsf(e.x) + fabsf(e.y)) + (fabsf(e.z) + fabsf(e.w));
-}
-
 // conflict of the vertex in slot vi with plane e; dup = planes identical to e
 template <int PRED>
 __device__ __forceinline__ bool in_conflict(const WarpCell& c, int vi, float4 e,
-                                            float se, uint64_t dup,
+                                            uint64_t dup,
                                             uint32_t& n_pred, uint32_t& n_esc) {
   uchar4 v = c.ver[vi];
   uint64_t vm = (1ull << v.x) | (1ull << v.y) | (1ull << v.z);
   if (dup & vm) return false;
   ++n_pred;
   if (PRED == RPD_PRED_FP32_FILTER) {
-    int s = filter_sign(c.u.f.K[vi], c.u.f.M[vi], e, se);
+    int s = filter_sign(c.u.f.K[vi], c.u.f.M[vi], e);
     if (s != 0) return s > 0;
     ++n_esc;
   }
@@ -208,7 +211,7 @@ __device__ __forceinline__ void swap_slots(WarpCell& c, int a, int b) {
   float4 k = c.u.f.K[a];
   c.u.f.K[a] = c.u.f.K[b];
   c.u.f.K[b] = k;
-  float m = c.u.f.M[a];
+  float4 m = c.u.f.M[a];
   c.u.f.M[a] = c.u.f.M[b];
   c.u.f.M[b] = m;
 }
@@ -218,9 +221,9 @@ __device__ __forceinline__ uint8_t tri_plane(const uchar4& t, int e) {
 }
 
 // cavity boundary as a circular list over plane ids (convex_cell.cu:618-678)
+// (bnext must be all kEnd on entry; the warp clears it before lane 0 runs)
 __device__ void compute_boundary(WarpCell& c, int nb_v, int& nb_r, int& first,
                                  int& status) {
-  for (int i = 0; i < kMaxP; ++i) c.bnext[i] = kEnd;
   first = kEnd;
   int nb_iter = 0;
   int t = nb_v;
@@ -266,13 +269,18 @@ __device__ void compute_boundary(WarpCell& c, int nb_v, int& nb_r, int& first,
   }
 }
 
-__device__ __forceinline__ int find_edge(const WarpCell& c, int nb_e, int p1, int p2) {
-  int lo = p1 < p2 ? p1 : p2, hi = p1 < p2 ? p2 : p1;
-  for (int e = 0; e < nb_e; ++e) {
-    uchar4 ed = c.edge[e];
-    if (ed.x == lo && ed.y == hi) return e;
-  }
-  return -1;
+// #adjacent cells of the edge between planes a and b.  The reference looks
+// the edge up in the cell's edge list (find_edge_id, convex_cell.cu:511-522)
+// and reads its count; that count is fixed when the edge is created: the
+// tet's own count for the six initial edges (both planes are tet faces,
+// convex_cell.cu:193-211) and max(h_a, h_b) for every edge made by new_edge
+// (:604-616).  Two existing planes never become adjacent later (a clip only
+// adds adjacencies to the new plane), so every edge queried by new_vertex
+// exists exactly once and its count follows from the two plane ids.
+__device__ __forceinline__ uint8_t edge_adj(const WarpCell& c, int a, int b) {
+  if (a < 4 && b < 4) return c.edge[cTetEdgeSlot[a][b]].z;
+  uint8_t ha = c.h[a], hb = c.h[b];
+  return ha > hb ? ha : hb;
 }
 
 // Adds plane e (already written to slot nb_p by the caller) and applies the
@@ -329,16 +337,10 @@ __device__ void apply_clip(WarpCell& c, CellState& s, const uint32_t* mask_in) {
     } else {
       uint8_t adj = 0;
       if (FULL) {
-        int e1 = find_edge(c, s.nb_e, cur, cir), e2 = find_edge(c, s.nb_e, cur, nx),
-            e3 = find_edge(c, s.nb_e, cir, nx);
-        if (e1 < 0 || e2 < 0 || e3 < 0) {
-          // the reference reads out of bounds here; reported as inconsistent
-          s.status = kInconsistentBoundary;
-          return;
-        }
-        adj = c.edge[e1].z;
-        if (c.edge[e2].z > adj) adj = c.edge[e2].z;
-        if (c.edge[e3].z > adj) adj = c.edge[e3].z;
+        adj = edge_adj(c, cur, cir);
+        uint8_t a2 = edge_adj(c, cur, nx), a3 = edge_adj(c, cir, nx);
+        if (a2 > adj) adj = a2;
+        if (a3 > adj) adj = a3;
       }
       c.ver[s.nb_v] = make_uchar4((uint8_t)cur, (uint8_t)cir, (uint8_t)nx, adj);
       s.nb_v++;
@@ -374,8 +376,7 @@ __device__ __forceinline__ uint64_t shfl64(uint64_t v, int src) {
 __device__ __forceinline__ void refresh_cofactors(WarpCell& c, int from, int to, int lane) {
   for (int v = from + lane; v < to; v += 32) {
     uchar4 t = c.ver[v];
-    float4 K;
-    float M;
+    float4 K, M;
     vertex_cofactors(c.pl[t.x], c.pl[t.y], c.pl[t.z], K, M);
     c.u.f.K[v] = K;
     c.u.f.M[v] = M;
@@ -397,7 +398,6 @@ __device__ void clip_list(WarpCell& c, CellState& s, const int32_t* list, int k,
     int count = (~valid == 0u) ? 32 : (__ffs(~valid) - 1);  // up to first -1
     float4 e_mine = make_float4(0.f, 0.f, 0.f, 0.f);
     if (lane < count) e_mine = make_plane(j);
-    float se_mine = plane_abs_sum(e_mine);
     // planes already in the cell that equal this lane's plane
     uint64_t dup_mine = 0;
     for (int p = 0; p < s.nb_p; ++p)
@@ -416,10 +416,9 @@ __device__ void clip_list(WarpCell& c, CellState& s, const int32_t* list, int k,
         int pi = lane >> lgV, vi = lane & (V - 1);
         int pidx = r + pi;
         float4 e = shfl4(e_mine, pidx & 31);
-        float se = __shfl_sync(0xffffffffu, se_mine, pidx & 31);
         uint64_t dup = shfl64(dup_mine, pidx & 31);
         bool cf = false;
-        if (pidx < count && vi < s.nb_v) cf = in_conflict<PRED>(c, vi, e, se, dup, n_pred, n_esc);
+        if (pidx < count && vi < s.nb_v) cf = in_conflict<PRED>(c, vi, e, dup, n_pred, n_esc);
         uint32_t m = __ballot_sync(0xffffffffu, cf);
         if (m == 0u) {
           r += 32 >> lgV;
@@ -430,13 +429,12 @@ __device__ void clip_list(WarpCell& c, CellState& s, const int32_t* list, int k,
         hit = r + pf;
       } else {
         float4 e = shfl4(e_mine, r);
-        float se = __shfl_sync(0xffffffffu, se_mine, r);
         uint64_t dup = shfl64(dup_mine, r);
         bool any = false;
         for (int w = 0; w < 3; ++w) {
           int vi = lane + 32 * w;
           bool cf = false;
-          if (vi < s.nb_v) cf = in_conflict<PRED>(c, vi, e, se, dup, n_pred, n_esc);
+          if (vi < s.nb_v) cf = in_conflict<PRED>(c, vi, e, dup, n_pred, n_esc);
           mask[w] = __ballot_sync(0xffffffffu, cf);
           any |= mask[w] != 0u;
         }
@@ -449,6 +447,8 @@ __device__ void clip_list(WarpCell& c, CellState& s, const int32_t* list, int k,
       // the plane of list entry `hit` clips: write it and update topology
       float4 e = shfl4(e_mine, hit);
       int jn = __shfl_sync(0xffffffffu, j, hit);
+      if (lane < kMaxP / 4) reinterpret_cast<uint32_t*>(c.bnext)[lane] = 0xffffffffu;
+      __syncwarp();
       if (lane == 0) {
         const int cur = s.nb_p;
         c.pl[cur] = e;
@@ -468,8 +468,7 @@ __device__ void clip_list(WarpCell& c, CellState& s, const int32_t* list, int k,
         for (int v = lane; v < s.nb_v; v += 32) {
           uchar4 t = c.ver[v];
           if (t.x == cur) {
-            float4 K;
-            float M;
+            float4 K, M;
             vertex_cofactors(c.pl[t.x], c.pl[t.y], c.pl[t.z], K, M);
             c.u.f.K[v] = K;
             c.u.f.M[v] = M;
@@ -487,83 +486,185 @@ __device__ void clip_list(WarpCell& c, CellState& s, const int32_t* list, int k,
 }
 
 // ------------------------------------------------------------------------
-// cell kernel
+// FP64-accurate reconstruction of the emitted cell
 // ------------------------------------------------------------------------
-__device__ __forceinline__ void tri2plane_d(const double* v0, const double* v1,
-                                            const double* v2, double* out) {
-  double ax = v1[0] - v0[0], ay = v1[1] - v0[1], az = v1[2] - v0[2];
-  double bx = v2[0] - v0[0], by = v2[1] - v0[1], bz = v2[2] - v0[2];
-  double nx = ay * bz - az * by;
-  double ny = az * bx - ax * bz;
-  double nz = ax * by - ay * bx;
-  out[0] = nx;
-  out[1] = ny;
-  out[2] = nz;
-  out[3] = -(v0[0] * nx + v0[1] * ny + v0[2] * nz);
+// The float planes above decide the topology exactly as the reference does.
+// The coordinates reported for the surviving vertices are rebuilt from the
+// FP64 inputs instead: every plane is recomputed in the frame centred on the
+// seed S (differences of FP64 coordinates, rounded once), and each vertex --
+// the intersection of its three planes, by Cramer's rule as in
+// compute_vertex_coordinates (convex_cell.cu:319-351) -- is solved in
+// double-float arithmetic on the FP32 pipe, then translated back by S in
+// FP64.  The cell volume uses the reference's per-vertex decomposition into
+// six tets (convex_cell.cu:986-1069) in FP32, about the tet centroid (small
+// coordinates, no cancellation against the scene's extent).
+
+__device__ __forceinline__ df dmul3(df a, df b, df c) { return df_mul(df_mul(a, b), c); }
+
+// 2x2 minor b_p c_q - b_q c_p
+__device__ __forceinline__ df minor2(df bp, df bq, df cp, df cq) {
+  return df_sub(df_mul(bp, cq), df_mul(bq, cp));
 }
 
-__device__ __forceinline__ void bisector_d(const double* S, const double* B, double* out) {
-  double dx = S[0] - B[0], dy = S[1] - B[1], dz = S[2] - B[2];
-  double ax = S[0] + B[0], ay = S[1] + B[1], az = S[2] + B[2];
-  double dot = (ax * dx + ay * dy + az * dz) + (B[3] - S[3]);
-  out[0] = dx;
-  out[1] = dy;
-  out[2] = dz;
-  out[3] = -dot * 0.5;
+__device__ __forceinline__ float3 f3sub(float3 a, float3 b) {
+  return make_float3(a.x - b.x, a.y - b.y, a.z - b.z);
 }
-
-__device__ __forceinline__ double det3d(double a11, double a12, double a13, double a21,
-                                        double a22, double a23, double a31, double a32,
-                                        double a33) {
-  return a11 * (a22 * a33 - a23 * a32) - a21 * (a12 * a33 - a13 * a32) +
-         a31 * (a12 * a23 - a13 * a22);
+__device__ __forceinline__ float f3dot(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float3 f3cross(float3 a, float3 b) {
+  return make_float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
 }
-
-__device__ __forceinline__ void vertex_d(const double* a, const double* b, const double* c,
-                                         double* out) {
-  double x = -det3d(a[3], a[1], a[2], b[3], b[1], b[2], c[3], c[1], c[2]);
-  double y = -det3d(a[0], a[3], a[2], b[0], b[3], b[2], c[0], c[3], c[2]);
-  double z = -det3d(a[0], a[1], a[3], b[0], b[1], b[3], c[0], c[1], c[3]);
-  double w = det3d(a[0], a[1], a[2], b[0], b[1], b[2], c[0], c[1], c[2]);
-  out[0] = x / w;
-  out[1] = y / w;
-  out[2] = z / w;
+__device__ __forceinline__ float3 f3axpy(float a, float3 x, float3 y) {
+  return make_float3(a * x.x + y.x, a * x.y + y.y, a * x.z + y.z);
 }
+__device__ __forceinline__ float det3f(float3 a, float3 b, float3 c) { return f3dot(a, f3cross(b, c)); }
 
-__device__ __forceinline__ void project_d(const double* P, const double* pl, double* out) {
-  double n2 = pl[0] * pl[0] + pl[1] * pl[1] + pl[2] * pl[2];
-  double lam = n2 > 0.0 ? (pl[0] * P[0] + pl[1] * P[1] + pl[2] * P[2] + pl[3]) / n2 : 0.0;
-  out[0] = P[0] - lam * pl[0];
-  out[1] = P[1] - lam * pl[1];
-  out[2] = P[2] - lam * pl[2];
-}
-
-// signed volume of the 6 flag tets of one vertex (the decomposition of
-// convex_cell.cu:986-1069, in FP64): C seed, A vertex, feet of C on the 3
-// faces and on the 3 edge lines through A
-__device__ double vertex_volume_d(const double* C, const double* A, const double* f0,
-                                  const double* f1, const double* f2) {
-  const double* f[3] = {f0, f1, f2};
-  double P[6][3];
-  for (int i = 0; i < 3; ++i) project_d(C, f[i], P[2 * i]);
+// signed volume of one vertex's six flag tets, origin O = (0,0,0):
+// feet of O on the three faces and on the three edge lines through A
+__device__ float vertex_volume_f(float3 A, const float3* n, const float* d) {
+  float3 P[6];
   for (int i = 0; i < 3; ++i) {
-    const double* u = f[i];
-    const double* v = f[(i + 1) % 3];
-    double n[4] = {u[1] * v[2] - u[2] * v[1], u[2] * v[0] - u[0] * v[2],
-                   u[0] * v[1] - u[1] * v[0], 0.0};
-    n[3] = -(C[0] * n[0] + C[1] * n[1] + C[2] * n[2]);
-    project_d(A, n, P[2 * i + 1]);
+    float n2 = f3dot(n[i], n[i]);
+    float lam = n2 > 0.f ? d[i] / n2 : 0.f;
+    P[2 * i] = make_float3(-lam * n[i].x, -lam * n[i].y, -lam * n[i].z);
   }
-  double vol = 0.0;
-  for (int i = 0; i < 6; ++i) {
-    const double* p = P[i];
-    const double* q = P[(i + 1) % 6];
-    double a0 = p[0] - A[0], a1 = p[1] - A[1], a2 = p[2] - A[2];
-    double b0 = q[0] - A[0], b1 = q[1] - A[1], b2 = q[2] - A[2];
-    double c0 = C[0] - A[0], c1 = C[1] - A[1], c2 = C[2] - A[2];
-    vol += -det3d(a0, a1, a2, b0, b1, b2, c0, c1, c2) / 6.0;
+  for (int i = 0; i < 3; ++i) {
+    float3 t = f3cross(n[i], n[(i + 1) % 3]);
+    float t2 = f3dot(t, t);
+    float lam = t2 > 0.f ? f3dot(t, A) / t2 : 0.f;
+    P[2 * i + 1] = f3axpy(-lam, t, A);
   }
-  return vol;
+  float3 mA = make_float3(-A.x, -A.y, -A.z);
+  float v = 0.f;
+  for (int i = 0; i < 6; ++i) v -= det3f(f3sub(P[i], A), f3sub(P[(i + 1) % 6], A), mA);
+  return v * (1.0f / 6.0f);
+}
+
+// intersection of three float planes, double-float Cramer (box kernel)
+__device__ void vertex_of_float_planes(float4 a4, float4 b4, float4 c4, double* out) {
+  df ax = df_make(a4.x, 0.f), ay = df_make(a4.y, 0.f), az = df_make(a4.z, 0.f),
+     aw = df_make(a4.w, 0.f);
+  df bx = df_make(b4.x, 0.f), by = df_make(b4.y, 0.f), bz = df_make(b4.z, 0.f),
+     bw = df_make(b4.w, 0.f);
+  df cx = df_make(c4.x, 0.f), cy = df_make(c4.y, 0.f), cz = df_make(c4.z, 0.f),
+     cw = df_make(c4.w, 0.f);
+  df mxy = minor2(bx, by, cx, cy), mxz = minor2(bx, bz, cx, cz), mxw = minor2(bx, bw, cx, cw);
+  df myz = minor2(by, bz, cy, cz), myw = minor2(by, bw, cy, cw), mzw = minor2(bz, bw, cz, cw);
+  df Dw = df_add(df_sub(df_mul(ax, myz), df_mul(ay, mxz)), df_mul(az, mxy));
+  df Dx = df_add(df_sub(df_mul(ay, mzw), df_mul(az, myw)), df_mul(aw, myz));
+  df Dy = df_add(df_sub(df_mul(ax, mzw), df_mul(az, mxw)), df_mul(aw, mxz));
+  df Dz = df_add(df_sub(df_mul(ax, myw), df_mul(ay, mxw)), df_mul(aw, mxy));
+  double w = df_to_double(Dw);
+  out[0] = -df_to_double(Dx) / w;
+  out[1] = df_to_double(Dy) / w;
+  out[2] = -df_to_double(Dz) / w;
+}
+
+// vertex (X, Y, Z) of the three seed-frame double-float planes pa, pb, pc
+__device__ __forceinline__ void cell_vertex(const WarpCell& c, int pa, int pb, int pc, df& X,
+                                            df& Y, df& Z) {
+  df ax = c.u.g.n[pa][0], ay = c.u.g.n[pa][1], az = c.u.g.n[pa][2], aw = c.u.g.d[pa];
+  df bx = c.u.g.n[pb][0], by = c.u.g.n[pb][1], bz = c.u.g.n[pb][2], bw = c.u.g.d[pb];
+  df cx = c.u.g.n[pc][0], cy = c.u.g.n[pc][1], cz = c.u.g.n[pc][2], cw = c.u.g.d[pc];
+  df mxy = minor2(bx, by, cx, cy), mxz = minor2(bx, bz, cx, cz), mxw = minor2(bx, bw, cx, cw);
+  df myz = minor2(by, bz, cy, cz), myw = minor2(by, bw, cy, cw), mzw = minor2(bz, bw, cz, cw);
+  df Dw = df_add(df_sub(df_mul(ax, myz), df_mul(ay, mxz)), df_mul(az, mxy));
+  df Dx = df_add(df_sub(df_mul(ay, mzw), df_mul(az, myw)), df_mul(aw, myz));
+  df Dy = df_add(df_sub(df_mul(ax, mzw), df_mul(az, mxw)), df_mul(aw, mxz));
+  df Dz = df_add(df_sub(df_mul(ax, myw), df_mul(ay, mxw)), df_mul(aw, mxy));
+  df inv = df_recip(Dw);
+  X = df_neg(df_mul(Dx, inv));
+  Y = df_mul(Dy, inv);
+  Z = df_neg(df_mul(Dz, inv));
+}
+
+__device__ __forceinline__ float vertex_volume_about(const WarpCell& c, uchar4 tr, df X, df Y,
+                                                     df Z, df Ox, df Oy, df Oz) {
+  float3 A = make_float3(df_sub(X, Ox).hi, df_sub(Y, Oy).hi, df_sub(Z, Oz).hi);
+  const int pl[3] = {tr.x, tr.y, tr.z};
+  float3 nn[3];
+  float dd[3];
+  for (int k = 0; k < 3; ++k) {
+    nn[k] = make_float3(c.u.g.n[pl[k]][0].hi, c.u.g.n[pl[k]][1].hi, c.u.g.n[pl[k]][2].hi);
+    dd[k] = c.u.g.dl[pl[k]];
+  }
+  return vertex_volume_f(A, nn, dd);
+}
+
+// writes xyz[3 * nb_v] and returns the cell volume
+__device__ double cell_geometry(WarpCell& c, const CellState& s, const ClipParams& p,
+                                const int* tvs, int sid, int lane, double* xyz) {
+  const double* S = p.site4d + 4 * (long long)sid;
+  const double Sx = S[0], Sy = S[1], Sz = S[2], Sw = S[3];
+  for (int i = lane; i < s.nb_p; i += 32) {
+    df nx, ny, nz, d;
+    if (i < 4) {
+      const double* a = p.vert3d + 3 * (long long)tvs[cFaceLv[i][0]];
+      const double* b = p.vert3d + 3 * (long long)tvs[cFaceLv[i][1]];
+      const double* e = p.vert3d + 3 * (long long)tvs[cFaceLv[i][2]];
+      df ax = df_from_double(b[0] - a[0]), ay = df_from_double(b[1] - a[1]),
+         az = df_from_double(b[2] - a[2]);
+      df bx = df_from_double(e[0] - a[0]), by = df_from_double(e[1] - a[1]),
+         bz = df_from_double(e[2] - a[2]);
+      nx = df_sub(df_mul(ay, bz), df_mul(az, by));
+      ny = df_sub(df_mul(az, bx), df_mul(ax, bz));
+      nz = df_sub(df_mul(ax, by), df_mul(ay, bx));
+      df v0x = df_from_double(a[0] - Sx), v0y = df_from_double(a[1] - Sy),
+         v0z = df_from_double(a[2] - Sz);
+      d = df_neg(df_add(df_add(df_mul(v0x, nx), df_mul(v0y, ny)), df_mul(v0z, nz)));
+    } else {
+      int2 id = c.id2[i];
+      int other = id.x == sid ? id.y : id.x;
+      const double* B = p.site4d + 4 * (long long)other;
+      // bisector in the seed frame: n = S - B, d = (|n|^2 + wS - wB) / 2
+      nx = df_from_double(Sx - B[0]);
+      ny = df_from_double(Sy - B[1]);
+      nz = df_from_double(Sz - B[2]);
+      df n2 = df_add(df_add(df_mul(nx, nx), df_mul(ny, ny)), df_mul(nz, nz));
+      df dw = df_from_double(Sw - B[3]);
+      d = df_add(n2, dw);
+      d = df_make(0.5f * d.hi, 0.5f * d.lo);
+    }
+    c.u.g.n[i][0] = nx;
+    c.u.g.n[i][1] = ny;
+    c.u.g.n[i][2] = nz;
+    c.u.g.d[i] = d;
+  }
+  __syncwarp();
+  // first pass: vertices lane, lane + 32, lane + 64
+  df X0, Y0, Z0;
+  uchar4 tr0 = make_uchar4(0, 0, 0, 0);
+  if (lane < s.nb_v) {
+    tr0 = c.ver[lane];
+    cell_vertex(c, tr0.x, tr0.y, tr0.z, X0, Y0, Z0);
+    xyz[3 * lane] = Sx + df_to_double(X0);
+    xyz[3 * lane + 1] = Sy + df_to_double(Y0);
+    xyz[3 * lane + 2] = Sz + df_to_double(Z0);
+  }
+  // volume origin O = the cell's vertex 0: the decomposition's terms then
+  // scale with the cell's own size
+  df Ox = df_make(__shfl_sync(0xffffffffu, X0.hi, 0), __shfl_sync(0xffffffffu, X0.lo, 0));
+  df Oy = df_make(__shfl_sync(0xffffffffu, Y0.hi, 0), __shfl_sync(0xffffffffu, Y0.lo, 0));
+  df Oz = df_make(__shfl_sync(0xffffffffu, Z0.hi, 0), __shfl_sync(0xffffffffu, Z0.lo, 0));
+  for (int i = lane; i < s.nb_p; i += 32) {
+    df n0 = c.u.g.n[i][0], n1 = c.u.g.n[i][1], n2 = c.u.g.n[i][2];
+    df dc = df_add(c.u.g.d[i], df_add(df_add(df_mul(n0, Ox), df_mul(n1, Oy)), df_mul(n2, Oz)));
+    c.u.g.dl[i] = dc.hi;
+  }
+  __syncwarp();
+  float vol = 0.f;
+  if (lane < s.nb_v) vol += vertex_volume_about(c, tr0, X0, Y0, Z0, Ox, Oy, Oz);
+  for (int v = lane + 32; v < s.nb_v; v += 32) {
+    uchar4 tr = c.ver[v];
+    df X, Y, Z;
+    cell_vertex(c, tr.x, tr.y, tr.z, X, Y, Z);
+    xyz[3 * v] = Sx + df_to_double(X);
+    xyz[3 * v + 1] = Sy + df_to_double(Y);
+    xyz[3 * v + 2] = Sz + df_to_double(Z);
+    vol += vertex_volume_about(c, tr, X, Y, Z, Ox, Oy, Oz);
+  }
+  double dv = (double)vol;
+  for (int o = 16; o > 0; o >>= 1) dv += __shfl_xor_sync(0xffffffffu, dv, o);
+  return dv;
 }
 
 template <int PRED>
@@ -659,31 +760,7 @@ __global__ void __launch_bounds__(kClipMaxThreads) clip_cells_kernel(ClipParams 
         double vol = 0.0;
         if (p.geometry) {
           __syncwarp();
-          // FP64 planes from FP64 inputs (cofactor storage is dead now)
-          const double* S = p.site4d + 4 * (long long)sid;
-          for (int i = lane; i < s.nb_p; i += 32) {
-            double* out = c.u.pd[i];
-            if (i < 4) {
-              int a = tvs[cFaceLv[i][0]], b = tvs[cFaceLv[i][1]], d = tvs[cFaceLv[i][2]];
-              tri2plane_d(p.vert3d + 3 * (long long)a, p.vert3d + 3 * (long long)b,
-                          p.vert3d + 3 * (long long)d, out);
-            } else {
-              int2 id = c.id2[i];
-              int other = id.x == sid ? id.y : id.x;
-              bisector_d(S, p.site4d + 4 * (long long)other, out);
-            }
-          }
-          __syncwarp();
-          for (int v = lane; v < s.nb_v; v += 32) {
-            uchar4 tr = c.ver[v];
-            double A[3];
-            vertex_d(c.u.pd[tr.x], c.u.pd[tr.y], c.u.pd[tr.z], A);
-            xyz[3 * v] = A[0];
-            xyz[3 * v + 1] = A[1];
-            xyz[3 * v + 2] = A[2];
-            vol += vertex_volume_d(S, A, c.u.pd[tr.x], c.u.pd[tr.y], c.u.pd[tr.z]);
-          }
-          for (int o = 16; o > 0; o >>= 1) vol += __shfl_xor_sync(0xffffffffu, vol, o);
+          vol = cell_geometry(c, s, p, tvs, sid, lane, xyz);
         } else {
           for (int i = lane; i < 3 * s.nb_v; i += 32) xyz[i] = 0.0;
         }
@@ -726,6 +803,7 @@ __global__ void __launch_bounds__(kClipMaxThreads) site_box_kernel(BoxParams p) 
       if (lane == 0) {
         p.site_box[2 * i] = make_float4(1.f, 1.f, 1.f, 0.f);  // empty box
         p.site_box[2 * i + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+        p.site_nplanes[i] = 0;
       }
       continue;
     }
@@ -775,20 +853,18 @@ __global__ void __launch_bounds__(kClipMaxThreads) site_box_kernel(BoxParams p) 
       if (!(D > 0.f) || !(d < 3.0e38f)) return make_float4(0.f, 0.f, 0.f, 1.f);  // no constraint
       return make_float4(e.x, e.y, e.z, d);
     };
-    clip_list<RPD_PRED_FP32_FILTER, false>(c, s, p.nbr + (long long)i * p.k, p.k, i, make_plane,
-                                           lane, n_pred, n_esc);
+    // any subset of the planes gives a superset polytope; the nearest k_box
+    // bisectors bound the cell well and keep the box clip small
+    clip_list<RPD_PRED_FP32_FILTER, false>(c, s, p.nbr + (long long)i * p.k, p.k_box, i,
+                                           make_plane, lane, n_pred, n_esc);
     float bl[3], bh[3];
     if (s.status == kSuccess) {
       bl[0] = bl[1] = bl[2] = 3.0e38f;
       bh[0] = bh[1] = bh[2] = -3.0e38f;
       for (int v = lane; v < s.nb_v; v += 32) {
         uchar4 tr = c.ver[v];
-        double a[4], b[4], d[4], X[3];
-        float4 fa = c.pl[tr.x], fb = c.pl[tr.y], fd = c.pl[tr.z];
-        a[0] = fa.x; a[1] = fa.y; a[2] = fa.z; a[3] = fa.w;
-        b[0] = fb.x; b[1] = fb.y; b[2] = fb.z; b[3] = fb.w;
-        d[0] = fd.x; d[1] = fd.y; d[2] = fd.z; d[3] = fd.w;
-        vertex_d(a, b, d, X);
+        double X[3];
+        vertex_of_float_planes(c.pl[tr.x], c.pl[tr.y], c.pl[tr.z], X);
         for (int k = 0; k < 3; ++k) {
           float xl = __double2float_rd(X[k]), xh = __double2float_ru(X[k]);
           if (!(X[k] == X[k])) { xl = lo[k]; xh = hi[k]; }
@@ -819,6 +895,28 @@ __global__ void __launch_bounds__(kClipMaxThreads) site_box_kernel(BoxParams p) 
       p.site_box[2 * i] = make_float4(bl[0], bl[1], bl[2], (float)s.status);
       p.site_box[2 * i + 1] = make_float4(bh[0], bh[1], bh[2], 0.f);
     }
+    // the planes that bound the grown cell (referenced by a vertex): the pair
+    // search tests grid cells and tet centroids against them
+    int npl = 0;
+    if (s.status == kSuccess) {
+      unsigned long long m = 0ull;
+      for (int v = lane; v < s.nb_v; v += 32) {
+        uchar4 tr = c.ver[v];
+        m |= (1ull << tr.x) | (1ull << tr.y) | (1ull << tr.z);
+      }
+      uint32_t lo = __reduce_or_sync(0xffffffffu, (uint32_t)m);
+      uint32_t hi = __reduce_or_sync(0xffffffffu, (uint32_t)(m >> 32));
+      unsigned long long act = ((unsigned long long)hi << 32) | lo;
+      npl = __popcll(act);
+      if (npl <= kBoxPlanes) {
+        for (int q = lane; q < s.nb_p; q += 32)
+          if ((act >> q) & 1ull)
+            p.site_planes[(long long)i * kBoxPlanes + __popcll(act & ((1ull << q) - 1ull))] = c.pl[q];
+      } else {
+        npl = 0;
+      }
+    }
+    if (lane == 0) p.site_nplanes[i] = npl;
     __syncwarp();
   }
   for (int o = 16; o > 0; o >>= 1) {
@@ -865,10 +963,12 @@ cudaError_t launch_clip_cells(const ClipParams& p, int pred_mode, int blocks, in
     cudaFuncSetAttribute(clip_cells_kernel<RPD_PRED_FP32_FILTER>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     clip_cells_kernel<RPD_PRED_FP32_FILTER><<<blocks, warps * 32, smem, st>>>(p);
+    note_launches(1);
   } else {
     cudaFuncSetAttribute(clip_cells_kernel<RPD_PRED_FP64>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     clip_cells_kernel<RPD_PRED_FP64><<<blocks, warps * 32, smem, st>>>(p);
+    note_launches(1);
   }
   return cudaGetLastError();
 }
@@ -877,6 +977,7 @@ cudaError_t launch_site_box(const BoxParams& p, int blocks, int warps, cudaStrea
   size_t smem = sizeof(WarpCell) * warps;
   cudaFuncSetAttribute(site_box_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   site_box_kernel<<<blocks, warps * 32, smem, st>>>(p);
+  note_launches(1);
   return cudaGetLastError();
 }
 

@@ -12,6 +12,11 @@ namespace rpd {
 
 constexpr int kClipMaxThreads = 512;
 
+// kernels launched since the last reset (host counter, one context at a time
+// per thread)
+void note_launches(int n);
+int take_launches();
+
 struct ClipParams {
   const float* vert3f;   // n_vert x 3, float copies of the mesh vertices
   const double* vert3d;  // n_vert x 3
@@ -39,8 +44,9 @@ struct ClipParams {
 struct BoxParams {
   const float4* site4f;
   const uint32_t* flags;
-  const int32_t* nbr;
+  const int32_t* nbr;     // lists (row stride k); the first k_box entries are used
   int k;
+  int k_box;
   int n_site;
   float4 box_lo, box_hi;  // mesh box grown by offset_r
   float offset_r;         // largest distance of a tet vertex to its centroid
@@ -48,8 +54,12 @@ struct BoxParams {
   float coord_scale;      // largest coordinate magnitude
   float abs_margin;
   float4* site_box;       // n_site x 2: (lo, status), (hi, 0)
+  float4* site_planes;    // n_site x kBoxPlanes: planes of the grown cell
+  int32_t* site_nplanes;  // n_site: count (0 = use the box only)
   unsigned long long* counters;
 };
+
+constexpr int kBoxPlanes = 48;
 
 size_t clip_smem_per_warp();
 int clip_blocks_per_sm(int pred_mode, int warps);
@@ -77,8 +87,11 @@ cudaError_t scan_exclusive(const int32_t* in, int32_t* out, long long n, int32_t
 cudaError_t grid_build_sites(const float4* pts, int n, const Grid& g, int32_t* cell_of,
                              int32_t* cell_count, int32_t* cell_start, int32_t* cell_fill,
                              int32_t* cell_items, int32_t* scan_tmp, cudaStream_t st);
-cudaError_t grid_build_tets(const float* vert3f, const int4* tets, int n_tet, const Grid& g,
-                            float4* centroid, int32_t* cell_of, int32_t* cell_count,
+cudaError_t tet_centroids(const float* vert3f, const int4* tets, int n_tet, float4* centroid,
+                          cudaStream_t st);
+// bins the tets of radius class `want` (all tets when cls is null) by centroid
+cudaError_t grid_build_tets(const float4* centroid, int n_tet, const uint8_t* cls, int want,
+                            const Grid& g, int32_t* cell_of, int32_t* cell_count,
                             int32_t* cell_start, int32_t* cell_fill, int32_t* cell_items,
                             int32_t* scan_tmp, cudaStream_t st);
 
@@ -87,7 +100,7 @@ cudaError_t grid_build_tets(const float* vert3f, const int4* tets, int n_tet, co
 cudaError_t launch_knn(const float4* site4f, int n_site, const Grid& g,
                        const int32_t* cell_start, const int32_t* cell_items, int k,
                        float w_max, int order_by_id, int32_t* nbr, float* keys,
-                       int32_t* status, cudaStream_t st);
+                       int32_t* nbr_dist, int32_t* status, cudaStream_t st);
 
 // candidate pairs: per site, tets whose centroid lies in the site's box and
 // that pass the reference rule; appends (tet, site) and counts per tet
@@ -104,6 +117,9 @@ struct PairParams {
   int k;
   int n_site;
   const float4* site_box;
+  const float4* site_planes;   // n_site x kBoxPlanes
+  const int32_t* site_nplanes;
+  float coord_scale;
   int2* pair_buf;            // (tet, site)
   unsigned long long* pair_cursor;
   long long pair_cap;

@@ -29,6 +29,14 @@
 
 namespace rpd {
 
+static thread_local int tl_launches = 0;
+void note_launches(int n) { tl_launches += n; }
+int take_launches() {
+  int n = tl_launches;
+  tl_launches = 0;
+  return n;
+}
+
 // ------------------------------------------------------------------------
 // scan
 // ------------------------------------------------------------------------
@@ -104,8 +112,11 @@ cudaError_t scan_exclusive(const int32_t* in, int32_t* out, long long n, int32_t
     return cudaMemsetAsync(out, 0, sizeof(int32_t), st);
   }
   scan_reduce_kernel<<<nb, kScanBlock, 0, st>>>(in, n, temp);
+  note_launches(1);
   scan_blocksums_kernel<<<1, kScanBlock, 0, st>>>(temp, nb);
+  note_launches(1);
   scan_apply_kernel<<<nb, kScanBlock, 0, st>>>(in, n, temp, nb, out);
+  note_launches(1);
   return cudaGetLastError();
 }
 
@@ -122,9 +133,13 @@ __device__ __forceinline__ int cell_index(const Grid& g, float x, float y, float
 }
 
 __global__ void bin_points_kernel(const float4* pts, int n, Grid g, int32_t* cell_of,
-                                  int32_t* cell_count) {
+                                  int32_t* cell_count, const uint8_t* cls, int want) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  if (cls && cls[i] != want) {
+    cell_of[i] = -1;
+    return;
+  }
   float4 p = pts[i];
   int c = cell_index(g, p.x, p.y, p.z);
   cell_of[i] = c;
@@ -136,6 +151,7 @@ __global__ void fill_cells_kernel(int n, const int32_t* cell_of, const int32_t* 
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   int c = cell_of[i];
+  if (c < 0) return;
   int slot = atomicAdd(cell_fill + c, 1);
   cell_items[cell_start[c] + slot] = i;
 }
@@ -164,8 +180,10 @@ static cudaError_t grid_finish(int n, const Grid& g, const int32_t* cell_of, int
   if (err != cudaSuccess) return err;
   cudaMemsetAsync(cell_fill, 0, sizeof(int32_t) * n_cells, st);
   fill_cells_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, cell_of, cell_start, cell_fill, cell_items);
+  note_launches(1);
   sort_cells_kernel<<<(int)((n_cells + 255) / 256), 256, 0, st>>>((int)n_cells, cell_start,
                                                                  cell_items);
+  note_launches(1);
   return cudaGetLastError();
 }
 
@@ -174,7 +192,10 @@ cudaError_t grid_build_sites(const float4* pts, int n, const Grid& g, int32_t* c
                              int32_t* cell_items, int32_t* scan_tmp, cudaStream_t st) {
   long long n_cells = (long long)g.nx * g.ny * g.nz;
   cudaMemsetAsync(cell_count, 0, sizeof(int32_t) * n_cells, st);
-  if (n > 0) bin_points_kernel<<<(n + 255) / 256, 256, 0, st>>>(pts, n, g, cell_of, cell_count);
+  if (n > 0) {
+    bin_points_kernel<<<(n + 255) / 256, 256, 0, st>>>(pts, n, g, cell_of, cell_count, nullptr, 0);
+    note_launches(1);
+  }
   return grid_finish(n, g, cell_of, cell_count, cell_start, cell_fill, cell_items, scan_tmp, st);
 }
 
@@ -201,16 +222,26 @@ __global__ void tet_centroid_kernel(const float* v, const int4* tets, int n_tet,
   out[t] = make_float4(cx, cy, cz, sqrtf(r2));
 }
 
-cudaError_t grid_build_tets(const float* vert3f, const int4* tets, int n_tet, const Grid& g,
-                            float4* centroid, int32_t* cell_of, int32_t* cell_count,
+cudaError_t tet_centroids(const float* vert3f, const int4* tets, int n_tet, float4* centroid,
+                          cudaStream_t st) {
+  if (n_tet > 0) {
+    tet_centroid_kernel<<<(n_tet + 255) / 256, 256, 0, st>>>(vert3f, tets, n_tet, centroid);
+    note_launches(1);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t grid_build_tets(const float4* centroid, int n_tet, const uint8_t* cls, int want,
+                            const Grid& g, int32_t* cell_of, int32_t* cell_count,
                             int32_t* cell_start, int32_t* cell_fill, int32_t* cell_items,
                             int32_t* scan_tmp, cudaStream_t st) {
-  if (n_tet > 0)
-    tet_centroid_kernel<<<(n_tet + 255) / 256, 256, 0, st>>>(vert3f, tets, n_tet, centroid);
   long long n_cells = (long long)g.nx * g.ny * g.nz;
   cudaMemsetAsync(cell_count, 0, sizeof(int32_t) * n_cells, st);
-  if (n_tet > 0)
-    bin_points_kernel<<<(n_tet + 255) / 256, 256, 0, st>>>(centroid, n_tet, g, cell_of, cell_count);
+  if (n_tet > 0) {
+    bin_points_kernel<<<(n_tet + 255) / 256, 256, 0, st>>>(centroid, n_tet, g, cell_of, cell_count,
+                                                          cls, want);
+    note_launches(1);
+  }
   return grid_finish(n_tet, g, cell_of, cell_count, cell_start, cell_fill, cell_items, scan_tmp,
                      st);
 }
@@ -307,7 +338,7 @@ __device__ __forceinline__ int next_pow2(int x) {
 __global__ void __launch_bounds__(kKnnWarps * 32) knn_kernel(
     const float4* site4f, int n_site, Grid g, const int32_t* cell_start,
     const int32_t* cell_items, int k, float w_max, int order_by_id, int32_t* nbr, float* keys,
-    int32_t* status) {
+    int32_t* nbr_dist, int32_t* status) {
   __shared__ unsigned long long sbuf[kKnnWarps][kKnnBuf];
   __shared__ int scnt[kKnnWarps];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -381,13 +412,10 @@ __global__ void __launch_bounds__(kKnnWarps * 32) knn_kernel(
   if (status && lane == 0) status[i] = done ? 0 : 1;  // 1: exhausted grid
   // outputs in distance order
   for (int q = lane; q < k; q += 32) {
-    if (q < cnt) {
-      if (keys) keys[(long long)i * k + q] = key_value((uint32_t)(buf[q] >> 32));
-      if (!order_by_id) nbr[(long long)i * k + q] = (int32_t)(uint32_t)buf[q];
-    } else {
-      if (keys) keys[(long long)i * k + q] = INFINITY;
-      if (!order_by_id) nbr[(long long)i * k + q] = -1;
-    }
+    int32_t id = q < cnt ? (int32_t)(uint32_t)buf[q] : -1;
+    if (keys) keys[(long long)i * k + q] = q < cnt ? key_value((uint32_t)(buf[q] >> 32)) : INFINITY;
+    if (!order_by_id) nbr[(long long)i * k + q] = id;
+    if (nbr_dist) nbr_dist[(long long)i * k + q] = id;
   }
   if (order_by_id) {
     __syncwarp();
@@ -408,11 +436,13 @@ __global__ void __launch_bounds__(kKnnWarps * 32) knn_kernel(
 
 cudaError_t launch_knn(const float4* site4f, int n_site, const Grid& g, const int32_t* cell_start,
                        const int32_t* cell_items, int k, float w_max, int order_by_id,
-                       int32_t* nbr, float* keys, int32_t* status, cudaStream_t st) {
+                       int32_t* nbr, float* keys, int32_t* nbr_dist, int32_t* status,
+                       cudaStream_t st) {
   if (n_site <= 0) return cudaSuccess;
   int blocks = (n_site + kKnnWarps - 1) / kKnnWarps;
   knn_kernel<<<blocks, kKnnWarps * 32, 0, st>>>(site4f, n_site, g, cell_start, cell_items, k,
-                                               w_max, order_by_id, nbr, keys, status);
+                                               w_max, order_by_id, nbr, keys, nbr_dist, status);
+  note_launches(1);
   return cudaGetLastError();
 }
 
@@ -431,12 +461,25 @@ __device__ __forceinline__ float pow_dist(float4 s, float3 v) {
 constexpr int kPairWarps = 4;
 
 __global__ void __launch_bounds__(kPairWarps * 32) pairs_kernel(PairParams p) {
+  __shared__ float4 spl[kPairWarps][kBoxPlanes];
   const int lane = threadIdx.x & 31;
+  const int wid = threadIdx.x >> 5;
   const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (i >= p.n_site) return;
   if (p.flags[i] != 1u) return;
   const float4 blo = p.site_box[2 * i], bhi = p.site_box[2 * i + 1];
   if (!(blo.x <= bhi.x && blo.y <= bhi.y && blo.z <= bhi.z)) return;
+  // planes of the site's grown cell, each loosened by its own float
+  // evaluation error so that the tests below never reject a centroid the
+  // exact planes accept
+  const int npl = p.site_nplanes[i];
+  float4* pl = spl[wid];
+  for (int q = lane; q < npl; q += 32) {
+    float4 e = p.site_planes[(long long)i * kBoxPlanes + q];
+    float tol = 4e-6f * ((fabsf(e.x) + fabsf(e.y) + fabsf(e.z)) * p.coord_scale + fabsf(e.w));
+    pl[q] = make_float4(e.x, e.y, e.z, e.w + tol);
+  }
+  __syncwarp();
   const float4 si = p.site4f[i];
   const Grid& g = p.tg;
   const int x0 = clampi((int)floorf((blo.x - g.lo.x) * g.inv_cell), 0, g.nx - 1);
@@ -448,16 +491,33 @@ __global__ void __launch_bounds__(kPairWarps * 32) pairs_kernel(PairParams p) {
   const int sx = x1 - x0 + 1, sy = y1 - y0 + 1, sz = z1 - z0 + 1;
   const int n_iter = sx * sy * sz;
   const int32_t* L = p.nbr + (long long)i * p.k;
+  // half extent of a grid cell, grown for the rounding of the binning
+  const float hc = 0.5f * g.cell * (1.0f + 1e-3f) + 1e-6f * p.coord_scale;
   auto cell_at = [&](int idx) -> int {
     int x = x0 + idx % sx, y = y0 + (idx / sx) % sy, z = z0 + idx / (sx * sy);
+    // reject cells lying entirely outside one plane of the grown cell
+    float cxm = g.lo.x + ((float)x + 0.5f) * g.cell;
+    float cym = g.lo.y + ((float)y + 0.5f) * g.cell;
+    float czm = g.lo.z + ((float)z + 0.5f) * g.cell;
+    for (int q = 0; q < npl; ++q) {
+      float4 e = pl[q];
+      float best = e.x * cxm + e.y * cym + e.z * czm + e.w +
+                   hc * (fabsf(e.x) + fabsf(e.y) + fabsf(e.z));
+      if (best < 0.f) return -1;
+    }
     return x + g.nx * (y + g.ny * z);
   };
   for_items(n_iter, cell_at, p.tcell_start, p.tcell_items, lane, [&](int t, bool valid) {
     bool pass = false;
     if (valid) {
       float4 c = p.centroid[t];
-      if (c.x >= blo.x && c.x <= bhi.x && c.y >= blo.y && c.y <= bhi.y && c.z >= blo.z &&
-          c.z <= bhi.z) {
+      bool in = c.x >= blo.x && c.x <= bhi.x && c.y >= blo.y && c.y <= bhi.y && c.z >= blo.z &&
+                c.z <= bhi.z;
+      for (int q = 0; q < npl && in; ++q) {
+        float4 e = pl[q];
+        in = e.x * c.x + e.y * c.y + e.z * c.z + e.w >= 0.f;
+      }
+      if (in) {
         int4 q = p.tets[t];
         float3 v[4];
         int id[4] = {q.x, q.y, q.z, q.w};
@@ -495,6 +555,7 @@ cudaError_t launch_pairs(const PairParams& p, cudaStream_t st) {
   if (p.n_site <= 0) return cudaSuccess;
   int blocks = (p.n_site + kPairWarps - 1) / kPairWarps;
   pairs_kernel<<<blocks, kPairWarps * 32, 0, st>>>(p);
+  note_launches(1);
   return cudaGetLastError();
 }
 
@@ -530,13 +591,17 @@ cudaError_t pairs_to_csr(const int2* pair_buf, long long n_pairs, int n_tet,
                          int32_t* pair_tet, int32_t* tet_k_out, cudaStream_t st) {
   cudaMemsetAsync(tet_fill, 0, sizeof(int32_t) * (size_t)n_tet, st);
   cudaMemsetAsync(tet_k_out, 0, sizeof(int32_t), st);
-  if (n_pairs > 0)
+  if (n_pairs > 0) {
     scatter_pairs_kernel<<<(int)((n_pairs + 255) / 256), 256, 0, st>>>(pair_buf, n_pairs,
                                                                       tet_offsets, tet_fill,
                                                                       pair_site);
-  if (n_tet > 0)
+    note_launches(1);
+  }
+  if (n_tet > 0) {
     sort_tet_pairs_kernel<<<(n_tet + 255) / 256, 256, 0, st>>>(n_tet, tet_offsets, pair_site,
                                                               pair_tet, tet_k_out);
+    note_launches(1);
+  }
   return cudaGetLastError();
 }
 
@@ -570,10 +635,14 @@ cudaError_t compact_cells(const rpd_cell_header* pair_headers, long long n_pairs
                           int32_t* pos_tmp, int32_t* scan_tmp, rpd_cell_header* out,
                           long long* n_out_dev, unsigned long long* status_hist, cudaStream_t st) {
   int nb = (int)((n_pairs + 255) / 256);
-  if (n_pairs > 0) flag_cells_kernel<<<nb, 256, 0, st>>>(pair_headers, n_pairs, flag_tmp, status_hist);
+  if (n_pairs > 0) {
+    flag_cells_kernel<<<nb, 256, 0, st>>>(pair_headers, n_pairs, flag_tmp, status_hist);
+    note_launches(1);
+  }
   cudaError_t err = scan_exclusive(flag_tmp, pos_tmp, n_pairs, scan_tmp, st);
   if (err != cudaSuccess) return err;
   gather_cells_kernel<<<nb > 0 ? nb : 1, 256, 0, st>>>(pair_headers, n_pairs, pos_tmp, out, n_out_dev);
+  note_launches(1);
   return cudaGetLastError();
 }
 
@@ -590,7 +659,10 @@ __global__ void ref_lists_kernel(const int32_t* ref, int k, int n_site, int32_t*
 cudaError_t neighbors_from_reference(const int32_t* ref, int k, int n_site, int32_t* nbr,
                                      cudaStream_t st) {
   long long n = (long long)n_site * k;
-  if (n > 0) ref_lists_kernel<<<(int)((n + 255) / 256), 256, 0, st>>>(ref, k, n_site, nbr);
+  if (n > 0) {
+    ref_lists_kernel<<<(int)((n + 255) / 256), 256, 0, st>>>(ref, k, n_site, nbr);
+    note_launches(1);
+  }
   return cudaGetLastError();
 }
 

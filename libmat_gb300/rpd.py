@@ -37,6 +37,7 @@ EXPORTS = [
     "rpd_destroy", "rpd_last_error", "rpd_set_mesh", "rpd_set_sites", "rpd_set_neighbors",
     "rpd_compute", "rpd_get_cells", "rpd_copy_cells_to_host", "rpd_copy_neighbors_to_host",
     "rpd_copy_pairs_to_host", "rpd_copy_pair_headers_to_host", "rpd_build_mesh_adjacency",
+    "rpd_host_alloc", "rpd_host_free",
 ]
 
 
@@ -55,7 +56,8 @@ class Stats(ctypes.Structure):
                 ("tet_k", ctypes.c_int32), ("knn_k", ctypes.c_int32),
                 ("ms_total", ctypes.c_float), ("ms_knn", ctypes.c_float),
                 ("ms_pairs", ctypes.c_float), ("ms_clip", ctypes.c_float),
-                ("ms_compact", ctypes.c_float)]
+                ("ms_compact", ctypes.c_float), ("ms_clip_kernel", ctypes.c_float),
+                ("n_launches", ctypes.c_int32)]
 
     def as_dict(self):
         d = {f: getattr(self, f) for f, _ in self._fields_ if f != "status_counts"}
@@ -111,6 +113,10 @@ def load(path=LIB_PATH):
     L.rpd_copy_pairs_to_host.argtypes = [vp, vp, vp, i64, c.POINTER(i64)]
     L.rpd_copy_pair_headers_to_host.restype = i32
     L.rpd_copy_pair_headers_to_host.argtypes = [vp, vp, i64, c.POINTER(i64)]
+    L.rpd_host_alloc.restype = vp
+    L.rpd_host_alloc.argtypes = [c.c_size_t]
+    L.rpd_host_free.restype = None
+    L.rpd_host_free.argtypes = [vp]
     L.rpd_build_mesh_adjacency.restype = i32
     L.rpd_build_mesh_adjacency.argtypes = [i32, vp, i32, vp, vp, vp, vp, vp]
     _lib = L
@@ -264,3 +270,29 @@ class RPD:
         self._check(self._L.rpd_copy_pairs_to_host(self._h, _p(offs), _p(sites), sites.size,
                                                    ctypes.byref(n)))
         return offs, sites[:n.value]
+
+
+class PinnedArray:
+    """A numpy array in page-locked host memory (rpd_host_alloc)."""
+
+    def __init__(self, shape, dtype):
+        self._L = load()
+        dt = np.dtype(dtype)
+        n = int(np.prod(shape)) * dt.itemsize
+        self._ptr = self._L.rpd_host_alloc(max(n, 1))
+        if not self._ptr:
+            raise MemoryError("rpd_host_alloc(%d) failed" % n)
+        buf = (ctypes.c_uint8 * max(n, 1)).from_address(self._ptr)
+        self.array = np.frombuffer(buf, dtype=dt, count=int(np.prod(shape))).reshape(shape)
+
+    def free(self):
+        if self._ptr:
+            self.array = None
+            self._L.rpd_host_free(self._ptr)
+            self._ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass

@@ -180,12 +180,8 @@ typedef struct {
   int32_t id;
 } kv;
 
-static int cmp_kv(const void* x, const void* y) {
-  const kv* p = (const kv*)x;
-  const kv* q = (const kv*)y;
-  if (p->key < q->key) return -1;
-  if (p->key > q->key) return 1;
-  return p->id < q->id ? -1 : (p->id > q->id);
+static int kv_less(float ka, int32_t ia, float kb, int32_t ib) {
+  return ka < kb || (ka == kb && ia < ib);
 }
 
 void orc_knn(int n_site, const float* site4, int k, int32_t* nbr, float* keys,
@@ -195,25 +191,32 @@ void orc_knn(int n_site, const float* site4, int k, int32_t* nbr, float* keys,
 #pragma omp parallel
 #endif
   {
-    kv* buf = (kv*)malloc(sizeof(kv) * (size_t)(n_site > 0 ? n_site : 1));
+    kv* best = (kv*)malloc(sizeof(kv) * (size_t)(k > 0 ? k : 1));
 #ifdef _OPENMP
 #pragma omp for schedule(dynamic, 64)
 #endif
     for (int i = 0; i < n_site; ++i) {
+      /* the k smallest (key, id) kept sorted by insertion */
       int m = 0;
       for (int j = 0; j < n_site; ++j) {
         if (j == i) continue;
-        buf[m].key = orc_bisector_key(site4 + 4 * (int64_t)i, site4 + 4 * (int64_t)j);
-        buf[m].id = j;
-        ++m;
+        float key = orc_bisector_key(site4 + 4 * (int64_t)i, site4 + 4 * (int64_t)j);
+        if (m == k && !kv_less(key, j, best[k - 1].key, best[k - 1].id)) continue;
+        int pos = m < k ? m : k - 1;
+        while (pos > 0 && kv_less(key, j, best[pos - 1].key, best[pos - 1].id)) {
+          best[pos] = best[pos - 1];
+          --pos;
+        }
+        best[pos].key = key;
+        best[pos].id = j;
+        if (m < k) ++m;
       }
-      qsort(buf, (size_t)m, sizeof(kv), cmp_kv);
       for (int r = 0; r < k; ++r) {
-        nbr[(int64_t)i * k + r] = r < m ? buf[r].id : -1;
-        if (keys) keys[(int64_t)i * k + r] = r < m ? buf[r].key : INFINITY;
+        nbr[(int64_t)i * k + r] = r < m ? best[r].id : -1;
+        if (keys) keys[(int64_t)i * k + r] = r < m ? best[r].key : INFINITY;
       }
     }
-    free(buf);
+    free(best);
   }
 }
 
@@ -358,27 +361,23 @@ static void minor3(float a1, float b1, float c1, float a2, float b2, float c2,
   *perm = fmaf(fabsf(a1), v1, fmaf(fabsf(b1), v2, fabsf(c1) * v3));
 }
 
-/* cofactors K[4] and the largest 3x3 permanent M of the vertex (p1,p2,p3) */
+/* cofactors K[4] of the vertex (p1,p2,p3) and the matching 3x3 permanents
+ * M[4] */
 static void vertex_cofactors(const float* p1, const float* p2, const float* p3,
                              float* K, float* M) {
-  float d, pm, mx = 0.0f;
+  float d;
   /* rows y z w */
-  minor3(p1[1], p1[2], p1[3], p2[1], p2[2], p2[3], p3[1], p3[2], p3[3], &d, &pm);
+  minor3(p1[1], p1[2], p1[3], p2[1], p2[2], p2[3], p3[1], p3[2], p3[3], &d, &M[0]);
   K[0] = -d;
-  mx = fmaxf(mx, pm);
   /* rows x z w */
-  minor3(p1[0], p1[2], p1[3], p2[0], p2[2], p2[3], p3[0], p3[2], p3[3], &d, &pm);
+  minor3(p1[0], p1[2], p1[3], p2[0], p2[2], p2[3], p3[0], p3[2], p3[3], &d, &M[1]);
   K[1] = d;
-  mx = fmaxf(mx, pm);
   /* rows x y w */
-  minor3(p1[0], p1[1], p1[3], p2[0], p2[1], p2[3], p3[0], p3[1], p3[3], &d, &pm);
+  minor3(p1[0], p1[1], p1[3], p2[0], p2[1], p2[3], p3[0], p3[1], p3[3], &d, &M[2]);
   K[2] = -d;
-  mx = fmaxf(mx, pm);
   /* rows x y z */
-  minor3(p1[0], p1[1], p1[2], p2[0], p2[1], p2[2], p3[0], p3[1], p3[2], &d, &pm);
+  minor3(p1[0], p1[1], p1[2], p2[0], p2[1], p2[2], p3[0], p3[1], p3[2], &d, &M[3]);
   K[3] = d;
-  mx = fmaxf(mx, pm);
-  *M = mx;
 }
 
 /* filter constants: 5u for the dot, 6u for the cofactor and FP64 terms,
@@ -387,13 +386,15 @@ static void vertex_cofactors(const float* p1, const float* p2, const float* p3,
 #define FILT_C2 (6.0f * 5.9604645e-08f)
 #define FILT_ABS 1e-30f
 
-static int filter_sign_k(const float* K, float M, const float* e) {
+/* bound: c1 sum|e_r K_r| + c2 sum|e_r| M_r (the 4x4 permanent) */
+static int filter_sign_k(const float* K, const float* M, const float* e) {
   float s = fmaf(e[3], K[3], fmaf(e[2], K[2], fmaf(e[1], K[1], e[0] * K[0])));
   float t = fmaf(fabsf(e[3]), fabsf(K[3]),
                  fmaf(fabsf(e[2]), fabsf(K[2]),
                       fmaf(fabsf(e[1]), fabsf(K[1]), fabsf(e[0]) * fabsf(K[0]))));
-  float se = (fabsf(e[0]) + fabsf(e[1])) + (fabsf(e[2]) + fabsf(e[3]));
-  float b = fmaf(FILT_C1, t, FILT_C2 * (M * se)) + FILT_ABS;
+  float pm = fmaf(fabsf(e[3]), M[3],
+                  fmaf(fabsf(e[2]), M[2], fmaf(fabsf(e[1]), M[1], fabsf(e[0]) * M[0])));
+  float b = fmaf(FILT_C1, t, FILT_C2 * pm) + FILT_ABS;
   if (s > b) return 1;
   if (s < -b) return -1;
   return 0;
@@ -401,8 +402,8 @@ static int filter_sign_k(const float* K, float M, const float* e) {
 
 int orc_filter_sign(const float* p1, const float* p2, const float* p3,
                     const float* e) {
-  float K[4], M;
-  vertex_cofactors(p1, p2, p3, K, &M);
+  float K[4], M[4];
+  vertex_cofactors(p1, p2, p3, K, M);
   return filter_sign_k(K, M, e);
 }
 
