@@ -109,6 +109,10 @@ typedef struct rpd_stats {
   float ms_knn, ms_pairs, ms_clip, ms_compact;
   float ms_clip_kernel;       /* the clip kernel alone (events around it) */
   int32_t n_launches;         /* kernels launched by this rpd_compute */
+  /* candidate search counters: [0] grid cells scanned, [1] cells kept after
+   * the grown-cell planes, [2] tets enumerated, [3] tets inside the grown
+   * cell (rule evaluated), [4] pairs, [5] site boxes without planes */
+  int64_t search[6];
 } rpd_stats;
 
 typedef struct rpd_cells_view {

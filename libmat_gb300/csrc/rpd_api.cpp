@@ -95,7 +95,7 @@ struct rpd_ctx {
   DevBuf<int32_t> s_cell_of, s_cell_count, s_cell_start, s_cell_fill, s_cell_items;
   DevBuf<int32_t> t_cell_of, t_cell_count, t_cell_start, t_cell_fill, t_cell_items;
   DevBuf<float4> centroid, site_box, site_planes;
-  DevBuf<int32_t> site_nplanes;
+  DevBuf<int32_t> site_nplanes, pair_ntasks, pair_taskoff;
   DevBuf<int32_t> scan_tmp;
 
   // pairs
@@ -244,7 +244,7 @@ void rpd_destroy(rpd_ctx* c) {
   c->t_cell_of.release(); c->t_cell_count.release(); c->t_cell_start.release();
   c->t_cell_fill.release(); c->t_cell_items.release();
   c->centroid.release(); c->site_box.release(); c->site_planes.release();
-  c->site_nplanes.release(); c->scan_tmp.release();
+  c->site_nplanes.release(); c->pair_ntasks.release(); c->pair_taskoff.release(); c->scan_tmp.release();
   c->pair_buf.release(); c->tet_count.release(); c->tet_offsets.release();
   c->tet_fill.release(); c->pair_site.release(); c->pair_tet.release();
   c->pair_headers.release(); c->cells.release(); c->payload.release();
@@ -295,21 +295,17 @@ rpd_status rpd_set_mesh(rpd_ctx* c, const double* xyz, int n_vert, const int32_t
     rad[t] = r;
     rmax = std::max(rmax, r);
   }
-  // radius classes: class 0 up to 1.5 x the median radius, then doubling
+  // two radius classes: up to the 99.5th percentile radius, and the rest
   std::vector<uint8_t> cls((size_t)n_tet);
   int ccount[rpd_ctx::kClasses] = {0};
   double crad[rpd_ctx::kClasses] = {0};
   {
     std::vector<double> tmp(rad);
-    std::nth_element(tmp.begin(), tmp.begin() + tmp.size() / 2, tmp.end());
-    double r0 = std::max(1.5 * tmp[tmp.size() / 2], 1e-300);
+    size_t q = std::min(tmp.size() - 1, (size_t)(0.995 * (double)tmp.size()));
+    std::nth_element(tmp.begin(), tmp.begin() + q, tmp.end());
+    double r0 = tmp[q];
     for (long long t = 0; t < n_tet; ++t) {
-      int k = 0;
-      double lim = r0;
-      while (rad[t] > lim && k < rpd_ctx::kClasses - 1) {
-        lim *= 2.0;
-        ++k;
-      }
+      int k = rad[t] <= r0 ? 0 : 1;
       cls[t] = (uint8_t)k;
       ccount[k]++;
       crad[k] = std::max(crad[k], rad[t]);
@@ -489,6 +485,7 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
       CK(c->pair_buf.ensure((size_t)cap), "alloc pairs");
       CK(cudaMemsetAsync(c->tet_count.ptr, 0, sizeof(int32_t) * (size_t)n_tet, st), "memset");
       CK(cudaMemsetAsync(c->scratch.ptr + 4, 0, sizeof(unsigned long long), st), "memset");
+      CK(cudaMemsetAsync(c->scratch.ptr + 20, 0, 6 * sizeof(unsigned long long), st), "memset");
       for (int cl = 0; cl < rpd_ctx::kClasses; ++cl) {
         if (c->class_count[cl] == 0) continue;
         Grid tg = make_grid(c->mesh_lo, c->mesh_hi, c->class_count[cl], 4.0);
@@ -545,7 +542,12 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
         pp.pair_cursor = c->scratch.ptr + 4;
         pp.pair_cap = (long long)c->pair_buf.cap;
         pp.tet_count = c->tet_count.ptr;
-        CK(launch_pairs(pp, st), "pairs");
+        pp.diag = c->scratch.ptr + 20;
+        CK(c->pair_ntasks.ensure((size_t)n_site), "alloc");
+        CK(c->pair_taskoff.ensure((size_t)n_site + 1), "alloc");
+        CK(c->scan_tmp.ensure(scan_temp_ints(std::max<long long>(std::max<long long>(nc, n_tet), n_site)) + 16), "alloc");
+        CK(launch_pairs(pp, c->pair_ntasks.ptr, c->pair_taskoff.ptr, c->scan_tmp.ptr,
+                        c->scratch.ptr + 27, c->num_sms, st), "pairs");
       }
       unsigned long long np = 0;
       CK(cudaMemcpyAsync(&np, c->scratch.ptr + 4, sizeof(np), cudaMemcpyDeviceToHost, st), "D2H");
@@ -650,6 +652,8 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
     cudaEventElapsedTime(&stats->ms_compact, c->ev[kEvClip], c->ev[kEvEnd]);
     cudaEventElapsedTime(&stats->ms_clip_kernel, c->ev[kEvClipK0], c->ev[kEvClipK1]);
     stats->n_launches = take_launches();
+    for (int i = 0; i < 6; ++i) stats->search[i] = (int64_t)host_scratch[20 + i];
+    stats->search[4] = c->n_pairs;
   }
   return RPD_OK;
 }

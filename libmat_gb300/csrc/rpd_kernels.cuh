@@ -124,8 +124,12 @@ struct PairParams {
   unsigned long long* pair_cursor;
   long long pair_cap;
   int32_t* tet_count;
+  unsigned long long* diag;  // search counters (see rpd_stats::search)
 };
-cudaError_t launch_pairs(const PairParams& p, cudaStream_t st);
+// n_tasks, task_off: n_site and n_site + 1 ints; work: one counter
+cudaError_t launch_pairs(const PairParams& p, int32_t* n_tasks, int32_t* task_off,
+                         int32_t* scan_tmp, unsigned long long* work, int num_sms,
+                         cudaStream_t st);
 
 // scatter the pair buffer into per-tet CSR and sort sites in each tet
 cudaError_t pairs_to_csr(const int2* pair_buf, long long n_pairs, int n_tet,

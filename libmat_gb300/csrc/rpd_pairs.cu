@@ -460,101 +460,174 @@ __device__ __forceinline__ float pow_dist(float4 s, float3 v) {
 
 constexpr int kPairWarps = 4;
 
-__global__ void __launch_bounds__(kPairWarps * 32) pairs_kernel(PairParams p) {
+// cell range of the site's box in the tet grid (empty range for no box)
+struct CellRange {
+  int x0, y0, z0, sx, sy, sz;
+};
+
+__device__ __forceinline__ CellRange site_cells(const PairParams& p, int i) {
+  CellRange r = {0, 0, 0, 0, 0, 0};
+  if (p.flags[i] != 1u) return r;
+  const float4 blo = p.site_box[2 * i], bhi = p.site_box[2 * i + 1];
+  if (!(blo.x <= bhi.x && blo.y <= bhi.y && blo.z <= bhi.z)) return r;
+  const Grid& g = p.tg;
+  r.x0 = clampi((int)floorf((blo.x - g.lo.x) * g.inv_cell), 0, g.nx - 1);
+  r.y0 = clampi((int)floorf((blo.y - g.lo.y) * g.inv_cell), 0, g.ny - 1);
+  r.z0 = clampi((int)floorf((blo.z - g.lo.z) * g.inv_cell), 0, g.nz - 1);
+  int x1 = clampi((int)floorf((bhi.x - g.lo.x) * g.inv_cell), 0, g.nx - 1);
+  int y1 = clampi((int)floorf((bhi.y - g.lo.y) * g.inv_cell), 0, g.ny - 1);
+  int z1 = clampi((int)floorf((bhi.z - g.lo.z) * g.inv_cell), 0, g.nz - 1);
+  r.sx = x1 - r.x0 + 1;
+  r.sy = y1 - r.y0 + 1;
+  r.sz = z1 - r.z0 + 1;
+  return r;
+}
+
+constexpr int kPairTaskCells = 512;
+
+// tasks per site: its box's grid cells in chunks of kPairTaskCells
+__global__ void pair_tasks_kernel(PairParams p, int32_t* n_tasks) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n_site) return;
+  CellRange r = site_cells(p, i);
+  long long n = (long long)r.sx * r.sy * r.sz;
+  n_tasks[i] = (int)((n + kPairTaskCells - 1) / kPairTaskCells);
+}
+
+// Persistent warps take (site, chunk of its box's cells) tasks from a work
+// counter, so a site with a large box is spread over many warps.
+__global__ void __launch_bounds__(kPairWarps * 32) pairs_kernel(PairParams p,
+                                                                const int32_t* task_off,
+                                                                unsigned long long* work) {
   __shared__ float4 spl[kPairWarps][kBoxPlanes];
   const int lane = threadIdx.x & 31;
   const int wid = threadIdx.x >> 5;
-  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (i >= p.n_site) return;
-  if (p.flags[i] != 1u) return;
-  const float4 blo = p.site_box[2 * i], bhi = p.site_box[2 * i + 1];
-  if (!(blo.x <= bhi.x && blo.y <= bhi.y && blo.z <= bhi.z)) return;
-  // planes of the site's grown cell, each loosened by its own float
-  // evaluation error so that the tests below never reject a centroid the
-  // exact planes accept
-  const int npl = p.site_nplanes[i];
-  float4* pl = spl[wid];
-  for (int q = lane; q < npl; q += 32) {
-    float4 e = p.site_planes[(long long)i * kBoxPlanes + q];
-    float tol = 4e-6f * ((fabsf(e.x) + fabsf(e.y) + fabsf(e.z)) * p.coord_scale + fabsf(e.w));
-    pl[q] = make_float4(e.x, e.y, e.z, e.w + tol);
-  }
-  __syncwarp();
-  const float4 si = p.site4f[i];
-  const Grid& g = p.tg;
-  const int x0 = clampi((int)floorf((blo.x - g.lo.x) * g.inv_cell), 0, g.nx - 1);
-  const int y0 = clampi((int)floorf((blo.y - g.lo.y) * g.inv_cell), 0, g.ny - 1);
-  const int z0 = clampi((int)floorf((blo.z - g.lo.z) * g.inv_cell), 0, g.nz - 1);
-  const int x1 = clampi((int)floorf((bhi.x - g.lo.x) * g.inv_cell), 0, g.nx - 1);
-  const int y1 = clampi((int)floorf((bhi.y - g.lo.y) * g.inv_cell), 0, g.ny - 1);
-  const int z1 = clampi((int)floorf((bhi.z - g.lo.z) * g.inv_cell), 0, g.nz - 1);
-  const int sx = x1 - x0 + 1, sy = y1 - y0 + 1, sz = z1 - z0 + 1;
-  const int n_iter = sx * sy * sz;
-  const int32_t* L = p.nbr + (long long)i * p.k;
-  // half extent of a grid cell, grown for the rounding of the binning
-  const float hc = 0.5f * g.cell * (1.0f + 1e-3f) + 1e-6f * p.coord_scale;
-  auto cell_at = [&](int idx) -> int {
-    int x = x0 + idx % sx, y = y0 + (idx / sx) % sy, z = z0 + idx / (sx * sy);
-    // reject cells lying entirely outside one plane of the grown cell
-    float cxm = g.lo.x + ((float)x + 0.5f) * g.cell;
-    float cym = g.lo.y + ((float)y + 0.5f) * g.cell;
-    float czm = g.lo.z + ((float)z + 0.5f) * g.cell;
-    for (int q = 0; q < npl; ++q) {
-      float4 e = pl[q];
-      float best = e.x * cxm + e.y * cym + e.z * czm + e.w +
-                   hc * (fabsf(e.x) + fabsf(e.y) + fabsf(e.z));
-      if (best < 0.f) return -1;
+  const long long n_tasks = task_off[p.n_site];
+  unsigned int n_cells_seen = 0, n_keep = 0, n_items = 0, n_in = 0;
+  for (;;) {
+    long long task = 0;
+    if (lane == 0) task = (long long)atomicAdd(work, 1ull);
+    task = __shfl_sync(0xffffffffu, task, 0);
+    if (task >= n_tasks) break;
+    // owning site: last i with task_off[i] <= task
+    int lo = 0, hi = p.n_site - 1;
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (task_off[mid] <= task) lo = mid;
+      else hi = mid - 1;
     }
-    return x + g.nx * (y + g.ny * z);
-  };
-  for_items(n_iter, cell_at, p.tcell_start, p.tcell_items, lane, [&](int t, bool valid) {
-    bool pass = false;
-    if (valid) {
-      float4 c = p.centroid[t];
-      bool in = c.x >= blo.x && c.x <= bhi.x && c.y >= blo.y && c.y <= bhi.y && c.z >= blo.z &&
-                c.z <= bhi.z;
-      for (int q = 0; q < npl && in; ++q) {
+    const int i = lo;
+    const int chunk = (int)(task - task_off[i]);
+    const CellRange cr = site_cells(p, i);
+    const int n_all = cr.sx * cr.sy * cr.sz;
+    const int c_begin = chunk * kPairTaskCells;
+    const int n_iter = min(kPairTaskCells, n_all - c_begin);
+    const float4 blo = p.site_box[2 * i], bhi = p.site_box[2 * i + 1];
+    // planes of the site's grown cell, each loosened by its own float
+    // evaluation error so that the tests below never reject a centroid the
+    // exact planes accept
+    const int npl = p.site_nplanes[i];
+    float4* pl = spl[wid];
+    __syncwarp();
+    for (int q = lane; q < npl; q += 32) {
+      float4 e = p.site_planes[(long long)i * kBoxPlanes + q];
+      float tol = 4e-6f * ((fabsf(e.x) + fabsf(e.y) + fabsf(e.z)) * p.coord_scale + fabsf(e.w));
+      pl[q] = make_float4(e.x, e.y, e.z, e.w + tol);
+    }
+    __syncwarp();
+    const float4 si = p.site4f[i];
+    const Grid& g = p.tg;
+    const int32_t* L = p.nbr + (long long)i * p.k;
+    n_cells_seen += n_iter;
+    // half extent of a grid cell, grown for the rounding of the binning
+    const float hc = 0.5f * g.cell * (1.0f + 1e-3f) + 1e-6f * p.coord_scale;
+    auto cell_at = [&](int idx) -> int {
+      idx += c_begin;
+      int x = cr.x0 + idx % cr.sx, y = cr.y0 + (idx / cr.sx) % cr.sy, z = cr.z0 + idx / (cr.sx * cr.sy);
+      // reject cells lying entirely outside one plane of the grown cell
+      float cxm = g.lo.x + ((float)x + 0.5f) * g.cell;
+      float cym = g.lo.y + ((float)y + 0.5f) * g.cell;
+      float czm = g.lo.z + ((float)z + 0.5f) * g.cell;
+      for (int q = 0; q < npl; ++q) {
         float4 e = pl[q];
-        in = e.x * c.x + e.y * c.y + e.z * c.z + e.w >= 0.f;
+        float best = e.x * cxm + e.y * cym + e.z * czm + e.w +
+                     hc * (fabsf(e.x) + fabsf(e.y) + fabsf(e.z));
+        if (best < 0.f) return -1;
       }
-      if (in) {
-        int4 q = p.tets[t];
-        float3 v[4];
-        int id[4] = {q.x, q.y, q.z, q.w};
-        float pdi[4];
-        for (int a = 0; a < 4; ++a) {
-          v[a] = make_float3(p.vert3f[3 * id[a]], p.vert3f[3 * id[a] + 1], p.vert3f[3 * id[a] + 2]);
-          pdi[a] = pow_dist(si, v[a]);
+      ++n_keep;
+      return x + g.nx * (y + g.ny * z);
+    };
+    for_items(n_iter, cell_at, p.tcell_start, p.tcell_items, lane, [&](int t, bool valid) {
+      bool pass = false;
+      if (valid) {
+        ++n_items;
+        float4 c = p.centroid[t];
+        bool in = c.x >= blo.x && c.x <= bhi.x && c.y >= blo.y && c.y <= bhi.y &&
+                  c.z >= blo.z && c.z <= bhi.z;
+        for (int q = 0; q < npl && in; ++q) {
+          float4 e = pl[q];
+          in = e.x * c.x + e.y * c.y + e.z * c.z + e.w >= 0.f;
         }
-        pass = true;
-        for (int r = 0; r < p.k && pass; ++r) {
-          int m = __ldg(L + r);
-          if (m == -1) continue;  // voronoi.cu:171 skips holes
-          float4 sm = __ldg(p.site4f + m);
-          bool hit = false;
-          for (int a = 0; a < 4; ++a) hit |= pow_dist(sm, v[a]) > pdi[a];
-          pass = hit;
+        if (in) {
+          ++n_in;
+          int4 q = p.tets[t];
+          float3 v[4];
+          int id[4] = {q.x, q.y, q.z, q.w};
+          float pdi[4];
+          for (int a = 0; a < 4; ++a) {
+            v[a] = make_float3(p.vert3f[3 * id[a]], p.vert3f[3 * id[a] + 1],
+                               p.vert3f[3 * id[a] + 2]);
+            pdi[a] = pow_dist(si, v[a]);
+          }
+          pass = true;
+          for (int r = 0; r < p.k && pass; ++r) {
+            int m = __ldg(L + r);
+            if (m == -1) continue;  // voronoi.cu:171 skips holes
+            float4 sm = __ldg(p.site4f + m);
+            bool hit = false;
+            for (int a = 0; a < 4; ++a) hit |= pow_dist(sm, v[a]) > pdi[a];
+            pass = hit;
+          }
         }
       }
-    }
-    uint32_t msk = __ballot_sync(0xffffffffu, pass);
-    if (msk) {
-      unsigned long long base = 0;
-      if (lane == 0) base = atomicAdd(p.pair_cursor, (unsigned long long)__popc(msk));
-      base = __shfl_sync(0xffffffffu, base, 0);
-      if (pass) {
-        unsigned long long slot = base + __popc(msk & ((1u << lane) - 1u));
-        if ((long long)slot < p.pair_cap) p.pair_buf[slot] = make_int2(t, i);
-        atomicAdd(p.tet_count + t, 1);
+      uint32_t msk = __ballot_sync(0xffffffffu, pass);
+      if (msk) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(p.pair_cursor, (unsigned long long)__popc(msk));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (pass) {
+          unsigned long long slot = base + __popc(msk & ((1u << lane) - 1u));
+          if ((long long)slot < p.pair_cap) p.pair_buf[slot] = make_int2(t, i);
+          atomicAdd(p.tet_count + t, 1);
+        }
       }
+    });
+  }
+  if (p.diag) {
+    n_keep = __reduce_add_sync(0xffffffffu, n_keep);
+    n_items = __reduce_add_sync(0xffffffffu, n_items);
+    n_in = __reduce_add_sync(0xffffffffu, n_in);
+    if (lane == 0) {
+      atomicAdd(p.diag + 0, (unsigned long long)n_cells_seen);
+      atomicAdd(p.diag + 1, (unsigned long long)n_keep);
+      atomicAdd(p.diag + 2, (unsigned long long)n_items);
+      atomicAdd(p.diag + 3, (unsigned long long)n_in);
     }
-  });
+  }
 }
 
-cudaError_t launch_pairs(const PairParams& p, cudaStream_t st) {
+cudaError_t launch_pairs(const PairParams& p, int32_t* n_tasks, int32_t* task_off,
+                         int32_t* scan_tmp, unsigned long long* work, int num_sms,
+                         cudaStream_t st) {
   if (p.n_site <= 0) return cudaSuccess;
-  int blocks = (p.n_site + kPairWarps - 1) / kPairWarps;
-  pairs_kernel<<<blocks, kPairWarps * 32, 0, st>>>(p);
+  pair_tasks_kernel<<<(p.n_site + 255) / 256, 256, 0, st>>>(p, n_tasks);
+  note_launches(1);
+  cudaError_t err = scan_exclusive(n_tasks, task_off, p.n_site, scan_tmp, st);
+  if (err != cudaSuccess) return err;
+  cudaMemsetAsync(work, 0, sizeof(unsigned long long), st);
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pairs_kernel, kPairWarps * 32, 0);
+  pairs_kernel<<<num_sms * (per_sm > 0 ? per_sm : 1), kPairWarps * 32, 0, st>>>(p, task_off, work);
   note_launches(1);
   return cudaGetLastError();
 }

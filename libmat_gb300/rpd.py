@@ -57,10 +57,11 @@ class Stats(ctypes.Structure):
                 ("ms_total", ctypes.c_float), ("ms_knn", ctypes.c_float),
                 ("ms_pairs", ctypes.c_float), ("ms_clip", ctypes.c_float),
                 ("ms_compact", ctypes.c_float), ("ms_clip_kernel", ctypes.c_float),
-                ("n_launches", ctypes.c_int32)]
+                ("n_launches", ctypes.c_int32), ("search", ctypes.c_int64 * 6)]
 
     def as_dict(self):
-        d = {f: getattr(self, f) for f, _ in self._fields_ if f != "status_counts"}
+        d = {f: getattr(self, f) for f, _ in self._fields_ if f not in ("status_counts", "search")}
+        d["search"] = [int(x) for x in self.search]
         d["status_counts"] = {STATUS_NAMES[i]: int(self.status_counts[i]) for i in range(10)}
         return d
 
