@@ -184,6 +184,26 @@ rpd_status rpd_copy_pairs_to_host(struct rpd_ctx* ctx, int32_t* tet_offsets,
                                   int32_t* pair_sites, int64_t capacity,
                                   int64_t* n_pairs);
 
+/* Compaction of a pair-header array without allocating device memory.
+ * No counterpart in the reference: it exists for callers that cannot call
+ * cudaMalloc during their run (work recorded into a stream they do not own,
+ * applications whose memory pool owns all device memory, code where an
+ * allocation would synchronise the device).  It performs the compaction
+ * step of rpd_compute: cells_out receives the records of pair_headers whose
+ * status is success, in pair order, *n_cells_out their count, and
+ * status_counts (optional, 11 entries: statuses 0..8, other, payload full)
+ * the status histogram; all pointers are device pointers the caller owns,
+ * cells_out holding n_pairs records.  Its only temporary lives in a fixed
+ * array inside the library (reserved on each GPU that loads it until exit),
+ * so n_pairs is limited to 2^25; larger inputs return RPD_ERR_CAPACITY.  The
+ * first call on a device looks up that array's address (call it once before
+ * any stream capture).  Calls share the array: calls that overlap on the GPU
+ * race and must be serialised by the caller.  Asynchronous on `stream`
+ * (a cudaStream_t, NULL = default stream). */
+rpd_status rpd_compact_cells_noalloc(const rpd_cell_header* pair_headers, int64_t n_pairs,
+                                     rpd_cell_header* cells_out, int64_t* n_cells_out,
+                                     uint64_t* status_counts, void* stream);
+
 /* Page-locked host buffers for fast host<->device copies (cudaMallocHost);
  * NULL on failure. */
 void* rpd_host_alloc(size_t bytes);

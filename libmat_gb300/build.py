@@ -25,6 +25,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2",
 CUDA_UNITS = {
     "rpd_clip.cu": ["-fmad=false"],
     "rpd_pairs.cu": ["-fmad=false"],
+    "rpd_noalloc.cu": [],
 }
 CXX_UNITS = ["rpd_api.cpp", "rpd_mesh.cpp"]
 

@@ -37,7 +37,7 @@ EXPORTS = [
     "rpd_destroy", "rpd_last_error", "rpd_set_mesh", "rpd_set_sites", "rpd_set_neighbors",
     "rpd_compute", "rpd_get_cells", "rpd_copy_cells_to_host", "rpd_copy_neighbors_to_host",
     "rpd_copy_pairs_to_host", "rpd_copy_pair_headers_to_host", "rpd_build_mesh_adjacency",
-    "rpd_host_alloc", "rpd_host_free",
+    "rpd_host_alloc", "rpd_host_free", "rpd_compact_cells_noalloc",
 ]
 
 
@@ -114,6 +114,8 @@ def load(path=LIB_PATH):
     L.rpd_copy_pairs_to_host.argtypes = [vp, vp, vp, i64, c.POINTER(i64)]
     L.rpd_copy_pair_headers_to_host.restype = i32
     L.rpd_copy_pair_headers_to_host.argtypes = [vp, vp, i64, c.POINTER(i64)]
+    L.rpd_compact_cells_noalloc.restype = i32
+    L.rpd_compact_cells_noalloc.argtypes = [vp, i64, vp, vp, vp, vp]
     L.rpd_host_alloc.restype = vp
     L.rpd_host_alloc.argtypes = [c.c_size_t]
     L.rpd_host_free.restype = None
