@@ -272,11 +272,15 @@ def run_ours(args):
     peak, peak_src = load_peaks()
     alg = clip_algorithmic_bytes(cfg, st.n_pairs, st.knn_k, st.payload_bytes)
     achieved = alg / (st.ms_clip_kernel / 1000.0) / 1e9
+    # DRAM bytes of one clip launch, from the ncu capture summarised in
+    # profiles/ (per pair on a smaller case of the same workload family,
+    # scaled by this launch's pairs: traffic grows with the pairs)
     traffic = None
-    tfile = os.path.join(ROOT, "profiles", "clip_traffic.json")
+    tfile = os.path.join(ROOT, "profiles", "clip_cells_kernel_ellipsoid_200k.md")
     if os.path.exists(tfile):
-        tj = json.load(open(tfile))
-        traffic = tj.get("bytes_per_pair", 0) * st.n_pairs or None
+        for ln in open(tfile):
+            if ln.startswith("traffic_bytes_per_pair:"):
+                traffic = float(ln.split(":")[1]) * st.n_pairs
 
     cpu = None
     if rank == 0 and not args.no_cpu:
