@@ -217,9 +217,10 @@ def run_ours(args):
     adj = rpd.mesh_adjacency(cfg["vert3d"].shape[0], cfg["tets"])
     nt, nv, ns = cfg["tets"].shape[0], cfg["vert3d"].shape[0], cfg["sites"].shape[0]
 
-    def engine(pred):
+    def engine(pred, certify):
         r = rpd.RPD(device=local if world > 1 else 0, predicate_mode=pred,
-                    neighbor_source=rpd.NEIGH_KNN, knn_k=args.k, clip_order=rpd.ORDER_SITE_ID)
+                    neighbor_source=rpd.NEIGH_KNN, knn_k=args.k, clip_order=rpd.ORDER_SITE_ID,
+                    certify=certify)
         r.set_mesh(cfg["vert3d"], cfg["tets"], adj["v_adjs"], adj["e_adj6"], adj["f_adjs"],
                    adj["f_ids"])
         r.set_sites(cfg["sites"], cfg["flags"])
@@ -238,8 +239,9 @@ def run_ours(args):
             st_last = st
         return ms, cells, st_last
 
-    # ---- fast path (the metric)
-    fast = engine(rpd.PRED_FP32_FILTER)
+    # ---- fast path (the metric): FP32-filter predicates, neighbours in
+    # ascending bisector distance, stop at the security-radius certificate
+    fast = engine(rpd.PRED_FP32_FILTER, True)
     barrier()
     with ClockSampler(local) as clk:
         ms, cells, st = timed(fast, args.steps, args.warmup)
@@ -252,18 +254,26 @@ def run_ours(args):
         total_ms = float(t.item())
     value = cells * world / (total_ms / 1000.0)
     fast_ph = fast.pair_headers()
+    fast_hash = fast.topology_hashes()
     fast_h, fast_p = fast.cells()
 
-    # ---- plain FP64 path
-    plain = engine(rpd.PRED_FP64)
+    # ---- plain FP64 path: whole list in site-id order, FP64 determinant on
+    # every predicate
+    plain = engine(rpd.PRED_FP64, False)
     pms, pcells, pst = timed(plain, max(1, args.steps // 2), 1)
     plain_value = pcells / (sum(pms) / 1000.0)
     plain_ph = plain.pair_headers()
+    plain_hash = plain.topology_hashes()
     plain_h, plain_p = plain.cells()
     plain.close()
+    # exact topology: same pairs, statuses and canonical topology of every
+    # cell (the certified path's records list fewer dead planes, so the raw
+    # bytes differ; the vertices' face-key triples do not)
     same_headers = all(np.array_equal(fast_ph[f], plain_ph[f])
-                       for f in ("tet_id", "site_id", "status", "nb_v", "nb_p", "nb_e"))
-    topo_ok = same_headers and _sample_topology_equal(fast_ph, fast_p, plain_ph, plain_p)
+                       for f in ("tet_id", "site_id", "status"))
+    n_topo_diff = int((fast_hash != plain_hash).sum())
+    topo_ok = same_headers and n_topo_diff == 0
+    geo = _geometry_error(fast_ph, fast_p, plain_ph, plain_p)
 
     # ---- end to end through the C ABI with host buffers
     e2e = _e2e(args, cfg, adj, rpd)
@@ -302,13 +312,16 @@ def run_ours(args):
         "config": {"workload": name, "n_tet": nt, "n_vert": nv, "n_site": ns, "knn_k": st.knn_k,
                    "n_pairs": st.n_pairs, "n_cells": st.n_cells,
                    "predicates": "fp32 filter, fp64 det when undecided",
-                   "neighbours": "gpu kNN, k smallest power-bisector distances, id order",
+                   "neighbours": "gpu kNN, k smallest power-bisector distances",
+                   "clipping": "ascending bisector distance, security-radius certificate",
                    "learned_k": False, "l2": "flushed between steps (256 MB write)",
                    "parallelism": "replicas" if world > 1 else "single gpu",
                    "generation_s": round(gen_s, 2)},
         "plain": {"value": plain_value, "ms_per_step": sum(pms) / len(pms),
                   "speedup_fast_over_plain": value / world / plain_value,
-                  "topology_bit_exact": bool(topo_ok)},
+                  "topology_bit_exact": bool(topo_ok), "cells_topology_differing": n_topo_diff,
+                  "predicates_evaluated": int(pst.n_predicates)},
+        "geometry_vs_plain": geo,
         "stage_ms": {"knn": st.ms_knn, "pairs": st.ms_pairs, "clip": st.ms_clip,
                      "clip_kernel": st.ms_clip_kernel, "compact": st.ms_compact},
         "predicates": {"evaluated": st.n_predicates, "escalated_fp64": st.n_escalated,
@@ -335,7 +348,7 @@ def run_fast_only(args):
     cfg, name, _ = make_workload(args)
     adj = rpd.mesh_adjacency(cfg["vert3d"].shape[0], cfg["tets"])
     r = rpd.RPD(predicate_mode=rpd.PRED_FP32_FILTER, neighbor_source=rpd.NEIGH_KNN,
-                knn_k=args.k, clip_order=rpd.ORDER_SITE_ID)
+                knn_k=args.k, clip_order=rpd.ORDER_SITE_ID, certify=True)
     r.set_mesh(cfg["vert3d"], cfg["tets"], adj["v_adjs"], adj["e_adj6"], adj["f_adjs"],
                adj["f_ids"])
     r.set_sites(cfg["sites"], cfg["flags"])
@@ -345,6 +358,45 @@ def run_fast_only(args):
         out.append(st.as_dict())
     r.close()
     print(json.dumps({"workload": name, "last": out[-1]}))
+
+
+def _geometry_error(h1, p1, h2, p2, n=20000):
+    """Max / RMS difference of FP64 vertex coordinates (relative to the
+    coordinate scale) and of cell volumes between two runs, on a sample of
+    cells with the same topology (vertex order may differ: compared as
+    sorted coordinate rows)."""
+    from libmat_gb300 import rpd
+
+    ok = np.flatnonzero(h1["status"] == rpd.SUCCESS)
+    if len(ok) == 0:
+        return None
+    rng = np.random.default_rng(1)
+    pick = rng.choice(ok, size=min(n, len(ok)), replace=False)
+    vmax, vsq, vn, wmax, wsq = 0.0, 0.0, 0, 0.0, 0.0
+    for q in pick:
+        a = _xyz(p1, h1, q)
+        b = _xyz(p2, h2, q)
+        if a.shape != b.shape:
+            continue
+        a = a[np.lexsort(a.T[::-1])]
+        b = b[np.lexsort(b.T[::-1])]
+        d = np.abs(a - b) / 1000.0
+        vmax = max(vmax, float(d.max()))
+        vsq += float((d * d).sum())
+        vn += d.size
+        rv = abs(h1["volume"][q] - h2["volume"][q]) / max(abs(h2["volume"][q]), 1e-30)
+        wmax = max(wmax, rv)
+        wsq += rv * rv
+    return {"vertex_max_rel": vmax, "vertex_rms_rel": (vsq / max(vn, 1)) ** 0.5,
+            "volume_max_rel": wmax, "volume_rms_rel": (wsq / len(pick)) ** 0.5,
+            "cells_sampled": int(len(pick))}
+
+
+def _xyz(p, h, q):
+    nv, np_, ne = int(h["nb_v"][q]), int(h["nb_p"][q]), int(h["nb_e"][q])
+    a = lambda x: (x + 15) // 16 * 16  # noqa: E731
+    start = int(h["offset"][q]) + 16 * np_ + a(8 * np_) + a(4 * nv) + a(4 * ne) + a(np_)
+    return p[start:start + 24 * nv].view(np.float64).reshape(-1, 3)
 
 
 def _sample_topology_equal(h1, p1, h2, p2, n=20000):
@@ -387,7 +439,7 @@ def _e2e(args, cfg, adj, rpd):
     s = pin("s", cfg["sites"])
     fl = pin("fl", cfg["flags"])
     r = rpd.RPD(predicate_mode=rpd.PRED_FP32_FILTER, neighbor_source=rpd.NEIGH_KNN,
-                knn_k=args.k, clip_order=rpd.ORDER_SITE_ID)
+                knn_k=args.k, clip_order=rpd.ORDER_SITE_ID, certify=True)
     r.set_mesh(v, t, va, e6, fa, fi)
     r.set_sites(s, fl)
     st = r.compute()

@@ -73,7 +73,11 @@ typedef struct rpd_config {
   int compute_geometry;  /* 1: FP64 vertex coordinates and cell volumes */
   int warps_per_block;   /* clip kernel block size in warps, 0 = default */
   int blocks_per_sm;     /* persistent grid: blocks per SM, 0 = default */
-  int reserved[8];
+  int certify;           /* 1 (RPD_NEIGH_KNN only): clip in ascending bisector
+                            distance and stop at the security-radius
+                            certificate; cells equal the plain path's up to
+                            the order of their records (same topology) */
+  int reserved[7];
 } rpd_config;
 
 /* One record per candidate (tet, site) pair; 32 bytes. */
@@ -113,6 +117,9 @@ typedef struct rpd_stats {
    * the grown-cell planes, [2] tets enumerated, [3] tets inside the grown
    * cell (rule evaluated), [4] pairs, [5] site boxes without planes */
   int64_t search[6];
+  int64_t n_reclipped;        /* cells whose shortened list (rpd_set_site_k)
+                                 ran out before the certificate held, clipped
+                                 again with the whole list */
 } rpd_stats;
 
 typedef struct rpd_cells_view {
@@ -155,6 +162,12 @@ rpd_status rpd_set_sites(struct rpd_ctx* ctx, const double* xyzw, int n_site,
 rpd_status rpd_set_neighbors(struct rpd_ctx* ctx, const int32_t* nbr, int k,
                              int layout);
 
+/* Per-site list lengths for certified clipping (config.certify): site i is
+ * clipped with its k_per_site[i] nearest neighbours first, and any of its
+ * cells not certified by then is clipped again with the whole list.  NULL
+ * clears it.  k_per_site may be a device pointer when on_device is 1. */
+rpd_status rpd_set_site_k(struct rpd_ctx* ctx, const int32_t* k_per_site, int on_device);
+
 /* Runs the whole path on the device: neighbour lists (RPD_NEIGH_KNN),
  * candidate pairs (the reference's rule, voronoi.cu:154-193), clipping,
  * compaction.  Blocks until done.  stats may be NULL. */
@@ -173,6 +186,13 @@ rpd_status rpd_copy_cells_to_host(struct rpd_ctx* ctx, rpd_cell_header* headers,
  * cells included, with their failure status), in (tet, site) order. */
 rpd_status rpd_copy_pair_headers_to_host(struct rpd_ctx* ctx, rpd_cell_header* headers,
                                          int64_t capacity, int64_t* n_pairs);
+
+/* Canonical topology hash of every pair of the last rpd_compute (0 for
+ * dropped cells): the sum over the cell's vertices of a hash of the sorted
+ * face keys (clip_id2) of its three planes and its #adjacent cells.  Equal
+ * hashes = equal cells up to the order of planes, vertices and edges. */
+rpd_status rpd_copy_topology_hashes_to_host(struct rpd_ctx* ctx, uint64_t* hashes,
+                                            int64_t capacity, int64_t* n_pairs);
 
 /* The neighbour lists used by the last rpd_compute (n_site x k, -1 padded),
  * copied to the host.  k_out receives k. */

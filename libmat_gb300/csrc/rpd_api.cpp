@@ -87,7 +87,10 @@ struct rpd_ctx {
 
   // neighbour lists
   int k = 0;
-  DevBuf<int32_t> nbr, nbr_dist, nbr_ref_tmp, knn_status;
+  DevBuf<int32_t> nbr, nbr_dist, nbr_ref_tmp, knn_status, site_klen, reclip_idx;
+  bool has_site_klen = false;
+  DevBuf<unsigned long long> topo_hash;
+  long long n_reclipped = 0;
   DevBuf<float> nbr_keys;
   bool has_user_nbr = false;
 
@@ -210,6 +213,7 @@ rpd_status rpd_create(const rpd_config* cfg, rpd_ctx** out) {
     return RPD_ERR_INVALID_ARGUMENT;
   if (c0.warps_per_block < 0 || c0.warps_per_block > kClipMaxThreads / 32 || c0.blocks_per_sm < 0)
     return RPD_ERR_INVALID_ARGUMENT;
+  if (c0.certify && c0.neighbor_source != RPD_NEIGH_KNN) return RPD_ERR_INVALID_ARGUMENT;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
     cudaGetLastError();
@@ -238,7 +242,8 @@ void rpd_destroy(rpd_ctx* c) {
   c->vert3f.release(); c->vert3d.release(); c->tets.release(); c->v_adjs.release();
   c->f_adjs.release(); c->f_ids.release(); c->e_adj6.release(); c->tet_class.release();
   c->site4f.release(); c->site4d.release(); c->flags.release();
-  c->nbr.release(); c->nbr_dist.release(); c->nbr_ref_tmp.release(); c->knn_status.release(); c->nbr_keys.release();
+  c->nbr.release(); c->nbr_dist.release(); c->site_klen.release(); c->reclip_idx.release();
+  c->topo_hash.release(); c->nbr_ref_tmp.release(); c->knn_status.release(); c->nbr_keys.release();
   c->s_cell_of.release(); c->s_cell_count.release(); c->s_cell_start.release();
   c->s_cell_fill.release(); c->s_cell_items.release();
   c->t_cell_of.release(); c->t_cell_count.release(); c->t_cell_start.release();
@@ -374,7 +379,10 @@ rpd_status rpd_set_sites(rpd_ctx* c, const double* xyzw, int n_site, const uint3
   CK(cudaMemcpyAsync(c->site4d.ptr, xyzw, (size_t)n_site * 32, cudaMemcpyHostToDevice, st), "H2D sites");
   CK(cudaMemcpyAsync(c->flags.ptr, fl.data(), (size_t)n_site * 4, cudaMemcpyHostToDevice, st), "H2D flags");
   CK(cudaStreamSynchronize(st), "set_sites sync");
-  if (c->n_site != n_site) c->has_user_nbr = false;
+  if (c->n_site != n_site) {
+    c->has_user_nbr = false;
+    c->has_site_klen = false;
+  }
   c->n_site = n_site;
   for (int a = 0; a < 3; ++a) {
     c->site_lo[a] = lo[a];
@@ -571,12 +579,24 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
   // ---- clipping
   const long long n_pairs = c->n_pairs;
   CK(c->pair_headers.ensure((size_t)std::max<long long>(n_pairs, 1)), "alloc headers");
+  CK(c->topo_hash.ensure((size_t)std::max<long long>(n_pairs, 1)), "alloc hashes");
   long long pcap = c->payload_cap_hint > 0 ? c->payload_cap_hint
                                            : std::max<long long>(1 << 24, 640ll * n_pairs);
   const int warps = c->cfg.warps_per_block > 0 ? c->cfg.warps_per_block : 4;
+  const int certify = c->cfg.certify ? 1 : 0;
   int bps = c->cfg.blocks_per_sm;
-  if (bps <= 0) bps = clip_blocks_per_sm(c->cfg.predicate_mode, warps);
+  if (bps <= 0) bps = clip_blocks_per_sm_cert(c->cfg.predicate_mode, certify, warps);
   int blocks = std::max(1, c->num_sms * bps);
+  // certificate margin: 16u (L + D), L the largest coordinate magnitude,
+  // D the largest distance between two sites
+  double L = 0.0, D2 = 0.0;
+  for (int a = 0; a < 3; ++a) {
+    L = std::max(L, std::max(std::fabs(c->site_lo[a]), std::fabs(c->site_hi[a])));
+    L = std::max(L, std::max(std::fabs(c->mesh_lo[a]), std::fabs(c->mesh_hi[a])));
+    D2 += (c->site_hi[a] - c->site_lo[a]) * (c->site_hi[a] - c->site_lo[a]);
+  }
+  const float cert_margin = (float)(16.0 * std::ldexp(1.0, -24) * (L + std::sqrt(D2)) + 1e-30);
+  c->n_reclipped = 0;
   for (int attempt = 0; attempt < 3; ++attempt) {
     CK(c->payload.ensure((size_t)pcap), "alloc payload");
     CK(cudaMemsetAsync(c->scratch.ptr, 0, 4 * sizeof(unsigned long long), st), "memset");
@@ -590,7 +610,7 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
     p.f_ids = c->f_ids.ptr;
     p.site4f = c->site4f.ptr;
     p.site4d = c->site4d.ptr;
-    p.nbr = c->nbr.ptr;
+    p.nbr = certify ? c->nbr_dist.ptr : c->nbr.ptr;
     p.k = c->k;
     p.pair_tet = c->pair_tet.ptr;
     p.pair_site = c->pair_site.ptr;
@@ -602,9 +622,35 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
     p.work = c->scratch.ptr + 1;
     p.counters = c->scratch.ptr + 2;
     p.geometry = c->cfg.compute_geometry;
+    p.keys = certify ? c->nbr_keys.ptr : nullptr;
+    p.site_klen = (certify && c->has_site_klen) ? c->site_klen.ptr : nullptr;
+    p.cert_margin = cert_margin;
+    p.pair_index = nullptr;
+    p.n_work = n_pairs;
+    p.topo_hash = c->topo_hash.ptr;
     CK(cudaEventRecord(c->ev[kEvClipK0], st), "event");
-    if (n_pairs > 0) CK(launch_clip_cells(p, c->cfg.predicate_mode, blocks, warps, st), "clip");
+    if (n_pairs > 0) CK(launch_clip_cells(p, c->cfg.predicate_mode, certify, blocks, warps, st), "clip");
     CK(cudaEventRecord(c->ev[kEvClipK1], st), "event");
+    if (p.site_klen && n_pairs > 0) {
+      // cells whose shortened list was not enough: clip them again whole
+      CK(c->flag_tmp.ensure((size_t)n_pairs + 1), "alloc");
+      CK(c->pos_tmp.ensure((size_t)n_pairs + 1), "alloc");
+      CK(c->reclip_idx.ensure((size_t)n_pairs), "alloc");
+      CK(c->scan_tmp.ensure(scan_temp_ints(std::max<long long>(n_pairs, n_tet)) + 16), "alloc");
+      CK(select_pairs(c->pair_headers.ptr, n_pairs, kSecurityRadiusNotReached, c->flag_tmp.ptr,
+                      c->pos_tmp.ptr, c->scan_tmp.ptr, c->reclip_idx.ptr, st), "select");
+      int32_t n_re = 0;
+      CK(cudaMemcpyAsync(&n_re, c->pos_tmp.ptr + n_pairs, sizeof(n_re), cudaMemcpyDeviceToHost, st), "D2H");
+      CK(cudaStreamSynchronize(st), "reclip sync");
+      c->n_reclipped = n_re;
+      if (n_re > 0) {
+        CK(cudaMemsetAsync(c->scratch.ptr + 1, 0, sizeof(unsigned long long), st), "memset");
+        p.site_klen = nullptr;
+        p.pair_index = c->reclip_idx.ptr;
+        p.n_work = n_re;
+        CK(launch_clip_cells(p, c->cfg.predicate_mode, certify, blocks, warps, st), "reclip");
+      }
+    }
     unsigned long long cur = 0;
     CK(cudaMemcpyAsync(&cur, c->scratch.ptr, sizeof(cur), cudaMemcpyDeviceToHost, st), "D2H");
     CK(cudaStreamSynchronize(st), "clip sync");
@@ -654,6 +700,7 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
     stats->n_launches = take_launches();
     for (int i = 0; i < 6; ++i) stats->search[i] = (int64_t)host_scratch[20 + i];
     stats->search[4] = c->n_pairs;
+    stats->n_reclipped = c->n_reclipped;
   }
   return RPD_OK;
 }
@@ -689,6 +736,39 @@ rpd_status rpd_copy_cells_to_host(rpd_ctx* c, rpd_cell_header* headers, int64_t 
     CK(cudaMemcpyAsync(payload, c->payload.ptr, (size_t)c->payload_bytes, cudaMemcpyDeviceToHost, st),
        "D2H payload");
   CK(cudaStreamSynchronize(st), "copy sync");
+  return RPD_OK;
+}
+
+rpd_status rpd_set_site_k(rpd_ctx* c, const int32_t* k_per_site, int on_device) {
+  if (!c) return RPD_ERR_INVALID_ARGUMENT;
+  if (!k_per_site) {
+    c->has_site_klen = false;
+    return RPD_OK;
+  }
+  if (!c->has_sites) return fail(c, RPD_ERR_NOT_READY, "rpd_set_site_k: set the sites first");
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  CK(c->site_klen.ensure((size_t)c->n_site), "alloc");
+  CK(cudaMemcpyAsync(c->site_klen.ptr, k_per_site, sizeof(int32_t) * (size_t)c->n_site,
+                     on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->stream),
+     "copy site k");
+  CK(cudaStreamSynchronize(c->stream), "sync");
+  c->has_site_klen = true;
+  c->has_result = false;
+  return RPD_OK;
+}
+
+rpd_status rpd_copy_topology_hashes_to_host(rpd_ctx* c, uint64_t* hashes, int64_t capacity,
+                                            int64_t* n_pairs) {
+  if (!c) return RPD_ERR_INVALID_ARGUMENT;
+  if (!c->has_result) return fail(c, RPD_ERR_NOT_READY, "rpd_copy_topology_hashes_to_host: no result");
+  if (n_pairs) *n_pairs = c->n_pairs;
+  if (!hashes) return RPD_OK;
+  if (capacity < c->n_pairs) return fail(c, RPD_ERR_CAPACITY, "rpd_copy_topology_hashes_to_host: buffer too small");
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  if (c->n_pairs > 0)
+    CK(cudaMemcpyAsync(hashes, c->topo_hash.ptr, sizeof(uint64_t) * (size_t)c->n_pairs,
+                       cudaMemcpyDeviceToHost, c->stream), "D2H");
+  CK(cudaStreamSynchronize(c->stream), "sync");
   return RPD_OK;
 }
 

@@ -388,14 +388,67 @@ __device__ __forceinline__ void refresh_cofactors(WarpCell& c, int from, int to,
 // ------------------------------------------------------------------------
 // make_plane(j) builds the plane of list entry j (bisector, or offset
 // bisector for the box kernel).
-template <int PRED, bool FULL, class MakePlane>
+// ------------------------------------------------------------------------
+// security-radius certificate (lists in ascending bisector distance)
+// ------------------------------------------------------------------------
+// Every vertex x of the cell satisfies x = K_xyz / K_w (K its cofactors), so
+// |x - S| <= (|K_xyz - K_w S| + e) / (|K_w| - e_w) with e, e_w the cofactor
+// error bounds (gamma_5 times the permanents M) and the rounding of the
+// translation.  A neighbour j whose power bisector lies at distance d_j from
+// the seed S cannot clip a cell inside the ball B(S, R): every point x of
+// the ball has exact bisector value >= |n_j| (d_j - |x - S|) > 0, and the
+// margin below covers the float rounding of the key d_j, of the float plane
+// itself (<= 9uL + 4u|w_i - w_j| / |n_j| for coordinates below L), and of the
+// predicate.  Keys ascend along the list, so one test of the next key
+// certifies every remaining neighbour.
+__device__ __forceinline__ float vertex_radius(float4 K, float4 M, float3 S) {
+  const float g = 6.0f * 5.9604645e-08f;
+  float ew = g * M.w;
+  float aw = fabsf(K.w);
+  if (!(aw > ew)) return INFINITY;
+  float nx = __fmaf_rn(-K.w, S.x, K.x), ny = __fmaf_rn(-K.w, S.y, K.y),
+        nz = __fmaf_rn(-K.w, S.z, K.z);
+  float ex = g * (M.x + fabsf(S.x) * M.w) + 2.4e-7f * fabsf(nx);
+  float ey = g * (M.y + fabsf(S.y) * M.w) + 2.4e-7f * fabsf(ny);
+  float ez = g * (M.z + fabsf(S.z) * M.w) + 2.4e-7f * fabsf(nz);
+  float ax = fabsf(nx) + ex, ay = fabsf(ny) + ey, az = fabsf(nz) + ez;
+  float num = sqrtf(ax * ax + ay * ay + az * az) * (1.0f + 1e-6f);
+  return num / (aw - ew) * (1.0f + 1e-6f);
+}
+
+__device__ __forceinline__ float cell_radius(const WarpCell& c, int nb_v, float3 S, int lane) {
+  float r = 0.f;
+  for (int v = lane; v < nb_v; v += 32) r = fmaxf(r, vertex_radius(c.u.f.K[v], c.u.f.M[v], S));
+  for (int o = 16; o > 0; o >>= 1) r = fmaxf(r, __shfl_xor_sync(0xffffffffu, r, o));
+  return r;
+}
+
+struct Cert {
+  const float* keys;  // key of each list entry (CERT), ascending
+  float3 S;           // seed
+  float margin;       // absolute part of the certificate's margin
+  bool certified;
+};
+
+// ------------------------------------------------------------------------
+// the neighbour loop shared by the cell kernel and the box kernel
+// ------------------------------------------------------------------------
+// make_plane(j) builds the plane of list entry j (bisector, or offset
+// bisector for the box kernel).  With CERT the list is in ascending key
+// order and clipping stops as soon as the certificate holds.
+template <int PRED, bool FULL, bool CERT, class MakePlane>
 __device__ void clip_list(WarpCell& c, CellState& s, const int32_t* list, int k,
                           int seed_id, MakePlane make_plane, int lane,
-                          uint32_t& n_pred, uint32_t& n_esc) {
+                          uint32_t& n_pred, uint32_t& n_esc, Cert& cert) {
+  constexpr bool kCof = PRED == RPD_PRED_FP32_FILTER || CERT;
+  float R = INFINITY;
+  if (CERT) R = cell_radius(c, s.nb_v, cert.S, lane);
   for (int base = 0; base < k && s.status == kSuccess; base += 32) {
     int j = (base + lane < k) ? __ldg(list + base + lane) : -1;
     uint32_t valid = __ballot_sync(0xffffffffu, j != -1);
     int count = (~valid == 0u) ? 32 : (__ffs(~valid) - 1);  // up to first -1
+    float key_mine = 0.f;
+    if (CERT && lane < count) key_mine = __ldg(cert.keys + base + lane);
     float4 e_mine = make_float4(0.f, 0.f, 0.f, 0.f);
     if (lane < count) e_mine = make_plane(j);
     // planes already in the cell that equal this lane's plane
@@ -404,6 +457,13 @@ __device__ void clip_list(WarpCell& c, CellState& s, const int32_t* list, int k,
       if (plane_eq(e_mine, c.pl[p])) dup_mine |= 1ull << p;
     int r = 0;
     while (r < count) {
+      if (CERT) {
+        float kr = __shfl_sync(0xffffffffu, key_mine, r);
+        if (kr * (1.0f - 64.0f * 5.9604645e-08f) - cert.margin > R) {
+          cert.certified = true;
+          return;
+        }
+      }
       if (s.nb_p >= kMaxP) {  // new_plane fails before any evaluation
         s.status = kVertexOverflow;
         break;
@@ -458,12 +518,9 @@ __device__ void clip_list(WarpCell& c, CellState& s, const int32_t* list, int k,
       }
       __syncwarp();
       broadcast_state(s);
-      // new vertices sit at the end; the surviving ones keep their
-      // cofactors (moved by the partition), so rebuild from the first new
-      if (s.status == kSuccess) {
-        // the vertices created by this clip are the last ones; their count
-        // is at most nb_v, so recompute slots whose planes include the new
-        // plane index (they are exactly the new ones)
+      // the vertices created by this clip are exactly those whose first
+      // plane is the new one; the surviving ones kept their cofactors
+      if (kCof && s.status == kSuccess) {
         const int cur = s.nb_p - 1;
         for (int v = lane; v < s.nb_v; v += 32) {
           uchar4 t = c.ver[v];
@@ -476,6 +533,7 @@ __device__ void clip_list(WarpCell& c, CellState& s, const int32_t* list, int k,
         }
       }
       __syncwarp();
+      if (CERT && s.status == kSuccess) R = cell_radius(c, s.nb_v, cert.S, lane);
       // later planes of this chunk identical to the new one
       if (plane_eq(e_mine, e)) dup_mine |= 1ull << (s.nb_p - 1);
       if (s.status != kSuccess) break;
@@ -667,7 +725,41 @@ __device__ double cell_geometry(WarpCell& c, const CellState& s, const ClipParam
   return dv;
 }
 
-template <int PRED>
+// canonical topology of a cell, independent of the clipping order: the sum
+// over its vertices of a hash of the sorted face keys (clip_id2) of the
+// vertex's three planes and its #adjacent cells (splitmix64 mixing, Steele,
+// Lea and Flood, OOPSLA 2014).  Planes that clipped intermediate vertices and
+// no longer bound the cell appear in no vertex, so they do not count.
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z += 0x9e3779b97f4a7c15ull;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+__device__ __forceinline__ uint64_t face_key(int2 id) {
+  return ((uint64_t)(uint32_t)id.x << 32) | (uint32_t)id.y;
+}
+
+__device__ uint64_t cell_topology_hash(const WarpCell& c, int nb_v, int lane) {
+  uint64_t h = 0;
+  for (int v = lane; v < nb_v; v += 32) {
+    uchar4 t = c.ver[v];
+    uint64_t a = face_key(c.id2[t.x]), b = face_key(c.id2[t.y]), d = face_key(c.id2[t.z]), x;
+    if (a > b) { x = a; a = b; b = x; }
+    if (b > d) { x = b; b = d; d = x; }
+    if (a > b) { x = a; a = b; b = x; }
+    uint64_t hv = mix64(a);
+    hv = mix64(hv ^ b);
+    hv = mix64(hv ^ d);
+    hv = mix64(hv ^ (uint64_t)t.w);
+    h += hv;
+  }
+  for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(0xffffffffu, h, o);
+  return h;
+}
+
+template <int PRED, bool CERT>
 __global__ void __launch_bounds__(kClipMaxThreads) clip_cells_kernel(ClipParams p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31;
@@ -679,7 +771,8 @@ __global__ void __launch_bounds__(kClipMaxThreads) clip_cells_kernel(ClipParams 
     long long q = 0;
     if (lane == 0) q = (long long)atomicAdd(p.work, 1ull);
     q = __shfl_sync(0xffffffffu, q, 0);
-    if (q >= p.n_pairs) break;
+    if (q >= p.n_work) break;
+    if (p.pair_index) q = __ldg(p.pair_index + q);
     const int t = __ldg(p.pair_tet + q);
     const int sid = __ldg(p.pair_site + q);
     const float4 seed = __ldg(p.site4f + sid);
@@ -710,7 +803,7 @@ __global__ void __launch_bounds__(kClipMaxThreads) clip_cells_kernel(ClipParams 
     s.nb_p = 4;
     s.nb_e = 6;
     s.status = kSuccess;
-    if (PRED == RPD_PRED_FP32_FILTER) {
+    if (PRED == RPD_PRED_FP32_FILTER || CERT) {
       refresh_cofactors(c, 0, 4, lane);
       __syncwarp();
     }
@@ -718,8 +811,19 @@ __global__ void __launch_bounds__(kClipMaxThreads) clip_cells_kernel(ClipParams 
     // ---- clip by the site's neighbour list
     const float4* site4f = p.site4f;
     auto make_plane = [&](int j) { return bisector_f(seed, __ldg(site4f + j)); };
-    clip_list<PRED, true>(c, s, p.nbr + (long long)sid * p.k, p.k, sid, make_plane, lane,
-                          n_pred, n_esc);
+    const int32_t* list = p.nbr + (long long)sid * p.k;
+    int klen = p.k;
+    if (p.site_klen) klen = min(klen, __ldg(p.site_klen + sid));
+    Cert cert;
+    cert.keys = CERT ? p.keys + (long long)sid * p.k : nullptr;
+    cert.S = make_float3(seed.x, seed.y, seed.z);
+    cert.margin = p.cert_margin;
+    cert.certified = false;
+    clip_list<PRED, true, CERT>(c, s, list, klen, sid, make_plane, lane, n_pred, n_esc, cert);
+    // a shortened list that ran out before the certificate held: the cell
+    // is clipped again with the whole list
+    if (CERT && s.status == kSuccess && !cert.certified && klen < p.k && __ldg(list + klen) != -1)
+      s.status = kSecurityRadiusNotReached;
 
     // ---- emit
     rpd_cell_header hd;
@@ -771,7 +875,12 @@ __global__ void __launch_bounds__(kClipMaxThreads) clip_cells_kernel(ClipParams 
         hd.volume = vol;
       }
     }
-    if (lane == 0) p.headers[q] = hd;
+    uint64_t th = 0;
+    if (p.topo_hash && hd.status == kSuccess) th = cell_topology_hash(c, s.nb_v, lane);
+    if (lane == 0) {
+      p.headers[q] = hd;
+      if (p.topo_hash) p.topo_hash[q] = th;
+    }
     __syncwarp();
   }
   // statistics
@@ -855,8 +964,11 @@ __global__ void __launch_bounds__(kClipMaxThreads) site_box_kernel(BoxParams p) 
     };
     // any subset of the planes gives a superset polytope; the nearest k_box
     // bisectors bound the cell well and keep the box clip small
-    clip_list<RPD_PRED_FP32_FILTER, false>(c, s, p.nbr + (long long)i * p.k, p.k_box, i,
-                                           make_plane, lane, n_pred, n_esc);
+    Cert nocert;
+    nocert.keys = nullptr;
+    nocert.certified = false;
+    clip_list<RPD_PRED_FP32_FILTER, false, false>(c, s, p.nbr + (long long)i * p.k, p.k_box, i,
+                                                  make_plane, lane, n_pred, n_esc, nocert);
     float bl[3], bh[3];
     if (s.status == kSuccess) {
       bl[0] = bl[1] = bl[2] = 3.0e38f;
@@ -931,22 +1043,23 @@ __global__ void __launch_bounds__(kClipMaxThreads) site_box_kernel(BoxParams p) 
 
 size_t clip_smem_per_warp() { return sizeof(WarpCell); }
 
-int clip_blocks_per_sm(int pred_mode, int warps) {
+template <int PRED, bool CERT>
+static int occ_of(int warps) {
   size_t smem = sizeof(WarpCell) * warps;
   int n = 0;
-  if (pred_mode == RPD_PRED_FP32_FILTER) {
-    cudaFuncSetAttribute(clip_cells_kernel<RPD_PRED_FP32_FILTER>,
-                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, clip_cells_kernel<RPD_PRED_FP32_FILTER>,
-                                                  warps * 32, smem);
-  } else {
-    cudaFuncSetAttribute(clip_cells_kernel<RPD_PRED_FP64>,
-                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, clip_cells_kernel<RPD_PRED_FP64>,
-                                                  warps * 32, smem);
-  }
+  cudaFuncSetAttribute(clip_cells_kernel<PRED, CERT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, clip_cells_kernel<PRED, CERT>, warps * 32, smem);
   return n > 0 ? n : 1;
 }
+
+int clip_blocks_per_sm_cert(int pred_mode, int certify, int warps) {
+  if (pred_mode == RPD_PRED_FP32_FILTER)
+    return certify ? occ_of<RPD_PRED_FP32_FILTER, true>(warps) : occ_of<RPD_PRED_FP32_FILTER, false>(warps);
+  return certify ? occ_of<RPD_PRED_FP64, true>(warps) : occ_of<RPD_PRED_FP64, false>(warps);
+}
+
+int clip_blocks_per_sm(int pred_mode, int warps) { return clip_blocks_per_sm_cert(pred_mode, 0, warps); }
 
 int box_blocks_per_sm(int warps) {
   size_t smem = sizeof(WarpCell) * warps;
@@ -956,19 +1069,23 @@ int box_blocks_per_sm(int warps) {
   return n > 0 ? n : 1;
 }
 
-cudaError_t launch_clip_cells(const ClipParams& p, int pred_mode, int blocks, int warps,
-                              cudaStream_t st) {
+template <int PRED, bool CERT>
+static void launch_one(const ClipParams& p, int blocks, int warps, cudaStream_t st) {
   size_t smem = sizeof(WarpCell) * warps;
+  cudaFuncSetAttribute(clip_cells_kernel<PRED, CERT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)smem);
+  clip_cells_kernel<PRED, CERT><<<blocks, warps * 32, smem, st>>>(p);
+  note_launches(1);
+}
+
+cudaError_t launch_clip_cells(const ClipParams& p, int pred_mode, int certify, int blocks,
+                              int warps, cudaStream_t st) {
   if (pred_mode == RPD_PRED_FP32_FILTER) {
-    cudaFuncSetAttribute(clip_cells_kernel<RPD_PRED_FP32_FILTER>,
-                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    clip_cells_kernel<RPD_PRED_FP32_FILTER><<<blocks, warps * 32, smem, st>>>(p);
-    note_launches(1);
+    if (certify) launch_one<RPD_PRED_FP32_FILTER, true>(p, blocks, warps, st);
+    else launch_one<RPD_PRED_FP32_FILTER, false>(p, blocks, warps, st);
   } else {
-    cudaFuncSetAttribute(clip_cells_kernel<RPD_PRED_FP64>,
-                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    clip_cells_kernel<RPD_PRED_FP64><<<blocks, warps * 32, smem, st>>>(p);
-    note_launches(1);
+    if (certify) launch_one<RPD_PRED_FP64, true>(p, blocks, warps, st);
+    else launch_one<RPD_PRED_FP64, false>(p, blocks, warps, st);
   }
   return cudaGetLastError();
 }

@@ -39,6 +39,14 @@ struct ClipParams {
   unsigned long long* work;      // work-queue counter, zeroed before launch
   unsigned long long* counters;  // [0] predicates, [1] escalated
   int geometry;
+  // distance-ordered lists with the security-radius certificate
+  const float* keys;             // n_site x k bisector distances (ascending), or null
+  const int32_t* site_klen;      // per-site list length, or null (= k)
+  float cert_margin;             // absolute margin of the certificate
+  // optional indirection: work item w clips pair pair_index[w]
+  const int32_t* pair_index;
+  long long n_work;
+  unsigned long long* topo_hash;  // n_pairs canonical topology hashes, or null
 };
 
 struct BoxParams {
@@ -64,8 +72,13 @@ constexpr int kBoxPlanes = 48;
 size_t clip_smem_per_warp();
 int clip_blocks_per_sm(int pred_mode, int warps);
 int box_blocks_per_sm(int warps);
-cudaError_t launch_clip_cells(const ClipParams& p, int pred_mode, int blocks, int warps,
-                              cudaStream_t st);
+cudaError_t launch_clip_cells(const ClipParams& p, int pred_mode, int certify, int blocks,
+                              int warps, cudaStream_t st);
+int clip_blocks_per_sm_cert(int pred_mode, int certify, int warps);
+// indices of the pairs whose header status equals `status`
+cudaError_t select_pairs(const rpd_cell_header* h, long long n, int status, int32_t* flag_tmp,
+                         int32_t* pos_tmp, int32_t* scan_tmp, int32_t* idx_out,
+                         cudaStream_t st);
 cudaError_t launch_site_box(const BoxParams& p, int blocks, int warps, cudaStream_t st);
 
 // ---- uniform grids, kNN, candidate pairs, scans (rpd_pairs.cu)

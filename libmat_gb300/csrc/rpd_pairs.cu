@@ -719,6 +719,35 @@ cudaError_t compact_cells(const rpd_cell_header* pair_headers, long long n_pairs
   return cudaGetLastError();
 }
 
+__global__ void flag_status_kernel(const rpd_cell_header* h, long long n, int status,
+                                   int32_t* flag) {
+  long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < n) flag[q] = h[q].status == status ? 1 : 0;
+}
+
+__global__ void scatter_index_kernel(const int32_t* flag, const int32_t* pos, long long n,
+                                     int32_t* idx) {
+  long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < n && flag[q]) idx[pos[q]] = (int32_t)q;
+}
+
+cudaError_t select_pairs(const rpd_cell_header* h, long long n, int status, int32_t* flag_tmp,
+                         int32_t* pos_tmp, int32_t* scan_tmp, int32_t* idx_out,
+                         cudaStream_t st) {
+  int nb = (int)((n + 255) / 256);
+  if (n > 0) {
+    flag_status_kernel<<<nb, 256, 0, st>>>(h, n, status, flag_tmp);
+    note_launches(1);
+  }
+  cudaError_t err = scan_exclusive(flag_tmp, pos_tmp, n, scan_tmp, st);
+  if (err != cudaSuccess) return err;
+  if (n > 0) {
+    scatter_index_kernel<<<nb, 256, 0, st>>>(flag_tmp, pos_tmp, n, idx_out);
+    note_launches(1);
+  }
+  return cudaGetLastError();
+}
+
 // ------------------------------------------------------------------------
 // reference site_knn layout ((k+1) rows x n_site) -> row-major lists
 // ------------------------------------------------------------------------

@@ -37,7 +37,8 @@ EXPORTS = [
     "rpd_destroy", "rpd_last_error", "rpd_set_mesh", "rpd_set_sites", "rpd_set_neighbors",
     "rpd_compute", "rpd_get_cells", "rpd_copy_cells_to_host", "rpd_copy_neighbors_to_host",
     "rpd_copy_pairs_to_host", "rpd_copy_pair_headers_to_host", "rpd_build_mesh_adjacency",
-    "rpd_host_alloc", "rpd_host_free", "rpd_compact_cells_noalloc",
+    "rpd_host_alloc", "rpd_host_free", "rpd_compact_cells_noalloc", "rpd_set_site_k",
+    "rpd_copy_topology_hashes_to_host",
 ]
 
 
@@ -46,7 +47,7 @@ class Config(ctypes.Structure):
                 ("neighbor_source", ctypes.c_int), ("knn_k", ctypes.c_int),
                 ("clip_order", ctypes.c_int), ("compute_geometry", ctypes.c_int),
                 ("warps_per_block", ctypes.c_int), ("blocks_per_sm", ctypes.c_int),
-                ("reserved", ctypes.c_int * 8)]
+                ("certify", ctypes.c_int), ("reserved", ctypes.c_int * 7)]
 
 
 class Stats(ctypes.Structure):
@@ -57,7 +58,8 @@ class Stats(ctypes.Structure):
                 ("ms_total", ctypes.c_float), ("ms_knn", ctypes.c_float),
                 ("ms_pairs", ctypes.c_float), ("ms_clip", ctypes.c_float),
                 ("ms_compact", ctypes.c_float), ("ms_clip_kernel", ctypes.c_float),
-                ("n_launches", ctypes.c_int32), ("search", ctypes.c_int64 * 6)]
+                ("n_launches", ctypes.c_int32), ("search", ctypes.c_int64 * 6),
+                ("n_reclipped", ctypes.c_int64)]
 
     def as_dict(self):
         d = {f: getattr(self, f) for f, _ in self._fields_ if f not in ("status_counts", "search")}
@@ -116,6 +118,10 @@ def load(path=LIB_PATH):
     L.rpd_copy_pair_headers_to_host.argtypes = [vp, vp, i64, c.POINTER(i64)]
     L.rpd_compact_cells_noalloc.restype = i32
     L.rpd_compact_cells_noalloc.argtypes = [vp, i64, vp, vp, vp, vp]
+    L.rpd_set_site_k.restype = i32
+    L.rpd_set_site_k.argtypes = [vp, vp, i32]
+    L.rpd_copy_topology_hashes_to_host.restype = i32
+    L.rpd_copy_topology_hashes_to_host.argtypes = [vp, vp, i64, c.POINTER(i64)]
     L.rpd_host_alloc.restype = vp
     L.rpd_host_alloc.argtypes = [c.c_size_t]
     L.rpd_host_free.restype = None
@@ -161,7 +167,7 @@ class RPD:
 
     def __init__(self, device=0, predicate_mode=PRED_FP32_FILTER, neighbor_source=NEIGH_KNN,
                  knn_k=64, clip_order=ORDER_SITE_ID, compute_geometry=True,
-                 warps_per_block=0, blocks_per_sm=0):
+                 warps_per_block=0, blocks_per_sm=0, certify=False):
         L = load()
         cfg = Config()
         L.rpd_config_default(ctypes.byref(cfg))
@@ -173,6 +179,7 @@ class RPD:
         cfg.compute_geometry = 1 if compute_geometry else 0
         cfg.warps_per_block = warps_per_block
         cfg.blocks_per_sm = blocks_per_sm
+        cfg.certify = 1 if certify else 0
         h = ctypes.c_void_p()
         s = L.rpd_create(ctypes.byref(cfg), ctypes.byref(h))
         if s != 0:
@@ -221,6 +228,22 @@ class RPD:
         n = np.ascontiguousarray(nbr, np.int32)
         k = n.shape[1] if layout == 0 else n.shape[0] - 1
         self._check(self._L.rpd_set_neighbors(self._h, _p(n), k, layout))
+
+    def set_site_k(self, k_per_site):
+        """Per-site list lengths for certified clipping (None clears)."""
+        if k_per_site is None:
+            self._check(self._L.rpd_set_site_k(self._h, None, 0))
+            return
+        a = np.ascontiguousarray(k_per_site, np.int32)
+        self._check(self._L.rpd_set_site_k(self._h, _p(a), 0))
+
+    def topology_hashes(self):
+        n = ctypes.c_int64()
+        self._check(self._L.rpd_copy_topology_hashes_to_host(self._h, None, 0, ctypes.byref(n)))
+        out = np.zeros(n.value, np.uint64)
+        self._check(self._L.rpd_copy_topology_hashes_to_host(self._h, _p(out), out.shape[0],
+                                                             ctypes.byref(n)))
+        return out
 
     def compute(self):
         st = Stats()

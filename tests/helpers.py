@@ -56,3 +56,33 @@ def tet_volumes(vert, tets):
     a = vert[tets[:, 0]]
     return np.abs(np.einsum("ij,ij->i", np.cross(vert[tets[:, 1]] - a, vert[tets[:, 2]] - a),
                             vert[tets[:, 3]] - a)) / 6.0
+
+
+M64 = (1 << 64) - 1
+
+
+def mix64(z):
+    z = (z + 0x9E3779B97F4A7C15) & M64
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & M64
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & M64
+    return z ^ (z >> 31)
+
+
+def topology_hash(payload, off, nb_v, nb_p, nb_e):
+    """Order-independent hash of a cell's topology: sum over vertices of a
+    hash of the sorted face keys of its three planes and its #adj (the
+    definition the engine's rpd_copy_topology_hashes_to_host uses)."""
+    s = section_sizes(int(nb_v), int(nb_p), int(nb_e))
+    off = int(off)
+    id2 = payload[off + s["plane"]:off + s["plane"] + 8 * int(nb_p)].view(np.int32).reshape(-1, 2)
+    ver = payload[off + s["plane"] + s["id2"]:][:4 * int(nb_v)].reshape(-1, 4)
+    keys = [((int(a) & 0xFFFFFFFF) << 32) | (int(b) & 0xFFFFFFFF) for a, b in id2]
+    h = 0
+    for t in ver:
+        a, b, d = sorted((keys[t[0]], keys[t[1]], keys[t[2]]))
+        hv = mix64(a)
+        hv = mix64(hv ^ b)
+        hv = mix64(hv ^ d)
+        hv = mix64(hv ^ int(t[3]))
+        h = (h + hv) & M64
+    return h
