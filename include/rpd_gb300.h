@@ -77,7 +77,10 @@ typedef struct rpd_config {
                             distance and stop at the security-radius
                             certificate; cells equal the plain path's up to
                             the order of their records (same topology) */
-  int reserved[7];
+  int clip_variant;      /* clip kernel register budget: 0 none (occupancy
+                            set by registers), 1 = 80 registers (6 blocks of
+                            4 warps per SM), 2 = 64 registers (8 blocks) */
+  int reserved[6];
 } rpd_config;
 
 /* One record per candidate (tet, site) pair; 32 bytes. */
@@ -167,6 +170,24 @@ rpd_status rpd_set_neighbors(struct rpd_ctx* ctx, const int32_t* nbr, int k,
  * cells not certified by then is clipped again with the whole list.  NULL
  * clears it.  k_per_site may be a device pointer when on_device is 1. */
 rpd_status rpd_set_site_k(struct rpd_ctx* ctx, const int32_t* k_per_site, int on_device);
+
+/* Autotuner: times rpd_compute on the context's current inputs for each
+ * candidate launch configuration of the clip kernel -- block size 2, 4 or 8
+ * warps, register budgets for 16, 24 or 32 resident warps per SM (the
+ * shared-memory budget per SM follows: 5.7 KB per warp) -- and, with
+ * config.certify, first-pass list lengths of 16, 32 or all neighbours
+ * (k-bucket; cells not certified by their bucket are clipped again whole).
+ * Keeps the fastest in the context (the cells are the same for every
+ * candidate).  repeats >= 1 timed runs per candidate (median). */
+typedef struct rpd_tuning {
+  int warps_per_block;
+  int clip_variant;
+  int k_bucket;        /* 0 = whole list */
+  int n_candidates;
+  float ms_clip_best;  /* clip stage of the chosen configuration */
+  float ms_clip_first; /* clip stage of the first candidate (defaults) */
+} rpd_tuning;
+rpd_status rpd_autotune(struct rpd_ctx* ctx, int repeats, rpd_tuning* result);
 
 /* Runs the whole path on the device: neighbour lists (RPD_NEIGH_KNN),
  * candidate pairs (the reference's rule, voronoi.cu:154-193), clipping,

@@ -214,6 +214,7 @@ rpd_status rpd_create(const rpd_config* cfg, rpd_ctx** out) {
   if (c0.warps_per_block < 0 || c0.warps_per_block > kClipMaxThreads / 32 || c0.blocks_per_sm < 0)
     return RPD_ERR_INVALID_ARGUMENT;
   if (c0.certify && c0.neighbor_source != RPD_NEIGH_KNN) return RPD_ERR_INVALID_ARGUMENT;
+  if (c0.clip_variant < 0 || c0.clip_variant > 2) return RPD_ERR_INVALID_ARGUMENT;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
     cudaGetLastError();
@@ -585,7 +586,8 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
   const int warps = c->cfg.warps_per_block > 0 ? c->cfg.warps_per_block : 4;
   const int certify = c->cfg.certify ? 1 : 0;
   int bps = c->cfg.blocks_per_sm;
-  if (bps <= 0) bps = clip_blocks_per_sm_cert(c->cfg.predicate_mode, certify, warps);
+  const int variant = c->cfg.clip_variant;
+  if (bps <= 0) bps = clip_blocks_per_sm_cert(c->cfg.predicate_mode, certify, warps, variant);
   int blocks = std::max(1, c->num_sms * bps);
   // certificate margin: 16u (L + D), L the largest coordinate magnitude,
   // D the largest distance between two sites
@@ -629,7 +631,7 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
     p.n_work = n_pairs;
     p.topo_hash = c->topo_hash.ptr;
     CK(cudaEventRecord(c->ev[kEvClipK0], st), "event");
-    if (n_pairs > 0) CK(launch_clip_cells(p, c->cfg.predicate_mode, certify, blocks, warps, st), "clip");
+    if (n_pairs > 0) CK(launch_clip_cells(p, c->cfg.predicate_mode, certify, variant, blocks, warps, st), "clip");
     CK(cudaEventRecord(c->ev[kEvClipK1], st), "event");
     if (p.site_klen && n_pairs > 0) {
       // cells whose shortened list was not enough: clip them again whole
@@ -648,7 +650,7 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
         p.site_klen = nullptr;
         p.pair_index = c->reclip_idx.ptr;
         p.n_work = n_re;
-        CK(launch_clip_cells(p, c->cfg.predicate_mode, certify, blocks, warps, st), "reclip");
+        CK(launch_clip_cells(p, c->cfg.predicate_mode, certify, variant, blocks, warps, st), "reclip");
       }
     }
     unsigned long long cur = 0;
@@ -701,6 +703,98 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
     for (int i = 0; i < 6; ++i) stats->search[i] = (int64_t)host_scratch[20 + i];
     stats->search[4] = c->n_pairs;
     stats->n_reclipped = c->n_reclipped;
+  }
+  return RPD_OK;
+}
+
+rpd_status rpd_autotune(rpd_ctx* c, int repeats, rpd_tuning* result) {
+  if (!c) return RPD_ERR_INVALID_ARGUMENT;
+  if (repeats < 1) repeats = 1;
+  struct Cand {
+    int warps, variant, bucket;
+  };
+  std::vector<Cand> cands;
+  const int w0 = c->cfg.warps_per_block > 0 ? c->cfg.warps_per_block : 4;
+  cands.push_back({w0, c->cfg.clip_variant, 0});
+  const int wlist[3] = {2, 4, 8};
+  for (int w : wlist) cands.push_back({w, 0, 0});
+  cands.push_back({4, 1, 0});
+  cands.push_back({4, 2, 0});
+  const rpd_config saved = c->cfg;
+  const bool saved_klen = c->has_site_klen;
+  std::vector<int32_t> saved_k;
+  if (saved_klen) {
+    saved_k.resize((size_t)c->n_site);
+    CK(cudaMemcpy(saved_k.data(), c->site_klen.ptr, sizeof(int32_t) * saved_k.size(),
+                  cudaMemcpyDeviceToHost), "D2H");
+  }
+  int buckets[3] = {0, 0, 0};
+  int nb = 1;
+  if (c->cfg.certify && c->cfg.neighbor_source == RPD_NEIGH_KNN) {
+    buckets[1] = 16;
+    buckets[2] = 32;
+    nb = 3;
+  }
+  float best = INFINITY, first = 0.f;
+  Cand best_c = cands[0];
+  int tried = 0;
+  for (int bi = 0; bi < nb; ++bi) {
+    for (size_t ci = 0; ci < cands.size(); ++ci) {
+      if (bi > 0 && ci == 0) continue;
+      Cand cd = cands[ci];
+      cd.bucket = buckets[bi];
+      c->cfg.warps_per_block = cd.warps;
+      c->cfg.clip_variant = cd.variant;
+      c->cfg.blocks_per_sm = 0;
+      if (cd.bucket > 0) {
+        std::vector<int32_t> kk((size_t)c->n_site, cd.bucket);
+        rpd_status s = rpd_set_site_k(c, kk.data(), 0);
+        if (s != RPD_OK) return s;
+      } else {
+        c->has_site_klen = false;
+      }
+      std::vector<float> t;
+      for (int r = 0; r < repeats + 1; ++r) {
+        rpd_stats st;
+        rpd_status s = rpd_compute(c, &st);
+        if (s != RPD_OK) {
+          c->cfg = saved;
+          return s;
+        }
+        if (r > 0) t.push_back(st.ms_clip);
+      }
+      std::sort(t.begin(), t.end());
+      float med = t[t.size() / 2];
+      if (tried == 0) first = med;
+      ++tried;
+      if (med < best) {
+        best = med;
+        best_c = cd;
+      }
+    }
+  }
+  c->cfg = saved;
+  c->cfg.warps_per_block = best_c.warps;
+  c->cfg.clip_variant = best_c.variant;
+  c->cfg.blocks_per_sm = 0;
+  if (best_c.bucket > 0) {
+    std::vector<int32_t> kk((size_t)c->n_site, best_c.bucket);
+    rpd_status s = rpd_set_site_k(c, kk.data(), 0);
+    if (s != RPD_OK) return s;
+  } else if (saved_klen) {
+    rpd_status s = rpd_set_site_k(c, saved_k.data(), 0);
+    if (s != RPD_OK) return s;
+  } else {
+    c->has_site_klen = false;
+  }
+  c->has_result = false;
+  if (result) {
+    result->warps_per_block = best_c.warps;
+    result->clip_variant = best_c.variant;
+    result->k_bucket = best_c.bucket;
+    result->n_candidates = tried;
+    result->ms_clip_best = best;
+    result->ms_clip_first = first;
   }
   return RPD_OK;
 }

@@ -759,8 +759,11 @@ __device__ uint64_t cell_topology_hash(const WarpCell& c, int nb_v, int lane) {
   return h;
 }
 
-template <int PRED, bool CERT>
-__global__ void __launch_bounds__(kClipMaxThreads) clip_cells_kernel(ClipParams p) {
+// MINB > 0 caps registers so that MINB blocks of 128 threads fit on an SM
+// (occupancy variants chosen by the autotuner)
+template <int PRED, bool CERT, int MINB>
+__global__ void __launch_bounds__(MINB > 0 ? 128 : kClipMaxThreads, MINB > 0 ? MINB : 1)
+    clip_cells_kernel(ClipParams p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31;
   const int wid = threadIdx.x >> 5;
@@ -1043,23 +1046,35 @@ __global__ void __launch_bounds__(kClipMaxThreads) site_box_kernel(BoxParams p) 
 
 size_t clip_smem_per_warp() { return sizeof(WarpCell); }
 
-template <int PRED, bool CERT>
+template <int PRED, bool CERT, int MINB>
 static int occ_of(int warps) {
   size_t smem = sizeof(WarpCell) * warps;
   int n = 0;
-  cudaFuncSetAttribute(clip_cells_kernel<PRED, CERT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)smem);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, clip_cells_kernel<PRED, CERT>, warps * 32, smem);
+  cudaFuncSetAttribute(clip_cells_kernel<PRED, CERT, MINB>,
+                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, clip_cells_kernel<PRED, CERT, MINB>,
+                                                warps * 32, smem);
   return n > 0 ? n : 1;
 }
 
-int clip_blocks_per_sm_cert(int pred_mode, int certify, int warps) {
-  if (pred_mode == RPD_PRED_FP32_FILTER)
-    return certify ? occ_of<RPD_PRED_FP32_FILTER, true>(warps) : occ_of<RPD_PRED_FP32_FILTER, false>(warps);
-  return certify ? occ_of<RPD_PRED_FP64, true>(warps) : occ_of<RPD_PRED_FP64, false>(warps);
+template <int PRED, bool CERT>
+static int occ_variant(int variant, int warps) {
+  if (variant == 1) return occ_of<PRED, CERT, 6>(4);
+  if (variant == 2) return occ_of<PRED, CERT, 8>(4);
+  return occ_of<PRED, CERT, 0>(warps);
 }
 
-int clip_blocks_per_sm(int pred_mode, int warps) { return clip_blocks_per_sm_cert(pred_mode, 0, warps); }
+int clip_blocks_per_sm_cert(int pred_mode, int certify, int warps, int variant) {
+  if (pred_mode == RPD_PRED_FP32_FILTER)
+    return certify ? occ_variant<RPD_PRED_FP32_FILTER, true>(variant, warps)
+                   : occ_variant<RPD_PRED_FP32_FILTER, false>(variant, warps);
+  return certify ? occ_variant<RPD_PRED_FP64, true>(variant, warps)
+                 : occ_variant<RPD_PRED_FP64, false>(variant, warps);
+}
+
+int clip_blocks_per_sm(int pred_mode, int warps) {
+  return clip_blocks_per_sm_cert(pred_mode, 0, warps, 0);
+}
 
 int box_blocks_per_sm(int warps) {
   size_t smem = sizeof(WarpCell) * warps;
@@ -1069,23 +1084,31 @@ int box_blocks_per_sm(int warps) {
   return n > 0 ? n : 1;
 }
 
-template <int PRED, bool CERT>
+template <int PRED, bool CERT, int MINB>
 static void launch_one(const ClipParams& p, int blocks, int warps, cudaStream_t st) {
   size_t smem = sizeof(WarpCell) * warps;
-  cudaFuncSetAttribute(clip_cells_kernel<PRED, CERT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)smem);
-  clip_cells_kernel<PRED, CERT><<<blocks, warps * 32, smem, st>>>(p);
+  cudaFuncSetAttribute(clip_cells_kernel<PRED, CERT, MINB>,
+                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  clip_cells_kernel<PRED, CERT, MINB><<<blocks, warps * 32, smem, st>>>(p);
   note_launches(1);
 }
 
-cudaError_t launch_clip_cells(const ClipParams& p, int pred_mode, int certify, int blocks,
-                              int warps, cudaStream_t st) {
+template <int PRED, bool CERT>
+static void launch_variant(const ClipParams& p, int variant, int blocks, int warps,
+                           cudaStream_t st) {
+  if (variant == 1) launch_one<PRED, CERT, 6>(p, blocks, 4, st);
+  else if (variant == 2) launch_one<PRED, CERT, 8>(p, blocks, 4, st);
+  else launch_one<PRED, CERT, 0>(p, blocks, warps, st);
+}
+
+cudaError_t launch_clip_cells(const ClipParams& p, int pred_mode, int certify, int variant,
+                              int blocks, int warps, cudaStream_t st) {
   if (pred_mode == RPD_PRED_FP32_FILTER) {
-    if (certify) launch_one<RPD_PRED_FP32_FILTER, true>(p, blocks, warps, st);
-    else launch_one<RPD_PRED_FP32_FILTER, false>(p, blocks, warps, st);
+    if (certify) launch_variant<RPD_PRED_FP32_FILTER, true>(p, variant, blocks, warps, st);
+    else launch_variant<RPD_PRED_FP32_FILTER, false>(p, variant, blocks, warps, st);
   } else {
-    if (certify) launch_one<RPD_PRED_FP64, true>(p, blocks, warps, st);
-    else launch_one<RPD_PRED_FP64, false>(p, blocks, warps, st);
+    if (certify) launch_variant<RPD_PRED_FP64, true>(p, variant, blocks, warps, st);
+    else launch_variant<RPD_PRED_FP64, false>(p, variant, blocks, warps, st);
   }
   return cudaGetLastError();
 }

@@ -72,9 +72,11 @@ constexpr int kBoxPlanes = 48;
 size_t clip_smem_per_warp();
 int clip_blocks_per_sm(int pred_mode, int warps);
 int box_blocks_per_sm(int warps);
-cudaError_t launch_clip_cells(const ClipParams& p, int pred_mode, int certify, int blocks,
-                              int warps, cudaStream_t st);
-int clip_blocks_per_sm_cert(int pred_mode, int certify, int warps);
+// variant: 0 = no register cap (warps per block as given), 1 = at most 80
+// registers (6 blocks of 4 warps per SM), 2 = at most 64 (8 blocks of 4 warps)
+cudaError_t launch_clip_cells(const ClipParams& p, int pred_mode, int certify, int variant,
+                              int blocks, int warps, cudaStream_t st);
+int clip_blocks_per_sm_cert(int pred_mode, int certify, int warps, int variant);
 // indices of the pairs whose header status equals `status`
 cudaError_t select_pairs(const rpd_cell_header* h, long long n, int status, int32_t* flag_tmp,
                          int32_t* pos_tmp, int32_t* scan_tmp, int32_t* idx_out,

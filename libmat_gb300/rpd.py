@@ -38,7 +38,7 @@ EXPORTS = [
     "rpd_compute", "rpd_get_cells", "rpd_copy_cells_to_host", "rpd_copy_neighbors_to_host",
     "rpd_copy_pairs_to_host", "rpd_copy_pair_headers_to_host", "rpd_build_mesh_adjacency",
     "rpd_host_alloc", "rpd_host_free", "rpd_compact_cells_noalloc", "rpd_set_site_k",
-    "rpd_copy_topology_hashes_to_host",
+    "rpd_copy_topology_hashes_to_host", "rpd_autotune",
 ]
 
 
@@ -47,7 +47,8 @@ class Config(ctypes.Structure):
                 ("neighbor_source", ctypes.c_int), ("knn_k", ctypes.c_int),
                 ("clip_order", ctypes.c_int), ("compute_geometry", ctypes.c_int),
                 ("warps_per_block", ctypes.c_int), ("blocks_per_sm", ctypes.c_int),
-                ("certify", ctypes.c_int), ("reserved", ctypes.c_int * 7)]
+                ("certify", ctypes.c_int), ("clip_variant", ctypes.c_int),
+                ("reserved", ctypes.c_int * 6)]
 
 
 class Stats(ctypes.Structure):
@@ -66,6 +67,15 @@ class Stats(ctypes.Structure):
         d["search"] = [int(x) for x in self.search]
         d["status_counts"] = {STATUS_NAMES[i]: int(self.status_counts[i]) for i in range(10)}
         return d
+
+
+class Tuning(ctypes.Structure):
+    _fields_ = [("warps_per_block", ctypes.c_int), ("clip_variant", ctypes.c_int),
+                ("k_bucket", ctypes.c_int), ("n_candidates", ctypes.c_int),
+                ("ms_clip_best", ctypes.c_float), ("ms_clip_first", ctypes.c_float)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
 
 
 class CellsView(ctypes.Structure):
@@ -118,6 +128,8 @@ def load(path=LIB_PATH):
     L.rpd_copy_pair_headers_to_host.argtypes = [vp, vp, i64, c.POINTER(i64)]
     L.rpd_compact_cells_noalloc.restype = i32
     L.rpd_compact_cells_noalloc.argtypes = [vp, i64, vp, vp, vp, vp]
+    L.rpd_autotune.restype = i32
+    L.rpd_autotune.argtypes = [vp, i32, c.POINTER(Tuning)]
     L.rpd_set_site_k.restype = i32
     L.rpd_set_site_k.argtypes = [vp, vp, i32]
     L.rpd_copy_topology_hashes_to_host.restype = i32
@@ -167,7 +179,7 @@ class RPD:
 
     def __init__(self, device=0, predicate_mode=PRED_FP32_FILTER, neighbor_source=NEIGH_KNN,
                  knn_k=64, clip_order=ORDER_SITE_ID, compute_geometry=True,
-                 warps_per_block=0, blocks_per_sm=0, certify=False):
+                 warps_per_block=0, blocks_per_sm=0, certify=False, clip_variant=0):
         L = load()
         cfg = Config()
         L.rpd_config_default(ctypes.byref(cfg))
@@ -180,6 +192,7 @@ class RPD:
         cfg.warps_per_block = warps_per_block
         cfg.blocks_per_sm = blocks_per_sm
         cfg.certify = 1 if certify else 0
+        cfg.clip_variant = clip_variant
         h = ctypes.c_void_p()
         s = L.rpd_create(ctypes.byref(cfg), ctypes.byref(h))
         if s != 0:
@@ -236,6 +249,12 @@ class RPD:
             return
         a = np.ascontiguousarray(k_per_site, np.int32)
         self._check(self._L.rpd_set_site_k(self._h, _p(a), 0))
+
+    def autotune(self, repeats=2):
+        """Picks the fastest clip launch configuration on the current inputs."""
+        t = Tuning()
+        self._check(self._L.rpd_autotune(self._h, repeats, ctypes.byref(t)))
+        return t
 
     def topology_hashes(self):
         n = ctypes.c_int64()

@@ -67,3 +67,18 @@ def test_short_lists_are_reclipped():
     assert st.n_reclipped > 0
     assert np.array_equal(h_full["status"], h_short["status"])
     assert np.array_equal(t_full, t_short)
+
+
+def test_autotune_keeps_cells():
+    cfg = W.config_small_cube(n=12, n_site=800, seed=25)
+    with engine(cfg, knn_k=64, certify=True) as r:
+        r.compute()
+        base = r.topology_hashes()
+        hb = r.pair_headers()
+        t = r.autotune(repeats=1)
+        assert t.n_candidates >= 6
+        assert t.warps_per_block in (2, 4, 8) and t.clip_variant in (0, 1, 2)
+        assert t.k_bucket in (0, 16, 32)
+        r.compute()
+        assert np.array_equal(r.topology_hashes(), base)
+        assert np.array_equal(r.pair_headers()["status"], hb["status"])
