@@ -80,7 +80,12 @@ typedef struct rpd_config {
   int clip_variant;      /* clip kernel register budget: 0 none (occupancy
                             set by registers), 1 = 80 registers (6 blocks of
                             4 warps per SM), 2 = 64 registers (8 blocks) */
-  int reserved[6];
+  int learned_k;         /* 1 (with certify): per-cell list lengths from the
+                            trained k-predictor (rpd_mlp_train); the first
+                            pass clips that many list entries and tests the
+                            certificate once, cells where it fails are
+                            clipped again with the whole list */
+  int reserved[5];
 } rpd_config;
 
 /* One record per candidate (tet, site) pair; 32 bytes. */
@@ -120,9 +125,12 @@ typedef struct rpd_stats {
    * the grown-cell planes, [2] tets enumerated, [3] tets inside the grown
    * cell (rule evaluated), [4] pairs, [5] site boxes without planes */
   int64_t search[6];
-  int64_t n_reclipped;        /* cells whose shortened list (rpd_set_site_k)
-                                 ran out before the certificate held, clipped
-                                 again with the whole list */
+  int64_t n_reclipped;        /* cells whose shortened list (rpd_set_site_k
+                                 or learned_k) ran out before the certificate
+                                 held, clipped again with the whole list: the
+                                 predictor's misses */
+  float ms_predict;           /* learned_k: features + inference (in ms_clip) */
+  int32_t learned;            /* 1 if the learned list lengths were used */
 } rpd_stats;
 
 typedef struct rpd_cells_view {
@@ -208,6 +216,15 @@ rpd_status rpd_copy_cells_to_host(struct rpd_ctx* ctx, rpd_cell_header* headers,
 rpd_status rpd_copy_pair_headers_to_host(struct rpd_ctx* ctx, rpd_cell_header* headers,
                                          int64_t capacity, int64_t* n_pairs);
 
+/* Caller-supplied list length of every candidate pair (certify only): the
+ * next rpd_compute clips pair q with the first k_per_pair[q] entries of its
+ * site's distance-ordered list, tests the certificate once, and clips the
+ * cells where it fails again with the whole list.  n_pairs must equal the
+ * compute's pair count (pairs are in (tet, site) order, as in
+ * rpd_copy_pair_headers_to_host).  NULL clears.  The k-predictor
+ * (learned_k) takes precedence. */
+rpd_status rpd_set_pair_k(struct rpd_ctx* ctx, const int32_t* k_per_pair, int64_t n_pairs);
+
 /* Canonical topology hash of every pair of the last rpd_compute (0 for
  * dropped cells): the sum over the cell's vertices of a hash of the sorted
  * face keys (clip_id2) of its three planes and its #adjacent cells.  Equal
@@ -244,6 +261,80 @@ rpd_status rpd_copy_pairs_to_host(struct rpd_ctx* ctx, int32_t* tet_offsets,
 rpd_status rpd_compact_cells_noalloc(const rpd_cell_header* pair_headers, int64_t n_pairs,
                                      rpd_cell_header* cells_out, int64_t* n_cells_out,
                                      uint64_t* status_counts, void* stream);
+
+/* ---- Learned list length (k-predictor) ----------------------------------
+ * No counterpart in the reference, whose lists have a fixed length.  A
+ * 12 -> 64 -> 64 -> 1 MLP (bf16 operands, fp32 accumulation, tensor-core
+ * mma) predicts log2 of the number of distance-ordered list entries a cell
+ * takes before its security-radius certificate holds.  Parameters are fp32,
+ * RPD_MLP_PARAMS of them: W1 [16][64] (feature x hidden), b1 [64], W2
+ * [64][64] (in x out), b2 [64], w3 [64], b3.  Features are 16 bf16 values
+ * per cell (12 used, 4 zero); bf16 crosses this interface as uint16_t bit
+ * patterns. */
+#define RPD_MLP_FEATURES 16
+#define RPD_MLP_PARAMS 5313
+
+/* Clips the current mesh and sites with the whole distance-ordered lists
+ * and the certificate (cells identical to the plain path's), then appends up
+ * to max_samples of the emitted cells (evenly strided over the pairs) to the
+ * context's training set: features and label log2(max(k*, 1)), k* the list
+ * entries the cell took.  Requires certify = 1 and RPD_NEIGH_KNN.  Call it
+ * on several meshes and site sets before rpd_mlp_train.  n_total receives
+ * the size of the training set. */
+rpd_status rpd_mlp_collect(struct rpd_ctx* ctx, int64_t max_samples, int64_t* n_total);
+rpd_status rpd_mlp_clear_samples(struct rpd_ctx* ctx);
+/* The training set (x: n x RPD_MLP_FEATURES bf16, labels y); NULL buffers
+ * query its size. */
+rpd_status rpd_mlp_copy_samples(struct rpd_ctx* ctx, uint16_t* x, float* y, int64_t capacity,
+                                int64_t* n_samples);
+
+typedef struct rpd_mlp_report {
+  int64_t n_train;         /* samples trained on */
+  int64_t n_calib;         /* held-out samples that set the margin */
+  float loss_first;        /* mean squared error (log2 units), first epoch */
+  float loss_last;         /* last epoch */
+  float calib_loss;        /* held-out mean squared error */
+  float margin;            /* added to the prediction before 2^(.) */
+  float calib_miss_rate;   /* held-out cells whose k* exceeds the predicted length */
+  float calib_mean_k;      /* mean predicted length over the held-out cells */
+  float const_k;           /* one length for all cells with the same miss rate */
+  float ms_train;          /* device time of the training loop */
+  int32_t steps;           /* optimiser steps */
+  int32_t epochs;
+  float label_var;         /* variance of the labels (the error of predicting their mean) */
+} rpd_mlp_report;
+
+/* Trains the predictor on the GPU (own forward/backward kernels, Adam,
+ * mini-batches of `batch` samples, `epochs` passes, learning rate lr) from
+ * a fresh initialisation drawn from `seed`.  A random 10% of the samples
+ * is held out: the margin is the (1 - miss_target) quantile of their
+ * residuals, so about miss_target of the cells are clipped twice. */
+rpd_status rpd_mlp_train(struct rpd_ctx* ctx, int epochs, int batch, float lr, float miss_target,
+                         uint64_t seed, rpd_mlp_report* report);
+
+/* Switches rpd_config.learned_k of a context (on = 0 or 1; 1 needs
+ * certify). */
+rpd_status rpd_mlp_enable(struct rpd_ctx* ctx, int on);
+
+/* Saves / loads the parameters (fp32, RPD_MLP_PARAMS) and the margin. */
+rpd_status rpd_mlp_get_params(struct rpd_ctx* ctx, float* params, int n_params, float* margin);
+rpd_status rpd_mlp_set_params(struct rpd_ctx* ctx, const float* params, int n_params,
+                              float margin);
+
+/* The network on caller rows (host buffers, n x RPD_MLP_FEATURES bf16):
+ * outputs y, and the gradient of mean((y - target)^2) (grads receives
+ * RPD_MLP_PARAMS floats, loss the mean squared error). */
+rpd_status rpd_mlp_forward(struct rpd_ctx* ctx, const uint16_t* x, int64_t n, float* y);
+rpd_status rpd_mlp_gradient(struct rpd_ctx* ctx, const uint16_t* x, const float* target,
+                            int64_t n, float* grads, float* loss);
+
+/* The feature rows of the last rpd_compute's pairs (learned_k, or the
+ * cells of the last rpd_mlp_collect), and the list lengths the predictor
+ * gave the pairs of the last learned_k compute (pair order). */
+rpd_status rpd_mlp_copy_features(struct rpd_ctx* ctx, uint16_t* x, int64_t capacity,
+                                 int64_t* n_rows);
+rpd_status rpd_mlp_copy_klen(struct rpd_ctx* ctx, int32_t* klen, int64_t capacity,
+                             int64_t* n_pairs);
 
 /* Page-locked host buffers for fast host<->device copies (cudaMallocHost);
  * NULL on failure. */

@@ -26,6 +26,7 @@ CUDA_UNITS = {
     "rpd_clip.cu": ["-fmad=false"],
     "rpd_pairs.cu": ["-fmad=false"],
     "rpd_noalloc.cu": [],
+    "rpd_mlp.cu": [],
 }
 CXX_UNITS = ["rpd_api.cpp", "rpd_mesh.cpp"]
 

@@ -15,6 +15,8 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <numeric>
+#include <random>
 #include <string>
 #include <vector>
 
@@ -40,14 +42,38 @@ struct DevBuf {
     if (e == cudaSuccess) cap = want;
     return e;
   }
+  // grows to n elements keeping the first `keep` (stream-ordered copy)
+  cudaError_t grow_keep(size_t n, size_t keep, cudaStream_t st) {
+    if (n <= cap && ptr) return cudaSuccess;
+    T* old = ptr;
+    size_t want = std::max<size_t>(n, std::max<size_t>(2 * cap, 1));
+    T* fresh = nullptr;
+    cudaError_t e = cudaMalloc((void**)&fresh, want * sizeof(T));
+    if (e != cudaSuccess) return e;
+    if (old && keep) {
+      e = cudaMemcpyAsync(fresh, old, keep * sizeof(T), cudaMemcpyDeviceToDevice, st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+      if (e != cudaSuccess) {
+        cudaFree(fresh);
+        return e;
+      }
+    }
+    if (old) cudaFree(old);
+    ptr = fresh;
+    cap = want;
+    return cudaSuccess;
+  }
   void release() {
     if (ptr) cudaFree(ptr);
     ptr = nullptr;
     cap = 0;
   }
+  ~DevBuf() { release(); }
 };
 
-enum Ev { kEvStart, kEvKnn, kEvPairs, kEvClipK0, kEvClipK1, kEvClip, kEvEnd, kEvCount };
+enum Ev {
+  kEvStart, kEvKnn, kEvPairs, kEvPred0, kEvPred1, kEvClipK0, kEvClipK1, kEvClip, kEvEnd, kEvCount
+};
 
 }  // namespace
 
@@ -115,6 +141,28 @@ struct rpd_ctx {
   DevBuf<long long> n_out;
   long long payload_cap_hint = 0;
 
+  // learned list length: features, predictor, training set
+  double mesh_volume = 0.0;
+  DevBuf<float4> bverts;        // boundary vertices
+  int n_bverts = 0;
+  DevBuf<float> site_bdist;     // site -> nearest boundary vertex distance
+  bool bdist_valid = false;
+  DevBuf<uint16_t> feat;        // bf16 rows of the last features launch
+  long long n_feat_rows = 0;
+  DevBuf<int32_t> pair_klen, consumed, sample_idx;
+  bool want_consumed = false;
+  bool last_learned = false;
+  DevBuf<int32_t> user_pair_k;   // rpd_set_pair_k
+  long long n_user_pair_k = -1;
+  DevBuf<float> mlp_params, mlp_grads, mlp_m, mlp_v, mlp_loss, mlp_y, mlp_target;
+  DevBuf<uint16_t> mlp_W1T, mlp_W2, mlp_W2T;
+  float mlp_margin = 0.f;
+  bool mlp_ready = false;
+  DevBuf<uint16_t> train_X;
+  DevBuf<float> train_y;
+  DevBuf<int32_t> train_idx;
+  long long n_train = 0;
+
   // results of the last compute
   long long n_pairs = 0, n_cells = 0, payload_bytes = 0;
   int tet_k = 0;
@@ -163,6 +211,58 @@ Grid make_grid(const double* lo, const double* hi, long long n_items, double per
   g.ny = n[1];
   g.nz = n[2];
   return g;
+}
+
+// bf16 features of n_rows pairs (pair_index[0..n_rows), or all pairs) into
+// c->feat; with `target`, the labels log2(max(consumed, 1)) as well
+rpd_status pair_features(rpd_ctx* c, const int32_t* pair_index, long long n_rows, float* target) {
+  cudaStream_t st = c->stream;
+  if (!c->bdist_valid) {
+    CK(c->site_bdist.ensure((size_t)c->n_site), "alloc");
+    CK(launch_boundary_distance(c->site4f.ptr, c->n_site, c->bverts.ptr, c->n_bverts,
+                                c->site_bdist.ptr, st), "boundary distance");
+    c->bdist_valid = true;
+  }
+  CK(c->feat.ensure((size_t)std::max<long long>(n_rows, 1) * kMlpFeatures), "alloc features");
+  FeatureParams fp;
+  fp.pair_tet = c->pair_tet.ptr;
+  fp.pair_site = c->pair_site.ptr;
+  fp.pair_index = pair_index;
+  fp.n_pairs = n_rows;
+  fp.site4f = c->site4f.ptr;
+  fp.vert3f = c->vert3f.ptr;
+  fp.tets = c->tets.ptr;
+  fp.centroid = c->centroid.ptr;
+  fp.keys = c->nbr_keys.ptr;
+  fp.k = c->k;
+  fp.cell_of = c->s_cell_of.ptr;
+  fp.cell_count = c->s_cell_count.ptr;
+  fp.site_bdist = c->site_bdist.ptr;
+  const double h = std::cbrt(std::max(c->mesh_volume, 1e-300) / (double)std::max(c->n_site, 1));
+  fp.inv_h = (float)(1.0 / h);
+  fp.X = c->feat.ptr;
+  fp.consumed = target ? c->consumed.ptr : nullptr;
+  fp.target = target;
+  CK(launch_pair_features(fp, st), "features");
+  c->n_feat_rows = n_rows;
+  return RPD_OK;
+}
+
+bool certify_on(const rpd_ctx* c) { return c->cfg.certify != 0; }
+
+MlpWeights mlp_view(const rpd_ctx* c) {
+  return mlp_weights_view(c->mlp_params.ptr, c->mlp_W1T.ptr, c->mlp_W2.ptr, c->mlp_W2T.ptr);
+}
+
+rpd_status mlp_alloc(rpd_ctx* c) {
+  CK(c->mlp_params.ensure(kMlpParams), "alloc");
+  CK(c->mlp_grads.ensure(kMlpParams), "alloc");
+  CK(c->mlp_m.ensure(kMlpParams), "alloc");
+  CK(c->mlp_v.ensure(kMlpParams), "alloc");
+  CK(c->mlp_W1T.ensure(kMlpFeatures * kMlpHidden), "alloc");
+  CK(c->mlp_W2.ensure(kMlpHidden * kMlpHidden), "alloc");
+  CK(c->mlp_W2T.ensure(kMlpHidden * kMlpHidden), "alloc");
+  return RPD_OK;
 }
 
 }  // namespace
@@ -215,6 +315,8 @@ rpd_status rpd_create(const rpd_config* cfg, rpd_ctx** out) {
     return RPD_ERR_INVALID_ARGUMENT;
   if (c0.certify && c0.neighbor_source != RPD_NEIGH_KNN) return RPD_ERR_INVALID_ARGUMENT;
   if (c0.clip_variant < 0 || c0.clip_variant > 2) return RPD_ERR_INVALID_ARGUMENT;
+  if (c0.learned_k < 0 || c0.learned_k > 1 || (c0.learned_k && !c0.certify))
+    return RPD_ERR_INVALID_ARGUMENT;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
     cudaGetLastError();
@@ -317,6 +419,29 @@ rpd_status rpd_set_mesh(rpd_ctx* c, const double* xyz, int n_vert, const int32_t
       crad[k] = std::max(crad[k], rad[t]);
     }
   }
+  // mesh volume and boundary vertices (vertices of faces with one tet; face
+  // f of a tet is the one opposite its vertex f)
+  double volume = 0.0;
+  std::vector<uint8_t> on_boundary((size_t)n_vert, 0);
+  for (long long t = 0; t < n_tet; ++t) {
+    const double* p0 = xyz + 3 * (long long)tets[4 * t];
+    double e[3][3];
+    for (int q = 1; q < 4; ++q)
+      for (int a = 0; a < 3; ++a) e[q - 1][a] = xyz[3 * (long long)tets[4 * t + q] + a] - p0[a];
+    volume += std::fabs(e[0][0] * (e[1][1] * e[2][2] - e[1][2] * e[2][1]) -
+                        e[0][1] * (e[1][0] * e[2][2] - e[1][2] * e[2][0]) +
+                        e[0][2] * (e[1][0] * e[2][1] - e[1][1] * e[2][0])) / 6.0;
+    for (int f = 0; f < 4; ++f)
+      if (f_adjs[4 * t + f] == 1)
+        for (int q = 0; q < 4; ++q)
+          if (q != f) on_boundary[(size_t)tets[4 * t + q]] = 1;
+  }
+  std::vector<float> bv;
+  for (long long v = 0; v < n_vert; ++v)
+    if (on_boundary[(size_t)v])
+      for (int a = 0; a < 4; ++a) bv.push_back(a < 3 ? vf[3 * v + a] : 0.f);
+  const int n_bv = (int)(bv.size() / 4);
+  CK(c->bverts.ensure((size_t)std::max(n_bv, 1)), "alloc boundary");
   CK(c->vert3f.ensure((size_t)n_vert * 3), "alloc vert3f");
   CK(c->vert3d.ensure((size_t)n_vert * 3), "alloc vert3d");
   CK(c->tets.ensure(n_tet), "alloc tets");
@@ -334,7 +459,12 @@ rpd_status rpd_set_mesh(rpd_ctx* c, const double* xyz, int n_vert, const int32_t
   CK(cudaMemcpyAsync(c->f_adjs.ptr, f_adjs, (size_t)n_tet * 16, cudaMemcpyHostToDevice, st), "H2D f_adjs");
   CK(cudaMemcpyAsync(c->f_ids.ptr, f_ids, (size_t)n_tet * 16, cudaMemcpyHostToDevice, st), "H2D f_ids");
   CK(cudaMemcpyAsync(c->tet_class.ptr, cls.data(), (size_t)n_tet, cudaMemcpyHostToDevice, st), "H2D classes");
+  if (n_bv > 0)
+    CK(cudaMemcpyAsync(c->bverts.ptr, bv.data(), bv.size() * 4, cudaMemcpyHostToDevice, st), "H2D boundary");
   CK(cudaStreamSynchronize(st), "set_mesh sync");
+  c->n_bverts = n_bv;
+  c->mesh_volume = volume;
+  c->bdist_valid = false;
   for (int k = 0; k < rpd_ctx::kClasses; ++k) {
     c->class_count[k] = ccount[k];
     c->class_radius[k] = crad[k];
@@ -390,6 +520,7 @@ rpd_status rpd_set_sites(rpd_ctx* c, const double* xyzw, int n_site, const uint3
     c->site_hi[a] = hi[a];
   }
   c->w_max = wmax;
+  c->bdist_valid = false;
   c->has_sites = true;
   c->has_result = false;
   return RPD_OK;
@@ -431,6 +562,12 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
   const bool knn = c->cfg.neighbor_source == RPD_NEIGH_KNN;
   if (!knn && !c->has_user_nbr)
     return fail(c, RPD_ERR_NOT_READY, "rpd_compute: neighbour lists required (rpd_set_neighbors)");
+  const bool learned = c->cfg.learned_k != 0;
+  if (learned && (!c->cfg.certify || !knn))
+    return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_compute: learned_k needs certify and GPU-built lists");
+  if (learned && !c->mlp_ready)
+    return fail(c, RPD_ERR_NOT_READY,
+                "rpd_compute: learned_k needs a predictor (rpd_mlp_train or rpd_mlp_set_params)");
   CK(cudaSetDevice(c->device), "cudaSetDevice");
   cudaStream_t st = c->stream;
   const int n_site = c->n_site, n_tet = c->n_tet;
@@ -577,8 +714,24 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
   }
   CK(cudaEventRecord(c->ev[kEvPairs], st), "event");
 
-  // ---- clipping
+  // ---- learned list lengths: features and inference per pair
   const long long n_pairs = c->n_pairs;
+  CK(cudaEventRecord(c->ev[kEvPred0], st), "event");
+  if (learned && n_pairs > 0) {
+    rpd_status fs = pair_features(c, nullptr, n_pairs, nullptr);
+    if (fs != RPD_OK) return fs;
+    CK(c->pair_klen.ensure((size_t)n_pairs), "alloc");
+    CK(launch_mlp_predict(c->feat.ptr, nullptr, n_pairs, mlp_view(c), c->mlp_margin, 1, c->k,
+                          c->pair_klen.ptr, nullptr, st), "predict");
+  }
+  const bool use_pair_k = !learned && certify_on(c) && c->n_user_pair_k >= 0;
+  if (use_pair_k && c->n_user_pair_k != n_pairs)
+    return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_compute: rpd_set_pair_k lengths do not match the pairs");
+  CK(cudaEventRecord(c->ev[kEvPred1], st), "event");
+  c->last_learned = learned;
+  if (c->want_consumed) CK(c->consumed.ensure((size_t)std::max<long long>(n_pairs, 1)), "alloc");
+
+  // ---- clipping
   CK(c->pair_headers.ensure((size_t)std::max<long long>(n_pairs, 1)), "alloc headers");
   CK(c->topo_hash.ensure((size_t)std::max<long long>(n_pairs, 1)), "alloc hashes");
   long long pcap = c->payload_cap_hint > 0 ? c->payload_cap_hint
@@ -600,6 +753,7 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
   const float cert_margin = (float)(16.0 * std::ldexp(1.0, -24) * (L + std::sqrt(D2)) + 1e-30);
   c->n_reclipped = 0;
   for (int attempt = 0; attempt < 3; ++attempt) {
+    CK(cudaMemsetAsync(c->scratch.ptr + 28, 0, sizeof(unsigned long long), st), "memset");
     CK(c->payload.ensure((size_t)pcap), "alloc payload");
     CK(cudaMemsetAsync(c->scratch.ptr, 0, 4 * sizeof(unsigned long long), st), "memset");
     ClipParams p;
@@ -625,7 +779,11 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
     p.counters = c->scratch.ptr + 2;
     p.geometry = c->cfg.compute_geometry;
     p.keys = certify ? c->nbr_keys.ptr : nullptr;
-    p.site_klen = (certify && c->has_site_klen) ? c->site_klen.ptr : nullptr;
+    p.site_klen = (certify && c->has_site_klen && !learned && !use_pair_k) ? c->site_klen.ptr : nullptr;
+    p.pair_klen = learned ? c->pair_klen.ptr : (use_pair_k ? c->user_pair_k.ptr : nullptr);
+    p.lazy_cert = (learned || use_pair_k) ? 1 : 0;
+    p.misses = c->scratch.ptr + 28;
+    p.consumed = (certify && c->want_consumed) ? c->consumed.ptr : nullptr;
     p.cert_margin = cert_margin;
     p.pair_index = nullptr;
     p.n_work = n_pairs;
@@ -633,7 +791,7 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
     CK(cudaEventRecord(c->ev[kEvClipK0], st), "event");
     if (n_pairs > 0) CK(launch_clip_cells(p, c->cfg.predicate_mode, certify, variant, blocks, warps, st), "clip");
     CK(cudaEventRecord(c->ev[kEvClipK1], st), "event");
-    if (p.site_klen && n_pairs > 0) {
+    if ((p.site_klen || p.pair_klen) && n_pairs > 0) {
       // cells whose shortened list was not enough: clip them again whole
       CK(c->flag_tmp.ensure((size_t)n_pairs + 1), "alloc");
       CK(c->pos_tmp.ensure((size_t)n_pairs + 1), "alloc");
@@ -648,6 +806,8 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
       if (n_re > 0) {
         CK(cudaMemsetAsync(c->scratch.ptr + 1, 0, sizeof(unsigned long long), st), "memset");
         p.site_klen = nullptr;
+        p.pair_klen = nullptr;
+        p.lazy_cert = 0;
         p.pair_index = c->reclip_idx.ptr;
         p.n_work = n_re;
         CK(launch_clip_cells(p, c->cfg.predicate_mode, certify, variant, blocks, warps, st), "reclip");
@@ -703,6 +863,8 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
     for (int i = 0; i < 6; ++i) stats->search[i] = (int64_t)host_scratch[20 + i];
     stats->search[4] = c->n_pairs;
     stats->n_reclipped = c->n_reclipped;
+    cudaEventElapsedTime(&stats->ms_predict, c->ev[kEvPred0], c->ev[kEvPred1]);
+    stats->learned = learned ? 1 : 0;
   }
   return RPD_OK;
 }
@@ -851,6 +1013,24 @@ rpd_status rpd_set_site_k(rpd_ctx* c, const int32_t* k_per_site, int on_device) 
   return RPD_OK;
 }
 
+rpd_status rpd_set_pair_k(rpd_ctx* c, const int32_t* k_per_pair, int64_t n_pairs) {
+  if (!c) return RPD_ERR_INVALID_ARGUMENT;
+  if (!k_per_pair) {
+    c->n_user_pair_k = -1;
+    return RPD_OK;
+  }
+  if (!c->cfg.certify) return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_set_pair_k: needs certify");
+  if (n_pairs < 0) return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_set_pair_k: n_pairs < 0");
+  for (int64_t i = 0; i < n_pairs; ++i)
+    if (k_per_pair[i] < 1) return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_set_pair_k: lengths must be >= 1");
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  CK(c->user_pair_k.ensure((size_t)std::max<int64_t>(n_pairs, 1)), "alloc");
+  if (n_pairs > 0)
+    CK(cudaMemcpy(c->user_pair_k.ptr, k_per_pair, sizeof(int32_t) * (size_t)n_pairs, cudaMemcpyHostToDevice), "H2D");
+  c->n_user_pair_k = n_pairs;
+  return RPD_OK;
+}
+
 rpd_status rpd_copy_topology_hashes_to_host(rpd_ctx* c, uint64_t* hashes, int64_t capacity,
                                             int64_t* n_pairs) {
   if (!c) return RPD_ERR_INVALID_ARGUMENT;
@@ -908,6 +1088,318 @@ rpd_status rpd_copy_pairs_to_host(rpd_ctx* c, int32_t* tet_offsets, int32_t* pai
     CK(cudaMemcpyAsync(pair_sites, c->pair_site.ptr, sizeof(int32_t) * (size_t)c->n_pairs,
                        cudaMemcpyDeviceToHost, c->stream), "D2H");
   CK(cudaStreamSynchronize(c->stream), "sync");
+  return RPD_OK;
+}
+
+// ---------------------------------------------------------------------------
+// learned list length
+// ---------------------------------------------------------------------------
+rpd_status rpd_mlp_collect(rpd_ctx* c, int64_t max_samples, int64_t* n_total) {
+  if (!c) return RPD_ERR_INVALID_ARGUMENT;
+  if (max_samples < 0) return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_mlp_collect: max_samples < 0");
+  if (!c->cfg.certify || c->cfg.neighbor_source != RPD_NEIGH_KNN)
+    return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_mlp_collect: needs certify and GPU-built lists");
+  // the plain method's cells: whole lists, certificate tested as it goes
+  const rpd_config saved = c->cfg;
+  const bool saved_klen = c->has_site_klen;
+  const long long saved_pair_k = c->n_user_pair_k;
+  c->cfg.learned_k = 0;
+  c->has_site_klen = false;
+  c->n_user_pair_k = -1;
+  c->want_consumed = true;
+  rpd_status s = rpd_compute(c, nullptr);
+  c->want_consumed = false;
+  c->cfg = saved;
+  c->has_site_klen = saved_klen;
+  c->n_user_pair_k = saved_pair_k;
+  if (s != RPD_OK) return s;
+  cudaStream_t st = c->stream;
+  const long long n_pairs = c->n_pairs;
+  if (n_pairs > 0 && max_samples > 0) {
+    CK(c->reclip_idx.ensure((size_t)n_pairs), "alloc");
+    CK(select_pairs(c->pair_headers.ptr, n_pairs, kSuccess, c->flag_tmp.ptr, c->pos_tmp.ptr,
+                    c->scan_tmp.ptr, c->reclip_idx.ptr, st), "select");
+    int32_t n_sel = 0;
+    CK(cudaMemcpyAsync(&n_sel, c->pos_tmp.ptr + n_pairs, sizeof(n_sel), cudaMemcpyDeviceToHost, st), "D2H");
+    CK(cudaStreamSynchronize(st), "collect sync");
+    if (n_sel > 0) {
+      // every stride-th emitted cell in (tet, site) order
+      const long long stride = (n_sel + max_samples - 1) / max_samples;
+      const long long take = (n_sel + stride - 1) / stride;
+      std::vector<int32_t> sel((size_t)n_sel), sub((size_t)take);
+      CK(cudaMemcpy(sel.data(), c->reclip_idx.ptr, sizeof(int32_t) * sel.size(), cudaMemcpyDeviceToHost), "D2H");
+      for (long long q = 0; q < take; ++q) sub[(size_t)q] = sel[(size_t)(q * stride)];
+      CK(c->sample_idx.ensure((size_t)take), "alloc");
+      CK(c->mlp_target.ensure((size_t)take), "alloc");
+      CK(cudaMemcpyAsync(c->sample_idx.ptr, sub.data(), sizeof(int32_t) * sub.size(), cudaMemcpyHostToDevice, st), "H2D");
+      s = pair_features(c, c->sample_idx.ptr, take, c->mlp_target.ptr);
+      if (s != RPD_OK) return s;
+      const size_t nf = kMlpFeatures;
+      CK(c->train_X.grow_keep((size_t)(c->n_train + take) * nf, (size_t)c->n_train * nf, st), "alloc");
+      CK(c->train_y.grow_keep((size_t)(c->n_train + take), (size_t)c->n_train, st), "alloc");
+      CK(cudaMemcpyAsync(c->train_X.ptr + (size_t)c->n_train * nf, c->feat.ptr,
+                         sizeof(uint16_t) * nf * (size_t)take, cudaMemcpyDeviceToDevice, st), "D2D");
+      CK(cudaMemcpyAsync(c->train_y.ptr + c->n_train, c->mlp_target.ptr, sizeof(float) * (size_t)take,
+                         cudaMemcpyDeviceToDevice, st), "D2D");
+      CK(cudaStreamSynchronize(st), "collect sync");
+      c->n_train += take;
+    }
+  }
+  if (n_total) *n_total = c->n_train;
+  return RPD_OK;
+}
+
+rpd_status rpd_mlp_clear_samples(rpd_ctx* c) {
+  if (!c) return RPD_ERR_INVALID_ARGUMENT;
+  c->n_train = 0;
+  return RPD_OK;
+}
+
+rpd_status rpd_mlp_copy_samples(rpd_ctx* c, uint16_t* x, float* y, int64_t capacity,
+                                int64_t* n_samples) {
+  if (!c) return RPD_ERR_INVALID_ARGUMENT;
+  if (n_samples) *n_samples = c->n_train;
+  if (!x && !y) return RPD_OK;
+  if (capacity < c->n_train) return fail(c, RPD_ERR_CAPACITY, "rpd_mlp_copy_samples: buffer too small");
+  if (c->n_train == 0) return RPD_OK;
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  if (x)
+    CK(cudaMemcpy(x, c->train_X.ptr, sizeof(uint16_t) * kMlpFeatures * (size_t)c->n_train,
+                  cudaMemcpyDeviceToHost), "D2H");
+  if (y) CK(cudaMemcpy(y, c->train_y.ptr, sizeof(float) * (size_t)c->n_train, cudaMemcpyDeviceToHost), "D2H");
+  return RPD_OK;
+}
+
+rpd_status rpd_mlp_train(rpd_ctx* c, int epochs, int batch, float lr, float miss_target,
+                         uint64_t seed, rpd_mlp_report* report) {
+  if (!c) return RPD_ERR_INVALID_ARGUMENT;
+  if (epochs < 1 || batch < 16 || !(lr > 0.f) || !(miss_target > 0.f && miss_target < 1.f))
+    return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_mlp_train: bad arguments");
+  if (c->n_train < 64) return fail(c, RPD_ERR_NOT_READY, "rpd_mlp_train: collect samples first");
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  cudaStream_t st = c->stream;
+  rpd_status s = mlp_alloc(c);
+  if (s != RPD_OK) return s;
+  const long long n = c->n_train;
+  std::vector<float> y_all((size_t)n);
+  CK(cudaMemcpy(y_all.data(), c->train_y.ptr, sizeof(float) * (size_t)n, cudaMemcpyDeviceToHost), "D2H");
+  // initialisation: uniform(+-sqrt(6 / fan_in)) weights (fan_in 12 for the
+  // used features), zero biases, b3 = mean label
+  std::mt19937_64 rng(seed);
+  std::vector<float> prm((size_t)kMlpParams, 0.f);
+  {
+    std::uniform_real_distribution<float> u1(-std::sqrt(6.f / 12.f), std::sqrt(6.f / 12.f));
+    std::uniform_real_distribution<float> u2(-std::sqrt(6.f / 64.f), std::sqrt(6.f / 64.f));
+    std::uniform_real_distribution<float> u3(-std::sqrt(1.f / 64.f), std::sqrt(1.f / 64.f));
+    size_t o = 0;
+    for (int f = 0; f < kMlpFeatures; ++f)
+      for (int h = 0; h < kMlpHidden; ++h) prm[o++] = f < 12 ? u1(rng) : 0.f;
+    o += kMlpHidden;  // b1
+    for (int e = 0; e < kMlpHidden * kMlpHidden; ++e) prm[o++] = u2(rng);
+    o += kMlpHidden;  // b2
+    for (int e = 0; e < kMlpHidden; ++e) prm[o++] = u3(rng);
+    double mean = 0.0;
+    for (float v : y_all) mean += v;
+    prm[o] = (float)(mean / (double)n);
+  }
+  CK(cudaMemcpyAsync(c->mlp_params.ptr, prm.data(), sizeof(float) * prm.size(), cudaMemcpyHostToDevice, st), "H2D");
+  CK(cudaMemsetAsync(c->mlp_grads.ptr, 0, sizeof(float) * kMlpParams, st), "memset");
+  CK(cudaMemsetAsync(c->mlp_m.ptr, 0, sizeof(float) * kMlpParams, st), "memset");
+  CK(cudaMemsetAsync(c->mlp_v.ptr, 0, sizeof(float) * kMlpParams, st), "memset");
+  CK(launch_mlp_sync_operands(c->mlp_params.ptr, c->mlp_W1T.ptr, c->mlp_W2.ptr, c->mlp_W2T.ptr, st), "sync");
+  // a random tenth held out for the margin
+  std::vector<int32_t> perm((size_t)n);
+  std::iota(perm.begin(), perm.end(), 0);
+  std::shuffle(perm.begin(), perm.end(), rng);
+  const long long n_cal = std::max<long long>(16, n / 10);
+  const long long n_tr = n - n_cal;
+  std::vector<int32_t> cal(perm.begin(), perm.begin() + n_cal), tr(perm.begin() + n_cal, perm.end());
+  CK(c->train_idx.ensure((size_t)n), "alloc");
+  CK(c->mlp_loss.ensure((size_t)epochs), "alloc");
+  CK(cudaMemsetAsync(c->mlp_loss.ptr, 0, sizeof(float) * (size_t)epochs, st), "memset");
+  const MlpWeights w = mlp_view(c);
+  CK(cudaEventRecord(c->ev[kEvStart], st), "event");
+  int step = 0;
+  for (int e = 0; e < epochs; ++e) {
+    std::shuffle(tr.begin(), tr.end(), rng);
+    // pageable source: the call returns once the indices are staged
+    CK(cudaMemcpyAsync(c->train_idx.ptr, tr.data(), sizeof(int32_t) * tr.size(), cudaMemcpyHostToDevice, st), "H2D");
+    for (long long b = 0; b < n_tr; b += batch) {
+      const long long nb = std::min<long long>(batch, n_tr - b);
+      CK(launch_mlp_grad(c->train_X.ptr, c->train_y.ptr, c->train_idx.ptr + b, nb, 1.0f / (float)nb,
+                         w, c->mlp_grads.ptr, c->mlp_loss.ptr + e, st), "grad");
+      CK(launch_mlp_adam(c->mlp_params.ptr, c->mlp_grads.ptr, c->mlp_m.ptr, c->mlp_v.ptr, ++step, lr,
+                         c->mlp_W1T.ptr, c->mlp_W2.ptr, c->mlp_W2T.ptr, st), "adam");
+    }
+    CK(cudaStreamSynchronize(st), "epoch sync");  // tr is reshuffled next
+  }
+  CK(cudaEventRecord(c->ev[kEvEnd], st), "event");
+  std::vector<float> losses((size_t)epochs);
+  CK(cudaMemcpyAsync(losses.data(), c->mlp_loss.ptr, sizeof(float) * losses.size(), cudaMemcpyDeviceToHost, st), "D2H");
+  // held-out predictions
+  CK(c->sample_idx.ensure((size_t)n_cal), "alloc");
+  CK(c->mlp_y.ensure((size_t)n_cal), "alloc");
+  CK(cudaMemcpyAsync(c->sample_idx.ptr, cal.data(), sizeof(int32_t) * cal.size(), cudaMemcpyHostToDevice, st), "H2D");
+  CK(launch_mlp_predict(c->train_X.ptr, c->sample_idx.ptr, n_cal, w, 0.f, 1, 1 << 20, nullptr,
+                        c->mlp_y.ptr, st), "predict");
+  std::vector<float> yc((size_t)n_cal);
+  CK(cudaMemcpyAsync(yc.data(), c->mlp_y.ptr, sizeof(float) * yc.size(), cudaMemcpyDeviceToHost, st), "D2H");
+  CK(cudaStreamSynchronize(st), "train sync");
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, c->ev[kEvStart], c->ev[kEvEnd]);
+  // margin: the (1 - miss_target) quantile of label - prediction
+  std::vector<float> resid((size_t)n_cal);
+  std::vector<int> kstar((size_t)n_cal);
+  double cal_loss = 0.0;
+  for (long long q = 0; q < n_cal; ++q) {
+    const float t = y_all[(size_t)cal[(size_t)q]];
+    resid[(size_t)q] = t - yc[(size_t)q];
+    cal_loss += (double)resid[(size_t)q] * resid[(size_t)q];
+    kstar[(size_t)q] = (int)std::lround(std::exp2((double)t));
+  }
+  std::vector<float> rs(resid);
+  std::sort(rs.begin(), rs.end());
+  const long long qi = std::min<long long>(n_cal - 1, (long long)std::ceil((1.0 - miss_target) * (double)n_cal) - 1);
+  const float margin = rs[(size_t)std::max<long long>(qi, 0)] + 1e-4f;
+  const int kmax = std::max(c->k, 1);
+  long long miss = 0;
+  double sum_k = 0.0;
+  for (long long q = 0; q < n_cal; ++q) {
+    int kk = (int)std::ceil(std::exp2(std::min(yc[(size_t)q] + margin, 10.0f)));
+    kk = std::min(std::max(kk, 1), kmax);
+    sum_k += kk;
+    if (kstar[(size_t)q] > kk) ++miss;
+  }
+  std::vector<int> ks(kstar);
+  std::sort(ks.begin(), ks.end());
+  const int const_k = ks[(size_t)std::max<long long>(qi, 0)];
+  c->mlp_margin = margin;
+  c->mlp_ready = true;
+  if (report) {
+    std::memset(report, 0, sizeof(*report));
+    report->n_train = n_tr;
+    report->n_calib = n_cal;
+    report->loss_first = losses.front() / (float)n_tr;
+    report->loss_last = losses.back() / (float)n_tr;
+    report->calib_loss = (float)(cal_loss / (double)n_cal);
+    report->margin = margin;
+    report->calib_miss_rate = (float)miss / (float)n_cal;
+    report->calib_mean_k = (float)(sum_k / (double)n_cal);
+    report->const_k = (float)std::min(const_k, kmax);
+    report->ms_train = ms;
+    report->steps = step;
+    report->epochs = epochs;
+    double mu = 0.0, m2 = 0.0;
+    for (float v : y_all) mu += v;
+    mu /= (double)n;
+    for (float v : y_all) m2 += ((double)v - mu) * ((double)v - mu);
+    report->label_var = (float)(m2 / (double)n);
+  }
+  return RPD_OK;
+}
+
+rpd_status rpd_mlp_enable(rpd_ctx* c, int on) {
+  if (!c) return RPD_ERR_INVALID_ARGUMENT;
+  if (on != 0 && on != 1) return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_mlp_enable: on must be 0 or 1");
+  if (on && !c->cfg.certify) return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_mlp_enable: needs certify");
+  c->cfg.learned_k = on;
+  return RPD_OK;
+}
+
+rpd_status rpd_mlp_get_params(rpd_ctx* c, float* params, int n_params, float* margin) {
+  if (!c) return RPD_ERR_INVALID_ARGUMENT;
+  if (!c->mlp_ready) return fail(c, RPD_ERR_NOT_READY, "rpd_mlp_get_params: no predictor");
+  if (params && n_params < kMlpParams) return fail(c, RPD_ERR_CAPACITY, "rpd_mlp_get_params: buffer too small");
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  if (params)
+    CK(cudaMemcpy(params, c->mlp_params.ptr, sizeof(float) * kMlpParams, cudaMemcpyDeviceToHost), "D2H");
+  if (margin) *margin = c->mlp_margin;
+  return RPD_OK;
+}
+
+rpd_status rpd_mlp_set_params(rpd_ctx* c, const float* params, int n_params, float margin) {
+  if (!c) return RPD_ERR_INVALID_ARGUMENT;
+  if (!params || n_params != kMlpParams || !std::isfinite(margin))
+    return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_mlp_set_params: expected RPD_MLP_PARAMS floats");
+  for (int i = 0; i < n_params; ++i)
+    if (!std::isfinite(params[i])) return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_mlp_set_params: non-finite parameter");
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  rpd_status s = mlp_alloc(c);
+  if (s != RPD_OK) return s;
+  cudaStream_t st = c->stream;
+  CK(cudaMemcpyAsync(c->mlp_params.ptr, params, sizeof(float) * kMlpParams, cudaMemcpyHostToDevice, st), "H2D");
+  CK(launch_mlp_sync_operands(c->mlp_params.ptr, c->mlp_W1T.ptr, c->mlp_W2.ptr, c->mlp_W2T.ptr, st), "sync");
+  CK(cudaStreamSynchronize(st), "set_params sync");
+  c->mlp_margin = margin;
+  c->mlp_ready = true;
+  return RPD_OK;
+}
+
+rpd_status rpd_mlp_forward(rpd_ctx* c, const uint16_t* x, int64_t n, float* y) {
+  if (!c) return RPD_ERR_INVALID_ARGUMENT;
+  if (n < 0 || (n > 0 && (!x || !y))) return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_mlp_forward: bad arguments");
+  if (!c->mlp_ready) return fail(c, RPD_ERR_NOT_READY, "rpd_mlp_forward: no predictor");
+  if (n == 0) return RPD_OK;
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  cudaStream_t st = c->stream;
+  CK(c->feat.ensure((size_t)n * kMlpFeatures), "alloc");
+  CK(c->mlp_y.ensure((size_t)n), "alloc");
+  CK(cudaMemcpyAsync(c->feat.ptr, x, sizeof(uint16_t) * kMlpFeatures * (size_t)n, cudaMemcpyHostToDevice, st), "H2D");
+  c->n_feat_rows = n;
+  CK(launch_mlp_predict(c->feat.ptr, nullptr, n, mlp_view(c), 0.f, 1, 1 << 20, nullptr, c->mlp_y.ptr, st), "predict");
+  CK(cudaMemcpyAsync(y, c->mlp_y.ptr, sizeof(float) * (size_t)n, cudaMemcpyDeviceToHost, st), "D2H");
+  CK(cudaStreamSynchronize(st), "forward sync");
+  return RPD_OK;
+}
+
+rpd_status rpd_mlp_gradient(rpd_ctx* c, const uint16_t* x, const float* target, int64_t n,
+                            float* grads, float* loss) {
+  if (!c) return RPD_ERR_INVALID_ARGUMENT;
+  if (n <= 0 || !x || !target || !grads) return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_mlp_gradient: bad arguments");
+  if (!c->mlp_ready) return fail(c, RPD_ERR_NOT_READY, "rpd_mlp_gradient: no parameters");
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  cudaStream_t st = c->stream;
+  CK(c->feat.ensure((size_t)n * kMlpFeatures), "alloc");
+  CK(c->mlp_target.ensure((size_t)n), "alloc");
+  CK(c->mlp_loss.ensure(1), "alloc");
+  CK(cudaMemcpyAsync(c->feat.ptr, x, sizeof(uint16_t) * kMlpFeatures * (size_t)n, cudaMemcpyHostToDevice, st), "H2D");
+  CK(cudaMemcpyAsync(c->mlp_target.ptr, target, sizeof(float) * (size_t)n, cudaMemcpyHostToDevice, st), "H2D");
+  CK(cudaMemsetAsync(c->mlp_grads.ptr, 0, sizeof(float) * kMlpParams, st), "memset");
+  CK(cudaMemsetAsync(c->mlp_loss.ptr, 0, sizeof(float), st), "memset");
+  c->n_feat_rows = n;
+  CK(launch_mlp_grad(c->feat.ptr, c->mlp_target.ptr, nullptr, n, 1.0f / (float)n, mlp_view(c),
+                     c->mlp_grads.ptr, c->mlp_loss.ptr, st), "grad");
+  float l = 0.f;
+  CK(cudaMemcpyAsync(grads, c->mlp_grads.ptr, sizeof(float) * kMlpParams, cudaMemcpyDeviceToHost, st), "D2H");
+  CK(cudaMemcpyAsync(&l, c->mlp_loss.ptr, sizeof(float), cudaMemcpyDeviceToHost, st), "D2H");
+  CK(cudaMemsetAsync(c->mlp_grads.ptr, 0, sizeof(float) * kMlpParams, st), "memset");
+  CK(cudaStreamSynchronize(st), "gradient sync");
+  if (loss) *loss = l / (float)n;
+  return RPD_OK;
+}
+
+rpd_status rpd_mlp_copy_features(rpd_ctx* c, uint16_t* x, int64_t capacity, int64_t* n_rows) {
+  if (!c) return RPD_ERR_INVALID_ARGUMENT;
+  if (n_rows) *n_rows = c->n_feat_rows;
+  if (!x) return RPD_OK;
+  if (capacity < c->n_feat_rows) return fail(c, RPD_ERR_CAPACITY, "rpd_mlp_copy_features: buffer too small");
+  if (c->n_feat_rows == 0) return RPD_OK;
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  CK(cudaMemcpy(x, c->feat.ptr, sizeof(uint16_t) * kMlpFeatures * (size_t)c->n_feat_rows,
+                cudaMemcpyDeviceToHost), "D2H");
+  return RPD_OK;
+}
+
+rpd_status rpd_mlp_copy_klen(rpd_ctx* c, int32_t* klen, int64_t capacity, int64_t* n_pairs) {
+  if (!c) return RPD_ERR_INVALID_ARGUMENT;
+  if (!c->has_result || !c->last_learned)
+    return fail(c, RPD_ERR_NOT_READY, "rpd_mlp_copy_klen: no learned_k result");
+  if (n_pairs) *n_pairs = c->n_pairs;
+  if (!klen) return RPD_OK;
+  if (capacity < c->n_pairs) return fail(c, RPD_ERR_CAPACITY, "rpd_mlp_copy_klen: buffer too small");
+  if (c->n_pairs == 0) return RPD_OK;
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  CK(cudaMemcpy(klen, c->pair_klen.ptr, sizeof(int32_t) * (size_t)c->n_pairs, cudaMemcpyDeviceToHost), "D2H");
   return RPD_OK;
 }
 

@@ -427,8 +427,14 @@ struct Cert {
   const float* keys;  // key of each list entry (CERT), ascending
   float3 S;           // seed
   float margin;       // absolute part of the certificate's margin
+  bool lazy;          // test the certificate once, after the whole (short) list
   bool certified;
+  int consumed;       // list entries taken before the certificate held
 };
+
+__device__ __forceinline__ bool cert_holds(float key, float R, float margin) {
+  return key * (1.0f - 64.0f * 5.9604645e-08f) - margin > R;
+}
 
 // ------------------------------------------------------------------------
 // the neighbour loop shared by the cell kernel and the box kernel
@@ -441,8 +447,10 @@ __device__ void clip_list(WarpCell& c, CellState& s, const int32_t* list, int k,
                           int seed_id, MakePlane make_plane, int lane,
                           uint32_t& n_pred, uint32_t& n_esc, Cert& cert) {
   constexpr bool kCof = PRED == RPD_PRED_FP32_FILTER || CERT;
+  const bool eager = CERT && !cert.lazy;
   float R = INFINITY;
-  if (CERT) R = cell_radius(c, s.nb_v, cert.S, lane);
+  if (eager) R = cell_radius(c, s.nb_v, cert.S, lane);
+  cert.consumed = k;
   for (int base = 0; base < k && s.status == kSuccess; base += 32) {
     int j = (base + lane < k) ? __ldg(list + base + lane) : -1;
     uint32_t valid = __ballot_sync(0xffffffffu, j != -1);
@@ -457,10 +465,11 @@ __device__ void clip_list(WarpCell& c, CellState& s, const int32_t* list, int k,
       if (plane_eq(e_mine, c.pl[p])) dup_mine |= 1ull << p;
     int r = 0;
     while (r < count) {
-      if (CERT) {
+      if (eager) {
         float kr = __shfl_sync(0xffffffffu, key_mine, r);
-        if (kr * (1.0f - 64.0f * 5.9604645e-08f) - cert.margin > R) {
+        if (cert_holds(kr, R, cert.margin)) {
           cert.certified = true;
+          cert.consumed = base + r;
           return;
         }
       }
@@ -533,13 +542,16 @@ __device__ void clip_list(WarpCell& c, CellState& s, const int32_t* list, int k,
         }
       }
       __syncwarp();
-      if (CERT && s.status == kSuccess) R = cell_radius(c, s.nb_v, cert.S, lane);
+      if (eager && s.status == kSuccess) R = cell_radius(c, s.nb_v, cert.S, lane);
       // later planes of this chunk identical to the new one
       if (plane_eq(e_mine, e)) dup_mine |= 1ull << (s.nb_p - 1);
       if (s.status != kSuccess) break;
       r = hit + 1;
     }
-    if (count < 32) break;  // the list ended (-1) inside this chunk
+    if (count < 32) {  // the list ended (-1) inside this chunk
+      cert.consumed = base + count;
+      break;
+    }
   }
 }
 
@@ -817,16 +829,30 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : kClipMaxThreads, MINB > 0 ? M
     const int32_t* list = p.nbr + (long long)sid * p.k;
     int klen = p.k;
     if (p.site_klen) klen = min(klen, __ldg(p.site_klen + sid));
+    if (p.pair_klen) klen = min(klen, __ldg(p.pair_klen + q));
     Cert cert;
     cert.keys = CERT ? p.keys + (long long)sid * p.k : nullptr;
     cert.S = make_float3(seed.x, seed.y, seed.z);
     cert.margin = p.cert_margin;
+    cert.lazy = p.lazy_cert != 0;
     cert.certified = false;
     clip_list<PRED, true, CERT>(c, s, list, klen, sid, make_plane, lane, n_pred, n_esc, cert);
     // a shortened list that ran out before the certificate held: the cell
-    // is clipped again with the whole list
-    if (CERT && s.status == kSuccess && !cert.certified && klen < p.k && __ldg(list + klen) != -1)
-      s.status = kSecurityRadiusNotReached;
+    // is clipped again with the whole list (status kSecurityRadiusNotReached
+    // marks it)
+    if (CERT && s.status == kSuccess && !cert.certified && klen < p.k && __ldg(list + klen) != -1) {
+      bool ok = false;
+      if (cert.lazy) {
+        // one certificate test after the whole short list
+        float R = cell_radius(c, s.nb_v, cert.S, lane);
+        ok = cert_holds(__ldg(cert.keys + klen), R, cert.margin);
+      }
+      if (!ok) {
+        if (p.misses && lane == 0) atomicAdd(p.misses, 1ull);
+        s.status = kSecurityRadiusNotReached;
+      }
+    }
+    if (p.consumed && lane == 0) p.consumed[q] = cert.consumed;
 
     // ---- emit
     rpd_cell_header hd;

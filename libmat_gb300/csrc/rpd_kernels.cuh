@@ -42,6 +42,10 @@ struct ClipParams {
   // distance-ordered lists with the security-radius certificate
   const float* keys;             // n_site x k bisector distances (ascending), or null
   const int32_t* site_klen;      // per-site list length, or null (= k)
+  const int32_t* pair_klen;      // per-pair list length, or null
+  int lazy_cert;                 // 1: one certificate test after the list
+  unsigned long long* misses;    // shortened lists whose certificate failed, or null
+  int32_t* consumed;             // per pair: list entries taken, or null
   float cert_margin;             // absolute margin of the certificate
   // optional indirection: work item w clips pair pair_index[w]
   const int32_t* pair_index;
@@ -160,5 +164,64 @@ cudaError_t compact_cells(const rpd_cell_header* pair_headers, long long n_pairs
 // reference site_knn layout -> row-major lists; validation of ids
 cudaError_t neighbors_from_reference(const int32_t* ref, int k, int n_site, int32_t* nbr,
                                      cudaStream_t st);
+
+// ---------------------------------------------------------------------------
+// learned list length (rpd_mlp.cu)
+// ---------------------------------------------------------------------------
+constexpr int kMlpFeatures = 16;  // 12 features, zero-padded to the mma's k
+constexpr int kMlpHidden = 64;
+// fp32 parameters: W1 [16][64], b1 [64], W2 [64][64] (in x out), b2 [64],
+// w3 [64], b3 [1]
+constexpr int kMlpParams = kMlpFeatures * kMlpHidden + kMlpHidden + kMlpHidden * kMlpHidden +
+                           kMlpHidden + kMlpHidden + 1;
+
+struct MlpWeights {
+  const uint16_t* W1T;  // bf16 [64][16] (hidden x feature)
+  const uint16_t* W2;   // bf16 [64][64] (in x out)
+  const uint16_t* W2T;  // bf16 [64][64] (out x in)
+  const float* b1;
+  const float* b2;
+  const float* w3;
+  const float* b3;
+};
+MlpWeights mlp_weights_view(const float* params, const uint16_t* W1T, const uint16_t* W2,
+                            const uint16_t* W2T);
+
+struct FeatureParams {
+  const int32_t* pair_tet;
+  const int32_t* pair_site;
+  const int32_t* pair_index;  // row q describes pair pair_index[q], or null
+  long long n_pairs;          // rows
+  const float4* site4f;
+  const float* vert3f;
+  const int4* tets;
+  const float4* centroid;     // per tet: centroid, w = radius
+  const float* keys;          // n_site x k ascending bisector distances
+  int k;
+  const int32_t* cell_of;     // site -> grid cell of the kNN grid
+  const int32_t* cell_count;  // sites per grid cell
+  const float* site_bdist;    // distance to the mesh boundary
+  float inv_h;                // 1 / mean site spacing
+  uint16_t* X;                // rows x 16 bf16 features
+  const int32_t* consumed;    // per pair: certifying list length (labels), or null
+  float* target;              // rows: log2(max(consumed, 1)), or null
+};
+
+cudaError_t launch_boundary_distance(const float4* site4f, int n_site, const float4* bverts,
+                                     int n_bv, float* dist, cudaStream_t st);
+cudaError_t launch_pair_features(const FeatureParams& p, cudaStream_t st);
+// y (optional) and list lengths klen (optional) of rows idx[0..n) (or 0..n)
+cudaError_t launch_mlp_predict(const uint16_t* X, const int32_t* idx, long long n,
+                               const MlpWeights& w, float margin, int kmin, int kmax,
+                               int32_t* klen, float* y, cudaStream_t st);
+// grads += scale * d(sum over rows of (y - target)^2)/dparams; loss_sum +=
+// the sum of squares; rows are idx[0..n) (or 0..n)
+cudaError_t launch_mlp_grad(const uint16_t* X, const float* target, const int32_t* idx,
+                            long long n, float scale, const MlpWeights& w, float* grads,
+                            float* loss_sum, cudaStream_t st);
+cudaError_t launch_mlp_adam(float* params, float* grads, float* m, float* v, int step, float lr,
+                            uint16_t* W1T, uint16_t* W2, uint16_t* W2T, cudaStream_t st);
+cudaError_t launch_mlp_sync_operands(const float* params, uint16_t* W1T, uint16_t* W2,
+                                     uint16_t* W2T, cudaStream_t st);
 
 }  // namespace rpd

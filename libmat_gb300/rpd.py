@@ -39,7 +39,13 @@ EXPORTS = [
     "rpd_copy_pairs_to_host", "rpd_copy_pair_headers_to_host", "rpd_build_mesh_adjacency",
     "rpd_host_alloc", "rpd_host_free", "rpd_compact_cells_noalloc", "rpd_set_site_k",
     "rpd_copy_topology_hashes_to_host", "rpd_autotune",
+    "rpd_mlp_collect", "rpd_mlp_clear_samples", "rpd_mlp_train", "rpd_mlp_enable",
+    "rpd_mlp_get_params", "rpd_mlp_set_params", "rpd_mlp_forward", "rpd_mlp_gradient",
+    "rpd_mlp_copy_features", "rpd_mlp_copy_klen", "rpd_mlp_copy_samples", "rpd_set_pair_k",
 ]
+
+MLP_FEATURES = 16
+MLP_PARAMS = 5313
 
 
 class Config(ctypes.Structure):
@@ -48,7 +54,7 @@ class Config(ctypes.Structure):
                 ("clip_order", ctypes.c_int), ("compute_geometry", ctypes.c_int),
                 ("warps_per_block", ctypes.c_int), ("blocks_per_sm", ctypes.c_int),
                 ("certify", ctypes.c_int), ("clip_variant", ctypes.c_int),
-                ("reserved", ctypes.c_int * 6)]
+                ("learned_k", ctypes.c_int), ("reserved", ctypes.c_int * 5)]
 
 
 class Stats(ctypes.Structure):
@@ -60,7 +66,8 @@ class Stats(ctypes.Structure):
                 ("ms_pairs", ctypes.c_float), ("ms_clip", ctypes.c_float),
                 ("ms_compact", ctypes.c_float), ("ms_clip_kernel", ctypes.c_float),
                 ("n_launches", ctypes.c_int32), ("search", ctypes.c_int64 * 6),
-                ("n_reclipped", ctypes.c_int64)]
+                ("n_reclipped", ctypes.c_int64), ("ms_predict", ctypes.c_float),
+                ("learned", ctypes.c_int32)]
 
     def as_dict(self):
         d = {f: getattr(self, f) for f, _ in self._fields_ if f not in ("status_counts", "search")}
@@ -73,6 +80,19 @@ class Tuning(ctypes.Structure):
     _fields_ = [("warps_per_block", ctypes.c_int), ("clip_variant", ctypes.c_int),
                 ("k_bucket", ctypes.c_int), ("n_candidates", ctypes.c_int),
                 ("ms_clip_best", ctypes.c_float), ("ms_clip_first", ctypes.c_float)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class MlpReport(ctypes.Structure):
+    _fields_ = [("n_train", ctypes.c_int64), ("n_calib", ctypes.c_int64),
+                ("loss_first", ctypes.c_float), ("loss_last", ctypes.c_float),
+                ("calib_loss", ctypes.c_float), ("margin", ctypes.c_float),
+                ("calib_miss_rate", ctypes.c_float), ("calib_mean_k", ctypes.c_float),
+                ("const_k", ctypes.c_float), ("ms_train", ctypes.c_float),
+                ("steps", ctypes.c_int32), ("epochs", ctypes.c_int32),
+                ("label_var", ctypes.c_float)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -134,6 +154,31 @@ def load(path=LIB_PATH):
     L.rpd_set_site_k.argtypes = [vp, vp, i32]
     L.rpd_copy_topology_hashes_to_host.restype = i32
     L.rpd_copy_topology_hashes_to_host.argtypes = [vp, vp, i64, c.POINTER(i64)]
+    L.rpd_mlp_collect.restype = i32
+    L.rpd_mlp_collect.argtypes = [vp, i64, c.POINTER(i64)]
+    L.rpd_mlp_clear_samples.restype = i32
+    L.rpd_mlp_clear_samples.argtypes = [vp]
+    L.rpd_mlp_train.restype = i32
+    L.rpd_mlp_train.argtypes = [vp, i32, i32, c.c_float, c.c_float, c.c_uint64,
+                                c.POINTER(MlpReport)]
+    L.rpd_mlp_enable.restype = i32
+    L.rpd_mlp_enable.argtypes = [vp, i32]
+    L.rpd_mlp_get_params.restype = i32
+    L.rpd_mlp_get_params.argtypes = [vp, vp, i32, c.POINTER(c.c_float)]
+    L.rpd_mlp_set_params.restype = i32
+    L.rpd_mlp_set_params.argtypes = [vp, vp, i32, c.c_float]
+    L.rpd_mlp_forward.restype = i32
+    L.rpd_mlp_forward.argtypes = [vp, vp, i64, vp]
+    L.rpd_mlp_gradient.restype = i32
+    L.rpd_mlp_gradient.argtypes = [vp, vp, vp, i64, vp, c.POINTER(c.c_float)]
+    L.rpd_mlp_copy_features.restype = i32
+    L.rpd_mlp_copy_features.argtypes = [vp, vp, i64, c.POINTER(i64)]
+    L.rpd_set_pair_k.restype = i32
+    L.rpd_set_pair_k.argtypes = [vp, vp, i64]
+    L.rpd_mlp_copy_samples.restype = i32
+    L.rpd_mlp_copy_samples.argtypes = [vp, vp, vp, i64, c.POINTER(i64)]
+    L.rpd_mlp_copy_klen.restype = i32
+    L.rpd_mlp_copy_klen.argtypes = [vp, vp, i64, c.POINTER(i64)]
     L.rpd_host_alloc.restype = vp
     L.rpd_host_alloc.argtypes = [c.c_size_t]
     L.rpd_host_free.restype = None
@@ -179,7 +224,8 @@ class RPD:
 
     def __init__(self, device=0, predicate_mode=PRED_FP32_FILTER, neighbor_source=NEIGH_KNN,
                  knn_k=64, clip_order=ORDER_SITE_ID, compute_geometry=True,
-                 warps_per_block=0, blocks_per_sm=0, certify=False, clip_variant=0):
+                 warps_per_block=0, blocks_per_sm=0, certify=False, clip_variant=0,
+                 learned_k=False):
         L = load()
         cfg = Config()
         L.rpd_config_default(ctypes.byref(cfg))
@@ -193,6 +239,7 @@ class RPD:
         cfg.blocks_per_sm = blocks_per_sm
         cfg.certify = 1 if certify else 0
         cfg.clip_variant = clip_variant
+        cfg.learned_k = 1 if learned_k else 0
         h = ctypes.c_void_p()
         s = L.rpd_create(ctypes.byref(cfg), ctypes.byref(h))
         if s != 0:
@@ -250,6 +297,14 @@ class RPD:
         a = np.ascontiguousarray(k_per_site, np.int32)
         self._check(self._L.rpd_set_site_k(self._h, _p(a), 0))
 
+    def set_pair_k(self, k_per_pair):
+        """Per-pair list lengths for the next certified compute (None clears)."""
+        if k_per_pair is None:
+            self._check(self._L.rpd_set_pair_k(self._h, None, 0))
+            return
+        a = np.ascontiguousarray(k_per_pair, np.int32)
+        self._check(self._L.rpd_set_pair_k(self._h, _p(a), a.shape[0]))
+
     def autotune(self, repeats=2):
         """Picks the fastest clip launch configuration on the current inputs."""
         t = Tuning()
@@ -262,6 +317,75 @@ class RPD:
         out = np.zeros(n.value, np.uint64)
         self._check(self._L.rpd_copy_topology_hashes_to_host(self._h, _p(out), out.shape[0],
                                                              ctypes.byref(n)))
+        return out
+
+    # ---- learned list length
+    def mlp_collect(self, max_samples):
+        """Appends up to max_samples labelled cells of the current inputs to
+        the training set; returns its size."""
+        n = ctypes.c_int64()
+        self._check(self._L.rpd_mlp_collect(self._h, int(max_samples), ctypes.byref(n)))
+        return n.value
+
+    def mlp_clear_samples(self):
+        self._check(self._L.rpd_mlp_clear_samples(self._h))
+
+    def mlp_samples(self):
+        """The training set: (features (n, 16) bf16 bits, labels)."""
+        n = ctypes.c_int64()
+        self._check(self._L.rpd_mlp_copy_samples(self._h, None, None, 0, ctypes.byref(n)))
+        x = np.zeros((n.value, MLP_FEATURES), np.uint16)
+        y = np.zeros(n.value, np.float32)
+        self._check(self._L.rpd_mlp_copy_samples(self._h, _p(x), _p(y), n.value, ctypes.byref(n)))
+        return x, y
+
+    def mlp_train(self, epochs=20, batch=512, lr=2e-3, miss_target=0.02, seed=0):
+        r = MlpReport()
+        self._check(self._L.rpd_mlp_train(self._h, epochs, batch, lr, miss_target, seed,
+                                          ctypes.byref(r)))
+        return r
+
+    def mlp_enable(self, on=True):
+        """Per-cell list lengths from the k-predictor (misses re-clipped)."""
+        self._check(self._L.rpd_mlp_enable(self._h, 1 if on else 0))
+
+    def mlp_params(self):
+        out = np.zeros(MLP_PARAMS, np.float32)
+        m = ctypes.c_float()
+        self._check(self._L.rpd_mlp_get_params(self._h, _p(out), MLP_PARAMS, ctypes.byref(m)))
+        return out, m.value
+
+    def mlp_set_params(self, params, margin=0.0):
+        a = np.ascontiguousarray(params, np.float32)
+        self._check(self._L.rpd_mlp_set_params(self._h, _p(a), a.shape[0], margin))
+
+    def mlp_forward(self, x_bf16):
+        x = np.ascontiguousarray(x_bf16, np.uint16)
+        y = np.zeros(x.shape[0], np.float32)
+        self._check(self._L.rpd_mlp_forward(self._h, _p(x), x.shape[0], _p(y)))
+        return y
+
+    def mlp_gradient(self, x_bf16, target):
+        x = np.ascontiguousarray(x_bf16, np.uint16)
+        t = np.ascontiguousarray(target, np.float32)
+        g = np.zeros(MLP_PARAMS, np.float32)
+        loss = ctypes.c_float()
+        self._check(self._L.rpd_mlp_gradient(self._h, _p(x), _p(t), x.shape[0], _p(g),
+                                             ctypes.byref(loss)))
+        return g, loss.value
+
+    def mlp_features(self):
+        n = ctypes.c_int64()
+        self._check(self._L.rpd_mlp_copy_features(self._h, None, 0, ctypes.byref(n)))
+        out = np.zeros((n.value, MLP_FEATURES), np.uint16)
+        self._check(self._L.rpd_mlp_copy_features(self._h, _p(out), n.value, ctypes.byref(n)))
+        return out
+
+    def mlp_klen(self):
+        n = ctypes.c_int64()
+        self._check(self._L.rpd_mlp_copy_klen(self._h, None, 0, ctypes.byref(n)))
+        out = np.zeros(n.value, np.int32)
+        self._check(self._L.rpd_mlp_copy_klen(self._h, _p(out), n.value, ctypes.byref(n)))
         return out
 
     def compute(self):
