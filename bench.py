@@ -8,7 +8,11 @@ synthetic data generated here.  One step = one rpd_compute: GPU kNN (k = 64),
 candidate pairs by the reference's rule, clipping, compaction, from
 device-resident mesh and sites to device-resident compact cells.
 
-  value   fast path: FP32 filter + FP64 fallback predicates (reference signs)
+  value   fast path: FP32 filter + FP64 fallback predicates (reference signs),
+          neighbours in ascending bisector distance with the security-radius
+          certificate, first-pass list lengths chosen by the autotuner among
+          16 / 32 / all neighbours and the k-predictor trained here (untimed
+          set-up: 200k labelled cells of two meshes with other seeds)
   plain   the plain FP64 path: FP64 determinant on every predicate
   e2e     the fast path through the C ABI with host buffers: mesh + sites
           host->device, compute, every cell device->host, per step
@@ -194,8 +198,38 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def train_predictor(args, r, rpd, W):
+    """Untimed set-up of the learned list length: labelled cells (the
+    certifying list length of every cell of the plain method) from training
+    meshes of the same distribution with other seeds, then training on the
+    GPU with the engine's own kernels.  Leaves the engine on the training
+    set's last mesh; the caller loads the evaluation inputs."""
+    t0 = time.time()
+    n = 0
+    per = args.train_cells // len(args.train_seeds)
+    for seed in args.train_seeds:
+        tc = W.config_ellipsoid(target_tets=args.tets, n_site=args.sites, seed=seed)
+        ta = rpd.mesh_adjacency(tc["vert3d"].shape[0], tc["tets"])
+        r.set_mesh(tc["vert3d"], tc["tets"], ta["v_adjs"], ta["e_adj6"], ta["f_adjs"], ta["f_ids"])
+        r.set_sites(tc["sites"], tc["flags"])
+        n = r.mlp_collect(per)
+    rep = r.mlp_train(epochs=args.epochs, batch=512, lr=2e-3, miss_target=args.miss_target,
+                      seed=7)
+    return {"samples": int(n), "train_meshes": ["ellipsoid seed %d" % s for s in args.train_seeds],
+            "report": rep.as_dict(), "setup_s": round(time.time() - t0, 2)}
+
+
+def _clip_ms(r, reps=3):
+    ts, st = [], None
+    for _ in range(reps):
+        st = r.compute()
+        ts.append(st.ms_clip)
+    return float(np.median(ts)), st
+
+
 def run_ours(args):
     from libmat_gb300 import rpd
+    from libmat_gb300 import workloads as W
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -217,13 +251,16 @@ def run_ours(args):
     adj = rpd.mesh_adjacency(cfg["vert3d"].shape[0], cfg["tets"])
     nt, nv, ns = cfg["tets"].shape[0], cfg["vert3d"].shape[0], cfg["sites"].shape[0]
 
+    def load(r):
+        r.set_mesh(cfg["vert3d"], cfg["tets"], adj["v_adjs"], adj["e_adj6"], adj["f_adjs"],
+                   adj["f_ids"])
+        r.set_sites(cfg["sites"], cfg["flags"])
+
     def engine(pred, certify):
         r = rpd.RPD(device=local if world > 1 else 0, predicate_mode=pred,
                     neighbor_source=rpd.NEIGH_KNN, knn_k=args.k, clip_order=rpd.ORDER_SITE_ID,
                     certify=certify)
-        r.set_mesh(cfg["vert3d"], cfg["tets"], adj["v_adjs"], adj["e_adj6"], adj["f_adjs"],
-                   adj["f_ids"])
-        r.set_sites(cfg["sites"], cfg["flags"])
+        load(r)
         return r
 
     def timed(r, steps, warmup):
@@ -240,12 +277,22 @@ def run_ours(args):
         return ms, cells, st_last
 
     # ---- fast path (the metric): FP32-filter predicates, neighbours in
-    # ascending bisector distance, stop at the security-radius certificate
-    fast = engine(rpd.PRED_FP32_FILTER, True)
+    # ascending bisector distance, the security-radius certificate, and the
+    # learned per-cell list length trained here (untimed set-up)
+    fast = rpd.RPD(device=local if world > 1 else 0, predicate_mode=rpd.PRED_FP32_FILTER,
+                   neighbor_source=rpd.NEIGH_KNN, knn_k=args.k, clip_order=rpd.ORDER_SITE_ID,
+                   certify=True)
+    learned = None
+    if not args.no_learned:
+        learned = train_predictor(args, fast, rpd, W)
+    load(fast)
     # the project's autotuner picks the clip kernel's block size, register
-    # (and so shared-memory) budget and first-pass list length on this
-    # workload; untimed set-up
+    # (and so shared-memory) budget and the first-pass list length (16, 32,
+    # all neighbours, or the predictor's per-cell lengths) on this workload
     tuning = fast.autotune(repeats=1).as_dict() if not args.no_tune else None
+    if args.force_learned and learned is not None:
+        fast.mlp_enable(True)
+    fast.configure(topology_hash=0)  # a validation aid, not part of the path
     barrier()
     with ClockSampler(local) as clk:
         ms, cells, st = timed(fast, args.steps, args.warmup)
@@ -257,16 +304,47 @@ def run_ours(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_ms = float(t.item())
     value = cells * world / (total_ms / 1000.0)
+    used_learned = bool(fast.config().learned_k)
+
+    # ---- validation run of the same configuration with topology hashes
+    fast.configure(topology_hash=1)
+    fast.compute()
     fast_ph = fast.pair_headers()
     fast_hash = fast.topology_hashes()
     fast_h, fast_p = fast.cells()
+
+    # ---- what the learned lengths do on this (unseen) mesh: clip stage
+    # with them, with the certificate tested as each cell is clipped (no
+    # network), and with the whole list (no certificate, no network)
+    if learned is not None:
+        base_cfg = fast.config()
+        fast.configure(learned_k=1, topology_hash=0)
+        ms_l, st_l = _clip_ms(fast)
+        klen = fast.mlp_klen()
+        fast.configure(learned_k=0)
+        fast.set_site_k(None)
+        ms_e, st_e = _clip_ms(fast)
+        fast.set_pair_k(np.full(st_e.n_pairs, args.k, np.int32))
+        ms_f, _ = _clip_ms(fast)
+        fast.set_pair_k(None)
+        fast.set_config(base_cfg)
+        learned["eval"] = {
+            "miss_rate": st_l.n_reclipped / max(st_l.n_pairs, 1),
+            "reclipped": int(st_l.n_reclipped), "mean_list_length": float(klen.mean()),
+            "const_k_same_miss_rate": learned["report"]["const_k"],
+            "ms_clip_learned": ms_l, "ms_predict": st_l.ms_predict,
+            "ms_clip_certificate_no_net": ms_e, "ms_clip_whole_list": ms_f,
+            "used_in_timed_runs": used_learned}
 
     # ---- plain FP64 path: whole list in site-id order, FP64 determinant on
     # every predicate
     plain = engine(rpd.PRED_FP64, False)
     plain_tuning = plain.autotune(repeats=1).as_dict() if not args.no_tune else None
+    plain.configure(topology_hash=0)
     pms, pcells, pst = timed(plain, max(1, args.steps // 2), 1)
     plain_value = pcells / (sum(pms) / 1000.0)
+    plain.configure(topology_hash=1)
+    plain.compute()
     plain_ph = plain.pair_headers()
     plain_hash = plain.topology_hashes()
     plain_h, plain_p = plain.cells()
@@ -280,8 +358,8 @@ def run_ours(args):
     topo_ok = same_headers and n_topo_diff == 0
     geo = _geometry_error(fast_ph, fast_p, plain_ph, plain_p)
 
-    # ---- end to end through the C ABI with host buffers
-    e2e = _e2e(args, cfg, adj, rpd)
+    # ---- end to end through the C ABI with host buffers, same configuration
+    e2e = _e2e(args, cfg, adj, rpd, fast)
 
     # ---- roofline of the clip kernel
     peak, peak_src = load_peaks()
@@ -319,7 +397,7 @@ def run_ours(args):
                    "predicates": "fp32 filter, fp64 det when undecided",
                    "neighbours": "gpu kNN, k smallest power-bisector distances",
                    "clipping": "ascending bisector distance, security-radius certificate",
-                   "learned_k": False, "l2": "flushed between steps (256 MB write)",
+                   "learned_k": used_learned, "l2": "flushed between steps (256 MB write)",
                    "parallelism": "replicas" if world > 1 else "single gpu",
                    "generation_s": round(gen_s, 2)},
         "plain": {"value": plain_value, "ms_per_step": sum(pms) / len(pms),
@@ -328,9 +406,11 @@ def run_ours(args):
                   "predicates_evaluated": int(pst.n_predicates), "tuning": plain_tuning},
         "geometry_vs_plain": geo,
         "tuning": tuning,
+        "learned": learned,
         "reclipped": int(st.n_reclipped),
         "stage_ms": {"knn": st.ms_knn, "pairs": st.ms_pairs, "clip": st.ms_clip,
-                     "clip_kernel": st.ms_clip_kernel, "compact": st.ms_compact},
+                     "clip_kernel": st.ms_clip_kernel, "predict": st.ms_predict,
+                     "compact": st.ms_compact},
         "predicates": {"evaluated": st.n_predicates, "escalated_fp64": st.n_escalated,
                        "escalation_rate": st.n_escalated / max(st.n_predicates, 1)},
         "status_counts": {rpd.STATUS_NAMES[i]: int(st.status_counts[i]) for i in range(10)
@@ -424,7 +504,7 @@ def _sample_topology_equal(h1, p1, h2, p2, n=20000):
     return True
 
 
-def _e2e(args, cfg, adj, rpd):
+def _e2e(args, cfg, adj, rpd, tuned):
     """The same metric through the C ABI with host buffers (page-locked):
     per step rpd_set_mesh + rpd_set_sites (host->device), rpd_compute, and
     rpd_copy_cells_to_host (device->host of every cell)."""
@@ -447,10 +527,17 @@ def _e2e(args, cfg, adj, rpd):
     fl = pin("fl", cfg["flags"])
     r = rpd.RPD(predicate_mode=rpd.PRED_FP32_FILTER, neighbor_source=rpd.NEIGH_KNN,
                 knn_k=args.k, clip_order=rpd.ORDER_SITE_ID, certify=True)
+    # the fast engine's tuned configuration and trained predictor
+    tc = tuned.config()
+    tc.topology_hash = 0
+    r.set_config(tc)
+    try:
+        params, margin = tuned.mlp_params()
+        r.mlp_set_params(params, margin)
+    except rpd.RPDError:
+        pass
     r.set_mesh(v, t, va, e6, fa, fi)
     r.set_sites(s, fl)
-    if not args.no_tune:
-        r.autotune(repeats=1)
     st = r.compute()
     hbuf = rpd.PinnedArray((int(st.n_cells * 1.1) + 1024,), rpd.HEADER_DTYPE)
     pbuf = rpd.PinnedArray((int(st.payload_bytes * 1.1) + (1 << 20),), np.uint8)
@@ -496,6 +583,13 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=20000)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner")
+    ap.add_argument("--no-learned", action="store_true", help="skip training the k-predictor")
+    ap.add_argument("--force-learned", action="store_true",
+                    help="time the learned lengths even if the autotuner prefers others")
+    ap.add_argument("--train-seeds", type=int, nargs="+", default=[41, 42])
+    ap.add_argument("--train-cells", type=int, default=200_000)
+    ap.add_argument("--epochs", type=int, default=20)
+    ap.add_argument("--miss-target", type=float, default=0.02)
     ap.add_argument("--fast-only", action="store_true",
                     help="only the timed fast path (for profiler launch lists)")
     args = ap.parse_args()

@@ -85,7 +85,13 @@ typedef struct rpd_config {
                             pass clips that many list entries and tests the
                             certificate once, cells where it fails are
                             clipped again with the whole list */
-  int reserved[5];
+  int box_planes;        /* RPD_NEIGH_KNN: nearest bisectors bounding each
+                            site's candidate region for the tets of common
+                            size (0 = default 32; the few largest tets use
+                            at most 12) */
+  int topology_hash;     /* 1 (default): canonical topology hash of every
+                            cell (rpd_copy_topology_hashes_to_host) */
+  int reserved[3];
 } rpd_config;
 
 /* One record per candidate (tet, site) pair; 32 bytes. */
@@ -148,6 +154,10 @@ void rpd_config_default(rpd_config* cfg);
 rpd_status rpd_create(const rpd_config* cfg, struct rpd_ctx** out);
 void rpd_destroy(struct rpd_ctx* ctx);
 const char* rpd_last_error(const struct rpd_ctx* ctx);
+/* Reads / replaces a context's configuration (same device; the mesh, sites
+ * and any trained predictor stay).  The next rpd_compute uses it. */
+rpd_status rpd_get_config(const struct rpd_ctx* ctx, rpd_config* cfg);
+rpd_status rpd_set_config(struct rpd_ctx* ctx, const rpd_config* cfg);
 
 /* Tet mesh (replaces copy_tet_data + load_num_adjacent_cells_and_ids,
  * voronoi.cu:324-415).  xyz: n_vert x 3 doubles; tets: n_tet x 4 vertex
@@ -184,7 +194,8 @@ rpd_status rpd_set_site_k(struct rpd_ctx* ctx, const int32_t* k_per_site, int on
  * warps, register budgets for 16, 24 or 32 resident warps per SM (the
  * shared-memory budget per SM follows: 5.7 KB per warp) -- and, with
  * config.certify, first-pass list lengths of 16, 32 or all neighbours
- * (k-bucket; cells not certified by their bucket are clipped again whole).
+ * (k-bucket; cells not certified by their bucket are clipped again whole)
+ * and, once a k-predictor is trained or loaded, its per-cell lengths.
  * Keeps the fastest in the context (the cells are the same for every
  * candidate).  repeats >= 1 timed runs per candidate (median). */
 typedef struct rpd_tuning {
@@ -194,6 +205,7 @@ typedef struct rpd_tuning {
   int n_candidates;
   float ms_clip_best;  /* clip stage of the chosen configuration */
   float ms_clip_first; /* clip stage of the first candidate (defaults) */
+  int learned_k;       /* 1: the k-predictor's lengths won (rpd_config.learned_k set) */
 } rpd_tuning;
 rpd_status rpd_autotune(struct rpd_ctx* ctx, int repeats, rpd_tuning* result);
 

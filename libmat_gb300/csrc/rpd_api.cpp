@@ -89,6 +89,7 @@ struct rpd_ctx {
   int n_vert = 0, n_tet = 0;
   DevBuf<float> vert3f;
   DevBuf<double> vert3d;
+  DevBuf<float2> vert2;  // double-float copies (geometry epilogue)
   DevBuf<int4> tets;
   DevBuf<int32_t> v_adjs, f_adjs, f_ids;
   DevBuf<uint8_t> e_adj6;
@@ -106,6 +107,7 @@ struct rpd_ctx {
   int n_site = 0;
   DevBuf<float4> site4f;
   DevBuf<double> site4d;
+  DevBuf<float2> site2;
   DevBuf<uint32_t> flags;
   double site_lo[3] = {0, 0, 0}, site_hi[3] = {0, 0, 0};
   float w_max = 0.f;
@@ -187,6 +189,12 @@ rpd_status cuda_fail(rpd_ctx* c, cudaError_t e, const char* where) {
     cudaError_t _e = (expr);                     \
     if (_e != cudaSuccess) return cuda_fail(c, _e, where); \
   } while (0)
+
+// double -> (hi, lo) float pair, hi + lo ~ x to about 48 bits
+float2 split_df(double x) {
+  const float h = (float)x;
+  return make_float2(h, (float)(x - (double)h));
+}
 
 Grid make_grid(const double* lo, const double* hi, long long n_items, double per_cell) {
   Grid g;
@@ -297,6 +305,21 @@ void rpd_config_default(rpd_config* cfg) {
   cfg->compute_geometry = 1;
   cfg->warps_per_block = 0;
   cfg->blocks_per_sm = 0;
+  cfg->topology_hash = 1;
+}
+
+static bool config_valid(const rpd_config& c0) {
+  if (c0.predicate_mode != RPD_PRED_FP64 && c0.predicate_mode != RPD_PRED_FP32_FILTER) return false;
+  if (c0.neighbor_source != RPD_NEIGH_USER && c0.neighbor_source != RPD_NEIGH_KNN) return false;
+  if (c0.neighbor_source == RPD_NEIGH_KNN && (c0.knn_k < 1 || c0.knn_k > 128)) return false;
+  if (c0.warps_per_block < 0 || c0.warps_per_block > kClipMaxThreads / 32 || c0.blocks_per_sm < 0)
+    return false;
+  if (c0.certify && c0.neighbor_source != RPD_NEIGH_KNN) return false;
+  if (c0.clip_variant < 0 || c0.clip_variant > 2) return false;
+  if (c0.box_planes < 0 || c0.box_planes > 128) return false;
+  if (c0.learned_k < 0 || c0.learned_k > 1 || (c0.learned_k && !c0.certify)) return false;
+  if (c0.topology_hash < 0 || c0.topology_hash > 1) return false;
+  return true;
 }
 
 rpd_status rpd_create(const rpd_config* cfg, rpd_ctx** out) {
@@ -305,18 +328,7 @@ rpd_status rpd_create(const rpd_config* cfg, rpd_ctx** out) {
   rpd_config c0;
   rpd_config_default(&c0);
   if (cfg) c0 = *cfg;
-  if (c0.predicate_mode != RPD_PRED_FP64 && c0.predicate_mode != RPD_PRED_FP32_FILTER)
-    return RPD_ERR_INVALID_ARGUMENT;
-  if (c0.neighbor_source != RPD_NEIGH_USER && c0.neighbor_source != RPD_NEIGH_KNN)
-    return RPD_ERR_INVALID_ARGUMENT;
-  if (c0.neighbor_source == RPD_NEIGH_KNN && (c0.knn_k < 1 || c0.knn_k > 128))
-    return RPD_ERR_INVALID_ARGUMENT;
-  if (c0.warps_per_block < 0 || c0.warps_per_block > kClipMaxThreads / 32 || c0.blocks_per_sm < 0)
-    return RPD_ERR_INVALID_ARGUMENT;
-  if (c0.certify && c0.neighbor_source != RPD_NEIGH_KNN) return RPD_ERR_INVALID_ARGUMENT;
-  if (c0.clip_variant < 0 || c0.clip_variant > 2) return RPD_ERR_INVALID_ARGUMENT;
-  if (c0.learned_k < 0 || c0.learned_k > 1 || (c0.learned_k && !c0.certify))
-    return RPD_ERR_INVALID_ARGUMENT;
+  if (!config_valid(c0)) return RPD_ERR_INVALID_ARGUMENT;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
     cudaGetLastError();
@@ -361,6 +373,24 @@ void rpd_destroy(rpd_ctx* c) {
     if (c->ev[i]) cudaEventDestroy(c->ev[i]);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
+}
+
+rpd_status rpd_get_config(const rpd_ctx* c, rpd_config* cfg) {
+  if (!c || !cfg) return RPD_ERR_INVALID_ARGUMENT;
+  *cfg = c->cfg;
+  return RPD_OK;
+}
+
+rpd_status rpd_set_config(rpd_ctx* c, const rpd_config* cfg) {
+  if (!c || !cfg) return RPD_ERR_INVALID_ARGUMENT;
+  if (!config_valid(*cfg)) return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_set_config: invalid configuration");
+  if (cfg->device != c->device)
+    return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_set_config: a context stays on its device");
+  if (cfg->neighbor_source != c->cfg.neighbor_source || cfg->knn_k != c->cfg.knn_k)
+    c->has_site_klen = false;
+  c->cfg = *cfg;
+  c->has_result = false;
+  return RPD_OK;
 }
 
 const char* rpd_last_error(const rpd_ctx* c) { return c ? c->err.c_str() : "no context"; }
@@ -443,6 +473,9 @@ rpd_status rpd_set_mesh(rpd_ctx* c, const double* xyz, int n_vert, const int32_t
   const int n_bv = (int)(bv.size() / 4);
   CK(c->bverts.ensure((size_t)std::max(n_bv, 1)), "alloc boundary");
   CK(c->vert3f.ensure((size_t)n_vert * 3), "alloc vert3f");
+  CK(c->vert2.ensure((size_t)n_vert * 3), "alloc vert2");
+  std::vector<float2> v2((size_t)n_vert * 3);
+  for (size_t i = 0; i < v2.size(); ++i) v2[i] = split_df(xyz[i]);
   CK(c->vert3d.ensure((size_t)n_vert * 3), "alloc vert3d");
   CK(c->tets.ensure(n_tet), "alloc tets");
   CK(c->v_adjs.ensure(n_vert), "alloc v_adjs");
@@ -453,6 +486,7 @@ rpd_status rpd_set_mesh(rpd_ctx* c, const double* xyz, int n_vert, const int32_t
   cudaStream_t st = c->stream;
   CK(cudaMemcpyAsync(c->vert3f.ptr, vf.data(), vf.size() * 4, cudaMemcpyHostToDevice, st), "H2D vert");
   CK(cudaMemcpyAsync(c->vert3d.ptr, xyz, (size_t)n_vert * 24, cudaMemcpyHostToDevice, st), "H2D vert");
+  CK(cudaMemcpyAsync(c->vert2.ptr, v2.data(), v2.size() * sizeof(float2), cudaMemcpyHostToDevice, st), "H2D vert");
   CK(cudaMemcpyAsync(c->tets.ptr, tets, (size_t)n_tet * 16, cudaMemcpyHostToDevice, st), "H2D tets");
   CK(cudaMemcpyAsync(c->v_adjs.ptr, v_adjs, (size_t)n_vert * 4, cudaMemcpyHostToDevice, st), "H2D v_adjs");
   CK(cudaMemcpyAsync(c->e_adj6.ptr, e_adj6, (size_t)n_tet * 6, cudaMemcpyHostToDevice, st), "H2D e_adj6");
@@ -504,10 +538,14 @@ rpd_status rpd_set_sites(rpd_ctx* c, const double* xyzw, int n_site, const uint3
   }
   CK(c->site4f.ensure(n_site), "alloc sites");
   CK(c->site4d.ensure((size_t)n_site * 4), "alloc sites");
+  CK(c->site2.ensure((size_t)n_site * 4), "alloc sites");
+  std::vector<float2> s2((size_t)n_site * 4);
+  for (size_t i = 0; i < s2.size(); ++i) s2[i] = split_df(xyzw[i]);
   CK(c->flags.ensure(n_site), "alloc flags");
   cudaStream_t st = c->stream;
   CK(cudaMemcpyAsync(c->site4f.ptr, sf.data(), sf.size() * 4, cudaMemcpyHostToDevice, st), "H2D sites");
   CK(cudaMemcpyAsync(c->site4d.ptr, xyzw, (size_t)n_site * 32, cudaMemcpyHostToDevice, st), "H2D sites");
+  CK(cudaMemcpyAsync(c->site2.ptr, s2.data(), s2.size() * sizeof(float2), cudaMemcpyHostToDevice, st), "H2D sites");
   CK(cudaMemcpyAsync(c->flags.ptr, fl.data(), (size_t)n_site * 4, cudaMemcpyHostToDevice, st), "H2D flags");
   CK(cudaStreamSynchronize(st), "set_sites sync");
   if (c->n_site != n_site) {
@@ -619,7 +657,7 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
     // the nearest bisectors bound each cell; with a GPU-built list the
     // distance-ordered copy gives them first, a user list is used whole
     const int32_t* box_list = knn ? c->nbr_dist.ptr : c->nbr.ptr;
-    const int k_box = knn ? std::min(c->k, 32) : c->k;
+    const int box0 = c->cfg.box_planes > 0 ? c->cfg.box_planes : 32;
     CK(c->site_box.ensure((size_t)n_site * 2), "alloc");
     CK(c->site_planes.ensure((size_t)n_site * kBoxPlanes), "alloc");
     CK(c->site_nplanes.ensure((size_t)n_site), "alloc");
@@ -651,7 +689,10 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
         bp.flags = c->flags.ptr;
         bp.nbr = box_list;
         bp.k = c->k;
-        bp.k_box = k_box;
+        // the nearest bisectors (distance-ordered GPU lists) for the common
+        // tets; the class of the largest tets has few tets, so a looser
+        // region costs little in the search and its box is cheap to clip
+        bp.k_box = knn ? std::min(c->k, cl == 0 ? box0 : std::min(box0, 12)) : c->k;
         bp.n_site = n_site;
         bp.box_lo = make_float4((float)(c->mesh_lo[0] - margin), (float)(c->mesh_lo[1] - margin),
                                 (float)(c->mesh_lo[2] - margin), 0.f);
@@ -766,6 +807,8 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
     p.f_ids = c->f_ids.ptr;
     p.site4f = c->site4f.ptr;
     p.site4d = c->site4d.ptr;
+    p.vert2 = c->vert2.ptr;
+    p.site2 = c->site2.ptr;
     p.nbr = certify ? c->nbr_dist.ptr : c->nbr.ptr;
     p.k = c->k;
     p.pair_tet = c->pair_tet.ptr;
@@ -787,7 +830,7 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
     p.cert_margin = cert_margin;
     p.pair_index = nullptr;
     p.n_work = n_pairs;
-    p.topo_hash = c->topo_hash.ptr;
+    p.topo_hash = c->cfg.topology_hash ? c->topo_hash.ptr : nullptr;
     CK(cudaEventRecord(c->ev[kEvClipK0], st), "event");
     if (n_pairs > 0) CK(launch_clip_cells(p, c->cfg.predicate_mode, certify, variant, blocks, warps, st), "clip");
     CK(cudaEventRecord(c->ev[kEvClipK1], st), "event");
@@ -890,12 +933,16 @@ rpd_status rpd_autotune(rpd_ctx* c, int repeats, rpd_tuning* result) {
     CK(cudaMemcpy(saved_k.data(), c->site_klen.ptr, sizeof(int32_t) * saved_k.size(),
                   cudaMemcpyDeviceToHost), "D2H");
   }
-  int buckets[3] = {0, 0, 0};
+  // first-pass list lengths: 0 = the whole list (certificate tested as the
+  // cell is clipped), 16 / 32 for every site (misses re-clipped), and -1 =
+  // the k-predictor's per-cell lengths when one is trained
+  int buckets[4] = {0, 0, 0, 0};
   int nb = 1;
   if (c->cfg.certify && c->cfg.neighbor_source == RPD_NEIGH_KNN) {
     buckets[1] = 16;
     buckets[2] = 32;
     nb = 3;
+    if (c->mlp_ready) buckets[nb++] = -1;
   }
   float best = INFINITY, first = 0.f;
   Cand best_c = cands[0];
@@ -908,6 +955,7 @@ rpd_status rpd_autotune(rpd_ctx* c, int repeats, rpd_tuning* result) {
       c->cfg.warps_per_block = cd.warps;
       c->cfg.clip_variant = cd.variant;
       c->cfg.blocks_per_sm = 0;
+      c->cfg.learned_k = cd.bucket < 0 ? 1 : 0;
       if (cd.bucket > 0) {
         std::vector<int32_t> kk((size_t)c->n_site, cd.bucket);
         rpd_status s = rpd_set_site_k(c, kk.data(), 0);
@@ -939,6 +987,7 @@ rpd_status rpd_autotune(rpd_ctx* c, int repeats, rpd_tuning* result) {
   c->cfg.warps_per_block = best_c.warps;
   c->cfg.clip_variant = best_c.variant;
   c->cfg.blocks_per_sm = 0;
+  c->cfg.learned_k = best_c.bucket < 0 ? 1 : 0;
   if (best_c.bucket > 0) {
     std::vector<int32_t> kk((size_t)c->n_site, best_c.bucket);
     rpd_status s = rpd_set_site_k(c, kk.data(), 0);
@@ -953,7 +1002,8 @@ rpd_status rpd_autotune(rpd_ctx* c, int repeats, rpd_tuning* result) {
   if (result) {
     result->warps_per_block = best_c.warps;
     result->clip_variant = best_c.variant;
-    result->k_bucket = best_c.bucket;
+    result->k_bucket = best_c.bucket > 0 ? best_c.bucket : 0;
+    result->learned_k = best_c.bucket < 0 ? 1 : 0;
     result->n_candidates = tried;
     result->ms_clip_best = best;
     result->ms_clip_first = first;
@@ -1035,6 +1085,8 @@ rpd_status rpd_copy_topology_hashes_to_host(rpd_ctx* c, uint64_t* hashes, int64_
                                             int64_t* n_pairs) {
   if (!c) return RPD_ERR_INVALID_ARGUMENT;
   if (!c->has_result) return fail(c, RPD_ERR_NOT_READY, "rpd_copy_topology_hashes_to_host: no result");
+  if (!c->cfg.topology_hash)
+    return fail(c, RPD_ERR_NOT_READY, "rpd_copy_topology_hashes_to_host: topology_hash is off");
   if (n_pairs) *n_pairs = c->n_pairs;
   if (!hashes) return RPD_OK;
   if (capacity < c->n_pairs) return fail(c, RPD_ERR_CAPACITY, "rpd_copy_topology_hashes_to_host: buffer too small");

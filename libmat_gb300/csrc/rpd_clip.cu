@@ -50,7 +50,7 @@ struct __align__(16) WarpCell {
     struct {
       df n[kMaxP][3];   // plane normal, seed frame, double-float (geometry)
       df d[kMaxP];      // plane offset, seed frame
-      float dl[kMaxP];  // plane offset in the frame of the tet centroid
+      float3 foot[kMaxP];  // foot of the volume origin on each plane
     } g;
   } u;
   int2 id2[kMaxP];
@@ -561,13 +561,14 @@ __device__ void clip_list(WarpCell& c, CellState& s, const int32_t* list, int k,
 // The float planes above decide the topology exactly as the reference does.
 // The coordinates reported for the surviving vertices are rebuilt from the
 // FP64 inputs instead: every plane is recomputed in the frame centred on the
-// seed S (differences of FP64 coordinates, rounded once), and each vertex --
-// the intersection of its three planes, by Cramer's rule as in
-// compute_vertex_coordinates (convex_cell.cu:319-351) -- is solved in
-// double-float arithmetic on the FP32 pipe, then translated back by S in
-// FP64.  The cell volume uses the reference's per-vertex decomposition into
-// six tets (convex_cell.cu:986-1069) in FP32, about the tet centroid (small
-// coordinates, no cancellation against the scene's extent).
+// seed S, from double-float copies of the FP64 mesh vertices and sites
+// (hi + lo, about 48 bits), and each vertex -- the intersection of its three
+// planes, by Cramer's rule as in compute_vertex_coordinates
+// (convex_cell.cu:319-351) -- is solved in double-float arithmetic on the
+// FP32 pipe, then translated back by S and rounded to FP64 with one FP64
+// add.  The cell volume uses the reference's per-vertex decomposition into
+// six tets (convex_cell.cu:986-1069) in FP32, about a point of the cell
+// (small coordinates, no cancellation against the scene's extent).
 
 __device__ __forceinline__ df dmul3(df a, df b, df c) { return df_mul(df_mul(a, b), c); }
 
@@ -588,19 +589,23 @@ __device__ __forceinline__ float3 f3axpy(float a, float3 x, float3 y) {
 }
 __device__ __forceinline__ float det3f(float3 a, float3 b, float3 c) { return f3dot(a, f3cross(b, c)); }
 
-// signed volume of one vertex's six flag tets, origin O = (0,0,0):
-// feet of O on the three faces and on the three edge lines through A
-__device__ float vertex_volume_f(float3 A, const float3* n, const float* d) {
+// foot of the origin O = (0,0,0) on the plane n.x + d = 0
+__device__ __forceinline__ float3 face_foot(float3 n, float d) {
+  const float n2 = f3dot(n, n);
+  const float lam = n2 > 0.f ? __fdividef(d, n2) : 0.f;
+  return make_float3(-lam * n.x, -lam * n.y, -lam * n.z);
+}
+
+// signed volume of one vertex's six flag tets, origin O = (0,0,0): feet of
+// O on the three faces (given) and on the three edge lines through A.  The
+// volume is reported in FP32, so the quotients use the fast division.
+__device__ float vertex_volume_f(float3 A, const float3* n, const float3* foot) {
   float3 P[6];
-  for (int i = 0; i < 3; ++i) {
-    float n2 = f3dot(n[i], n[i]);
-    float lam = n2 > 0.f ? d[i] / n2 : 0.f;
-    P[2 * i] = make_float3(-lam * n[i].x, -lam * n[i].y, -lam * n[i].z);
-  }
+  for (int i = 0; i < 3; ++i) P[2 * i] = foot[i];
   for (int i = 0; i < 3; ++i) {
     float3 t = f3cross(n[i], n[(i + 1) % 3]);
     float t2 = f3dot(t, t);
-    float lam = t2 > 0.f ? f3dot(t, A) / t2 : 0.f;
+    float lam = t2 > 0.f ? __fdividef(f3dot(t, A), t2) : 0.f;
     P[2 * i + 1] = f3axpy(-lam, t, A);
   }
   float3 mA = make_float3(-A.x, -A.y, -A.z);
@@ -648,50 +653,96 @@ __device__ __forceinline__ void cell_vertex(const WarpCell& c, int pa, int pb, i
 }
 
 __device__ __forceinline__ float vertex_volume_about(const WarpCell& c, uchar4 tr, df X, df Y,
-                                                     df Z, df Ox, df Oy, df Oz) {
-  float3 A = make_float3(df_sub(X, Ox).hi, df_sub(Y, Oy).hi, df_sub(Z, Oz).hi);
+                                                     df Z, float3 O) {
+  float3 A = make_float3(df_sub(X, df_make(O.x, 0.f)).hi, df_sub(Y, df_make(O.y, 0.f)).hi,
+                         df_sub(Z, df_make(O.z, 0.f)).hi);
   const int pl[3] = {tr.x, tr.y, tr.z};
-  float3 nn[3];
-  float dd[3];
+  float3 nn[3], ft[3];
   for (int k = 0; k < 3; ++k) {
     nn[k] = make_float3(c.u.g.n[pl[k]][0].hi, c.u.g.n[pl[k]][1].hi, c.u.g.n[pl[k]][2].hi);
-    dd[k] = c.u.g.dl[pl[k]];
+    ft[k] = c.u.g.foot[pl[k]];
   }
-  return vertex_volume_f(A, nn, dd);
+  return vertex_volume_f(A, nn, ft);
+}
+
+__device__ __forceinline__ df ldf(const float2* p) {
+  const float2 v = __ldg(p);
+  return df_make(v.x, v.y);
+}
+
+// exact float -> double widening with integer operations (IEEE-754 binary32
+// to binary64: same sign, exponent re-biased by 1023 - 127, fraction shifted
+// by 29 bits); zeros, subnormals, infinities and NaNs take the conversion
+// instruction
+__device__ __forceinline__ double widen(float f) {
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t e = (u >> 23) & 0xffu;
+  if (e == 0u || e == 0xffu) return (double)f;
+  const uint64_t bits = ((uint64_t)(u >> 31) << 63) | ((uint64_t)(e + 896u) << 52) |
+                        ((uint64_t)(u & 0x7fffffu) << 29);
+  return __longlong_as_double((long long)bits);
+}
+
+// S + X (double-float) rounded to double: hi and lo widen exactly, one add
+__device__ __forceinline__ double df_translate(df S, df X) {
+  const df t = df_add(S, X);
+  return widen(t.hi) + widen(t.lo);
+}
+
+// float intersection of three planes (Cramer); used only as the origin of
+// the volume decomposition, so any point near the cell will do
+__device__ float3 float_vertex(const WarpCell& c, uchar4 tr) {
+  const int pl[3] = {tr.x, tr.y, tr.z};
+  float a[3][4];
+  for (int k = 0; k < 3; ++k) {
+    a[k][0] = c.u.g.n[pl[k]][0].hi;
+    a[k][1] = c.u.g.n[pl[k]][1].hi;
+    a[k][2] = c.u.g.n[pl[k]][2].hi;
+    a[k][3] = c.u.g.d[pl[k]].hi;
+  }
+  // n_k . x = -d_k
+  const float3 n0 = make_float3(a[0][0], a[0][1], a[0][2]);
+  const float3 n1 = make_float3(a[1][0], a[1][1], a[1][2]);
+  const float3 n2 = make_float3(a[2][0], a[2][1], a[2][2]);
+  const float3 c12 = f3cross(n1, n2), c20 = f3cross(n2, n0), c01 = f3cross(n0, n1);
+  const float det = f3dot(n0, c12);
+  const float s = -1.0f / det;
+  float3 x = make_float3(s * (a[0][3] * c12.x + a[1][3] * c20.x + a[2][3] * c01.x),
+                         s * (a[0][3] * c12.y + a[1][3] * c20.y + a[2][3] * c01.y),
+                         s * (a[0][3] * c12.z + a[1][3] * c20.z + a[2][3] * c01.z));
+  if (!(isfinite(x.x) && isfinite(x.y) && isfinite(x.z))) x = make_float3(0.f, 0.f, 0.f);
+  return x;
 }
 
 // writes xyz[3 * nb_v] and returns the cell volume
 __device__ double cell_geometry(WarpCell& c, const CellState& s, const ClipParams& p,
                                 const int* tvs, int sid, int lane, double* xyz) {
-  const double* S = p.site4d + 4 * (long long)sid;
-  const double Sx = S[0], Sy = S[1], Sz = S[2], Sw = S[3];
+  const float2* S2 = p.site2 + 4 * (long long)sid;
+  const df Sx = ldf(S2), Sy = ldf(S2 + 1), Sz = ldf(S2 + 2), Sw = ldf(S2 + 3);
   for (int i = lane; i < s.nb_p; i += 32) {
     df nx, ny, nz, d;
     if (i < 4) {
-      const double* a = p.vert3d + 3 * (long long)tvs[cFaceLv[i][0]];
-      const double* b = p.vert3d + 3 * (long long)tvs[cFaceLv[i][1]];
-      const double* e = p.vert3d + 3 * (long long)tvs[cFaceLv[i][2]];
-      df ax = df_from_double(b[0] - a[0]), ay = df_from_double(b[1] - a[1]),
-         az = df_from_double(b[2] - a[2]);
-      df bx = df_from_double(e[0] - a[0]), by = df_from_double(e[1] - a[1]),
-         bz = df_from_double(e[2] - a[2]);
+      const float2* a = p.vert2 + 3 * (long long)tvs[cFaceLv[i][0]];
+      const float2* b = p.vert2 + 3 * (long long)tvs[cFaceLv[i][1]];
+      const float2* e = p.vert2 + 3 * (long long)tvs[cFaceLv[i][2]];
+      const df a0 = ldf(a), a1 = ldf(a + 1), a2 = ldf(a + 2);
+      const df ax = df_sub(ldf(b), a0), ay = df_sub(ldf(b + 1), a1), az = df_sub(ldf(b + 2), a2);
+      const df bx = df_sub(ldf(e), a0), by = df_sub(ldf(e + 1), a1), bz = df_sub(ldf(e + 2), a2);
       nx = df_sub(df_mul(ay, bz), df_mul(az, by));
       ny = df_sub(df_mul(az, bx), df_mul(ax, bz));
       nz = df_sub(df_mul(ax, by), df_mul(ay, bx));
-      df v0x = df_from_double(a[0] - Sx), v0y = df_from_double(a[1] - Sy),
-         v0z = df_from_double(a[2] - Sz);
+      const df v0x = df_sub(a0, Sx), v0y = df_sub(a1, Sy), v0z = df_sub(a2, Sz);
       d = df_neg(df_add(df_add(df_mul(v0x, nx), df_mul(v0y, ny)), df_mul(v0z, nz)));
     } else {
-      int2 id = c.id2[i];
-      int other = id.x == sid ? id.y : id.x;
-      const double* B = p.site4d + 4 * (long long)other;
+      const int2 id = c.id2[i];
+      const int other = id.x == sid ? id.y : id.x;
+      const float2* B = p.site2 + 4 * (long long)other;
       // bisector in the seed frame: n = S - B, d = (|n|^2 + wS - wB) / 2
-      nx = df_from_double(Sx - B[0]);
-      ny = df_from_double(Sy - B[1]);
-      nz = df_from_double(Sz - B[2]);
-      df n2 = df_add(df_add(df_mul(nx, nx), df_mul(ny, ny)), df_mul(nz, nz));
-      df dw = df_from_double(Sw - B[3]);
-      d = df_add(n2, dw);
+      nx = df_sub(Sx, ldf(B));
+      ny = df_sub(Sy, ldf(B + 1));
+      nz = df_sub(Sz, ldf(B + 2));
+      const df n2 = df_add(df_add(df_mul(nx, nx), df_mul(ny, ny)), df_mul(nz, nz));
+      d = df_add(n2, df_sub(Sw, ldf(B + 3)));
       d = df_make(0.5f * d.hi, 0.5f * d.lo);
     }
     c.u.g.n[i][0] = nx;
@@ -700,41 +751,29 @@ __device__ double cell_geometry(WarpCell& c, const CellState& s, const ClipParam
     c.u.g.d[i] = d;
   }
   __syncwarp();
-  // first pass: vertices lane, lane + 32, lane + 64
-  df X0, Y0, Z0;
-  uchar4 tr0 = make_uchar4(0, 0, 0, 0);
-  if (lane < s.nb_v) {
-    tr0 = c.ver[lane];
-    cell_vertex(c, tr0.x, tr0.y, tr0.z, X0, Y0, Z0);
-    xyz[3 * lane] = Sx + df_to_double(X0);
-    xyz[3 * lane + 1] = Sy + df_to_double(Y0);
-    xyz[3 * lane + 2] = Sz + df_to_double(Z0);
-  }
-  // volume origin O = the cell's vertex 0: the decomposition's terms then
-  // scale with the cell's own size
-  df Ox = df_make(__shfl_sync(0xffffffffu, X0.hi, 0), __shfl_sync(0xffffffffu, X0.lo, 0));
-  df Oy = df_make(__shfl_sync(0xffffffffu, Y0.hi, 0), __shfl_sync(0xffffffffu, Y0.lo, 0));
-  df Oz = df_make(__shfl_sync(0xffffffffu, Z0.hi, 0), __shfl_sync(0xffffffffu, Z0.lo, 0));
+  // volume origin O near the cell (its vertex 0, in float): the
+  // decomposition's terms then scale with the cell's own size
+  const float3 O = float_vertex(c, c.ver[0]);
   for (int i = lane; i < s.nb_p; i += 32) {
-    df n0 = c.u.g.n[i][0], n1 = c.u.g.n[i][1], n2 = c.u.g.n[i][2];
-    df dc = df_add(c.u.g.d[i], df_add(df_add(df_mul(n0, Ox), df_mul(n1, Oy)), df_mul(n2, Oz)));
-    c.u.g.dl[i] = dc.hi;
+    const df n0 = c.u.g.n[i][0], n1 = c.u.g.n[i][1], n2 = c.u.g.n[i][2];
+    const df dc = df_add(c.u.g.d[i], df_add(df_add(df_mul(n0, df_make(O.x, 0.f)),
+                                                   df_mul(n1, df_make(O.y, 0.f))),
+                                            df_mul(n2, df_make(O.z, 0.f))));
+    c.u.g.foot[i] = face_foot(make_float3(n0.hi, n1.hi, n2.hi), dc.hi);
   }
   __syncwarp();
   float vol = 0.f;
-  if (lane < s.nb_v) vol += vertex_volume_about(c, tr0, X0, Y0, Z0, Ox, Oy, Oz);
-  for (int v = lane + 32; v < s.nb_v; v += 32) {
-    uchar4 tr = c.ver[v];
+  for (int v = lane; v < s.nb_v; v += 32) {
+    const uchar4 tr = c.ver[v];
     df X, Y, Z;
     cell_vertex(c, tr.x, tr.y, tr.z, X, Y, Z);
-    xyz[3 * v] = Sx + df_to_double(X);
-    xyz[3 * v + 1] = Sy + df_to_double(Y);
-    xyz[3 * v + 2] = Sz + df_to_double(Z);
-    vol += vertex_volume_about(c, tr, X, Y, Z, Ox, Oy, Oz);
+    xyz[3 * v] = df_translate(Sx, X);
+    xyz[3 * v + 1] = df_translate(Sy, Y);
+    xyz[3 * v + 2] = df_translate(Sz, Z);
+    vol += vertex_volume_about(c, tr, X, Y, Z, O);
   }
-  double dv = (double)vol;
-  for (int o = 16; o > 0; o >>= 1) dv += __shfl_xor_sync(0xffffffffu, dv, o);
-  return dv;
+  for (int o = 16; o > 0; o >>= 1) vol += __shfl_xor_sync(0xffffffffu, vol, o);
+  return (double)vol;
 }
 
 // canonical topology of a cell, independent of the clipping order: the sum

@@ -27,6 +27,8 @@ struct ClipParams {
   const int32_t* f_ids;   // n_tet x 4
   const float4* site4f;   // n_site, (x, y, z, w) float
   const double* site4d;   // n_site x 4
+  const float2* vert2;    // n_vert x 3 double-float (hi, lo) vertex coordinates
+  const float2* site2;    // n_site x 4 double-float (x, y, z, w)
   const int32_t* nbr;     // n_site x k, -1 padded
   int k;
   const int32_t* pair_tet;

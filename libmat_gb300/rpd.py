@@ -42,6 +42,7 @@ EXPORTS = [
     "rpd_mlp_collect", "rpd_mlp_clear_samples", "rpd_mlp_train", "rpd_mlp_enable",
     "rpd_mlp_get_params", "rpd_mlp_set_params", "rpd_mlp_forward", "rpd_mlp_gradient",
     "rpd_mlp_copy_features", "rpd_mlp_copy_klen", "rpd_mlp_copy_samples", "rpd_set_pair_k",
+    "rpd_get_config", "rpd_set_config",
 ]
 
 MLP_FEATURES = 16
@@ -54,7 +55,8 @@ class Config(ctypes.Structure):
                 ("clip_order", ctypes.c_int), ("compute_geometry", ctypes.c_int),
                 ("warps_per_block", ctypes.c_int), ("blocks_per_sm", ctypes.c_int),
                 ("certify", ctypes.c_int), ("clip_variant", ctypes.c_int),
-                ("learned_k", ctypes.c_int), ("reserved", ctypes.c_int * 5)]
+                ("learned_k", ctypes.c_int), ("box_planes", ctypes.c_int),
+                ("topology_hash", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
 
 
 class Stats(ctypes.Structure):
@@ -79,7 +81,8 @@ class Stats(ctypes.Structure):
 class Tuning(ctypes.Structure):
     _fields_ = [("warps_per_block", ctypes.c_int), ("clip_variant", ctypes.c_int),
                 ("k_bucket", ctypes.c_int), ("n_candidates", ctypes.c_int),
-                ("ms_clip_best", ctypes.c_float), ("ms_clip_first", ctypes.c_float)]
+                ("ms_clip_best", ctypes.c_float), ("ms_clip_first", ctypes.c_float),
+                ("learned_k", ctypes.c_int)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -173,6 +176,10 @@ def load(path=LIB_PATH):
     L.rpd_mlp_gradient.argtypes = [vp, vp, vp, i64, vp, c.POINTER(c.c_float)]
     L.rpd_mlp_copy_features.restype = i32
     L.rpd_mlp_copy_features.argtypes = [vp, vp, i64, c.POINTER(i64)]
+    L.rpd_get_config.restype = i32
+    L.rpd_get_config.argtypes = [vp, c.POINTER(Config)]
+    L.rpd_set_config.restype = i32
+    L.rpd_set_config.argtypes = [vp, c.POINTER(Config)]
     L.rpd_set_pair_k.restype = i32
     L.rpd_set_pair_k.argtypes = [vp, vp, i64]
     L.rpd_mlp_copy_samples.restype = i32
@@ -225,7 +232,7 @@ class RPD:
     def __init__(self, device=0, predicate_mode=PRED_FP32_FILTER, neighbor_source=NEIGH_KNN,
                  knn_k=64, clip_order=ORDER_SITE_ID, compute_geometry=True,
                  warps_per_block=0, blocks_per_sm=0, certify=False, clip_variant=0,
-                 learned_k=False):
+                 learned_k=False, box_planes=0, topology_hash=True):
         L = load()
         cfg = Config()
         L.rpd_config_default(ctypes.byref(cfg))
@@ -240,6 +247,8 @@ class RPD:
         cfg.certify = 1 if certify else 0
         cfg.clip_variant = clip_variant
         cfg.learned_k = 1 if learned_k else 0
+        cfg.box_planes = box_planes
+        cfg.topology_hash = 1 if topology_hash else 0
         h = ctypes.c_void_p()
         s = L.rpd_create(ctypes.byref(cfg), ctypes.byref(h))
         if s != 0:
@@ -296,6 +305,24 @@ class RPD:
             return
         a = np.ascontiguousarray(k_per_site, np.int32)
         self._check(self._L.rpd_set_site_k(self._h, _p(a), 0))
+
+    def config(self):
+        cfg = Config()
+        self._check(self._L.rpd_get_config(self._h, ctypes.byref(cfg)))
+        return cfg
+
+    def set_config(self, cfg):
+        """Replaces the whole configuration (a Config from config())."""
+        self._check(self._L.rpd_set_config(self._h, ctypes.byref(cfg)))
+
+    def configure(self, **fields):
+        """Changes configuration fields (e.g. topology_hash=0, clip_variant=2)."""
+        cfg = self.config()
+        for k, v in fields.items():
+            if not hasattr(cfg, k):
+                raise KeyError(k)
+            setattr(cfg, k, int(v))
+        self._check(self._L.rpd_set_config(self._h, ctypes.byref(cfg)))
 
     def set_pair_k(self, k_per_pair):
         """Per-pair list lengths for the next certified compute (None clears)."""
