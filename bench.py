@@ -54,6 +54,10 @@ def make_workload(args):
     if args.config == "small":
         cfg = W.config_small_cube()
         name = "cube_20x20x20x6_48k_tets_2k_sites"
+    elif args.config == "lattice":
+        cfg = W.config_lattice(n=args.lattice_n, m=args.lattice_m)
+        name = "lattice_%d^3_points_%d^3_sites_5pct_perturbed_1e-12" % (args.lattice_n,
+                                                                       args.lattice_m)
     else:
         cfg = W.config_ellipsoid(target_tets=args.tets, n_site=args.sites, seed=2)
         name = "ellipsoid_%dk_tets_%dk_sites" % (round(args.tets / 1000), round(args.sites / 1000))
@@ -427,6 +431,61 @@ def run_ours(args):
     print(json.dumps(line))
 
 
+def run_stress(args):
+    """Near-degenerate predicate stress (--config lattice): lattice cube mesh,
+    lattice sites with equal radii (exact ties), 5% perturbed by N(0, 1e-12).
+    Measures how many predicates the FP32 filter escalates to FP64 and how
+    many FP64 signs are uncertain (decided exactly in RPD_PRED_EXACT), and
+    checks the FP32-filter path's topology against the FP64 path's."""
+    from libmat_gb300 import rpd
+
+    cfg, name, gen_s = make_workload(args)
+    adj = rpd.mesh_adjacency(cfg["vert3d"].shape[0], cfg["tets"])
+
+    def engine(pred, certify=False):
+        r = rpd.RPD(predicate_mode=pred, neighbor_source=rpd.NEIGH_KNN, knn_k=args.k,
+                    clip_order=rpd.ORDER_SITE_ID, certify=certify)
+        r.set_mesh(cfg["vert3d"], cfg["tets"], adj["v_adjs"], adj["e_adj6"], adj["f_adjs"],
+                   adj["f_ids"])
+        r.set_sites(cfg["sites"], cfg["flags"])
+        return r
+
+    out = {}
+    for label, pred, cert in (("plain_fp64", rpd.PRED_FP64, False),
+                              ("fp32_filter", rpd.PRED_FP32_FILTER, False),
+                              ("fp32_filter_certified", rpd.PRED_FP32_FILTER, True),
+                              ("exact", rpd.PRED_EXACT, False)):
+        r = engine(pred, cert)
+        r.configure(topology_hash=0)
+        for _ in range(args.warmup):
+            r.compute()
+        ms, cells = [], 0
+        for _ in range(args.steps):
+            st = r.compute()
+            ms.append(st.ms_total)
+            cells += st.n_cells
+        r.configure(topology_hash=1)
+        st = r.compute()
+        out[label] = {"cells_per_s": cells / (sum(ms) / 1000.0), "ms_per_step": float(np.median(ms)),
+                      "n_pairs": st.n_pairs, "n_cells": st.n_cells,
+                      "predicates": st.n_predicates, "escalated_fp64": st.n_escalated,
+                      "escalated_fraction": st.n_escalated / max(st.n_predicates, 1),
+                      "fp64_uncertain_exact": st.n_fp64_uncertain,
+                      "exact_fraction": st.n_fp64_uncertain / max(st.n_predicates, 1),
+                      "exact_flips": st.n_exact_flips,
+                      "status": r.pair_headers()["status"], "hash": r.topology_hashes()}
+        r.close()
+    base = out["plain_fp64"]
+    for label, o in out.items():
+        o["same_status_as_fp64"] = bool(np.array_equal(o["status"], base["status"]))
+        o["cells_topology_differing_from_fp64"] = int((o["hash"] != base["hash"]).sum())
+    for o in out.values():
+        del o["status"], o["hash"]
+    print(json.dumps({"workload": name, "n_tet": int(cfg["tets"].shape[0]),
+                      "n_site": int(cfg["sites"].shape[0]), "knn_k": args.k,
+                      "generation_s": round(gen_s, 2), "runs": out}))
+
+
 def run_fast_only(args):
     """Set-up plus warmup + steps computes of the fast path, nothing else:
     the command profiled by ncu (launch lists and kernel captures)."""
@@ -435,7 +494,8 @@ def run_fast_only(args):
     cfg, name, _ = make_workload(args)
     adj = rpd.mesh_adjacency(cfg["vert3d"].shape[0], cfg["tets"])
     r = rpd.RPD(predicate_mode=rpd.PRED_FP32_FILTER, neighbor_source=rpd.NEIGH_KNN,
-                knn_k=args.k, clip_order=rpd.ORDER_SITE_ID, certify=True)
+                knn_k=args.k, clip_order=rpd.ORDER_SITE_ID, certify=True,
+                clip_variant=args.clip_variant, topology_hash=False)
     r.set_mesh(cfg["vert3d"], cfg["tets"], adj["v_adjs"], adj["e_adj6"], adj["f_adjs"],
                adj["f_ids"])
     r.set_sites(cfg["sites"], cfg["flags"])
@@ -575,7 +635,9 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="ellipsoid", choices=["ellipsoid", "small"])
+    ap.add_argument("--config", default="ellipsoid", choices=["ellipsoid", "small", "lattice"])
+    ap.add_argument("--lattice-n", type=int, default=100, help="lattice mesh grid points per axis")
+    ap.add_argument("--lattice-m", type=int, default=50, help="lattice sites per axis")
     ap.add_argument("--tets", type=int, default=1_000_000)
     ap.add_argument("--sites", type=int, default=50_000)
     ap.add_argument("--k", type=int, default=64)
@@ -590,11 +652,18 @@ def main():
     ap.add_argument("--train-cells", type=int, default=200_000)
     ap.add_argument("--epochs", type=int, default=20)
     ap.add_argument("--miss-target", type=float, default=0.02)
+    ap.add_argument("--clip-variant", type=int, default=2,
+                    help="--fast-only: clip kernel register budget (2 = the tuned choice)")
     ap.add_argument("--fast-only", action="store_true",
                     help="only the timed fast path (for profiler launch lists)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.config == "lattice":
+        from __graft_entry__ import build
+
+        build()
+        run_stress(args)
     elif args.fast_only:
         from __graft_entry__ import build
 

@@ -45,9 +45,16 @@ typedef enum rpd_status {
  * conflict. */
 typedef enum rpd_predicate_mode {
   RPD_PRED_FP64 = 0,        /* FP64 determinant for every predicate */
-  RPD_PRED_FP32_FILTER = 1  /* FP32 cofactor filter with a proven error
+  RPD_PRED_FP32_FILTER = 1, /* FP32 cofactor filter with a proven error
                                bound; FP64 determinant only when the filter
                                cannot decide.  Same signs as RPD_PRED_FP64. */
+  RPD_PRED_EXACT = 2        /* FP32 filter, then FP64 with its error bound,
+                               then the exact sign by floating-point
+                               expansions where FP64 cannot certify it: the
+                               true sign of the float planes' determinant.
+                               Not in the reference: cells can differ from
+                               it exactly where its FP64 sign is wrong
+                               (counted in rpd_stats.n_exact_flips). */
 } rpd_predicate_mode;
 
 /* Where the per-site neighbour lists come from. */
@@ -137,6 +144,12 @@ typedef struct rpd_stats {
                                  predictor's misses */
   float ms_predict;           /* learned_k: features + inference (in ms_clip) */
   int32_t learned;            /* 1 if the learned list lengths were used */
+  int64_t n_fp64_uncertain;   /* RPD_PRED_EXACT: escalated predicates whose
+                                 FP64 sign is not certified by the FP64 error
+                                 bound, decided by exact arithmetic */
+  int64_t n_exact_flips;      /* RPD_PRED_EXACT: of those, exact sign !=
+                                 FP64 sign (where the reference errs) */
+  float ms_epilogue;          /* coordinates, volumes, hashes (in ms_clip) */
 } rpd_stats;
 
 typedef struct rpd_cells_view {

@@ -72,7 +72,8 @@ struct DevBuf {
 };
 
 enum Ev {
-  kEvStart, kEvKnn, kEvPairs, kEvPred0, kEvPred1, kEvClipK0, kEvClipK1, kEvClip, kEvEnd, kEvCount
+  kEvStart, kEvKnn, kEvPairs, kEvPred0, kEvPred1, kEvClipK0, kEvClipK1, kEvEpi0, kEvClip, kEvEnd,
+  kEvCount
 };
 
 }  // namespace
@@ -309,7 +310,9 @@ void rpd_config_default(rpd_config* cfg) {
 }
 
 static bool config_valid(const rpd_config& c0) {
-  if (c0.predicate_mode != RPD_PRED_FP64 && c0.predicate_mode != RPD_PRED_FP32_FILTER) return false;
+  if (c0.predicate_mode != RPD_PRED_FP64 && c0.predicate_mode != RPD_PRED_FP32_FILTER &&
+      c0.predicate_mode != RPD_PRED_EXACT)
+    return false;
   if (c0.neighbor_source != RPD_NEIGH_USER && c0.neighbor_source != RPD_NEIGH_KNN) return false;
   if (c0.neighbor_source == RPD_NEIGH_KNN && (c0.knn_k < 1 || c0.knn_k > 128)) return false;
   if (c0.warps_per_block < 0 || c0.warps_per_block > kClipMaxThreads / 32 || c0.blocks_per_sm < 0)
@@ -794,7 +797,7 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
   const float cert_margin = (float)(16.0 * std::ldexp(1.0, -24) * (L + std::sqrt(D2)) + 1e-30);
   c->n_reclipped = 0;
   for (int attempt = 0; attempt < 3; ++attempt) {
-    CK(cudaMemsetAsync(c->scratch.ptr + 28, 0, sizeof(unsigned long long), st), "memset");
+    CK(cudaMemsetAsync(c->scratch.ptr + 28, 0, 3 * sizeof(unsigned long long), st), "memset");
     CK(c->payload.ensure((size_t)pcap), "alloc payload");
     CK(cudaMemsetAsync(c->scratch.ptr, 0, 4 * sizeof(unsigned long long), st), "memset");
     ClipParams p;
@@ -820,6 +823,7 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
     p.payload_cap = (unsigned long long)c->payload.cap;
     p.work = c->scratch.ptr + 1;
     p.counters = c->scratch.ptr + 2;
+    p.exact_counters = c->scratch.ptr + 29;
     p.geometry = c->cfg.compute_geometry;
     p.keys = certify ? c->nbr_keys.ptr : nullptr;
     p.site_klen = (certify && c->has_site_klen && !learned && !use_pair_k) ? c->site_klen.ptr : nullptr;
@@ -865,6 +869,20 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
     if (attempt == 2) return fail(c, RPD_ERR_CAPACITY, "rpd_compute: payload buffer");
   }
   c->payload_cap_hint = std::max<long long>(c->payload_cap_hint, c->payload_bytes + c->payload_bytes / 8 + (1 << 20));
+  // coordinates, volumes and topology hashes of the emitted cells
+  CK(cudaEventRecord(c->ev[kEvEpi0], st), "event");
+  {
+    EpilogueParams ep;
+    ep.headers = c->pair_headers.ptr;
+    ep.n_pairs = n_pairs;
+    ep.payload = c->payload.ptr;
+    ep.tets = c->tets.ptr;
+    ep.vert2 = c->vert2.ptr;
+    ep.site2 = c->site2.ptr;
+    ep.geometry = c->cfg.compute_geometry;
+    ep.topo_hash = c->cfg.topology_hash ? c->topo_hash.ptr : nullptr;
+    CK(launch_cell_epilogue(ep, c->num_sms, st), "epilogue");
+  }
   CK(cudaEventRecord(c->ev[kEvClip], st), "event");
 
   // ---- compaction
@@ -908,6 +926,9 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
     stats->n_reclipped = c->n_reclipped;
     cudaEventElapsedTime(&stats->ms_predict, c->ev[kEvPred0], c->ev[kEvPred1]);
     stats->learned = learned ? 1 : 0;
+    stats->n_fp64_uncertain = (int64_t)host_scratch[29];
+    stats->n_exact_flips = (int64_t)host_scratch[30];
+    cudaEventElapsedTime(&stats->ms_epilogue, c->ev[kEvEpi0], c->ev[kEvClip]);
   }
   return RPD_OK;
 }

@@ -171,23 +171,217 @@ __device__ __forceinline__ int filter_sign(float4 K, float4 M, float4 e) {
   return s > b ? 1 : (s < -b ? -1 : 0);
 }
 
+// ------------------------------------------------------------------------
+// FP64 error bound and exact sign of det4x4 (RPD_PRED_EXACT)
+// ------------------------------------------------------------------------
+// det4x4_ref evaluated with the same operations, plus the same expression
+// over absolute values P.  Products of two floats are exact in FP64; every
+// other operation rounds once, at most 8 along any path of the expression,
+// so |computed - exact| <= gamma_8 P < 10 * 2^-53 * P.
+__device__ __forceinline__ double det4x4_with_bound(float4 p1, float4 p2, float4 p3, float4 e,
+                                                    double& bound) {
+  const double a11 = p1.x, a12 = p2.x, a13 = p3.x, a14 = e.x;
+  const double a21 = p1.y, a22 = p2.y, a23 = p3.y, a24 = e.y;
+  const double a31 = p1.z, a32 = p2.z, a33 = p3.z, a34 = e.z;
+  const double a41 = p1.w, a42 = p2.w, a43 = p3.w, a44 = e.w;
+  const double m12 = a21 * a12 - a11 * a22, P12 = fabs(a21 * a12) + fabs(a11 * a22);
+  const double m13 = a31 * a12 - a11 * a32, P13 = fabs(a31 * a12) + fabs(a11 * a32);
+  const double m14 = a41 * a12 - a11 * a42, P14 = fabs(a41 * a12) + fabs(a11 * a42);
+  const double m23 = a31 * a22 - a21 * a32, P23 = fabs(a31 * a22) + fabs(a21 * a32);
+  const double m24 = a41 * a22 - a21 * a42, P24 = fabs(a41 * a22) + fabs(a21 * a42);
+  const double m34 = a41 * a32 - a31 * a42, P34 = fabs(a41 * a32) + fabs(a31 * a42);
+  const double m123 = m23 * a13 - m13 * a23 + m12 * a33;
+  const double m124 = m24 * a13 - m14 * a23 + m12 * a43;
+  const double m134 = m34 * a13 - m14 * a33 + m13 * a43;
+  const double m234 = m34 * a23 - m24 * a33 + m23 * a43;
+  const double P123 = P23 * fabs(a13) + P13 * fabs(a23) + P12 * fabs(a33);
+  const double P124 = P24 * fabs(a13) + P14 * fabs(a23) + P12 * fabs(a43);
+  const double P134 = P34 * fabs(a13) + P14 * fabs(a33) + P13 * fabs(a43);
+  const double P234 = P34 * fabs(a23) + P24 * fabs(a33) + P23 * fabs(a43);
+  const double P = P234 * fabs(a14) + P134 * fabs(a24) + P124 * fabs(a34) + P123 * fabs(a44);
+  bound = 10.0 * 1.1102230246251565e-16 * P + 1e-300;
+  return (m234 * a14 - m134 * a24 + m124 * a34 - m123 * a44);
+}
+
+// Exact sign by floating-point expansions (Shewchuk, "Adaptive precision
+// floating-point arithmetic and fast robust geometric predicates", Discrete
+// Comput. Geom. 18, 1997): TwoSum, TwoProduct (with FMA),
+// FAST-EXPANSION-SUM and SCALE-EXPANSION, both with zero elimination.
+// Expansions are nonoverlapping, in increasing magnitude.
+__device__ __forceinline__ void ex_two_sum(double a, double b, double& x, double& y) {
+  x = a + b;
+  const double bv = x - a;
+  const double av = x - bv;
+  y = (a - av) + (b - bv);
+}
+__device__ __forceinline__ void ex_fast_two_sum(double a, double b, double& x, double& y) {
+  x = a + b;
+  y = b - (x - a);
+}
+__device__ __forceinline__ void ex_two_prod(double a, double b, double& x, double& y) {
+  x = a * b;
+  y = fma(a, b, -x);
+}
+
+__device__ int ex_sum(int elen, const double* e, int flen, const double* f, double* h) {
+  int ei = 0, fi = 0, hi = 0;
+  double en = e[0], fn = f[0], Q, Qn, hh;
+  if ((fn > en) == (fn > -en)) {
+    Q = en;
+    en = ++ei < elen ? e[ei] : 0.0;
+  } else {
+    Q = fn;
+    fn = ++fi < flen ? f[fi] : 0.0;
+  }
+  if (ei < elen && fi < flen) {
+    if ((fn > en) == (fn > -en)) {
+      ex_fast_two_sum(en, Q, Qn, hh);
+      en = ++ei < elen ? e[ei] : 0.0;
+    } else {
+      ex_fast_two_sum(fn, Q, Qn, hh);
+      fn = ++fi < flen ? f[fi] : 0.0;
+    }
+    Q = Qn;
+    if (hh != 0.0) h[hi++] = hh;
+    while (ei < elen && fi < flen) {
+      if ((fn > en) == (fn > -en)) {
+        ex_two_sum(Q, en, Qn, hh);
+        en = ++ei < elen ? e[ei] : 0.0;
+      } else {
+        ex_two_sum(Q, fn, Qn, hh);
+        fn = ++fi < flen ? f[fi] : 0.0;
+      }
+      Q = Qn;
+      if (hh != 0.0) h[hi++] = hh;
+    }
+  }
+  while (ei < elen) {
+    ex_two_sum(Q, en, Qn, hh);
+    en = ++ei < elen ? e[ei] : 0.0;
+    Q = Qn;
+    if (hh != 0.0) h[hi++] = hh;
+  }
+  while (fi < flen) {
+    ex_two_sum(Q, fn, Qn, hh);
+    fn = ++fi < flen ? f[fi] : 0.0;
+    Q = Qn;
+    if (hh != 0.0) h[hi++] = hh;
+  }
+  if (Q != 0.0 || hi == 0) h[hi++] = Q;
+  return hi;
+}
+
+__device__ int ex_scale(int elen, const double* e, double b, double* h) {
+  int hi = 0;
+  double Q, hh, p1, p0, sum;
+  ex_two_prod(e[0], b, Q, hh);
+  if (hh != 0.0) h[hi++] = hh;
+  for (int i = 1; i < elen; ++i) {
+    ex_two_prod(e[i], b, p1, p0);
+    ex_two_sum(Q, p0, sum, hh);
+    if (hh != 0.0) h[hi++] = hh;
+    ex_fast_two_sum(p1, sum, Q, hh);
+    if (hh != 0.0) h[hi++] = hh;
+  }
+  if (Q != 0.0 || hi == 0) h[hi++] = Q;
+  return hi;
+}
+
+// 2x2 minor a*b - c*d of floats (both products exact in FP64)
+__device__ __forceinline__ int ex_minor2(double a, double b, double c, double d, double* h) {
+  double x, y;
+  ex_two_sum(a * b, -(c * d), x, y);
+  int n = 0;
+  if (y != 0.0) h[n++] = y;
+  if (x != 0.0 || n == 0) h[n++] = x;
+  return n;
+}
+
+// u*a - v*b + w*c for expansions u, v, w (<= lu, lv, lw terms)
+__device__ int ex_combine3(const double* u, int lu, double a, const double* v, int lv, double b,
+                           const double* w, int lw, double c, double* h) {
+  double t1[24], t2[24], t3[24], t12[48];
+  const int n1 = ex_scale(lu, u, a, t1);
+  const int n2 = ex_scale(lv, v, -b, t2);
+  const int n3 = ex_scale(lw, w, c, t3);
+  const int n12 = ex_sum(n1, t1, n2, t2, t12);
+  return ex_sum(n12, t12, n3, t3, h);
+}
+
+// exact sign of det4x4_ref's determinant (same matrix, no rounding)
+__device__ __noinline__ int det4x4_exact_sign(float4 p1, float4 p2, float4 p3, float4 e) {
+  const double a11 = p1.x, a12 = p2.x, a13 = p3.x, a14 = e.x;
+  const double a21 = p1.y, a22 = p2.y, a23 = p3.y, a24 = e.y;
+  const double a31 = p1.z, a32 = p2.z, a33 = p3.z, a34 = e.z;
+  const double a41 = p1.w, a42 = p2.w, a43 = p3.w, a44 = e.w;
+  double m12[2], m13[2], m14[2], m23[2], m24[2], m34[2];
+  const int l12 = ex_minor2(a21, a12, a11, a22, m12);
+  const int l13 = ex_minor2(a31, a12, a11, a32, m13);
+  const int l14 = ex_minor2(a41, a12, a11, a42, m14);
+  const int l23 = ex_minor2(a31, a22, a21, a32, m23);
+  const int l24 = ex_minor2(a41, a22, a21, a42, m24);
+  const int l34 = ex_minor2(a41, a32, a31, a42, m34);
+  double m123[12], m124[12], m134[12], m234[12];
+  const int l123 = ex_combine3(m23, l23, a13, m13, l13, a23, m12, l12, a33, m123);
+  const int l124 = ex_combine3(m24, l24, a13, m14, l14, a23, m12, l12, a43, m124);
+  const int l134 = ex_combine3(m34, l34, a13, m14, l14, a33, m13, l13, a43, m134);
+  const int l234 = ex_combine3(m34, l34, a23, m24, l24, a33, m23, l23, a43, m234);
+  // m234 a14 - m134 a24 + m124 a34 - m123 a44
+  double t1[24], t2[24], t3[24], t4[24], s12[48], s34[48], d[96];
+  const int n1 = ex_scale(l234, m234, a14, t1);
+  const int n2 = ex_scale(l134, m134, -a24, t2);
+  const int n3 = ex_scale(l124, m124, a34, t3);
+  const int n4 = ex_scale(l123, m123, -a44, t4);
+  const int n12 = ex_sum(n1, t1, n2, t2, s12);
+  const int n34 = ex_sum(n3, t3, n4, t4, s34);
+  const int n = ex_sum(n12, s12, n34, s34, d);
+  const double top = d[n - 1];
+  return top > 0.0 ? 1 : (top < 0.0 ? -1 : 0);
+}
+
 __device__ __forceinline__ bool plane_eq(float4 a, float4 b) {
   return a.x == b.x && a.y == b.y && a.z == b.z && a.w == b.w;
+}
+
+// predicate statistics of a thread: evaluated, escalated to FP64; and where
+// the escalations of RPD_PRED_EXACT count their FP64-uncertain / exact-flip
+// cases
+struct PredCount {
+  uint32_t pred, esc;
+  unsigned long long* exact;
+};
+
+__host__ __device__ constexpr bool uses_filter(int pred) {
+  return pred == RPD_PRED_FP32_FILTER || pred == RPD_PRED_EXACT;
+}
+
+// RPD_PRED_EXACT: the predicates the filter cannot decide, out of line
+// (rare).  counts (optional): [0] FP64 signs not certified by their error
+// bound (decided exactly), [1] exact signs different from the FP64 sign
+__device__ __noinline__ bool exact_conflict(float4 p1, float4 p2, float4 p3, float4 e,
+                                            unsigned long long* counts) {
+  double bound;
+  const double d = det4x4_with_bound(p1, p2, p3, e, bound);
+  if (fabs(d) > bound) return d > 0.0;
+  if (counts) atomicAdd(counts, 1ull);
+  const int xs = det4x4_exact_sign(p1, p2, p3, e);
+  if (counts && (xs > 0) != (d > 0.0)) atomicAdd(counts + 1, 1ull);
+  return xs > 0;
 }
 
 // conflict of the vertex in slot vi with plane e; dup = planes identical to e
 template <int PRED>
 __device__ __forceinline__ bool in_conflict(const WarpCell& c, int vi, float4 e,
-                                            uint64_t dup,
-                                            uint32_t& n_pred, uint32_t& n_esc) {
+                                            uint64_t dup, PredCount& pc) {
   uchar4 v = c.ver[vi];
   uint64_t vm = (1ull << v.x) | (1ull << v.y) | (1ull << v.z);
   if (dup & vm) return false;
-  ++n_pred;
-  if (PRED == RPD_PRED_FP32_FILTER) {
+  ++pc.pred;
+  if (uses_filter(PRED)) {
     int s = filter_sign(c.u.f.K[vi], c.u.f.M[vi], e);
     if (s != 0) return s > 0;
-    ++n_esc;
+    ++pc.esc;
+    if (PRED == RPD_PRED_EXACT) return exact_conflict(c.pl[v.x], c.pl[v.y], c.pl[v.z], e, pc.exact);
   }
   return det4x4_ref(c.pl[v.x], c.pl[v.y], c.pl[v.z], e) > 0.0;
 }
@@ -445,8 +639,8 @@ __device__ __forceinline__ bool cert_holds(float key, float R, float margin) {
 template <int PRED, bool FULL, bool CERT, class MakePlane>
 __device__ void clip_list(WarpCell& c, CellState& s, const int32_t* list, int k,
                           int seed_id, MakePlane make_plane, int lane,
-                          uint32_t& n_pred, uint32_t& n_esc, Cert& cert) {
-  constexpr bool kCof = PRED == RPD_PRED_FP32_FILTER || CERT;
+                          PredCount& pc, Cert& cert) {
+  constexpr bool kCof = uses_filter(PRED) || CERT;
   const bool eager = CERT && !cert.lazy;
   float R = INFINITY;
   if (eager) R = cell_radius(c, s.nb_v, cert.S, lane);
@@ -487,7 +681,7 @@ __device__ void clip_list(WarpCell& c, CellState& s, const int32_t* list, int k,
         float4 e = shfl4(e_mine, pidx & 31);
         uint64_t dup = shfl64(dup_mine, pidx & 31);
         bool cf = false;
-        if (pidx < count && vi < s.nb_v) cf = in_conflict<PRED>(c, vi, e, dup, n_pred, n_esc);
+        if (pidx < count && vi < s.nb_v) cf = in_conflict<PRED>(c, vi, e, dup, pc);
         uint32_t m = __ballot_sync(0xffffffffu, cf);
         if (m == 0u) {
           r += 32 >> lgV;
@@ -503,7 +697,7 @@ __device__ void clip_list(WarpCell& c, CellState& s, const int32_t* list, int k,
         for (int w = 0; w < 3; ++w) {
           int vi = lane + 32 * w;
           bool cf = false;
-          if (vi < s.nb_v) cf = in_conflict<PRED>(c, vi, e, dup, n_pred, n_esc);
+          if (vi < s.nb_v) cf = in_conflict<PRED>(c, vi, e, dup, pc);
           mask[w] = __ballot_sync(0xffffffffu, cf);
           any |= mask[w] != 0u;
         }
@@ -635,7 +829,8 @@ __device__ void vertex_of_float_planes(float4 a4, float4 b4, float4 c4, double* 
 }
 
 // vertex (X, Y, Z) of the three seed-frame double-float planes pa, pb, pc
-__device__ __forceinline__ void cell_vertex(const WarpCell& c, int pa, int pb, int pc, df& X,
+template <class Cell>
+__device__ __forceinline__ void cell_vertex(const Cell& c, int pa, int pb, int pc, df& X,
                                             df& Y, df& Z) {
   df ax = c.u.g.n[pa][0], ay = c.u.g.n[pa][1], az = c.u.g.n[pa][2], aw = c.u.g.d[pa];
   df bx = c.u.g.n[pb][0], by = c.u.g.n[pb][1], bz = c.u.g.n[pb][2], bw = c.u.g.d[pb];
@@ -652,7 +847,8 @@ __device__ __forceinline__ void cell_vertex(const WarpCell& c, int pa, int pb, i
   Z = df_neg(df_mul(Dz, inv));
 }
 
-__device__ __forceinline__ float vertex_volume_about(const WarpCell& c, uchar4 tr, df X, df Y,
+template <class Cell>
+__device__ __forceinline__ float vertex_volume_about(const Cell& c, uchar4 tr, df X, df Y,
                                                      df Z, float3 O) {
   float3 A = make_float3(df_sub(X, df_make(O.x, 0.f)).hi, df_sub(Y, df_make(O.y, 0.f)).hi,
                          df_sub(Z, df_make(O.z, 0.f)).hi);
@@ -691,7 +887,8 @@ __device__ __forceinline__ double df_translate(df S, df X) {
 
 // float intersection of three planes (Cramer); used only as the origin of
 // the volume decomposition, so any point near the cell will do
-__device__ float3 float_vertex(const WarpCell& c, uchar4 tr) {
+template <class Cell>
+__device__ float3 float_vertex(const Cell& c, uchar4 tr) {
   const int pl[3] = {tr.x, tr.y, tr.z};
   float a[3][4];
   for (int k = 0; k < 3; ++k) {
@@ -714,17 +911,20 @@ __device__ float3 float_vertex(const WarpCell& c, uchar4 tr) {
   return x;
 }
 
-// writes xyz[3 * nb_v] and returns the cell volume
-__device__ double cell_geometry(WarpCell& c, const CellState& s, const ClipParams& p,
-                                const int* tvs, int sid, int lane, double* xyz) {
-  const float2* S2 = p.site2 + 4 * (long long)sid;
+// writes xyz[3 * nb_v] and returns the cell volume; c holds the cell's
+// id2 and ver, c.u.g is filled here
+template <class Cell>
+__device__ double cell_geometry(Cell& c, int nb_v, int nb_p, const float2* vert2,
+                                const float2* site2, const int* tvs, int sid, int lane,
+                                double* xyz) {
+  const float2* S2 = site2 + 4 * (long long)sid;
   const df Sx = ldf(S2), Sy = ldf(S2 + 1), Sz = ldf(S2 + 2), Sw = ldf(S2 + 3);
-  for (int i = lane; i < s.nb_p; i += 32) {
+  for (int i = lane; i < nb_p; i += 32) {
     df nx, ny, nz, d;
     if (i < 4) {
-      const float2* a = p.vert2 + 3 * (long long)tvs[cFaceLv[i][0]];
-      const float2* b = p.vert2 + 3 * (long long)tvs[cFaceLv[i][1]];
-      const float2* e = p.vert2 + 3 * (long long)tvs[cFaceLv[i][2]];
+      const float2* a = vert2 + 3 * (long long)tvs[cFaceLv[i][0]];
+      const float2* b = vert2 + 3 * (long long)tvs[cFaceLv[i][1]];
+      const float2* e = vert2 + 3 * (long long)tvs[cFaceLv[i][2]];
       const df a0 = ldf(a), a1 = ldf(a + 1), a2 = ldf(a + 2);
       const df ax = df_sub(ldf(b), a0), ay = df_sub(ldf(b + 1), a1), az = df_sub(ldf(b + 2), a2);
       const df bx = df_sub(ldf(e), a0), by = df_sub(ldf(e + 1), a1), bz = df_sub(ldf(e + 2), a2);
@@ -736,7 +936,7 @@ __device__ double cell_geometry(WarpCell& c, const CellState& s, const ClipParam
     } else {
       const int2 id = c.id2[i];
       const int other = id.x == sid ? id.y : id.x;
-      const float2* B = p.site2 + 4 * (long long)other;
+      const float2* B = site2 + 4 * (long long)other;
       // bisector in the seed frame: n = S - B, d = (|n|^2 + wS - wB) / 2
       nx = df_sub(Sx, ldf(B));
       ny = df_sub(Sy, ldf(B + 1));
@@ -754,7 +954,7 @@ __device__ double cell_geometry(WarpCell& c, const CellState& s, const ClipParam
   // volume origin O near the cell (its vertex 0, in float): the
   // decomposition's terms then scale with the cell's own size
   const float3 O = float_vertex(c, c.ver[0]);
-  for (int i = lane; i < s.nb_p; i += 32) {
+  for (int i = lane; i < nb_p; i += 32) {
     const df n0 = c.u.g.n[i][0], n1 = c.u.g.n[i][1], n2 = c.u.g.n[i][2];
     const df dc = df_add(c.u.g.d[i], df_add(df_add(df_mul(n0, df_make(O.x, 0.f)),
                                                    df_mul(n1, df_make(O.y, 0.f))),
@@ -763,7 +963,7 @@ __device__ double cell_geometry(WarpCell& c, const CellState& s, const ClipParam
   }
   __syncwarp();
   float vol = 0.f;
-  for (int v = lane; v < s.nb_v; v += 32) {
+  for (int v = lane; v < nb_v; v += 32) {
     const uchar4 tr = c.ver[v];
     df X, Y, Z;
     cell_vertex(c, tr.x, tr.y, tr.z, X, Y, Z);
@@ -792,7 +992,8 @@ __device__ __forceinline__ uint64_t face_key(int2 id) {
   return ((uint64_t)(uint32_t)id.x << 32) | (uint32_t)id.y;
 }
 
-__device__ uint64_t cell_topology_hash(const WarpCell& c, int nb_v, int lane) {
+template <class Cell>
+__device__ uint64_t cell_topology_hash(const Cell& c, int nb_v, int lane) {
   uint64_t h = 0;
   for (int v = lane; v < nb_v; v += 32) {
     uchar4 t = c.ver[v];
@@ -819,7 +1020,7 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : kClipMaxThreads, MINB > 0 ? M
   const int lane = threadIdx.x & 31;
   const int wid = threadIdx.x >> 5;
   WarpCell& c = reinterpret_cast<WarpCell*>(smem_raw)[wid];
-  uint32_t n_pred = 0, n_esc = 0;
+  PredCount pc = {0u, 0u, p.exact_counters};
 
   for (;;) {
     long long q = 0;
@@ -857,7 +1058,7 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : kClipMaxThreads, MINB > 0 ? M
     s.nb_p = 4;
     s.nb_e = 6;
     s.status = kSuccess;
-    if (PRED == RPD_PRED_FP32_FILTER || CERT) {
+    if (uses_filter(PRED) || CERT) {
       refresh_cofactors(c, 0, 4, lane);
       __syncwarp();
     }
@@ -875,7 +1076,7 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : kClipMaxThreads, MINB > 0 ? M
     cert.margin = p.cert_margin;
     cert.lazy = p.lazy_cert != 0;
     cert.certified = false;
-    clip_list<PRED, true, CERT>(c, s, list, klen, sid, make_plane, lane, n_pred, n_esc, cert);
+    clip_list<PRED, true, CERT>(c, s, list, klen, sid, make_plane, lane, pc, cert);
     // a shortened list that ran out before the certificate held: the cell
     // is clipped again with the whole list (status kSecurityRadiusNotReached
     // marks it)
@@ -928,38 +1129,96 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : kClipMaxThreads, MINB > 0 ? M
           reinterpret_cast<uint32_t*>(dst + L.ver)[i] = 0u;
         for (int i = s.nb_e + lane; i < (int)(al16(4u * s.nb_e) / 4); i += 32)
           reinterpret_cast<uint32_t*>(dst + L.edge)[i] = 0u;
-        double* xyz = reinterpret_cast<double*>(dst + L.xyz);
-        double vol = 0.0;
-        if (p.geometry) {
-          __syncwarp();
-          vol = cell_geometry(c, s, p, tvs, sid, lane, xyz);
-        } else {
-          for (int i = lane; i < 3 * s.nb_v; i += 32) xyz[i] = 0.0;
-        }
+        // coordinates, volume and topology hash: cell_epilogue_kernel
         hd.nb_v = (uint8_t)s.nb_v;
         hd.nb_p = (uint8_t)s.nb_p;
         hd.nb_e = (uint8_t)s.nb_e;
         hd.offset = off;
-        hd.volume = vol;
       }
     }
-    uint64_t th = 0;
-    if (p.topo_hash && hd.status == kSuccess) th = cell_topology_hash(c, s.nb_v, lane);
-    if (lane == 0) {
-      p.headers[q] = hd;
-      if (p.topo_hash) p.topo_hash[q] = th;
-    }
+    if (lane == 0) p.headers[q] = hd;
     __syncwarp();
   }
   // statistics
   for (int o = 16; o > 0; o >>= 1) {
-    n_pred += __shfl_xor_sync(0xffffffffu, n_pred, o);
-    n_esc += __shfl_xor_sync(0xffffffffu, n_esc, o);
+    pc.pred += __shfl_xor_sync(0xffffffffu, pc.pred, o);
+    pc.esc += __shfl_xor_sync(0xffffffffu, pc.esc, o);
   }
   if (lane == 0) {
-    atomicAdd(p.counters + 0, (unsigned long long)n_pred);
-    atomicAdd(p.counters + 1, (unsigned long long)n_esc);
+    atomicAdd(p.counters + 0, (unsigned long long)pc.pred);
+    atomicAdd(p.counters + 1, (unsigned long long)pc.esc);
   }
+}
+
+// ------------------------------------------------------------------------
+// epilogue: FP64-accurate coordinates and volume, canonical topology hash,
+// of every emitted cell, from its record (plane ids and dual triangles)
+// ------------------------------------------------------------------------
+// The clip kernel leaves these to a separate pass: it keeps the clip
+// kernel's code (and its instruction-cache footprint) to the topology
+// update, and every warp here runs the same short program.  The first four
+// planes of every record are the tet's faces, in order; the others are
+// bisectors with the site pair in id2.
+struct GeomCell {
+  struct {
+    struct {
+      df n[kMaxP][3];
+      df d[kMaxP];
+      float3 foot[kMaxP];
+    } g;
+  } u;
+  int2 id2[kMaxP];
+  uchar4 ver[kMaxT];
+};
+
+__global__ void __launch_bounds__(256) cell_epilogue_kernel(EpilogueParams p) {
+  __shared__ GeomCell cells[8];
+  const int lane = threadIdx.x & 31;
+  GeomCell& c = cells[threadIdx.x >> 5];
+  const long long n_warps = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long q = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < p.n_pairs;
+       q += n_warps) {
+    const rpd_cell_header hd = p.headers[q];
+    if (hd.status != kSuccess) {
+      if (p.topo_hash && lane == 0) p.topo_hash[q] = 0ull;
+      continue;
+    }
+    const int nb_v = hd.nb_v, nb_p = hd.nb_p;
+    const PayloadLayout L(nb_v, nb_p, hd.nb_e);
+    uint8_t* rec = p.payload + hd.offset;
+    for (int i = lane; i < nb_p; i += 32) c.id2[i] = reinterpret_cast<const int2*>(rec + L.id2)[i];
+    for (int i = lane; i < nb_v; i += 32) c.ver[i] = reinterpret_cast<const uchar4*>(rec + L.ver)[i];
+    __syncwarp();
+    double* xyz = reinterpret_cast<double*>(rec + L.xyz);
+    double vol = 0.0;
+    if (p.geometry) {
+      const int4 tv = __ldg(p.tets + hd.tet_id);
+      const int tvs[4] = {tv.x, tv.y, tv.z, tv.w};
+      vol = cell_geometry(c, nb_v, nb_p, p.vert2, p.site2, tvs, hd.site_id, lane, xyz);
+    } else {
+      for (int i = lane; i < 3 * nb_v; i += 32) xyz[i] = 0.0;
+    }
+    uint64_t th = 0;
+    if (p.topo_hash) th = cell_topology_hash(c, nb_v, lane);
+    if (lane == 0) {
+      p.headers[q].volume = vol;
+      if (p.topo_hash) p.topo_hash[q] = th;
+    }
+    __syncwarp();
+  }
+}
+
+cudaError_t launch_cell_epilogue(const EpilogueParams& p, int num_sms, cudaStream_t st) {
+  if (p.n_pairs <= 0) return cudaSuccess;
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cell_epilogue_kernel, 256, 0);
+  if (per_sm < 1) per_sm = 1;
+  long long want = (p.n_pairs + 7) / 8;
+  long long blocks = (long long)num_sms * per_sm * 4;
+  if (blocks > want) blocks = want;
+  cell_epilogue_kernel<<<(unsigned)blocks, 256, 0, st>>>(p);
+  note_launches(1);
+  return cudaGetLastError();
 }
 
 // ------------------------------------------------------------------------
@@ -971,7 +1230,7 @@ __global__ void __launch_bounds__(kClipMaxThreads) site_box_kernel(BoxParams p) 
   const int lane = threadIdx.x & 31;
   const int wid = threadIdx.x >> 5;
   WarpCell& c = reinterpret_cast<WarpCell*>(smem_raw)[wid];
-  uint32_t n_pred = 0, n_esc = 0;
+  PredCount pc = {0u, 0u, nullptr};
   const int warps_total = (gridDim.x * blockDim.x) >> 5;
   for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < p.n_site; i += warps_total) {
     float lo[3] = {p.box_lo.x, p.box_lo.y, p.box_lo.z};
@@ -1036,7 +1295,7 @@ __global__ void __launch_bounds__(kClipMaxThreads) site_box_kernel(BoxParams p) 
     nocert.keys = nullptr;
     nocert.certified = false;
     clip_list<RPD_PRED_FP32_FILTER, false, false>(c, s, p.nbr + (long long)i * p.k, p.k_box, i,
-                                                  make_plane, lane, n_pred, n_esc, nocert);
+                                                  make_plane, lane, pc, nocert);
     float bl[3], bh[3];
     if (s.status == kSuccess) {
       bl[0] = bl[1] = bl[2] = 3.0e38f;
@@ -1100,12 +1359,12 @@ __global__ void __launch_bounds__(kClipMaxThreads) site_box_kernel(BoxParams p) 
     __syncwarp();
   }
   for (int o = 16; o > 0; o >>= 1) {
-    n_pred += __shfl_xor_sync(0xffffffffu, n_pred, o);
-    n_esc += __shfl_xor_sync(0xffffffffu, n_esc, o);
+    pc.pred += __shfl_xor_sync(0xffffffffu, pc.pred, o);
+    pc.esc += __shfl_xor_sync(0xffffffffu, pc.esc, o);
   }
   if (lane == 0 && p.counters) {
-    atomicAdd(p.counters + 0, (unsigned long long)n_pred);
-    atomicAdd(p.counters + 1, (unsigned long long)n_esc);
+    atomicAdd(p.counters + 0, (unsigned long long)pc.pred);
+    atomicAdd(p.counters + 1, (unsigned long long)pc.esc);
   }
 }
 
@@ -1133,6 +1392,9 @@ int clip_blocks_per_sm_cert(int pred_mode, int certify, int warps, int variant) 
   if (pred_mode == RPD_PRED_FP32_FILTER)
     return certify ? occ_variant<RPD_PRED_FP32_FILTER, true>(variant, warps)
                    : occ_variant<RPD_PRED_FP32_FILTER, false>(variant, warps);
+  if (pred_mode == RPD_PRED_EXACT)
+    return certify ? occ_variant<RPD_PRED_EXACT, true>(variant, warps)
+                   : occ_variant<RPD_PRED_EXACT, false>(variant, warps);
   return certify ? occ_variant<RPD_PRED_FP64, true>(variant, warps)
                  : occ_variant<RPD_PRED_FP64, false>(variant, warps);
 }
@@ -1171,6 +1433,9 @@ cudaError_t launch_clip_cells(const ClipParams& p, int pred_mode, int certify, i
   if (pred_mode == RPD_PRED_FP32_FILTER) {
     if (certify) launch_variant<RPD_PRED_FP32_FILTER, true>(p, variant, blocks, warps, st);
     else launch_variant<RPD_PRED_FP32_FILTER, false>(p, variant, blocks, warps, st);
+  } else if (pred_mode == RPD_PRED_EXACT) {
+    if (certify) launch_variant<RPD_PRED_EXACT, true>(p, variant, blocks, warps, st);
+    else launch_variant<RPD_PRED_EXACT, false>(p, variant, blocks, warps, st);
   } else {
     if (certify) launch_variant<RPD_PRED_FP64, true>(p, variant, blocks, warps, st);
     else launch_variant<RPD_PRED_FP64, false>(p, variant, blocks, warps, st);

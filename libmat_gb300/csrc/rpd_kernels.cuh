@@ -40,6 +40,7 @@ struct ClipParams {
   unsigned long long payload_cap;
   unsigned long long* work;      // work-queue counter, zeroed before launch
   unsigned long long* counters;  // [0] predicates, [1] escalated
+  unsigned long long* exact_counters;  // [0] FP64 sign uncertain, [1] exact != FP64, or null
   int geometry;
   // distance-ordered lists with the security-radius certificate
   const float* keys;             // n_site x k bisector distances (ascending), or null
@@ -54,6 +55,20 @@ struct ClipParams {
   long long n_work;
   unsigned long long* topo_hash;  // n_pairs canonical topology hashes, or null
 };
+
+// coordinates, volume and topology hash of the emitted cells (after the
+// clip passes, before compaction)
+struct EpilogueParams {
+  rpd_cell_header* headers;  // n_pairs; volume written for emitted cells
+  long long n_pairs;
+  uint8_t* payload;          // xyz sections written
+  const int4* tets;
+  const float2* vert2;
+  const float2* site2;
+  int geometry;                   // 0: xyz zero, volume 0
+  unsigned long long* topo_hash;  // n_pairs, or null
+};
+cudaError_t launch_cell_epilogue(const EpilogueParams& p, int num_sms, cudaStream_t st);
 
 struct BoxParams {
   const float4* site4f;

@@ -15,6 +15,7 @@ LIB_PATH = os.path.join(HERE, "librpd_gb300.so")
 
 PRED_FP64 = 0
 PRED_FP32_FILTER = 1
+PRED_EXACT = 2
 NEIGH_USER = 0
 NEIGH_KNN = 1
 ORDER_SITE_ID = 0
@@ -69,7 +70,8 @@ class Stats(ctypes.Structure):
                 ("ms_compact", ctypes.c_float), ("ms_clip_kernel", ctypes.c_float),
                 ("n_launches", ctypes.c_int32), ("search", ctypes.c_int64 * 6),
                 ("n_reclipped", ctypes.c_int64), ("ms_predict", ctypes.c_float),
-                ("learned", ctypes.c_int32)]
+                ("learned", ctypes.c_int32), ("n_fp64_uncertain", ctypes.c_int64),
+                ("n_exact_flips", ctypes.c_int64), ("ms_epilogue", ctypes.c_float)]
 
     def as_dict(self):
         d = {f: getattr(self, f) for f, _ in self._fields_ if f not in ("status_counts", "search")}

@@ -147,10 +147,11 @@ def config_ellipsoid(target_tets=1_000_000, n_site=50_000, seed=2,
 
 def config_lattice(n=100, m=50, radius=0.01, perturb_frac=0.05, sigma=1e-12,
                    seed=5):
-    """Near-degenerate stress: lattice cube (n^3 cubes x 6 tets), m^3 sites on
-    a lattice with equal radii, a fraction perturbed by N(0, sigma)."""
+    """Near-degenerate stress: lattice cube with n grid points per axis
+    ((n-1)^3 cubes x 6 tets), m^3 sites on a lattice with equal radii, a
+    fraction perturbed by N(0, sigma)."""
     rng = np.random.default_rng(seed)
-    vert, tets = cube_grid_mesh(n)
+    vert, tets = cube_grid_mesh(n - 1)
     g = (np.arange(m) + 0.5) / m
     z, y, x = np.meshgrid(g, g, g, indexing="ij")
     xyz = np.stack([x.ravel(), y.ravel(), z.ravel()], axis=1)

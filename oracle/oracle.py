@@ -58,6 +58,10 @@ def lib():
         L.orc_det4x4_ref.argtypes = [vp, vp, vp, vp]
         L.orc_filter_sign.restype = i32
         L.orc_filter_sign.argtypes = [vp, vp, vp, vp]
+        L.orc_det4x4_bound.restype = ctypes.c_double
+        L.orc_det4x4_bound.argtypes = [vp, vp, vp, vp, vp]
+        L.orc_det4x4_exact_sign.restype = i32
+        L.orc_det4x4_exact_sign.argtypes = [vp, vp, vp, vp]
         L.orc_bisector_key.restype = ctypes.c_float
         L.orc_bisector_key.argtypes = [vp, vp]
         _lib = L
@@ -156,7 +160,7 @@ def clip_cells(mesh, sites, nbr, offs, pair_sites, pred_mode=0, n_threads=None):
     pair_sites = np.ascontiguousarray(pair_sites, np.int32)
     n_pairs = int(offs[-1])
     headers = np.zeros(max(n_pairs, 1), HEADER_DTYPE)
-    stats = np.zeros(2, np.int64)
+    stats = np.zeros(4, np.int64)
     cap = max(4096, 1024 * n_pairs)
     for _ in range(3):
         payload = np.zeros(cap, np.uint8)
@@ -227,3 +231,15 @@ def det4x4_ref(p1, p2, p3, e):
 def filter_sign(p1, p2, p3, e):
     a = [np.ascontiguousarray(x, np.float32) for x in (p1, p2, p3, e)]
     return int(lib().orc_filter_sign(*[_p(x) for x in a]))
+
+
+def det4x4_bound(p1, p2, p3, e):
+    a = [np.ascontiguousarray(x, np.float32) for x in (p1, p2, p3, e)]
+    b = np.zeros(1, np.float64)
+    d = float(lib().orc_det4x4_bound(*[_p(x) for x in a], _p(b)))
+    return d, float(b[0])
+
+
+def det4x4_exact_sign(p1, p2, p3, e):
+    a = [np.ascontiguousarray(x, np.float32) for x in (p1, p2, p3, e)]
+    return int(lib().orc_det4x4_exact_sign(*[_p(x) for x in a]))

@@ -306,7 +306,7 @@ typedef struct {
   float seed[4];
   int seed_id;
   int pred_mode;
-  int64_t n_pred, n_esc;
+  int64_t n_pred, n_esc, n_unc, n_flip;
 } cell_t;
 
 /* include/common_cuda.h:195-213 in double */
@@ -407,6 +407,147 @@ int orc_filter_sign(const float* p1, const float* p2, const float* p3,
   return filter_sign_k(K, M, e);
 }
 
+/* ---- RPD_PRED_EXACT (an extension, not in the reference): det4x4_ref's
+ * FP64 value with an error bound, and the exact sign of the determinant by
+ * floating-point expansions (Shewchuk, Discrete Comput. Geom. 18, 1997:
+ * TwoSum, TwoProduct via fma, FAST-EXPANSION-SUM and SCALE-EXPANSION with
+ * zero elimination).  This file is compiled with -ffp-contract=off. */
+double orc_det4x4_bound(const float* p1, const float* p2, const float* p3, const float* e,
+                        double* bound) {
+  const double a11 = p1[0], a12 = p2[0], a13 = p3[0], a14 = e[0];
+  const double a21 = p1[1], a22 = p2[1], a23 = p3[1], a24 = e[1];
+  const double a31 = p1[2], a32 = p2[2], a33 = p3[2], a34 = e[2];
+  const double a41 = p1[3], a42 = p2[3], a43 = p3[3], a44 = e[3];
+  const double P12 = fabs(a21 * a12) + fabs(a11 * a22), P13 = fabs(a31 * a12) + fabs(a11 * a32);
+  const double P14 = fabs(a41 * a12) + fabs(a11 * a42), P23 = fabs(a31 * a22) + fabs(a21 * a32);
+  const double P24 = fabs(a41 * a22) + fabs(a21 * a42), P34 = fabs(a41 * a32) + fabs(a31 * a42);
+  const double P123 = P23 * fabs(a13) + P13 * fabs(a23) + P12 * fabs(a33);
+  const double P124 = P24 * fabs(a13) + P14 * fabs(a23) + P12 * fabs(a43);
+  const double P134 = P34 * fabs(a13) + P14 * fabs(a33) + P13 * fabs(a43);
+  const double P234 = P34 * fabs(a23) + P24 * fabs(a33) + P23 * fabs(a43);
+  const double P = P234 * fabs(a14) + P134 * fabs(a24) + P124 * fabs(a34) + P123 * fabs(a44);
+  *bound = 10.0 * 1.1102230246251565e-16 * P + 1e-300;
+  return orc_det4x4_ref(p1, p2, p3, e);
+}
+
+static void x_two_sum(double a, double b, double* x, double* y) {
+  *x = a + b;
+  double bv = *x - a, av = *x - bv;
+  *y = (a - av) + (b - bv);
+}
+static void x_fast_two_sum(double a, double b, double* x, double* y) {
+  *x = a + b;
+  *y = b - (*x - a);
+}
+static void x_two_prod(double a, double b, double* x, double* y) {
+  *x = a * b;
+  *y = fma(a, b, -*x);
+}
+
+static int x_sum(int elen, const double* e, int flen, const double* f, double* h) {
+  int ei = 0, fi = 0, hi = 0;
+  double en = e[0], fn = f[0], Q, Qn, hh;
+  if ((fn > en) == (fn > -en)) {
+    Q = en;
+    en = ++ei < elen ? e[ei] : 0.0;
+  } else {
+    Q = fn;
+    fn = ++fi < flen ? f[fi] : 0.0;
+  }
+  if (ei < elen && fi < flen) {
+    if ((fn > en) == (fn > -en)) {
+      x_fast_two_sum(en, Q, &Qn, &hh);
+      en = ++ei < elen ? e[ei] : 0.0;
+    } else {
+      x_fast_two_sum(fn, Q, &Qn, &hh);
+      fn = ++fi < flen ? f[fi] : 0.0;
+    }
+    Q = Qn;
+    if (hh != 0.0) h[hi++] = hh;
+    while (ei < elen && fi < flen) {
+      if ((fn > en) == (fn > -en)) {
+        x_two_sum(Q, en, &Qn, &hh);
+        en = ++ei < elen ? e[ei] : 0.0;
+      } else {
+        x_two_sum(Q, fn, &Qn, &hh);
+        fn = ++fi < flen ? f[fi] : 0.0;
+      }
+      Q = Qn;
+      if (hh != 0.0) h[hi++] = hh;
+    }
+  }
+  while (ei < elen) {
+    x_two_sum(Q, en, &Qn, &hh);
+    en = ++ei < elen ? e[ei] : 0.0;
+    Q = Qn;
+    if (hh != 0.0) h[hi++] = hh;
+  }
+  while (fi < flen) {
+    x_two_sum(Q, fn, &Qn, &hh);
+    fn = ++fi < flen ? f[fi] : 0.0;
+    Q = Qn;
+    if (hh != 0.0) h[hi++] = hh;
+  }
+  if (Q != 0.0 || hi == 0) h[hi++] = Q;
+  return hi;
+}
+
+static int x_scale(int elen, const double* e, double b, double* h) {
+  int hi = 0;
+  double Q, hh, p1, p0, sum;
+  x_two_prod(e[0], b, &Q, &hh);
+  if (hh != 0.0) h[hi++] = hh;
+  for (int i = 1; i < elen; ++i) {
+    x_two_prod(e[i], b, &p1, &p0);
+    x_two_sum(Q, p0, &sum, &hh);
+    if (hh != 0.0) h[hi++] = hh;
+    x_fast_two_sum(p1, sum, &Q, &hh);
+    if (hh != 0.0) h[hi++] = hh;
+  }
+  if (Q != 0.0 || hi == 0) h[hi++] = Q;
+  return hi;
+}
+
+static int x_minor2(double a, double b, double c, double d, double* h) {
+  double x, y;
+  x_two_sum(a * b, -(c * d), &x, &y);
+  int n = 0;
+  if (y != 0.0) h[n++] = y;
+  if (x != 0.0 || n == 0) h[n++] = x;
+  return n;
+}
+
+static int x_combine3(const double* u, int lu, double a, const double* v, int lv, double b,
+                      const double* w, int lw, double c, double* h) {
+  double t1[24], t2[24], t3[24], t12[48];
+  int n1 = x_scale(lu, u, a, t1), n2 = x_scale(lv, v, -b, t2), n3 = x_scale(lw, w, c, t3);
+  int n12 = x_sum(n1, t1, n2, t2, t12);
+  return x_sum(n12, t12, n3, t3, h);
+}
+
+int orc_det4x4_exact_sign(const float* p1, const float* p2, const float* p3, const float* e) {
+  const double a11 = p1[0], a12 = p2[0], a13 = p3[0], a14 = e[0];
+  const double a21 = p1[1], a22 = p2[1], a23 = p3[1], a24 = e[1];
+  const double a31 = p1[2], a32 = p2[2], a33 = p3[2], a34 = e[2];
+  const double a41 = p1[3], a42 = p2[3], a43 = p3[3], a44 = e[3];
+  double m12[2], m13[2], m14[2], m23[2], m24[2], m34[2];
+  int l12 = x_minor2(a21, a12, a11, a22, m12), l13 = x_minor2(a31, a12, a11, a32, m13);
+  int l14 = x_minor2(a41, a12, a11, a42, m14), l23 = x_minor2(a31, a22, a21, a32, m23);
+  int l24 = x_minor2(a41, a22, a21, a42, m24), l34 = x_minor2(a41, a32, a31, a42, m34);
+  double m123[12], m124[12], m134[12], m234[12];
+  int l123 = x_combine3(m23, l23, a13, m13, l13, a23, m12, l12, a33, m123);
+  int l124 = x_combine3(m24, l24, a13, m14, l14, a23, m12, l12, a43, m124);
+  int l134 = x_combine3(m34, l34, a13, m14, l14, a33, m13, l13, a43, m134);
+  int l234 = x_combine3(m34, l34, a23, m24, l24, a33, m23, l23, a43, m234);
+  double t1[24], t2[24], t3[24], t4[24], s12[48], s34[48], d[96];
+  int n1 = x_scale(l234, m234, a14, t1), n2 = x_scale(l134, m134, -a24, t2);
+  int n3 = x_scale(l124, m124, a34, t3), n4 = x_scale(l123, m123, -a44, t4);
+  int n12 = x_sum(n1, t1, n2, t2, s12), n34 = x_sum(n3, t3, n4, t4, s34);
+  int n = x_sum(n12, s12, n34, s34, d);
+  double top = d[n - 1];
+  return top > 0.0 ? 1 : (top < 0.0 ? -1 : 0);
+}
+
 static int plane_eq(const float* a, const float* b) {
   return a[0] == b[0] && a[1] == b[1] && a[2] == b[2] && a[3] == b[3];
 }
@@ -418,10 +559,18 @@ static int in_conflict(cell_t* c, const uint8_t* v, const float* e) {
   const float* p3 = c->pl[v[2]];
   if (plane_eq(e, p1) || plane_eq(e, p2) || plane_eq(e, p3)) return 0;
   c->n_pred++;
-  if (c->pred_mode == 1) {
+  if (c->pred_mode == 1 || c->pred_mode == 2) {
     int s = orc_filter_sign(p1, p2, p3, e);
     if (s != 0) return s > 0;
     c->n_esc++;
+  }
+  if (c->pred_mode == 2) {
+    double bound, d = orc_det4x4_bound(p1, p2, p3, e, &bound);
+    if (fabs(d) > bound) return d > 0.0;
+    c->n_unc++;
+    int xs = orc_det4x4_exact_sign(p1, p2, p3, e);
+    if ((xs > 0) != (d > 0.0)) c->n_flip++;
+    return xs > 0;
   }
   double det = orc_det4x4_ref(p1, p2, p3, e);
   return det > 0.0;
@@ -803,9 +952,9 @@ int64_t orc_clip_cells(int n_vert, const float* vert3, const double* vert3d,
   /* per pair: owning thread and offset in that thread's buffer */
   int32_t* own = (int32_t*)malloc(sizeof(int32_t) * (size_t)(n_pairs > 0 ? n_pairs : 1));
   int64_t* loff = (int64_t*)malloc(sizeof(int64_t) * (size_t)(n_pairs > 0 ? n_pairs : 1));
-  int64_t tot_pred = 0, tot_esc = 0;
+  int64_t tot_pred = 0, tot_esc = 0, tot_unc = 0, tot_flip = 0;
 #ifdef _OPENMP
-#pragma omp parallel for schedule(dynamic, 16) reduction(+ : tot_pred, tot_esc)
+#pragma omp parallel for schedule(dynamic, 16) reduction(+ : tot_pred, tot_esc, tot_unc, tot_flip)
 #endif
   for (int t = 0; t < n_tet; ++t) {
     int me = 0;
@@ -816,7 +965,7 @@ int64_t orc_clip_cells(int n_vert, const float* vert3, const double* vert3d,
     for (int32_t q = tet_offsets[t]; q < tet_offsets[t + 1]; ++q) {
       int s = pair_sites[q];
       c.pred_mode = pred_mode;
-      c.n_pred = c.n_esc = 0;
+      c.n_pred = c.n_esc = c.n_unc = c.n_flip = 0;
       c.seed_id = s;
       memcpy(c.seed, site4 + 4 * (int64_t)s, sizeof(float) * 4);
       cell_init(&c, vert3, tets + 4 * (int64_t)t, v_adjs, e_adj6 + 6 * (int64_t)t,
@@ -829,6 +978,8 @@ int64_t orc_clip_cells(int n_vert, const float* vert3, const double* vert3d,
       }
       tot_pred += c.n_pred;
       tot_esc += c.n_esc;
+      tot_unc += c.n_unc;
+      tot_flip += c.n_flip;
       orc_cell_header* h = &headers[q];
       h->tet_id = t;
       h->site_id = s;
@@ -863,6 +1014,8 @@ int64_t orc_clip_cells(int n_vert, const float* vert3, const double* vert3d,
   if (stats) {
     stats[0] = tot_pred;
     stats[1] = tot_esc;
+    stats[2] = tot_unc;
+    stats[3] = tot_flip;
   }
   if (off <= payload_capacity && payload) {
 #ifdef _OPENMP

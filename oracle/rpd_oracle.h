@@ -123,6 +123,11 @@ double orc_det4x4_ref(const float* p1, const float* p2, const float* p3,
 /* returns +1/-1 when the FP32 filter decides, 0 when it cannot */
 int orc_filter_sign(const float* p1, const float* p2, const float* p3,
                     const float* e);
+/* pred_mode 2 (an extension): the FP64 determinant with its error bound,
+ * and the exact sign by floating-point expansions */
+double orc_det4x4_bound(const float* p1, const float* p2, const float* p3, const float* e,
+                        double* bound);
+int orc_det4x4_exact_sign(const float* p1, const float* p2, const float* p3, const float* e);
 
 #ifdef __cplusplus
 }

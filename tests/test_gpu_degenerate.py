@@ -1,0 +1,79 @@
+"""Near-degenerate predicate stress (the lattice configuration at a small
+size): sites on a lattice with equal radii (cospherical / coplanar power
+bisectors, exact ties), 5% perturbed by N(0, 1e-12).  The FP32-filtered
+path must still give the FP64 path's cells bit for bit; the exact mode must
+give the oracle's exact-mode cells, and reports where the FP64 signs are
+wrong."""
+import numpy as np
+import pytest
+
+from libmat_gb300 import rpd
+from libmat_gb300 import workloads as W
+from oracle import oracle as O
+from tests.helpers import SUCCESS, compare_cells
+
+pytestmark = pytest.mark.gpu
+
+
+def run(cfg, adj, pred, certify=False):
+    with rpd.RPD(predicate_mode=pred, neighbor_source=rpd.NEIGH_KNN, knn_k=64,
+                 certify=certify) as r:
+        r.set_mesh(cfg["vert3d"], cfg["tets"], adj["v_adjs"], adj["e_adj6"], adj["f_adjs"],
+                   adj["f_ids"])
+        r.set_sites(cfg["sites"], cfg["flags"])
+        st = r.compute()
+        out = dict(st=st, ph=r.pair_headers(), hashes=r.topology_hashes())
+        out["h"], out["p"] = r.cells()
+        if not certify:
+            out["nbr"] = r.neighbor_lists(cfg["sites"].shape[0])
+            out["offs"], out["ps"] = r.pairs(cfg["tets"].shape[0])
+    return out
+
+
+@pytest.fixture(scope="module")
+def lattice():
+    cfg = W.config_lattice(n=16, m=8)
+    adj = rpd.mesh_adjacency(cfg["vert3d"].shape[0], cfg["tets"])
+    return cfg, adj
+
+
+def test_filter_equals_fp64_on_ties(lattice):
+    cfg, adj = lattice
+    a = run(cfg, adj, rpd.PRED_FP64)
+    b = run(cfg, adj, rpd.PRED_FP32_FILTER)
+    assert a["st"].n_pairs == b["st"].n_pairs
+    assert compare_cells(a["ph"], a["p"], b["ph"], b["p"]) == 0
+    # the lattice forces many escalations (exact ties cannot be decided in FP32)
+    assert b["st"].n_escalated > 0.001 * b["st"].n_predicates
+    # and the oracle (FP64 signs) agrees
+    mesh = dict(vert3d=cfg["vert3d"], tets=cfg["tets"], **{k: adj[k] for k in
+                ("v_adjs", "e_adj6", "f_adjs", "f_ids")})
+    oh, op, _ = O.clip_cells(mesh, cfg["sites"], a["nbr"], a["offs"], a["ps"], pred_mode=0)
+    assert compare_cells(a["ph"], a["p"], oh, op) == 0
+
+
+def test_exact_mode_matches_oracle_exact_mode(lattice):
+    cfg, adj = lattice
+    x = run(cfg, adj, rpd.PRED_EXACT)
+    mesh = dict(vert3d=cfg["vert3d"], tets=cfg["tets"], **{k: adj[k] for k in
+                ("v_adjs", "e_adj6", "f_adjs", "f_ids")})
+    oh, op, ost = O.clip_cells(mesh, cfg["sites"], x["nbr"], x["offs"], x["ps"], pred_mode=2)
+    assert compare_cells(x["ph"], x["p"], oh, op) == 0
+    st = x["st"]
+    # the GPU evaluates a few planes speculatively per vote, so its counts
+    # are slightly above the oracle's sequential ones
+    assert st.n_escalated >= ost[1] and st.n_fp64_uncertain >= ost[2] > 0
+    assert 0 <= st.n_exact_flips <= st.n_fp64_uncertain
+
+
+def test_certified_order_on_ties_reported(lattice):
+    """Distance order resolves exact ties in another order than the site-id
+    order; the cells then may differ (both are valid restricted cells).
+    Statuses of the pairs must agree and most cells must be identical."""
+    cfg, adj = lattice
+    a = run(cfg, adj, rpd.PRED_FP64)
+    c = run(cfg, adj, rpd.PRED_FP32_FILTER, certify=True)
+    assert a["st"].n_pairs == c["st"].n_pairs
+    ok = a["ph"]["status"] == SUCCESS
+    same = (a["hashes"] == c["hashes"])[ok].mean()
+    assert same > 0.5
