@@ -722,6 +722,7 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
         pp.site4f = c->site4f.ptr;
         pp.flags = c->flags.ptr;
         pp.nbr = c->nbr.ptr;
+        pp.rule_nbr = knn ? c->nbr_dist.ptr : nullptr;
         pp.k = c->k;
         pp.n_site = n_site;
         pp.site_box = c->site_box.ptr;

@@ -808,8 +808,9 @@ __device__ float vertex_volume_f(float3 A, const float3* n, const float3* foot) 
   return v * (1.0f / 6.0f);
 }
 
-// intersection of three float planes, double-float Cramer (box kernel)
-__device__ void vertex_of_float_planes(float4 a4, float4 b4, float4 c4, double* out) {
+// intersection of three float planes, double-float Cramer (box kernel):
+// per coordinate a float interval [lo, hi] around the double-float value
+__device__ void vertex_of_float_planes(float4 a4, float4 b4, float4 c4, float* lo, float* hi) {
   df ax = df_make(a4.x, 0.f), ay = df_make(a4.y, 0.f), az = df_make(a4.z, 0.f),
      aw = df_make(a4.w, 0.f);
   df bx = df_make(b4.x, 0.f), by = df_make(b4.y, 0.f), bz = df_make(b4.z, 0.f),
@@ -822,10 +823,12 @@ __device__ void vertex_of_float_planes(float4 a4, float4 b4, float4 c4, double* 
   df Dx = df_add(df_sub(df_mul(ay, mzw), df_mul(az, myw)), df_mul(aw, myz));
   df Dy = df_add(df_sub(df_mul(ax, mzw), df_mul(az, mxw)), df_mul(aw, mxz));
   df Dz = df_add(df_sub(df_mul(ax, myw), df_mul(ay, mxw)), df_mul(aw, mxy));
-  double w = df_to_double(Dw);
-  out[0] = -df_to_double(Dx) / w;
-  out[1] = df_to_double(Dy) / w;
-  out[2] = -df_to_double(Dz) / w;
+  const df inv = df_recip(Dw);
+  const df X[3] = {df_neg(df_mul(Dx, inv)), df_mul(Dy, inv), df_neg(df_mul(Dz, inv))};
+  for (int k = 0; k < 3; ++k) {
+    lo[k] = __fadd_rd(X[k].hi, X[k].lo);
+    hi[k] = __fadd_ru(X[k].hi, X[k].lo);
+  }
 }
 
 // vertex (X, Y, Z) of the three seed-frame double-float planes pa, pb, pc
@@ -1225,7 +1228,7 @@ cudaError_t launch_cell_epilogue(const EpilogueParams& p, int num_sms, cudaStrea
 // box kernel: bounding box of a site's cell grown by an offset, used to
 // enumerate candidate tets (see rpd_pairs.cu)
 // ------------------------------------------------------------------------
-__global__ void __launch_bounds__(kClipMaxThreads) site_box_kernel(BoxParams p) {
+__global__ void __launch_bounds__(128, 6) site_box_kernel(BoxParams p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31;
   const int wid = threadIdx.x >> 5;
@@ -1302,13 +1305,15 @@ __global__ void __launch_bounds__(kClipMaxThreads) site_box_kernel(BoxParams p) 
       bh[0] = bh[1] = bh[2] = -3.0e38f;
       for (int v = lane; v < s.nb_v; v += 32) {
         uchar4 tr = c.ver[v];
-        double X[3];
-        vertex_of_float_planes(c.pl[tr.x], c.pl[tr.y], c.pl[tr.z], X);
+        float xl[3], xh[3];
+        vertex_of_float_planes(c.pl[tr.x], c.pl[tr.y], c.pl[tr.z], xl, xh);
         for (int k = 0; k < 3; ++k) {
-          float xl = __double2float_rd(X[k]), xh = __double2float_ru(X[k]);
-          if (!(X[k] == X[k])) { xl = lo[k]; xh = hi[k]; }
-          bl[k] = fminf(bl[k], xl);
-          bh[k] = fmaxf(bh[k], xh);
+          if (!(xl[k] == xl[k]) || !(xh[k] == xh[k])) {  // degenerate vertex
+            xl[k] = lo[k];
+            xh[k] = hi[k];
+          }
+          bl[k] = fminf(bl[k], xl[k]);
+          bh[k] = fmaxf(bh[k], xh[k]);
         }
       }
       for (int o = 16; o > 0; o >>= 1)

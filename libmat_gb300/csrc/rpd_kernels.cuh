@@ -150,6 +150,7 @@ struct PairParams {
   const float4* site4f;
   const uint32_t* flags;
   const int32_t* nbr;
+  const int32_t* rule_nbr;  // the same lists in another order (rule evaluation), or null
   int k;
   int n_site;
   const float4* site_box;

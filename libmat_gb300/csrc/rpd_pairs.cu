@@ -537,7 +537,9 @@ __global__ void __launch_bounds__(kPairWarps * 32) pairs_kernel(PairParams p,
     __syncwarp();
     const float4 si = p.site4f[i];
     const Grid& g = p.tg;
-    const int32_t* L = p.nbr + (long long)i * p.k;
+    // the rule is over the whole list; in ascending bisector distance (when
+    // the GPU built it) the neighbour that dominates a far tet comes first
+    const int32_t* L = (p.rule_nbr ? p.rule_nbr : p.nbr) + (long long)i * p.k;
     n_cells_seen += n_iter;
     // half extent of a grid cell, grown for the rounding of the binning
     const float hc = 0.5f * g.cell * (1.0f + 1e-3f) + 1e-6f * p.coord_scale;
