@@ -47,6 +47,25 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
+def compare_topology(ph_fast, hash_fast, ph_plain, hash_plain):
+    """Cells of a fast run against the plain FP64 path's, pair by pair:
+    canonical topology of the cells both emit, statuses elsewhere.  The
+    reference's fixed capacities (64 planes, 96 vertices, 152 edges) drop
+    cells whose clipping in site-id order overflows them; clipping in
+    ascending bisector distance builds fewer intermediate vertices and edges
+    and can emit those cells -- counted apart, not as differences."""
+    assert np.array_equal(ph_fast["tet_id"], ph_plain["tet_id"])
+    assert np.array_equal(ph_fast["site_id"], ph_plain["site_id"])
+    sf, sp = ph_fast["status"], ph_plain["status"]
+    both = (sf == 4) & (sp == 4)
+    overflow = np.isin(sp, [0, 1, 7]) & (sf == 4)
+    other = (sf != sp) & ~overflow
+    n_topo = int((hash_fast[both] != hash_plain[both]).sum())
+    return {"topology_bit_exact": bool(n_topo == 0 and not other.any()),
+            "cells_topology_differing": n_topo, "status_differing": int(other.sum()),
+            "reference_capacity_drops_emitted": int(overflow.sum())}
+
+
 def make_workload(args):
     from libmat_gb300 import workloads as W
 
@@ -358,10 +377,8 @@ def run_ours(args):
     # exact topology: same pairs, statuses and canonical topology of every
     # cell (the certified path's records list fewer dead planes, so the raw
     # bytes differ; the vertices' face-key triples do not)
-    same_headers = all(np.array_equal(fast_ph[f], plain_ph[f])
-                       for f in ("tet_id", "site_id", "status"))
-    n_topo_diff = int((fast_hash != plain_hash).sum())
-    topo_ok = same_headers and n_topo_diff == 0
+    cmp = compare_topology(fast_ph, fast_hash, plain_ph, plain_hash)
+    topo_ok, n_topo_diff = cmp["topology_bit_exact"], cmp["cells_topology_differing"]
     geo = _geometry_error(fast_ph, fast_p, plain_ph, plain_p)
 
     # ---- end to end through the C ABI with host buffers, same configuration
@@ -411,6 +428,8 @@ def run_ours(args):
         "plain": {"value": plain_value, "ms_per_step": sum(pms) / len(pms),
                   "speedup_fast_over_plain": value / world / plain_value,
                   "topology_bit_exact": bool(topo_ok), "cells_topology_differing": n_topo_diff,
+                  "status_differing": cmp["status_differing"],
+                  "reference_capacity_drops_emitted": cmp["reference_capacity_drops_emitted"],
                   "predicates_evaluated": int(pst.n_predicates), "tuning": plain_tuning},
         "geometry_vs_plain": geo,
         "tuning": tuning,
@@ -488,6 +507,101 @@ def run_stress(args):
     print(json.dumps({"workload": name, "n_tet": int(cfg["tets"].shape[0]),
                       "n_site": int(cfg["sites"].shape[0]), "knn_k": args.k,
                       "generation_s": round(gen_s, 2), "runs": out}))
+
+
+def run_batch(args):
+    """Batched uneven workload (--config batch): 256 independent meshes (cube
+    or ellipsoid, random rotation and scale, tets log-uniform in [2k, 200k],
+    sites log-uniform in [100, 20k], uniform in the volume, radii U[0.005,
+    0.04]) in one batch: the per-mesh front end replayed from a CUDA graph,
+    one persistent clip launch for all meshes, autotuned.  Beside it: the
+    same batch with the front end launched directly, a loop of single-mesh
+    computes, and the plain FP64 batch (topology reference)."""
+    from libmat_gb300 import rpd
+    from libmat_gb300 import workloads as W
+
+    t0 = time.time()
+    ms = W.config_batch(n_mesh=args.batch_meshes, seed=3)
+    for cfg in ms:
+        cfg["adj"] = rpd.mesh_adjacency(cfg["vert3d"].shape[0], cfg["tets"])
+    gen_s = time.time() - t0
+    n_tet = sum(m["tets"].shape[0] for m in ms)
+    n_site = sum(m["sites"].shape[0] for m in ms)
+
+    def make(pred, certify, graph=True):
+        b = rpd.Batch(predicate_mode=pred, knn_k=args.k, certify=certify, use_graph=graph,
+                      topology_hash=False)
+        for cfg in ms:
+            a = cfg["adj"]
+            b.add_mesh(cfg["vert3d"], cfg["tets"], a["v_adjs"], a["e_adj6"], a["f_adjs"],
+                       a["f_ids"], cfg["sites"], cfg["flags"])
+        return b
+
+    def timed(b):
+        for _ in range(args.warmup):
+            b.compute()
+        ms_, cells, st = [], 0, None
+        for _ in range(args.steps):
+            flush_l2()
+            st = b.compute()
+            ms_.append(st.ms_total)
+            cells += st.n_cells
+        return cells / (sum(ms_) / 1000.0), float(np.median(ms_)), st
+
+    out = {}
+    fast = make(rpd.PRED_FP32_FILTER, True)
+    tuning = fast.autotune(repeats=1).as_dict() if not args.no_tune else None
+    with ClockSampler(0) as clk:
+        v, m_, st = timed(fast)
+    out["batch_graph"] = {"cells_per_s": v, "ms_per_step": m_, "n_launches": int(st.n_launches),
+                          "stage_ms": {"front_end": st.ms_knn, "pairs_csr": st.ms_pairs,
+                                       "clip": st.ms_clip, "clip_kernel": st.ms_clip_kernel,
+                                       "epilogue": st.ms_epilogue, "compact": st.ms_compact}}
+    n_cells, n_pairs = int(st.n_cells), int(st.n_pairs)
+    fast.configure(topology_hash=1)
+    fast.compute()
+    fh, fph = fast.topology_hashes(), fast.pair_headers()
+    fast.close()
+    nog = make(rpd.PRED_FP32_FILTER, True, graph=False)
+    v, m_, st = timed(nog)
+    out["batch_no_graph"] = {"cells_per_s": v, "ms_per_step": m_}
+    nog.close()
+    # one single-mesh compute per mesh (same configuration), back to back
+    singles = []
+    for cfg in ms:
+        a = cfg["adj"]
+        r = rpd.RPD(predicate_mode=rpd.PRED_FP32_FILTER, neighbor_source=rpd.NEIGH_KNN,
+                    knn_k=args.k, certify=True, topology_hash=False)
+        r.set_mesh(cfg["vert3d"], cfg["tets"], a["v_adjs"], a["e_adj6"], a["f_adjs"], a["f_ids"])
+        r.set_sites(cfg["sites"], cfg["flags"])
+        if tuning:
+            r.configure(warps_per_block=tuning["warps_per_block"], clip_variant=tuning["clip_variant"])
+        singles.append(r)
+    for r in singles:
+        r.compute()
+    t1 = time.perf_counter()
+    cells = 0
+    for _ in range(args.steps):
+        for r in singles:
+            cells += r.compute().n_cells
+    out["per_mesh_loop"] = {"cells_per_s": cells / (time.perf_counter() - t1),
+                            "note": "host wall clock over 256 rpd_compute calls per step"}
+    for r in singles:
+        r.close()
+    plain = make(rpd.PRED_FP64, False)
+    v, m_, st = timed(plain)
+    out["plain_fp64_batch"] = {"cells_per_s": v, "ms_per_step": m_}
+    plain.configure(topology_hash=1)
+    plain.compute()
+    ph, pph = plain.topology_hashes(), plain.pair_headers()
+    plain.close()
+    cmp = compare_topology(fph, fh, pph, ph)
+    print(json.dumps({
+        "workload": "batch_%d_meshes_cube_or_ellipsoid_tets_2k-200k_sites_100-20k" % len(ms),
+        "n_mesh": len(ms), "n_tet": n_tet, "n_site": n_site, "n_pairs": n_pairs,
+        "n_cells": n_cells, "knn_k": args.k, "generation_s": round(gen_s, 1), "tuning": tuning,
+        "vs_plain_fp64": cmp, "runs": out,
+        "clocks": clk.summary()}))
 
 
 def run_fast_only(args):
@@ -639,7 +753,9 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="ellipsoid", choices=["ellipsoid", "small", "lattice"])
+    ap.add_argument("--config", default="ellipsoid",
+                    choices=["ellipsoid", "small", "lattice", "batch"])
+    ap.add_argument("--batch-meshes", type=int, default=256)
     ap.add_argument("--lattice-n", type=int, default=100, help="lattice mesh grid points per axis")
     ap.add_argument("--lattice-m", type=int, default=50, help="lattice sites per axis")
     ap.add_argument("--tets", type=int, default=1_000_000)
@@ -668,6 +784,11 @@ def main():
 
         build()
         run_stress(args)
+    elif args.config == "batch":
+        from __graft_entry__ import build
+
+        build()
+        run_batch(args)
     elif args.fast_only:
         from __graft_entry__ import build
 

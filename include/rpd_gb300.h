@@ -361,6 +361,50 @@ rpd_status rpd_mlp_copy_features(struct rpd_ctx* ctx, uint16_t* x, int64_t capac
 rpd_status rpd_mlp_copy_klen(struct rpd_ctx* ctx, int32_t* klen, int64_t capacity,
                              int64_t* n_pairs);
 
+/* ---- Batches of independent meshes ---------------------------------------
+ * No counterpart in the reference, which runs one mesh per call.  A batch
+ * concatenates many meshes (each with its own sites) into one context; the
+ * per-mesh front end (neighbour lists, candidate pairs) is recorded once into
+ * a CUDA graph and replayed, and all meshes' cells are clipped by one
+ * persistent kernel launch.  Neighbour lists are GPU-built (RPD_NEIGH_KNN);
+ * learned_k is not available for batches.  Cells of every mesh equal those
+ * of a single-mesh rpd_compute of that mesh. */
+struct rpd_batch;
+rpd_status rpd_batch_create(const rpd_config* cfg, struct rpd_batch** out);
+void rpd_batch_destroy(struct rpd_batch* batch);
+const char* rpd_batch_last_error(const struct rpd_batch* batch);
+/* Appends a mesh and its sites (same layouts as rpd_set_mesh /
+ * rpd_set_sites; tets hold the mesh's own vertex ids).  mesh_index receives
+ * the mesh's index in the batch. */
+rpd_status rpd_batch_add_mesh(struct rpd_batch* batch, const double* xyz, int n_vert,
+                              const int32_t* tets, int n_tet, const int32_t* v_adjs,
+                              const uint8_t* e_adj6, const int32_t* f_adjs, const int32_t* f_ids,
+                              const double* xyzw, int n_site, const uint32_t* flags,
+                              int* mesh_index);
+int rpd_batch_size(const struct rpd_batch* batch);
+/* 1 (default): record the front end into a CUDA graph and replay it; 0:
+ * launch it directly every time. */
+rpd_status rpd_batch_set_graph(struct rpd_batch* batch, int use_graph);
+/* All meshes; stats are for the whole batch (ms_knn: the front end of all
+ * meshes, kNN and candidate search). */
+rpd_status rpd_batch_compute(struct rpd_batch* batch, rpd_stats* stats);
+/* Autotuner of the batch's clip stage (as rpd_autotune). */
+rpd_status rpd_batch_autotune(struct rpd_batch* batch, int repeats, rpd_tuning* result);
+/* Range of mesh `mesh` in the compacted cells of the batch's context
+ * (rpd_get_cells(rpd_batch_context(batch)) -- there, tet and site ids are
+ * the batch's). */
+rpd_status rpd_batch_mesh_cells(struct rpd_batch* batch, int mesh, int64_t* first_cell,
+                                int64_t* n_cells);
+/* The cells of one mesh with the mesh's own tet and site ids (headers and
+ * the site pairs of the plane ids) and consecutive payload offsets; NULL
+ * buffers query the sizes. */
+rpd_status rpd_batch_copy_mesh_cells(struct rpd_batch* batch, int mesh, rpd_cell_header* headers,
+                                     int64_t max_cells, void* payload, int64_t payload_capacity,
+                                     int64_t* n_cells, int64_t* payload_bytes);
+/* The context holding the batch (configuration, statistics views).  Do not
+ * call rpd_set_mesh / rpd_set_sites / rpd_compute on it. */
+struct rpd_ctx* rpd_batch_context(struct rpd_batch* batch);
+
 /* Page-locked host buffers for fast host<->device copies (cudaMallocHost);
  * NULL on failure. */
 void* rpd_host_alloc(size_t bytes);

@@ -28,7 +28,7 @@ CUDA_UNITS = {
     "rpd_noalloc.cu": [],
     "rpd_mlp.cu": [],
 }
-CXX_UNITS = ["rpd_api.cpp", "rpd_mesh.cpp"]
+CXX_UNITS = ["rpd_api.cpp", "rpd_mesh.cpp", "rpd_batch.cpp"]
 
 
 def nvcc():

@@ -26,151 +26,7 @@
 
 using namespace rpd;
 
-namespace {
-
-template <class T>
-struct DevBuf {
-  T* ptr = nullptr;
-  size_t cap = 0;  // elements
-  cudaError_t ensure(size_t n) {
-    if (n <= cap && ptr) return cudaSuccess;
-    if (ptr) cudaFree(ptr);
-    ptr = nullptr;
-    cap = 0;
-    size_t want = std::max<size_t>(n, 1);
-    cudaError_t e = cudaMalloc((void**)&ptr, want * sizeof(T));
-    if (e == cudaSuccess) cap = want;
-    return e;
-  }
-  // grows to n elements keeping the first `keep` (stream-ordered copy)
-  cudaError_t grow_keep(size_t n, size_t keep, cudaStream_t st) {
-    if (n <= cap && ptr) return cudaSuccess;
-    T* old = ptr;
-    size_t want = std::max<size_t>(n, std::max<size_t>(2 * cap, 1));
-    T* fresh = nullptr;
-    cudaError_t e = cudaMalloc((void**)&fresh, want * sizeof(T));
-    if (e != cudaSuccess) return e;
-    if (old && keep) {
-      e = cudaMemcpyAsync(fresh, old, keep * sizeof(T), cudaMemcpyDeviceToDevice, st);
-      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-      if (e != cudaSuccess) {
-        cudaFree(fresh);
-        return e;
-      }
-    }
-    if (old) cudaFree(old);
-    ptr = fresh;
-    cap = want;
-    return cudaSuccess;
-  }
-  void release() {
-    if (ptr) cudaFree(ptr);
-    ptr = nullptr;
-    cap = 0;
-  }
-  ~DevBuf() { release(); }
-};
-
-enum Ev {
-  kEvStart, kEvKnn, kEvPairs, kEvPred0, kEvPred1, kEvClipK0, kEvClipK1, kEvEpi0, kEvClip, kEvEnd,
-  kEvCount
-};
-
-}  // namespace
-
-struct rpd_ctx {
-  rpd_config cfg;
-  int device = 0;
-  int num_sms = 0;
-  cudaStream_t stream = nullptr;
-  cudaEvent_t ev[kEvCount] = {};
-  std::string err;
-
-  // mesh
-  int n_vert = 0, n_tet = 0;
-  DevBuf<float> vert3f;
-  DevBuf<double> vert3d;
-  DevBuf<float2> vert2;  // double-float copies (geometry epilogue)
-  DevBuf<int4> tets;
-  DevBuf<int32_t> v_adjs, f_adjs, f_ids;
-  DevBuf<uint8_t> e_adj6;
-  double mesh_lo[3] = {0, 0, 0}, mesh_hi[3] = {0, 0, 0};
-  double tet_radius = 0.0;
-  // tets grouped by radius (largest vertex distance to the centroid): the
-  // candidate search offsets each site's cell by its class's largest radius
-  static constexpr int kClasses = 8;
-  DevBuf<uint8_t> tet_class;
-  int class_count[kClasses] = {0};
-  double class_radius[kClasses] = {0};
-  bool has_mesh = false;
-
-  // sites
-  int n_site = 0;
-  DevBuf<float4> site4f;
-  DevBuf<double> site4d;
-  DevBuf<float2> site2;
-  DevBuf<uint32_t> flags;
-  double site_lo[3] = {0, 0, 0}, site_hi[3] = {0, 0, 0};
-  float w_max = 0.f;
-  bool has_sites = false;
-
-  // neighbour lists
-  int k = 0;
-  DevBuf<int32_t> nbr, nbr_dist, nbr_ref_tmp, knn_status, site_klen, reclip_idx;
-  bool has_site_klen = false;
-  DevBuf<unsigned long long> topo_hash;
-  long long n_reclipped = 0;
-  DevBuf<float> nbr_keys;
-  bool has_user_nbr = false;
-
-  // grids
-  DevBuf<int32_t> s_cell_of, s_cell_count, s_cell_start, s_cell_fill, s_cell_items;
-  DevBuf<int32_t> t_cell_of, t_cell_count, t_cell_start, t_cell_fill, t_cell_items;
-  DevBuf<float4> centroid, site_box, site_planes;
-  DevBuf<int32_t> site_nplanes, pair_ntasks, pair_taskoff;
-  DevBuf<int32_t> scan_tmp;
-
-  // pairs
-  DevBuf<int2> pair_buf;
-  DevBuf<int32_t> tet_count, tet_offsets, tet_fill, pair_site, pair_tet;
-  long long pair_cap_hint = 0;
-
-  // cells
-  DevBuf<rpd_cell_header> pair_headers, cells;
-  DevBuf<uint8_t> payload;
-  DevBuf<int32_t> flag_tmp, pos_tmp;
-  DevBuf<unsigned long long> scratch;  // [0] payload cursor [1] work [2..3] counters
-                                       // [4] pair cursor [8..18] status hist
-  DevBuf<long long> n_out;
-  long long payload_cap_hint = 0;
-
-  // learned list length: features, predictor, training set
-  double mesh_volume = 0.0;
-  DevBuf<float4> bverts;        // boundary vertices
-  int n_bverts = 0;
-  DevBuf<float> site_bdist;     // site -> nearest boundary vertex distance
-  bool bdist_valid = false;
-  DevBuf<uint16_t> feat;        // bf16 rows of the last features launch
-  long long n_feat_rows = 0;
-  DevBuf<int32_t> pair_klen, consumed, sample_idx;
-  bool want_consumed = false;
-  bool last_learned = false;
-  DevBuf<int32_t> user_pair_k;   // rpd_set_pair_k
-  long long n_user_pair_k = -1;
-  DevBuf<float> mlp_params, mlp_grads, mlp_m, mlp_v, mlp_loss, mlp_y, mlp_target;
-  DevBuf<uint16_t> mlp_W1T, mlp_W2, mlp_W2T;
-  float mlp_margin = 0.f;
-  bool mlp_ready = false;
-  DevBuf<uint16_t> train_X;
-  DevBuf<float> train_y;
-  DevBuf<int32_t> train_idx;
-  long long n_train = 0;
-
-  // results of the last compute
-  long long n_pairs = 0, n_cells = 0, payload_bytes = 0;
-  int tet_k = 0;
-  bool has_result = false;
-};
+#include "rpd_ctx.hpp"
 
 namespace {
 
@@ -597,166 +453,21 @@ rpd_status rpd_set_neighbors(rpd_ctx* c, const int32_t* nbr, int k, int layout) 
   return RPD_OK;
 }
 
-rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
-  if (!c) return RPD_ERR_INVALID_ARGUMENT;
-  if (!c->has_mesh || !c->has_sites) return fail(c, RPD_ERR_NOT_READY, "rpd_compute: mesh and sites required");
-  const bool knn = c->cfg.neighbor_source == RPD_NEIGH_KNN;
-  if (!knn && !c->has_user_nbr)
-    return fail(c, RPD_ERR_NOT_READY, "rpd_compute: neighbour lists required (rpd_set_neighbors)");
-  const bool learned = c->cfg.learned_k != 0;
-  if (learned && (!c->cfg.certify || !knn))
-    return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_compute: learned_k needs certify and GPU-built lists");
-  if (learned && !c->mlp_ready)
-    return fail(c, RPD_ERR_NOT_READY,
-                "rpd_compute: learned_k needs a predictor (rpd_mlp_train or rpd_mlp_set_params)");
-  CK(cudaSetDevice(c->device), "cudaSetDevice");
+// CSR of the pairs, clipping (+ re-clip), epilogue, compaction and the
+// statistics: the part of a compute after the candidate pairs are in
+// pair_buf / tet_count (n_pairs of them)
+static rpd_status finish_compute(rpd_ctx* c, bool knn, bool learned, rpd_stats* stats) {
   cudaStream_t st = c->stream;
-  const int n_site = c->n_site, n_tet = c->n_tet;
-  CK(c->scratch.ensure(32), "alloc scratch");
-  CK(cudaMemsetAsync(c->scratch.ptr, 0, 32 * sizeof(unsigned long long), st), "memset");
-  take_launches();
-  CK(cudaEventRecord(c->ev[kEvStart], st), "event");
-
-  // ---- neighbour lists
-  if (knn) {
-    c->k = c->cfg.knn_k;
-    Grid g = make_grid(c->site_lo, c->site_hi, n_site, 2.0);
-    long long nc = (long long)g.nx * g.ny * g.nz;
-    CK(c->s_cell_of.ensure(n_site), "alloc");
-    CK(c->s_cell_count.ensure(nc), "alloc");
-    CK(c->s_cell_start.ensure(nc + 1), "alloc");
-    CK(c->s_cell_fill.ensure(nc), "alloc");
-    CK(c->s_cell_items.ensure(n_site), "alloc");
-    CK(c->scan_tmp.ensure(scan_temp_ints(std::max<long long>(nc, n_tet)) + 16), "alloc");
-    CK(c->nbr.ensure((size_t)n_site * c->k), "alloc nbr");
-    CK(c->nbr_keys.ensure((size_t)n_site * c->k), "alloc nbr");
-    CK(c->nbr_dist.ensure((size_t)n_site * c->k), "alloc nbr");
-    CK(c->knn_status.ensure(n_site), "alloc");
-    CK(grid_build_sites(c->site4f.ptr, n_site, g, c->s_cell_of.ptr, c->s_cell_count.ptr,
-                        c->s_cell_start.ptr, c->s_cell_fill.ptr, c->s_cell_items.ptr,
-                        c->scan_tmp.ptr, st), "site grid");
-    CK(launch_knn(c->site4f.ptr, n_site, g, c->s_cell_start.ptr, c->s_cell_items.ptr, c->k,
-                  c->w_max, c->cfg.clip_order == RPD_ORDER_SITE_ID ? 1 : 0, c->nbr.ptr,
-                  c->nbr_keys.ptr, c->nbr_dist.ptr, c->knn_status.ptr, st), "knn");
-  }
-  CK(cudaEventRecord(c->ev[kEvKnn], st), "event");
-
-  // ---- candidate pairs
-  {
-    CK(c->centroid.ensure(n_tet), "alloc");
-    CK(c->t_cell_of.ensure(n_tet), "alloc");
-    CK(c->t_cell_items.ensure(n_tet), "alloc");
-    CK(tet_centroids(c->vert3f.ptr, c->tets.ptr, n_tet, c->centroid.ptr, st), "centroids");
-    double diag2 = 0.0, cs = 0.0;
-    for (int a = 0; a < 3; ++a) {
-      double l = std::min(c->mesh_lo[a], c->site_lo[a]), h = std::max(c->mesh_hi[a], c->site_hi[a]);
-      diag2 += (h - l) * (h - l);
-      cs = std::max(cs, std::max(std::fabs(l), std::fabs(h)));
-    }
-    const double u = std::ldexp(1.0, -24);
-    double ext = 0.0;
-    for (int a = 0; a < 3; ++a) ext = std::max(ext, c->mesh_hi[a] - c->mesh_lo[a]);
-    const double margin = 1e-4 * ext + 1e-6 * cs;
-    // the nearest bisectors bound each cell; with a GPU-built list the
-    // distance-ordered copy gives them first, a user list is used whole
-    const int32_t* box_list = knn ? c->nbr_dist.ptr : c->nbr.ptr;
-    const int box0 = c->cfg.box_planes > 0 ? c->cfg.box_planes : 32;
-    CK(c->site_box.ensure((size_t)n_site * 2), "alloc");
-    CK(c->site_planes.ensure((size_t)n_site * kBoxPlanes), "alloc");
-    CK(c->site_nplanes.ensure((size_t)n_site), "alloc");
-    CK(c->tet_count.ensure(n_tet), "alloc");
-    CK(c->tet_offsets.ensure((size_t)n_tet + 1), "alloc");
-    CK(c->tet_fill.ensure(n_tet), "alloc");
-    long long cap = c->pair_cap_hint > 0 ? c->pair_cap_hint : std::max<long long>(1 << 20, 16ll * n_tet);
-    for (int attempt = 0; attempt < 3; ++attempt) {
-      CK(c->pair_buf.ensure((size_t)cap), "alloc pairs");
-      CK(cudaMemsetAsync(c->tet_count.ptr, 0, sizeof(int32_t) * (size_t)n_tet, st), "memset");
-      CK(cudaMemsetAsync(c->scratch.ptr + 4, 0, sizeof(unsigned long long), st), "memset");
-      CK(cudaMemsetAsync(c->scratch.ptr + 20, 0, 6 * sizeof(unsigned long long), st), "memset");
-      for (int cl = 0; cl < rpd_ctx::kClasses; ++cl) {
-        if (c->class_count[cl] == 0) continue;
-        Grid tg = make_grid(c->mesh_lo, c->mesh_hi, c->class_count[cl], 4.0);
-        long long nc = (long long)tg.nx * tg.ny * tg.nz;
-        CK(c->t_cell_count.ensure(nc), "alloc");
-        CK(c->t_cell_start.ensure(nc + 1), "alloc");
-        CK(c->t_cell_fill.ensure(nc), "alloc");
-        CK(c->scan_tmp.ensure(scan_temp_ints(std::max<long long>(nc, n_tet)) + 16), "alloc");
-        CK(grid_build_tets(c->centroid.ptr, n_tet, c->tet_class.ptr, cl, tg, c->t_cell_of.ptr,
-                           c->t_cell_count.ptr, c->t_cell_start.ptr, c->t_cell_fill.ptr,
-                           c->t_cell_items.ptr, c->scan_tmp.ptr, st), "tet grid");
-        // per-site boxes: every tet of this class that passes the rule has
-        // its centroid in the site's cell pushed out by the class radius
-        const double R = c->class_radius[cl] * (1.0 + 1e-5) + 1e-6 * cs;
-        BoxParams bp;
-        bp.site4f = c->site4f.ptr;
-        bp.flags = c->flags.ptr;
-        bp.nbr = box_list;
-        bp.k = c->k;
-        // the nearest bisectors (distance-ordered GPU lists) for the common
-        // tets; the class of the largest tets has few tets, so a looser
-        // region costs little in the search and its box is cheap to clip
-        bp.k_box = knn ? std::min(c->k, cl == 0 ? box0 : std::min(box0, 12)) : c->k;
-        bp.n_site = n_site;
-        bp.box_lo = make_float4((float)(c->mesh_lo[0] - margin), (float)(c->mesh_lo[1] - margin),
-                                (float)(c->mesh_lo[2] - margin), 0.f);
-        bp.box_hi = make_float4((float)(c->mesh_hi[0] + margin), (float)(c->mesh_hi[1] + margin),
-                                (float)(c->mesh_hi[2] + margin), 0.f);
-        bp.offset_r = (float)R;
-        bp.offset_e = (float)(48.0 * u * (diag2 + std::fabs((double)c->w_max)));
-        bp.coord_scale = (float)cs;
-        bp.abs_margin = (float)margin;
-        bp.site_box = c->site_box.ptr;
-        bp.site_planes = c->site_planes.ptr;
-        bp.site_nplanes = c->site_nplanes.ptr;
-        bp.counters = nullptr;
-        int bw = 4;
-        int bblocks = std::max(1, std::min((n_site + bw - 1) / bw, c->num_sms * box_blocks_per_sm(bw)));
-        CK(launch_site_box(bp, bblocks, bw, st), "site boxes");
-        PairParams pp;
-        pp.vert3f = c->vert3f.ptr;
-        pp.tets = c->tets.ptr;
-        pp.centroid = c->centroid.ptr;
-        pp.tg = tg;
-        pp.tcell_start = c->t_cell_start.ptr;
-        pp.tcell_items = c->t_cell_items.ptr;
-        pp.site4f = c->site4f.ptr;
-        pp.flags = c->flags.ptr;
-        pp.nbr = c->nbr.ptr;
-        pp.rule_nbr = knn ? c->nbr_dist.ptr : nullptr;
-        pp.k = c->k;
-        pp.n_site = n_site;
-        pp.site_box = c->site_box.ptr;
-        pp.site_planes = c->site_planes.ptr;
-        pp.site_nplanes = c->site_nplanes.ptr;
-        pp.coord_scale = (float)cs;
-        pp.pair_buf = c->pair_buf.ptr;
-        pp.pair_cursor = c->scratch.ptr + 4;
-        pp.pair_cap = (long long)c->pair_buf.cap;
-        pp.tet_count = c->tet_count.ptr;
-        pp.diag = c->scratch.ptr + 20;
-        CK(c->pair_ntasks.ensure((size_t)n_site), "alloc");
-        CK(c->pair_taskoff.ensure((size_t)n_site + 1), "alloc");
-        CK(c->scan_tmp.ensure(scan_temp_ints(std::max<long long>(std::max<long long>(nc, n_tet), n_site)) + 16), "alloc");
-        CK(launch_pairs(pp, c->pair_ntasks.ptr, c->pair_taskoff.ptr, c->scan_tmp.ptr,
-                        c->scratch.ptr + 27, c->num_sms, st), "pairs");
-      }
-      unsigned long long np = 0;
-      CK(cudaMemcpyAsync(&np, c->scratch.ptr + 4, sizeof(np), cudaMemcpyDeviceToHost, st), "D2H");
-      CK(cudaStreamSynchronize(st), "pairs sync");
-      c->n_pairs = (long long)np;
-      if ((long long)np <= (long long)c->pair_buf.cap) break;
-      cap = (long long)np + (long long)np / 8 + 1024;
-      if (attempt == 2) return fail(c, RPD_ERR_CAPACITY, "rpd_compute: pair buffer");
-    }
-    if (c->n_pairs > INT32_MAX) return fail(c, RPD_ERR_CAPACITY, "rpd_compute: more than 2^31 pairs");
-    c->pair_cap_hint = std::max<long long>(c->pair_cap_hint, c->n_pairs + c->n_pairs / 8 + 1024);
-    CK(scan_exclusive(c->tet_count.ptr, c->tet_offsets.ptr, n_tet, c->scan_tmp.ptr, st), "scan");
-    CK(c->pair_site.ensure((size_t)c->n_pairs), "alloc");
-    CK(c->pair_tet.ensure((size_t)c->n_pairs), "alloc");
-    CK(pairs_to_csr(c->pair_buf.ptr, c->n_pairs, n_tet, c->tet_offsets.ptr, c->tet_fill.ptr,
-                    c->pair_site.ptr, c->pair_tet.ptr,
-                    reinterpret_cast<int32_t*>(c->scratch.ptr + 5), st), "csr");
-  }
+  const int n_tet = c->n_tet;
+  CK(c->tet_offsets.ensure((size_t)n_tet + 1), "alloc");
+  CK(c->tet_fill.ensure(n_tet), "alloc");
+  CK(c->scan_tmp.ensure(scan_temp_ints(std::max<long long>(c->n_pairs, n_tet)) + 16), "alloc");
+  CK(scan_exclusive(c->tet_count.ptr, c->tet_offsets.ptr, n_tet, c->scan_tmp.ptr, st), "scan");
+  CK(c->pair_site.ensure((size_t)c->n_pairs), "alloc");
+  CK(c->pair_tet.ensure((size_t)c->n_pairs), "alloc");
+  CK(pairs_to_csr(c->pair_buf.ptr, c->n_pairs, n_tet, c->tet_offsets.ptr, c->tet_fill.ptr,
+                  c->pair_site.ptr, c->pair_tet.ptr,
+                  reinterpret_cast<int32_t*>(c->scratch.ptr + 5), st), "csr");
   CK(cudaEventRecord(c->ev[kEvPairs], st), "event");
 
   // ---- learned list lengths: features and inference per pair
@@ -932,6 +643,166 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
     cudaEventElapsedTime(&stats->ms_epilogue, c->ev[kEvEpi0], c->ev[kEvClip]);
   }
   return RPD_OK;
+}
+
+rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
+  if (!c) return RPD_ERR_INVALID_ARGUMENT;
+  if (!c->has_mesh || !c->has_sites) return fail(c, RPD_ERR_NOT_READY, "rpd_compute: mesh and sites required");
+  const bool knn = c->cfg.neighbor_source == RPD_NEIGH_KNN;
+  if (!knn && !c->has_user_nbr)
+    return fail(c, RPD_ERR_NOT_READY, "rpd_compute: neighbour lists required (rpd_set_neighbors)");
+  const bool learned = c->cfg.learned_k != 0;
+  if (learned && (!c->cfg.certify || !knn))
+    return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_compute: learned_k needs certify and GPU-built lists");
+  if (learned && !c->mlp_ready)
+    return fail(c, RPD_ERR_NOT_READY,
+                "rpd_compute: learned_k needs a predictor (rpd_mlp_train or rpd_mlp_set_params)");
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  cudaStream_t st = c->stream;
+  const int n_site = c->n_site, n_tet = c->n_tet;
+  CK(c->scratch.ensure(32), "alloc scratch");
+  CK(cudaMemsetAsync(c->scratch.ptr, 0, 32 * sizeof(unsigned long long), st), "memset");
+  take_launches();
+  CK(cudaEventRecord(c->ev[kEvStart], st), "event");
+
+  // ---- neighbour lists
+  if (knn) {
+    c->k = c->cfg.knn_k;
+    Grid g = make_grid(c->site_lo, c->site_hi, n_site, 2.0);
+    long long nc = (long long)g.nx * g.ny * g.nz;
+    CK(c->s_cell_of.ensure(n_site), "alloc");
+    CK(c->s_cell_count.ensure(nc), "alloc");
+    CK(c->s_cell_start.ensure(nc + 1), "alloc");
+    CK(c->s_cell_fill.ensure(nc), "alloc");
+    CK(c->s_cell_items.ensure(n_site), "alloc");
+    CK(c->scan_tmp.ensure(scan_temp_ints(std::max<long long>(nc, n_tet)) + 16), "alloc");
+    CK(c->nbr.ensure((size_t)n_site * c->k), "alloc nbr");
+    CK(c->nbr_keys.ensure((size_t)n_site * c->k), "alloc nbr");
+    CK(c->nbr_dist.ensure((size_t)n_site * c->k), "alloc nbr");
+    CK(c->knn_status.ensure(n_site), "alloc");
+    CK(grid_build_sites(c->site4f.ptr, n_site, g, c->s_cell_of.ptr, c->s_cell_count.ptr,
+                        c->s_cell_start.ptr, c->s_cell_fill.ptr, c->s_cell_items.ptr,
+                        c->scan_tmp.ptr, st), "site grid");
+    CK(launch_knn(c->site4f.ptr, n_site, g, c->s_cell_start.ptr, c->s_cell_items.ptr, c->k,
+                  c->w_max, c->cfg.clip_order == RPD_ORDER_SITE_ID ? 1 : 0, c->nbr.ptr,
+                  c->nbr_keys.ptr, c->nbr_dist.ptr, c->knn_status.ptr, st), "knn");
+  }
+  CK(cudaEventRecord(c->ev[kEvKnn], st), "event");
+
+  // ---- candidate pairs
+  {
+    CK(c->centroid.ensure(n_tet), "alloc");
+    CK(c->t_cell_of.ensure(n_tet), "alloc");
+    CK(c->t_cell_items.ensure(n_tet), "alloc");
+    CK(tet_centroids(c->vert3f.ptr, c->tets.ptr, n_tet, c->centroid.ptr, st), "centroids");
+    double diag2 = 0.0, cs = 0.0;
+    for (int a = 0; a < 3; ++a) {
+      double l = std::min(c->mesh_lo[a], c->site_lo[a]), h = std::max(c->mesh_hi[a], c->site_hi[a]);
+      diag2 += (h - l) * (h - l);
+      cs = std::max(cs, std::max(std::fabs(l), std::fabs(h)));
+    }
+    const double u = std::ldexp(1.0, -24);
+    double ext = 0.0;
+    for (int a = 0; a < 3; ++a) ext = std::max(ext, c->mesh_hi[a] - c->mesh_lo[a]);
+    const double margin = 1e-4 * ext + 1e-6 * cs;
+    // the nearest bisectors bound each cell; with a GPU-built list the
+    // distance-ordered copy gives them first, a user list is used whole
+    const int32_t* box_list = knn ? c->nbr_dist.ptr : c->nbr.ptr;
+    const int box0 = c->cfg.box_planes > 0 ? c->cfg.box_planes : 32;
+    CK(c->site_box.ensure((size_t)n_site * 2), "alloc");
+    CK(c->site_planes.ensure((size_t)n_site * kBoxPlanes), "alloc");
+    CK(c->site_nplanes.ensure((size_t)n_site), "alloc");
+    CK(c->tet_count.ensure(n_tet), "alloc");
+    CK(c->tet_offsets.ensure((size_t)n_tet + 1), "alloc");
+    CK(c->tet_fill.ensure(n_tet), "alloc");
+    long long cap = c->pair_cap_hint > 0 ? c->pair_cap_hint : std::max<long long>(1 << 20, 16ll * n_tet);
+    for (int attempt = 0; attempt < 3; ++attempt) {
+      CK(c->pair_buf.ensure((size_t)cap), "alloc pairs");
+      CK(cudaMemsetAsync(c->tet_count.ptr, 0, sizeof(int32_t) * (size_t)n_tet, st), "memset");
+      CK(cudaMemsetAsync(c->scratch.ptr + 4, 0, sizeof(unsigned long long), st), "memset");
+      CK(cudaMemsetAsync(c->scratch.ptr + 20, 0, 6 * sizeof(unsigned long long), st), "memset");
+      for (int cl = 0; cl < rpd_ctx::kClasses; ++cl) {
+        if (c->class_count[cl] == 0) continue;
+        Grid tg = make_grid(c->mesh_lo, c->mesh_hi, c->class_count[cl], 4.0);
+        long long nc = (long long)tg.nx * tg.ny * tg.nz;
+        CK(c->t_cell_count.ensure(nc), "alloc");
+        CK(c->t_cell_start.ensure(nc + 1), "alloc");
+        CK(c->t_cell_fill.ensure(nc), "alloc");
+        CK(c->scan_tmp.ensure(scan_temp_ints(std::max<long long>(nc, n_tet)) + 16), "alloc");
+        CK(grid_build_tets(c->centroid.ptr, n_tet, c->tet_class.ptr, cl, tg, c->t_cell_of.ptr,
+                           c->t_cell_count.ptr, c->t_cell_start.ptr, c->t_cell_fill.ptr,
+                           c->t_cell_items.ptr, c->scan_tmp.ptr, st), "tet grid");
+        // per-site boxes: every tet of this class that passes the rule has
+        // its centroid in the site's cell pushed out by the class radius
+        const double R = c->class_radius[cl] * (1.0 + 1e-5) + 1e-6 * cs;
+        BoxParams bp;
+        bp.site4f = c->site4f.ptr;
+        bp.flags = c->flags.ptr;
+        bp.site_base = 0;
+        bp.nbr = box_list;
+        bp.k = c->k;
+        // the nearest bisectors (distance-ordered GPU lists) for the common
+        // tets; the class of the largest tets has few tets, so a looser
+        // region costs little in the search and its box is cheap to clip
+        bp.k_box = knn ? std::min(c->k, cl == 0 ? box0 : std::min(box0, 12)) : c->k;
+        bp.n_site = n_site;
+        bp.box_lo = make_float4((float)(c->mesh_lo[0] - margin), (float)(c->mesh_lo[1] - margin),
+                                (float)(c->mesh_lo[2] - margin), 0.f);
+        bp.box_hi = make_float4((float)(c->mesh_hi[0] + margin), (float)(c->mesh_hi[1] + margin),
+                                (float)(c->mesh_hi[2] + margin), 0.f);
+        bp.offset_r = (float)R;
+        bp.offset_e = (float)(48.0 * u * (diag2 + std::fabs((double)c->w_max)));
+        bp.coord_scale = (float)cs;
+        bp.abs_margin = (float)margin;
+        bp.site_box = c->site_box.ptr;
+        bp.site_planes = c->site_planes.ptr;
+        bp.site_nplanes = c->site_nplanes.ptr;
+        bp.counters = nullptr;
+        int bw = 4;
+        int bblocks = std::max(1, std::min((n_site + bw - 1) / bw, c->num_sms * box_blocks_per_sm(bw)));
+        CK(launch_site_box(bp, bblocks, bw, st), "site boxes");
+        PairParams pp;
+        pp.vert3f = c->vert3f.ptr;
+        pp.tets = c->tets.ptr;
+        pp.centroid = c->centroid.ptr;
+        pp.tet_base = 0;
+        pp.site_base = 0;
+        pp.tg = tg;
+        pp.tcell_start = c->t_cell_start.ptr;
+        pp.tcell_items = c->t_cell_items.ptr;
+        pp.site4f = c->site4f.ptr;
+        pp.flags = c->flags.ptr;
+        pp.nbr = c->nbr.ptr;
+        pp.rule_nbr = knn ? c->nbr_dist.ptr : nullptr;
+        pp.k = c->k;
+        pp.n_site = n_site;
+        pp.site_box = c->site_box.ptr;
+        pp.site_planes = c->site_planes.ptr;
+        pp.site_nplanes = c->site_nplanes.ptr;
+        pp.coord_scale = (float)cs;
+        pp.pair_buf = c->pair_buf.ptr;
+        pp.pair_cursor = c->scratch.ptr + 4;
+        pp.pair_cap = (long long)c->pair_buf.cap;
+        pp.tet_count = c->tet_count.ptr;
+        pp.diag = c->scratch.ptr + 20;
+        CK(c->pair_ntasks.ensure((size_t)n_site), "alloc");
+        CK(c->pair_taskoff.ensure((size_t)n_site + 1), "alloc");
+        CK(c->scan_tmp.ensure(scan_temp_ints(std::max<long long>(std::max<long long>(nc, n_tet), n_site)) + 16), "alloc");
+        CK(launch_pairs(pp, c->pair_ntasks.ptr, c->pair_taskoff.ptr, c->scan_tmp.ptr,
+                        c->scratch.ptr + 27, c->num_sms, st), "pairs");
+      }
+      unsigned long long np = 0;
+      CK(cudaMemcpyAsync(&np, c->scratch.ptr + 4, sizeof(np), cudaMemcpyDeviceToHost, st), "D2H");
+      CK(cudaStreamSynchronize(st), "pairs sync");
+      c->n_pairs = (long long)np;
+      if ((long long)np <= (long long)c->pair_buf.cap) break;
+      cap = (long long)np + (long long)np / 8 + 1024;
+      if (attempt == 2) return fail(c, RPD_ERR_CAPACITY, "rpd_compute: pair buffer");
+    }
+    if (c->n_pairs > INT32_MAX) return fail(c, RPD_ERR_CAPACITY, "rpd_compute: more than 2^31 pairs");
+    c->pair_cap_hint = std::max<long long>(c->pair_cap_hint, c->n_pairs + c->n_pairs / 8 + 1024);
+  }
+  return finish_compute(c, knn, learned, stats);
 }
 
 rpd_status rpd_autotune(rpd_ctx* c, int repeats, rpd_tuning* result) {
@@ -1491,3 +1362,12 @@ void rpd_host_free(void* p) {
 }
 
 }  // extern "C"
+
+rpd_status rpd_fail(rpd_ctx* c, rpd_status s, const std::string& msg) { return fail(c, s, msg); }
+rpd_status rpd_cuda_fail(rpd_ctx* c, cudaError_t e, const char* where) { return cuda_fail(c, e, where); }
+Grid rpd_make_grid(const double* lo, const double* hi, long long n_items, double per_cell) {
+  return make_grid(lo, hi, n_items, per_cell);
+}
+rpd_status rpd_finish_compute(rpd_ctx* c, bool knn, bool learned, rpd_stats* stats) {
+  return finish_compute(c, knn, learned, stats);
+}

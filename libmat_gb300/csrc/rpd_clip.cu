@@ -1238,7 +1238,7 @@ __global__ void __launch_bounds__(128, 6) site_box_kernel(BoxParams p) {
   for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < p.n_site; i += warps_total) {
     float lo[3] = {p.box_lo.x, p.box_lo.y, p.box_lo.z};
     float hi[3] = {p.box_hi.x, p.box_hi.y, p.box_hi.z};
-    if (p.flags[i] != 1u) {
+    if (p.flags[p.site_base + i] != 1u) {
       if (lane == 0) {
         p.site_box[2 * i] = make_float4(1.f, 1.f, 1.f, 0.f);  // empty box
         p.site_box[2 * i + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -1246,7 +1246,7 @@ __global__ void __launch_bounds__(128, 6) site_box_kernel(BoxParams p) {
       }
       continue;
     }
-    const float4 seed = p.site4f[i];
+    const float4 seed = p.site4f[p.site_base + i];
     // box planes x>=lo, x<=hi, y>=lo, y<=hi, z>=lo, z<=hi
     if (lane < 6) {
       int ax = lane >> 1;
@@ -1297,7 +1297,8 @@ __global__ void __launch_bounds__(128, 6) site_box_kernel(BoxParams p) {
     Cert nocert;
     nocert.keys = nullptr;
     nocert.certified = false;
-    clip_list<RPD_PRED_FP32_FILTER, false, false>(c, s, p.nbr + (long long)i * p.k, p.k_box, i,
+    clip_list<RPD_PRED_FP32_FILTER, false, false>(c, s, p.nbr + (long long)i * p.k, p.k_box,
+                                                  p.site_base + i,
                                                   make_plane, lane, pc, nocert);
     float bl[3], bh[3];
     if (s.status == kSuccess) {

@@ -1,0 +1,179 @@
+// rpd_ctx.hpp -- the engine context behind the C ABI (host side, internal):
+// device buffers, the stream, the events and the results of the last
+// compute.  Shared by rpd_api.cpp (single meshes) and rpd_batch.cpp (batches
+// of meshes).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <string>
+
+#include "../../include/rpd_gb300.h"
+#include "rpd_common.cuh"
+#include "rpd_kernels.cuh"
+
+using namespace rpd;
+
+namespace rpd_host {
+
+template <class T>
+struct DevBuf {
+  T* ptr = nullptr;
+  size_t cap = 0;  // elements
+  cudaError_t ensure(size_t n) {
+    if (n <= cap && ptr) return cudaSuccess;
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+    size_t want = std::max<size_t>(n, 1);
+    cudaError_t e = cudaMalloc((void**)&ptr, want * sizeof(T));
+    if (e == cudaSuccess) cap = want;
+    return e;
+  }
+  // grows to n elements keeping the first `keep` (stream-ordered copy)
+  cudaError_t grow_keep(size_t n, size_t keep, cudaStream_t st) {
+    if (n <= cap && ptr) return cudaSuccess;
+    T* old = ptr;
+    size_t want = std::max<size_t>(n, std::max<size_t>(2 * cap, 1));
+    T* fresh = nullptr;
+    cudaError_t e = cudaMalloc((void**)&fresh, want * sizeof(T));
+    if (e != cudaSuccess) return e;
+    if (old && keep) {
+      e = cudaMemcpyAsync(fresh, old, keep * sizeof(T), cudaMemcpyDeviceToDevice, st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+      if (e != cudaSuccess) {
+        cudaFree(fresh);
+        return e;
+      }
+    }
+    if (old) cudaFree(old);
+    ptr = fresh;
+    cap = want;
+    return cudaSuccess;
+  }
+  void release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+  }
+  ~DevBuf() { release(); }
+};
+
+enum Ev {
+  kEvStart, kEvKnn, kEvPairs, kEvPred0, kEvPred1, kEvClipK0, kEvClipK1, kEvEpi0, kEvClip, kEvEnd,
+  kEvCount
+};
+
+}  // namespace rpd_host
+
+using namespace rpd_host;
+
+struct rpd_ctx {
+  rpd_config cfg;
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[kEvCount] = {};
+  std::string err;
+
+  // mesh
+  int n_vert = 0, n_tet = 0;
+  DevBuf<float> vert3f;
+  DevBuf<double> vert3d;
+  DevBuf<float2> vert2;  // double-float copies (geometry epilogue)
+  DevBuf<int4> tets;
+  DevBuf<int32_t> v_adjs, f_adjs, f_ids;
+  DevBuf<uint8_t> e_adj6;
+  double mesh_lo[3] = {0, 0, 0}, mesh_hi[3] = {0, 0, 0};
+  double tet_radius = 0.0;
+  // tets grouped by radius (largest vertex distance to the centroid): the
+  // candidate search offsets each site's cell by its class's largest radius
+  static constexpr int kClasses = 8;
+  DevBuf<uint8_t> tet_class;
+  int class_count[kClasses] = {0};
+  double class_radius[kClasses] = {0};
+  bool has_mesh = false;
+
+  // sites
+  int n_site = 0;
+  DevBuf<float4> site4f;
+  DevBuf<double> site4d;
+  DevBuf<float2> site2;
+  DevBuf<uint32_t> flags;
+  double site_lo[3] = {0, 0, 0}, site_hi[3] = {0, 0, 0};
+  float w_max = 0.f;
+  bool has_sites = false;
+
+  // neighbour lists
+  int k = 0;
+  DevBuf<int32_t> nbr, nbr_dist, nbr_ref_tmp, knn_status, site_klen, reclip_idx;
+  bool has_site_klen = false;
+  DevBuf<unsigned long long> topo_hash;
+  long long n_reclipped = 0;
+  DevBuf<float> nbr_keys;
+  bool has_user_nbr = false;
+
+  // grids
+  DevBuf<int32_t> s_cell_of, s_cell_count, s_cell_start, s_cell_fill, s_cell_items;
+  DevBuf<int32_t> t_cell_of, t_cell_count, t_cell_start, t_cell_fill, t_cell_items;
+  DevBuf<float4> centroid, site_box, site_planes;
+  DevBuf<int32_t> site_nplanes, pair_ntasks, pair_taskoff;
+  DevBuf<int32_t> scan_tmp;
+
+  // pairs
+  DevBuf<int2> pair_buf;
+  DevBuf<int32_t> tet_count, tet_offsets, tet_fill, pair_site, pair_tet;
+  long long pair_cap_hint = 0;
+
+  // cells
+  DevBuf<rpd_cell_header> pair_headers, cells;
+  DevBuf<uint8_t> payload;
+  DevBuf<int32_t> flag_tmp, pos_tmp;
+  DevBuf<unsigned long long> scratch;  // [0] payload cursor [1] work [2..3] counters
+                                       // [4] pair cursor [8..18] status hist
+  DevBuf<long long> n_out;
+  long long payload_cap_hint = 0;
+
+  // learned list length: features, predictor, training set
+  double mesh_volume = 0.0;
+  DevBuf<float4> bverts;        // boundary vertices
+  int n_bverts = 0;
+  DevBuf<float> site_bdist;     // site -> nearest boundary vertex distance
+  bool bdist_valid = false;
+  DevBuf<uint16_t> feat;        // bf16 rows of the last features launch
+  long long n_feat_rows = 0;
+  DevBuf<int32_t> pair_klen, consumed, sample_idx;
+  bool want_consumed = false;
+  bool last_learned = false;
+  DevBuf<int32_t> user_pair_k;   // rpd_set_pair_k
+  long long n_user_pair_k = -1;
+  DevBuf<float> mlp_params, mlp_grads, mlp_m, mlp_v, mlp_loss, mlp_y, mlp_target;
+  DevBuf<uint16_t> mlp_W1T, mlp_W2, mlp_W2T;
+  float mlp_margin = 0.f;
+  bool mlp_ready = false;
+  DevBuf<uint16_t> train_X;
+  DevBuf<float> train_y;
+  DevBuf<int32_t> train_idx;
+  long long n_train = 0;
+
+  // results of the last compute
+  long long n_pairs = 0, n_cells = 0, payload_bytes = 0;
+  int tet_k = 0;
+  bool has_result = false;
+};
+
+// internal helpers of rpd_api.cpp used by the batch code
+rpd_status rpd_fail(rpd_ctx* c, rpd_status s, const std::string& msg);
+rpd_status rpd_cuda_fail(rpd_ctx* c, cudaError_t e, const char* where);
+Grid rpd_make_grid(const double* lo, const double* hi, long long n_items, double per_cell);
+// CSR, clipping, epilogue, compaction and statistics once pair_buf /
+// tet_count hold the candidate pairs (c->n_pairs of them)
+rpd_status rpd_finish_compute(rpd_ctx* c, bool knn, bool learned, rpd_stats* stats);
+
+#define RPD_CK(ctx, expr, where)                                      \
+  do {                                                                \
+    cudaError_t _e = (expr);                                          \
+    if (_e != cudaSuccess) return rpd_cuda_fail((ctx), _e, (where));  \
+  } while (0)

@@ -70,10 +70,14 @@ struct EpilogueParams {
 };
 cudaError_t launch_cell_epilogue(const EpilogueParams& p, int num_sms, cudaStream_t st);
 
+// Sites i of the box, pair and kNN kernels are 0..n_site-1 of one mesh;
+// site_base (tet_base) turns them into the indices of the arrays that hold
+// every mesh of a batch (0 for a single mesh).  Neighbour ids are global.
 struct BoxParams {
-  const float4* site4f;
-  const uint32_t* flags;
-  const int32_t* nbr;     // lists (row stride k); the first k_box entries are used
+  const float4* site4f;   // all sites
+  const uint32_t* flags;  // all sites
+  int site_base;
+  const int32_t* nbr;     // this mesh's rows (stride k); the first k_box entries are used
   int k;
   int k_box;
   int n_site;
@@ -136,20 +140,22 @@ cudaError_t grid_build_tets(const float4* centroid, int n_tet, const uint8_t* cl
 cudaError_t launch_knn(const float4* site4f, int n_site, const Grid& g,
                        const int32_t* cell_start, const int32_t* cell_items, int k,
                        float w_max, int order_by_id, int32_t* nbr, float* keys,
-                       int32_t* nbr_dist, int32_t* status, cudaStream_t st);
+                       int32_t* nbr_dist, int32_t* status, cudaStream_t st, int id_offset = 0);
 
 // candidate pairs: per site, tets whose centroid lies in the site's box and
 // that pass the reference rule; appends (tet, site) and counts per tet
 struct PairParams {
-  const float* vert3f;
-  const int4* tets;
-  const float4* centroid;
+  const float* vert3f;     // all vertices (tets hold global vertex ids)
+  const int4* tets;        // this mesh's tets
+  const float4* centroid;  // this mesh's tets
+  int tet_base;            // index of this mesh's first tet among all tets
+  int site_base;
   Grid tg;
   const int32_t* tcell_start;
   const int32_t* tcell_items;
-  const float4* site4f;
-  const uint32_t* flags;
-  const int32_t* nbr;
+  const float4* site4f;   // all sites
+  const uint32_t* flags;  // all sites
+  const int32_t* nbr;     // this mesh's rows
   const int32_t* rule_nbr;  // the same lists in another order (rule evaluation), or null
   int k;
   int n_site;
@@ -178,6 +184,18 @@ cudaError_t compact_cells(const rpd_cell_header* pair_headers, long long n_pairs
                           int32_t* flag_tmp, int32_t* pos_tmp, int32_t* scan_tmp,
                           rpd_cell_header* out, long long* n_out_dev,
                           unsigned long long* status_hist, cudaStream_t st);
+
+// batches: first compacted cell of each mesh (n_mesh + 1 entries); record
+// sizes; gather of one mesh's records with mesh-local ids
+cudaError_t mesh_cell_ranges(const rpd_cell_header* cells, const long long* n_cells,
+                             const int32_t* tet_base, int n_mesh, long long* first,
+                             cudaStream_t st);
+cudaError_t record_sizes(const rpd_cell_header* cells, long long n, unsigned long long* size,
+                         cudaStream_t st);
+cudaError_t gather_records(const rpd_cell_header* cells, long long n,
+                           const unsigned long long* new_off, const uint8_t* payload,
+                           int tet_base, int site_base, rpd_cell_header* hout, uint8_t* out,
+                           cudaStream_t st);
 
 // reference site_knn layout -> row-major lists; validation of ids
 cudaError_t neighbors_from_reference(const int32_t* ref, int k, int n_site, int32_t* nbr,

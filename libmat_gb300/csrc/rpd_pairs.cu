@@ -338,7 +338,7 @@ __device__ __forceinline__ int next_pow2(int x) {
 __global__ void __launch_bounds__(kKnnWarps * 32) knn_kernel(
     const float4* site4f, int n_site, Grid g, const int32_t* cell_start,
     const int32_t* cell_items, int k, float w_max, int order_by_id, int32_t* nbr, float* keys,
-    int32_t* nbr_dist, int32_t* status) {
+    int32_t* nbr_dist, int32_t* status, int id_offset) {
   __shared__ unsigned long long sbuf[kKnnWarps][kKnnBuf];
   __shared__ int scnt[kKnnWarps];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -412,7 +412,7 @@ __global__ void __launch_bounds__(kKnnWarps * 32) knn_kernel(
   if (status && lane == 0) status[i] = done ? 0 : 1;  // 1: exhausted grid
   // outputs in distance order
   for (int q = lane; q < k; q += 32) {
-    int32_t id = q < cnt ? (int32_t)(uint32_t)buf[q] : -1;
+    int32_t id = q < cnt ? (int32_t)(uint32_t)buf[q] + id_offset : -1;
     if (keys) keys[(long long)i * k + q] = q < cnt ? key_value((uint32_t)(buf[q] >> 32)) : INFINITY;
     if (!order_by_id) nbr[(long long)i * k + q] = id;
     if (nbr_dist) nbr_dist[(long long)i * k + q] = id;
@@ -430,18 +430,19 @@ __global__ void __launch_bounds__(kKnnWarps * 32) knn_kernel(
     __syncwarp();
     warp_bitonic_sort(buf, n, lane);
     for (int q = lane; q < k; q += 32)
-      nbr[(long long)i * k + q] = q < cnt ? (int32_t)buf[q] : -1;
+      nbr[(long long)i * k + q] = q < cnt ? (int32_t)buf[q] + id_offset : -1;
   }
 }
 
 cudaError_t launch_knn(const float4* site4f, int n_site, const Grid& g, const int32_t* cell_start,
                        const int32_t* cell_items, int k, float w_max, int order_by_id,
                        int32_t* nbr, float* keys, int32_t* nbr_dist, int32_t* status,
-                       cudaStream_t st) {
+                       cudaStream_t st, int id_offset) {
   if (n_site <= 0) return cudaSuccess;
   int blocks = (n_site + kKnnWarps - 1) / kKnnWarps;
   knn_kernel<<<blocks, kKnnWarps * 32, 0, st>>>(site4f, n_site, g, cell_start, cell_items, k,
-                                               w_max, order_by_id, nbr, keys, nbr_dist, status);
+                                               w_max, order_by_id, nbr, keys, nbr_dist, status,
+                                               id_offset);
   note_launches(1);
   return cudaGetLastError();
 }
@@ -467,7 +468,7 @@ struct CellRange {
 
 __device__ __forceinline__ CellRange site_cells(const PairParams& p, int i) {
   CellRange r = {0, 0, 0, 0, 0, 0};
-  if (p.flags[i] != 1u) return r;
+  if (p.flags[p.site_base + i] != 1u) return r;
   const float4 blo = p.site_box[2 * i], bhi = p.site_box[2 * i + 1];
   if (!(blo.x <= bhi.x && blo.y <= bhi.y && blo.z <= bhi.z)) return r;
   const Grid& g = p.tg;
@@ -535,7 +536,7 @@ __global__ void __launch_bounds__(kPairWarps * 32) pairs_kernel(PairParams p,
       pl[q] = make_float4(e.x, e.y, e.z, e.w + tol);
     }
     __syncwarp();
-    const float4 si = p.site4f[i];
+    const float4 si = p.site4f[p.site_base + i];
     const Grid& g = p.tg;
     // the rule is over the whole list; in ascending bisector distance (when
     // the GPU built it) the neighbour that dominates a far tet comes first
@@ -599,8 +600,9 @@ __global__ void __launch_bounds__(kPairWarps * 32) pairs_kernel(PairParams p,
         base = __shfl_sync(0xffffffffu, base, 0);
         if (pass) {
           unsigned long long slot = base + __popc(msk & ((1u << lane) - 1u));
-          if ((long long)slot < p.pair_cap) p.pair_buf[slot] = make_int2(t, i);
-          atomicAdd(p.tet_count + t, 1);
+          if ((long long)slot < p.pair_cap)
+            p.pair_buf[slot] = make_int2(t + p.tet_base, i + p.site_base);
+          atomicAdd(p.tet_count + p.tet_base + t, 1);
         }
       }
     });
@@ -767,6 +769,99 @@ cudaError_t neighbors_from_reference(const int32_t* ref, int k, int n_site, int3
     ref_lists_kernel<<<(int)((n + 255) / 256), 256, 0, st>>>(ref, k, n_site, nbr);
     note_launches(1);
   }
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------------
+// batches of meshes
+// ------------------------------------------------------------------------
+// first compacted cell of every mesh: cells are in ascending tet id and the
+// meshes' tets are consecutive ranges starting at tet_base[m]
+__global__ void mesh_cell_ranges_kernel(const rpd_cell_header* cells, const long long* n_cells,
+                                        const int32_t* tet_base, int n_mesh, long long* first) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m > n_mesh) return;
+  const long long n = *n_cells;
+  if (m == n_mesh) {
+    first[m] = n;
+    return;
+  }
+  const int key = tet_base[m];
+  long long lo = 0, hi = n;
+  while (lo < hi) {
+    const long long mid = (lo + hi) >> 1;
+    if (cells[mid].tet_id < key) lo = mid + 1;
+    else hi = mid;
+  }
+  first[m] = lo;
+}
+
+cudaError_t mesh_cell_ranges(const rpd_cell_header* cells, const long long* n_cells,
+                             const int32_t* tet_base, int n_mesh, long long* first,
+                             cudaStream_t st) {
+  mesh_cell_ranges_kernel<<<(n_mesh + 1 + 127) / 128, 128, 0, st>>>(cells, n_cells, tet_base,
+                                                                     n_mesh, first);
+  note_launches(1);
+  return cudaGetLastError();
+}
+
+// records of cells [0, n) copied to consecutive offsets new_off[q] of out,
+// with mesh-local ids: tet - tet_base, site - site_base in the headers and
+// in the site pairs of the bisector planes (planes 4.. of a record)
+__global__ void gather_records_kernel(const rpd_cell_header* cells, long long n,
+                                      const unsigned long long* new_off, const uint8_t* payload,
+                                      int tet_base, int site_base, rpd_cell_header* hout,
+                                      uint8_t* out) {
+  const int lane = threadIdx.x & 31;
+  const long long n_warps = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long q = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < n; q += n_warps) {
+    rpd_cell_header h = cells[q];
+    const PayloadLayout L(h.nb_v, h.nb_p, h.nb_e);
+    const uint4* src = reinterpret_cast<const uint4*>(payload + h.offset);
+    uint4* dst = reinterpret_cast<uint4*>(out + new_off[q]);
+    for (uint32_t i = lane; i < L.total / 16u; i += 32) dst[i] = src[i];
+    __syncwarp();
+    int2* id2 = reinterpret_cast<int2*>(out + new_off[q] + L.id2);
+    for (int i = 4 + lane; i < h.nb_p; i += 32) {
+      int2 v = id2[i];
+      id2[i] = make_int2(v.x - site_base, v.y - site_base);
+    }
+    if (lane == 0) {
+      h.tet_id -= tet_base;
+      h.site_id -= site_base;
+      h.offset = new_off[q];
+      hout[q] = h;
+    }
+  }
+}
+
+cudaError_t gather_records(const rpd_cell_header* cells, long long n,
+                           const unsigned long long* new_off, const uint8_t* payload,
+                           int tet_base, int site_base, rpd_cell_header* hout, uint8_t* out,
+                           cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  long long blocks = (n + 7) / 8;
+  if (blocks > 65535) blocks = 65535;
+  gather_records_kernel<<<(unsigned)blocks, 256, 0, st>>>(cells, n, new_off, payload, tet_base,
+                                                          site_base, hout, out);
+  note_launches(1);
+  return cudaGetLastError();
+}
+
+// record sizes of cells [0, n) (for the offsets of a gather)
+__global__ void record_sizes_kernel(const rpd_cell_header* cells, long long n,
+                                    unsigned long long* size) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const rpd_cell_header h = cells[q];
+  size[q] = PayloadLayout(h.nb_v, h.nb_p, h.nb_e).total;
+}
+
+cudaError_t record_sizes(const rpd_cell_header* cells, long long n, unsigned long long* size,
+                         cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  record_sizes_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(cells, n, size);
+  note_launches(1);
   return cudaGetLastError();
 }
 

@@ -44,6 +44,9 @@ EXPORTS = [
     "rpd_mlp_get_params", "rpd_mlp_set_params", "rpd_mlp_forward", "rpd_mlp_gradient",
     "rpd_mlp_copy_features", "rpd_mlp_copy_klen", "rpd_mlp_copy_samples", "rpd_set_pair_k",
     "rpd_get_config", "rpd_set_config",
+    "rpd_batch_create", "rpd_batch_destroy", "rpd_batch_last_error", "rpd_batch_add_mesh",
+    "rpd_batch_size", "rpd_batch_set_graph", "rpd_batch_compute", "rpd_batch_autotune",
+    "rpd_batch_mesh_cells", "rpd_batch_copy_mesh_cells", "rpd_batch_context",
 ]
 
 MLP_FEATURES = 16
@@ -182,6 +185,30 @@ def load(path=LIB_PATH):
     L.rpd_get_config.argtypes = [vp, c.POINTER(Config)]
     L.rpd_set_config.restype = i32
     L.rpd_set_config.argtypes = [vp, c.POINTER(Config)]
+    L.rpd_batch_create.restype = i32
+    L.rpd_batch_create.argtypes = [c.POINTER(Config), c.POINTER(vp)]
+    L.rpd_batch_destroy.restype = None
+    L.rpd_batch_destroy.argtypes = [vp]
+    L.rpd_batch_last_error.restype = c.c_char_p
+    L.rpd_batch_last_error.argtypes = [vp]
+    L.rpd_batch_add_mesh.restype = i32
+    L.rpd_batch_add_mesh.argtypes = [vp, vp, i32, vp, i32, vp, vp, vp, vp, vp, i32, vp,
+                                     c.POINTER(i32)]
+    L.rpd_batch_size.restype = i32
+    L.rpd_batch_size.argtypes = [vp]
+    L.rpd_batch_set_graph.restype = i32
+    L.rpd_batch_set_graph.argtypes = [vp, i32]
+    L.rpd_batch_compute.restype = i32
+    L.rpd_batch_compute.argtypes = [vp, c.POINTER(Stats)]
+    L.rpd_batch_autotune.restype = i32
+    L.rpd_batch_autotune.argtypes = [vp, i32, c.POINTER(Tuning)]
+    L.rpd_batch_mesh_cells.restype = i32
+    L.rpd_batch_mesh_cells.argtypes = [vp, i32, c.POINTER(i64), c.POINTER(i64)]
+    L.rpd_batch_copy_mesh_cells.restype = i32
+    L.rpd_batch_copy_mesh_cells.argtypes = [vp, i32, vp, i64, vp, i64, c.POINTER(i64),
+                                            c.POINTER(i64)]
+    L.rpd_batch_context.restype = vp
+    L.rpd_batch_context.argtypes = [vp]
     L.rpd_set_pair_k.restype = i32
     L.rpd_set_pair_k.argtypes = [vp, vp, i64]
     L.rpd_mlp_copy_samples.restype = i32
@@ -468,6 +495,128 @@ class RPD:
         self._check(self._L.rpd_copy_pairs_to_host(self._h, _p(offs), _p(sites), sites.size,
                                                    ctypes.byref(n)))
         return offs, sites[:n.value]
+
+
+class Batch:
+    """Many independent meshes clipped together (rpd_batch_*)."""
+
+    def __init__(self, device=0, predicate_mode=PRED_FP32_FILTER, knn_k=64,
+                 clip_order=ORDER_SITE_ID, compute_geometry=True, certify=False, clip_variant=0,
+                 topology_hash=True, use_graph=True):
+        L = load()
+        cfg = Config()
+        L.rpd_config_default(ctypes.byref(cfg))
+        cfg.device = device
+        cfg.predicate_mode = predicate_mode
+        cfg.neighbor_source = NEIGH_KNN
+        cfg.knn_k = knn_k
+        cfg.clip_order = clip_order
+        cfg.compute_geometry = 1 if compute_geometry else 0
+        cfg.certify = 1 if certify else 0
+        cfg.clip_variant = clip_variant
+        cfg.topology_hash = 1 if topology_hash else 0
+        h = ctypes.c_void_p()
+        s = L.rpd_batch_create(ctypes.byref(cfg), ctypes.byref(h))
+        if s != 0:
+            raise RPDError(s, L.rpd_status_string(s).decode())
+        self._L = L
+        self._h = h
+        self._L.rpd_batch_set_graph(h, 1 if use_graph else 0)
+        self.meshes = []
+
+    def close(self):
+        if self._h:
+            self._L.rpd_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, s):
+        if s != 0:
+            raise RPDError(s, self._L.rpd_batch_last_error(self._h).decode())
+
+    def add_mesh(self, vert3d, tets, v_adjs, e_adj6, f_adjs, f_ids, sites, flags=None):
+        v = np.ascontiguousarray(vert3d, np.float64)
+        t = np.ascontiguousarray(tets, np.int32)
+        s = np.ascontiguousarray(sites, np.float64)
+        f = None if flags is None else np.ascontiguousarray(flags, np.uint32)
+        idx = ctypes.c_int()
+        self._check(self._L.rpd_batch_add_mesh(
+            self._h, _p(v), v.shape[0], _p(t), t.shape[0],
+            _p(np.ascontiguousarray(v_adjs, np.int32)), _p(np.ascontiguousarray(e_adj6, np.uint8)),
+            _p(np.ascontiguousarray(f_adjs, np.int32)), _p(np.ascontiguousarray(f_ids, np.int32)),
+            _p(s), s.shape[0], _p(f), ctypes.byref(idx)))
+        self.meshes.append((t.shape[0], s.shape[0]))
+        return idx.value
+
+    def compute(self):
+        st = Stats()
+        self._check(self._L.rpd_batch_compute(self._h, ctypes.byref(st)))
+        return st
+
+    def autotune(self, repeats=1):
+        t = Tuning()
+        self._check(self._L.rpd_batch_autotune(self._h, repeats, ctypes.byref(t)))
+        return t
+
+    def mesh_cells(self, mesh):
+        """(headers, payload) of one mesh with its own tet / site ids."""
+        n = ctypes.c_int64()
+        b = ctypes.c_int64()
+        self._check(self._L.rpd_batch_copy_mesh_cells(self._h, mesh, None, 0, None, 0,
+                                                      ctypes.byref(n), ctypes.byref(b)))
+        h = np.zeros(max(n.value, 1), HEADER_DTYPE)
+        p = np.zeros(max(b.value, 1), np.uint8)
+        self._check(self._L.rpd_batch_copy_mesh_cells(self._h, mesh, _p(h), h.shape[0], _p(p),
+                                                      p.nbytes, ctypes.byref(n), ctypes.byref(b)))
+        return h[:n.value], p[:b.value]
+
+    def _ctx(self):
+        return ctypes.c_void_p(self._L.rpd_batch_context(self._h))
+
+    def topology_hashes(self):
+        """Topology hashes of all pairs of all meshes (batch order)."""
+        c = self._ctx()
+        n = ctypes.c_int64()
+        self._check(self._L.rpd_copy_topology_hashes_to_host(c, None, 0, ctypes.byref(n)))
+        out = np.zeros(max(n.value, 1), np.uint64)
+        self._check(self._L.rpd_copy_topology_hashes_to_host(c, _p(out), out.shape[0],
+                                                             ctypes.byref(n)))
+        return out[:n.value]
+
+    def pair_headers(self):
+        """Headers of all pairs of all meshes (batch tet / site ids)."""
+        c = self._ctx()
+        n = ctypes.c_int64()
+        self._check(self._L.rpd_copy_pair_headers_to_host(c, None, 0, ctypes.byref(n)))
+        out = np.zeros(max(n.value, 1), HEADER_DTYPE)
+        self._check(self._L.rpd_copy_pair_headers_to_host(c, _p(out), out.shape[0],
+                                                          ctypes.byref(n)))
+        return out[:n.value]
+
+    def configure(self, **fields):
+        c = self._ctx()
+        cfg = Config()
+        self._check(self._L.rpd_get_config(c, ctypes.byref(cfg)))
+        for k, v in fields.items():
+            setattr(cfg, k, int(v))
+        self._check(self._L.rpd_set_config(c, ctypes.byref(cfg)))
+
+    def mesh_range(self, mesh):
+        f = ctypes.c_int64()
+        n = ctypes.c_int64()
+        self._check(self._L.rpd_batch_mesh_cells(self._h, mesh, ctypes.byref(f), ctypes.byref(n)))
+        return f.value, n.value
 
 
 class PinnedArray:

@@ -173,3 +173,52 @@ def random_small(n_cube=4, n_site=40, seed=0, r_range=(0.01, 0.08)):
     v, x, rr = _normalise(vert, xyz, r)
     return dict(vert3d=v, tets=tets, sites=_pack_sites(x, rr),
                 flags=np.ones(n_site, np.uint32))
+
+
+def _random_rotation(rng):
+    q = rng.normal(size=4)
+    q /= np.linalg.norm(q)
+    w, x, y, z = q
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                     [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                     [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+
+
+def batch_mesh(i, seed=3, tet_range=(2_000, 200_000), site_range=(100, 20_000),
+               r_range=(0.005, 0.04)):
+    """Mesh i of the 'batched uneven' workload: a unit cube or an ellipsoid
+    (semi-axes 1.0/0.6/0.4), randomly rotated and scaled, with log-uniform
+    tet and site counts, sites uniform in the volume, radii uniform; seeded
+    by (seed, i).  Rotation and scale are applied before the mesh is mapped
+    to [0, 1000]^3 (so they change its shape in that frame, not its size)."""
+    rng = np.random.default_rng([seed, i])
+    n_tet = int(np.exp(rng.uniform(np.log(tet_range[0]), np.log(tet_range[1]))))
+    n_site = int(np.exp(rng.uniform(np.log(site_range[0]), np.log(site_range[1]))))
+    cube = rng.uniform() < 0.5
+    if cube:
+        n = max(2, int(round((n_tet / 6.0) ** (1.0 / 3.0))))
+        vert, tets = cube_grid_mesh(n)
+        xyz = rng.uniform(0.0, 1.0, size=(n_site, 3))
+    else:
+        axes = np.array([1.0, 0.6, 0.4])
+        vert, tets = ellipsoid_mesh(max(n_tet, 500), axes=tuple(axes), seed=int(rng.integers(1 << 30)))
+        pts = []
+        while sum(len(q) for q in pts) < n_site:
+            q = rng.uniform(-1, 1, size=(2 * n_site, 3)) * axes
+            q = q[((q / axes) ** 2).sum(axis=1) <= 1.0]
+            pts.append(q)
+        xyz = np.concatenate(pts)[:n_site]
+    R = _random_rotation(rng) * rng.uniform(0.5, 2.0)
+    vert = vert @ R.T
+    xyz = xyz @ R.T
+    r = rng.uniform(r_range[0], r_range[1], size=n_site) * np.abs(np.linalg.det(R)) ** (1.0 / 3.0)
+    if np.linalg.det(R) < 0:  # keep tets positively oriented
+        tets = tets[:, [1, 0, 2, 3]].copy()
+    v, x, rr = _normalise(vert, xyz, r)
+    return dict(vert3d=v, tets=tets.astype(np.int32), sites=_pack_sites(x, rr),
+                flags=np.ones(n_site, np.uint32), kind="cube" if cube else "ellipsoid")
+
+
+def config_batch(n_mesh=256, seed=3, **kw):
+    """The 'batched uneven' workload: n_mesh independent meshes (batch_mesh)."""
+    return [batch_mesh(i, seed=seed, **kw) for i in range(n_mesh)]
