@@ -38,6 +38,19 @@ struct BatchMesh {
 
 }  // namespace
 
+// scratch of one front-end lane (a stream on which whole meshes run)
+struct FrontLane {
+  cudaStream_t stream = nullptr;
+  cudaEvent_t done = nullptr;
+  DevBuf<int32_t> s_cell_count, s_cell_start, s_cell_fill, s_cell_items;
+  DevBuf<int32_t> t_cell_of, t_cell_count, t_cell_start, t_cell_fill, t_cell_items;
+  DevBuf<int32_t> scan_tmp, pair_ntasks, pair_taskoff;
+  DevBuf<unsigned long long> work;  // the pair kernel's task counter
+  std::vector<int> meshes;           // meshes of this lane
+};
+
+constexpr int kFrontLanes = 8;
+
 struct rpd_batch {
   rpd_ctx* ctx = nullptr;
   std::vector<BatchMesh> meshes;
@@ -47,10 +60,11 @@ struct rpd_batch {
   std::vector<uint8_t> e_adj6, tet_class;
   std::vector<uint32_t> flags;
   bool uploaded = false;
-  // per-mesh scratch of the front end (sized for the largest mesh)
-  DevBuf<int32_t> s_cell_count, s_cell_start, s_cell_fill, s_cell_items;
-  DevBuf<int32_t> t_cell_of, t_cell_count, t_cell_start, t_cell_fill, t_cell_items;
-  DevBuf<int32_t> scan_tmp, pair_ntasks, pair_taskoff, tet_base_dev;
+  // front-end lanes: meshes spread over streams that run concurrently, each
+  // with scratch sized for its largest mesh
+  FrontLane lanes[kFrontLanes];
+  cudaEvent_t fork = nullptr;
+  DevBuf<int32_t> tet_base_dev;
   DevBuf<long long> mesh_first_dev;
   std::vector<long long> mesh_first;
   // the captured front end
@@ -113,32 +127,53 @@ rpd_status upload(rpd_batch* b) {
   BCK(c->centroid.ensure((size_t)n_tet), "alloc");
   BCK(c->tet_count.ensure((size_t)n_tet), "alloc");
   BCK(c->scratch.ensure(32), "alloc");
-  long long max_sc = 1, max_tc = 1, max_site = 1, max_tet = 1;
-  for (BatchMesh& m : b->meshes) {
-    m.site_grid = rpd_make_grid(m.site_lo, m.site_hi, m.n_site, 2.0);
-    max_sc = std::max<long long>(max_sc, (long long)m.site_grid.nx * m.site_grid.ny * m.site_grid.nz);
-    for (int cl = 0; cl < 2; ++cl) {
-      if (m.class_count[cl] == 0) continue;
-      m.tet_grid[cl] = rpd_make_grid(m.mesh_lo, m.mesh_hi, m.class_count[cl], 4.0);
-      const Grid& g = m.tet_grid[cl];
-      max_tc = std::max<long long>(max_tc, (long long)g.nx * g.ny * g.nz);
-    }
-    max_site = std::max<long long>(max_site, m.n_site);
-    max_tet = std::max<long long>(max_tet, m.n_tet);
+  // meshes to lanes, largest first onto the least loaded lane
+  std::vector<int> order(b->meshes.size());
+  for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
+  auto work = [&](int i) { return (double)b->meshes[(size_t)i].n_tet + 4.0 * b->meshes[(size_t)i].n_site; };
+  std::sort(order.begin(), order.end(), [&](int x, int y) { return work(x) > work(y); });
+  double load[kFrontLanes] = {0};
+  for (FrontLane& L : b->lanes) L.meshes.clear();
+  for (int i : order) {
+    int best = 0;
+    for (int l = 1; l < kFrontLanes; ++l)
+      if (load[l] < load[best]) best = l;
+    load[best] += work(i);
+    b->lanes[best].meshes.push_back(i);
   }
-  BCK(b->s_cell_count.ensure((size_t)max_sc), "alloc");
-  BCK(b->s_cell_start.ensure((size_t)max_sc + 1), "alloc");
-  BCK(b->s_cell_fill.ensure((size_t)max_sc), "alloc");
-  BCK(b->s_cell_items.ensure((size_t)max_site), "alloc");
-  BCK(b->t_cell_of.ensure((size_t)max_tet), "alloc");
-  BCK(b->t_cell_items.ensure((size_t)max_tet), "alloc");
-  BCK(b->t_cell_count.ensure((size_t)max_tc), "alloc");
-  BCK(b->t_cell_start.ensure((size_t)max_tc + 1), "alloc");
-  BCK(b->t_cell_fill.ensure((size_t)max_tc), "alloc");
-  const long long scan_n = std::max(std::max(max_sc, max_tc), std::max(max_site, max_tet)) + 1;
-  BCK(b->scan_tmp.ensure(scan_temp_ints(scan_n) + 16), "alloc");
-  BCK(b->pair_ntasks.ensure((size_t)max_site), "alloc");
-  BCK(b->pair_taskoff.ensure((size_t)max_site + 1), "alloc");
+  for (FrontLane& L : b->lanes) {
+    if (!L.stream) BCK(cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking), "stream");
+    if (!L.done) BCK(cudaEventCreateWithFlags(&L.done, cudaEventDisableTiming), "event");
+    long long max_sc = 1, max_tc = 1, max_site = 1, max_tet = 1;
+    for (int i : L.meshes) {
+      BatchMesh& m = b->meshes[(size_t)i];
+      m.site_grid = rpd_make_grid(m.site_lo, m.site_hi, m.n_site, 2.0);
+      max_sc = std::max<long long>(max_sc, (long long)m.site_grid.nx * m.site_grid.ny * m.site_grid.nz);
+      for (int cl = 0; cl < 2; ++cl) {
+        if (m.class_count[cl] == 0) continue;
+        m.tet_grid[cl] = rpd_make_grid(m.mesh_lo, m.mesh_hi, m.class_count[cl], 4.0);
+        const Grid& g = m.tet_grid[cl];
+        max_tc = std::max<long long>(max_tc, (long long)g.nx * g.ny * g.nz);
+      }
+      max_site = std::max<long long>(max_site, m.n_site);
+      max_tet = std::max<long long>(max_tet, m.n_tet);
+    }
+    BCK(L.s_cell_count.ensure((size_t)max_sc), "alloc");
+    BCK(L.s_cell_start.ensure((size_t)max_sc + 1), "alloc");
+    BCK(L.s_cell_fill.ensure((size_t)max_sc), "alloc");
+    BCK(L.s_cell_items.ensure((size_t)max_site), "alloc");
+    BCK(L.t_cell_of.ensure((size_t)max_tet), "alloc");
+    BCK(L.t_cell_items.ensure((size_t)max_tet), "alloc");
+    BCK(L.t_cell_count.ensure((size_t)max_tc), "alloc");
+    BCK(L.t_cell_start.ensure((size_t)max_tc + 1), "alloc");
+    BCK(L.t_cell_fill.ensure((size_t)max_tc), "alloc");
+    const long long scan_n = std::max(std::max(max_sc, max_tc), std::max(max_site, max_tet)) + 1;
+    BCK(L.scan_tmp.ensure(scan_temp_ints(scan_n) + 16), "alloc");
+    BCK(L.pair_ntasks.ensure((size_t)max_site), "alloc");
+    BCK(L.pair_taskoff.ensure((size_t)max_site + 1), "alloc");
+    BCK(L.work.ensure(1), "alloc");
+  }
+  if (!b->fork) BCK(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming), "event");
   std::vector<int32_t> tb(b->meshes.size());
   for (size_t m = 0; m < b->meshes.size(); ++m) tb[m] = b->meshes[m].tet_base;
   BCK(b->tet_base_dev.ensure(tb.size()), "alloc");
@@ -163,16 +198,22 @@ rpd_status front_end(rpd_batch* b) {
   BCK(cudaMemsetAsync(c->scratch.ptr, 0, 32 * sizeof(unsigned long long), st), "memset");
   BCK(cudaMemsetAsync(c->tet_count.ptr, 0, sizeof(int32_t) * (size_t)c->n_tet, st), "memset");
   const double u = std::ldexp(1.0, -24);
-  for (const BatchMesh& m : b->meshes) {
+  BCK(cudaEventRecord(b->fork, st), "fork");
+  for (FrontLane& L : b->lanes) {
+   if (L.meshes.empty()) continue;
+   BCK(cudaStreamWaitEvent(L.stream, b->fork, 0), "fork wait");
+   const cudaStream_t ls = L.stream;
+   for (int mi : L.meshes) {
+    const BatchMesh& m = b->meshes[(size_t)mi];
     const int sb = m.site_base, tb = m.tet_base;
     // neighbour lists: the mesh's own site grid, ids offset to the batch
     BCK(grid_build_sites(c->site4f.ptr + sb, m.n_site, m.site_grid, c->s_cell_of.ptr + sb,
-                         b->s_cell_count.ptr, b->s_cell_start.ptr, b->s_cell_fill.ptr,
-                         b->s_cell_items.ptr, b->scan_tmp.ptr, st), "site grid");
-    BCK(launch_knn(c->site4f.ptr + sb, m.n_site, m.site_grid, b->s_cell_start.ptr,
-                   b->s_cell_items.ptr, k, m.w_max, c->cfg.clip_order == RPD_ORDER_SITE_ID ? 1 : 0,
+                         L.s_cell_count.ptr, L.s_cell_start.ptr, L.s_cell_fill.ptr,
+                         L.s_cell_items.ptr, L.scan_tmp.ptr, ls), "site grid");
+    BCK(launch_knn(c->site4f.ptr + sb, m.n_site, m.site_grid, L.s_cell_start.ptr,
+                   L.s_cell_items.ptr, k, m.w_max, c->cfg.clip_order == RPD_ORDER_SITE_ID ? 1 : 0,
                    c->nbr.ptr + (long long)sb * k, c->nbr_keys.ptr + (long long)sb * k,
-                   c->nbr_dist.ptr + (long long)sb * k, c->knn_status.ptr + sb, st, sb),
+                   c->nbr_dist.ptr + (long long)sb * k, c->knn_status.ptr + sb, ls, sb),
         "knn");
     // candidate pairs per radius class (as rpd_compute, with this mesh's bounds)
     double diag2 = 0.0, cs = 0.0, ext = 0.0;
@@ -188,8 +229,8 @@ rpd_status front_end(rpd_batch* b) {
       if (m.class_count[cl] == 0) continue;
       const Grid& tg = m.tet_grid[cl];
       BCK(grid_build_tets(c->centroid.ptr + tb, m.n_tet, c->tet_class.ptr + tb, cl, tg,
-                          b->t_cell_of.ptr, b->t_cell_count.ptr, b->t_cell_start.ptr,
-                          b->t_cell_fill.ptr, b->t_cell_items.ptr, b->scan_tmp.ptr, st),
+                          L.t_cell_of.ptr, L.t_cell_count.ptr, L.t_cell_start.ptr,
+                          L.t_cell_fill.ptr, L.t_cell_items.ptr, L.scan_tmp.ptr, ls),
           "tet grid");
       const double R = m.class_radius[cl] * (1.0 + 1e-5) + 1e-6 * cs;
       BoxParams bp;
@@ -214,7 +255,7 @@ rpd_status front_end(rpd_batch* b) {
       bp.counters = nullptr;
       const int bw = 4;
       const int bblocks = std::max(1, std::min((m.n_site + bw - 1) / bw, c->num_sms * box_blocks_per_sm(bw)));
-      BCK(launch_site_box(bp, bblocks, bw, st), "site boxes");
+      BCK(launch_site_box(bp, bblocks, bw, ls), "site boxes");
       PairParams pp;
       pp.vert3f = c->vert3f.ptr;
       pp.tets = c->tets.ptr + tb;
@@ -222,8 +263,8 @@ rpd_status front_end(rpd_batch* b) {
       pp.tet_base = tb;
       pp.site_base = sb;
       pp.tg = tg;
-      pp.tcell_start = b->t_cell_start.ptr;
-      pp.tcell_items = b->t_cell_items.ptr;
+      pp.tcell_start = L.t_cell_start.ptr;
+      pp.tcell_items = L.t_cell_items.ptr;
       pp.site4f = c->site4f.ptr;
       pp.flags = c->flags.ptr;
       pp.nbr = c->nbr.ptr + (long long)sb * k;
@@ -239,9 +280,12 @@ rpd_status front_end(rpd_batch* b) {
       pp.pair_cap = (long long)c->pair_buf.cap;
       pp.tet_count = c->tet_count.ptr;
       pp.diag = c->scratch.ptr + 20;
-      BCK(launch_pairs(pp, b->pair_ntasks.ptr, b->pair_taskoff.ptr, b->scan_tmp.ptr,
-                       c->scratch.ptr + 27, c->num_sms, st), "pairs");
+      BCK(launch_pairs(pp, L.pair_ntasks.ptr, L.pair_taskoff.ptr, L.scan_tmp.ptr, L.work.ptr,
+                       c->num_sms, ls), "pairs");
     }
+   }
+   BCK(cudaEventRecord(L.done, ls), "join");
+   BCK(cudaStreamWaitEvent(st, L.done, 0), "join wait");
   }
   return RPD_OK;
 }
@@ -270,6 +314,14 @@ void rpd_batch_destroy(rpd_batch* b) {
   if (!b) return;
   if (b->ctx) cudaSetDevice(b->ctx->device);
   drop_graph(b);
+  for (FrontLane& L : b->lanes) {
+    if (L.stream) {
+      cudaStreamSynchronize(L.stream);
+      cudaStreamDestroy(L.stream);
+    }
+    if (L.done) cudaEventDestroy(L.done);
+  }
+  if (b->fork) cudaEventDestroy(b->fork);
   rpd_destroy(b->ctx);
   delete b;
 }
