@@ -346,6 +346,7 @@ rpd_status rpd_set_mesh(rpd_ctx* c, const double* xyz, int n_vert, const int32_t
   CK(cudaMemcpyAsync(c->vert3f.ptr, vf.data(), vf.size() * 4, cudaMemcpyHostToDevice, st), "H2D vert");
   CK(cudaMemcpyAsync(c->vert3d.ptr, xyz, (size_t)n_vert * 24, cudaMemcpyHostToDevice, st), "H2D vert");
   CK(cudaMemcpyAsync(c->vert2.ptr, v2.data(), v2.size() * sizeof(float2), cudaMemcpyHostToDevice, st), "H2D vert");
+  CK(c->face2.ensure((size_t)n_tet * 16), "alloc faces");
   CK(cudaMemcpyAsync(c->tets.ptr, tets, (size_t)n_tet * 16, cudaMemcpyHostToDevice, st), "H2D tets");
   CK(cudaMemcpyAsync(c->v_adjs.ptr, v_adjs, (size_t)n_vert * 4, cudaMemcpyHostToDevice, st), "H2D v_adjs");
   CK(cudaMemcpyAsync(c->e_adj6.ptr, e_adj6, (size_t)n_tet * 6, cudaMemcpyHostToDevice, st), "H2D e_adj6");
@@ -354,6 +355,7 @@ rpd_status rpd_set_mesh(rpd_ctx* c, const double* xyz, int n_vert, const int32_t
   CK(cudaMemcpyAsync(c->tet_class.ptr, cls.data(), (size_t)n_tet, cudaMemcpyHostToDevice, st), "H2D classes");
   if (n_bv > 0)
     CK(cudaMemcpyAsync(c->bverts.ptr, bv.data(), bv.size() * 4, cudaMemcpyHostToDevice, st), "H2D boundary");
+  CK(launch_tet_face_planes(c->vert3d.ptr, c->tets.ptr, n_tet, c->face2.ptr, st), "face planes");
   CK(cudaStreamSynchronize(st), "set_mesh sync");
   c->n_bverts = n_bv;
   c->mesh_volume = volume;
@@ -588,8 +590,7 @@ static rpd_status finish_compute(rpd_ctx* c, bool knn, bool learned, rpd_stats* 
     ep.headers = c->pair_headers.ptr;
     ep.n_pairs = n_pairs;
     ep.payload = c->payload.ptr;
-    ep.tets = c->tets.ptr;
-    ep.vert2 = c->vert2.ptr;
+    ep.face2 = c->face2.ptr;
     ep.site2 = c->site2.ptr;
     ep.geometry = c->cfg.compute_geometry;
     ep.topo_hash = c->cfg.topology_hash ? c->topo_hash.ptr : nullptr;
@@ -694,7 +695,9 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
     CK(c->centroid.ensure(n_tet), "alloc");
     CK(c->t_cell_of.ensure(n_tet), "alloc");
     CK(c->t_cell_items.ensure(n_tet), "alloc");
-    CK(tet_centroids(c->vert3f.ptr, c->tets.ptr, n_tet, c->centroid.ptr, st), "centroids");
+    CK(c->tet_xyz.ensure((size_t)n_tet * 3), "alloc");
+    CK(tet_centroids(c->vert3f.ptr, c->tets.ptr, n_tet, c->centroid.ptr, st, c->tet_xyz.ptr),
+       "centroids");
     double diag2 = 0.0, cs = 0.0;
     for (int a = 0; a < 3; ++a) {
       double l = std::min(c->mesh_lo[a], c->site_lo[a]), h = std::max(c->mesh_hi[a], c->site_hi[a]);
@@ -765,6 +768,7 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
         pp.vert3f = c->vert3f.ptr;
         pp.tets = c->tets.ptr;
         pp.centroid = c->centroid.ptr;
+        pp.tet_xyz = c->tet_xyz.ptr;
         pp.tet_base = 0;
         pp.site_base = 0;
         pp.tg = tg;

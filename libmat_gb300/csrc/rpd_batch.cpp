@@ -180,7 +180,9 @@ rpd_status upload(rpd_batch* b) {
   BCK(cudaMemcpy(b->tet_base_dev.ptr, tb.data(), tb.size() * 4, cudaMemcpyHostToDevice), "H2D");
   BCK(b->mesh_first_dev.ensure(b->meshes.size() + 1), "alloc");
   // tet centroids (and radii) do not change: once
-  BCK(tet_centroids(c->vert3f.ptr, c->tets.ptr, n_tet, c->centroid.ptr, st), "centroids");
+  BCK(c->tet_xyz.ensure((size_t)n_tet * 3), "alloc");
+  BCK(tet_centroids(c->vert3f.ptr, c->tets.ptr, n_tet, c->centroid.ptr, st, c->tet_xyz.ptr),
+      "centroids");
   long long cap = c->pair_cap_hint > 0 ? c->pair_cap_hint : std::max<long long>(1 << 20, 8ll * n_tet);
   BCK(c->pair_buf.ensure((size_t)cap), "alloc pairs");
   BCK(cudaStreamSynchronize(st), "upload sync");
@@ -260,6 +262,7 @@ rpd_status front_end(rpd_batch* b) {
       pp.vert3f = c->vert3f.ptr;
       pp.tets = c->tets.ptr + tb;
       pp.centroid = c->centroid.ptr + tb;
+      pp.tet_xyz = c->tet_xyz.ptr + 3ll * tb;
       pp.tet_base = tb;
       pp.site_base = sb;
       pp.tg = tg;

@@ -768,7 +768,7 @@ __device__ __forceinline__ df dmul3(df a, df b, df c) { return df_mul(df_mul(a, 
 
 // 2x2 minor b_p c_q - b_q c_p
 __device__ __forceinline__ df minor2(df bp, df bq, df cp, df cq) {
-  return df_sub(df_mul(bp, cq), df_mul(bq, cp));
+  return df_sub_s(df_mul(bp, cq), df_mul(bq, cp));
 }
 
 __device__ __forceinline__ float3 f3sub(float3 a, float3 b) {
@@ -819,10 +819,10 @@ __device__ void vertex_of_float_planes(float4 a4, float4 b4, float4 c4, float* l
      cw = df_make(c4.w, 0.f);
   df mxy = minor2(bx, by, cx, cy), mxz = minor2(bx, bz, cx, cz), mxw = minor2(bx, bw, cx, cw);
   df myz = minor2(by, bz, cy, cz), myw = minor2(by, bw, cy, cw), mzw = minor2(bz, bw, cz, cw);
-  df Dw = df_add(df_sub(df_mul(ax, myz), df_mul(ay, mxz)), df_mul(az, mxy));
-  df Dx = df_add(df_sub(df_mul(ay, mzw), df_mul(az, myw)), df_mul(aw, myz));
-  df Dy = df_add(df_sub(df_mul(ax, mzw), df_mul(az, mxw)), df_mul(aw, mxz));
-  df Dz = df_add(df_sub(df_mul(ax, myw), df_mul(ay, mxw)), df_mul(aw, mxy));
+  df Dw = df_add_s(df_sub_s(df_mul(ax, myz), df_mul(ay, mxz)), df_mul(az, mxy));
+  df Dx = df_add_s(df_sub_s(df_mul(ay, mzw), df_mul(az, myw)), df_mul(aw, myz));
+  df Dy = df_add_s(df_sub_s(df_mul(ax, mzw), df_mul(az, mxw)), df_mul(aw, mxz));
+  df Dz = df_add_s(df_sub_s(df_mul(ax, myw), df_mul(ay, mxw)), df_mul(aw, mxy));
   const df inv = df_recip(Dw);
   const df X[3] = {df_neg(df_mul(Dx, inv)), df_mul(Dy, inv), df_neg(df_mul(Dz, inv))};
   for (int k = 0; k < 3; ++k) {
@@ -840,10 +840,10 @@ __device__ __forceinline__ void cell_vertex(const Cell& c, int pa, int pb, int p
   df cx = c.u.g.n[pc][0], cy = c.u.g.n[pc][1], cz = c.u.g.n[pc][2], cw = c.u.g.d[pc];
   df mxy = minor2(bx, by, cx, cy), mxz = minor2(bx, bz, cx, cz), mxw = minor2(bx, bw, cx, cw);
   df myz = minor2(by, bz, cy, cz), myw = minor2(by, bw, cy, cw), mzw = minor2(bz, bw, cz, cw);
-  df Dw = df_add(df_sub(df_mul(ax, myz), df_mul(ay, mxz)), df_mul(az, mxy));
-  df Dx = df_add(df_sub(df_mul(ay, mzw), df_mul(az, myw)), df_mul(aw, myz));
-  df Dy = df_add(df_sub(df_mul(ax, mzw), df_mul(az, mxw)), df_mul(aw, mxz));
-  df Dz = df_add(df_sub(df_mul(ax, myw), df_mul(ay, mxw)), df_mul(aw, mxy));
+  df Dw = df_add_s(df_sub_s(df_mul(ax, myz), df_mul(ay, mxz)), df_mul(az, mxy));
+  df Dx = df_add_s(df_sub_s(df_mul(ay, mzw), df_mul(az, myw)), df_mul(aw, myz));
+  df Dy = df_add_s(df_sub_s(df_mul(ax, mzw), df_mul(az, mxw)), df_mul(aw, mxz));
+  df Dz = df_add_s(df_sub_s(df_mul(ax, myw), df_mul(ay, mxw)), df_mul(aw, mxy));
   df inv = df_recip(Dw);
   X = df_neg(df_mul(Dx, inv));
   Y = df_mul(Dy, inv);
@@ -853,8 +853,8 @@ __device__ __forceinline__ void cell_vertex(const Cell& c, int pa, int pb, int p
 template <class Cell>
 __device__ __forceinline__ float vertex_volume_about(const Cell& c, uchar4 tr, df X, df Y,
                                                      df Z, float3 O) {
-  float3 A = make_float3(df_sub(X, df_make(O.x, 0.f)).hi, df_sub(Y, df_make(O.y, 0.f)).hi,
-                         df_sub(Z, df_make(O.z, 0.f)).hi);
+  float3 A = make_float3(df_sub_s(X, df_make(O.x, 0.f)).hi, df_sub_s(Y, df_make(O.y, 0.f)).hi,
+                         df_sub_s(Z, df_make(O.z, 0.f)).hi);
   const int pl[3] = {tr.x, tr.y, tr.z};
   float3 nn[3], ft[3];
   for (int k = 0; k < 3; ++k) {
@@ -884,7 +884,7 @@ __device__ __forceinline__ double widen(float f) {
 
 // S + X (double-float) rounded to double: hi and lo widen exactly, one add
 __device__ __forceinline__ double df_translate(df S, df X) {
-  const df t = df_add(S, X);
+  const df t = df_add_s(S, X);
   return widen(t.hi) + widen(t.lo);
 }
 
@@ -917,35 +917,30 @@ __device__ float3 float_vertex(const Cell& c, uchar4 tr) {
 // writes xyz[3 * nb_v] and returns the cell volume; c holds the cell's
 // id2 and ver, c.u.g is filled here
 template <class Cell>
-__device__ double cell_geometry(Cell& c, int nb_v, int nb_p, const float2* vert2,
-                                const float2* site2, const int* tvs, int sid, int lane,
-                                double* xyz) {
+__device__ double cell_geometry(Cell& c, int nb_v, int nb_p, const float2* face2,
+                                const float2* site2, int tet, int sid, int lane, double* xyz) {
   const float2* S2 = site2 + 4 * (long long)sid;
   const df Sx = ldf(S2), Sy = ldf(S2 + 1), Sz = ldf(S2 + 2), Sw = ldf(S2 + 3);
   for (int i = lane; i < nb_p; i += 32) {
     df nx, ny, nz, d;
     if (i < 4) {
-      const float2* a = vert2 + 3 * (long long)tvs[cFaceLv[i][0]];
-      const float2* b = vert2 + 3 * (long long)tvs[cFaceLv[i][1]];
-      const float2* e = vert2 + 3 * (long long)tvs[cFaceLv[i][2]];
-      const df a0 = ldf(a), a1 = ldf(a + 1), a2 = ldf(a + 2);
-      const df ax = df_sub(ldf(b), a0), ay = df_sub(ldf(b + 1), a1), az = df_sub(ldf(b + 2), a2);
-      const df bx = df_sub(ldf(e), a0), by = df_sub(ldf(e + 1), a1), bz = df_sub(ldf(e + 2), a2);
-      nx = df_sub(df_mul(ay, bz), df_mul(az, by));
-      ny = df_sub(df_mul(az, bx), df_mul(ax, bz));
-      nz = df_sub(df_mul(ax, by), df_mul(ay, bx));
-      const df v0x = df_sub(a0, Sx), v0y = df_sub(a1, Sy), v0z = df_sub(a2, Sz);
-      d = df_neg(df_add(df_add(df_mul(v0x, nx), df_mul(v0y, ny)), df_mul(v0z, nz)));
+      // the tet's face plane (FP64, once per mesh), moved to the seed frame:
+      // d' = d + n . S
+      const float2* f = face2 + 16 * (long long)tet + 4 * i;
+      nx = ldf(f);
+      ny = ldf(f + 1);
+      nz = ldf(f + 2);
+      d = df_add_s(ldf(f + 3), df_add_s(df_add_s(df_mul(nx, Sx), df_mul(ny, Sy)), df_mul(nz, Sz)));
     } else {
       const int2 id = c.id2[i];
       const int other = id.x == sid ? id.y : id.x;
       const float2* B = site2 + 4 * (long long)other;
       // bisector in the seed frame: n = S - B, d = (|n|^2 + wS - wB) / 2
-      nx = df_sub(Sx, ldf(B));
-      ny = df_sub(Sy, ldf(B + 1));
-      nz = df_sub(Sz, ldf(B + 2));
-      const df n2 = df_add(df_add(df_mul(nx, nx), df_mul(ny, ny)), df_mul(nz, nz));
-      d = df_add(n2, df_sub(Sw, ldf(B + 3)));
+      nx = df_sub_s(Sx, ldf(B));
+      ny = df_sub_s(Sy, ldf(B + 1));
+      nz = df_sub_s(Sz, ldf(B + 2));
+      const df n2 = df_add_s(df_add_s(df_mul(nx, nx), df_mul(ny, ny)), df_mul(nz, nz));
+      d = df_add_s(n2, df_sub_s(Sw, ldf(B + 3)));
       d = df_make(0.5f * d.hi, 0.5f * d.lo);
     }
     c.u.g.n[i][0] = nx;
@@ -959,7 +954,7 @@ __device__ double cell_geometry(Cell& c, int nb_v, int nb_p, const float2* vert2
   const float3 O = float_vertex(c, c.ver[0]);
   for (int i = lane; i < nb_p; i += 32) {
     const df n0 = c.u.g.n[i][0], n1 = c.u.g.n[i][1], n2 = c.u.g.n[i][2];
-    const df dc = df_add(c.u.g.d[i], df_add(df_add(df_mul(n0, df_make(O.x, 0.f)),
+    const df dc = df_add_s(c.u.g.d[i], df_add_s(df_add_s(df_mul(n0, df_make(O.x, 0.f)),
                                                    df_mul(n1, df_make(O.y, 0.f))),
                                             df_mul(n2, df_make(O.z, 0.f))));
     c.u.g.foot[i] = face_foot(make_float3(n0.hi, n1.hi, n2.hi), dc.hi);
@@ -1195,9 +1190,7 @@ __global__ void __launch_bounds__(256) cell_epilogue_kernel(EpilogueParams p) {
     double* xyz = reinterpret_cast<double*>(rec + L.xyz);
     double vol = 0.0;
     if (p.geometry) {
-      const int4 tv = __ldg(p.tets + hd.tet_id);
-      const int tvs[4] = {tv.x, tv.y, tv.z, tv.w};
-      vol = cell_geometry(c, nb_v, nb_p, p.vert2, p.site2, tvs, hd.site_id, lane, xyz);
+      vol = cell_geometry(c, nb_v, nb_p, p.face2, p.site2, hd.tet_id, hd.site_id, lane, xyz);
     } else {
       for (int i = lane; i < 3 * nb_v; i += 32) xyz[i] = 0.0;
     }
@@ -1209,6 +1202,38 @@ __global__ void __launch_bounds__(256) cell_epilogue_kernel(EpilogueParams p) {
     }
     __syncwarp();
   }
+}
+
+// face planes of every tet in FP64 (inward normals as tri2plane,
+// common_cuda.h:248-254: n = (b - a) x (e - a), d = -a . n), stored as
+// double-float (nx, ny, nz, d) per face
+__global__ void tet_face_planes_kernel(const double* vert, const int4* tets, int n_tet, float2* out) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_tet) return;
+  const int4 q = tets[t];
+  const int id[4] = {q.x, q.y, q.z, q.w};
+  for (int i = 0; i < 4; ++i) {
+    const double* a = vert + 3 * (long long)id[cFaceLv[i][0]];
+    const double* b = vert + 3 * (long long)id[cFaceLv[i][1]];
+    const double* e = vert + 3 * (long long)id[cFaceLv[i][2]];
+    const double ux = b[0] - a[0], uy = b[1] - a[1], uz = b[2] - a[2];
+    const double vx = e[0] - a[0], vy = e[1] - a[1], vz = e[2] - a[2];
+    const double nx = uy * vz - uz * vy, ny = uz * vx - ux * vz, nz = ux * vy - uy * vx;
+    const double d = -(a[0] * nx + a[1] * ny + a[2] * nz);
+    const double v[4] = {nx, ny, nz, d};
+    for (int k = 0; k < 4; ++k) {
+      const df x = df_from_double(v[k]);
+      out[16ll * t + 4 * i + k] = make_float2(x.hi, x.lo);
+    }
+  }
+}
+
+cudaError_t launch_tet_face_planes(const double* vert3d, const int4* tets, int n_tet, float2* out,
+                                   cudaStream_t st) {
+  if (n_tet <= 0) return cudaSuccess;
+  tet_face_planes_kernel<<<(n_tet + 255) / 256, 256, 0, st>>>(vert3d, tets, n_tet, out);
+  note_launches(1);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_cell_epilogue(const EpilogueParams& p, int num_sms, cudaStream_t st) {

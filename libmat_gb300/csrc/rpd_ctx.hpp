@@ -83,6 +83,7 @@ struct rpd_ctx {
   DevBuf<float> vert3f;
   DevBuf<double> vert3d;
   DevBuf<float2> vert2;  // double-float copies (geometry epilogue)
+  DevBuf<float2> face2;  // double-float face planes of every tet (geometry epilogue)
   DevBuf<int4> tets;
   DevBuf<int32_t> v_adjs, f_adjs, f_ids;
   DevBuf<uint8_t> e_adj6;
@@ -118,7 +119,7 @@ struct rpd_ctx {
   // grids
   DevBuf<int32_t> s_cell_of, s_cell_count, s_cell_start, s_cell_fill, s_cell_items;
   DevBuf<int32_t> t_cell_of, t_cell_count, t_cell_start, t_cell_fill, t_cell_items;
-  DevBuf<float4> centroid, site_box, site_planes;
+  DevBuf<float4> centroid, site_box, site_planes, tet_xyz;
   DevBuf<int32_t> site_nplanes, pair_ntasks, pair_taskoff;
   DevBuf<int32_t> scan_tmp;
 

@@ -66,6 +66,19 @@ __device__ __forceinline__ df df_neg(df x) { return df_make(-x.hi, -x.lo); }
 
 __device__ __forceinline__ df df_sub(df x, df y) { return df_add(x, df_neg(y)); }
 
+// SloppyDWPlusDW (Joldes, Muller, Popescu, Alg. 5): one TwoSum instead of
+// two.  Its relative error is bounded only for operands of one sign, but its
+// absolute error stays below about 3u^2 (|x| + |y|) -- which is what the
+// forward error analysis of a determinant or a dot product needs (errors
+// relative to the magnitudes of the summed products).  Used by the geometry.
+__device__ __forceinline__ df df_add_s(df x, df y) {
+  df s = two_sum(x.hi, y.hi);
+  float v = x.lo + y.lo;
+  float w = s.lo + v;
+  return fast_two_sum(s.hi, w);
+}
+__device__ __forceinline__ df df_sub_s(df x, df y) { return df_add_s(x, df_neg(y)); }
+
 __device__ __forceinline__ df df_mul(df x, df y) {
   df c = two_prod(x.hi, y.hi);
   float t = x.hi * y.lo;

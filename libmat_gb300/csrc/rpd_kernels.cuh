@@ -62,13 +62,15 @@ struct EpilogueParams {
   rpd_cell_header* headers;  // n_pairs; volume written for emitted cells
   long long n_pairs;
   uint8_t* payload;          // xyz sections written
-  const int4* tets;
-  const float2* vert2;
+  const float2* face2;            // n_tet x 16: double-float tet face planes
   const float2* site2;
   int geometry;                   // 0: xyz zero, volume 0
   unsigned long long* topo_hash;  // n_pairs, or null
 };
 cudaError_t launch_cell_epilogue(const EpilogueParams& p, int num_sms, cudaStream_t st);
+// double-float (nx, ny, nz, d) of the four face planes of every tet, from FP64
+cudaError_t launch_tet_face_planes(const double* vert3d, const int4* tets, int n_tet, float2* out,
+                                   cudaStream_t st);
 
 // Sites i of the box, pair and kNN kernels are 0..n_site-1 of one mesh;
 // site_base (tet_base) turns them into the indices of the arrays that hold
@@ -127,8 +129,10 @@ cudaError_t scan_exclusive(const int32_t* in, int32_t* out, long long n, int32_t
 cudaError_t grid_build_sites(const float4* pts, int n, const Grid& g, int32_t* cell_of,
                              int32_t* cell_count, int32_t* cell_start, int32_t* cell_fill,
                              int32_t* cell_items, int32_t* scan_tmp, cudaStream_t st);
+// centroid (w = largest vertex distance) of every tet and, optionally, its
+// four vertices packed in three float4
 cudaError_t tet_centroids(const float* vert3f, const int4* tets, int n_tet, float4* centroid,
-                          cudaStream_t st);
+                          cudaStream_t st, float4* tet_xyz = nullptr);
 // bins the tets of radius class `want` (all tets when cls is null) by centroid
 cudaError_t grid_build_tets(const float4* centroid, int n_tet, const uint8_t* cls, int want,
                             const Grid& g, int32_t* cell_of, int32_t* cell_count,
@@ -148,6 +152,7 @@ struct PairParams {
   const float* vert3f;     // all vertices (tets hold global vertex ids)
   const int4* tets;        // this mesh's tets
   const float4* centroid;  // this mesh's tets
+  const float4* tet_xyz;   // this mesh's tets: vertices packed in 3 float4
   int tet_base;            // index of this mesh's first tet among all tets
   int site_base;
   Grid tg;

@@ -200,7 +200,8 @@ cudaError_t grid_build_sites(const float4* pts, int n, const Grid& g, int32_t* c
 }
 
 // centroid and radius (largest vertex distance) of every tet
-__global__ void tet_centroid_kernel(const float* v, const int4* tets, int n_tet, float4* out) {
+__global__ void tet_centroid_kernel(const float* v, const int4* tets, int n_tet, float4* out,
+                                    float4* xyz) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n_tet) return;
   int4 q = tets[t];
@@ -220,12 +221,21 @@ __global__ void tet_centroid_kernel(const float* v, const int4* tets, int n_tet,
     r2 = fmaxf(r2, dx * dx + dy * dy + dz * dz);
   }
   out[t] = make_float4(cx, cy, cz, sqrtf(r2));
+  if (xyz) {  // the four vertices, packed: (v0, v1.x) (v1.yz, v2.xy) (v2.z, v3)
+    float f[12];
+    for (int k = 0; k < 4; ++k)
+      for (int a = 0; a < 3; ++a) f[3 * k + a] = v[3 * id[k] + a];
+    xyz[3ll * t] = make_float4(f[0], f[1], f[2], f[3]);
+    xyz[3ll * t + 1] = make_float4(f[4], f[5], f[6], f[7]);
+    xyz[3ll * t + 2] = make_float4(f[8], f[9], f[10], f[11]);
+  }
 }
 
 cudaError_t tet_centroids(const float* vert3f, const int4* tets, int n_tet, float4* centroid,
-                          cudaStream_t st) {
+                          cudaStream_t st, float4* tet_xyz) {
   if (n_tet > 0) {
-    tet_centroid_kernel<<<(n_tet + 255) / 256, 256, 0, st>>>(vert3f, tets, n_tet, centroid);
+    tet_centroid_kernel<<<(n_tet + 255) / 256, 256, 0, st>>>(vert3f, tets, n_tet, centroid,
+                                                              tet_xyz);
     note_launches(1);
   }
   return cudaGetLastError();
@@ -460,6 +470,7 @@ __device__ __forceinline__ float pow_dist(float4 s, float3 v) {
 }
 
 constexpr int kPairWarps = 4;
+constexpr int kPairMaxK = 128;  // longest neighbour list (rpd_config.knn_k <= 128)
 
 // cell range of the site's box in the tet grid (empty range for no box)
 struct CellRange {
@@ -501,6 +512,7 @@ __global__ void __launch_bounds__(kPairWarps * 32) pairs_kernel(PairParams p,
                                                                 const int32_t* task_off,
                                                                 unsigned long long* work) {
   __shared__ float4 spl[kPairWarps][kBoxPlanes];
+  __shared__ float4 snb[kPairWarps][kPairMaxK];  // the site's neighbours (rule order)
   const int lane = threadIdx.x & 31;
   const int wid = threadIdx.x >> 5;
   const long long n_tasks = task_off[p.n_site];
@@ -541,6 +553,14 @@ __global__ void __launch_bounds__(kPairWarps * 32) pairs_kernel(PairParams p,
     // the rule is over the whole list; in ascending bisector distance (when
     // the GPU built it) the neighbour that dominates a far tet comes first
     const int32_t* L = (p.rule_nbr ? p.rule_nbr : p.nbr) + (long long)i * p.k;
+    float4* nb = snb[wid];
+    // a hole (-1) never rejects a tet: weight -inf makes its power distance +inf
+    const int k_staged = min(p.k, kPairMaxK);
+    for (int r = lane; r < k_staged; r += 32) {
+      const int m = __ldg(L + r);
+      nb[r] = m < 0 ? make_float4(0.f, 0.f, 0.f, -INFINITY) : __ldg(p.site4f + m);
+    }
+    __syncwarp();
     n_cells_seen += n_iter;
     // half extent of a grid cell, grown for the rounding of the binning
     const float hc = 0.5f * g.cell * (1.0f + 1e-3f) + 1e-6f * p.coord_scale;
@@ -573,20 +593,22 @@ __global__ void __launch_bounds__(kPairWarps * 32) pairs_kernel(PairParams p,
         }
         if (in) {
           ++n_in;
-          int4 q = p.tets[t];
-          float3 v[4];
-          int id[4] = {q.x, q.y, q.z, q.w};
+          const float4 q0 = __ldg(p.tet_xyz + 3ll * t), q1 = __ldg(p.tet_xyz + 3ll * t + 1),
+                       q2 = __ldg(p.tet_xyz + 3ll * t + 2);
+          const float3 v[4] = {make_float3(q0.x, q0.y, q0.z), make_float3(q0.w, q1.x, q1.y),
+                               make_float3(q1.z, q1.w, q2.x), make_float3(q2.y, q2.z, q2.w)};
           float pdi[4];
-          for (int a = 0; a < 4; ++a) {
-            v[a] = make_float3(p.vert3f[3 * id[a]], p.vert3f[3 * id[a] + 1],
-                               p.vert3f[3 * id[a] + 2]);
-            pdi[a] = pow_dist(si, v[a]);
-          }
+          for (int a = 0; a < 4; ++a) pdi[a] = pow_dist(si, v[a]);
           pass = true;
+          // voronoi.cu:154-193; holes (-1) are skipped (voronoi.cu:171)
           for (int r = 0; r < p.k && pass; ++r) {
-            int m = __ldg(L + r);
-            if (m == -1) continue;  // voronoi.cu:171 skips holes
-            float4 sm = __ldg(p.site4f + m);
+            float4 sm;
+            if (r < k_staged) {
+              sm = nb[r];
+            } else {  // lists longer than the staging (user lists)
+              const int m = __ldg(L + r);
+              sm = m < 0 ? make_float4(0.f, 0.f, 0.f, -INFINITY) : __ldg(p.site4f + m);
+            }
             bool hit = false;
             for (int a = 0; a < 4; ++a) hit |= pow_dist(sm, v[a]) > pdi[a];
             pass = hit;
