@@ -519,6 +519,8 @@ static rpd_status finish_compute(rpd_ctx* c, bool knn, bool learned, rpd_stats* 
     p.vert3d = c->vert3d.ptr;
     p.tets = c->tets.ptr;
     p.v_adjs = c->v_adjs.ptr;
+    p.tet_xyz = c->tet_xyz.ptr;
+    p.tet_vadj = c->tet_vadj.ptr;
     p.e_adj6 = c->e_adj6.ptr;
     p.f_adjs = c->f_adjs.ptr;
     p.f_ids = c->f_ids.ptr;
@@ -696,7 +698,9 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
     CK(c->t_cell_of.ensure(n_tet), "alloc");
     CK(c->t_cell_items.ensure(n_tet), "alloc");
     CK(c->tet_xyz.ensure((size_t)n_tet * 3), "alloc");
-    CK(tet_centroids(c->vert3f.ptr, c->tets.ptr, n_tet, c->centroid.ptr, st, c->tet_xyz.ptr),
+    CK(c->tet_vadj.ensure((size_t)n_tet), "alloc");
+    CK(tet_centroids(c->vert3f.ptr, c->tets.ptr, n_tet, c->centroid.ptr, st, c->tet_xyz.ptr,
+                     c->v_adjs.ptr, c->tet_vadj.ptr),
        "centroids");
     double diag2 = 0.0, cs = 0.0;
     for (int a = 0; a < 3; ++a) {

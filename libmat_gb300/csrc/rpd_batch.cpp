@@ -181,7 +181,9 @@ rpd_status upload(rpd_batch* b) {
   BCK(b->mesh_first_dev.ensure(b->meshes.size() + 1), "alloc");
   // tet centroids (and radii) do not change: once
   BCK(c->tet_xyz.ensure((size_t)n_tet * 3), "alloc");
-  BCK(tet_centroids(c->vert3f.ptr, c->tets.ptr, n_tet, c->centroid.ptr, st, c->tet_xyz.ptr),
+  BCK(c->tet_vadj.ensure((size_t)n_tet), "alloc");
+  BCK(tet_centroids(c->vert3f.ptr, c->tets.ptr, n_tet, c->centroid.ptr, st, c->tet_xyz.ptr,
+                    c->v_adjs.ptr, c->tet_vadj.ptr),
       "centroids");
   long long cap = c->pair_cap_hint > 0 ? c->pair_cap_hint : std::max<long long>(1 << 20, 8ll * n_tet);
   BCK(c->pair_buf.ensure((size_t)cap), "alloc pairs");

@@ -46,6 +46,7 @@ struct __align__(16) WarpCell {
     struct {
       float4 K[kMaxT];  // cofactors of each vertex (filter)
       float4 M[kMaxT];  // 3x3 permanents matching each cofactor (filter)
+      float rad[kMaxT]; // bound on each vertex's distance to the seed (certificate)
     } f;
     struct {
       df n[kMaxP][3];   // plane normal, seed frame, double-float (geometry)
@@ -408,6 +409,9 @@ __device__ __forceinline__ void swap_slots(WarpCell& c, int a, int b) {
   float4 m = c.u.f.M[a];
   c.u.f.M[a] = c.u.f.M[b];
   c.u.f.M[b] = m;
+  float r = c.u.f.rad[a];
+  c.u.f.rad[a] = c.u.f.rad[b];
+  c.u.f.rad[b] = r;
 }
 
 __device__ __forceinline__ uint8_t tri_plane(const uchar4& t, int e) {
@@ -566,17 +570,6 @@ __device__ __forceinline__ uint64_t shfl64(uint64_t v, int src) {
   return ((uint64_t)hi << 32) | lo;
 }
 
-// recompute the filter cofactors of vertex slots [from, to)
-__device__ __forceinline__ void refresh_cofactors(WarpCell& c, int from, int to, int lane) {
-  for (int v = from + lane; v < to; v += 32) {
-    uchar4 t = c.ver[v];
-    float4 K, M;
-    vertex_cofactors(c.pl[t.x], c.pl[t.y], c.pl[t.z], K, M);
-    c.u.f.K[v] = K;
-    c.u.f.M[v] = M;
-  }
-}
-
 // ------------------------------------------------------------------------
 // the neighbour loop shared by the cell kernel and the box kernel
 // ------------------------------------------------------------------------
@@ -610,11 +603,27 @@ __device__ __forceinline__ float vertex_radius(float4 K, float4 M, float3 S) {
   return num / (aw - ew) * (1.0f + 1e-6f);
 }
 
-__device__ __forceinline__ float cell_radius(const WarpCell& c, int nb_v, float3 S, int lane) {
+// the cell radius: the largest of the vertices' cached bounds
+__device__ __forceinline__ float cell_radius(const WarpCell& c, int nb_v, int lane) {
   float r = 0.f;
-  for (int v = lane; v < nb_v; v += 32) r = fmaxf(r, vertex_radius(c.u.f.K[v], c.u.f.M[v], S));
+  for (int v = lane; v < nb_v; v += 32) r = fmaxf(r, c.u.f.rad[v]);
   for (int o = 16; o > 0; o >>= 1) r = fmaxf(r, __shfl_xor_sync(0xffffffffu, r, o));
   return r;
+}
+
+// recompute the filter cofactors (and with RAD the radius bounds about the
+// seed S) of vertex slots [from, to)
+template <bool RAD>
+__device__ __forceinline__ void refresh_cofactors(WarpCell& c, int from, int to, int lane,
+                                                  float3 S) {
+  for (int v = from + lane; v < to; v += 32) {
+    uchar4 t = c.ver[v];
+    float4 K, M;
+    vertex_cofactors(c.pl[t.x], c.pl[t.y], c.pl[t.z], K, M);
+    c.u.f.K[v] = K;
+    c.u.f.M[v] = M;
+    if (RAD) c.u.f.rad[v] = vertex_radius(K, M, S);
+  }
 }
 
 struct Cert {
@@ -643,7 +652,7 @@ __device__ void clip_list(WarpCell& c, CellState& s, const int32_t* list, int k,
   constexpr bool kCof = uses_filter(PRED) || CERT;
   const bool eager = CERT && !cert.lazy;
   float R = INFINITY;
-  if (eager) R = cell_radius(c, s.nb_v, cert.S, lane);
+  if (eager) R = cell_radius(c, s.nb_v, lane);
   cert.consumed = k;
   for (int base = 0; base < k && s.status == kSuccess; base += 32) {
     int j = (base + lane < k) ? __ldg(list + base + lane) : -1;
@@ -732,11 +741,12 @@ __device__ void clip_list(WarpCell& c, CellState& s, const int32_t* list, int k,
             vertex_cofactors(c.pl[t.x], c.pl[t.y], c.pl[t.z], K, M);
             c.u.f.K[v] = K;
             c.u.f.M[v] = M;
+            if (CERT) c.u.f.rad[v] = vertex_radius(K, M, cert.S);
           }
         }
       }
       __syncwarp();
-      if (eager && s.status == kSuccess) R = cell_radius(c, s.nb_v, cert.S, lane);
+      if (eager && s.status == kSuccess) R = cell_radius(c, s.nb_v, lane);
       // later planes of this chunk identical to the new one
       if (plane_eq(e_mine, e)) dup_mine |= 1ull << (s.nb_p - 1);
       if (s.status != kSuccess) break;
@@ -1030,21 +1040,22 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : kClipMaxThreads, MINB > 0 ? M
     const int sid = __ldg(p.pair_site + q);
     const float4 seed = __ldg(p.site4f + sid);
 
-    // ---- cell = tet (convex_cell.cu:116-214)
-    const int4 tv = __ldg(p.tets + t);
-    const int tvs[4] = {tv.x, tv.y, tv.z, tv.w};
+    // ---- cell = tet (convex_cell.cu:116-214); the tet's float vertices and
+    // vertex counts come packed per tet (one dependent load less)
     if (lane < 4) {
-      int a = tvs[cFaceLv[lane][0]], b = tvs[cFaceLv[lane][1]], d = tvs[cFaceLv[lane][2]];
-      float3 v0 = make_float3(p.vert3f[3 * a], p.vert3f[3 * a + 1], p.vert3f[3 * a + 2]);
-      float3 v1 = make_float3(p.vert3f[3 * b], p.vert3f[3 * b + 1], p.vert3f[3 * b + 2]);
-      float3 v2 = make_float3(p.vert3f[3 * d], p.vert3f[3 * d + 1], p.vert3f[3 * d + 2]);
-      c.pl[lane] = tri2plane_f(v0, v1, v2);
+      const float4 q0 = __ldg(p.tet_xyz + 3ll * t), q1 = __ldg(p.tet_xyz + 3ll * t + 1),
+                   q2 = __ldg(p.tet_xyz + 3ll * t + 2);
+      const float3 tvx[4] = {make_float3(q0.x, q0.y, q0.z), make_float3(q0.w, q1.x, q1.y),
+                             make_float3(q1.z, q1.w, q2.x), make_float3(q2.y, q2.z, q2.w)};
+      c.pl[lane] = tri2plane_f(tvx[cFaceLv[lane][0]], tvx[cFaceLv[lane][1]], tvx[cFaceLv[lane][2]]);
       c.h[lane] = (uint8_t)__ldg(p.f_adjs + 4 * t + lane);
       c.id2[lane] = make_int2(__ldg(p.f_ids + 4 * t + lane), -1);
     } else if (lane < 8) {
       int i = lane - 4;
+      const uchar4 va = __ldg(p.tet_vadj + t);
+      const uint8_t vi = i == 0 ? va.x : (i == 1 ? va.y : (i == 2 ? va.z : va.w));
       c.ver[i] = make_uchar4((uint8_t)cTetTri[i][0], (uint8_t)cTetTri[i][1],
-                             (uint8_t)cTetTri[i][2], (uint8_t)__ldg(p.v_adjs + tvs[i]));
+                             (uint8_t)cTetTri[i][2], vi);
     } else if (lane < 14) {
       int e = lane - 8;
       c.edge[e] = make_uchar4((uint8_t)cEdgeFaces[e][0], (uint8_t)cEdgeFaces[e][1],
@@ -1057,7 +1068,7 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : kClipMaxThreads, MINB > 0 ? M
     s.nb_e = 6;
     s.status = kSuccess;
     if (uses_filter(PRED) || CERT) {
-      refresh_cofactors(c, 0, 4, lane);
+      refresh_cofactors<CERT>(c, 0, 4, lane, make_float3(seed.x, seed.y, seed.z));
       __syncwarp();
     }
 
@@ -1082,7 +1093,7 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : kClipMaxThreads, MINB > 0 ? M
       bool ok = false;
       if (cert.lazy) {
         // one certificate test after the whole short list
-        float R = cell_radius(c, s.nb_v, cert.S, lane);
+        float R = cell_radius(c, s.nb_v, lane);
         ok = cert_holds(__ldg(cert.keys + klen), R, cert.margin);
       }
       if (!ok) {
@@ -1302,7 +1313,7 @@ __global__ void __launch_bounds__(128, 6) site_box_kernel(BoxParams p) {
     s.nb_p = 6;
     s.nb_e = 0;
     s.status = kSuccess;
-    refresh_cofactors(c, 0, 8, lane);
+    refresh_cofactors<false>(c, 0, 8, lane, make_float3(0.f, 0.f, 0.f));
     __syncwarp();
     const float4* site4f = p.site4f;
     const float R = p.offset_r, E = p.offset_e;

@@ -22,6 +22,8 @@ struct ClipParams {
   const double* vert3d;  // n_vert x 3
   const int4* tets;
   const int32_t* v_adjs;
+  const float4* tet_xyz;  // n_tet x 3: the tet's float vertices, packed
+  const uchar4* tet_vadj; // n_tet: #tets of each of the tet's vertices (uint8, as recorded)
   const uint8_t* e_adj6;  // n_tet x 6
   const int32_t* f_adjs;  // n_tet x 4
   const int32_t* f_ids;   // n_tet x 4
@@ -130,9 +132,10 @@ cudaError_t grid_build_sites(const float4* pts, int n, const Grid& g, int32_t* c
                              int32_t* cell_count, int32_t* cell_start, int32_t* cell_fill,
                              int32_t* cell_items, int32_t* scan_tmp, cudaStream_t st);
 // centroid (w = largest vertex distance) of every tet and, optionally, its
-// four vertices packed in three float4
+// four vertices packed in three float4 and its vertices' tet counts (uint8)
 cudaError_t tet_centroids(const float* vert3f, const int4* tets, int n_tet, float4* centroid,
-                          cudaStream_t st, float4* tet_xyz = nullptr);
+                          cudaStream_t st, float4* tet_xyz = nullptr,
+                          const int32_t* v_adjs = nullptr, uchar4* tet_vadj = nullptr);
 // bins the tets of radius class `want` (all tets when cls is null) by centroid
 cudaError_t grid_build_tets(const float4* centroid, int n_tet, const uint8_t* cls, int want,
                             const Grid& g, int32_t* cell_of, int32_t* cell_count,

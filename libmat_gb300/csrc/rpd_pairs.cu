@@ -201,7 +201,7 @@ cudaError_t grid_build_sites(const float4* pts, int n, const Grid& g, int32_t* c
 
 // centroid and radius (largest vertex distance) of every tet
 __global__ void tet_centroid_kernel(const float* v, const int4* tets, int n_tet, float4* out,
-                                    float4* xyz) {
+                                    float4* xyz, const int32_t* v_adjs, uchar4* vadj) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n_tet) return;
   int4 q = tets[t];
@@ -229,13 +229,17 @@ __global__ void tet_centroid_kernel(const float* v, const int4* tets, int n_tet,
     xyz[3ll * t + 1] = make_float4(f[4], f[5], f[6], f[7]);
     xyz[3ll * t + 2] = make_float4(f[8], f[9], f[10], f[11]);
   }
+  if (vadj)
+    vadj[t] = make_uchar4((uint8_t)v_adjs[id[0]], (uint8_t)v_adjs[id[1]], (uint8_t)v_adjs[id[2]],
+                          (uint8_t)v_adjs[id[3]]);
 }
 
 cudaError_t tet_centroids(const float* vert3f, const int4* tets, int n_tet, float4* centroid,
-                          cudaStream_t st, float4* tet_xyz) {
+                          cudaStream_t st, float4* tet_xyz, const int32_t* v_adjs,
+                          uchar4* tet_vadj) {
   if (n_tet > 0) {
     tet_centroid_kernel<<<(n_tet + 255) / 256, 256, 0, st>>>(vert3f, tets, n_tet, centroid,
-                                                              tet_xyz);
+                                                              tet_xyz, v_adjs, tet_vadj);
     note_launches(1);
   }
   return cudaGetLastError();
