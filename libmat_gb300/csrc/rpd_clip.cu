@@ -59,11 +59,13 @@ struct __align__(16) WarpCell {
   uchar4 edge[kMaxE];
   uint8_t h[kMaxP];
   uint8_t bnext[kMaxP];
+  uint8_t perm[kMaxT];  // during a clip: the slot each surviving vertex came from
 };
 
 struct CellState {
   int nb_v, nb_p, nb_e;
   int status;
+  int kept;  // vertices that survived the last clip (slots [0, kept))
 };
 
 // local faces / edges of a tet (convex_cell.h:25-29, convex_cell.cu:193-211)
@@ -398,21 +400,6 @@ __device__ __forceinline__ void putbit(uint32_t* m, int i, bool b) {
   m[i >> 5] = b ? (m[i >> 5] | bit) : (m[i >> 5] & ~bit);
 }
 
-template <bool FULL>
-__device__ __forceinline__ void swap_slots(WarpCell& c, int a, int b) {
-  uchar4 t = c.ver[a];
-  c.ver[a] = c.ver[b];
-  c.ver[b] = t;
-  float4 k = c.u.f.K[a];
-  c.u.f.K[a] = c.u.f.K[b];
-  c.u.f.K[b] = k;
-  float4 m = c.u.f.M[a];
-  c.u.f.M[a] = c.u.f.M[b];
-  c.u.f.M[b] = m;
-  float r = c.u.f.rad[a];
-  c.u.f.rad[a] = c.u.f.rad[b];
-  c.u.f.rad[b] = r;
-}
 
 __device__ __forceinline__ uint8_t tri_plane(const uchar4& t, int e) {
   return e == 0 ? t.x : (e == 1 ? t.y : t.z);
@@ -487,24 +474,50 @@ __device__ __forceinline__ uint8_t edge_adj(const WarpCell& c, int a, int b) {
 // otherwise only the polytope (box clipping for the candidate filter).
 template <bool FULL>
 __device__ void apply_clip(WarpCell& c, CellState& s, const uint32_t* mask_in) {
-  uint32_t m[3] = {mask_in[0], mask_in[1], mask_in[2]};
+  // conflict bits of vertex slots 0..95 in registers (32-bit words)
+  uint32_t m0 = mask_in[0], m1 = mask_in[1], m2 = mask_in[2];
   const int cur = s.nb_p;
   s.nb_p++;
-  // conflict partition, exactly the reference's swap-to-tail loop
+  // conflict partition, exactly the reference's swap-to-tail loop.  Only the
+  // dual triangles move here; perm records where each slot's vertex came
+  // from, and the warp moves the cofactors afterwards (the conflict bit of
+  // a slot at or past the shrinking end is never read again)
   int nb_v = s.nb_v, nb_r = 0, i = 0;
   while (i < nb_v) {
-    if (getbit(m, i)) {
+    const uint32_t wi = i < 32 ? m0 : (i < 64 ? m1 : m2);
+    if ((wi >> (i & 31)) & 1u) {
       nb_v--;
-      swap_slots<FULL>(c, i, nb_v);
-      bool bi = getbit(m, i), bn = getbit(m, nb_v);
-      putbit(m, i, bn);
-      putbit(m, nb_v, bi);
+      const uchar4 tv = c.ver[i];
+      c.ver[i] = c.ver[nb_v];
+      c.ver[nb_v] = tv;
+      if (FULL) {  // cell kernel: the cofactors move with the triangle
+        const float4 k = c.u.f.K[i];
+        c.u.f.K[i] = c.u.f.K[nb_v];
+        c.u.f.K[nb_v] = k;
+        const float4 mm = c.u.f.M[i];
+        c.u.f.M[i] = c.u.f.M[nb_v];
+        c.u.f.M[nb_v] = mm;
+        const float r = c.u.f.rad[i];
+        c.u.f.rad[i] = c.u.f.rad[nb_v];
+        c.u.f.rad[nb_v] = r;
+      } else {  // box kernel: the warp moves them afterwards (perm)
+        const uint8_t pv = c.perm[i];
+        c.perm[i] = c.perm[nb_v];
+        c.perm[nb_v] = pv;
+      }
+      const uint32_t wn = nb_v < 32 ? m0 : (nb_v < 64 ? m1 : m2);
+      const uint32_t bit = 1u << (i & 31);
+      const uint32_t nw = ((wn >> (nb_v & 31)) & 1u) ? (wi | bit) : (wi & ~bit);
+      if (i < 32) m0 = nw;
+      else if (i < 64) m1 = nw;
+      else m2 = nw;
       nb_r++;
     } else {
       i++;
     }
   }
   s.nb_v = nb_v;
+  s.kept = nb_v;
   if (nb_v == 0) {
     s.status = kNoIntersection;
     return;
@@ -513,6 +526,7 @@ __device__ void apply_clip(WarpCell& c, CellState& s, const uint32_t* mask_in) {
   compute_boundary(c, nb_v, nb_r, first, s.status);
   if (s.status != kSuccess) return;
   if (first == kEnd) return;
+  const uint8_t hcur = c.h[cur];
   if (FULL) {
     int cir = first;
     do {
@@ -520,32 +534,46 @@ __device__ void apply_clip(WarpCell& c, CellState& s, const uint32_t* mask_in) {
         s.status = kEdgeOverflow;
         return;
       }
-      uint8_t ha = c.h[cur], hb = c.h[cir];
-      c.edge[s.nb_e] = make_uchar4((uint8_t)(cur < cir ? cur : cir),
-                                   (uint8_t)(cur < cir ? cir : cur), ha > hb ? ha : hb, 0);
+      // cur > cir: the new plane has the largest index
+      const uint8_t hb = c.h[cir];
+      c.edge[s.nb_e] = make_uchar4((uint8_t)cir, (uint8_t)cur, hcur > hb ? hcur : hb, 0);
       s.nb_e++;
       cir = c.bnext[cir];
     } while (cir != first);
   }
+  // new vertices around the cavity boundary; the planes and face counts of
+  // consecutive boundary planes carry over from one step to the next
+  const float4 pcur = c.pl[cur];
   int cir = first;
+  float4 pcir = c.pl[cir];
+  uint8_t hcir = c.h[cir];
   do {
-    int nx = c.bnext[cir];
+    const int nx = c.bnext[cir];
+    const float4 pnx = c.pl[nx];
+    const uint8_t hnx = c.h[nx];
     if (s.nb_v + 1 >= kMaxT) {
       s.status = kTriangleOverflow;
     } else {
       uint8_t adj = 0;
       if (FULL) {
-        adj = edge_adj(c, cur, cir);
-        uint8_t a2 = edge_adj(c, cur, nx), a3 = edge_adj(c, cir, nx);
-        if (a2 > adj) adj = a2;
-        if (a3 > adj) adj = a3;
+        // max of the counts of the vertex's three edges (edge_adj): the two
+        // edges on the new plane have max(h_cur, h_other); the third is a
+        // tet edge (its own count) when both its planes are tet faces
+        adj = hcur > hcir ? hcur : hcir;
+        if (hnx > adj) adj = hnx;
+        if (cir < 4 && nx < 4) {
+          const uint8_t te = c.edge[cTetEdgeSlot[cir][nx]].z;
+          if (te > adj) adj = te;
+        }
       }
       c.ver[s.nb_v] = make_uchar4((uint8_t)cur, (uint8_t)cir, (uint8_t)nx, adj);
       s.nb_v++;
     }
-    if (FULL && det3x3_f(c.pl[cur], c.pl[cir], c.pl[nx]) == 0.f) s.status = kNeedsPerturb;
+    if (FULL && det3x3_f(pcur, pcir, pnx) == 0.f) s.status = kNeedsPerturb;
     if (s.status != kSuccess) return;
     cir = nx;
+    pcir = pnx;
+    hcir = hnx;
   } while (cir != first);
 }
 
@@ -554,6 +582,7 @@ __device__ __forceinline__ void broadcast_state(CellState& s) {
   s.nb_p = __shfl_sync(0xffffffffu, s.nb_p, 0);
   s.nb_e = __shfl_sync(0xffffffffu, s.nb_e, 0);
   s.status = __shfl_sync(0xffffffffu, s.status, 0);
+  s.kept = __shfl_sync(0xffffffffu, s.kept, 0);
 }
 
 __device__ __forceinline__ float4 shfl4(float4 v, int src) {
@@ -720,6 +749,8 @@ __device__ void clip_list(WarpCell& c, CellState& s, const int32_t* list, int k,
       float4 e = shfl4(e_mine, hit);
       int jn = __shfl_sync(0xffffffffu, j, hit);
       if (lane < kMaxP / 4) reinterpret_cast<uint32_t*>(c.bnext)[lane] = 0xffffffffu;
+      if (kCof && !FULL)
+        for (int v = lane; v < s.nb_v; v += 32) c.perm[v] = (uint8_t)v;
       __syncwarp();
       if (lane == 0) {
         const int cur = s.nb_p;
@@ -730,6 +761,21 @@ __device__ void clip_list(WarpCell& c, CellState& s, const int32_t* list, int k,
       }
       __syncwarp();
       broadcast_state(s);
+      // the surviving vertices' cofactors follow their dual triangles: a
+      // survivor moved into slot v < kept came from a slot >= kept (the
+      // partition only swaps with its shrinking end), so sources and
+      // targets never overlap
+      if (kCof && !FULL && s.status == kSuccess) {
+        for (int v = lane; v < s.kept; v += 32) {
+          const int src = c.perm[v];
+          if (src != v) {
+            c.u.f.K[v] = c.u.f.K[src];
+            c.u.f.M[v] = c.u.f.M[src];
+            if (CERT) c.u.f.rad[v] = c.u.f.rad[src];
+          }
+        }
+        __syncwarp();
+      }
       // the vertices created by this clip are exactly those whose first
       // plane is the new one; the surviving ones kept their cofactors
       if (kCof && s.status == kSuccess) {
@@ -1045,9 +1091,14 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : kClipMaxThreads, MINB > 0 ? M
     if (lane < 4) {
       const float4 q0 = __ldg(p.tet_xyz + 3ll * t), q1 = __ldg(p.tet_xyz + 3ll * t + 1),
                    q2 = __ldg(p.tet_xyz + 3ll * t + 2);
-      const float3 tvx[4] = {make_float3(q0.x, q0.y, q0.z), make_float3(q0.w, q1.x, q1.y),
-                             make_float3(q1.z, q1.w, q2.x), make_float3(q2.y, q2.z, q2.w)};
-      c.pl[lane] = tri2plane_f(tvx[cFaceLv[lane][0]], tvx[cFaceLv[lane][1]], tvx[cFaceLv[lane][2]]);
+      const float3 t0 = make_float3(q0.x, q0.y, q0.z), t1 = make_float3(q0.w, q1.x, q1.y),
+                   t2 = make_float3(q1.z, q1.w, q2.x), t3 = make_float3(q2.y, q2.z, q2.w);
+      // face `lane` (cFaceLv): (2,1,3), (0,2,3), (1,0,3), (0,1,2), selected
+      // without indexing a local array by lane
+      const float3 fa = lane == 0 ? t2 : (lane == 1 ? t0 : (lane == 2 ? t1 : t0));
+      const float3 fb = lane == 0 ? t1 : (lane == 1 ? t2 : (lane == 2 ? t0 : t1));
+      const float3 fc = lane == 3 ? t2 : t3;
+      c.pl[lane] = tri2plane_f(fa, fb, fc);
       c.h[lane] = (uint8_t)__ldg(p.f_adjs + 4 * t + lane);
       c.id2[lane] = make_int2(__ldg(p.f_ids + 4 * t + lane), -1);
     } else if (lane < 8) {
