@@ -27,6 +27,7 @@ CUDA_UNITS = {
     "rpd_pairs.cu": ["-fmad=false"],
     "rpd_noalloc.cu": [],
     "rpd_mlp.cu": [],
+    "rpd_prep.cu": [],
 }
 CXX_UNITS = ["rpd_api.cpp", "rpd_mesh.cpp", "rpd_batch.cpp"]
 

@@ -82,6 +82,16 @@ Grid make_grid(const double* lo, const double* hi, long long n_items, double per
 // c->feat; with `target`, the labels log2(max(consumed, 1)) as well
 rpd_status pair_features(rpd_ctx* c, const int32_t* pair_index, long long n_rows, float* target) {
   cudaStream_t st = c->stream;
+  if (c->n_bverts < 0) {  // boundary vertices, from the marks of rpd_set_mesh
+    CK(c->bverts.ensure((size_t)c->n_vert), "alloc");
+    CK(c->prep_hist.ensure(kRadiusBins), "alloc");
+    CK(boundary_list(c->bmark.ptr, c->vert3f.ptr, c->n_vert, c->bverts.ptr, c->prep_hist.ptr, st),
+       "boundary");
+    int32_t nb = 0;
+    CK(cudaMemcpyAsync(&nb, c->prep_hist.ptr, sizeof(nb), cudaMemcpyDeviceToHost, st), "D2H");
+    CK(cudaStreamSynchronize(st), "boundary sync");
+    c->n_bverts = nb;
+  }
   if (!c->bdist_valid) {
     CK(c->site_bdist.ensure((size_t)c->n_site), "alloc");
     CK(launch_boundary_distance(c->site4f.ptr, c->n_site, c->bverts.ptr, c->n_bverts,
@@ -261,118 +271,76 @@ rpd_status rpd_set_mesh(rpd_ctx* c, const double* xyz, int n_vert, const int32_t
   if (n_vert <= 0 || n_tet <= 0 || !xyz || !tets || !v_adjs || !e_adj6 || !f_adjs || !f_ids)
     return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_set_mesh: empty mesh or null buffer");
   CK(cudaSetDevice(c->device), "cudaSetDevice");
-  // validate ids and compute the box and the largest tet radius on the host
-  double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-  std::vector<float> vf((size_t)n_vert * 3);
-  for (long long i = 0; i < (long long)n_vert * 3; ++i) {
-    if (!std::isfinite(xyz[i])) return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_set_mesh: non-finite vertex");
-    vf[i] = (float)xyz[i];
-    lo[i % 3] = std::min(lo[i % 3], xyz[i]);
-    hi[i % 3] = std::max(hi[i % 3], xyz[i]);
-  }
-  std::vector<double> rad((size_t)n_tet);
-  double rmax = 0.0;
-  for (long long t = 0; t < n_tet; ++t) {
-    double cen[3] = {0, 0, 0};
-    for (int q = 0; q < 4; ++q) {
-      int v = tets[4 * t + q];
-      if (v < 0 || v >= n_vert) return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_set_mesh: vertex id out of range");
-      for (int a = 0; a < 3; ++a) cen[a] += 0.25 * xyz[3 * (long long)v + a];
-    }
-    double r = 0.0;
-    for (int q = 0; q < 4; ++q) {
-      int v = tets[4 * t + q];
-      double d2 = 0;
-      for (int a = 0; a < 3; ++a) {
-        double d = xyz[3 * (long long)v + a] - cen[a];
-        d2 += d * d;
-      }
-      r = std::max(r, std::sqrt(d2));
-    }
-    rad[t] = r;
-    rmax = std::max(rmax, r);
-  }
-  // two radius classes: up to the 99.5th percentile radius, and the rest
-  std::vector<uint8_t> cls((size_t)n_tet);
-  int ccount[rpd_ctx::kClasses] = {0};
-  double crad[rpd_ctx::kClasses] = {0};
-  {
-    std::vector<double> tmp(rad);
-    size_t q = std::min(tmp.size() - 1, (size_t)(0.995 * (double)tmp.size()));
-    std::nth_element(tmp.begin(), tmp.begin() + q, tmp.end());
-    double r0 = tmp[q];
-    for (long long t = 0; t < n_tet; ++t) {
-      int k = rad[t] <= r0 ? 0 : 1;
-      cls[t] = (uint8_t)k;
-      ccount[k]++;
-      crad[k] = std::max(crad[k], rad[t]);
-    }
-  }
-  // mesh volume and boundary vertices (vertices of faces with one tet; face
-  // f of a tet is the one opposite its vertex f)
-  double volume = 0.0;
-  std::vector<uint8_t> on_boundary((size_t)n_vert, 0);
-  for (long long t = 0; t < n_tet; ++t) {
-    const double* p0 = xyz + 3 * (long long)tets[4 * t];
-    double e[3][3];
-    for (int q = 1; q < 4; ++q)
-      for (int a = 0; a < 3; ++a) e[q - 1][a] = xyz[3 * (long long)tets[4 * t + q] + a] - p0[a];
-    volume += std::fabs(e[0][0] * (e[1][1] * e[2][2] - e[1][2] * e[2][1]) -
-                        e[0][1] * (e[1][0] * e[2][2] - e[1][2] * e[2][0]) +
-                        e[0][2] * (e[1][0] * e[2][1] - e[1][1] * e[2][0])) / 6.0;
-    for (int f = 0; f < 4; ++f)
-      if (f_adjs[4 * t + f] == 1)
-        for (int q = 0; q < 4; ++q)
-          if (q != f) on_boundary[(size_t)tets[4 * t + q]] = 1;
-  }
-  std::vector<float> bv;
-  for (long long v = 0; v < n_vert; ++v)
-    if (on_boundary[(size_t)v])
-      for (int a = 0; a < 4; ++a) bv.push_back(a < 3 ? vf[3 * v + a] : 0.f);
-  const int n_bv = (int)(bv.size() / 4);
-  CK(c->bverts.ensure((size_t)std::max(n_bv, 1)), "alloc boundary");
+  c->has_mesh = false;
+  c->has_result = false;
+  cudaStream_t st = c->stream;
+  // the raw arrays go to the device; everything derived is computed there
+  CK(c->vert3d.ensure((size_t)n_vert * 3), "alloc vert3d");
   CK(c->vert3f.ensure((size_t)n_vert * 3), "alloc vert3f");
   CK(c->vert2.ensure((size_t)n_vert * 3), "alloc vert2");
-  std::vector<float2> v2((size_t)n_vert * 3);
-  for (size_t i = 0; i < v2.size(); ++i) v2[i] = split_df(xyz[i]);
-  CK(c->vert3d.ensure((size_t)n_vert * 3), "alloc vert3d");
   CK(c->tets.ensure(n_tet), "alloc tets");
   CK(c->v_adjs.ensure(n_vert), "alloc v_adjs");
   CK(c->e_adj6.ensure((size_t)n_tet * 6), "alloc e_adj6");
   CK(c->f_adjs.ensure((size_t)n_tet * 4), "alloc f_adjs");
   CK(c->f_ids.ensure((size_t)n_tet * 4), "alloc f_ids");
   CK(c->tet_class.ensure(n_tet), "alloc classes");
-  cudaStream_t st = c->stream;
-  CK(cudaMemcpyAsync(c->vert3f.ptr, vf.data(), vf.size() * 4, cudaMemcpyHostToDevice, st), "H2D vert");
-  CK(cudaMemcpyAsync(c->vert3d.ptr, xyz, (size_t)n_vert * 24, cudaMemcpyHostToDevice, st), "H2D vert");
-  CK(cudaMemcpyAsync(c->vert2.ptr, v2.data(), v2.size() * sizeof(float2), cudaMemcpyHostToDevice, st), "H2D vert");
+  CK(c->tet_rad.ensure(n_tet), "alloc radii");
+  CK(c->bmark.ensure(n_vert), "alloc marks");
   CK(c->face2.ensure((size_t)n_tet * 16), "alloc faces");
+  CK(c->prep.ensure(1), "alloc");
+  CK(c->prep_hist.ensure(kRadiusBins), "alloc");
+  CK(cudaMemcpyAsync(c->vert3d.ptr, xyz, (size_t)n_vert * 24, cudaMemcpyHostToDevice, st), "H2D vert");
   CK(cudaMemcpyAsync(c->tets.ptr, tets, (size_t)n_tet * 16, cudaMemcpyHostToDevice, st), "H2D tets");
   CK(cudaMemcpyAsync(c->v_adjs.ptr, v_adjs, (size_t)n_vert * 4, cudaMemcpyHostToDevice, st), "H2D v_adjs");
   CK(cudaMemcpyAsync(c->e_adj6.ptr, e_adj6, (size_t)n_tet * 6, cudaMemcpyHostToDevice, st), "H2D e_adj6");
   CK(cudaMemcpyAsync(c->f_adjs.ptr, f_adjs, (size_t)n_tet * 16, cudaMemcpyHostToDevice, st), "H2D f_adjs");
   CK(cudaMemcpyAsync(c->f_ids.ptr, f_ids, (size_t)n_tet * 16, cudaMemcpyHostToDevice, st), "H2D f_ids");
-  CK(cudaMemcpyAsync(c->tet_class.ptr, cls.data(), (size_t)n_tet, cudaMemcpyHostToDevice, st), "H2D classes");
-  if (n_bv > 0)
-    CK(cudaMemcpyAsync(c->bverts.ptr, bv.data(), bv.size() * 4, cudaMemcpyHostToDevice, st), "H2D boundary");
-  CK(launch_tet_face_planes(c->vert3d.ptr, c->tets.ptr, n_tet, c->face2.ptr, st), "face planes");
+  CK(mesh_prep_init(c->prep.ptr, st), "prep");
+  CK(mesh_prep_geometry(c->vert3d.ptr, n_vert, c->tets.ptr, c->f_adjs.ptr, n_tet, c->vert3f.ptr,
+                        c->vert2.ptr, c->tet_rad.ptr, c->bmark.ptr, c->prep.ptr, st), "prep");
+  MeshPrepOut po;
+  CK(cudaMemcpyAsync(&po, c->prep.ptr, sizeof(po), cudaMemcpyDeviceToHost, st), "D2H");
   CK(cudaStreamSynchronize(st), "set_mesh sync");
-  c->n_bverts = n_bv;
-  c->mesh_volume = volume;
-  c->bdist_valid = false;
+  if (po.bad & 1u) return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_set_mesh: non-finite vertex");
+  if (po.bad & 2u) return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_set_mesh: vertex id out of range");
+  const double rmax = key_to_double(po.rmax_key);
+  // two radius classes: up to the 99.5th-percentile radius (upper edge of
+  // its histogram bin), and the rest
+  std::vector<int32_t> hist(kRadiusBins);
+  CK(mesh_prep_histogram(c->tet_rad.ptr, n_tet, rmax, c->prep_hist.ptr, st), "histogram");
+  CK(cudaMemcpyAsync(hist.data(), c->prep_hist.ptr, sizeof(int32_t) * kRadiusBins,
+                     cudaMemcpyDeviceToHost, st), "D2H");
+  CK(cudaStreamSynchronize(st), "set_mesh sync");
+  const long long want = std::min<long long>(n_tet, (long long)std::ceil(0.995 * (double)n_tet));
+  long long acc = 0;
+  int bin = kRadiusBins - 1;
+  for (int b = 0; b < kRadiusBins; ++b) {
+    acc += hist[(size_t)b];
+    if (acc >= want) {
+      bin = b;
+      break;
+    }
+  }
+  const double r0 = rmax * (double)(bin + 1) / (double)kRadiusBins;
+  CK(mesh_prep_classify(c->tet_rad.ptr, n_tet, r0, c->tet_class.ptr, c->prep.ptr, st), "classes");
+  CK(launch_tet_face_planes(c->vert3d.ptr, c->tets.ptr, n_tet, c->face2.ptr, st), "face planes");
+  CK(cudaMemcpyAsync(&po, c->prep.ptr, sizeof(po), cudaMemcpyDeviceToHost, st), "D2H");
+  CK(cudaStreamSynchronize(st), "set_mesh sync");
   for (int k = 0; k < rpd_ctx::kClasses; ++k) {
-    c->class_count[k] = ccount[k];
-    c->class_radius[k] = crad[k];
+    c->class_count[k] = k < 2 ? po.class_count[k] : 0;
+    c->class_radius[k] = k < 2 && po.class_count[k] > 0 ? key_to_double(po.class_rmax_key[k]) : 0.0;
   }
   c->n_vert = n_vert;
   c->n_tet = n_tet;
   for (int a = 0; a < 3; ++a) {
-    c->mesh_lo[a] = lo[a];
-    c->mesh_hi[a] = hi[a];
+    c->mesh_lo[a] = key_to_double(po.lo_key[a]);
+    c->mesh_hi[a] = key_to_double(po.hi_key[a]);
   }
   c->tet_radius = rmax;
+  c->mesh_volume = po.volume;
+  c->n_bverts = -1;  // boundary vertex list built on first use
+  c->bdist_valid = false;
   c->has_mesh = true;
-  c->has_result = false;
   return RPD_OK;
 }
 

@@ -140,6 +140,10 @@ struct rpd_ctx {
 
   // learned list length: features, predictor, training set
   double mesh_volume = 0.0;
+  DevBuf<double> tet_rad;       // FP64 radius of every tet
+  DevBuf<uint8_t> bmark;        // boundary vertex marks
+  DevBuf<MeshPrepOut> prep;
+  DevBuf<int32_t> prep_hist;
   DevBuf<float4> bverts;        // boundary vertices
   int n_bverts = 0;
   DevBuf<float> site_bdist;     // site -> nearest boundary vertex distance

@@ -210,6 +210,34 @@ cudaError_t neighbors_from_reference(const int32_t* ref, int k, int n_site, int3
                                      cudaStream_t st);
 
 // ---------------------------------------------------------------------------
+// mesh preparation on the device (rpd_prep.cu)
+// ---------------------------------------------------------------------------
+constexpr int kRadiusBins = 4096;
+struct MeshPrepOut {
+  unsigned int bad;                    // 1: non-finite vertex, 2: vertex id out of range
+  unsigned long long lo_key[3], hi_key[3];  // bounding box (order-preserving keys)
+  double volume;
+  unsigned long long rmax_key;         // largest tet radius
+  int class_count[2];
+  unsigned long long class_rmax_key[2];
+};
+double key_to_double(unsigned long long k);
+cudaError_t mesh_prep_init(MeshPrepOut* out, cudaStream_t st);
+// float and double-float vertices, box, id check, FP64 tet radii, volume,
+// boundary vertex marks (bmark may be null)
+cudaError_t mesh_prep_geometry(const double* xyz, int n_vert, const int4* tets,
+                               const int32_t* f_adjs, int n_tet, float* vert3f, float2* vert2,
+                               double* rad, uint8_t* bmark, MeshPrepOut* out, cudaStream_t st);
+cudaError_t mesh_prep_histogram(const double* rad, int n_tet, double rmax, int32_t* hist,
+                                cudaStream_t st);
+// class 0: radius <= r0; counts and largest radius per class
+cudaError_t mesh_prep_classify(const double* rad, int n_tet, double r0, uint8_t* cls,
+                               MeshPrepOut* out, cudaStream_t st);
+// marked vertices as float4 (x, y, z, 0), count in *n_bv (device)
+cudaError_t boundary_list(const uint8_t* bmark, const float* vert3f, int n_vert, float4* bverts,
+                          int32_t* n_bv, cudaStream_t st);
+
+// ---------------------------------------------------------------------------
 // learned list length (rpd_mlp.cu)
 // ---------------------------------------------------------------------------
 constexpr int kMlpFeatures = 16;  // 12 features, zero-padded to the mma's k
