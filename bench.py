@@ -72,6 +72,21 @@ def compare_topology(ph_fast, hash_fast, ph_plain, hash_plain):
             "reference_capacity_drops_emitted": int(overflow.sum())}
 
 
+def replica_throughput(local_ms, local_cells, dist=None, device="cpu"):
+    """Whole-job throughput of N replicas: cells of all ranks over the slowest
+    rank's time (max over ranks, as the timing rules ask).  Returns (cells/s,
+    max ms, total cells)."""
+    if dist is None:
+        return local_cells / (local_ms / 1000.0), local_ms, local_cells
+    import torch
+
+    t = torch.tensor([local_ms], dtype=torch.float64, device=device)
+    n = torch.tensor([local_cells], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(n, op=dist.ReduceOp.SUM)
+    return float(n.item()) / (float(t.item()) / 1000.0), float(t.item()), int(n.item())
+
+
 def make_workload(args):
     from libmat_gb300 import workloads as W
 
@@ -327,14 +342,7 @@ def run_ours(args):
     barrier()
     with ClockSampler(local) as clk:
         ms, cells, st = timed(fast, args.steps, args.warmup)
-    total_ms = sum(ms)
-    if dist is not None:
-        import torch
-
-        t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = cells * world / (total_ms / 1000.0)
+    value, total_ms, _ = replica_throughput(sum(ms), cells, dist, "cuda")
     used_learned = bool(fast.config().learned_k)
 
     # ---- validation run of the same configuration with topology hashes
