@@ -971,13 +971,24 @@ __device__ float3 float_vertex(const Cell& c, uchar4 tr) {
 }
 
 // writes xyz[3 * nb_v] and returns the cell volume; c holds the cell's
-// id2 and ver, c.u.g is filled here
-template <class Cell>
-__device__ double cell_geometry(Cell& c, int nb_v, int nb_p, const float2* face2,
+// id2 and ver, c.u.g is filled here.  W lanes (a whole warp or a half) work
+// on the cell; lane is 0..W-1.  Every lane of the warp calls this the same
+// number of times (its __syncwarp and shuffles span the warp); a lane group
+// with no cell passes active = false.
+template <int W, class Cell>
+__device__ double cell_geometry(Cell& c, bool active, int nb_v, int nb_p, const float2* face2,
                                 const float2* site2, int tet, int sid, int lane, double* xyz) {
-  const float2* S2 = site2 + 4 * (long long)sid;
-  const df Sx = ldf(S2), Sy = ldf(S2 + 1), Sz = ldf(S2 + 2), Sw = ldf(S2 + 3);
-  for (int i = lane; i < nb_p; i += 32) {
+  df Sx = df_make(0.f, 0.f), Sy = Sx, Sz = Sx, Sw = Sx;
+  if (active) {
+    const float2* S2 = site2 + 4 * (long long)sid;
+    Sx = ldf(S2);
+    Sy = ldf(S2 + 1);
+    Sz = ldf(S2 + 2);
+    Sw = ldf(S2 + 3);
+  } else {
+    nb_v = nb_p = 0;
+  }
+  for (int i = lane; i < nb_p; i += W) {
     df nx, ny, nz, d;
     if (i < 4) {
       // the tet's face plane (FP64, once per mesh), moved to the seed frame:
@@ -1007,8 +1018,8 @@ __device__ double cell_geometry(Cell& c, int nb_v, int nb_p, const float2* face2
   __syncwarp();
   // volume origin O near the cell (its vertex 0, in float): the
   // decomposition's terms then scale with the cell's own size
-  const float3 O = float_vertex(c, c.ver[0]);
-  for (int i = lane; i < nb_p; i += 32) {
+  const float3 O = active ? float_vertex(c, c.ver[0]) : make_float3(0.f, 0.f, 0.f);
+  for (int i = lane; i < nb_p; i += W) {
     const df n0 = c.u.g.n[i][0], n1 = c.u.g.n[i][1], n2 = c.u.g.n[i][2];
     const df dc = df_add_s(c.u.g.d[i], df_add_s(df_add_s(df_mul(n0, df_make(O.x, 0.f)),
                                                    df_mul(n1, df_make(O.y, 0.f))),
@@ -1017,7 +1028,7 @@ __device__ double cell_geometry(Cell& c, int nb_v, int nb_p, const float2* face2
   }
   __syncwarp();
   float vol = 0.f;
-  for (int v = lane; v < nb_v; v += 32) {
+  for (int v = lane; v < nb_v; v += W) {
     const uchar4 tr = c.ver[v];
     df X, Y, Z;
     cell_vertex(c, tr.x, tr.y, tr.z, X, Y, Z);
@@ -1026,7 +1037,7 @@ __device__ double cell_geometry(Cell& c, int nb_v, int nb_p, const float2* face2
     xyz[3 * v + 2] = df_translate(Sz, Z);
     vol += vertex_volume_about(c, tr, X, Y, Z, O);
   }
-  for (int o = 16; o > 0; o >>= 1) vol += __shfl_xor_sync(0xffffffffu, vol, o);
+  for (int o = W / 2; o > 0; o >>= 1) vol += __shfl_xor_sync(0xffffffffu, vol, o);
   return (double)vol;
 }
 
@@ -1046,10 +1057,10 @@ __device__ __forceinline__ uint64_t face_key(int2 id) {
   return ((uint64_t)(uint32_t)id.x << 32) | (uint32_t)id.y;
 }
 
-template <class Cell>
+template <int W, class Cell>
 __device__ uint64_t cell_topology_hash(const Cell& c, int nb_v, int lane) {
   uint64_t h = 0;
-  for (int v = lane; v < nb_v; v += 32) {
+  for (int v = lane; v < nb_v; v += W) {
     uchar4 t = c.ver[v];
     uint64_t a = face_key(c.id2[t.x]), b = face_key(c.id2[t.y]), d = face_key(c.id2[t.z]), x;
     if (a > b) { x = a; a = b; b = x; }
@@ -1061,7 +1072,7 @@ __device__ uint64_t cell_topology_hash(const Cell& c, int nb_v, int lane) {
     hv = mix64(hv ^ (uint64_t)t.w);
     h += hv;
   }
-  for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(0xffffffffu, h, o);
+  for (int o = W / 2; o > 0; o >>= 1) h += __shfl_xor_sync(0xffffffffu, h, o);
   return h;
 }
 
@@ -1231,39 +1242,64 @@ struct GeomCell {
   uchar4 ver[kMaxT];
 };
 
-__global__ void __launch_bounds__(256) cell_epilogue_kernel(EpilogueParams p) {
-  __shared__ GeomCell cells[8];
+constexpr int kEpiWarps = 4;
+
+// two cells per warp, one per half-warp: most cells have fewer than 16
+// planes and few more vertices, so 16 lanes keep busier than 32
+__global__ void __launch_bounds__(kEpiWarps * 32) cell_epilogue_kernel(EpilogueParams p) {
+  __shared__ GeomCell cells[2 * kEpiWarps];
   const int lane = threadIdx.x & 31;
-  GeomCell& c = cells[threadIdx.x >> 5];
+  const int half = lane >> 4, hl = lane & 15;
+  GeomCell& c = cells[2 * (threadIdx.x >> 5) + half];
   const long long n_warps = ((long long)gridDim.x * blockDim.x) >> 5;
-  for (long long q = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < p.n_pairs;
-       q += n_warps) {
-    const rpd_cell_header hd = p.headers[q];
-    if (hd.status != kSuccess) {
-      if (p.topo_hash && lane == 0) p.topo_hash[q] = 0ull;
-      continue;
+  for (long long base = (((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 2;
+       base < p.n_pairs; base += 2 * n_warps) {
+    const long long q = base + half;
+    rpd_cell_header hd;
+    bool active = false;
+    if (q < p.n_pairs) {
+      hd = p.headers[q];
+      active = hd.status == kSuccess;
+      if (!active && p.topo_hash && hl == 0) p.topo_hash[q] = 0ull;
     }
-    const int nb_v = hd.nb_v, nb_p = hd.nb_p;
-    const PayloadLayout L(nb_v, nb_p, hd.nb_e);
-    uint8_t* rec = p.payload + hd.offset;
-    for (int i = lane; i < nb_p; i += 32) c.id2[i] = reinterpret_cast<const int2*>(rec + L.id2)[i];
-    for (int i = lane; i < nb_v; i += 32) c.ver[i] = reinterpret_cast<const uchar4*>(rec + L.ver)[i];
+    const int nb_v = active ? hd.nb_v : 0, nb_p = active ? hd.nb_p : 0;
+    uint8_t* rec = nullptr;
+    PayloadLayout L(nb_v, nb_p, active ? hd.nb_e : 0);
+    if (active) {
+      rec = p.payload + hd.offset;
+      for (int i = hl; i < nb_p; i += 16) c.id2[i] = reinterpret_cast<const int2*>(rec + L.id2)[i];
+      for (int i = hl; i < nb_v; i += 16) c.ver[i] = reinterpret_cast<const uchar4*>(rec + L.ver)[i];
+    }
     __syncwarp();
-    double* xyz = reinterpret_cast<double*>(rec + L.xyz);
+    double* xyz = active ? reinterpret_cast<double*>(rec + L.xyz) : nullptr;
     double vol = 0.0;
     if (p.geometry) {
-      vol = cell_geometry(c, nb_v, nb_p, p.face2, p.site2, hd.tet_id, hd.site_id, lane, xyz);
-    } else {
-      for (int i = lane; i < 3 * nb_v; i += 32) xyz[i] = 0.0;
+      vol = cell_geometry<16>(c, active, nb_v, nb_p, p.face2, p.site2, active ? hd.tet_id : 0,
+                              active ? hd.site_id : 0, hl, xyz);
+    } else if (active) {
+      for (int i = hl; i < 3 * nb_v; i += 16) xyz[i] = 0.0;
     }
     uint64_t th = 0;
-    if (p.topo_hash) th = cell_topology_hash(c, nb_v, lane);
-    if (lane == 0) {
+    if (p.topo_hash) th = cell_topology_hash<16>(c, nb_v, hl);
+    if (active && hl == 0) {
       p.headers[q].volume = vol;
       if (p.topo_hash) p.topo_hash[q] = th;
     }
     __syncwarp();
   }
+}
+
+cudaError_t launch_cell_epilogue(const EpilogueParams& p, int num_sms, cudaStream_t st) {
+  if (p.n_pairs <= 0) return cudaSuccess;
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cell_epilogue_kernel, kEpiWarps * 32, 0);
+  if (per_sm < 1) per_sm = 1;
+  const long long want = (p.n_pairs + 2 * kEpiWarps - 1) / (2 * kEpiWarps);
+  long long blocks = (long long)num_sms * per_sm * 4;
+  if (blocks > want) blocks = want;
+  cell_epilogue_kernel<<<(unsigned)blocks, kEpiWarps * 32, 0, st>>>(p);
+  note_launches(1);
+  return cudaGetLastError();
 }
 
 // face planes of every tet in FP64 (inward normals as tri2plane,
@@ -1294,19 +1330,6 @@ cudaError_t launch_tet_face_planes(const double* vert3d, const int4* tets, int n
                                    cudaStream_t st) {
   if (n_tet <= 0) return cudaSuccess;
   tet_face_planes_kernel<<<(n_tet + 255) / 256, 256, 0, st>>>(vert3d, tets, n_tet, out);
-  note_launches(1);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_cell_epilogue(const EpilogueParams& p, int num_sms, cudaStream_t st) {
-  if (p.n_pairs <= 0) return cudaSuccess;
-  int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cell_epilogue_kernel, 256, 0);
-  if (per_sm < 1) per_sm = 1;
-  long long want = (p.n_pairs + 7) / 8;
-  long long blocks = (long long)num_sms * per_sm * 4;
-  if (blocks > want) blocks = want;
-  cell_epilogue_kernel<<<(unsigned)blocks, 256, 0, st>>>(p);
   note_launches(1);
   return cudaGetLastError();
 }
