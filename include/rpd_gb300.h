@@ -183,6 +183,20 @@ rpd_status rpd_set_mesh(struct rpd_ctx* ctx, const double* xyz, int n_vert,
                         const uint8_t* e_adj6, const int32_t* f_adjs,
                         const int32_t* f_ids);
 
+/* What rpd_set_mesh derived on the device (for checks and diagnostics):
+ * bounding box, total volume, largest tet radius (largest vertex distance
+ * to the tet's centroid, FP64), and the two radius classes the candidate
+ * search uses -- their tet counts and largest radii. */
+typedef struct rpd_mesh_info {
+  int32_t n_vert, n_tet;
+  double lo[3], hi[3];
+  double volume;
+  double tet_radius;
+  int32_t class_count[2];
+  double class_radius[2];
+} rpd_mesh_info;
+rpd_status rpd_get_mesh_info(const struct rpd_ctx* ctx, rpd_mesh_info* info);
+
 /* Sites: xyzw = n_site x 4 doubles (centre, weight = squared radius);
  * flags: 1 = compute this site's cells (SiteFlag::is_selected,
  * voronoi_common.h:7), 0 = neighbour only.  flags may be NULL (all 1). */

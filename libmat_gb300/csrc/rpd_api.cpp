@@ -250,6 +250,25 @@ rpd_status rpd_get_config(const rpd_ctx* c, rpd_config* cfg) {
   return RPD_OK;
 }
 
+rpd_status rpd_get_mesh_info(const rpd_ctx* c, rpd_mesh_info* info) {
+  if (!c || !info) return RPD_ERR_INVALID_ARGUMENT;
+  if (!c->has_mesh) return RPD_ERR_NOT_READY;
+  *info = rpd_mesh_info{};
+  info->n_vert = c->n_vert;
+  info->n_tet = c->n_tet;
+  for (int a = 0; a < 3; ++a) {
+    info->lo[a] = c->mesh_lo[a];
+    info->hi[a] = c->mesh_hi[a];
+  }
+  info->volume = c->mesh_volume;
+  info->tet_radius = c->tet_radius;
+  for (int k = 0; k < 2; ++k) {
+    info->class_count[k] = c->class_count[k];
+    info->class_radius[k] = c->class_radius[k];
+  }
+  return RPD_OK;
+}
+
 rpd_status rpd_set_config(rpd_ctx* c, const rpd_config* cfg) {
   if (!c || !cfg) return RPD_ERR_INVALID_ARGUMENT;
   if (!config_valid(*cfg)) return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_set_config: invalid configuration");

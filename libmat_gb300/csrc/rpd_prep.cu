@@ -31,15 +31,17 @@ __device__ __forceinline__ unsigned long long dkey(double x) {
 
 constexpr int kPrepBlock = 256;
 
+// block-wide reduction; the result is valid in warp 0.  `identity` fills the
+// slots past the block's warp count (0 for sums, the neutral key for min/max).
 template <class T, class Op>
-__device__ T block_reduce(T v, Op op, T* sh) {
+__device__ T block_reduce(T v, Op op, T* sh, T identity) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int o = 16; o > 0; o >>= 1) v = op(v, __shfl_xor_sync(0xffffffffu, v, o));
   __syncthreads();
   if (lane == 0) sh[wid] = v;
   __syncthreads();
   if (wid == 0) {
-    v = lane < (int)(blockDim.x >> 5) ? sh[lane] : sh[0];
+    v = lane < (int)(blockDim.x >> 5) ? sh[lane] : identity;
     for (int o = 16; o > 0; o >>= 1) v = op(v, __shfl_xor_sync(0xffffffffu, v, o));
   }
   return v;
@@ -67,8 +69,8 @@ __global__ void __launch_bounds__(kPrepBlock) vert_prep_kernel(const double* xyz
   for (int a = 0; a < 3; ++a) {
     const unsigned long long kl = v < n_vert && ok ? dkey(x[a]) : ~0ull;
     const unsigned long long kh = v < n_vert && ok ? dkey(x[a]) : 0ull;
-    const unsigned long long rl = block_reduce(kl, mn, sh);
-    const unsigned long long rh = block_reduce(kh, mx, sh);
+    const unsigned long long rl = block_reduce(kl, mn, sh, ~0ull);
+    const unsigned long long rh = block_reduce(kh, mx, sh, 0ull);
     if (threadIdx.x == 0) {
       atomicMin(&out->lo_key[a], rl);
       atomicMax(&out->hi_key[a], rh);
@@ -123,9 +125,9 @@ __global__ void __launch_bounds__(kPrepBlock) tet_prep_kernel(const double* xyz,
               if (k != f) bmark[id[k]] = 1;
     }
   }
-  const double vs = block_reduce(vol, [](double a, double b) { return a + b; }, shd);
-  const unsigned long long rk =
-      block_reduce(dkey(r), [](unsigned long long a, unsigned long long b) { return a > b ? a : b; }, shk);
+  const double vs = block_reduce(vol, [](double a, double b) { return a + b; }, shd, 0.0);
+  const unsigned long long rk = block_reduce(
+      dkey(r), [](unsigned long long a, unsigned long long b) { return a > b ? a : b; }, shk, 0ull);
   if (threadIdx.x == 0) {
     atomicAdd(&out->volume, vs);
     atomicMax(&out->rmax_key, rk);
@@ -147,14 +149,30 @@ __global__ void radius_hist_kernel(const double* rad, int n_tet, double rmax, in
     if (sh[i]) atomicAdd(&hist[i], sh[i]);
 }
 
-__global__ void classify_kernel(const double* rad, int n_tet, double r0, uint8_t* cls,
-                                MeshPrepOut* out) {
+__global__ void __launch_bounds__(kPrepBlock) classify_kernel(const double* rad, int n_tet,
+                                                              double r0, uint8_t* cls,
+                                                              MeshPrepOut* out) {
+  __shared__ int shc[32];
+  __shared__ unsigned long long shk[32];
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n_tet) return;
-  const int k = rad[t] <= r0 ? 0 : 1;
-  cls[t] = (uint8_t)k;
-  atomicAdd(&out->class_count[k], 1);
-  atomicMax(&out->class_rmax_key[k], dkey(rad[t]));
+  int k = -1;
+  unsigned long long key = 0ull;
+  if (t < n_tet) {
+    k = rad[t] <= r0 ? 0 : 1;
+    cls[t] = (uint8_t)k;
+    key = dkey(rad[t]);
+  }
+  // one atomic per block and class (the classes' counters are contended)
+  for (int cl = 0; cl < 2; ++cl) {
+    const int n = block_reduce(k == cl ? 1 : 0, [](int a, int b) { return a + b; }, shc, 0);
+    const unsigned long long mk = block_reduce(
+        k == cl ? key : 0ull, [](unsigned long long a, unsigned long long b) { return a > b ? a : b; },
+        shk, 0ull);
+    if (threadIdx.x == 0 && n > 0) {
+      atomicAdd(&out->class_count[cl], n);
+      atomicMax(&out->class_rmax_key[cl], mk);
+    }
+  }
 }
 
 // boundary vertices (marked) appended as float4 (x, y, z, 0)
@@ -214,7 +232,8 @@ cudaError_t mesh_prep_histogram(const double* rad, int n_tet, double rmax, int32
 
 cudaError_t mesh_prep_classify(const double* rad, int n_tet, double r0, uint8_t* cls,
                                MeshPrepOut* out, cudaStream_t st) {
-  classify_kernel<<<(n_tet + 255) / 256, 256, 0, st>>>(rad, n_tet, r0, cls, out);
+  classify_kernel<<<(n_tet + kPrepBlock - 1) / kPrepBlock, kPrepBlock, 0, st>>>(rad, n_tet, r0, cls,
+                                                                               out);
   note_launches(1);
   return cudaGetLastError();
 }

@@ -43,7 +43,7 @@ EXPORTS = [
     "rpd_mlp_collect", "rpd_mlp_clear_samples", "rpd_mlp_train", "rpd_mlp_enable",
     "rpd_mlp_get_params", "rpd_mlp_set_params", "rpd_mlp_forward", "rpd_mlp_gradient",
     "rpd_mlp_copy_features", "rpd_mlp_copy_klen", "rpd_mlp_copy_samples", "rpd_set_pair_k",
-    "rpd_get_config", "rpd_set_config",
+    "rpd_get_config", "rpd_set_config", "rpd_get_mesh_info",
     "rpd_batch_create", "rpd_batch_destroy", "rpd_batch_last_error", "rpd_batch_add_mesh",
     "rpd_batch_size", "rpd_batch_set_graph", "rpd_batch_compute", "rpd_batch_autotune",
     "rpd_batch_mesh_cells", "rpd_batch_copy_mesh_cells", "rpd_batch_context",
@@ -61,6 +61,13 @@ class Config(ctypes.Structure):
                 ("certify", ctypes.c_int), ("clip_variant", ctypes.c_int),
                 ("learned_k", ctypes.c_int), ("box_planes", ctypes.c_int),
                 ("topology_hash", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
+
+
+class MeshInfo(ctypes.Structure):
+    _fields_ = [("n_vert", ctypes.c_int32), ("n_tet", ctypes.c_int32),
+                ("lo", ctypes.c_double * 3), ("hi", ctypes.c_double * 3),
+                ("volume", ctypes.c_double), ("tet_radius", ctypes.c_double),
+                ("class_count", ctypes.c_int32 * 2), ("class_radius", ctypes.c_double * 2)]
 
 
 class Stats(ctypes.Structure):
@@ -185,6 +192,8 @@ def load(path=LIB_PATH):
     L.rpd_get_config.argtypes = [vp, c.POINTER(Config)]
     L.rpd_set_config.restype = i32
     L.rpd_set_config.argtypes = [vp, c.POINTER(Config)]
+    L.rpd_get_mesh_info.restype = i32
+    L.rpd_get_mesh_info.argtypes = [vp, c.POINTER(MeshInfo)]
     L.rpd_batch_create.restype = i32
     L.rpd_batch_create.argtypes = [c.POINTER(Config), c.POINTER(vp)]
     L.rpd_batch_destroy.restype = None
@@ -339,6 +348,15 @@ class RPD:
         cfg = Config()
         self._check(self._L.rpd_get_config(self._h, ctypes.byref(cfg)))
         return cfg
+
+    def mesh_info(self):
+        """What set_mesh derived on the device: dict with lo, hi, volume,
+        tet_radius, class_count, class_radius."""
+        m = MeshInfo()
+        self._check(self._L.rpd_get_mesh_info(self._h, ctypes.byref(m)))
+        return dict(n_vert=m.n_vert, n_tet=m.n_tet, lo=list(m.lo), hi=list(m.hi),
+                    volume=m.volume, tet_radius=m.tet_radius,
+                    class_count=list(m.class_count), class_radius=list(m.class_radius))
 
     def set_config(self, cfg):
         """Replaces the whole configuration (a Config from config())."""
