@@ -351,6 +351,13 @@ def run_ours(args):
     fast_ph = fast.pair_headers()
     fast_hash = fast.topology_hashes()
     fast_h, fast_p = fast.cells()
+    # ---- per-cell topology of the emitted cells (what libmat's consumers
+    # rebuild on the host: active planes and edges, face cycles, Euler
+    # numbers), on the device; reported beside the step, not inside it
+    topo_ms = sorted(fast.compute_topology() for _ in range(3))[1]
+    topo_h, topo_rec = fast.topology()
+    topology = {"ms": topo_ms, "cells_per_s": len(topo_h) / (topo_ms / 1000.0),
+                "record_bytes": int(topo_rec.size), "flagged": int((topo_h["flags"] != 0).sum())}
 
     # ---- what the learned lengths do on this (unseen) mesh: clip stage
     # with them, with the certificate tested as each cell is clipped (no
@@ -457,6 +464,7 @@ def run_ours(args):
         "status_counts": {rpd.STATUS_NAMES[i]: int(st.status_counts[i]) for i in range(10)
                           if st.status_counts[i]},
         "e2e": e2e,
+        "topology": topology,
         "gpu_launches": int(st.n_launches) * args.steps,
         "roofline": {"bound": "hbm", "kernel": "clip_cells_kernel", "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,

@@ -271,6 +271,53 @@ rpd_status rpd_set_pair_k(struct rpd_ctx* ctx, const int32_t* k_per_pair, int64_
 rpd_status rpd_copy_topology_hashes_to_host(struct rpd_ctx* ctx, uint64_t* hashes,
                                             int64_t capacity, int64_t* n_pairs);
 
+/* ---- per-cell topology of the emitted cells, on the device --------------
+ * What libmat's consumers rebuild on the host for every ConvexCellHost
+ * (src/rpd3d_base/voronoi_defs.cxx): reload_active (:76-106, active planes
+ * and edges), reload_pc_explicit (:108-188, the vertex cycle of every active
+ * face and the face -> active face map), cal_cell_euler (:190-222) and
+ * cal_halfplane_facet_euler (:224-266, for each active bisector plane's
+ * neighbour).  One header per emitted cell, in rpd_get_cells order; record
+ * at `offset` (16-byte aligned, zero padded):
+ *   float  facet_euler[nb_p]  cal_halfplane_facet_euler(neighbour of plane p)
+ *                             for active bisector planes, 0 otherwise
+ *   uint8  active[nb_p]       active_clipping_planes: vertices on plane p
+ *   int8   lf2active[nb_p]    pc_lf2active_map (-1: inactive)
+ *   uint8  active_e[nb_e]     active_edges (0 / 1)
+ *   uint8  faces[3 nb_v]      pc_local_active_faces, concatenated in active
+ *                             face order; face of plane p has active[p]
+ *                             vertex slots
+ * flags: RPD_TOPO_VERTEX_NULL when a vertex's float coordinates
+ * (compute_vertex_coordinates) are NaN -- the reference then leaves the
+ * faces empty, so faces are 255 and lf2active -1; RPD_TOPO_OPEN_FACE when a
+ * face's cycle does not close (not possible for a valid cell). */
+#define RPD_TOPO_VERTEX_NULL 1
+#define RPD_TOPO_OPEN_FACE 2
+typedef struct rpd_topo_header {
+  uint64_t offset;  /* byte offset of the cell's record */
+  float euler;      /* cal_cell_euler (ConvexCellHost::euler is a float) */
+  uint8_t n_faces;  /* active faces */
+  uint8_t flags;
+  uint8_t pad[2];
+} rpd_topo_header;
+size_t rpd_topo_bytes(int nb_v, int nb_p, int nb_e);
+
+/* Computes the topology of the last rpd_compute's cells (ms may be NULL:
+ * device time of the pass). */
+rpd_status rpd_compute_topology(struct rpd_ctx* ctx, float* ms);
+
+typedef struct rpd_topo_view {
+  int64_t n_cells;
+  const rpd_topo_header* headers; /* device pointer */
+  const uint8_t* records;         /* device pointer */
+  int64_t bytes;
+} rpd_topo_view;
+rpd_status rpd_get_topology(struct rpd_ctx* ctx, rpd_topo_view* view);
+/* NULL buffers: sizes only. */
+rpd_status rpd_copy_topology_to_host(struct rpd_ctx* ctx, rpd_topo_header* headers,
+                                     int64_t max_cells, void* records, int64_t capacity,
+                                     int64_t* n_cells, int64_t* bytes);
+
 /* The neighbour lists used by the last rpd_compute (n_site x k, -1 padded),
  * copied to the host.  k_out receives k. */
 rpd_status rpd_copy_neighbors_to_host(struct rpd_ctx* ctx, int32_t* nbr,

@@ -28,6 +28,7 @@ CUDA_UNITS = {
     "rpd_noalloc.cu": [],
     "rpd_mlp.cu": [],
     "rpd_prep.cu": [],
+    "rpd_topo.cu": ["-fmad=false"],
 }
 CXX_UNITS = ["rpd_api.cpp", "rpd_mesh.cpp", "rpd_batch.cpp"]
 

@@ -161,6 +161,8 @@ size_t rpd_payload_bytes(int nb_v, int nb_p, int nb_e) {
   return PayloadLayout(nb_v, nb_p, nb_e).total;
 }
 
+size_t rpd_topo_bytes(int nb_v, int nb_p, int nb_e) { return TopoLayout(nb_v, nb_p, nb_e).total; }
+
 void rpd_config_default(rpd_config* cfg) {
   if (!cfg) return;
   std::memset(cfg, 0, sizeof(*cfg));
@@ -604,6 +606,7 @@ static rpd_status finish_compute(rpd_ctx* c, bool knn, bool learned, rpd_stats* 
   c->n_cells = n_cells;
   c->tet_k = (int)reinterpret_cast<int32_t*>(host_scratch + 5)[0];
   c->has_result = true;
+  c->has_topology = false;
   if (host_scratch[8 + 10] != 0)
     return fail(c, RPD_ERR_CAPACITY, "rpd_compute: cells lost to a full payload buffer");
   if (stats) {
@@ -966,6 +969,69 @@ rpd_status rpd_set_pair_k(rpd_ctx* c, const int32_t* k_per_pair, int64_t n_pairs
   if (n_pairs > 0)
     CK(cudaMemcpy(c->user_pair_k.ptr, k_per_pair, sizeof(int32_t) * (size_t)n_pairs, cudaMemcpyHostToDevice), "H2D");
   c->n_user_pair_k = n_pairs;
+  return RPD_OK;
+}
+
+// ---- per-cell topology of the emitted cells ------------------------------
+rpd_status rpd_compute_topology(rpd_ctx* c, float* ms) {
+  if (!c) return RPD_ERR_INVALID_ARGUMENT;
+  if (!c->has_result) return fail(c, RPD_ERR_NOT_READY, "rpd_compute_topology: no result");
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  cudaStream_t st = c->stream;
+  const long long n = c->n_cells;
+  CK(c->topo_units.ensure((size_t)std::max(n, 1ll)), "alloc");
+  CK(c->topo_off.ensure((size_t)n + 1), "alloc");
+  CK(c->topo_h.ensure((size_t)std::max(n, 1ll)), "alloc");
+  CK(c->scan_tmp.ensure(scan_temp_ints(std::max(n, 1ll))), "alloc");
+  CK(cudaEventRecord(c->ev[kEvTopo0], st), "event");
+  CK(topo_units(c->cells.ptr, n, c->topo_units.ptr, st), "topology sizes");
+  CK(scan_exclusive(c->topo_units.ptr, c->topo_off.ptr, n, c->scan_tmp.ptr, st), "topology scan");
+  int32_t units = 0;
+  CK(cudaMemcpyAsync(&units, c->topo_off.ptr + n, sizeof(units), cudaMemcpyDeviceToHost, st), "D2H");
+  CK(cudaStreamSynchronize(st), "topology sync");
+  const long long bytes = 16ll * units;
+  CK(c->topo_buf.ensure((size_t)std::max(bytes, 16ll)), "alloc");
+  CK(topo_fill(c->cells.ptr, n, c->payload.ptr, c->topo_off.ptr, c->topo_h.ptr, c->topo_buf.ptr,
+               c->num_sms, st), "topology");
+  CK(cudaEventRecord(c->ev[kEvTopo1], st), "event");
+  CK(cudaStreamSynchronize(st), "topology sync");
+  if (ms) CK(cudaEventElapsedTime(ms, c->ev[kEvTopo0], c->ev[kEvTopo1]), "event time");
+  c->topo_bytes = bytes;
+  c->has_topology = true;
+  return RPD_OK;
+}
+
+rpd_status rpd_get_topology(rpd_ctx* c, rpd_topo_view* v) {
+  if (!c || !v) return RPD_ERR_INVALID_ARGUMENT;
+  if (!c->has_result || !c->has_topology)
+    return fail(c, RPD_ERR_NOT_READY, "rpd_get_topology: call rpd_compute_topology first");
+  v->n_cells = c->n_cells;
+  v->headers = c->topo_h.ptr;
+  v->records = c->topo_buf.ptr;
+  v->bytes = c->topo_bytes;
+  return RPD_OK;
+}
+
+rpd_status rpd_copy_topology_to_host(rpd_ctx* c, rpd_topo_header* headers, int64_t max_cells,
+                                     void* records, int64_t capacity, int64_t* n_cells,
+                                     int64_t* bytes) {
+  if (!c) return RPD_ERR_INVALID_ARGUMENT;
+  if (!c->has_result || !c->has_topology)
+    return fail(c, RPD_ERR_NOT_READY, "rpd_copy_topology_to_host: call rpd_compute_topology first");
+  if (n_cells) *n_cells = c->n_cells;
+  if (bytes) *bytes = c->topo_bytes;
+  if (!headers && !records) return RPD_OK;
+  if ((headers && max_cells < c->n_cells) || (records && capacity < c->topo_bytes))
+    return fail(c, RPD_ERR_CAPACITY, "rpd_copy_topology_to_host: buffers too small");
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  cudaStream_t st = c->stream;
+  if (headers && c->n_cells > 0)
+    CK(cudaMemcpyAsync(headers, c->topo_h.ptr, sizeof(rpd_topo_header) * (size_t)c->n_cells,
+                       cudaMemcpyDeviceToHost, st), "D2H topology");
+  if (records && c->topo_bytes > 0)
+    CK(cudaMemcpyAsync(records, c->topo_buf.ptr, (size_t)c->topo_bytes, cudaMemcpyDeviceToHost, st),
+       "D2H topology");
+  CK(cudaStreamSynchronize(st), "copy sync");
   return RPD_OK;
 }
 

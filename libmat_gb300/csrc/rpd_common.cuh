@@ -54,4 +54,17 @@ struct PayloadLayout {
   }
 };
 
+// per-cell topology record (rpd_topo_header): sections in this order
+struct TopoLayout {
+  uint32_t facet_euler, active, lf2active, active_e, faces, total;
+  __host__ __device__ TopoLayout(int nv, int np, int ne) {
+    facet_euler = 0;
+    active = 4u * np;
+    lf2active = active + np;
+    active_e = lf2active + np;
+    faces = active_e + ne;
+    total = al16(faces + 3u * nv);
+  }
+};
+
 }  // namespace rpd

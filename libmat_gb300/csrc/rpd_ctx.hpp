@@ -63,7 +63,7 @@ struct DevBuf {
 
 enum Ev {
   kEvStart, kEvKnn, kEvPairs, kEvPred0, kEvPred1, kEvClipK0, kEvClipK1, kEvEpi0, kEvClip, kEvEnd,
-  kEvCount
+  kEvTopo0, kEvTopo1, kEvCount
 };
 
 }  // namespace rpd_host
@@ -131,6 +131,12 @@ struct rpd_ctx {
 
   // cells
   DevBuf<rpd_cell_header> pair_headers, cells;
+  // per-cell topology of the emitted cells (rpd_compute_topology)
+  DevBuf<int32_t> topo_units, topo_off;
+  DevBuf<rpd_topo_header> topo_h;
+  DevBuf<uint8_t> topo_buf;
+  long long topo_bytes = 0;
+  bool has_topology = false;
   DevBuf<uint8_t> payload;
   DevBuf<int32_t> flag_tmp, pos_tmp;
   DevBuf<unsigned long long> scratch;  // [0] payload cursor [1] work [2..3] counters

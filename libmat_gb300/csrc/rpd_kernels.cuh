@@ -205,6 +205,13 @@ cudaError_t gather_records(const rpd_cell_header* cells, long long n,
                            int tet_base, int site_base, rpd_cell_header* hout, uint8_t* out,
                            cudaStream_t st);
 
+// per-cell topology (rpd_topo.cu): record sizes in 16-byte units, then the
+// records at the scanned offsets (unit_off, 16-byte units)
+cudaError_t topo_units(const rpd_cell_header* cells, long long n, int32_t* units, cudaStream_t st);
+cudaError_t topo_fill(const rpd_cell_header* cells, long long n, const uint8_t* payload,
+                      const int32_t* unit_off, rpd_topo_header* out_h, uint8_t* out, int num_sms,
+                      cudaStream_t st);
+
 // reference site_knn layout -> row-major lists; validation of ids
 cudaError_t neighbors_from_reference(const int32_t* ref, int k, int n_site, int32_t* nbr,
                                      cudaStream_t st);

@@ -32,6 +32,14 @@ HEADER_DTYPE = np.dtype([
     ("offset", "<u8"), ("volume", "<f8"),
 ])
 
+# rpd_topo_header (per-cell topology, rpd_compute_topology), 16 bytes
+TOPO_DTYPE = np.dtype([
+    ("offset", "<u8"), ("euler", "<f4"), ("n_faces", "u1"), ("flags", "u1"),
+    ("pad", "u1", (2,)),
+])
+TOPO_VERTEX_NULL = 1
+TOPO_OPEN_FACE = 2
+
 # every symbol declared in include/rpd_gb300.h
 EXPORTS = [
     "rpd_status_string", "rpd_config_default", "rpd_payload_bytes", "rpd_create",
@@ -44,6 +52,7 @@ EXPORTS = [
     "rpd_mlp_get_params", "rpd_mlp_set_params", "rpd_mlp_forward", "rpd_mlp_gradient",
     "rpd_mlp_copy_features", "rpd_mlp_copy_klen", "rpd_mlp_copy_samples", "rpd_set_pair_k",
     "rpd_get_config", "rpd_set_config", "rpd_get_mesh_info",
+    "rpd_topo_bytes", "rpd_compute_topology", "rpd_get_topology", "rpd_copy_topology_to_host",
     "rpd_batch_create", "rpd_batch_destroy", "rpd_batch_last_error", "rpd_batch_add_mesh",
     "rpd_batch_size", "rpd_batch_set_graph", "rpd_batch_compute", "rpd_batch_autotune",
     "rpd_batch_mesh_cells", "rpd_batch_copy_mesh_cells", "rpd_batch_context",
@@ -194,6 +203,14 @@ def load(path=LIB_PATH):
     L.rpd_set_config.argtypes = [vp, c.POINTER(Config)]
     L.rpd_get_mesh_info.restype = i32
     L.rpd_get_mesh_info.argtypes = [vp, c.POINTER(MeshInfo)]
+    L.rpd_topo_bytes.restype = c.c_size_t
+    L.rpd_topo_bytes.argtypes = [i32, i32, i32]
+    L.rpd_compute_topology.restype = i32
+    L.rpd_compute_topology.argtypes = [vp, c.POINTER(c.c_float)]
+    L.rpd_get_topology.restype = i32
+    L.rpd_get_topology.argtypes = [vp, vp]
+    L.rpd_copy_topology_to_host.restype = i32
+    L.rpd_copy_topology_to_host.argtypes = [vp, vp, i64, vp, i64, c.POINTER(i64), c.POINTER(i64)]
     L.rpd_batch_create.restype = i32
     L.rpd_batch_create.argtypes = [c.POINTER(Config), c.POINTER(vp)]
     L.rpd_batch_destroy.restype = None
@@ -483,6 +500,27 @@ class RPD:
         self._check(self._L.rpd_copy_cells_to_host(self._h, _p(h), h.shape[0], _p(p), p.nbytes,
                                                    ctypes.byref(n), ctypes.byref(b)))
         return h[:n.value], p[:b.value]
+
+    def compute_topology(self):
+        """Per-cell topology of the emitted cells on the device (active
+        planes and edges, face cycles, Euler numbers); returns its device
+        time in ms."""
+        ms = ctypes.c_float()
+        self._check(self._L.rpd_compute_topology(self._h, ctypes.byref(ms)))
+        return ms.value
+
+    def topology(self):
+        """The per-cell topology copied to the host: (TOPO_DTYPE headers,
+        record bytes), one header per emitted cell in cells() order."""
+        n = ctypes.c_int64()
+        b = ctypes.c_int64()
+        self._check(self._L.rpd_copy_topology_to_host(self._h, None, 0, None, 0,
+                                                      ctypes.byref(n), ctypes.byref(b)))
+        h = np.zeros(max(n.value, 1), TOPO_DTYPE)
+        r = np.zeros(max(b.value, 16), np.uint8)
+        self._check(self._L.rpd_copy_topology_to_host(self._h, _p(h), h.shape[0], _p(r), r.nbytes,
+                                                      ctypes.byref(n), ctypes.byref(b)))
+        return h[:n.value], r[:b.value]
 
     def pair_headers(self):
         """Headers of all candidate pairs (dropped ones included)."""

@@ -7,6 +7,9 @@
   (src/rpd3d/convex_cell.cu) compiled for the CPU through ref_shim/, built
   only when the reference sources are present (they are not on the GPU
   machines; the tests that need it skip there).
+* ``_ref/libreftopo.so`` -- the reference's own per-cell topology
+  (src/rpd3d_base/voronoi_defs.cxx) behind ref_topo_driver.cpp, same
+  condition.
 """
 import os
 import subprocess
@@ -60,6 +63,27 @@ def build_ref(force=False):
     return out
 
 
+def build_ref_topo(force=False):
+    """Returns the path of _ref/libreftopo.so -- the reference's own
+    ConvexCellHost topology (src/rpd3d_base/voronoi_defs.cxx) behind
+    ref_topo_driver.cpp -- or None without reference sources."""
+    defs = os.path.join(REF_ROOT, "src", "rpd3d_base", "voronoi_defs.cxx")
+    if not os.path.exists(defs):
+        return None
+    outdir = os.path.join(HERE, "_ref")
+    os.makedirs(outdir, exist_ok=True)
+    out = os.path.join(outdir, "libreftopo.so")
+    drv = os.path.join(HERE, "ref_topo_driver.cpp")
+    if force or _stale(out, [drv, defs, os.path.join(HERE, "rpd_oracle.h")]):
+        _run(["g++", "-O2", "-fPIC", "-shared", "-std=c++17", "-DNDEBUG",
+              "-ffp-contract=off", "-w", "-pthread",
+              "-I" + os.path.join(REF_ROOT, "include"),
+              "-I" + os.path.join(REF_ROOT, "src", "rpd3d_base"),
+              drv, defs, "-o", out])
+    return out
+
+
 if __name__ == "__main__":
     print(build_oracle(force="-f" in sys.argv))
     print(build_ref(force="-f" in sys.argv))
+    print(build_ref_topo(force="-f" in sys.argv))

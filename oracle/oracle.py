@@ -23,8 +23,16 @@ assert HEADER_DTYPE.itemsize == 32
 
 SUCCESS = 4
 
+# per-cell topology header (orc_topo_header / rpd_topo_header), 16 bytes
+TOPO_DTYPE = np.dtype([
+    ("offset", "<u8"), ("euler", "<f4"), ("n_faces", "u1"), ("flags", "u1"),
+    ("pad", "u1", (2,)),
+])
+assert TOPO_DTYPE.itemsize == 16
+
 _lib = None
 _ref = None
+_reftopo = None
 
 
 def _p(a):
@@ -64,6 +72,10 @@ def lib():
         L.orc_det4x4_exact_sign.argtypes = [vp, vp, vp, vp]
         L.orc_bisector_key.restype = ctypes.c_float
         L.orc_bisector_key.argtypes = [vp, vp]
+        L.orc_topo_bytes.restype = ctypes.c_size_t
+        L.orc_topo_bytes.argtypes = [i32, i32, i32]
+        L.orc_cell_topology.restype = i64
+        L.orc_cell_topology.argtypes = [i64, vp, vp, vp, vp, i64]
         _lib = L
     return _lib
 
@@ -83,6 +95,21 @@ def ref_lib():
                                      i32]
         _ref = L
     return _ref
+
+
+def ref_topo_lib():
+    """The reference's own ConvexCellHost topology on the CPU, or None."""
+    global _reftopo
+    if _reftopo is None:
+        path = _build.build_ref_topo()
+        if path is None:
+            return None
+        L = ctypes.CDLL(path)
+        vp, i32, i64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64
+        L.ref_cell_topology.restype = i64
+        L.ref_cell_topology.argtypes = [i64, vp, vp, vp, vp, i64, i32]
+        _reftopo = L
+    return _reftopo
 
 
 def nthreads():
@@ -243,3 +270,47 @@ def det4x4_bound(p1, p2, p3, e):
 def det4x4_exact_sign(p1, p2, p3, e):
     a = [np.ascontiguousarray(x, np.float32) for x in (p1, p2, p3, e)]
     return int(lib().orc_det4x4_exact_sign(*[_p(x) for x in a]))
+
+
+def _emitted(headers, payload):
+    """The emitted cells (status success) of a pair-header array."""
+    h = np.ascontiguousarray(headers[headers["status"] == SUCCESS])
+    return h, np.ascontiguousarray(payload, np.uint8)
+
+
+def cell_topology(cells, payload):
+    """Per-cell topology of emitted cells (oracle restatement of
+    ConvexCellHost::reload_active / reload_pc_explicit / cal_cell_euler /
+    cal_halfplane_facet_euler).  cells: HEADER_DTYPE records of emitted
+    cells, in output order.  Returns (TOPO_DTYPE headers, record bytes)."""
+    h, payload = _emitted(cells, payload)
+    n = h.shape[0]
+    th = np.zeros(max(n, 1), TOPO_DTYPE)
+    size = int(lib().orc_cell_topology(n, _p(h), _p(payload), _p(th), None, 0))
+    out = np.zeros(max(size, 16), np.uint8)
+    used = lib().orc_cell_topology(n, _p(h), _p(payload), _p(th), _p(out), out.size)
+    if used < 0:
+        raise RuntimeError("oracle topology sizing failed")
+    return th[:n], out[:used]
+
+
+def ref_cell_topology(cells, payload, n_threads=None):
+    """The same computed by the reference's own voronoi_defs.cxx, or None
+    without the reference sources."""
+    L = ref_topo_lib()
+    if L is None:
+        return None
+    h, payload = _emitted(cells, payload)
+    n = h.shape[0]
+    th = np.zeros(max(n, 1), TOPO_DTYPE)
+    size = sum(topo_bytes(c["nb_v"], c["nb_p"], c["nb_e"]) for c in h)
+    out = np.zeros(max(size, 16), np.uint8)
+    used = L.ref_cell_topology(n, _p(h), _p(payload), _p(th), _p(out), out.size,
+                               n_threads or nthreads())
+    if used < 0:
+        raise RuntimeError("reference topology capacity too small")
+    return th[:n], out[:used]
+
+
+def topo_bytes(nb_v, nb_p, nb_e):
+    return int(lib().orc_topo_bytes(int(nb_v), int(nb_p), int(nb_e)))

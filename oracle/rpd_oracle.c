@@ -1034,3 +1034,178 @@ int64_t orc_clip_cells(int n_vert, const float* vert3, const double* vert3d,
   free(loff);
   return off <= payload_capacity ? off : -1;
 }
+
+/* ------------------------------------------------------------------------
+ * Per-cell topology of emitted cells: restates ConvexCellHost's host-side
+ * reconstruction (src/rpd3d_base/voronoi_defs.cxx) on the packed record.
+ * ---------------------------------------------------------------------- */
+size_t orc_topo_bytes(int nb_v, int nb_p, int nb_e) {
+  return al16((size_t)6 * nb_p + (size_t)nb_e + (size_t)3 * nb_v);
+}
+
+/* include/common_cxx.h:128-135 */
+static float orc_cdet2(float a11, float a12, float a21, float a22) {
+  return a11 * a22 - a12 * a21;
+}
+static float orc_cdet3(float a11, float a12, float a13, float a21, float a22,
+                       float a23, float a31, float a32, float a33) {
+  return a11 * orc_cdet2(a22, a23, a32, a33) - a21 * orc_cdet2(a12, a13, a32, a33) +
+         a31 * orc_cdet2(a12, a13, a22, a23);
+}
+
+/* compute_vertex_coordinates with the perspective divide
+ * (voronoi_defs.cxx:33-74): is any coordinate NaN? */
+static int orc_vertex_null(const float* p1, const float* p2, const float* p3) {
+  float x = -orc_cdet3(p1[3], p1[1], p1[2], p2[3], p2[1], p2[2], p3[3], p3[1], p3[2]);
+  float y = -orc_cdet3(p1[0], p1[3], p1[2], p2[0], p2[3], p2[2], p3[0], p3[3], p3[2]);
+  float z = -orc_cdet3(p1[0], p1[1], p1[3], p2[0], p2[1], p2[3], p3[0], p3[1], p3[3]);
+  float w = orc_cdet3(p1[0], p1[1], p1[2], p2[0], p2[1], p2[2], p3[0], p3[1], p3[2]);
+  float px = x / w, py = y / w, pz = z / w;
+  return isnan(px) || isnan(py) || isnan(pz);
+}
+
+static int orc_on_plane(const uint8_t* v, int p) { return v[0] == p || v[1] == p || v[2] == p; }
+
+static void orc_one_topology(const orc_cell_header* h, const uint8_t* rec,
+                             orc_topo_header* th, uint8_t* out) {
+  const int nv = h->nb_v, np = h->nb_p, ne = h->nb_e;
+  const size_t o_id2 = (size_t)16 * np, o_ver = o_id2 + al16((size_t)8 * np),
+               o_edge = o_ver + al16((size_t)4 * nv), o_h = o_edge + al16((size_t)4 * ne);
+  const float* pl = (const float*)rec;
+  const int32_t* id2 = (const int32_t*)(rec + o_id2);
+  const uint8_t* ver = rec + o_ver;
+  const uint8_t* edge = rec + o_edge;
+  const uint8_t* hh = rec + o_h;
+  float* facet = (float*)out;
+  uint8_t* act = out + (size_t)4 * np;
+  int8_t* lf2a = (int8_t*)(act + np);
+  uint8_t* acte = act + (size_t)2 * np;
+  uint8_t* faces = acte + ne;
+  int cnt[ORC_MAX_P];
+  int tab_v[ORC_MAX_T], tab_lp[ORC_MAX_T];
+  memset(out, 0, orc_topo_bytes(nv, np, ne));
+  th->flags = 0;
+  th->pad[0] = th->pad[1] = 0;
+
+  /* reload_active (:76-106): vertices per plane, then edges whose two
+   * planes are active and share at least two vertices */
+  for (int p = 0; p < np; ++p) cnt[p] = 0;
+  for (int t = 0; t < nv; ++t)
+    for (int k = 0; k < 3; ++k)
+      if (ver[4 * t + k] < np) cnt[ver[4 * t + k]]++;
+  for (int e = 0; e < ne; ++e) {
+    const int x = edge[4 * e], y = edge[4 * e + 1];
+    acte[e] = 0;
+    if (x >= np || y >= np || cnt[x] <= 0 || cnt[y] <= 0) continue;
+    int common = 0;
+    for (int t = 0; t < nv; ++t)
+      if (orc_on_plane(ver + 4 * t, x) && orc_on_plane(ver + 4 * t, y)) common++;
+    if (common >= 2) acte[e] = 1;
+  }
+
+  /* reload_pc_explicit (:108-188): a NaN vertex stops it before the faces */
+  int vnull = 0;
+  for (int t = 0; t < nv && !vnull; ++t) {
+    const uint8_t* v = ver + 4 * t;
+    if (v[0] < np && v[1] < np && v[2] < np)
+      vnull = orc_vertex_null(pl + 4 * v[0], pl + 4 * v[1], pl + 4 * v[2]);
+  }
+  int lf = 0, slot = 0;
+  for (int plane = 0; plane < np; ++plane) {
+    act[plane] = (uint8_t)cnt[plane];
+    lf2a[plane] = -1;
+    if (cnt[plane] <= 0) continue;
+    if (!vnull) {
+      int n = 0;
+      for (int t = 0; t < nv; ++t) {
+        const uint8_t* v = ver + 4 * t;
+        if (v[0] == plane) { tab_v[n] = t; tab_lp[n++] = 0; }
+        else if (v[1] == plane) { tab_v[n] = t; tab_lp[n++] = 1; }
+        else if (v[2] == plane) { tab_v[n] = t; tab_lp[n++] = 2; }
+      }
+      /* from the first vertex, the next is the first j whose plane before
+       * `plane` is the plane after it in vertex i */
+      int i = 0, got = 0;
+      while (got < n) {
+        const int ind_i = (tab_lp[i] + 1) % 3;
+        int j = 0;
+        for (; j < n; ++j) {
+          const int ind_j = (tab_lp[j] + 2) % 3;
+          if (ver[4 * tab_v[i] + ind_i] == ver[4 * tab_v[j] + ind_j]) break;
+        }
+        if (j == n) { /* the cycle does not close: the reference reads past
+                         its list here */
+          th->flags |= 2;
+          for (int r = got; r < n; ++r) faces[slot + r] = 255;
+          break;
+        }
+        faces[slot + got++] = (uint8_t)tab_v[i];
+        i = j;
+      }
+      lf2a[plane] = (int8_t)lf;
+      lf++;
+    }
+    slot += cnt[plane];
+  }
+  if (vnull) {
+    memset(faces, 255, (size_t)3 * nv);
+    th->flags |= 1;
+    lf = 0;
+  }
+  th->n_faces = (uint8_t)lf;
+
+  /* cal_cell_euler (:190-222) */
+  double sum_v = 0.0, sum_f = 0.0, sum_e = 0.0;
+  for (int t = 0; t < nv; ++t) {
+    const int v_adj = ver[4 * t + 3];
+    sum_v += 1.f / v_adj;
+  }
+  for (int p = 0; p < np; ++p)
+    if (cnt[p] > 0) sum_f += 1. / (float)hh[p];
+  for (int e = 0; e < ne; ++e)
+    if (acte[e] > 0) sum_e += 1. / edge[4 * e + 2];
+  th->euler = (float)(sum_v - sum_e + sum_f);
+
+  /* cal_halfplane_facet_euler (:224-266) for every active bisector plane:
+   * the face is the first active plane whose id pair holds the neighbour */
+  for (int p = 0; p < np; ++p) {
+    facet[p] = 0.f;
+    if (cnt[p] <= 0 || id2[2 * p + 1] == -1) continue;
+    const int nb = id2[2 * p] == h->site_id ? id2[2 * p + 1] : id2[2 * p];
+    int clip = -1;
+    for (int r = 0; r < np; ++r) {
+      if (cnt[r] <= 0) continue;
+      if (id2[2 * r] == nb || id2[2 * r + 1] == nb) { clip = r; break; }
+    }
+    double sv = 0.0, se = 0.0, sf = 1.0;
+    for (int t = 0; t < nv; ++t) {
+      if (!orc_on_plane(ver + 4 * t, clip)) continue;
+      const int v_adj = ver[4 * t + 3];
+      sv += 1.f / v_adj;
+    }
+    for (int e = 0; e < ne; ++e) {
+      if (edge[4 * e] != clip && edge[4 * e + 1] != clip) continue;
+      if (acte[e] <= 0) continue;
+      se += 1. / edge[4 * e + 2];
+    }
+    facet[p] = (float)(sv - se + sf);
+  }
+}
+
+int64_t orc_cell_topology(int64_t n_cells, const orc_cell_header* cells,
+                          const uint8_t* payload, orc_topo_header* headers,
+                          uint8_t* out, int64_t capacity) {
+  int64_t off = 0;
+  for (int64_t q = 0; q < n_cells; ++q) {
+    if (headers) headers[q].offset = (uint64_t)off;
+    off += (int64_t)orc_topo_bytes(cells[q].nb_v, cells[q].nb_p, cells[q].nb_e);
+  }
+  if (!out || !headers) return off;
+  if (off > capacity) return -1;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 256)
+#endif
+  for (int64_t q = 0; q < n_cells; ++q)
+    orc_one_topology(cells + q, payload + cells[q].offset, headers + q, out + headers[q].offset);
+  return off;
+}

@@ -117,6 +117,29 @@ int64_t orc_clip_cells(int n_vert, const float* vert3, const double* vert3d,
                        uint8_t* payload, int64_t payload_capacity,
                        int64_t* stats, int n_threads);
 
+/* ---- per-cell topology of emitted cells: ConvexCellHost::reload_active
+ * (src/rpd3d_base/voronoi_defs.cxx:76-106), reload_pc_explicit (:108-188),
+ * cal_cell_euler (:190-222) and cal_halfplane_facet_euler (:224-266) for
+ * each active bisector plane's neighbour.  One 16-byte header per cell
+ *   uint64 offset; float euler; uint8 n_faces, flags, pad[2]
+ * and a record at offset:
+ *   float facet_euler[nb_p]; uint8 active[nb_p]; int8 lf2active[nb_p];
+ *   uint8 active_e[nb_e]; uint8 faces[3 nb_v]; zero padding to 16 bytes.
+ * flags: 1 = a vertex's float coordinates are NaN (faces left empty:
+ * 255, lf2active -1, n_faces 0), 2 = a face cycle did not close.
+ * cells/payload: n_cells emitted cells in orc_clip_cells' format.  Returns
+ * the record bytes (offsets follow cell order), or -1 if capacity is too
+ * small (out may be NULL to query the size). */
+typedef struct {
+  uint64_t offset;
+  float euler;
+  uint8_t n_faces, flags, pad[2];
+} orc_topo_header;
+size_t orc_topo_bytes(int nb_v, int nb_p, int nb_e);
+int64_t orc_cell_topology(int64_t n_cells, const orc_cell_header* cells,
+                          const uint8_t* payload, orc_topo_header* headers,
+                          uint8_t* out, int64_t capacity);
+
 /* ---- single predicates, exposed for filter tests */
 double orc_det4x4_ref(const float* p1, const float* p2, const float* p3,
                       const float* e);

@@ -20,6 +20,11 @@ def golden_cases():
     d = os.path.join(ROOT, "tests", "golden")
     out = {}
     for f in sorted(os.listdir(d)):
-        if f.endswith(".npz"):
+        if f.endswith(".npz") and not f.endswith("_topo.npz"):
             out[f[:-4]] = dict(np.load(os.path.join(d, f)))
+    # the reference's per-cell topology of each case's cells
+    for name, case in out.items():
+        t = os.path.join(d, name + "_topo.npz")
+        if os.path.exists(t):
+            case.update(dict(np.load(t)))
     return out
