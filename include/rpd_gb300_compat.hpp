@@ -24,6 +24,19 @@
  * site_cell_vol receives the FP64 volume of each site's cells (the
  * reference zeroes it).  num_itr_global, v2tets, nb_Lloyd_iter and
  * preferred_tet_k are unused, as in the reference.
+ *
+ * Topology: the cells come back with what update_power_cells
+ * (src/rpd3d_base/rpd_update.cxx:568-638) would otherwise rebuild on the
+ * host -- reload_active's active_clipping_planes / active_edges and
+ * reload_pc_explicit's pc_local_active_faces / pc_lf2active_map / pc_points
+ * (src/rpd3d_base/voronoi_defs.cxx:76-188) -- computed on the device by
+ * rpd_compute_topology, with is_active_updated and is_pc_explicit set, so
+ * the consumer skips both.  pc_points are filled by the caller's own
+ * ConvexCellHost::compute_vertex_coordinates.  A cell with a NaN vertex is
+ * left as the reference returns it (the consumer's reload_pc_explicit then
+ * reports it).  euler stays -1, as in the reference's records
+ * (cal_cell_euler computes it on demand).  Define
+ * RPD_GB300_COMPAT_NO_TOPOLOGY to return the cells without topology.
  */
 #ifndef RPD_GB300_COMPAT_HPP
 #define RPD_GB300_COMPAT_HPP
@@ -173,6 +186,47 @@ inline std::vector<ConvexCellHost> compute_clipped_voro_diagram_GPU(
     vol_acc[h.site_id] += h.volume;
   }
   for (int i = 0; i < n_site; ++i) site_cell_vol[i] = (float)vol_acc[i];
+#ifndef RPD_GB300_COMPAT_NO_TOPOLOGY
+  check(rpd_compute_topology(g.c, nullptr), g.c, "rpd_compute_topology");
+  int64_t n_topo = 0, topo_bytes = 0;
+  check(rpd_copy_topology_to_host(g.c, nullptr, 0, nullptr, 0, &n_topo, &topo_bytes), g.c,
+        "topology");
+  std::vector<rpd_topo_header> th((size_t)n_topo + 1);
+  std::vector<uint8_t> trec((size_t)topo_bytes + 16);
+  check(rpd_copy_topology_to_host(g.c, th.data(), n_topo, trec.data(), (int64_t)trec.size(),
+                                  &n_topo, &topo_bytes), g.c, "topology");
+  for (long long q = 0; q < n_cells; ++q) {
+    ConvexCellHost& cc = out[q];
+    const int nv = cc.nb_v, np = cc.nb_p, ne = cc.nb_e;
+    const uint8_t* r = trec.data() + th[q].offset;
+    const uint8_t* act = r + 4 * np;
+    const int8_t* lf2a = reinterpret_cast<const int8_t*>(act + np);
+    const uint8_t* acte = act + 2 * np;
+    const uint8_t* faces = acte + ne;
+    cc.active_clipping_planes.assign((size_t)np + 1, 0);
+    for (int p = 0; p < np; ++p) cc.active_clipping_planes[p] = act[p];
+    cc.active_edges.assign((size_t)ne + 1, 0);
+    for (int e = 0; e < ne; ++e) cc.active_edges[e] = acte[e];
+    cc.is_active_updated = true;
+    if (th[q].flags & RPD_TOPO_VERTEX_NULL) continue;
+    cc.pc_points.clear();
+    for (int i = 0; i < nv; ++i) {
+      const auto v = cc.compute_vertex_coordinates(cmake_uchar3(cc.ver_data_trans[i]));
+      cc.pc_points.push_back(cmake_float3(v.x, v.y, v.z));
+    }
+    cc.pc_local_active_faces.assign(th[q].n_faces, std::vector<int>());
+    cc.pc_lf2active_map.assign((size_t)np, -1);
+    size_t slot = 0;
+    for (int p = 0; p < np; ++p) {
+      if (act[p] == 0) continue;
+      cc.pc_lf2active_map[p] = lf2a[p];
+      std::vector<int>& f = cc.pc_local_active_faces[(size_t)lf2a[p]];
+      for (int k = 0; k < act[p]; ++k) f.push_back(faces[slot + k]);
+      slot += act[p];
+    }
+    cc.is_pc_explicit = true;
+  }
+#endif
   return out;
 }
 

@@ -23,7 +23,7 @@ def compat_exe(tmp_path_factory):
     lib = libbuild.build()
     out = str(tmp_path_factory.mktemp("compat") / "compat_main")
     cuda_inc = os.path.join(libbuild.cuda_home(), "include")
-    subprocess.run(["g++", "-O1", "-std=c++17", os.path.join(ROOT, "tests", "cpp", "compat_main.cpp"),
+    subprocess.run(["g++", "-O1", "-std=c++17", "-ffp-contract=off", os.path.join(ROOT, "tests", "cpp", "compat_main.cpp"),
                     "-I" + os.path.join(ROOT, "include"), "-I" + cuda_inc, "-o", out,
                     lib, "-Wl,-rpath," + os.path.dirname(lib)], check=True)
     return out
@@ -54,6 +54,32 @@ def write_input(path, c):
         site_knn.tofile(f)
 
 
+def topo_sections(rec, th, nv, np_, ne):
+    o = int(th["offset"])
+    return (rec[o:o + 4 * np_].view(np.float32), rec[o + 4 * np_:o + 5 * np_],
+            rec[o + 5 * np_:o + 6 * np_].view(np.int8), rec[o + 6 * np_:o + 6 * np_ + ne],
+            rec[o + 6 * np_ + ne:o + 6 * np_ + ne + 3 * nv])
+
+
+def _det3(a11, a12, a13, a21, a22, a23, a31, a32, a33):
+    # include/common_cxx.h:128-135, one float32 rounding per operation
+    d1 = a22 * a33 - a23 * a32
+    d2 = a12 * a33 - a13 * a32
+    d3 = a12 * a23 - a13 * a22
+    return a11 * d1 - a21 * d2 + a31 * d3
+
+
+def float_vertices(pl, ver):
+    """compute_vertex_coordinates of every vertex (float32, perspective
+    divide), voronoi_defs.cxx:33-74."""
+    a, b, c = (pl[ver[:, i].astype(np.int64)].astype(np.float32) for i in range(3))
+    x = -_det3(a[:, 3], a[:, 1], a[:, 2], b[:, 3], b[:, 1], b[:, 2], c[:, 3], c[:, 1], c[:, 2])
+    y = -_det3(a[:, 0], a[:, 3], a[:, 2], b[:, 0], b[:, 3], b[:, 2], c[:, 0], c[:, 3], c[:, 2])
+    z = -_det3(a[:, 0], a[:, 1], a[:, 3], b[:, 0], b[:, 1], b[:, 3], c[:, 0], c[:, 1], c[:, 3])
+    w = _det3(a[:, 0], a[:, 1], a[:, 2], b[:, 0], b[:, 1], b[:, 2], c[:, 0], c[:, 1], c[:, 2])
+    return np.stack([x / w, y / w, z / w], axis=1).astype(np.float32)
+
+
 @pytest.mark.parametrize("name", ["random_full", "cube_k64", "dups_flags_holes", "lattice_ties"])
 def test_compat_entry_point_returns_reference_cells(golden_cases, compat_exe, tmp_path, name):
     c = golden_cases[name]
@@ -63,6 +89,8 @@ def test_compat_entry_point_returns_reference_cells(golden_cases, compat_exe, tm
     raw = np.fromfile(outp, np.uint8)
     rh = ref_headers(c)
     ok = np.flatnonzero(rh["status"] == SUCCESS)
+    th_ref = c["topo_headers"].reshape(-1).view(O.TOPO_DTYPE)
+    trec_ref = c["topo_records"]
     n = int(raw[:4].view(np.int32)[0])
     assert n == len(ok)
     pos = 4
@@ -90,5 +118,31 @@ def test_compat_entry_point_returns_reference_cells(golden_cases, compat_exe, tm
         pos += 3 * ne
         ref_e = ref[base + s["plane"] + s["id2"] + s["ver"]:][:4 * ne].reshape(-1, 4)[:, :3]
         assert np.array_equal(edges, ref_e)
+        # topology filled by the shim = the reference's own reload_active /
+        # reload_pc_explicit (golden topology of the same cell)
+        upd, expl, nf = [int(x) for x in raw[pos:pos + 12].view(np.int32)]
+        pos += 12
+        assert upd == 1 and expl == 1
+        gh = th_ref[j]
+        facet, gact, glf, gacte, gfaces = topo_sections(trec_ref, gh, nv, np_, ne)
+        assert nf == int(gh["n_faces"])
+        act = raw[pos:pos + 4 * (np_ + 1)].view(np.int32)
+        pos += 4 * (np_ + 1)
+        assert np.array_equal(act[:np_], gact) and act[np_] == 0
+        acte = raw[pos:pos + 4 * (ne + 1)].view(np.int32)
+        pos += 4 * (ne + 1)
+        assert np.array_equal(acte[:ne], gacte) and acte[ne] == 0
+        faces = []
+        for _ in range(nf):
+            m = int(raw[pos:pos + 4].view(np.int32)[0])
+            faces.extend(raw[pos + 4:pos + 4 + 4 * m].view(np.int32).tolist())
+            pos += 4 + 4 * m
+        assert faces == gfaces.tolist()
+        lf = raw[pos:pos + 4 * np_].view(np.int32)
+        pos += 4 * np_
+        assert np.array_equal(lf, glf)
+        pts = raw[pos:pos + 12 * nv].view(np.float32).reshape(-1, 3)
+        pos += 12 * nv
+        assert np.array_equal(pts, float_vertices(planes[:, :4], ver.reshape(-1, 4)))
     vol = raw[pos:].view(np.float32)
     assert vol.shape[0] == c["sites"].shape[0]
