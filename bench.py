@@ -643,6 +643,8 @@ def run_fast_only(args):
     for i in range(args.warmup + args.steps):
         st = r.compute()
         out.append(st.as_dict())
+    if args.topology:
+        out[-1]["ms_topology"] = r.compute_topology()
     r.close()
     print(json.dumps({"workload": name, "last": out[-1]}))
 
@@ -796,6 +798,8 @@ def main():
     ap.add_argument("--miss-target", type=float, default=0.02)
     ap.add_argument("--clip-variant", type=int, default=2,
                     help="--fast-only: clip kernel register budget (2 = the tuned choice)")
+    ap.add_argument("--topology", action="store_true",
+                    help="--fast-only: also run the per-cell topology pass after the last step")
     ap.add_argument("--fast-only", action="store_true",
                     help="only the timed fast path (for profiler launch lists)")
     args = ap.parse_args()

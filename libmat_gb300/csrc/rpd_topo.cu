@@ -31,6 +31,7 @@
 #include <cuda_runtime.h>
 
 #include "rpd_common.cuh"
+#include "rpd_hostfloat.cuh"
 #include "rpd_kernels.cuh"
 
 namespace rpd {
@@ -60,24 +61,6 @@ __device__ __forceinline__ int next_bit(uint32_t m0, uint32_t m1, uint32_t m2, i
     if (m) return 32 * w + __ffs(m) - 1;
   }
   return -1;
-}
-
-// compute_vertex_coordinates (voronoi_defs.cxx:33-74) with the host's cdet3x3
-// (include/common_cxx.h:128-135): NaN after the perspective divide
-__device__ __forceinline__ float cdet2(float a11, float a12, float a21, float a22) {
-  return a11 * a22 - a12 * a21;
-}
-__device__ __forceinline__ float cdet3(float a11, float a12, float a13, float a21, float a22,
-                                       float a23, float a31, float a32, float a33) {
-  return a11 * cdet2(a22, a23, a32, a33) - a21 * cdet2(a12, a13, a32, a33) +
-         a31 * cdet2(a12, a13, a22, a23);
-}
-__device__ bool vertex_is_null(float4 p1, float4 p2, float4 p3) {
-  const float x = -cdet3(p1.w, p1.y, p1.z, p2.w, p2.y, p2.z, p3.w, p3.y, p3.z);
-  const float y = -cdet3(p1.x, p1.w, p1.z, p2.x, p2.w, p2.z, p3.x, p3.w, p3.z);
-  const float z = -cdet3(p1.x, p1.y, p1.w, p2.x, p2.y, p2.w, p3.x, p3.y, p3.w);
-  const float w = cdet3(p1.x, p1.y, p1.z, p2.x, p2.y, p2.z, p3.x, p3.y, p3.z);
-  return isnan(x / w) || isnan(y / w) || isnan(z / w);
 }
 
 __global__ void topo_units_kernel(const rpd_cell_header* cells, long long n, int32_t* units) {
@@ -117,7 +100,7 @@ __global__ void __launch_bounds__(kTopoWarps * 32)
       if (tr.y < np) atomicOr(&c.vm[tr.y][t >> 5], bit);
       if (tr.z < np) atomicOr(&c.vm[tr.z][t >> 5], bit);
       if (tr.x < np && tr.y < np && tr.z < np)
-        null_mine |= vertex_is_null(pl[tr.x], pl[tr.y], pl[tr.z]);
+        null_mine |= is_null_vertex(host_float_vertex(pl[tr.x], pl[tr.y], pl[tr.z]));
     }
     const bool vnull = __any_sync(full, null_mine);
     __syncwarp();
