@@ -318,6 +318,38 @@ rpd_status rpd_copy_topology_to_host(struct rpd_ctx* ctx, rpd_topo_header* heade
                                      int64_t max_cells, void* records, int64_t capacity,
                                      int64_t* n_cells, int64_t* bytes);
 
+/* ---- polygon soup of the emitted cells, on the device ------------------
+ * libmat's Houdini export, get_one_convex_cell_faces_const
+ * (src/IO/IO_CUDA/io_cuda.cxx:21-141) over every emitted cell in
+ * rpd_get_cells order: the cell's vertices (float, by
+ * ConvexCellHost::compute_vertex_coordinates) are appended to one point
+ * list -- a NaN vertex ends the cell (the points before it stay, no faces);
+ * every active face becomes one polygon over its vertex cycle (point ids
+ * global), or with triangulate the fan (c0, cp, cp+1); boundary_only keeps
+ * bisector faces and tet faces whose face id is below max_sf_fid.  Each
+ * polygon carries its cell's site and the site across the face (-1 for a
+ * tet face).  Computes the per-cell topology first when needed. */
+rpd_status rpd_compute_polygons(struct rpd_ctx* ctx, int triangulate, int boundary_only,
+                                int max_sf_fid, float* ms);
+
+typedef struct rpd_polygon_view {
+  int64_t n_points;
+  const float* points;          /* device, n_points x 3 */
+  int64_t n_polys;
+  const int64_t* poly_offsets;  /* device, n_polys + 1 offsets into indices */
+  int64_t n_indices;
+  const uint32_t* indices;      /* device, point ids */
+  const int32_t* poly_site;     /* device, n_polys */
+  const int32_t* poly_adj_site; /* device, n_polys */
+} rpd_polygon_view;
+rpd_status rpd_get_polygons(struct rpd_ctx* ctx, rpd_polygon_view* view);
+/* NULL buffers: sizes only.  points: 3 floats per point; offsets: n_polys + 1. */
+rpd_status rpd_copy_polygons_to_host(struct rpd_ctx* ctx, float* points, int64_t max_points,
+                                     int64_t* poly_offsets, uint32_t* indices,
+                                     int64_t max_indices, int32_t* poly_site,
+                                     int32_t* poly_adj_site, int64_t max_polys,
+                                     int64_t* n_points, int64_t* n_polys, int64_t* n_indices);
+
 /* The neighbour lists used by the last rpd_compute (n_site x k, -1 padded),
  * copied to the host.  k_out receives k. */
 rpd_status rpd_copy_neighbors_to_host(struct rpd_ctx* ctx, int32_t* nbr,

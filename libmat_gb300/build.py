@@ -29,6 +29,7 @@ CUDA_UNITS = {
     "rpd_mlp.cu": [],
     "rpd_prep.cu": [],
     "rpd_topo.cu": ["-fmad=false"],
+    "rpd_poly.cu": ["-fmad=false"],
 }
 CXX_UNITS = ["rpd_api.cpp", "rpd_mesh.cpp", "rpd_batch.cpp"]
 

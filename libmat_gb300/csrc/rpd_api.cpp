@@ -607,6 +607,7 @@ static rpd_status finish_compute(rpd_ctx* c, bool knn, bool learned, rpd_stats* 
   c->tet_k = (int)reinterpret_cast<int32_t*>(host_scratch + 5)[0];
   c->has_result = true;
   c->has_topology = false;
+  c->has_polygons = false;
   if (host_scratch[8 + 10] != 0)
     return fail(c, RPD_ERR_CAPACITY, "rpd_compute: cells lost to a full payload buffer");
   if (stats) {
@@ -1031,6 +1032,116 @@ rpd_status rpd_copy_topology_to_host(rpd_ctx* c, rpd_topo_header* headers, int64
   if (records && c->topo_bytes > 0)
     CK(cudaMemcpyAsync(records, c->topo_buf.ptr, (size_t)c->topo_bytes, cudaMemcpyDeviceToHost, st),
        "D2H topology");
+  CK(cudaStreamSynchronize(st), "copy sync");
+  return RPD_OK;
+}
+
+// ---- polygon soup of the emitted cells ----------------------------------
+rpd_status rpd_compute_polygons(rpd_ctx* c, int triangulate, int boundary_only, int max_sf_fid,
+                                float* ms) {
+  if (!c) return RPD_ERR_INVALID_ARGUMENT;
+  if (!c->has_result) return fail(c, RPD_ERR_NOT_READY, "rpd_compute_polygons: no result");
+  if (!c->has_topology) {
+    const rpd_status s = rpd_compute_topology(c, nullptr);
+    if (s != RPD_OK) return s;
+  }
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  cudaStream_t st = c->stream;
+  const long long n = c->n_cells;
+  CK(c->poly_cnt.ensure((size_t)std::max(3 * n, 3ll)), "alloc");
+  CK(c->poly_off.ensure((size_t)(3 * (n + 1))), "alloc");
+  CK(c->poly_scan_tmp.ensure(scan64_temp(std::max(n, 1ll))), "alloc");
+  PolyParams p;
+  p.cells = c->cells.ptr;
+  p.n = n;
+  p.payload = c->payload.ptr;
+  p.topo_h = c->topo_h.ptr;
+  p.topo = c->topo_buf.ptr;
+  p.triangulate = triangulate != 0;
+  p.boundary_only = boundary_only != 0;
+  p.max_sf_fid = max_sf_fid;
+  p.cnt_points = c->poly_cnt.ptr;
+  p.cnt_polys = c->poly_cnt.ptr + n;
+  p.cnt_indices = c->poly_cnt.ptr + 2 * n;
+  long long* off = c->poly_off.ptr;
+  p.off_points = off;
+  p.off_polys = off + (n + 1);
+  p.off_indices = off + 2 * (n + 1);
+  CK(cudaEventRecord(c->ev[kEvTopo0], st), "event");
+  CK(poly_count(p, st), "polygon counts");
+  for (int k = 0; k < 3; ++k)
+    CK(scan64_exclusive(c->poly_cnt.ptr + k * n, off + k * (n + 1), n, c->poly_scan_tmp.ptr, st),
+       "polygon scan");
+  long long tot[3];
+  for (int k = 0; k < 3; ++k)
+    CK(cudaMemcpyAsync(&tot[k], off + k * (n + 1) + n, sizeof(long long), cudaMemcpyDeviceToHost,
+                       st), "D2H");
+  CK(cudaStreamSynchronize(st), "polygon sync");
+  if (tot[0] > 0xffffffffll)
+    return fail(c, RPD_ERR_CAPACITY, "rpd_compute_polygons: more than 2^32 points");
+  CK(c->poly_points.ensure((size_t)std::max(3 * tot[0], 3ll)), "alloc");
+  CK(c->poly_offsets.ensure((size_t)tot[1] + 1), "alloc");
+  CK(c->poly_indices.ensure((size_t)std::max(tot[2], 1ll)), "alloc");
+  CK(c->poly_site.ensure((size_t)std::max(tot[1], 1ll)), "alloc");
+  CK(c->poly_adj.ensure((size_t)std::max(tot[1], 1ll)), "alloc");
+  p.points = c->poly_points.ptr;
+  p.poly_offsets = c->poly_offsets.ptr;
+  p.indices = c->poly_indices.ptr;
+  p.poly_site = c->poly_site.ptr;
+  p.poly_adj_site = c->poly_adj.ptr;
+  CK(poly_fill(p, st), "polygons");
+  CK(cudaMemcpyAsync(c->poly_offsets.ptr + tot[1], off + 2 * (n + 1) + n, sizeof(long long),
+                     cudaMemcpyDeviceToDevice, st), "polygon end");
+  CK(cudaEventRecord(c->ev[kEvTopo1], st), "event");
+  CK(cudaStreamSynchronize(st), "polygon sync");
+  if (ms) CK(cudaEventElapsedTime(ms, c->ev[kEvTopo0], c->ev[kEvTopo1]), "event time");
+  c->n_poly_points = tot[0];
+  c->n_polys = tot[1];
+  c->n_poly_indices = tot[2];
+  c->has_polygons = true;
+  return RPD_OK;
+}
+
+rpd_status rpd_get_polygons(rpd_ctx* c, rpd_polygon_view* v) {
+  if (!c || !v) return RPD_ERR_INVALID_ARGUMENT;
+  if (!c->has_result || !c->has_polygons)
+    return fail(c, RPD_ERR_NOT_READY, "rpd_get_polygons: call rpd_compute_polygons first");
+  v->n_points = c->n_poly_points;
+  v->points = c->poly_points.ptr;
+  v->n_polys = c->n_polys;
+  v->poly_offsets = reinterpret_cast<const int64_t*>(c->poly_offsets.ptr);
+  v->n_indices = c->n_poly_indices;
+  v->indices = c->poly_indices.ptr;
+  v->poly_site = c->poly_site.ptr;
+  v->poly_adj_site = c->poly_adj.ptr;
+  return RPD_OK;
+}
+
+rpd_status rpd_copy_polygons_to_host(rpd_ctx* c, float* points, int64_t max_points,
+                                     int64_t* poly_offsets, uint32_t* indices, int64_t max_indices,
+                                     int32_t* poly_site, int32_t* poly_adj_site, int64_t max_polys,
+                                     int64_t* n_points, int64_t* n_polys, int64_t* n_indices) {
+  if (!c) return RPD_ERR_INVALID_ARGUMENT;
+  if (!c->has_result || !c->has_polygons)
+    return fail(c, RPD_ERR_NOT_READY, "rpd_copy_polygons_to_host: call rpd_compute_polygons first");
+  if (n_points) *n_points = c->n_poly_points;
+  if (n_polys) *n_polys = c->n_polys;
+  if (n_indices) *n_indices = c->n_poly_indices;
+  if (!points && !poly_offsets && !indices && !poly_site && !poly_adj_site) return RPD_OK;
+  if ((points && max_points < c->n_poly_points) || (indices && max_indices < c->n_poly_indices) ||
+      ((poly_offsets || poly_site || poly_adj_site) && max_polys < c->n_polys))
+    return fail(c, RPD_ERR_CAPACITY, "rpd_copy_polygons_to_host: buffers too small");
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  cudaStream_t st = c->stream;
+  auto d2h = [&](void* dst, const void* src, size_t bytes) {
+    return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st) : cudaSuccess;
+  };
+  if (points) CK(d2h(points, c->poly_points.ptr, sizeof(float) * 3 * (size_t)c->n_poly_points), "D2H");
+  if (poly_offsets)
+    CK(d2h(poly_offsets, c->poly_offsets.ptr, sizeof(long long) * ((size_t)c->n_polys + 1)), "D2H");
+  if (indices) CK(d2h(indices, c->poly_indices.ptr, sizeof(uint32_t) * (size_t)c->n_poly_indices), "D2H");
+  if (poly_site) CK(d2h(poly_site, c->poly_site.ptr, sizeof(int32_t) * (size_t)c->n_polys), "D2H");
+  if (poly_adj_site) CK(d2h(poly_adj_site, c->poly_adj.ptr, sizeof(int32_t) * (size_t)c->n_polys), "D2H");
   CK(cudaStreamSynchronize(st), "copy sync");
   return RPD_OK;
 }

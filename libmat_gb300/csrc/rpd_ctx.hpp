@@ -137,6 +137,16 @@ struct rpd_ctx {
   DevBuf<uint8_t> topo_buf;
   long long topo_bytes = 0;
   bool has_topology = false;
+  // polygon soup of the emitted cells (rpd_compute_polygons)
+  DevBuf<int32_t> poly_cnt;        // 3 x n_cells: points, polygons, indices per cell
+  DevBuf<long long> poly_off;      // 3 x (n_cells + 1)
+  DevBuf<long long> poly_scan_tmp;
+  DevBuf<float> poly_points;
+  DevBuf<long long> poly_offsets;
+  DevBuf<uint32_t> poly_indices;
+  DevBuf<int32_t> poly_site, poly_adj;
+  long long n_poly_points = 0, n_polys = 0, n_poly_indices = 0;
+  bool has_polygons = false;
   DevBuf<uint8_t> payload;
   DevBuf<int32_t> flag_tmp, pos_tmp;
   DevBuf<unsigned long long> scratch;  // [0] payload cursor [1] work [2..3] counters

@@ -212,6 +212,29 @@ cudaError_t topo_fill(const rpd_cell_header* cells, long long n, const uint8_t* 
                       const int32_t* unit_off, rpd_topo_header* out_h, uint8_t* out, int num_sms,
                       cudaStream_t st);
 
+// polygon soup of the emitted cells (rpd_poly.cu)
+struct PolyParams {
+  const rpd_cell_header* cells;  // emitted cells
+  long long n;
+  const uint8_t* payload;
+  const rpd_topo_header* topo_h;  // their per-cell topology
+  const uint8_t* topo;
+  int triangulate, boundary_only, max_sf_fid;
+  int32_t *cnt_points, *cnt_polys, *cnt_indices;        // per cell
+  const long long *off_points, *off_polys, *off_indices;  // exclusive scans (n + 1)
+  float* points;          // 3 per point
+  long long* poly_offsets;  // into indices (n_polys + 1)
+  uint32_t* indices;
+  int32_t *poly_site, *poly_adj_site;
+};
+cudaError_t poly_count(const PolyParams& p, cudaStream_t st);
+cudaError_t poly_fill(const PolyParams& p, cudaStream_t st);
+// exclusive scan of n int32 counts into n + 1 int64 (out[n] = total); temp:
+// scan64_temp(n) entries
+size_t scan64_temp(long long n);
+cudaError_t scan64_exclusive(const int32_t* in, long long* out, long long n, long long* temp,
+                             cudaStream_t st);
+
 // reference site_knn layout -> row-major lists; validation of ids
 cudaError_t neighbors_from_reference(const int32_t* ref, int k, int n_site, int32_t* nbr,
                                      cudaStream_t st);

@@ -53,6 +53,7 @@ EXPORTS = [
     "rpd_mlp_copy_features", "rpd_mlp_copy_klen", "rpd_mlp_copy_samples", "rpd_set_pair_k",
     "rpd_get_config", "rpd_set_config", "rpd_get_mesh_info",
     "rpd_topo_bytes", "rpd_compute_topology", "rpd_get_topology", "rpd_copy_topology_to_host",
+    "rpd_compute_polygons", "rpd_get_polygons", "rpd_copy_polygons_to_host",
     "rpd_batch_create", "rpd_batch_destroy", "rpd_batch_last_error", "rpd_batch_add_mesh",
     "rpd_batch_size", "rpd_batch_set_graph", "rpd_batch_compute", "rpd_batch_autotune",
     "rpd_batch_mesh_cells", "rpd_batch_copy_mesh_cells", "rpd_batch_context",
@@ -211,6 +212,13 @@ def load(path=LIB_PATH):
     L.rpd_get_topology.argtypes = [vp, vp]
     L.rpd_copy_topology_to_host.restype = i32
     L.rpd_copy_topology_to_host.argtypes = [vp, vp, i64, vp, i64, c.POINTER(i64), c.POINTER(i64)]
+    L.rpd_compute_polygons.restype = i32
+    L.rpd_compute_polygons.argtypes = [vp, i32, i32, i32, c.POINTER(c.c_float)]
+    L.rpd_get_polygons.restype = i32
+    L.rpd_get_polygons.argtypes = [vp, vp]
+    L.rpd_copy_polygons_to_host.restype = i32
+    L.rpd_copy_polygons_to_host.argtypes = [vp, vp, i64, vp, vp, i64, vp, vp, i64,
+                                            c.POINTER(i64), c.POINTER(i64), c.POINTER(i64)]
     L.rpd_batch_create.restype = i32
     L.rpd_batch_create.argtypes = [c.POINTER(Config), c.POINTER(vp)]
     L.rpd_batch_destroy.restype = None
@@ -521,6 +529,33 @@ class RPD:
         self._check(self._L.rpd_copy_topology_to_host(self._h, _p(h), h.shape[0], _p(r), r.nbytes,
                                                       ctypes.byref(n), ctypes.byref(b)))
         return h[:n.value], r[:b.value]
+
+    def compute_polygons(self, triangulate=False, boundary_only=False, max_sf_fid=0):
+        """Polygon soup of the emitted cells on the device (libmat's Houdini
+        export); returns its device time in ms."""
+        ms = ctypes.c_float()
+        self._check(self._L.rpd_compute_polygons(self._h, int(triangulate), int(boundary_only),
+                                                 int(max_sf_fid), ctypes.byref(ms)))
+        return ms.value
+
+    def polygons(self):
+        """The polygon soup copied to the host: dict(points (n, 3) float32,
+        poly_offsets, indices, poly_site, poly_adj_site)."""
+        a, b, d = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        self._check(self._L.rpd_copy_polygons_to_host(self._h, None, 0, None, None, 0, None, None,
+                                                      0, ctypes.byref(a), ctypes.byref(b),
+                                                      ctypes.byref(d)))
+        npt, npoly, nidx = a.value, b.value, d.value
+        pts = np.zeros((max(npt, 1), 3), np.float32)
+        offs = np.zeros(npoly + 1, np.int64)
+        idx = np.zeros(max(nidx, 1), np.uint32)
+        site = np.zeros(max(npoly, 1), np.int32)
+        adj = np.zeros(max(npoly, 1), np.int32)
+        self._check(self._L.rpd_copy_polygons_to_host(
+            self._h, _p(pts), npt, _p(offs), _p(idx), nidx, _p(site), _p(adj), npoly,
+            ctypes.byref(a), ctypes.byref(b), ctypes.byref(d)))
+        return dict(points=pts[:npt], poly_offsets=offs, indices=idx[:nidx],
+                    poly_site=site[:npoly], poly_adj_site=adj[:npoly])
 
     def pair_headers(self):
         """Headers of all candidate pairs (dropped ones included)."""

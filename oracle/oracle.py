@@ -76,6 +76,9 @@ def lib():
         L.orc_topo_bytes.argtypes = [i32, i32, i32]
         L.orc_cell_topology.restype = i64
         L.orc_cell_topology.argtypes = [i64, vp, vp, vp, vp, i64]
+        L.orc_cell_polygons.restype = i32
+        L.orc_cell_polygons.argtypes = [i64, vp, vp, i32, i32, i32, vp, i64, vp, vp, i64,
+                                        vp, vp, i64, vp]
         _lib = L
     return _lib
 
@@ -314,3 +317,26 @@ def ref_cell_topology(cells, payload, n_threads=None):
 
 def topo_bytes(nb_v, nb_p, nb_e):
     return int(lib().orc_topo_bytes(int(nb_v), int(nb_p), int(nb_e)))
+
+
+def cell_polygons(cells, payload, triangulate=False, boundary_only=False, max_sf_fid=0):
+    """Polygon soup of emitted cells (oracle restatement of
+    get_one_convex_cell_faces_const).  Returns dict(points (n, 3) float32,
+    poly_offsets, indices, poly_site, poly_adj_site)."""
+    h, payload = _emitted(cells, payload)
+    n = h.shape[0]
+    counts = np.zeros(3, np.int64)
+    args = (n, _p(h), _p(payload), int(triangulate), int(boundary_only), int(max_sf_fid))
+    if lib().orc_cell_polygons(*args, None, 0, None, None, 0, None, None, 0, _p(counts)) != 0:
+        raise RuntimeError("oracle polygon count failed")
+    npt, npoly, nidx = (int(x) for x in counts)
+    pts = np.zeros((max(npt, 1), 3), np.float32)
+    offs = np.zeros(npoly + 1, np.int64)
+    idx = np.zeros(max(nidx, 1), np.uint32)
+    site = np.zeros(max(npoly, 1), np.int32)
+    adj = np.zeros(max(npoly, 1), np.int32)
+    if lib().orc_cell_polygons(*args, _p(pts), npt, _p(offs), _p(idx), nidx, _p(site), _p(adj),
+                               npoly, _p(counts)) != 0:
+        raise RuntimeError("oracle polygon fill failed")
+    return dict(points=pts[:npt], poly_offsets=offs, indices=idx[:nidx], poly_site=site[:npoly],
+                poly_adj_site=adj[:npoly])

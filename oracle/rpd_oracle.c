@@ -1209,3 +1209,114 @@ int64_t orc_cell_topology(int64_t n_cells, const orc_cell_header* cells,
     orc_one_topology(cells + q, payload + cells[q].offset, headers + q, out + headers[q].offset);
   return off;
 }
+
+/* ------------------------------------------------------------------------
+ * Polygon soup: restates get_one_convex_cell_faces_const
+ * (src/IO/IO_CUDA/io_cuda.cxx:21-141) on the packed records, cell after cell.
+ * ---------------------------------------------------------------------- */
+int orc_cell_polygons(int64_t n_cells, const orc_cell_header* cells,
+                      const uint8_t* payload, int triangulate, int boundary_only,
+                      int max_sf_fid, float* points, int64_t max_points,
+                      int64_t* poly_offsets, uint32_t* indices, int64_t max_indices,
+                      int32_t* poly_site, int32_t* poly_adj_site, int64_t max_polys,
+                      int64_t* counts) {
+  int64_t n_pts = 0, n_poly = 0, n_idx = 0;
+  const int write = points != NULL;
+  int tab_v[ORC_MAX_T], tab_lp[ORC_MAX_T], cyc[ORC_MAX_T];
+  for (int64_t q = 0; q < n_cells; ++q) {
+    const orc_cell_header* h = cells + q;
+    const int nv = h->nb_v, np = h->nb_p, ne = h->nb_e;
+    const uint8_t* rec = payload + h->offset;
+    const size_t o_id2 = (size_t)16 * np, o_ver = o_id2 + al16((size_t)8 * np);
+    const float* pl = (const float*)rec;
+    const int32_t* id2 = (const int32_t*)(rec + o_id2);
+    const uint8_t* ver = rec + o_ver;
+    (void)ne;
+    const int64_t row = n_pts;
+    /* the cell's vertices; a NaN one ends the cell */
+    int null_seen = 0;
+    for (int t = 0; t < nv; ++t) {
+      const float* p1 = pl + 4 * ver[4 * t];
+      const float* p2 = pl + 4 * ver[4 * t + 1];
+      const float* p3 = pl + 4 * ver[4 * t + 2];
+      float x = -orc_cdet3(p1[3], p1[1], p1[2], p2[3], p2[1], p2[2], p3[3], p3[1], p3[2]);
+      float y = -orc_cdet3(p1[0], p1[3], p1[2], p2[0], p2[3], p2[2], p3[0], p3[3], p3[2]);
+      float z = -orc_cdet3(p1[0], p1[1], p1[3], p2[0], p2[1], p2[3], p3[0], p3[1], p3[3]);
+      float w = orc_cdet3(p1[0], p1[1], p1[2], p2[0], p2[1], p2[2], p3[0], p3[1], p3[2]);
+      float px = x / w, py = y / w, pz = z / w;
+      if (isnan(px) || isnan(py) || isnan(pz)) { null_seen = 1; break; }
+      if (write) {
+        if (n_pts >= max_points) return -1;
+        points[3 * n_pts] = px;
+        points[3 * n_pts + 1] = py;
+        points[3 * n_pts + 2] = pz;
+      }
+      n_pts++;
+    }
+    if (null_seen) continue;
+    /* active planes: vertices per plane (reload_active) */
+    int cnt[ORC_MAX_P];
+    for (int p = 0; p < np; ++p) cnt[p] = 0;
+    for (int t = 0; t < nv; ++t)
+      for (int k = 0; k < 3; ++k)
+        if (ver[4 * t + k] < np) cnt[ver[4 * t + k]]++;
+    for (int plane = 0; plane < np; ++plane) {
+      if (cnt[plane] <= 0) continue;
+      const int hx = id2[2 * plane], hy = id2[2 * plane + 1];
+      if (boundary_only && !(hy != -1 || (hy == -1 && hx < max_sf_fid))) continue;
+      int n = 0;
+      for (int t = 0; t < nv; ++t) {
+        const uint8_t* v = ver + 4 * t;
+        if (v[0] == plane) { tab_v[n] = t; tab_lp[n++] = 0; }
+        else if (v[1] == plane) { tab_v[n] = t; tab_lp[n++] = 1; }
+        else if (v[2] == plane) { tab_v[n] = t; tab_lp[n++] = 2; }
+      }
+      int i = 0, got = 0;
+      while (got < n) {
+        const int ind_i = (tab_lp[i] + 1) % 3;
+        int j = 0;
+        for (; j < n; ++j)
+          if (ver[4 * tab_v[i] + ind_i] == ver[4 * tab_v[j] + (tab_lp[j] + 2) % 3]) break;
+        if (j == n) break; /* open cycle: not a valid cell */
+        cyc[got++] = tab_v[i];
+        i = j;
+      }
+      const int adj = hy != -1 ? (hx == h->site_id ? hy : hx) : -1;
+      if (triangulate) {
+        for (int k = 1; k < got - 1; ++k) {
+          if (write) {
+            if (n_poly >= max_polys || n_idx + 3 > max_indices) return -1;
+            poly_offsets[n_poly] = n_idx;
+            indices[n_idx] = (uint32_t)(row + cyc[0]);
+            indices[n_idx + 1] = (uint32_t)(row + cyc[k]);
+            indices[n_idx + 2] = (uint32_t)(row + cyc[(k + 1) % got]);
+            poly_site[n_poly] = h->site_id;
+            poly_adj_site[n_poly] = adj;
+          }
+          n_poly++;
+          n_idx += 3;
+        }
+      } else {
+        if (write) {
+          if (n_poly >= max_polys || n_idx + got > max_indices) return -1;
+          poly_offsets[n_poly] = n_idx;
+          for (int k = 0; k < got; ++k) indices[n_idx + k] = (uint32_t)(row + cyc[k]);
+          poly_site[n_poly] = h->site_id;
+          poly_adj_site[n_poly] = adj;
+        }
+        n_poly++;
+        n_idx += got;
+      }
+    }
+  }
+  if (write) {
+    if (n_poly + 1 > max_polys + 1) return -1;
+    poly_offsets[n_poly] = n_idx;
+  }
+  if (counts) {
+    counts[0] = n_pts;
+    counts[1] = n_poly;
+    counts[2] = n_idx;
+  }
+  return 0;
+}

@@ -140,6 +140,20 @@ int64_t orc_cell_topology(int64_t n_cells, const orc_cell_header* cells,
                           const uint8_t* payload, orc_topo_header* headers,
                           uint8_t* out, int64_t capacity);
 
+/* ---- polygon soup of emitted cells: get_one_convex_cell_faces_const
+ * (src/IO/IO_CUDA/io_cuda.cxx:21-141) over the cells in order.  points:
+ * 3 floats per point (compute_vertex_coordinates); a NaN vertex ends its
+ * cell (earlier points stay, no faces).  poly_offsets[n_polys + 1] into
+ * indices (global point ids); poly_site / poly_adj_site per polygon.
+ * counts[3] receives (points, polygons, indices); with NULL outputs only the
+ * counts are computed.  Returns 0, or -1 when a capacity is too small. */
+int orc_cell_polygons(int64_t n_cells, const orc_cell_header* cells,
+                      const uint8_t* payload, int triangulate, int boundary_only,
+                      int max_sf_fid, float* points, int64_t max_points,
+                      int64_t* poly_offsets, uint32_t* indices, int64_t max_indices,
+                      int32_t* poly_site, int32_t* poly_adj_site, int64_t max_polys,
+                      int64_t* counts);
+
 /* ---- single predicates, exposed for filter tests */
 double orc_det4x4_ref(const float* p1, const float* p2, const float* p3,
                       const float* e);

@@ -86,3 +86,32 @@ def topology_hash(payload, off, nb_v, nb_p, nb_e):
         hv = mix64(hv ^ int(t[3]))
         h = (h + hv) & M64
     return h
+
+
+def _det3(a11, a12, a13, a21, a22, a23, a31, a32, a33):
+    # include/common_cxx.h:128-135, one float32 rounding per operation
+    d1 = a22 * a33 - a23 * a32
+    d2 = a12 * a33 - a13 * a32
+    d3 = a12 * a23 - a13 * a22
+    return a11 * d1 - a21 * d2 + a31 * d3
+
+
+def float_vertices(pl, ver):
+    """compute_vertex_coordinates of every vertex (float32, perspective
+    divide), voronoi_defs.cxx:33-74.  pl: (n_p, 4) float32 planes; ver:
+    (n_v, 4) uint8 dual triangles."""
+    a, b, c = (pl[ver[:, i].astype(np.int64)].astype(np.float32) for i in range(3))
+    x = -_det3(a[:, 3], a[:, 1], a[:, 2], b[:, 3], b[:, 1], b[:, 2], c[:, 3], c[:, 1], c[:, 2])
+    y = -_det3(a[:, 0], a[:, 3], a[:, 2], b[:, 0], b[:, 3], b[:, 2], c[:, 0], c[:, 3], c[:, 2])
+    z = -_det3(a[:, 0], a[:, 1], a[:, 3], b[:, 0], b[:, 1], b[:, 3], c[:, 0], c[:, 1], c[:, 3])
+    w = _det3(a[:, 0], a[:, 1], a[:, 2], b[:, 0], b[:, 1], b[:, 2], c[:, 0], c[:, 1], c[:, 2])
+    return np.stack([x / w, y / w, z / w], axis=1).astype(np.float32)
+
+
+def cell_planes_ver(payload, off, nb_v, nb_p):
+    """(planes (n_p, 4) float32, ver (n_v, 4) uint8) of one packed cell."""
+    s = section_sizes(int(nb_v), int(nb_p), 0)
+    o = int(off)
+    pl = payload[o:o + 16 * int(nb_p)].view(np.float32).reshape(-1, 4)
+    ver = payload[o + s["plane"] + s["id2"]:][:4 * int(nb_v)].reshape(-1, 4)
+    return pl, ver

@@ -11,7 +11,7 @@ import pytest
 
 from oracle import oracle as O
 from tests.conftest import ROOT
-from tests.helpers import SUCCESS, ref_headers, section_sizes
+from tests.helpers import SUCCESS, float_vertices, ref_headers, section_sizes
 
 pytestmark = pytest.mark.gpu
 
@@ -59,25 +59,6 @@ def topo_sections(rec, th, nv, np_, ne):
     return (rec[o:o + 4 * np_].view(np.float32), rec[o + 4 * np_:o + 5 * np_],
             rec[o + 5 * np_:o + 6 * np_].view(np.int8), rec[o + 6 * np_:o + 6 * np_ + ne],
             rec[o + 6 * np_ + ne:o + 6 * np_ + ne + 3 * nv])
-
-
-def _det3(a11, a12, a13, a21, a22, a23, a31, a32, a33):
-    # include/common_cxx.h:128-135, one float32 rounding per operation
-    d1 = a22 * a33 - a23 * a32
-    d2 = a12 * a33 - a13 * a32
-    d3 = a12 * a23 - a13 * a22
-    return a11 * d1 - a21 * d2 + a31 * d3
-
-
-def float_vertices(pl, ver):
-    """compute_vertex_coordinates of every vertex (float32, perspective
-    divide), voronoi_defs.cxx:33-74."""
-    a, b, c = (pl[ver[:, i].astype(np.int64)].astype(np.float32) for i in range(3))
-    x = -_det3(a[:, 3], a[:, 1], a[:, 2], b[:, 3], b[:, 1], b[:, 2], c[:, 3], c[:, 1], c[:, 2])
-    y = -_det3(a[:, 0], a[:, 3], a[:, 2], b[:, 0], b[:, 3], b[:, 2], c[:, 0], c[:, 3], c[:, 2])
-    z = -_det3(a[:, 0], a[:, 1], a[:, 3], b[:, 0], b[:, 1], b[:, 3], c[:, 0], c[:, 1], c[:, 3])
-    w = _det3(a[:, 0], a[:, 1], a[:, 2], b[:, 0], b[:, 1], b[:, 2], c[:, 0], c[:, 1], c[:, 2])
-    return np.stack([x / w, y / w, z / w], axis=1).astype(np.float32)
 
 
 @pytest.mark.parametrize("name", ["random_full", "cube_k64", "dups_flags_holes", "lattice_ties"])
