@@ -94,7 +94,7 @@ typedef struct rpd_config {
                             clipped again with the whole list */
   int box_planes;        /* RPD_NEIGH_KNN: nearest bisectors bounding each
                             site's candidate region for the tets of common
-                            size (0 = default 32; the few largest tets use
+                            size (0 = default 44; the few largest tets use
                             at most 12) */
   int topology_hash;     /* 1 (default): canonical topology hash of every
                             cell (rpd_copy_topology_hashes_to_host) */

@@ -706,7 +706,7 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
     // the nearest bisectors bound each cell; with a GPU-built list the
     // distance-ordered copy gives them first, a user list is used whole
     const int32_t* box_list = knn ? c->nbr_dist.ptr : c->nbr.ptr;
-    const int box0 = c->cfg.box_planes > 0 ? c->cfg.box_planes : 32;
+    const int box0 = c->cfg.box_planes > 0 ? c->cfg.box_planes : kDefaultBoxPlanes;
     CK(c->site_box.ensure((size_t)n_site * 2), "alloc");
     CK(c->site_planes.ensure((size_t)n_site * kBoxPlanes), "alloc");
     CK(c->site_nplanes.ensure((size_t)n_site), "alloc");

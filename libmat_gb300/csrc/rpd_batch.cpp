@@ -228,7 +228,7 @@ rpd_status front_end(rpd_batch* b) {
       ext = std::max(ext, m.mesh_hi[a] - m.mesh_lo[a]);
     }
     const double margin = 1e-4 * ext + 1e-6 * cs;
-    const int box0 = c->cfg.box_planes > 0 ? c->cfg.box_planes : 32;
+    const int box0 = c->cfg.box_planes > 0 ? c->cfg.box_planes : kDefaultBoxPlanes;
     for (int cl = 0; cl < 2; ++cl) {
       if (m.class_count[cl] == 0) continue;
       const Grid& tg = m.tet_grid[cl];

@@ -1462,13 +1462,13 @@ __global__ void __launch_bounds__(128, 6) site_box_kernel(BoxParams p) {
       uint32_t lo = __reduce_or_sync(0xffffffffu, (uint32_t)m);
       uint32_t hi = __reduce_or_sync(0xffffffffu, (uint32_t)(m >> 32));
       unsigned long long act = ((unsigned long long)hi << 32) | lo;
-      npl = __popcll(act);
-      if (npl <= kBoxPlanes) {
-        for (int q = lane; q < s.nb_p; q += 32)
-          if ((act >> q) & 1ull)
-            p.site_planes[(long long)i * kBoxPlanes + __popcll(act & ((1ull << q) - 1ull))] = c.pl[q];
-      } else {
-        npl = 0;
+      // any subset of them bounds a superset of the grown cell: beyond the
+      // storage, the first kBoxPlanes are kept
+      npl = min(__popcll(act), kBoxPlanes);
+      for (int q = lane; q < s.nb_p; q += 32) {
+        const int rank = __popcll(act & ((1ull << q) - 1ull));
+        if (((act >> q) & 1ull) && rank < kBoxPlanes)
+          p.site_planes[(long long)i * kBoxPlanes + rank] = c.pl[q];
       }
     }
     if (lane == 0) p.site_nplanes[i] = npl;

@@ -97,6 +97,11 @@ struct BoxParams {
 };
 
 constexpr int kBoxPlanes = 48;
+// nearest bisectors that bound each site's candidate region for the tets of
+// common size (rpd_config.box_planes = 0); measured on the 1M-tet ellipsoid:
+// 32 -> 9.07 ms, 40 -> 8.72, 44 -> 8.60, 48 -> 8.65, 56 -> 9.29 ms for the
+// pair search
+constexpr int kDefaultBoxPlanes = 44;
 
 size_t clip_smem_per_warp();
 int clip_blocks_per_sm(int pred_mode, int warps);
