@@ -318,6 +318,23 @@ rpd_status rpd_copy_topology_to_host(struct rpd_ctx* ctx, rpd_topo_header* heade
                                      int64_t max_cells, void* records, int64_t capacity,
                                      int64_t* n_cells, int64_t* bytes);
 
+/* ---- distance to local medial primitives --------------------------------
+ * libmat's dist2mat (ClosestDistanceToLocalMat / compute_closest_dist2mat,
+ * src/dist2mat/dist2mat.cu:195-310): for every sample point (xyz), the
+ * smallest signed distance |p - c| - r to the spheres of its primitives
+ * (prims[offsets[s] .. offsets[s] + counts[s]), each three sphere ids:
+ * (-1, -1, s) a sphere, (-1, a, b) a cone, (a, b, c) a slab; spheres are
+ * (x, y, z, r)) and the index of the closest primitive in its list (the
+ * reference's choice among equal minima; -1 for an empty list, whose
+ * distance is 1e16).  on_device = 1: every pointer is device memory and the
+ * call runs on the context's stream (spheres 16-byte aligned); 0: host
+ * memory, copied in and out.  Out-of-range sphere ids or lists are
+ * reported (RPD_ERR_INVALID_ARGUMENT) before any distance is computed. */
+rpd_status rpd_dist2mat(struct rpd_ctx* ctx, const float* spheres, int n_spheres,
+                        const float* samples, int n_samples, const uint32_t* offsets,
+                        const uint32_t* counts, const int32_t* prims, int64_t n_prims,
+                        float* dist, int32_t* closest, int on_device);
+
 /* ---- polygon soup of the emitted cells, on the device ------------------
  * libmat's Houdini export, get_one_convex_cell_faces_const
  * (src/IO/IO_CUDA/io_cuda.cxx:21-141) over every emitted cell in

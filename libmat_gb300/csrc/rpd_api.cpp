@@ -1036,6 +1036,71 @@ rpd_status rpd_copy_topology_to_host(rpd_ctx* c, rpd_topo_header* headers, int64
   return RPD_OK;
 }
 
+// ---- distance to local medial primitives ---------------------------------
+rpd_status rpd_dist2mat(rpd_ctx* c, const float* spheres, int n_spheres, const float* samples,
+                        int n_samples, const uint32_t* offsets, const uint32_t* counts,
+                        const int32_t* prims, int64_t n_prims, float* dist, int32_t* closest,
+                        int on_device) {
+  if (!c) return RPD_ERR_INVALID_ARGUMENT;
+  if (n_samples < 0 || n_spheres < 0 || n_prims < 0 || (n_samples > 0 && (!samples || !offsets ||
+      !counts || !dist || !closest)) || (n_prims > 0 && (!prims || !spheres)))
+    return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_dist2mat: missing input");
+  if (n_samples == 0) return RPD_OK;
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  cudaStream_t st = c->stream;
+  const float4* d_sph = reinterpret_cast<const float4*>(spheres);
+  const float3* d_smp = reinterpret_cast<const float3*>(samples);
+  const int3* d_prm = reinterpret_cast<const int3*>(prims);
+  const uint32_t *d_off = offsets, *d_cnt = counts;
+  float* d_dist = dist;
+  int32_t* d_cl = closest;
+  auto h2d = [&](void* dst, const void* src, size_t bytes) {
+    return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st) : cudaSuccess;
+  };
+  if (!on_device || (reinterpret_cast<uintptr_t>(spheres) & 15u)) {
+    CK(c->d2m_spheres.ensure((size_t)std::max(n_spheres, 1)), "alloc");
+    if (n_spheres > 0)
+      CK(cudaMemcpyAsync(c->d2m_spheres.ptr, spheres, sizeof(float4) * (size_t)n_spheres,
+                         on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st),
+         "copy spheres");
+    d_sph = c->d2m_spheres.ptr;
+  }
+  if (!on_device) {
+    CK(c->d2m_samples.ensure((size_t)n_samples), "alloc");
+    CK(c->d2m_prims.ensure((size_t)std::max<int64_t>(n_prims, 1)), "alloc");
+    CK(c->d2m_offsets.ensure((size_t)n_samples), "alloc");
+    CK(c->d2m_counts.ensure((size_t)n_samples), "alloc");
+    CK(c->d2m_dist.ensure((size_t)n_samples), "alloc");
+    CK(c->d2m_closest.ensure((size_t)n_samples), "alloc");
+    CK(h2d(c->d2m_samples.ptr, samples, sizeof(float3) * (size_t)n_samples), "H2D");
+    CK(h2d(c->d2m_prims.ptr, prims, sizeof(int3) * (size_t)n_prims), "H2D");
+    CK(h2d(c->d2m_offsets.ptr, offsets, sizeof(uint32_t) * (size_t)n_samples), "H2D");
+    CK(h2d(c->d2m_counts.ptr, counts, sizeof(uint32_t) * (size_t)n_samples), "H2D");
+    d_smp = c->d2m_samples.ptr;
+    d_prm = c->d2m_prims.ptr;
+    d_off = c->d2m_offsets.ptr;
+    d_cnt = c->d2m_counts.ptr;
+    d_dist = c->d2m_dist.ptr;
+    d_cl = c->d2m_closest.ptr;
+  }
+  CK(c->d2m_bad.ensure(1), "alloc");
+  CK(check_dist2mat(d_prm, n_prims, n_spheres, d_off, d_cnt, n_samples, c->d2m_bad.ptr, st),
+     "dist2mat check");
+  unsigned int bad = 0;
+  CK(cudaMemcpyAsync(&bad, c->d2m_bad.ptr, sizeof(bad), cudaMemcpyDeviceToHost, st), "D2H");
+  CK(cudaStreamSynchronize(st), "dist2mat sync");
+  if (bad) return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_dist2mat: sphere id or list out of range");
+  CK(launch_dist2mat(d_smp, n_samples, d_sph, d_prm, d_off, d_cnt, d_dist, d_cl, st), "dist2mat");
+  if (!on_device) {
+    CK(cudaMemcpyAsync(dist, d_dist, sizeof(float) * (size_t)n_samples, cudaMemcpyDeviceToHost, st),
+       "D2H");
+    CK(cudaMemcpyAsync(closest, d_cl, sizeof(int32_t) * (size_t)n_samples, cudaMemcpyDeviceToHost,
+                       st), "D2H");
+  }
+  CK(cudaStreamSynchronize(st), "dist2mat sync");
+  return RPD_OK;
+}
+
 // ---- polygon soup of the emitted cells ----------------------------------
 rpd_status rpd_compute_polygons(rpd_ctx* c, int triangulate, int boundary_only, int max_sf_fid,
                                 float* ms) {

@@ -147,6 +147,14 @@ struct rpd_ctx {
   DevBuf<int32_t> poly_site, poly_adj;
   long long n_poly_points = 0, n_polys = 0, n_poly_indices = 0;
   bool has_polygons = false;
+  // rpd_dist2mat scratch (host inputs are copied here)
+  DevBuf<float4> d2m_spheres;
+  DevBuf<float3> d2m_samples;
+  DevBuf<int3> d2m_prims;
+  DevBuf<uint32_t> d2m_offsets, d2m_counts;
+  DevBuf<float> d2m_dist;
+  DevBuf<int32_t> d2m_closest;
+  DevBuf<unsigned int> d2m_bad;
   DevBuf<uint8_t> payload;
   DevBuf<int32_t> flag_tmp, pos_tmp;
   DevBuf<unsigned long long> scratch;  // [0] payload cursor [1] work [2..3] counters

@@ -240,6 +240,15 @@ size_t scan64_temp(long long n);
 cudaError_t scan64_exclusive(const int32_t* in, long long* out, long long n, long long* temp,
                              cudaStream_t st);
 
+// distance to local medial primitives (rpd_dist2mat.cu): ids checked first
+// (*bad counts offending primitives / samples)
+cudaError_t check_dist2mat(const int3* prims, long long n_prims, int n_spheres,
+                           const uint32_t* offsets, const uint32_t* counts, int n_samples,
+                           unsigned int* bad, cudaStream_t st);
+cudaError_t launch_dist2mat(const float3* samples, int n_samples, const float4* spheres,
+                            const int3* prims, const uint32_t* offsets, const uint32_t* counts,
+                            float* dist, int32_t* closest, cudaStream_t st);
+
 // reference site_knn layout -> row-major lists; validation of ids
 cudaError_t neighbors_from_reference(const int32_t* ref, int k, int n_site, int32_t* nbr,
                                      cudaStream_t st);

@@ -53,7 +53,7 @@ EXPORTS = [
     "rpd_mlp_copy_features", "rpd_mlp_copy_klen", "rpd_mlp_copy_samples", "rpd_set_pair_k",
     "rpd_get_config", "rpd_set_config", "rpd_get_mesh_info",
     "rpd_topo_bytes", "rpd_compute_topology", "rpd_get_topology", "rpd_copy_topology_to_host",
-    "rpd_compute_polygons", "rpd_get_polygons", "rpd_copy_polygons_to_host",
+    "rpd_compute_polygons", "rpd_get_polygons", "rpd_copy_polygons_to_host", "rpd_dist2mat",
     "rpd_batch_create", "rpd_batch_destroy", "rpd_batch_last_error", "rpd_batch_add_mesh",
     "rpd_batch_size", "rpd_batch_set_graph", "rpd_batch_compute", "rpd_batch_autotune",
     "rpd_batch_mesh_cells", "rpd_batch_copy_mesh_cells", "rpd_batch_context",
@@ -212,6 +212,8 @@ def load(path=LIB_PATH):
     L.rpd_get_topology.argtypes = [vp, vp]
     L.rpd_copy_topology_to_host.restype = i32
     L.rpd_copy_topology_to_host.argtypes = [vp, vp, i64, vp, i64, c.POINTER(i64), c.POINTER(i64)]
+    L.rpd_dist2mat.restype = i32
+    L.rpd_dist2mat.argtypes = [vp, vp, i32, vp, i32, vp, vp, vp, i64, vp, vp, i32]
     L.rpd_compute_polygons.restype = i32
     L.rpd_compute_polygons.argtypes = [vp, i32, i32, i32, c.POINTER(c.c_float)]
     L.rpd_get_polygons.restype = i32
@@ -529,6 +531,23 @@ class RPD:
         self._check(self._L.rpd_copy_topology_to_host(self._h, _p(h), h.shape[0], _p(r), r.nbytes,
                                                       ctypes.byref(n), ctypes.byref(b)))
         return h[:n.value], r[:b.value]
+
+    def dist2mat(self, spheres, samples, offsets, counts, prims):
+        """libmat's dist2mat on the device: per sample, the smallest signed
+        distance to its medial primitives and the closest one's index in its
+        list.  spheres (n, 4) float32 (x, y, z, r); samples (m, 3); offsets,
+        counts (m,) uint32; prims (k, 3) int32.  Returns (dist, closest)."""
+        sph = np.ascontiguousarray(spheres, np.float32)
+        smp = np.ascontiguousarray(samples, np.float32)
+        off = np.ascontiguousarray(offsets, np.uint32)
+        cnt = np.ascontiguousarray(counts, np.uint32)
+        prm = np.ascontiguousarray(prims, np.int32)
+        m = smp.shape[0]
+        dist = np.zeros(m, np.float32)
+        closest = np.zeros(m, np.int32)
+        self._check(self._L.rpd_dist2mat(self._h, _p(sph), sph.shape[0], _p(smp), m, _p(off),
+                                         _p(cnt), _p(prm), prm.shape[0], _p(dist), _p(closest), 0))
+        return dist, closest
 
     def compute_polygons(self, triangulate=False, boundary_only=False, max_sf_fid=0):
         """Polygon soup of the emitted cells on the device (libmat's Houdini

@@ -13,7 +13,7 @@ from tests.conftest import ROOT
 def declared_symbols():
     src = open(ROOT + "/include/rpd_gb300.h").read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    return sorted(set(re.findall(r"\b(rpd_[a-z_]+)\s*\(", src)))
+    return sorted(set(re.findall(r"\b(rpd_[a-z0-9_]+)\s*\(", src)))
 
 
 def test_exports_every_declared_symbol():
