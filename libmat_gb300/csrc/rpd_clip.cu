@@ -376,16 +376,20 @@ __device__ __noinline__ bool exact_conflict(float4 p1, float4 p2, float4 p3, flo
 template <int PRED>
 __device__ __forceinline__ bool in_conflict(const WarpCell& c, int vi, float4 e,
                                             uint64_t dup, PredCount& pc) {
-  uchar4 v = c.ver[vi];
-  uint64_t vm = (1ull << v.x) | (1ull << v.y) | (1ull << v.z);
-  if (dup & vm) return false;
+  if (dup != 0ull) {  // rare: the plane equals one of the cell's
+    const uchar4 v = c.ver[vi];
+    if (dup & ((1ull << v.x) | (1ull << v.y) | (1ull << v.z))) return false;
+  }
   ++pc.pred;
   if (uses_filter(PRED)) {
     int s = filter_sign(c.u.f.K[vi], c.u.f.M[vi], e);
     if (s != 0) return s > 0;
     ++pc.esc;
+    const uchar4 v = c.ver[vi];
     if (PRED == RPD_PRED_EXACT) return exact_conflict(c.pl[v.x], c.pl[v.y], c.pl[v.z], e, pc.exact);
+    return det4x4_ref(c.pl[v.x], c.pl[v.y], c.pl[v.z], e) > 0.0;
   }
+  const uchar4 v = c.ver[vi];
   return det4x4_ref(c.pl[v.x], c.pl[v.y], c.pl[v.z], e) > 0.0;
 }
 
@@ -695,6 +699,7 @@ __device__ void clip_list(WarpCell& c, CellState& s, const int32_t* list, int k,
     uint64_t dup_mine = 0;
     for (int p = 0; p < s.nb_p; ++p)
       if (plane_eq(e_mine, c.pl[p])) dup_mine |= 1ull << p;
+    bool any_dup = __any_sync(0xffffffffu, dup_mine != 0ull);
     int r = 0;
     while (r < count) {
       if (eager) {
@@ -717,7 +722,7 @@ __device__ void clip_list(WarpCell& c, CellState& s, const int32_t* list, int k,
         int pi = lane >> lgV, vi = lane & (V - 1);
         int pidx = r + pi;
         float4 e = shfl4(e_mine, pidx & 31);
-        uint64_t dup = shfl64(dup_mine, pidx & 31);
+        uint64_t dup = any_dup ? shfl64(dup_mine, pidx & 31) : 0ull;
         bool cf = false;
         if (pidx < count && vi < s.nb_v) cf = in_conflict<PRED>(c, vi, e, dup, pc);
         uint32_t m = __ballot_sync(0xffffffffu, cf);
@@ -730,7 +735,7 @@ __device__ void clip_list(WarpCell& c, CellState& s, const int32_t* list, int k,
         hit = r + pf;
       } else {
         float4 e = shfl4(e_mine, r);
-        uint64_t dup = shfl64(dup_mine, r);
+        uint64_t dup = any_dup ? shfl64(dup_mine, r) : 0ull;
         bool any = false;
         for (int w = 0; w < 3; ++w) {
           int vi = lane + 32 * w;
@@ -795,6 +800,7 @@ __device__ void clip_list(WarpCell& c, CellState& s, const int32_t* list, int k,
       if (eager && s.status == kSuccess) R = cell_radius(c, s.nb_v, lane);
       // later planes of this chunk identical to the new one
       if (plane_eq(e_mine, e)) dup_mine |= 1ull << (s.nb_p - 1);
+      any_dup = __any_sync(0xffffffffu, dup_mine != 0ull);
       if (s.status != kSuccess) break;
       r = hit + 1;
     }
