@@ -415,11 +415,14 @@ def run_ours(args):
     # profiles/ (per pair on a smaller case of the same workload family,
     # scaled by this launch's pairs: traffic grows with the pairs)
     traffic = None
+    issue = None
     tfile = os.path.join(ROOT, "profiles", "clip_cells_kernel_ellipsoid_200k.md")
     if os.path.exists(tfile):
         for ln in open(tfile):
             if ln.startswith("traffic_bytes_per_pair:"):
                 traffic = float(ln.split(":")[1]) * st.n_pairs
+            if ln.startswith("issue_active_frac:"):
+                issue = float(ln.split(":")[1])
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -469,7 +472,10 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "kernel": "clip_cells_kernel", "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                      "peak_source": peak_src,
-                     "algorithmic_bytes": alg},
+                     "algorithmic_bytes": alg,
+                     # the bound that applies: instruction issue (ncu
+                     # smsp__issue_active of the same kernel, the profile above)
+                     "issue_active_frac": issue},
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
     }
