@@ -318,6 +318,19 @@ rpd_status rpd_copy_topology_to_host(struct rpd_ctx* ctx, rpd_topo_header* heade
                                      int64_t max_cells, void* records, int64_t capacity,
                                      int64_t* n_cells, int64_t* bytes);
 
+/* ---- incremental update ---------------------------------------------------
+ * libmat's RPD3D_GPU::calculate_partial (src/rpd3d_api/rpd_api.cxx:147-316):
+ * after rpd_compute (and rpd_set_sites with the same site count, e.g. moved
+ * or resized spheres), recomputes the cells of the sites with recompute[i]
+ * != 0 -- the changed sites and those whose cells they can change, libmat's
+ * spheres_and_1rings -- with the context's current sites, and merges them
+ * with the previous cells: cells of the other sites are kept as they were
+ * (merge_convex_cells).  The merged cells are the rpd_get_cells /
+ * rpd_copy_cells_to_host result, in (tet, site) order; stats and the
+ * pair-level outputs (pair headers, pairs, topology hashes) describe the
+ * recomputed sites' pairs.  Site flags of rpd_set_sites still apply. */
+rpd_status rpd_compute_partial(struct rpd_ctx* ctx, const uint32_t* recompute, rpd_stats* stats);
+
 /* ---- distance to local medial primitives --------------------------------
  * libmat's dist2mat (ClosestDistanceToLocalMat / compute_closest_dist2mat,
  * src/dist2mat/dist2mat.cu:195-310): for every sample point (xyz), the

@@ -31,6 +31,7 @@ CUDA_UNITS = {
     "rpd_topo.cu": ["-fmad=false"],
     "rpd_poly.cu": ["-fmad=false"],
     "rpd_dist2mat.cu": ["-fmad=false"],
+    "rpd_partial.cu": [],
 }
 CXX_UNITS = ["rpd_api.cpp", "rpd_mesh.cpp", "rpd_batch.cpp"]
 

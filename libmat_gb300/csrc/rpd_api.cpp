@@ -294,6 +294,7 @@ rpd_status rpd_set_mesh(rpd_ctx* c, const double* xyz, int n_vert, const int32_t
   CK(cudaSetDevice(c->device), "cudaSetDevice");
   c->has_mesh = false;
   c->has_result = false;
+  c->cells_for_mesh = false;
   cudaStream_t st = c->stream;
   // the raw arrays go to the device; everything derived is computed there
   CK(c->vert3d.ensure((size_t)n_vert * 3), "alloc vert3d");
@@ -401,6 +402,7 @@ rpd_status rpd_set_sites(rpd_ctx* c, const double* xyzw, int n_site, const uint3
   if (c->n_site != n_site) {
     c->has_user_nbr = false;
     c->has_site_klen = false;
+    c->cells_for_mesh = false;  // site ids of the previous cells no longer apply
   }
   c->n_site = n_site;
   for (int a = 0; a < 3; ++a) {
@@ -608,8 +610,10 @@ static rpd_status finish_compute(rpd_ctx* c, bool knn, bool learned, rpd_stats* 
   c->has_result = true;
   c->has_topology = false;
   c->has_polygons = false;
+  c->cells_for_mesh = false;
   if (host_scratch[8 + 10] != 0)
     return fail(c, RPD_ERR_CAPACITY, "rpd_compute: cells lost to a full payload buffer");
+  c->cells_for_mesh = true;
   if (stats) {
     std::memset(stats, 0, sizeof(*stats));
     stats->n_pairs = n_pairs;
@@ -1033,6 +1037,80 @@ rpd_status rpd_copy_topology_to_host(rpd_ctx* c, rpd_topo_header* headers, int64
     CK(cudaMemcpyAsync(records, c->topo_buf.ptr, (size_t)c->topo_bytes, cudaMemcpyDeviceToHost, st),
        "D2H topology");
   CK(cudaStreamSynchronize(st), "copy sync");
+  return RPD_OK;
+}
+
+// ---- incremental update ---------------------------------------------------
+rpd_status rpd_compute_partial(rpd_ctx* c, const uint32_t* recompute, rpd_stats* stats) {
+  if (!c || !recompute) return RPD_ERR_INVALID_ARGUMENT;
+  if (!c->cells_for_mesh)
+    return fail(c, RPD_ERR_NOT_READY,
+                "rpd_compute_partial: needs the cells of a previous rpd_compute on this mesh and "
+                "site count");
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  cudaStream_t st = c->stream;
+  const int n_site = c->n_site;
+  // the previous cells move aside; the partial compute runs with the
+  // recomputed sites' flags (and the caller's: unselected sites stay so)
+  c->cells.swap(c->prev_cells);
+  c->payload.swap(c->prev_payload);
+  const long long n_old = c->n_cells;
+  c->cells_for_mesh = false;
+  CK(c->partial_flags.ensure((size_t)n_site), "alloc");
+  CK(c->user_flags.ensure((size_t)n_site), "alloc");
+  std::vector<uint32_t> rf((size_t)n_site), uf((size_t)n_site);
+  CK(cudaMemcpyAsync(uf.data(), c->flags.ptr, sizeof(uint32_t) * (size_t)n_site,
+                     cudaMemcpyDeviceToHost, st), "D2H flags");
+  CK(cudaStreamSynchronize(st), "sync");
+  for (int i = 0; i < n_site; ++i) {
+    rf[(size_t)i] = recompute[i] ? 1u : 0u;
+    uf[(size_t)i] = uf[(size_t)i] == 1u && rf[(size_t)i] ? 1u : 0u;
+  }
+  CK(cudaMemcpyAsync(c->partial_flags.ptr, rf.data(), sizeof(uint32_t) * (size_t)n_site,
+                     cudaMemcpyHostToDevice, st), "H2D flags");
+  CK(cudaMemcpyAsync(c->user_flags.ptr, uf.data(), sizeof(uint32_t) * (size_t)n_site,
+                     cudaMemcpyHostToDevice, st), "H2D flags");
+  c->flags.swap(c->user_flags);  // user_flags now holds the caller's flags
+  rpd_status s = rpd_compute(c, stats);
+  c->flags.swap(c->user_flags);
+  if (s != RPD_OK) return s;
+  // merge: kept old cells (sites not recomputed) and the new cells, in
+  // (tet, site) order
+  const long long n_new = c->n_cells, n = n_old + n_new;
+  CK(c->merge_keep.ensure((size_t)std::max(n_old, 1ll)), "alloc");
+  CK(c->merge_keep_pos.ensure((size_t)n_old + 1), "alloc");
+  CK(c->scan_tmp.ensure(scan_temp_ints(std::max(n_old, 1ll)) + 16), "alloc");
+  CK(merge_keep(c->prev_cells.ptr, n_old, c->partial_flags.ptr, c->merge_keep.ptr, st), "merge");
+  CK(scan_exclusive(c->merge_keep.ptr, c->merge_keep_pos.ptr, n_old, c->scan_tmp.ptr, st), "merge scan");
+  int32_t n_kept = 0;
+  CK(cudaMemcpyAsync(&n_kept, c->merge_keep_pos.ptr + n_old, sizeof(n_kept), cudaMemcpyDeviceToHost,
+                     st), "D2H");
+  CK(cudaStreamSynchronize(st), "sync");
+  const long long n_out = n_kept + n_new;
+  if (n_out > n) return fail(c, RPD_ERR_CUDA, "rpd_compute_partial: inconsistent merge");
+  CK(c->merge_src.ensure((size_t)std::max(n_out, 1ll)), "alloc");
+  CK(c->merge_units.ensure((size_t)std::max(n_out, 1ll)), "alloc");
+  CK(c->merge_off.ensure((size_t)n_out + 1), "alloc");
+  CK(c->merge_scan.ensure(scan64_temp(std::max(n_out, 1ll))), "alloc");
+  CK(merge_slots(c->prev_cells.ptr, n_old, c->merge_keep.ptr, c->merge_keep_pos.ptr, c->cells.ptr,
+                 n_new, n_out, c->merge_src.ptr, c->merge_units.ptr, st), "merge slots");
+  CK(scan64_exclusive(c->merge_units.ptr, c->merge_off.ptr, n_out, c->merge_scan.ptr, st),
+     "merge scan");
+  long long units = 0;
+  CK(cudaMemcpyAsync(&units, c->merge_off.ptr + n_out, sizeof(units), cudaMemcpyDeviceToHost, st),
+     "D2H");
+  CK(cudaStreamSynchronize(st), "sync");
+  CK(c->merged_cells.ensure((size_t)std::max(n_out, 1ll)), "alloc");
+  CK(c->merged_payload.ensure((size_t)std::max(16 * units, 16ll)), "alloc");
+  CK(merge_gather(c->merge_src.ptr, n_out, c->merge_off.ptr, c->prev_cells.ptr, c->prev_payload.ptr,
+                  c->cells.ptr, c->payload.ptr, c->merged_cells.ptr, c->merged_payload.ptr,
+                  c->num_sms, st), "merge gather");
+  CK(cudaStreamSynchronize(st), "sync");
+  c->cells.swap(c->merged_cells);
+  c->payload.swap(c->merged_payload);
+  c->n_cells = n_out;
+  c->payload_bytes = 16 * units;
+  c->cells_for_mesh = true;
   return RPD_OK;
 }
 

@@ -495,6 +495,7 @@ rpd_status rpd_batch_compute(rpd_batch* b, rpd_stats* stats) {
   if (c->n_pairs > INT32_MAX) return bfail(b, RPD_ERR_CAPACITY, "rpd_batch_compute: more than 2^31 pairs");
   c->pair_cap_hint = std::max<long long>(c->pair_cap_hint, c->n_pairs + c->n_pairs / 8 + 1024);
   rpd_status s = rpd_finish_compute(c, true, false, stats);
+  c->cells_for_mesh = false;  // a batch's cells are not one mesh's (no partial update)
   if (s != RPD_OK) return bfail(b, s, rpd_last_error(c));
   // first compacted cell of every mesh
   const int nm = (int)b->meshes.size();

@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <utility>
 #include <cstdint>
 #include <string>
 
@@ -57,6 +58,10 @@ struct DevBuf {
     if (ptr) cudaFree(ptr);
     ptr = nullptr;
     cap = 0;
+  }
+  void swap(DevBuf& o) {
+    std::swap(ptr, o.ptr);
+    std::swap(cap, o.cap);
   }
   ~DevBuf() { release(); }
 };
@@ -147,6 +152,14 @@ struct rpd_ctx {
   DevBuf<int32_t> poly_site, poly_adj;
   long long n_poly_points = 0, n_polys = 0, n_poly_indices = 0;
   bool has_polygons = false;
+  // rpd_compute_partial: the previous cells, the merge's buffers, the
+  // recomputed sites' flags
+  bool cells_for_mesh = false;  // cells / payload hold every cell of the current mesh and sites
+  DevBuf<rpd_cell_header> prev_cells, merged_cells;
+  DevBuf<uint8_t> prev_payload, merged_payload;
+  DevBuf<int32_t> merge_keep, merge_keep_pos, merge_units;
+  DevBuf<long long> merge_src, merge_off, merge_scan;
+  DevBuf<uint32_t> partial_flags, user_flags;
   // rpd_dist2mat scratch (host inputs are copied here)
   DevBuf<float4> d2m_spheres;
   DevBuf<float3> d2m_samples;

@@ -240,6 +240,19 @@ size_t scan64_temp(long long n);
 cudaError_t scan64_exclusive(const int32_t* in, long long* out, long long n, long long* temp,
                              cudaStream_t st);
 
+// merge of a partial recompute (rpd_partial.cu): keep[a] = old cell a's site
+// not recomputed; slots of the merged (tet, site) order; gather of records
+cudaError_t merge_keep(const rpd_cell_header* old_cells, long long n_old, const uint32_t* recomputed,
+                       int32_t* keep, cudaStream_t st);
+cudaError_t merge_slots(const rpd_cell_header* old_cells, long long n_old, const int32_t* keep,
+                        const int32_t* keep_pos, const rpd_cell_header* new_cells, long long n_new,
+                        long long n_out, long long* src, int32_t* units, cudaStream_t st);
+cudaError_t merge_gather(const long long* src, long long n, const long long* off,
+                         const rpd_cell_header* old_cells, const uint8_t* old_payload,
+                         const rpd_cell_header* new_cells, const uint8_t* new_payload,
+                         rpd_cell_header* out_cells, uint8_t* out_payload, int num_sms,
+                         cudaStream_t st);
+
 // distance to local medial primitives (rpd_dist2mat.cu): ids checked first
 // (*bad counts offending primitives / samples)
 cudaError_t check_dist2mat(const int3* prims, long long n_prims, int n_spheres,

@@ -54,6 +54,7 @@ EXPORTS = [
     "rpd_get_config", "rpd_set_config", "rpd_get_mesh_info",
     "rpd_topo_bytes", "rpd_compute_topology", "rpd_get_topology", "rpd_copy_topology_to_host",
     "rpd_compute_polygons", "rpd_get_polygons", "rpd_copy_polygons_to_host", "rpd_dist2mat",
+    "rpd_compute_partial",
     "rpd_batch_create", "rpd_batch_destroy", "rpd_batch_last_error", "rpd_batch_add_mesh",
     "rpd_batch_size", "rpd_batch_set_graph", "rpd_batch_compute", "rpd_batch_autotune",
     "rpd_batch_mesh_cells", "rpd_batch_copy_mesh_cells", "rpd_batch_context",
@@ -212,6 +213,8 @@ def load(path=LIB_PATH):
     L.rpd_get_topology.argtypes = [vp, vp]
     L.rpd_copy_topology_to_host.restype = i32
     L.rpd_copy_topology_to_host.argtypes = [vp, vp, i64, vp, i64, c.POINTER(i64), c.POINTER(i64)]
+    L.rpd_compute_partial.restype = i32
+    L.rpd_compute_partial.argtypes = [vp, vp, c.POINTER(Stats)]
     L.rpd_dist2mat.restype = i32
     L.rpd_dist2mat.argtypes = [vp, vp, i32, vp, i32, vp, vp, vp, i64, vp, vp, i32]
     L.rpd_compute_polygons.restype = i32
@@ -531,6 +534,15 @@ class RPD:
         self._check(self._L.rpd_copy_topology_to_host(self._h, _p(h), h.shape[0], _p(r), r.nbytes,
                                                       ctypes.byref(n), ctypes.byref(b)))
         return h[:n.value], r[:b.value]
+
+    def compute_partial(self, recompute):
+        """Recomputes the cells of the sites with recompute[i] != 0 and
+        merges them with the previous cells (libmat's calculate_partial);
+        returns the partial compute's stats."""
+        fl = np.ascontiguousarray(np.asarray(recompute) != 0, np.uint32)
+        st = Stats()
+        self._check(self._L.rpd_compute_partial(self._h, _p(fl), ctypes.byref(st)))
+        return st
 
     def dist2mat(self, spheres, samples, offsets, counts, prims):
         """libmat's dist2mat on the device: per sample, the smallest signed
