@@ -318,6 +318,77 @@ rpd_status rpd_copy_topology_to_host(struct rpd_ctx* ctx, rpd_topo_header* heade
                                      int64_t max_cells, void* records, int64_t capacity,
                                      int64_t* n_cells, int64_t* bytes);
 
+/* ---- power cells of the emitted cells ------------------------------------
+ * What libmat's get_all_voro_info (src/rpd3d_base/rpd_update.cxx:80-340)
+ * gathers for every medial sphere into its PowerCell
+ * (src/matbase/medial_sphere.h:145-260), as flat device arrays (cell ids
+ * are rpd_get_cells indices, site ids the context's):
+ *   site_cells[site_cell_off[s] ..]   cells of site s, ascending (cell_ids)
+ *   cell_nbrs[cell_nbr_off[c] ..]     cells of the same site across c's
+ *                                     tet faces, ascending (cell_neighbors)
+ *   cell_tfids[cell_tfid_off[c] ..]   c's active tet faces, ascending
+ *                                     (cell_to_tfids)
+ *   facet_keys / facet_cells          (site << 32 | neighbour site) and cell
+ *                                     of every active bisector face, sorted
+ *                                     by site, neighbour, cell
+ *                                     (facet_neigh_to_cells); per site from
+ *                                     site_facet_off
+ *   edges                             7 int32 per active edge on two
+ *                                     bisectors: site, neighbour min, max,
+ *                                     cell, its two vertices on both faces,
+ *                                     0; sorted by site, neighbours, cell,
+ *                                     edge (e_to_cells, edge_2endvertices);
+ *                                     per site from site_edge_off
+ *   vertex_*                          every vertex with two or more
+ *                                     neighbour sites among its planes: cell,
+ *                                     vertex slot, the sorted neighbour
+ *                                     triple (-1 for a tet face), float
+ *                                     position, surface face id or -1
+ *                                     (vertex_2id, vertex_2pos); per cell from
+ *                                     cell_vertex_off
+ *   surface_*                         every active tet face with id <=
+ *                                     max_sf_fid: cell, face id, centroid of
+ *                                     its vertex cycle (cell_to_surfv2fid);
+ *                                     per cell from cell_surface_off
+ * Feature-edge records (TetMesh::tet_es2fe_map) are not part of it.  Computes
+ * the per-cell topology first when needed. */
+rpd_status rpd_compute_power_cells(struct rpd_ctx* ctx, int max_sf_fid, float* ms);
+
+typedef struct rpd_power_cells_view {
+  int32_t n_site;
+  int64_t n_cells;
+  const int64_t* site_cell_off;
+  const uint32_t* site_cells;
+  const int64_t* cell_nbr_off;
+  const int32_t* cell_nbrs;
+  const int64_t* cell_tfid_off;
+  const int32_t* cell_tfids;
+  int64_t n_facets;
+  const int64_t* site_facet_off;
+  const uint64_t* facet_keys;
+  const uint32_t* facet_cells;
+  int64_t n_edges;
+  const int64_t* site_edge_off;
+  const int32_t* edges;
+  int64_t n_vertices;
+  const int64_t* cell_vertex_off;
+  const int32_t* vertex_cell;
+  const int32_t* vertex_lvid;
+  const int32_t* vertex_ids;  /* 3 per vertex */
+  const float* vertex_pos;    /* 3 per vertex */
+  const int32_t* vertex_sfid;
+  int64_t n_surface;
+  const int64_t* cell_surface_off;
+  const int32_t* surface_cell;
+  const int32_t* surface_fid;
+  const float* surface_pos;   /* 3 per face */
+} rpd_power_cells_view;
+rpd_status rpd_get_power_cells(struct rpd_ctx* ctx, rpd_power_cells_view* view);
+
+/* Copies `bytes` from a device pointer of one of the views above to host
+ * memory, on the context's stream (for callers without CUDA of their own). */
+rpd_status rpd_copy_device_to_host(struct rpd_ctx* ctx, void* dst, const void* src, int64_t bytes);
+
 /* ---- incremental update ---------------------------------------------------
  * libmat's RPD3D_GPU::calculate_partial (src/rpd3d_api/rpd_api.cxx:147-316):
  * after rpd_compute (and rpd_set_sites with the same site count, e.g. moved

@@ -32,6 +32,8 @@ CUDA_UNITS = {
     "rpd_poly.cu": ["-fmad=false"],
     "rpd_dist2mat.cu": ["-fmad=false"],
     "rpd_partial.cu": [],
+    "rpd_sort.cu": [],
+    "rpd_powercell.cu": ["-fmad=false"],
 }
 CXX_UNITS = ["rpd_api.cpp", "rpd_mesh.cpp", "rpd_batch.cpp"]
 

@@ -610,6 +610,7 @@ static rpd_status finish_compute(rpd_ctx* c, bool knn, bool learned, rpd_stats* 
   c->has_result = true;
   c->has_topology = false;
   c->has_polygons = false;
+  c->has_power_cells = false;
   c->cells_for_mesh = false;
   if (host_scratch[8 + 10] != 0)
     return fail(c, RPD_ERR_CAPACITY, "rpd_compute: cells lost to a full payload buffer");
@@ -1037,6 +1038,187 @@ rpd_status rpd_copy_topology_to_host(rpd_ctx* c, rpd_topo_header* headers, int64
     CK(cudaMemcpyAsync(records, c->topo_buf.ptr, (size_t)c->topo_bytes, cudaMemcpyDeviceToHost, st),
        "D2H topology");
   CK(cudaStreamSynchronize(st), "copy sync");
+  return RPD_OK;
+}
+
+// ---- power cells of the emitted cells -------------------------------------
+rpd_status rpd_compute_power_cells(rpd_ctx* c, int max_sf_fid, float* ms) {
+  if (!c) return RPD_ERR_INVALID_ARGUMENT;
+  if (!c->has_result) return fail(c, RPD_ERR_NOT_READY, "rpd_compute_power_cells: no result");
+  if (!c->has_topology) {
+    const rpd_status s = rpd_compute_topology(c, nullptr);
+    if (s != RPD_OK) return s;
+  }
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  cudaStream_t st = c->stream;
+  const long long n = c->n_cells;
+  const int n_site = c->n_site;
+  if (n > 0x7fffffffll) return fail(c, RPD_ERR_CAPACITY, "rpd_compute_power_cells: too many cells");
+  CK(cudaEventRecord(c->ev[kEvTopo0], st), "event");
+  CK(c->pc_cnt.ensure((size_t)std::max(5 * n, 5ll)), "alloc");
+  CK(c->pc_off.ensure((size_t)(5 * (n + 1))), "alloc");
+  CK(c->pc_scan.ensure(scan64_temp(std::max(n, 1ll)) + 16), "alloc");
+  PowerCellParams p = {};
+  p.cells = c->cells.ptr;
+  p.n = n;
+  p.payload = c->payload.ptr;
+  p.topo_h = c->topo_h.ptr;
+  p.topo = c->topo_buf.ptr;
+  p.max_sf_fid = max_sf_fid;
+  p.cnt = c->pc_cnt.ptr;
+  p.off = c->pc_off.ptr;
+  CK(pc_count(p, st), "power cell counts");
+  for (int k = 0; k < 5; ++k)
+    CK(scan64_exclusive(c->pc_cnt.ptr + k * n, c->pc_off.ptr + k * (n + 1), n, c->pc_scan.ptr, st),
+       "power cell scan");
+  long long tot[5];
+  for (int k = 0; k < 5; ++k)
+    CK(cudaMemcpyAsync(&tot[k], c->pc_off.ptr + k * (n + 1) + n, sizeof(long long),
+                       cudaMemcpyDeviceToHost, st), "D2H");
+  CK(cudaStreamSynchronize(st), "sync");
+  const long long n_tf = tot[0], n_fa = tot[1], n_ed = tot[2], n_vx = tot[3], n_sf = tot[4];
+  // key / value segments: tet faces, facets, edges, sites
+  const long long seg[4] = {n_tf, n_fa, n_ed, n};
+  const long long n_keys = n_tf + n_fa + n_ed + n;
+  const long long max_seg = std::max(std::max(n_tf, n_fa), std::max(n_ed, n));
+  if (max_seg > 0x7fffffffll) return fail(c, RPD_ERR_CAPACITY, "rpd_compute_power_cells: too many records");
+  CK(c->pc_keys.ensure((size_t)std::max(n_keys, 1ll)), "alloc");
+  CK(c->pc_vals.ensure((size_t)std::max(n_keys, 1ll)), "alloc");
+  CK(c->pc_keys_tmp.ensure((size_t)std::max(max_seg, 1ll)), "alloc");
+  CK(c->pc_vals_tmp.ensure((size_t)std::max(max_seg, 1ll)), "alloc");
+  const size_t nh = radix_hist_ints(std::max(max_seg, 1ll));
+  CK(c->pc_hist.ensure(nh), "alloc");
+  CK(c->pc_scan_i.ensure(scan_temp_ints((long long)nh) + 16), "alloc");
+  CK(c->pc_tf_fid.ensure((size_t)std::max(n_tf, 1ll)), "alloc");
+  CK(c->pc_ed_fields.ensure((size_t)std::max(6 * n_ed, 6ll)), "alloc");
+  CK(c->pc_ed_out.ensure((size_t)std::max(7 * n_ed, 7ll)), "alloc");
+  CK(c->pc_vx_i.ensure((size_t)std::max(6 * n_vx, 6ll)), "alloc");
+  CK(c->pc_vx_pos.ensure((size_t)std::max(3 * n_vx, 3ll)), "alloc");
+  CK(c->pc_sf_i.ensure((size_t)std::max(2 * n_sf, 2ll)), "alloc");
+  CK(c->pc_sf_pos.ensure((size_t)std::max(3 * n_sf, 3ll)), "alloc");
+  CK(c->pc_site_off.ensure((size_t)(3 * ((long long)n_site + 1))), "alloc");
+  CK(c->pc_nbr_cnt.ensure((size_t)std::max(n, 1ll)), "alloc");
+  CK(c->pc_nbr_fill.ensure((size_t)std::max(n, 1ll)), "alloc");
+  CK(c->pc_nbr_off.ensure((size_t)n + 1), "alloc");
+  unsigned long long* keys[4];
+  uint32_t* vals[4];
+  long long at = 0;
+  for (int k = 0; k < 4; ++k) {
+    keys[k] = c->pc_keys.ptr + at;
+    vals[k] = c->pc_vals.ptr + at;
+    at += seg[k];
+  }
+  p.tf_fid = c->pc_tf_fid.ptr;
+  p.tf_key = keys[0];
+  p.tf_val = vals[0];
+  p.fa_key = keys[1];
+  p.fa_val = vals[1];
+  p.ed_key = keys[2];
+  p.ed_val = vals[2];
+  int32_t* ef = c->pc_ed_fields.ptr;
+  p.ed_site = ef;
+  p.ed_n0 = ef + n_ed;
+  p.ed_n1 = ef + 2 * n_ed;
+  p.ed_cell = ef + 3 * n_ed;
+  p.ed_lv0 = ef + 4 * n_ed;
+  p.ed_lv1 = ef + 5 * n_ed;
+  p.ed_out = c->pc_ed_out.ptr;
+  int32_t* vi = c->pc_vx_i.ptr;
+  p.vx_cell = vi;
+  p.vx_lvid = vi + n_vx;
+  p.vx_sfid = vi + 2 * n_vx;
+  p.vx_ids = vi + 3 * n_vx;
+  p.vx_pos = c->pc_vx_pos.ptr;
+  p.sf_cell = c->pc_sf_i.ptr;
+  p.sf_fid = c->pc_sf_i.ptr + n_sf;
+  p.sf_pos = c->pc_sf_pos.ptr;
+  p.site_key = keys[3];
+  p.site_val = vals[3];
+  p.nbr_cnt = c->pc_nbr_cnt.ptr;
+  p.nbr_fill = c->pc_nbr_fill.ptr;
+  p.nbr_off = c->pc_nbr_off.ptr;
+  CK(pc_fill(p, st), "power cell records");
+  // stable sorts: by (site, key) for faces and facets; edges by the
+  // neighbour pair, then by site; cells by site
+  int site_bits = 1;
+  while ((1ll << site_bits) < (long long)std::max(n_site, 1)) ++site_bits;
+  auto sort = [&](int k, int bits) {
+    return radix_sort_pairs(keys[k], vals[k], seg[k], bits, c->pc_keys_tmp.ptr, c->pc_vals_tmp.ptr,
+                            c->pc_hist.ptr, c->pc_scan_i.ptr, st);
+  };
+  CK(sort(0, 32 + site_bits), "sort");
+  CK(sort(1, 32 + site_bits), "sort");
+  CK(sort(2, 32 + site_bits), "sort");
+  CK(pc_edges_finish(p, n_ed, 0, st), "edge keys");
+  CK(sort(2, site_bits), "sort");
+  CK(pc_edges_finish(p, n_ed, 1, st), "edge gather");
+  CK(sort(3, site_bits), "sort");
+  long long* so = c->pc_site_off.ptr;
+  CK(pc_site_offsets(keys[3], n, n_site, 0, so, st), "offsets");
+  CK(pc_site_offsets(keys[1], n_fa, n_site, 32, so + (n_site + 1), st), "offsets");
+  CK(pc_site_offsets(keys[2], n_ed, n_site, 0, so + 2 * (n_site + 1), st), "offsets");
+  // neighbour cells across tet faces
+  CK(cudaMemsetAsync(c->pc_nbr_cnt.ptr, 0, sizeof(int32_t) * (size_t)std::max(n, 1ll), st), "memset");
+  CK(cudaMemsetAsync(c->pc_nbr_fill.ptr, 0, sizeof(int32_t) * (size_t)std::max(n, 1ll), st), "memset");
+  CK(pc_neighbours(p, n_tf, 0, st), "neighbours");
+  CK(scan64_exclusive(c->pc_nbr_cnt.ptr, c->pc_nbr_off.ptr, n, c->pc_scan.ptr, st), "scan");
+  long long n_nbr = 0;
+  CK(cudaMemcpyAsync(&n_nbr, c->pc_nbr_off.ptr + n, sizeof(n_nbr), cudaMemcpyDeviceToHost, st), "D2H");
+  CK(cudaStreamSynchronize(st), "sync");
+  CK(c->pc_nbr.ensure((size_t)std::max(n_nbr, 1ll)), "alloc");
+  p.nbr = c->pc_nbr.ptr;
+  CK(pc_neighbours(p, n_tf, 1, st), "neighbours");
+  CK(pc_neighbours(p, n_tf, 2, st), "neighbours");
+  CK(cudaEventRecord(c->ev[kEvTopo1], st), "event");
+  CK(cudaStreamSynchronize(st), "sync");
+  if (ms) CK(cudaEventElapsedTime(ms, c->ev[kEvTopo0], c->ev[kEvTopo1]), "event time");
+  rpd_power_cells_view& v = c->pc_view;
+  v.n_site = n_site;
+  v.n_cells = n;
+  v.site_cell_off = reinterpret_cast<const int64_t*>(so);
+  v.site_cells = vals[3];
+  v.cell_nbr_off = reinterpret_cast<const int64_t*>(c->pc_nbr_off.ptr);
+  v.cell_nbrs = c->pc_nbr.ptr;
+  v.cell_tfid_off = reinterpret_cast<const int64_t*>(c->pc_off.ptr);
+  v.cell_tfids = c->pc_tf_fid.ptr;
+  v.n_facets = n_fa;
+  v.site_facet_off = reinterpret_cast<const int64_t*>(so + (n_site + 1));
+  v.facet_keys = reinterpret_cast<const uint64_t*>(keys[1]);
+  v.facet_cells = vals[1];
+  v.n_edges = n_ed;
+  v.site_edge_off = reinterpret_cast<const int64_t*>(so + 2 * (n_site + 1));
+  v.edges = c->pc_ed_out.ptr;
+  v.n_vertices = n_vx;
+  v.cell_vertex_off = reinterpret_cast<const int64_t*>(c->pc_off.ptr + 3 * (n + 1));
+  v.vertex_cell = p.vx_cell;
+  v.vertex_lvid = p.vx_lvid;
+  v.vertex_ids = p.vx_ids;
+  v.vertex_pos = p.vx_pos;
+  v.vertex_sfid = p.vx_sfid;
+  v.n_surface = n_sf;
+  v.cell_surface_off = reinterpret_cast<const int64_t*>(c->pc_off.ptr + 4 * (n + 1));
+  v.surface_cell = p.sf_cell;
+  v.surface_fid = p.sf_fid;
+  v.surface_pos = p.sf_pos;
+  c->pc_n_nbr = n_nbr;
+  c->has_power_cells = true;
+  return RPD_OK;
+}
+
+rpd_status rpd_get_power_cells(rpd_ctx* c, rpd_power_cells_view* v) {
+  if (!c || !v) return RPD_ERR_INVALID_ARGUMENT;
+  if (!c->has_result || !c->has_power_cells)
+    return fail(c, RPD_ERR_NOT_READY, "rpd_get_power_cells: call rpd_compute_power_cells first");
+  *v = c->pc_view;
+  return RPD_OK;
+}
+
+rpd_status rpd_copy_device_to_host(rpd_ctx* c, void* dst, const void* src, int64_t bytes) {
+  if (!c || bytes < 0 || (bytes > 0 && (!dst || !src))) return RPD_ERR_INVALID_ARGUMENT;
+  if (bytes == 0) return RPD_OK;
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  CK(cudaMemcpyAsync(dst, src, (size_t)bytes, cudaMemcpyDeviceToHost, c->stream), "D2H");
+  CK(cudaStreamSynchronize(c->stream), "copy sync");
   return RPD_OK;
 }
 

@@ -160,6 +160,17 @@ struct rpd_ctx {
   DevBuf<int32_t> merge_keep, merge_keep_pos, merge_units;
   DevBuf<long long> merge_src, merge_off, merge_scan;
   DevBuf<uint32_t> partial_flags, user_flags;
+  // rpd_compute_power_cells
+  DevBuf<int32_t> pc_cnt, pc_tf_fid, pc_ed_fields, pc_ed_out, pc_vx_i, pc_sf_i, pc_nbr_cnt,
+      pc_nbr_fill, pc_nbr, pc_hist, pc_scan_i;
+  DevBuf<long long> pc_off, pc_scan, pc_site_off, pc_nbr_off;
+  DevBuf<unsigned long long> pc_keys, pc_keys_tmp;
+  DevBuf<uint32_t> pc_vals, pc_vals_tmp;
+  DevBuf<float> pc_vx_pos, pc_sf_pos;
+  long long pc_n[5] = {0, 0, 0, 0, 0};
+  long long pc_n_nbr = 0;
+  bool has_power_cells = false;
+  rpd_power_cells_view pc_view = {};
   // rpd_dist2mat scratch (host inputs are copied here)
   DevBuf<float4> d2m_spheres;
   DevBuf<float3> d2m_samples;

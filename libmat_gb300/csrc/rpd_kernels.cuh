@@ -253,6 +253,56 @@ cudaError_t merge_gather(const long long* src, long long n, const long long* off
                          rpd_cell_header* out_cells, uint8_t* out_payload, int num_sms,
                          cudaStream_t st);
 
+// stable radix sort of (key, value) pairs by the low `bits` key bits
+// (rpd_sort.cu); hist and scan_tmp: radix_hist_ints(n) and
+// scan_temp_ints(radix_hist_ints(n)) ints
+size_t radix_hist_ints(long long n);
+cudaError_t radix_sort_pairs(unsigned long long* keys, uint32_t* vals, long long n, int bits,
+                             unsigned long long* keys_tmp, uint32_t* vals_tmp, int32_t* hist,
+                             int32_t* scan_tmp, cudaStream_t st);
+
+// power cells of the emitted cells (rpd_powercell.cu)
+struct PowerCellParams {
+  const rpd_cell_header* cells;
+  long long n;
+  const uint8_t* payload;
+  const rpd_topo_header* topo_h;
+  const uint8_t* topo;
+  int max_sf_fid;
+  int32_t* cnt;           // 5 x n: tet faces, facets, edges, vertices, surface faces
+  const long long* off;   // 5 x (n + 1), their exclusive scans
+  // tet faces: fid per cell (ascending), and (site, fid) keys / cell values
+  int32_t* tf_fid;
+  unsigned long long* tf_key;
+  uint32_t* tf_val;
+  // facets: (site, neighbour) keys, cell values
+  unsigned long long* fa_key;
+  uint32_t* fa_val;
+  // edges: keys / values for the sorts, fields by record, sorted output (7 per edge)
+  unsigned long long* ed_key;
+  uint32_t* ed_val;
+  int32_t *ed_site, *ed_n0, *ed_n1, *ed_cell, *ed_lv0, *ed_lv1;
+  int32_t* ed_out;
+  // vertices
+  int32_t *vx_cell, *vx_lvid, *vx_ids, *vx_sfid;
+  float* vx_pos;
+  // surface faces
+  int32_t *sf_cell, *sf_fid;
+  float* sf_pos;
+  // neighbour cells (CSR per cell)
+  int32_t *nbr_cnt, *nbr_fill, *nbr;
+  const long long* nbr_off;
+  // cells by site
+  unsigned long long* site_key;
+  uint32_t* site_val;
+};
+cudaError_t pc_count(const PowerCellParams& p, cudaStream_t st);
+cudaError_t pc_fill(const PowerCellParams& p, cudaStream_t st);
+cudaError_t pc_edges_finish(const PowerCellParams& p, long long n_ed, int pass, cudaStream_t st);
+cudaError_t pc_neighbours(const PowerCellParams& p, long long n_tf, int pass, cudaStream_t st);
+cudaError_t pc_site_offsets(const unsigned long long* keys, long long n, int n_site, int shift,
+                            long long* off, cudaStream_t st);
+
 // distance to local medial primitives (rpd_dist2mat.cu): ids checked first
 // (*bad counts offending primitives / samples)
 cudaError_t check_dist2mat(const int3* prims, long long n_prims, int n_spheres,

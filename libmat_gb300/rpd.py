@@ -54,7 +54,8 @@ EXPORTS = [
     "rpd_get_config", "rpd_set_config", "rpd_get_mesh_info",
     "rpd_topo_bytes", "rpd_compute_topology", "rpd_get_topology", "rpd_copy_topology_to_host",
     "rpd_compute_polygons", "rpd_get_polygons", "rpd_copy_polygons_to_host", "rpd_dist2mat",
-    "rpd_compute_partial",
+    "rpd_compute_partial", "rpd_compute_power_cells", "rpd_get_power_cells",
+    "rpd_copy_device_to_host",
     "rpd_batch_create", "rpd_batch_destroy", "rpd_batch_last_error", "rpd_batch_add_mesh",
     "rpd_batch_size", "rpd_batch_set_graph", "rpd_batch_compute", "rpd_batch_autotune",
     "rpd_batch_mesh_cells", "rpd_batch_copy_mesh_cells", "rpd_batch_context",
@@ -79,6 +80,21 @@ class MeshInfo(ctypes.Structure):
                 ("lo", ctypes.c_double * 3), ("hi", ctypes.c_double * 3),
                 ("volume", ctypes.c_double), ("tet_radius", ctypes.c_double),
                 ("class_count", ctypes.c_int32 * 2), ("class_radius", ctypes.c_double * 2)]
+
+
+class PowerCellsView(ctypes.Structure):
+    _fields_ = [("n_site", ctypes.c_int32), ("n_cells", ctypes.c_int64)] + [
+        (f, ctypes.c_void_p) for f in ("site_cell_off", "site_cells", "cell_nbr_off", "cell_nbrs",
+                                       "cell_tfid_off", "cell_tfids")] + [
+        ("n_facets", ctypes.c_int64)] + [
+        (f, ctypes.c_void_p) for f in ("site_facet_off", "facet_keys", "facet_cells")] + [
+        ("n_edges", ctypes.c_int64)] + [(f, ctypes.c_void_p) for f in ("site_edge_off", "edges")] + [
+        ("n_vertices", ctypes.c_int64)] + [
+        (f, ctypes.c_void_p) for f in ("cell_vertex_off", "vertex_cell", "vertex_lvid", "vertex_ids",
+                                       "vertex_pos", "vertex_sfid")] + [
+        ("n_surface", ctypes.c_int64)] + [
+        (f, ctypes.c_void_p) for f in ("cell_surface_off", "surface_cell", "surface_fid",
+                                       "surface_pos")]
 
 
 class Stats(ctypes.Structure):
@@ -213,6 +229,12 @@ def load(path=LIB_PATH):
     L.rpd_get_topology.argtypes = [vp, vp]
     L.rpd_copy_topology_to_host.restype = i32
     L.rpd_copy_topology_to_host.argtypes = [vp, vp, i64, vp, i64, c.POINTER(i64), c.POINTER(i64)]
+    L.rpd_compute_power_cells.restype = i32
+    L.rpd_compute_power_cells.argtypes = [vp, i32, c.POINTER(c.c_float)]
+    L.rpd_get_power_cells.restype = i32
+    L.rpd_get_power_cells.argtypes = [vp, c.POINTER(PowerCellsView)]
+    L.rpd_copy_device_to_host.restype = i32
+    L.rpd_copy_device_to_host.argtypes = [vp, vp, vp, i64]
     L.rpd_compute_partial.restype = i32
     L.rpd_compute_partial.argtypes = [vp, vp, c.POINTER(Stats)]
     L.rpd_dist2mat.restype = i32
@@ -534,6 +556,49 @@ class RPD:
         self._check(self._L.rpd_copy_topology_to_host(self._h, _p(h), h.shape[0], _p(r), r.nbytes,
                                                       ctypes.byref(n), ctypes.byref(b)))
         return h[:n.value], r[:b.value]
+
+    def compute_power_cells(self, max_sf_fid=-1):
+        """The power cells of the emitted cells on the device (libmat's
+        get_all_voro_info); returns the device time in ms."""
+        ms = ctypes.c_float()
+        self._check(self._L.rpd_compute_power_cells(self._h, int(max_sf_fid), ctypes.byref(ms)))
+        return ms.value
+
+    def _d2h(self, ptr, dtype, count):
+        out = np.zeros(max(int(count), 1), dtype)
+        if count > 0:
+            self._check(self._L.rpd_copy_device_to_host(self._h, _p(out), ptr, out.nbytes))
+        return out[:int(count)]
+
+    def power_cells(self):
+        """The power cells copied to the host: dict of numpy arrays named as
+        the fields of rpd_power_cells_view."""
+        v = PowerCellsView()
+        self._check(self._L.rpd_get_power_cells(self._h, ctypes.byref(v)))
+        ns, n = v.n_site, v.n_cells
+        d = {}
+        d["site_cell_off"] = self._d2h(v.site_cell_off, np.int64, ns + 1)
+        d["site_cells"] = self._d2h(v.site_cells, np.uint32, n)
+        d["cell_nbr_off"] = self._d2h(v.cell_nbr_off, np.int64, n + 1)
+        d["cell_nbrs"] = self._d2h(v.cell_nbrs, np.int32, d["cell_nbr_off"][-1])
+        d["cell_tfid_off"] = self._d2h(v.cell_tfid_off, np.int64, n + 1)
+        d["cell_tfids"] = self._d2h(v.cell_tfids, np.int32, d["cell_tfid_off"][-1])
+        d["site_facet_off"] = self._d2h(v.site_facet_off, np.int64, ns + 1)
+        d["facet_keys"] = self._d2h(v.facet_keys, np.uint64, v.n_facets)
+        d["facet_cells"] = self._d2h(v.facet_cells, np.uint32, v.n_facets)
+        d["site_edge_off"] = self._d2h(v.site_edge_off, np.int64, ns + 1)
+        d["edges"] = self._d2h(v.edges, np.int32, 7 * v.n_edges).reshape(-1, 7)
+        d["cell_vertex_off"] = self._d2h(v.cell_vertex_off, np.int64, n + 1)
+        d["vertex_cell"] = self._d2h(v.vertex_cell, np.int32, v.n_vertices)
+        d["vertex_lvid"] = self._d2h(v.vertex_lvid, np.int32, v.n_vertices)
+        d["vertex_ids"] = self._d2h(v.vertex_ids, np.int32, 3 * v.n_vertices).reshape(-1, 3)
+        d["vertex_pos"] = self._d2h(v.vertex_pos, np.float32, 3 * v.n_vertices).reshape(-1, 3)
+        d["vertex_sfid"] = self._d2h(v.vertex_sfid, np.int32, v.n_vertices)
+        d["cell_surface_off"] = self._d2h(v.cell_surface_off, np.int64, n + 1)
+        d["surface_cell"] = self._d2h(v.surface_cell, np.int32, v.n_surface)
+        d["surface_fid"] = self._d2h(v.surface_fid, np.int32, v.n_surface)
+        d["surface_pos"] = self._d2h(v.surface_pos, np.float32, 3 * v.n_surface).reshape(-1, 3)
+        return d
 
     def compute_partial(self, recompute):
         """Recomputes the cells of the sites with recompute[i] != 0 and
