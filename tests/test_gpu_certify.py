@@ -82,3 +82,25 @@ def test_autotune_keeps_cells():
         r.compute()
         assert np.array_equal(r.topology_hashes(), base)
         assert np.array_equal(r.pair_headers()["status"], hb["status"])
+
+
+def test_longest_lists_and_no_geometry():
+    """k = 128 (the longest GPU-built list) with the certificate against the
+    plain path, and the clipping without the FP64 geometry pass: the same
+    cells."""
+    cfg = W.config_ellipsoid(target_tets=30000, n_site=2000, seed=25)
+    with engine(cfg, knn_k=128, predicate_mode=rpd.PRED_FP64) as r:
+        r.compute()
+        hp = r.pair_headers()
+        tp = r.topology_hashes()
+    with engine(cfg, knn_k=128, predicate_mode=rpd.PRED_FP32_FILTER, certify=True) as r:
+        r.compute()
+        hf = r.pair_headers()
+        tf = r.topology_hashes()
+        r.configure(compute_geometry=0)
+        r.compute()
+        hg = r.pair_headers()
+        tg = r.topology_hashes()
+    assert np.array_equal(hp["status"], hf["status"]) and np.array_equal(tp, tf)
+    assert np.array_equal(hg["status"], hf["status"]) and np.array_equal(tg, tf)
+    assert np.all(hg["volume"] == 0.0)

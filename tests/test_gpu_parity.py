@@ -83,12 +83,12 @@ def test_volume_partition_complete_lists(golden_cases):
     assert np.allclose(per_tet, tet_volumes(c["vert3d"], c["tets"]), rtol=1e-6)
 
 
+@pytest.mark.parametrize("k", [32, 64, 128])
 @pytest.mark.parametrize("order", [rpd.ORDER_DISTANCE, rpd.ORDER_SITE_ID])
-def test_knn_matches_oracle(order):
+def test_knn_matches_oracle(order, k):
     for cfg in (W.config_small_cube(n=6, n_site=300, seed=4),
                 W.config_ellipsoid(target_tets=20000, n_site=3000, seed=9)):
         s4f = cfg["sites"].astype(np.float32)
-        k = 64
         with rpd.RPD(neighbor_source=rpd.NEIGH_KNN, knn_k=k, clip_order=order) as r:
             adj = rpd.mesh_adjacency(cfg["vert3d"].shape[0], cfg["tets"])
             r.set_mesh(cfg["vert3d"], cfg["tets"], adj["v_adjs"], adj["e_adj6"],
