@@ -475,6 +475,11 @@ __device__ __forceinline__ float pow_dist(float4 s, float3 v) {
 
 constexpr int kPairWarps = 4;
 constexpr int kPairMaxK = 128;  // longest neighbour list (rpd_config.knn_k <= 128)
+// the rule in two parts: each lane tries its own tet against the first
+// kRuleFirst neighbours; the tets that survive wait in a per-warp queue
+// (kRuleQueue entries) and are finished 32 at a time, one per lane
+constexpr int kRuleFirst = 8;
+constexpr int kRuleQueue = 64;
 
 // cell range of the site's box in the tet grid (empty range for no box)
 struct CellRange {
@@ -517,6 +522,9 @@ __global__ void __launch_bounds__(kPairWarps * 32) pairs_kernel(PairParams p,
                                                                 unsigned long long* work) {
   __shared__ float4 spl[kPairWarps][kBoxPlanes];
   __shared__ float4 snb[kPairWarps][kPairMaxK];  // the site's neighbours (rule order)
+  // queued tets: vertices (12 floats), power distances to the site (4), id
+  __shared__ float sq_v[kPairWarps][16][kRuleQueue];
+  __shared__ int sq_t[kPairWarps][kRuleQueue];
   const int lane = threadIdx.x & 31;
   const int wid = threadIdx.x >> 5;
   const long long n_tasks = task_off[p.n_site];
@@ -565,6 +573,12 @@ __global__ void __launch_bounds__(kPairWarps * 32) pairs_kernel(PairParams p,
       nb[r] = m < 0 ? make_float4(0.f, 0.f, 0.f, -INFINITY) : __ldg(p.site4f + m);
     }
     __syncwarp();
+    // neighbour r of the rule order (staged, or read for long user lists)
+    auto rule_site = [&](int r) -> float4 {
+      if (r < k_staged) return nb[r];
+      const int m = __ldg(L + r);
+      return m < 0 ? make_float4(0.f, 0.f, 0.f, -INFINITY) : __ldg(p.site4f + m);
+    };
     n_cells_seen += n_iter;
     // half extent of a grid cell, grown for the rounding of the binning
     const float hc = 0.5f * g.cell * (1.0f + 1e-3f) + 1e-6f * p.coord_scale;
@@ -584,8 +598,59 @@ __global__ void __launch_bounds__(kPairWarps * 32) pairs_kernel(PairParams p,
       ++n_keep;
       return x + g.nx * (y + g.ny * z);
     };
-    for_items(n_iter, cell_at, p.tcell_start, p.tcell_items, lane, [&](int t, bool valid) {
+    // a tet that passed the rule becomes a pair
+    auto emit = [&](bool pass, int t) {
+      uint32_t msk = __ballot_sync(0xffffffffu, pass);
+      if (msk) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(p.pair_cursor, (unsigned long long)__popc(msk));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (pass) {
+          unsigned long long slot = base + __popc(msk & ((1u << lane) - 1u));
+          if ((long long)slot < p.pair_cap)
+            p.pair_buf[slot] = make_int2(t + p.tet_base, i + p.site_base);
+          atomicAdd(p.tet_count + p.tet_base + t, 1);
+        }
+      }
+    };
+    float(*qv)[kRuleQueue] = sq_v[wid];
+    int* qt = sq_t[wid];
+    int qn = 0;  // queued tets (warp-uniform)
+    // the first n queued tets, one per lane, against the rest of the list;
+    // the others move to the front
+    auto drain = [&](int n) {
       bool pass = false;
+      int t = -1;
+      if (lane < n) {
+        float3 v[4];
+        float pdi[4];
+        for (int a = 0; a < 4; ++a) {
+          v[a] = make_float3(qv[3 * a][lane], qv[3 * a + 1][lane], qv[3 * a + 2][lane]);
+          pdi[a] = qv[12 + a][lane];
+        }
+        t = qt[lane];
+        pass = true;
+        for (int r = kRuleFirst; r < p.k && pass; ++r) {
+          const float4 sm = rule_site(r);
+          bool hit = false;
+          for (int a = 0; a < 4; ++a) hit |= pow_dist(sm, v[a]) > pdi[a];
+          pass = hit;
+        }
+      }
+      emit(pass, t);
+      __syncwarp();
+      const int rest = qn - n;  // < 32: sources n.., targets 0.. do not overlap
+      if (lane < rest) {
+        for (int w = 0; w < 16; ++w) qv[w][lane] = qv[w][n + lane];
+        qt[lane] = qt[n + lane];
+      }
+      __syncwarp();
+      qn = rest;
+    };
+    for_items(n_iter, cell_at, p.tcell_start, p.tcell_items, lane, [&](int t, bool valid) {
+      bool pass = false, survive = false;
+      float3 v[4] = {};
+      float pdi[4] = {};
       if (valid) {
         ++n_items;
         float4 c = p.centroid[t];
@@ -599,39 +664,46 @@ __global__ void __launch_bounds__(kPairWarps * 32) pairs_kernel(PairParams p,
           ++n_in;
           const float4 q0 = __ldg(p.tet_xyz + 3ll * t), q1 = __ldg(p.tet_xyz + 3ll * t + 1),
                        q2 = __ldg(p.tet_xyz + 3ll * t + 2);
-          const float3 v[4] = {make_float3(q0.x, q0.y, q0.z), make_float3(q0.w, q1.x, q1.y),
-                               make_float3(q1.z, q1.w, q2.x), make_float3(q2.y, q2.z, q2.w)};
-          float pdi[4];
+          v[0] = make_float3(q0.x, q0.y, q0.z);
+          v[1] = make_float3(q0.w, q1.x, q1.y);
+          v[2] = make_float3(q1.z, q1.w, q2.x);
+          v[3] = make_float3(q2.y, q2.z, q2.w);
           for (int a = 0; a < 4; ++a) pdi[a] = pow_dist(si, v[a]);
+          // voronoi.cu:154-193 (holes, -1, never reject: voronoi.cu:171):
+          // a candidate iff every neighbour m has a tet vertex where
+          // pd_m > pd_i; the order of the neighbours does not matter
           pass = true;
-          // voronoi.cu:154-193; holes (-1) are skipped (voronoi.cu:171)
-          for (int r = 0; r < p.k && pass; ++r) {
-            float4 sm;
-            if (r < k_staged) {
-              sm = nb[r];
-            } else {  // lists longer than the staging (user lists)
-              const int m = __ldg(L + r);
-              sm = m < 0 ? make_float4(0.f, 0.f, 0.f, -INFINITY) : __ldg(p.site4f + m);
-            }
+          for (int r = 0; r < min(p.k, kRuleFirst) && pass; ++r) {
+            const float4 sm = rule_site(r);
             bool hit = false;
             for (int a = 0; a < 4; ++a) hit |= pow_dist(sm, v[a]) > pdi[a];
             pass = hit;
           }
+          if (pass && p.k > kRuleFirst) {
+            survive = true;
+            pass = false;
+          }
         }
       }
-      uint32_t msk = __ballot_sync(0xffffffffu, pass);
-      if (msk) {
-        unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(p.pair_cursor, (unsigned long long)__popc(msk));
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (pass) {
-          unsigned long long slot = base + __popc(msk & ((1u << lane) - 1u));
-          if ((long long)slot < p.pair_cap)
-            p.pair_buf[slot] = make_int2(t + p.tet_base, i + p.site_base);
-          atomicAdd(p.tet_count + p.tet_base + t, 1);
+      // (the whole warp from here) survivors join the queue: qn <= 31
+      // before, so there is room for 32 more
+      const uint32_t sv = __ballot_sync(0xffffffffu, survive);
+      if (survive) {
+        const int pos = qn + __popc(sv & ((1u << lane) - 1u));
+        for (int a = 0; a < 4; ++a) {
+          qv[3 * a][pos] = v[a].x;
+          qv[3 * a + 1][pos] = v[a].y;
+          qv[3 * a + 2][pos] = v[a].z;
+          qv[12 + a][pos] = pdi[a];
         }
+        qt[pos] = t;
       }
+      qn += __popc(sv);
+      emit(pass, t);
+      __syncwarp();
+      if (qn >= 32) drain(32);
     });
+    if (qn > 0) drain(qn);
   }
   if (p.diag) {
     n_keep = __reduce_add_sync(0xffffffffu, n_keep);
