@@ -350,9 +350,35 @@ rpd_status rpd_copy_topology_to_host(struct rpd_ctx* ctx, rpd_topo_header* heade
  *                                     max_sf_fid: cell, face id, centroid of
  *                                     its vertex cycle (cell_to_surfv2fid);
  *                                     per cell from cell_surface_off
- * Feature-edge records (TetMesh::tet_es2fe_map) are not part of it.  Computes
- * the per-cell topology first when needed. */
+ *   se_covered, ce_covered            with feature edges set
+ *                                     (rpd_set_feature_edges), 5 int32 per
+ *                                     record: cell, the two vertices (slot
+ *                                     order) on both faces of an active tet
+ *                                     edge that the map lists as sharp
+ *                                     (fe_type 1) or concave (2), fe_line_id,
+ *                                     fe_id (se_covered_lvids,
+ *                                     ce_covered_lvids); per cell from
+ *                                     cell_*_covered_off, sorted, unique
+ *   se_line_end, se_line_end_pos      for each of those two vertices (any
+ *                                     fe_type) with a bisector among its
+ *                                     planes: cell, vertex slot, the first
+ *                                     such bisector's neighbour site,
+ *                                     fe_line_id, and the float position
+ *                                     (se_line_endpos); per cell from
+ *                                     cell_se_line_end_off, sorted, unique
+ * Computes the per-cell topology first when needed. */
 rpd_status rpd_compute_power_cells(struct rpd_ctx* ctx, int max_sf_fid, float* ms);
+
+/* libmat's TetMesh::tet_es2fe_map (<tid, lfid_min, lfid_max> -> <fe_type,
+ * fe_id, fe_line_id>, src/rpd3d_base/rpd_update.cxx:77-82), one record per
+ * key; lf_min < lf_max are local faces (0..3) of tet tet_id.  Of records
+ * with the same key the last one counts (a map's last assignment).  Used by
+ * the following rpd_compute_power_cells calls; n = 0 clears it. */
+typedef struct rpd_feature_edge {
+  int32_t tet_id, lf_min, lf_max;
+  int32_t fe_type, fe_id, fe_line_id; /* fe_type: 1 sharp (SE), 2 concave (CE) */
+} rpd_feature_edge;
+rpd_status rpd_set_feature_edges(struct rpd_ctx* ctx, const rpd_feature_edge* edges, int64_t n);
 
 typedef struct rpd_power_cells_view {
   int32_t n_site;
@@ -382,6 +408,16 @@ typedef struct rpd_power_cells_view {
   const int32_t* surface_cell;
   const int32_t* surface_fid;
   const float* surface_pos;   /* 3 per face */
+  int64_t n_se_covered;
+  const int64_t* cell_se_covered_off;
+  const int32_t* se_covered;  /* 5 per record */
+  int64_t n_ce_covered;
+  const int64_t* cell_ce_covered_off;
+  const int32_t* ce_covered;  /* 5 per record */
+  int64_t n_se_line_end;
+  const int64_t* cell_se_line_end_off;
+  const int32_t* se_line_end;       /* 4 per record */
+  const float* se_line_end_pos;     /* 3 per record */
 } rpd_power_cells_view;
 rpd_status rpd_get_power_cells(struct rpd_ctx* ctx, rpd_power_cells_view* view);
 

@@ -1042,6 +1042,47 @@ rpd_status rpd_copy_topology_to_host(rpd_ctx* c, rpd_topo_header* headers, int64
 }
 
 // ---- power cells of the emitted cells -------------------------------------
+rpd_status rpd_set_feature_edges(rpd_ctx* c, const rpd_feature_edge* fe, int64_t n) {
+  if (!c) return RPD_ERR_INVALID_ARGUMENT;
+  if (n < 0 || (n > 0 && !fe)) return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_set_feature_edges: bad arguments");
+  for (int64_t i = 0; i < n; ++i)
+    if (fe[i].tet_id < 0 || fe[i].lf_min < 0 || fe[i].lf_min >= fe[i].lf_max || fe[i].lf_max > 3)
+      return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_set_feature_edges: bad tet id or local faces");
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  // keys in ascending order; of equal keys the last record (a map's last
+  // assignment)
+  std::vector<unsigned long long> key((size_t)n);
+  for (int64_t i = 0; i < n; ++i)
+    key[i] = ((unsigned long long)(uint32_t)fe[i].tet_id << 4) | (unsigned)(fe[i].lf_min << 2) |
+             (unsigned)fe[i].lf_max;
+  std::vector<int64_t> order((size_t)n);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return key[a] < key[b]; });
+  std::vector<unsigned long long> uk;
+  std::vector<int32_t> uv;
+  for (size_t j = 0; j < order.size(); ++j) {
+    if (j + 1 < order.size() && key[order[j + 1]] == key[order[j]]) continue;
+    const rpd_feature_edge& r = fe[order[j]];
+    uk.push_back(key[order[j]]);
+    uv.push_back(r.fe_type);
+    uv.push_back(r.fe_id);
+    uv.push_back(r.fe_line_id);
+  }
+  const long long m = (long long)uk.size();
+  CK(c->fe_keys.ensure((size_t)std::max(m, 1ll)), "alloc");
+  CK(c->fe_vals.ensure((size_t)std::max(3 * m, 3ll)), "alloc");
+  if (m > 0) {
+    CK(cudaMemcpyAsync(c->fe_keys.ptr, uk.data(), sizeof(unsigned long long) * (size_t)m,
+                       cudaMemcpyHostToDevice, c->stream), "H2D");
+    CK(cudaMemcpyAsync(c->fe_vals.ptr, uv.data(), sizeof(int32_t) * (size_t)(3 * m),
+                       cudaMemcpyHostToDevice, c->stream), "H2D");
+  }
+  CK(cudaStreamSynchronize(c->stream), "sync");
+  c->n_fe = m;
+  c->has_power_cells = false;
+  return RPD_OK;
+}
+
 rpd_status rpd_compute_power_cells(rpd_ctx* c, int max_sf_fid, float* ms) {
   if (!c) return RPD_ERR_INVALID_ARGUMENT;
   if (!c->has_result) return fail(c, RPD_ERR_NOT_READY, "rpd_compute_power_cells: no result");
@@ -1055,8 +1096,8 @@ rpd_status rpd_compute_power_cells(rpd_ctx* c, int max_sf_fid, float* ms) {
   const int n_site = c->n_site;
   if (n > 0x7fffffffll) return fail(c, RPD_ERR_CAPACITY, "rpd_compute_power_cells: too many cells");
   CK(cudaEventRecord(c->ev[kEvTopo0], st), "event");
-  CK(c->pc_cnt.ensure((size_t)std::max(5 * n, 5ll)), "alloc");
-  CK(c->pc_off.ensure((size_t)(5 * (n + 1))), "alloc");
+  CK(c->pc_cnt.ensure((size_t)std::max(8 * n, 8ll)), "alloc");
+  CK(c->pc_off.ensure((size_t)(8 * (n + 1))), "alloc");
   CK(c->pc_scan.ensure(scan64_temp(std::max(n, 1ll)) + 16), "alloc");
   PowerCellParams p = {};
   p.cells = c->cells.ptr;
@@ -1067,16 +1108,25 @@ rpd_status rpd_compute_power_cells(rpd_ctx* c, int max_sf_fid, float* ms) {
   p.max_sf_fid = max_sf_fid;
   p.cnt = c->pc_cnt.ptr;
   p.off = c->pc_off.ptr;
+  p.fe_keys = c->fe_keys.ptr;
+  p.fe_vals = c->fe_vals.ptr;
+  p.n_fe = c->n_fe;
   CK(pc_count(p, st), "power cell counts");
-  for (int k = 0; k < 5; ++k)
+  // feature-edge rows only with a map set; else their offsets are all 0
+  const int n_rows = c->n_fe > 0 ? 8 : 5;
+  if (c->n_fe > 0) CK(pc_feature_edges(p, 0, st), "feature edge counts");
+  else CK(cudaMemsetAsync(c->pc_off.ptr + 5 * (n + 1), 0, sizeof(long long) * (size_t)(3 * (n + 1)), st),
+          "memset");
+  for (int k = 0; k < n_rows; ++k)
     CK(scan64_exclusive(c->pc_cnt.ptr + k * n, c->pc_off.ptr + k * (n + 1), n, c->pc_scan.ptr, st),
        "power cell scan");
-  long long tot[5];
-  for (int k = 0; k < 5; ++k)
+  long long tot[8];
+  for (int k = 0; k < 8; ++k)
     CK(cudaMemcpyAsync(&tot[k], c->pc_off.ptr + k * (n + 1) + n, sizeof(long long),
                        cudaMemcpyDeviceToHost, st), "D2H");
   CK(cudaStreamSynchronize(st), "sync");
   const long long n_tf = tot[0], n_fa = tot[1], n_ed = tot[2], n_vx = tot[3], n_sf = tot[4];
+  const long long n_se = tot[5], n_ce = tot[6], n_end = tot[7];
   // key / value segments: tet faces, facets, edges, sites
   const long long seg[4] = {n_tf, n_fa, n_ed, n};
   const long long n_keys = n_tf + n_fa + n_ed + n;
@@ -1100,6 +1150,8 @@ rpd_status rpd_compute_power_cells(rpd_ctx* c, int max_sf_fid, float* ms) {
   CK(c->pc_nbr_cnt.ensure((size_t)std::max(n, 1ll)), "alloc");
   CK(c->pc_nbr_fill.ensure((size_t)std::max(n, 1ll)), "alloc");
   CK(c->pc_nbr_off.ensure((size_t)n + 1), "alloc");
+  CK(c->pc_fe_i.ensure((size_t)std::max(5 * n_se + 5 * n_ce + 4 * n_end, 1ll)), "alloc");
+  CK(c->pc_fe_pos.ensure((size_t)std::max(3 * n_end, 3ll)), "alloc");
   unsigned long long* keys[4];
   uint32_t* vals[4];
   long long at = 0;
@@ -1138,6 +1190,11 @@ rpd_status rpd_compute_power_cells(rpd_ctx* c, int max_sf_fid, float* ms) {
   p.nbr_fill = c->pc_nbr_fill.ptr;
   p.nbr_off = c->pc_nbr_off.ptr;
   CK(pc_fill(p, st), "power cell records");
+  p.se = c->pc_fe_i.ptr;
+  p.ce = p.se + 5 * n_se;
+  p.se_end = p.ce + 5 * n_ce;
+  p.se_end_pos = c->pc_fe_pos.ptr;
+  if (n_se + n_ce + n_end > 0) CK(pc_feature_edges(p, 1, st), "feature edge records");
   // stable sorts: by (site, key) for faces and facets; edges by the
   // neighbour pair, then by site; cells by site
   int site_bits = 1;
@@ -1200,6 +1257,16 @@ rpd_status rpd_compute_power_cells(rpd_ctx* c, int max_sf_fid, float* ms) {
   v.surface_cell = p.sf_cell;
   v.surface_fid = p.sf_fid;
   v.surface_pos = p.sf_pos;
+  v.n_se_covered = n_se;
+  v.cell_se_covered_off = reinterpret_cast<const int64_t*>(c->pc_off.ptr + 5 * (n + 1));
+  v.se_covered = p.se;
+  v.n_ce_covered = n_ce;
+  v.cell_ce_covered_off = reinterpret_cast<const int64_t*>(c->pc_off.ptr + 6 * (n + 1));
+  v.ce_covered = p.ce;
+  v.n_se_line_end = n_end;
+  v.cell_se_line_end_off = reinterpret_cast<const int64_t*>(c->pc_off.ptr + 7 * (n + 1));
+  v.se_line_end = p.se_end;
+  v.se_line_end_pos = p.se_end_pos;
   c->pc_n_nbr = n_nbr;
   c->has_power_cells = true;
   return RPD_OK;

@@ -167,6 +167,12 @@ struct rpd_ctx {
   DevBuf<unsigned long long> pc_keys, pc_keys_tmp;
   DevBuf<uint32_t> pc_vals, pc_vals_tmp;
   DevBuf<float> pc_vx_pos, pc_sf_pos;
+  DevBuf<int32_t> pc_fe_i;
+  DevBuf<float> pc_fe_pos;
+  // TetMesh::tet_es2fe_map: sorted unique keys and (type, id, line) values
+  DevBuf<unsigned long long> fe_keys;
+  DevBuf<int32_t> fe_vals;
+  long long n_fe = 0;
   long long pc_n[5] = {0, 0, 0, 0, 0};
   long long pc_n_nbr = 0;
   bool has_power_cells = false;

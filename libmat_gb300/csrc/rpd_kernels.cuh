@@ -269,8 +269,9 @@ struct PowerCellParams {
   const rpd_topo_header* topo_h;
   const uint8_t* topo;
   int max_sf_fid;
-  int32_t* cnt;           // 5 x n: tet faces, facets, edges, vertices, surface faces
-  const long long* off;   // 5 x (n + 1), their exclusive scans
+  int32_t* cnt;           // 8 x n: tet faces, facets, edges, vertices, surface faces,
+                          // sharp edges, concave edges, sharp-line endpoints
+  const long long* off;   // 8 x (n + 1), their exclusive scans
   // tet faces: fid per cell (ascending), and (site, fid) keys / cell values
   int32_t* tf_fid;
   unsigned long long* tf_key;
@@ -295,10 +296,19 @@ struct PowerCellParams {
   // cells by site
   unsigned long long* site_key;
   uint32_t* site_val;
+  // feature edges: sorted unique keys (tet << 4 | lf_min << 2 | lf_max) and
+  // (fe_type, fe_id, fe_line_id) per key; records 5, 5, 4 int32 + 3 floats
+  const unsigned long long* fe_keys;
+  const int32_t* fe_vals;
+  long long n_fe;
+  int32_t *se, *ce, *se_end;
+  float* se_end_pos;
 };
 cudaError_t pc_count(const PowerCellParams& p, cudaStream_t st);
 cudaError_t pc_fill(const PowerCellParams& p, cudaStream_t st);
 cudaError_t pc_edges_finish(const PowerCellParams& p, long long n_ed, int pass, cudaStream_t st);
+// feature-edge counts (fill = 0, into cnt rows 5..7) or records (fill = 1)
+cudaError_t pc_feature_edges(const PowerCellParams& p, int fill, cudaStream_t st);
 cudaError_t pc_neighbours(const PowerCellParams& p, long long n_tf, int pass, cudaStream_t st);
 cudaError_t pc_site_offsets(const unsigned long long* keys, long long n, int n_site, int shift,
                             long long* off, cudaStream_t st);

@@ -17,6 +17,17 @@
 // each kind (count, 64-bit scan, fill), and stable radix sorts put the
 // keyed ones into the maps' order: by site, then key, then cell.
 //
+// With TetMesh::tet_es2fe_map given (sorted unique keys tet << 4 | lf_min
+// << 2 | lf_max, rpd_set_feature_edges), the feature-edge records of
+// rpd_update.cxx:206-254 too: for every active edge of the cell between two
+// faces of its tet that the map lists, {cell, the edge's two vertices, line,
+// fe id} for sharp (se_covered_lvids) and concave (ce_covered_lvids) edges,
+// and for each of the two vertices with a bisector among its planes the
+// first such bisector's site, the line and the vertex position
+// (se_line_endpos).  A record depends only on the pair of faces, so a cell
+// has at most 6 of each kind and 12 endpoints, sorted and made unique per
+// cell by one thread.
+//
 // Compiled with -fmad=false (the float positions and centroids are the
 // reference's host float arithmetic).
 
@@ -98,6 +109,150 @@ __device__ __forceinline__ int vertex_neighbours(const PcCell& c, int t, int max
     }
   }
   return n;
+}
+
+// index of key in the sorted feature-edge keys, or -1
+__device__ __forceinline__ long long fe_find(const PowerCellParams& p, unsigned long long key) {
+  long long lo = 0, hi = p.n_fe;
+  while (lo < hi) {
+    const long long mid = (lo + hi) >> 1;
+    if (p.fe_keys[mid] < key) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo < p.n_fe && p.fe_keys[lo] == key ? lo : -1;
+}
+
+template <int N>
+__device__ __forceinline__ bool lex_less(const int (&a)[N], const int (&b)[N]) {
+  for (int i = 0; i < N; ++i)
+    if (a[i] != b[i]) return a[i] < b[i];
+  return false;
+}
+
+// sorts rec[0, n) ascending and drops repeats; returns the new count
+template <int N, int M>
+__device__ int sort_unique(int (&rec)[M][N], int n) {
+  for (int a = 1; a < n; ++a)
+    for (int b = a; b > 0 && lex_less(rec[b], rec[b - 1]); --b)
+      for (int i = 0; i < N; ++i) {
+        const int t = rec[b][i];
+        rec[b][i] = rec[b - 1][i];
+        rec[b - 1][i] = t;
+      }
+  int m = 0;
+  for (int a = 0; a < n; ++a) {
+    bool same = m > 0;
+    for (int i = 0; i < N && same; ++i) same = rec[m - 1][i] == rec[a][i];
+    if (same) continue;
+    for (int i = 0; i < N; ++i) rec[m][i] = rec[a][i];
+    ++m;
+  }
+  return m;
+}
+
+struct FeCell {
+  int nse, nce, nend;
+  int se[6][4], ce[6][4];  // lvid1, lvid2, fe_line_id, fe_id
+  int end[12][3];          // lvid, neighbour site, fe_line_id
+};
+
+// the feature-edge records of cell q (without the cell id), sorted and unique
+__device__ void fe_cell(const PowerCellParams& p, const PcCell& c, int tet, FeCell& o) {
+  o.nse = o.nce = o.nend = 0;
+  if (p.n_fe <= 0) return;
+  // pairs of tet faces (both without a neighbour site) joined by an active edge
+  uint32_t pairs = 0;
+  for (int e = 0; e < c.ne; ++e) {
+    if (!c.acte[e]) continue;
+    const uchar4 ed = c.edge[e];
+    const int a = ed.x < ed.y ? ed.x : ed.y, b = ed.x < ed.y ? ed.y : ed.x;
+    if (b >= 4 || a == b || c.id2[a].y != -1 || c.id2[b].y != -1) continue;
+    pairs |= 1u << (4 * a + b);
+  }
+  // face cycle offsets of the tet faces
+  int cyc[5];
+  cyc[0] = 0;
+  for (int f = 0; f < 4; ++f) cyc[f + 1] = cyc[f] + (f < c.np ? c.act[f] : 0);
+  while (pairs) {
+    const int bit = __ffs(pairs) - 1;
+    pairs &= pairs - 1;
+    const int a = bit >> 2, b = bit & 3;
+    const long long k = fe_find(p, ((unsigned long long)(uint32_t)tet << 4) | (unsigned)(a << 2) | (unsigned)b);
+    if (k < 0) continue;
+    const int type = p.fe_vals[3 * k], fid = p.fe_vals[3 * k + 1], line = p.fe_vals[3 * k + 2];
+    // the two smallest vertices on both faces' cycles
+    int lv0 = -1, lv1 = -1;
+    for (int i = cyc[a]; i < cyc[a + 1]; ++i) {
+      const int x = c.faces[i];
+      bool both = false;
+      for (int j = cyc[b]; j < cyc[b + 1]; ++j) both |= c.faces[j] == x;
+      if (!both || x == lv0 || x == lv1) continue;
+      if (lv0 < 0 || x < lv0) {
+        lv1 = lv0;
+        lv0 = x;
+      } else if (lv1 < 0 || x < lv1) {
+        lv1 = x;
+      }
+    }
+    if (type == 1 || type == 2) {
+      int(&r)[4] = type == 1 ? o.se[o.nse++] : o.ce[o.nce++];
+      r[0] = lv0;
+      r[1] = lv1;
+      r[2] = line;
+      r[3] = fid;
+    }
+    for (int v = 0; v < 2; ++v) {
+      const int lv = v == 0 ? lv0 : lv1;
+      if (lv < 0 || lv >= c.nv) continue;
+      const uchar4 vv = c.ver[lv];
+      for (int i = 0; i < 3; ++i) {
+        const int2 hp = c.id2[pid(c, plane_at(vv, i))];
+        if (hp.y == -1) continue;
+        o.end[o.nend][0] = lv;
+        o.end[o.nend][1] = neigh_of(hp, c.site);
+        o.end[o.nend][2] = line;
+        ++o.nend;
+        break;
+      }
+    }
+  }
+  o.nse = sort_unique(o.se, o.nse);
+  o.nce = sort_unique(o.ce, o.nce);
+  o.nend = sort_unique(o.end, o.nend);
+}
+
+__global__ void pc_fe_kernel(PowerCellParams p, int fill) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= p.n) return;
+  const PcCell c = pc_cell(p, q);
+  FeCell o;
+  fe_cell(p, c, p.cells[q].tet_id, o);
+  if (!fill) {
+    p.cnt[5 * p.n + q] = o.nse;
+    p.cnt[6 * p.n + q] = o.nce;
+    p.cnt[7 * p.n + q] = o.nend;
+    return;
+  }
+  const int cell = (int)q;
+  long long at = p.off[5 * (p.n + 1) + q];
+  for (int i = 0; i < o.nse; ++i, ++at) {
+    p.se[5 * at] = cell;
+    for (int j = 0; j < 4; ++j) p.se[5 * at + 1 + j] = o.se[i][j];
+  }
+  at = p.off[6 * (p.n + 1) + q];
+  for (int i = 0; i < o.nce; ++i, ++at) {
+    p.ce[5 * at] = cell;
+    for (int j = 0; j < 4; ++j) p.ce[5 * at + 1 + j] = o.ce[i][j];
+  }
+  at = p.off[7 * (p.n + 1) + q];
+  for (int i = 0; i < o.nend; ++i, ++at) {
+    p.se_end[4 * at] = cell;
+    for (int j = 0; j < 3; ++j) p.se_end[4 * at + 1 + j] = o.end[i][j];
+    const float3 x = vertex_pos(c, o.end[i][0]);
+    p.se_end_pos[3 * at] = x.x;
+    p.se_end_pos[3 * at + 1] = x.y;
+    p.se_end_pos[3 * at + 2] = x.z;
+  }
 }
 
 __global__ void pc_count_kernel(PowerCellParams p) {
@@ -332,6 +487,13 @@ cudaError_t pc_fill(const PowerCellParams& p, cudaStream_t st) {
   pc_fill_kernel<<<(unsigned)((p.n + 255) / 256), 256, 0, st>>>(p);
   pc_site_keys_kernel<<<(unsigned)((p.n + 255) / 256), 256, 0, st>>>(p);
   note_launches(2);
+  return cudaGetLastError();
+}
+
+cudaError_t pc_feature_edges(const PowerCellParams& p, int fill, cudaStream_t st) {
+  if (p.n <= 0) return cudaSuccess;
+  pc_fe_kernel<<<(unsigned)((p.n + 127) / 128), 128, 0, st>>>(p, fill);
+  note_launches(1);
   return cudaGetLastError();
 }
 

@@ -55,7 +55,7 @@ EXPORTS = [
     "rpd_topo_bytes", "rpd_compute_topology", "rpd_get_topology", "rpd_copy_topology_to_host",
     "rpd_compute_polygons", "rpd_get_polygons", "rpd_copy_polygons_to_host", "rpd_dist2mat",
     "rpd_compute_partial", "rpd_compute_power_cells", "rpd_get_power_cells",
-    "rpd_copy_device_to_host",
+    "rpd_set_feature_edges", "rpd_copy_device_to_host",
     "rpd_batch_create", "rpd_batch_destroy", "rpd_batch_last_error", "rpd_batch_add_mesh",
     "rpd_batch_size", "rpd_batch_set_graph", "rpd_batch_compute", "rpd_batch_autotune",
     "rpd_batch_mesh_cells", "rpd_batch_copy_mesh_cells", "rpd_batch_context",
@@ -94,7 +94,13 @@ class PowerCellsView(ctypes.Structure):
                                        "vertex_pos", "vertex_sfid")] + [
         ("n_surface", ctypes.c_int64)] + [
         (f, ctypes.c_void_p) for f in ("cell_surface_off", "surface_cell", "surface_fid",
-                                       "surface_pos")]
+                                       "surface_pos")] + [
+        ("n_se_covered", ctypes.c_int64)] + [
+        (f, ctypes.c_void_p) for f in ("cell_se_covered_off", "se_covered")] + [
+        ("n_ce_covered", ctypes.c_int64)] + [
+        (f, ctypes.c_void_p) for f in ("cell_ce_covered_off", "ce_covered")] + [
+        ("n_se_line_end", ctypes.c_int64)] + [
+        (f, ctypes.c_void_p) for f in ("cell_se_line_end_off", "se_line_end", "se_line_end_pos")]
 
 
 class Stats(ctypes.Structure):
@@ -233,6 +239,8 @@ def load(path=LIB_PATH):
     L.rpd_compute_power_cells.argtypes = [vp, i32, c.POINTER(c.c_float)]
     L.rpd_get_power_cells.restype = i32
     L.rpd_get_power_cells.argtypes = [vp, c.POINTER(PowerCellsView)]
+    L.rpd_set_feature_edges.restype = i32
+    L.rpd_set_feature_edges.argtypes = [vp, vp, i64]
     L.rpd_copy_device_to_host.restype = i32
     L.rpd_copy_device_to_host.argtypes = [vp, vp, vp, i64]
     L.rpd_compute_partial.restype = i32
@@ -564,6 +572,14 @@ class RPD:
         self._check(self._L.rpd_compute_power_cells(self._h, int(max_sf_fid), ctypes.byref(ms)))
         return ms.value
 
+    def set_feature_edges(self, records):
+        """libmat's TetMesh::tet_es2fe_map as (m, 6) int records (tet, lf_min,
+        lf_max, fe_type, fe_id, fe_line_id), in insertion order; None or an
+        empty array clears it."""
+        r = np.ascontiguousarray(np.zeros((0, 6)) if records is None else records,
+                                 np.int32).reshape(-1, 6)
+        self._check(self._L.rpd_set_feature_edges(self._h, _p(r), r.shape[0]))
+
     def _d2h(self, ptr, dtype, count):
         out = np.zeros(max(int(count), 1), dtype)
         if count > 0:
@@ -598,6 +614,14 @@ class RPD:
         d["surface_cell"] = self._d2h(v.surface_cell, np.int32, v.n_surface)
         d["surface_fid"] = self._d2h(v.surface_fid, np.int32, v.n_surface)
         d["surface_pos"] = self._d2h(v.surface_pos, np.float32, 3 * v.n_surface).reshape(-1, 3)
+        for name in ("se_covered", "ce_covered"):
+            m = getattr(v, "n_" + name)
+            d["cell_%s_off" % name] = self._d2h(getattr(v, "cell_%s_off" % name), np.int64, n + 1)
+            d[name] = self._d2h(getattr(v, name), np.int32, 5 * m).reshape(-1, 5)
+        m = v.n_se_line_end
+        d["cell_se_line_end_off"] = self._d2h(v.cell_se_line_end_off, np.int64, n + 1)
+        d["se_line_end"] = self._d2h(v.se_line_end, np.int32, 4 * m).reshape(-1, 4)
+        d["se_line_end_pos"] = self._d2h(v.se_line_end_pos, np.float32, 3 * m).reshape(-1, 3)
         return d
 
     def compute_partial(self, recompute):

@@ -8,7 +8,10 @@ per site ascending, then key, then cell.  Positions and face centroids are
 float32, one rounding per operation: compute_vertex_coordinates
 (src/rpd3d_base/voronoi_defs.cxx:33-74, include/common_cxx.h:128-135) and
 get_cell_v2surffid's running float sum and division (rpd_update.cxx:20-42).
-The feature-edge records (tet_es2fe_map) are not restated.
+The feature-edge records follow rpd_update.cxx:206-254 with
+convert_e_lfids_to_lvids (:44-67), the map TetMesh::tet_es2fe_map given as
+records (tet, lf_min, lf_max, fe_type, fe_id, fe_line_id) in insertion
+order (a later record with the same key replaces an earlier one).
 """
 import numpy as np
 
@@ -61,9 +64,16 @@ def _cell(h, payload, th, rec):
                 face=face, null=bool(th["flags"] & 1))
 
 
-def power_cells(cells, payload, n_site, max_sf_fid):
-    """cells: emitted cells (HEADER_DTYPE, output order).  Returns the
-    arrays of rpd_power_cells_view."""
+SE, CE = 1, 2  # EdgeType (src/inputs/input_types.h:13-17)
+
+
+def power_cells(cells, payload, n_site, max_sf_fid, feature_edges=None):
+    """cells: emitted cells (HEADER_DTYPE, output order); feature_edges:
+    (m, 6) int records or None.  Returns the arrays of rpd_power_cells_view."""
+    fe = {}
+    if feature_edges is not None:
+        for r in np.asarray(feature_edges, np.int64).reshape(-1, 6):
+            fe[(int(r[0]), int(r[1]), int(r[2]))] = (int(r[3]), int(r[4]), int(r[5]))
     h = np.ascontiguousarray(cells[cells["status"] == O.SUCCESS])
     th, rec = O.cell_topology(h, payload)
     n = h.shape[0]
@@ -73,6 +83,7 @@ def power_cells(cells, payload, n_site, max_sf_fid):
     nbrs = [set() for _ in range(n)]
     tfids = [set() for _ in range(n)]
     facets, edges, verts, surf = [], [], {}, {}
+    se_cov, ce_cov, se_end = [set() for _ in range(n)], [set() for _ in range(n)], {}
     for s in range(n_site):
         facet_neigh_to_cells, tfid_to_cells, edge_2endvertices = {}, {}, {}
         for q in by_site[s]:  # ascending cell id
@@ -112,6 +123,29 @@ def power_cells(cells, payload, n_site, max_sf_fid):
                     continue
                 ex, ey = int(c["edge"][e][0]), int(c["edge"][e][1])
                 h1, h2 = id2[ex], id2[ey]
+                if h1[1] == -1 and h2[1] == -1:  # an edge of the tet
+                    lf = (min(ex, ey), max(ex, ey))
+                    info = fe.get((int(h["tet_id"][q]), lf[0], lf[1]))
+                    if info is None:
+                        continue
+                    # the two smallest vertices on both faces' cycles
+                    common = sorted(set(c["face"][lf[0]]) & set(c["face"][lf[1]]))
+                    lv = (common + [-1, -1])[:2]
+                    covered = (q, lv[0], lv[1], info[2], info[1])
+                    if info[0] == SE:
+                        se_cov[q].add(covered)
+                    elif info[0] == CE:
+                        ce_cov[q].add(covered)
+                    for lvid in lv:
+                        if lvid < 0:
+                            continue
+                        for i in range(3):
+                            hp = id2[ver[lvid][i]]
+                            if hp[1] == -1:
+                                continue
+                            nb = int(hp[1]) if int(hp[0]) == s else int(hp[0])
+                            se_end[(q, lvid, nb, info[2])] = _vertex(pl, ver[lvid])
+                            break
                 if h1[1] == -1 or h2[1] == -1:
                     continue
                 n1 = int(h1[1]) if int(h1[0]) == s else int(h1[0])
@@ -155,4 +189,12 @@ def power_cells(cells, payload, n_site, max_sf_fid):
     out["surface_fid"] = np.array([f for q in sk for f, _ in surf[q]], np.int32)
     out["surface_pos"] = np.array([p for q in sk for _, p in surf[q]], np.float32).reshape(-1, 3)
     out["cell_surface_off"] = np.searchsorted(out["surface_cell"], np.arange(n + 1)).astype(np.int64)
+    for name, cov in (("se_covered", se_cov), ("ce_covered", ce_cov)):
+        out["cell_%s_off" % name] = np.cumsum([0] + [len(x) for x in cov]).astype(np.int64)
+        out[name] = np.array([r for x in cov for r in sorted(x)], np.int32).reshape(-1, 5)
+    ek = sorted(se_end)
+    out["se_line_end"] = np.array(ek, np.int32).reshape(-1, 4)
+    out["se_line_end_pos"] = np.array([se_end[k] for k in ek], np.float32).reshape(-1, 3)
+    out["cell_se_line_end_off"] = np.searchsorted(out["se_line_end"][:, 0],
+                                                  np.arange(n + 1)).astype(np.int64)
     return out

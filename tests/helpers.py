@@ -115,3 +115,25 @@ def cell_planes_ver(payload, off, nb_v, nb_p):
     pl = payload[o:o + 16 * int(nb_p)].view(np.float32).reshape(-1, 4)
     ver = payload[o + s["plane"] + s["id2"]:][:4 * int(nb_v)].reshape(-1, 4)
     return pl, ver
+
+
+TET_FACE_PAIRS = [(a, b) for a in range(4) for b in range(a + 1, 4)]
+
+
+def feature_edge_records(n_tet, seed, frac=0.3):
+    """Seeded stand-in for TetMesh::tet_es2fe_map: (m, 6) int32 records (tet,
+    lf_min, lf_max, fe_type, fe_id, fe_line_id) on about frac of the tets,
+    types sharp (1), concave (2) and unknown (-1), in shuffled order, then a
+    tenth of the keys again with other values (the later record counts)."""
+    rng = np.random.default_rng(seed)
+    recs = []
+    for t in rng.choice(n_tet, size=max(1, int(frac * n_tet)), replace=False):
+        for j in rng.choice(6, size=int(rng.integers(1, 4)), replace=False):
+            a, b = TET_FACE_PAIRS[j]
+            recs.append((t, a, b, rng.choice([1, 2, -1]), rng.integers(0, 1000), rng.integers(0, 50)))
+    recs = np.array(recs, np.int64)
+    recs = recs[rng.permutation(len(recs))]
+    again = recs[rng.choice(len(recs), size=len(recs) // 10, replace=False)].copy()
+    again[:, 3] = rng.choice([1, 2], size=len(again))
+    again[:, 4] += 1000
+    return np.concatenate([recs, again]).astype(np.int32)

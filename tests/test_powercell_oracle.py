@@ -40,3 +40,59 @@ def test_power_cell_structure(golden_cases):
         v = pc["vertex_ids"]
         assert np.all(np.diff(v, axis=1) > 0)
         assert len(pc["surface_cell"]) > 0 and np.all(pc["surface_fid"] < nb)
+
+
+def test_feature_edge_records(golden_cases):
+    """se/ce records and sharp-line endpoints against a second derivation:
+    the edge's vertices from the dual triangles (both tet faces among the
+    vertex's planes) instead of the face cycles."""
+    from tests.helpers import feature_edge_records, float_vertices, cell_planes_ver
+    for name in ("cube_k64", "random_full"):
+        c = golden_cases[name]
+        h = ref_headers(c)
+        cells = h[h["status"] == SUCCESS]
+        n_tet = c["tets"].shape[0]
+        recs = feature_edge_records(n_tet, seed=5)
+        fe = {(int(r[0]), int(r[1]), int(r[2])): (int(r[3]), int(r[4]), int(r[5])) for r in recs}
+        nb = int((c["f_adjs"] == 1).sum())
+        pc = P.power_cells(h, c["ref_payload"], c["sites"].shape[0], nb - 1, recs)
+        plain = P.power_cells(h, c["ref_payload"], c["sites"].shape[0], nb - 1)
+        fe_keys = ("se_covered", "ce_covered", "se_line_end")
+        for k in plain:  # the other arrays do not depend on the feature edges
+            if not any(x in k for x in fe_keys):
+                assert np.array_equal(plain[k], pc[k]), k
+        want = {1: set(), 2: set()}
+        ends = {}
+        for q in range(len(cells)):
+            pl, ver = cell_planes_ver(c["ref_payload"], cells["offset"][q], cells["nb_v"][q],
+                                      cells["nb_p"][q])
+            xyz = float_vertices(pl, ver)
+            o = int(cells["offset"][q])
+            n_p = int(cells["nb_p"][q])
+            id2 = c["ref_payload"][o + 16 * n_p:o + 24 * n_p].view(np.int32).reshape(-1, 2)
+            for a, b in [(a, b) for a in range(4) for b in range(a + 1, 4)]:
+                info = fe.get((int(cells["tet_id"][q]), a, b))
+                if info is None:
+                    continue
+                on = [v for v in range(len(ver)) if a in ver[v][:3] and b in ver[v][:3]]
+                if len(on) < 2:  # no edge of the cell on this tet edge
+                    continue
+                lv = sorted(on)[:2]
+                if info[0] in want:
+                    want[info[0]].add((q, lv[0], lv[1], info[2], info[1]))
+                for v in lv:
+                    for i in range(3):
+                        hp = id2[ver[v][i]]
+                        if hp[1] != -1:
+                            s = int(cells["site_id"][q])
+                            ends[(q, v, int(hp[1]) if int(hp[0]) == s else int(hp[0]), info[2])] = xyz[v]
+                            break
+        for t, key in ((1, "se_covered"), (2, "ce_covered")):
+            assert set(map(tuple, pc[key].tolist())) == want[t], (name, key)
+            off = pc["cell_%s_off" % key]
+            assert off[-1] == len(pc[key]) and np.all(np.diff(off) >= 0)
+        got = {tuple(k): p for k, p in zip(pc["se_line_end"].tolist(), pc["se_line_end_pos"])}
+        assert set(got) == set(ends), name
+        for k in got:
+            assert np.array_equal(got[k], ends[k]), (name, k)
+        assert len(want[1]) > 0 and len(want[2]) > 0 and len(ends) > 0
