@@ -480,6 +480,27 @@ typedef struct rpd_polygon_view {
   const int32_t* poly_adj_site; /* device, n_polys */
 } rpd_polygon_view;
 rpd_status rpd_get_polygons(struct rpd_ctx* ctx, rpd_polygon_view* view);
+
+/* Slicing plane of the following rpd_compute_polygons calls, as
+ * save_convex_cells_houdini applies it (src/IO/IO_CUDA/io_cuda.cxx:166-170):
+ * a cell whose barycenter -- the float mean of its float vertices,
+ * compute_cell_barycenter (io_cuda.cxx:6-17) -- has dot(bary - pos, normal)
+ * >= 0 in double (is_slice_by_plane, src/IO/IO_CXX/io.cxx:810-820) is left
+ * out, points and faces.  libmat's plane: pos = (xmax / 2.2, 0, 0), normal =
+ * (-1, 0, 0).  enable = 0 turns slicing off. */
+rpd_status rpd_set_polygon_slice(struct rpd_ctx* ctx, int enable, const double* pos,
+                                 const double* normal);
+
+/* The polygon soup of the last rpd_compute_polygons written to `path` as a
+ * Houdini binary geometry file, byte for byte what libmat's
+ * save_convex_cells_houdini writes through IO::GeometryWriter
+ * (src/IO/IO_CUDA/io_utils.cpp:106-231): big-endian, version 5, point
+ * attribute P (x, y, z, 1), primitive attribute PrimAttr = the polygon's
+ * site, point ids 16-bit up to 65536 points, else 32-bit.  The file image is
+ * assembled on the device and written through a pinned staging buffer;
+ * *bytes (optional) receives its size.  No points: RPD_ERR_INVALID_ARGUMENT
+ * (the reference writer throws). */
+rpd_status rpd_write_polygons_bgeo(struct rpd_ctx* ctx, const char* path, int64_t* bytes);
 /* NULL buffers: sizes only.  points: 3 floats per point; offsets: n_polys + 1. */
 rpd_status rpd_copy_polygons_to_host(struct rpd_ctx* ctx, float* points, int64_t max_points,
                                      int64_t* poly_offsets, uint32_t* indices,

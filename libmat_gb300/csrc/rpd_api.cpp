@@ -1452,6 +1452,8 @@ rpd_status rpd_compute_polygons(rpd_ctx* c, int triangulate, int boundary_only, 
   p.triangulate = triangulate != 0;
   p.boundary_only = boundary_only != 0;
   p.max_sf_fid = max_sf_fid;
+  p.slice = c->poly_slice;
+  for (int k = 0; k < 6; ++k) p.slice_plane[k] = c->poly_slice_plane[k];
   p.cnt_points = c->poly_cnt.ptr;
   p.cnt_polys = c->poly_cnt.ptr + n;
   p.cnt_indices = c->poly_cnt.ptr + 2 * n;
@@ -1492,6 +1494,96 @@ rpd_status rpd_compute_polygons(rpd_ctx* c, int triangulate, int boundary_only, 
   c->n_poly_indices = tot[2];
   c->has_polygons = true;
   return RPD_OK;
+}
+
+rpd_status rpd_set_polygon_slice(rpd_ctx* c, int enable, const double* pos, const double* normal) {
+  if (!c) return RPD_ERR_INVALID_ARGUMENT;
+  if (!enable) {
+    c->poly_slice = 0;
+    return RPD_OK;
+  }
+  if (!pos || !normal) return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_set_polygon_slice: no plane");
+  for (int k = 0; k < 3; ++k)
+    if (!std::isfinite(pos[k]) || !std::isfinite(normal[k]))
+      return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_set_polygon_slice: non-finite plane");
+  for (int k = 0; k < 3; ++k) {
+    c->poly_slice_plane[k] = pos[k];
+    c->poly_slice_plane[3 + k] = normal[k];
+  }
+  c->poly_slice = 1;
+  return RPD_OK;
+}
+
+namespace {
+void be32(uint8_t* d, uint32_t v) {
+  d[0] = (uint8_t)(v >> 24);
+  d[1] = (uint8_t)(v >> 16);
+  d[2] = (uint8_t)(v >> 8);
+  d[3] = (uint8_t)v;
+}
+}  // namespace
+
+rpd_status rpd_write_polygons_bgeo(rpd_ctx* c, const char* path, int64_t* bytes) {
+  if (!c || !path) return RPD_ERR_INVALID_ARGUMENT;
+  if (!c->has_result || !c->has_polygons)
+    return fail(c, RPD_ERR_NOT_READY, "rpd_write_polygons_bgeo: call rpd_compute_polygons first");
+  const long long n_pts = c->n_poly_points, n_polys = c->n_polys, n_idx = c->n_poly_indices;
+  if (n_pts == 0) return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_write_polygons_bgeo: no points");
+  if (n_pts > 0x7fffffffll || n_polys > 0x7fffffffll)
+    return fail(c, RPD_ERR_CAPACITY, "rpd_write_polygons_bgeo: counts above the format's int range");
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  cudaStream_t st = c->stream;
+  const int wide = n_pts > (1ll << 16);
+  const long long hdr = 41, pts = 16 * n_pts, attr = 20, polys = 13 * n_polys + (wide ? 4 : 2) * n_idx;
+  const long long total = hdr + pts + attr + polys + 2;
+  CK(c->bgeo_img.ensure((size_t)total), "alloc");
+  uint8_t* img = c->bgeo_img.ptr;
+  // header: 'Bgeo', 'V', version 5, points, polygons, point groups, primitive
+  // groups, point attributes besides P, vertex attributes, primitive
+  // attributes (PrimAttr), detail attributes
+  uint8_t h[41];
+  h[0] = 'B';
+  h[1] = 'g';
+  h[2] = 'e';
+  h[3] = 'o';
+  h[4] = 'V';
+  const uint32_t hv[9] = {5u, (uint32_t)n_pts, (uint32_t)n_polys, 0u, 0u, 0u, 0u, 1u, 0u};
+  for (int k = 0; k < 9; ++k) be32(h + 5 + 4 * k, hv[k]);
+  // PrimAttr: name length, name, size 1, type integer, default 0
+  uint8_t a[20] = {0, 8, 'P', 'r', 'i', 'm', 'A', 't', 't', 'r', 0, 1};
+  be32(a + 12, 1u);
+  be32(a + 16, 0u);
+  const uint8_t foot[2] = {0x00, 0xff};
+  CK(cudaMemcpyAsync(img, h, sizeof(h), cudaMemcpyHostToDevice, st), "H2D");
+  CK(cudaMemcpyAsync(img + hdr + pts, a, sizeof(a), cudaMemcpyHostToDevice, st), "H2D");
+  CK(cudaMemcpyAsync(img + total - 2, foot, sizeof(foot), cudaMemcpyHostToDevice, st), "H2D");
+  CK(bgeo_fill(c->poly_points.ptr, n_pts, c->poly_offsets.ptr, c->poly_indices.ptr, c->poly_site.ptr,
+               n_polys, wide, img + hdr, img + hdr + pts + attr, c->num_sms, st),
+     "bgeo image");
+  CK(cudaStreamSynchronize(st), "bgeo sync");
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_write_polygons_bgeo: cannot open the file");
+  // through a pinned staging buffer, 32 MB at a time
+  const size_t chunk = (size_t)32 << 20;
+  void* stage = nullptr;
+  if (cudaMallocHost(&stage, chunk) != cudaSuccess) {
+    std::fclose(f);
+    return fail(c, RPD_ERR_OUT_OF_MEMORY, "rpd_write_polygons_bgeo: pinned staging buffer");
+  }
+  rpd_status res = RPD_OK;
+  for (long long at = 0; at < total && res == RPD_OK; at += (long long)chunk) {
+    const size_t nb = (size_t)std::min((long long)chunk, total - at);
+    if (cudaMemcpyAsync(stage, img + at, nb, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      res = fail(c, RPD_ERR_CUDA, "rpd_write_polygons_bgeo: D2H");
+    else if (std::fwrite(stage, 1, nb, f) != nb)
+      res = fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_write_polygons_bgeo: write failed");
+  }
+  cudaFreeHost(stage);
+  if (std::fclose(f) != 0 && res == RPD_OK)
+    res = fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_write_polygons_bgeo: write failed");
+  if (res == RPD_OK && bytes) *bytes = total;
+  return res;
 }
 
 rpd_status rpd_get_polygons(rpd_ctx* c, rpd_polygon_view* v) {

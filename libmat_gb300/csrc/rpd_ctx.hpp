@@ -152,6 +152,9 @@ struct rpd_ctx {
   DevBuf<int32_t> poly_site, poly_adj;
   long long n_poly_points = 0, n_polys = 0, n_poly_indices = 0;
   bool has_polygons = false;
+  int poly_slice = 0;               // rpd_set_polygon_slice
+  double poly_slice_plane[6] = {};  // pos, normal
+  DevBuf<uint8_t> bgeo_img;         // Houdini file image
   // rpd_compute_partial: the previous cells, the merge's buffers, the
   // recomputed sites' flags
   bool cells_for_mesh = false;  // cells / payload hold every cell of the current mesh and sites

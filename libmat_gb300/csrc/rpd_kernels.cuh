@@ -225,6 +225,8 @@ struct PolyParams {
   const rpd_topo_header* topo_h;  // their per-cell topology
   const uint8_t* topo;
   int triangulate, boundary_only, max_sf_fid;
+  int slice;               // leave out the cells on the plane's positive side
+  double slice_plane[6];   // pos, normal
   int32_t *cnt_points, *cnt_polys, *cnt_indices;        // per cell
   const long long *off_points, *off_polys, *off_indices;  // exclusive scans (n + 1)
   float* points;          // 3 per point
@@ -234,6 +236,12 @@ struct PolyParams {
 };
 cudaError_t poly_count(const PolyParams& p, cudaStream_t st);
 cudaError_t poly_fill(const PolyParams& p, cudaStream_t st);
+// the points (16 bytes each) and polygons (13 + 2 or 4 bytes per id) of a
+// Houdini binary geometry file, big-endian, at the two section starts
+cudaError_t bgeo_fill(const float* points, long long n_points, const long long* poly_offsets,
+                      const uint32_t* indices, const int32_t* poly_site, long long n_polys,
+                      int wide, uint8_t* points_out, uint8_t* polys_out, int num_sms,
+                      cudaStream_t st);
 // exclusive scan of n int32 counts into n + 1 int64 (out[n] = total); temp:
 // scan64_temp(n) entries
 size_t scan64_temp(long long n);

@@ -15,8 +15,22 @@
 // reload_pc_explicit's), one thread per cell counts its points, polygons and
 // indices, 64-bit scans give every cell its output ranges, and a second pass
 // writes them.  Compiled with -fmad=false (the float vertex formula).
+//
+// With a slicing plane, a cell is left out (no points, no faces) when
+// save_convex_cells_houdini would skip it (io_cuda.cxx:166-170): its
+// barycenter (compute_cell_barycenter, io_cuda.cxx:6-17: the float sum of
+// its float vertices divided by (float) nb_v) has dot(bary - pos, normal)
+// >= 0 in double (is_slice_by_plane, src/IO/IO_CXX/io.cxx:810-820).
+//
+// The Houdini file (IO::GeometryWriter::OutputGeometry, io_utils.cpp:106-231)
+// is assembled on the device: its points one byte per thread (coalesced),
+// its polygons one thread each at 13 + id size x (index offset) bytes from
+// the section start; the host adds the fixed header, attribute definition
+// and footer.
 
 #include <cuda_runtime.h>
+
+#include <algorithm>
 
 #include "rpd_common.cuh"
 #include "rpd_hostfloat.cuh"
@@ -128,13 +142,32 @@ __device__ __forceinline__ float3 cell_point(const PolyCell& c, int t) {
   return host_float_vertex(c.pl[min((int)v.x, m)], c.pl[min((int)v.y, m)], c.pl[min((int)v.z, m)]);
 }
 
+__device__ bool sliced(const PolyCell& c, const PolyParams& p) {
+  float bx = 0.f, by = 0.f, bz = 0.f;
+  for (int t = 0; t < c.nv; ++t) {
+    const float3 v = cell_point(c, t);
+    bx = v.x + bx;
+    by = v.y + by;
+    bz = v.z + bz;
+  }
+  const float fn = (float)c.nv;
+  bx = bx / fn;
+  by = by / fn;
+  bz = bz / fn;
+  const double dx = (double)bx - p.slice_plane[0], dy = (double)by - p.slice_plane[1],
+               dz = (double)bz - p.slice_plane[2];
+  return dx * p.slice_plane[3] + dy * p.slice_plane[4] + dz * p.slice_plane[5] >= 0.0;
+}
+
 __global__ void poly_count_kernel(PolyParams p) {
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= p.n) return;
   rpd_cell_header hd;
   const PolyCell c = poly_cell(p, q, hd);
   int pts = c.nv, polys = 0, idx = 0;
-  if (c.vnull) {
+  if (p.slice && sliced(c, p)) {
+    pts = 0;
+  } else if (c.vnull) {
     // the points before the first NaN vertex stay, no faces
     pts = 0;
     while (pts < c.nv && !is_null_vertex(cell_point(c, pts))) ++pts;
@@ -203,7 +236,72 @@ __global__ void poly_fill_kernel(PolyParams p) {
   }
 }
 
+__device__ __forceinline__ void put_be32(uint8_t* d, uint32_t v) {
+  d[0] = (uint8_t)(v >> 24);
+  d[1] = (uint8_t)(v >> 16);
+  d[2] = (uint8_t)(v >> 8);
+  d[3] = (uint8_t)v;
+}
+
+// byte j of the points section: point j / 16, word (j / 4) % 4 (x, y, z,
+// 1.0f), big-endian
+__global__ void bgeo_points_kernel(const float* points, long long n_bytes, uint8_t* out) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < n_bytes; j += stride) {
+    const long long pt = j >> 4;
+    const int w = (int)((j >> 2) & 3), b = (int)(j & 3);
+    const float f = w < 3 ? points[3 * pt + w] : 1.0f;
+    out[j] = (uint8_t)(__float_as_uint(f) >> (24 - 8 * b));
+  }
+}
+
+// polygon i: int 1, int count, '<', the ids (16- or 32-bit), int site
+__global__ void bgeo_polys_kernel(const long long* poly_offsets, const uint32_t* indices,
+                                  const int32_t* poly_site, long long n_polys, int wide,
+                                  uint8_t* out) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n_polys; i += stride) {
+    const long long a = poly_offsets[i], e = poly_offsets[i + 1];
+    uint8_t* d = out + 13 * i + (wide ? 4 : 2) * a;
+    put_be32(d, 1u);
+    put_be32(d + 4, (uint32_t)(e - a));
+    d[8] = (uint8_t)'<';
+    d += 9;
+    for (long long k = a; k < e; ++k) {
+      const uint32_t v = indices[k];
+      if (wide) {
+        put_be32(d, v);
+        d += 4;
+      } else {
+        d[0] = (uint8_t)(v >> 8);
+        d[1] = (uint8_t)v;
+        d += 2;
+      }
+    }
+    put_be32(d, (uint32_t)poly_site[i]);
+  }
+}
+
 }  // namespace
+
+cudaError_t bgeo_fill(const float* points, long long n_points, const long long* poly_offsets,
+                      const uint32_t* indices, const int32_t* poly_site, long long n_polys,
+                      int wide, uint8_t* points_out, uint8_t* polys_out, int num_sms,
+                      cudaStream_t st) {
+  const long long cap = (long long)num_sms * 8;
+  if (n_points > 0) {
+    const long long nb = 16 * n_points;
+    bgeo_points_kernel<<<(unsigned)std::min((nb + 255) / 256, cap), 256, 0, st>>>(points, nb,
+                                                                                  points_out);
+    note_launches(1);
+  }
+  if (n_polys > 0) {
+    bgeo_polys_kernel<<<(unsigned)std::min((n_polys + 255) / 256, cap), 256, 0, st>>>(
+        poly_offsets, indices, poly_site, n_polys, wide, polys_out);
+    note_launches(1);
+  }
+  return cudaGetLastError();
+}
 
 size_t scan64_temp(long long n) { return (size_t)((n + kScan64 - 1) / kScan64) + 1; }
 

@@ -55,7 +55,8 @@ EXPORTS = [
     "rpd_topo_bytes", "rpd_compute_topology", "rpd_get_topology", "rpd_copy_topology_to_host",
     "rpd_compute_polygons", "rpd_get_polygons", "rpd_copy_polygons_to_host", "rpd_dist2mat",
     "rpd_compute_partial", "rpd_compute_power_cells", "rpd_get_power_cells",
-    "rpd_set_feature_edges", "rpd_copy_device_to_host",
+    "rpd_set_feature_edges", "rpd_copy_device_to_host", "rpd_set_polygon_slice",
+    "rpd_write_polygons_bgeo",
     "rpd_batch_create", "rpd_batch_destroy", "rpd_batch_last_error", "rpd_batch_add_mesh",
     "rpd_batch_size", "rpd_batch_set_graph", "rpd_batch_compute", "rpd_batch_autotune",
     "rpd_batch_mesh_cells", "rpd_batch_copy_mesh_cells", "rpd_batch_context",
@@ -241,6 +242,10 @@ def load(path=LIB_PATH):
     L.rpd_get_power_cells.argtypes = [vp, c.POINTER(PowerCellsView)]
     L.rpd_set_feature_edges.restype = i32
     L.rpd_set_feature_edges.argtypes = [vp, vp, i64]
+    L.rpd_set_polygon_slice.restype = i32
+    L.rpd_set_polygon_slice.argtypes = [vp, i32, vp, vp]
+    L.rpd_write_polygons_bgeo.restype = i32
+    L.rpd_write_polygons_bgeo.argtypes = [vp, c.c_char_p, c.POINTER(i64)]
     L.rpd_copy_device_to_host.restype = i32
     L.rpd_copy_device_to_host.argtypes = [vp, vp, vp, i64]
     L.rpd_compute_partial.restype = i32
@@ -657,6 +662,24 @@ class RPD:
         self._check(self._L.rpd_compute_polygons(self._h, int(triangulate), int(boundary_only),
                                                  int(max_sf_fid), ctypes.byref(ms)))
         return ms.value
+
+    def set_polygon_slice(self, pos=None, normal=None):
+        """Slicing plane of the following compute_polygons calls (libmat's
+        is_slice_by_plane, as save_convex_cells_houdini applies it); None
+        turns it off."""
+        if pos is None:
+            self._check(self._L.rpd_set_polygon_slice(self._h, 0, None, None))
+            return
+        a = np.ascontiguousarray(pos, np.float64)
+        b = np.ascontiguousarray(normal, np.float64)
+        self._check(self._L.rpd_set_polygon_slice(self._h, 1, _p(a), _p(b)))
+
+    def write_polygons_bgeo(self, path):
+        """Writes the last polygon soup as a Houdini binary geometry file
+        (libmat's save_convex_cells_houdini format); returns its size."""
+        n = ctypes.c_int64()
+        self._check(self._L.rpd_write_polygons_bgeo(self._h, str(path).encode(), ctypes.byref(n)))
+        return n.value
 
     def polygons(self):
         """The polygon soup copied to the host: dict(points (n, 3) float32,

@@ -10,6 +10,10 @@
 * ``_ref/libreftopo.so`` -- the reference's own per-cell topology
   (src/rpd3d_base/voronoi_defs.cxx) behind ref_topo_driver.cpp, same
   condition.
+* ``_ref/librefbgeo.so`` -- the reference's own Houdini geometry writer
+  (src/IO/IO_CUDA/io_utils.cpp) behind ref_bgeo_driver.cpp, through
+  ref_io_shim/ (CUDA's vector structs, an empty json header), same
+  condition.
 """
 import os
 import subprocess
@@ -83,7 +87,27 @@ def build_ref_topo(force=False):
     return out
 
 
+def build_ref_bgeo(force=False):
+    """Returns the path of _ref/librefbgeo.so -- the reference's own Houdini
+    geometry writer behind ref_bgeo_driver.cpp -- or None without reference
+    sources."""
+    io_dir = os.path.join(REF_ROOT, "src", "IO", "IO_CUDA")
+    src = os.path.join(io_dir, "io_utils.cpp")
+    if not os.path.exists(src):
+        return None
+    outdir = os.path.join(HERE, "_ref")
+    os.makedirs(outdir, exist_ok=True)
+    out = os.path.join(outdir, "librefbgeo.so")
+    drv = os.path.join(HERE, "ref_bgeo_driver.cpp")
+    shim = os.path.join(HERE, "ref_io_shim")
+    if force or _stale(out, [drv, src, os.path.join(shim, "cuda_runtime.h")]):
+        _run(["g++", "-O2", "-fPIC", "-shared", "-std=c++17", "-DNDEBUG", "-w",
+              "-I" + shim, "-I" + io_dir, drv, src, "-o", out])
+    return out
+
+
 if __name__ == "__main__":
     print(build_oracle(force="-f" in sys.argv))
     print(build_ref(force="-f" in sys.argv))
     print(build_ref_topo(force="-f" in sys.argv))
+    print(build_ref_bgeo(force="-f" in sys.argv))

@@ -77,7 +77,7 @@ def lib():
         L.orc_cell_topology.restype = i64
         L.orc_cell_topology.argtypes = [i64, vp, vp, vp, vp, i64]
         L.orc_cell_polygons.restype = i32
-        L.orc_cell_polygons.argtypes = [i64, vp, vp, i32, i32, i32, vp, i64, vp, vp, i64,
+        L.orc_cell_polygons.argtypes = [i64, vp, vp, i32, i32, i32, vp, vp, i64, vp, vp, i64,
                                         vp, vp, i64, vp]
         _lib = L
     return _lib
@@ -319,14 +319,20 @@ def topo_bytes(nb_v, nb_p, nb_e):
     return int(lib().orc_topo_bytes(int(nb_v), int(nb_p), int(nb_e)))
 
 
-def cell_polygons(cells, payload, triangulate=False, boundary_only=False, max_sf_fid=0):
+def cell_polygons(cells, payload, triangulate=False, boundary_only=False, max_sf_fid=0,
+                  slice_plane=None):
     """Polygon soup of emitted cells (oracle restatement of
-    get_one_convex_cell_faces_const).  Returns dict(points (n, 3) float32,
-    poly_offsets, indices, poly_site, poly_adj_site)."""
+    get_one_convex_cell_faces_const; with slice_plane = (pos, normal), the
+    cells save_convex_cells_houdini slices away are left out).  Returns
+    dict(points (n, 3) float32, poly_offsets, indices, poly_site,
+    poly_adj_site)."""
     h, payload = _emitted(cells, payload)
     n = h.shape[0]
     counts = np.zeros(3, np.int64)
-    args = (n, _p(h), _p(payload), int(triangulate), int(boundary_only), int(max_sf_fid))
+    sl = None if slice_plane is None else np.ascontiguousarray(
+        np.concatenate([np.asarray(slice_plane[0], np.float64), np.asarray(slice_plane[1], np.float64)]))
+    args = (n, _p(h), _p(payload), int(triangulate), int(boundary_only), int(max_sf_fid),
+            None if sl is None else _p(sl))
     if lib().orc_cell_polygons(*args, None, 0, None, None, 0, None, None, 0, _p(counts)) != 0:
         raise RuntimeError("oracle polygon count failed")
     npt, npoly, nidx = (int(x) for x in counts)

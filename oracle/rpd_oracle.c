@@ -1214,9 +1214,41 @@ int64_t orc_cell_topology(int64_t n_cells, const orc_cell_header* cells,
  * Polygon soup: restates get_one_convex_cell_faces_const
  * (src/IO/IO_CUDA/io_cuda.cxx:21-141) on the packed records, cell after cell.
  * ---------------------------------------------------------------------- */
+/* compute_vertex_coordinates of vertex t (voronoi_defs.cxx:33-74), float */
+static void orc_float_vertex(const float* pl, const uint8_t* ver, int t, float* out) {
+  const float* p1 = pl + 4 * ver[4 * t];
+  const float* p2 = pl + 4 * ver[4 * t + 1];
+  const float* p3 = pl + 4 * ver[4 * t + 2];
+  float x = -orc_cdet3(p1[3], p1[1], p1[2], p2[3], p2[1], p2[2], p3[3], p3[1], p3[2]);
+  float y = -orc_cdet3(p1[0], p1[3], p1[2], p2[0], p2[3], p2[2], p3[0], p3[3], p3[2]);
+  float z = -orc_cdet3(p1[0], p1[1], p1[3], p2[0], p2[1], p2[3], p3[0], p3[1], p3[3]);
+  float w = orc_cdet3(p1[0], p1[1], p1[2], p2[0], p2[1], p2[2], p3[0], p3[1], p3[2]);
+  out[0] = x / w;
+  out[1] = y / w;
+  out[2] = z / w;
+}
+
+/* save_convex_cells_houdini's slicing (io_cuda.cxx:166-170): the cell's
+ * barycenter, compute_cell_barycenter (io_cuda.cxx:6-17: float sum of the
+ * float vertices, divided by (float) nb_v), and is_slice_by_plane
+ * (io.cxx:810-820: dot(bary - pos, normal) >= 0 in double, GEO::dot's
+ * order) with plane = {pos, normal} */
+static int orc_sliced(const float* pl, const uint8_t* ver, int nv, const double* plane) {
+  float b[3] = {0.f, 0.f, 0.f}, v[3];
+  for (int t = 0; t < nv; ++t) {
+    orc_float_vertex(pl, ver, t, v);
+    for (int k = 0; k < 3; ++k) b[k] = v[k] + b[k];
+  }
+  for (int k = 0; k < 3; ++k) b[k] = b[k] / (float)nv;
+  const double dx = (double)b[0] - plane[0], dy = (double)b[1] - plane[1],
+               dz = (double)b[2] - plane[2];
+  const double dist = dx * plane[3] + dy * plane[4] + dz * plane[5];
+  return dist >= 0;
+}
+
 int orc_cell_polygons(int64_t n_cells, const orc_cell_header* cells,
                       const uint8_t* payload, int triangulate, int boundary_only,
-                      int max_sf_fid, float* points, int64_t max_points,
+                      int max_sf_fid, const double* slice, float* points, int64_t max_points,
                       int64_t* poly_offsets, uint32_t* indices, int64_t max_indices,
                       int32_t* poly_site, int32_t* poly_adj_site, int64_t max_polys,
                       int64_t* counts) {
@@ -1232,18 +1264,14 @@ int orc_cell_polygons(int64_t n_cells, const orc_cell_header* cells,
     const int32_t* id2 = (const int32_t*)(rec + o_id2);
     const uint8_t* ver = rec + o_ver;
     (void)ne;
+    if (slice && orc_sliced(pl, ver, nv, slice)) continue;
     const int64_t row = n_pts;
     /* the cell's vertices; a NaN one ends the cell */
     int null_seen = 0;
     for (int t = 0; t < nv; ++t) {
-      const float* p1 = pl + 4 * ver[4 * t];
-      const float* p2 = pl + 4 * ver[4 * t + 1];
-      const float* p3 = pl + 4 * ver[4 * t + 2];
-      float x = -orc_cdet3(p1[3], p1[1], p1[2], p2[3], p2[1], p2[2], p3[3], p3[1], p3[2]);
-      float y = -orc_cdet3(p1[0], p1[3], p1[2], p2[0], p2[3], p2[2], p3[0], p3[3], p3[2]);
-      float z = -orc_cdet3(p1[0], p1[1], p1[3], p2[0], p2[1], p2[3], p3[0], p3[1], p3[3]);
-      float w = orc_cdet3(p1[0], p1[1], p1[2], p2[0], p2[1], p2[2], p3[0], p3[1], p3[2]);
-      float px = x / w, py = y / w, pz = z / w;
+      float xyz[3];
+      orc_float_vertex(pl, ver, t, xyz);
+      const float px = xyz[0], py = xyz[1], pz = xyz[2];
       if (isnan(px) || isnan(py) || isnan(pz)) { null_seen = 1; break; }
       if (write) {
         if (n_pts >= max_points) return -1;

@@ -149,7 +149,8 @@ int64_t orc_cell_topology(int64_t n_cells, const orc_cell_header* cells,
  * counts are computed.  Returns 0, or -1 when a capacity is too small. */
 int orc_cell_polygons(int64_t n_cells, const orc_cell_header* cells,
                       const uint8_t* payload, int triangulate, int boundary_only,
-                      int max_sf_fid, float* points, int64_t max_points,
+                      int max_sf_fid, const double* slice /* NULL or pos[3], normal[3] */,
+                      float* points, int64_t max_points,
                       int64_t* poly_offsets, uint32_t* indices, int64_t max_indices,
                       int32_t* poly_site, int32_t* poly_adj_site, int64_t max_polys,
                       int64_t* counts);
