@@ -649,8 +649,11 @@ def run_fast_only(args):
     for i in range(args.warmup + args.steps):
         st = r.compute()
         out.append(st.as_dict())
-    if args.topology:
+    if args.topology or args.power_cells:
         out[-1]["ms_topology"] = r.compute_topology()
+    if args.power_cells:  # get_all_voro_info + the connected components
+        nb = int((adj["f_adjs"] == 1).sum())
+        out[-1]["ms_power_cells"] = r.compute_power_cells(nb - 1)
     r.close()
     print(json.dumps({"workload": name, "last": out[-1]}))
 
@@ -806,6 +809,8 @@ def main():
                     help="--fast-only: clip kernel register budget (2 = the tuned choice)")
     ap.add_argument("--topology", action="store_true",
                     help="--fast-only: also run the per-cell topology pass after the last step")
+    ap.add_argument("--power-cells", action="store_true",
+                    help="--fast-only: also run the topology and power-cell passes after the last step")
     ap.add_argument("--fast-only", action="store_true",
                     help="only the timed fast path (for profiler launch lists)")
     args = ap.parse_args()

@@ -366,6 +366,21 @@ rpd_status rpd_copy_topology_to_host(struct rpd_ctx* ctx, rpd_topo_header* heade
  *                                     fe_line_id, and the float position
  *                                     (se_line_endpos); per cell from
  *                                     cell_se_line_end_off, sorted, unique
+ *   cell_cc, facet_cc, edge_cc        update_power_cells' connected
+ *                                     components (rpd_update.cxx:454-530)
+ *                                     over cell_nbrs: per cell the index of
+ *                                     its component among its site's cells
+ *                                     (cc_cells), per facet record among the
+ *                                     cells of its (site, neighbour) key
+ *                                     (facet_cc_cells, components ordered by
+ *                                     size, then smallest cell), per edge
+ *                                     record among the cells of its (site,
+ *                                     neighbour pair) (edge_cc_cells); other
+ *                                     components are ordered by smallest
+ *                                     cell, as get_CC_given_neighbors finds
+ *                                     them.  The *_surf_v2fids lists are the
+ *                                     surface records of a component's cells
+ *                                     in ascending cell order.
  * Computes the per-cell topology first when needed. */
 rpd_status rpd_compute_power_cells(struct rpd_ctx* ctx, int max_sf_fid, float* ms);
 
@@ -418,6 +433,9 @@ typedef struct rpd_power_cells_view {
   const int64_t* cell_se_line_end_off;
   const int32_t* se_line_end;       /* 4 per record */
   const float* se_line_end_pos;     /* 3 per record */
+  const int32_t* cell_cc;     /* n_cells */
+  const int32_t* facet_cc;    /* n_facets */
+  const int32_t* edge_cc;     /* n_edges */
 } rpd_power_cells_view;
 rpd_status rpd_get_power_cells(struct rpd_ctx* ctx, rpd_power_cells_view* view);
 

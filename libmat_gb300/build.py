@@ -34,6 +34,7 @@ CUDA_UNITS = {
     "rpd_partial.cu": [],
     "rpd_sort.cu": [],
     "rpd_powercell.cu": ["-fmad=false"],
+    "rpd_cc.cu": [],
 }
 CXX_UNITS = ["rpd_api.cpp", "rpd_mesh.cpp", "rpd_batch.cpp"]
 

@@ -1226,8 +1226,46 @@ rpd_status rpd_compute_power_cells(rpd_ctx* c, int max_sf_fid, float* ms) {
   p.nbr = c->pc_nbr.ptr;
   CK(pc_neighbours(p, n_tf, 1, st), "neighbours");
   CK(pc_neighbours(p, n_tf, 2, st), "neighbours");
+  // connected components: cc_cells, facet_cc_cells, edge_cc_cells
+  const long long n_all = n + n_fa + n_ed;
+  if (n_all > 0x7fffffffll) return fail(c, RPD_ERR_CAPACITY, "rpd_compute_power_cells: too many records");
+  // int32: parent, root, rank, flag, croot (n_all each), size (n_fa), the
+  // three labels (n_all); int64: pos, gstart (n_all + 1), gid (n_all)
+  CK(c->pc_cc_i.ensure((size_t)(6 * n_all + n_fa + 1)), "alloc");
+  CK(c->pc_cc_l.ensure((size_t)(3 * n_all + 2 + power_cell_components_temp(n_all))), "alloc");
+  CK(c->pc_cc_err.ensure(1), "alloc");
+  CK(cudaMemsetAsync(c->pc_cc_err.ptr, 0, sizeof(unsigned int), st), "memset");
+  CcParams cp = {};
+  cp.n = n;
+  cp.n_fa = n_fa;
+  cp.n_ed = n_ed;
+  cp.nbr_off = c->pc_nbr_off.ptr;
+  cp.nbrs = c->pc_nbr.ptr;
+  cp.site_key = keys[3];
+  cp.site_cells = vals[3];
+  cp.facet_keys = keys[1];
+  cp.facet_cells = vals[1];
+  cp.edges = c->pc_ed_out.ptr;
+  cp.parent = c->pc_cc_i.ptr;
+  cp.root = cp.parent + n_all;
+  cp.rank = cp.root + n_all;
+  cp.flag = cp.rank + n_all;
+  cp.croot = cp.flag + n_all;
+  cp.size = cp.croot + n_all;
+  cp.cell_cc = cp.size + n_fa;
+  cp.facet_cc = cp.cell_cc + n;
+  cp.edge_cc = cp.facet_cc + n_fa;
+  cp.pos = c->pc_cc_l.ptr;
+  cp.gstart = cp.pos + (n_all + 1);
+  cp.gid = cp.gstart + (n_all + 1);
+  cp.scan_tmp = cp.gid + n_all;
+  cp.err = c->pc_cc_err.ptr;
+  CK(power_cell_components(cp, st), "components");
+  unsigned int cc_err = 0;
+  CK(cudaMemcpyAsync(&cc_err, c->pc_cc_err.ptr, sizeof(cc_err), cudaMemcpyDeviceToHost, st), "D2H");
   CK(cudaEventRecord(c->ev[kEvTopo1], st), "event");
   CK(cudaStreamSynchronize(st), "sync");
+  if (cc_err) return fail(c, RPD_ERR_CUDA, "rpd_compute_power_cells: component search did not finish");
   if (ms) CK(cudaEventElapsedTime(ms, c->ev[kEvTopo0], c->ev[kEvTopo1]), "event time");
   rpd_power_cells_view& v = c->pc_view;
   v.n_site = n_site;
@@ -1267,6 +1305,9 @@ rpd_status rpd_compute_power_cells(rpd_ctx* c, int max_sf_fid, float* ms) {
   v.cell_se_line_end_off = reinterpret_cast<const int64_t*>(c->pc_off.ptr + 7 * (n + 1));
   v.se_line_end = p.se_end;
   v.se_line_end_pos = p.se_end_pos;
+  v.cell_cc = cp.cell_cc;
+  v.facet_cc = cp.facet_cc;
+  v.edge_cc = cp.edge_cc;
   c->pc_n_nbr = n_nbr;
   c->has_power_cells = true;
   return RPD_OK;

@@ -171,6 +171,9 @@ struct rpd_ctx {
   DevBuf<uint32_t> pc_vals, pc_vals_tmp;
   DevBuf<float> pc_vx_pos, pc_sf_pos;
   DevBuf<int32_t> pc_fe_i;
+  DevBuf<int32_t> pc_cc_i;      // union-find arrays and the component labels
+  DevBuf<long long> pc_cc_l;    // their scans and group ranges
+  DevBuf<unsigned int> pc_cc_err;
   DevBuf<float> pc_fe_pos;
   // TetMesh::tet_es2fe_map: sorted unique keys and (type, id, line) values
   DevBuf<unsigned long long> fe_keys;

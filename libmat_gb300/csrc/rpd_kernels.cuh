@@ -317,6 +317,28 @@ cudaError_t pc_fill(const PowerCellParams& p, cudaStream_t st);
 cudaError_t pc_edges_finish(const PowerCellParams& p, long long n_ed, int pass, cudaStream_t st);
 // feature-edge counts (fill = 0, into cnt rows 5..7) or records (fill = 1)
 cudaError_t pc_feature_edges(const PowerCellParams& p, int fill, cudaStream_t st);
+
+// connected components of the power cells (rpd_cc.cu): per cell, facet
+// record and edge record the index of its component in its group
+struct CcParams {
+  long long n, n_fa, n_ed;
+  const long long* nbr_off;  // n + 1: cells across tet faces
+  const int32_t* nbrs;
+  const unsigned long long* site_key;  // n: site of site_cells[u] (sorted)
+  const uint32_t* site_cells;
+  const unsigned long long* facet_keys;  // sorted, cells ascending per key
+  const uint32_t* facet_cells;
+  const int32_t* edges;  // 7 per record, sorted
+  // n_total = n + n_fa + n_ed entries each (pos, gstart: n_total + 1)
+  int32_t *parent, *root, *rank, *flag, *croot;
+  long long *pos, *gid, *gstart;
+  int32_t* size;      // n_fa: distinct cells per facet component
+  long long* scan_tmp;  // power_cell_components_temp(n_total)
+  int32_t *cell_cc, *facet_cc, *edge_cc;
+  unsigned int* err;
+};
+size_t power_cell_components_temp(long long n_total);
+cudaError_t power_cell_components(const CcParams& p, cudaStream_t st);
 cudaError_t pc_neighbours(const PowerCellParams& p, long long n_tf, int pass, cudaStream_t st);
 cudaError_t pc_site_offsets(const unsigned long long* keys, long long n, int n_site, int shift,
                             long long* off, cudaStream_t st);

@@ -101,7 +101,8 @@ class PowerCellsView(ctypes.Structure):
         ("n_ce_covered", ctypes.c_int64)] + [
         (f, ctypes.c_void_p) for f in ("cell_ce_covered_off", "ce_covered")] + [
         ("n_se_line_end", ctypes.c_int64)] + [
-        (f, ctypes.c_void_p) for f in ("cell_se_line_end_off", "se_line_end", "se_line_end_pos")]
+        (f, ctypes.c_void_p) for f in ("cell_se_line_end_off", "se_line_end", "se_line_end_pos",
+                                       "cell_cc", "facet_cc", "edge_cc")]
 
 
 class Stats(ctypes.Structure):
@@ -627,6 +628,9 @@ class RPD:
         d["cell_se_line_end_off"] = self._d2h(v.cell_se_line_end_off, np.int64, n + 1)
         d["se_line_end"] = self._d2h(v.se_line_end, np.int32, 4 * m).reshape(-1, 4)
         d["se_line_end_pos"] = self._d2h(v.se_line_end_pos, np.float32, 3 * m).reshape(-1, 3)
+        d["cell_cc"] = self._d2h(v.cell_cc, np.int32, n)
+        d["facet_cc"] = self._d2h(v.facet_cc, np.int32, v.n_facets)
+        d["edge_cc"] = self._d2h(v.edge_cc, np.int32, v.n_edges)
         return d
 
     def compute_partial(self, recompute):

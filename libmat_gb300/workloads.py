@@ -113,6 +113,30 @@ def config_small_cube(n=20, n_site=2000, seed=1):
                 flags=np.ones(n_site, np.uint32))
 
 
+def config_slotted_cube(n=10, n_site=80, n_slot_sites=12, seed=4):
+    """A non-convex domain: the n^3 x 6-tet unit cube without the tets of a
+    one-cube-wide slot (x in [0.4, 0.5], y < 0.8, all z), so that power
+    cells of the sites placed in the slot reach both walls and fall into
+    several connected pieces.  Unused vertices are dropped."""
+    rng = np.random.default_rng(seed)
+    vert, tets = cube_grid_mesh(n)
+    c = vert[tets].mean(axis=1)
+    keep = ~((c[:, 0] > 0.4) & (c[:, 0] < 0.5) & (c[:, 1] < 0.8))
+    tets = tets[keep]
+    used = np.unique(tets)
+    remap = np.full(vert.shape[0], -1, np.int64)
+    remap[used] = np.arange(used.shape[0])
+    vert, tets = vert[used], remap[tets].astype(np.int32)
+    xyz = rng.uniform(0.05, 0.95, size=(n_site, 3))
+    slot = np.stack([np.full(n_slot_sites, 0.45), rng.uniform(0.05, 0.7, n_slot_sites),
+                     rng.uniform(0.05, 0.95, n_slot_sites)], axis=1)
+    xyz = np.concatenate([xyz, slot])
+    r = rng.uniform(0.01, 0.05, size=xyz.shape[0])
+    v, x, rr = _normalise(vert, xyz, r)
+    return dict(vert3d=v, tets=tets, sites=_pack_sites(x, rr),
+                flags=np.ones(xyz.shape[0], np.uint32))
+
+
 def config_ellipsoid(target_tets=1_000_000, n_site=50_000, seed=2,
                      axes=(1.0, 0.6, 0.4)):
     """The 'plain vs FP32-filtered at scale' workload: jittered-grid Delaunay

@@ -67,6 +67,28 @@ def _cell(h, payload, th, rec):
 SE, CE = 1, 2  # EdgeType (src/inputs/input_types.h:13-17)
 
 
+def _cc(to_visit, neighbors):
+    """get_CC_given_neighbors (include/common_cxx.h:447-488): breadth-first
+    from the smallest unvisited id, neighbours in ascending order, only
+    those in to_visit; returns the components (sets) in discovery order."""
+    from collections import deque
+    inside, visited, left, out = set(to_visit), set(), set(to_visit), []
+    while left:
+        queue, one = deque([min(left)]), set()
+        while queue:
+            c = queue.popleft()
+            if c in visited:
+                continue
+            visited.add(c)
+            left.discard(c)
+            one.add(c)
+            for nb in sorted(neighbors.get(c, ())):
+                if nb in inside:
+                    queue.append(nb)
+        out.append(one)
+    return out
+
+
 def power_cells(cells, payload, n_site, max_sf_fid, feature_edges=None):
     """cells: emitted cells (HEADER_DTYPE, output order); feature_edges:
     (m, 6) int records or None.  Returns the arrays of rpd_power_cells_view."""
@@ -84,6 +106,7 @@ def power_cells(cells, payload, n_site, max_sf_fid, feature_edges=None):
     tfids = [set() for _ in range(n)]
     facets, edges, verts, surf = [], [], {}, {}
     se_cov, ce_cov, se_end = [set() for _ in range(n)], [set() for _ in range(n)], {}
+    cell_cc, facet_cc, edge_cc = np.zeros(n, np.int32), {}, {}
     for s in range(n_site):
         facet_neigh_to_cells, tfid_to_cells, edge_2endvertices = {}, {}, {}
         for q in by_site[s]:  # ascending cell id
@@ -158,6 +181,21 @@ def power_cells(cells, payload, n_site, max_sf_fid, feature_edges=None):
                 c1, c2 = sorted(cs)
                 nbrs[c1].add(c2)
                 nbrs[c2].add(c1)
+        # update_pc_cc_info, update_pc_facet_cc_info (components sorted by
+        # size, stably: libstdc++'s std::sort on at most 16 elements),
+        # update_pc_edge_cc_info (rpd_update.cxx:454-530)
+        site_nbrs = {q: nbrs[q] for q in by_site[s]}
+        for j, comp in enumerate(_cc(by_site[s], site_nbrs)):
+            for q in comp:
+                cell_cc[q] = j
+        for neigh, cs in facet_neigh_to_cells.items():
+            for j, comp in enumerate(sorted(_cc(cs, site_nbrs), key=len)):
+                for q in comp:
+                    facet_cc[(s, neigh, q)] = j
+        for key, rows in edge_2endvertices.items():
+            for j, comp in enumerate(_cc({q for q, _, _ in rows}, site_nbrs)):
+                for q in comp:
+                    edge_cc[(s, key, q)] = j
         for neigh in sorted(facet_neigh_to_cells):
             for q in sorted(facet_neigh_to_cells[neigh]):
                 facets.append(((s << 32) | neigh, q))
@@ -173,6 +211,9 @@ def power_cells(cells, payload, n_site, max_sf_fid, feature_edges=None):
     out["cell_tfids"] = np.array([f for x in tfids for f in sorted(x)], np.int32)
     out["facet_keys"] = np.array([k for k, _ in facets], np.uint64)
     out["facet_cells"] = np.array([q for _, q in facets], np.uint32)
+    out["cell_cc"] = cell_cc
+    out["facet_cc"] = np.array([facet_cc[(k >> 32, k & 0xffffffff, q)] for k, q in facets], np.int32)
+    out["edge_cc"] = np.array([edge_cc[(e[0], (e[1], e[2]), e[3])] for e in edges], np.int32)
     fs = np.array([k >> 32 for k, _ in facets], np.int64)
     out["site_facet_off"] = np.searchsorted(fs, np.arange(n_site + 1)).astype(np.int64)
     out["edges"] = np.array(edges, np.int32).reshape(-1, 7)

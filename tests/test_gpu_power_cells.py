@@ -67,3 +67,23 @@ def test_power_cells_match_oracle_knn():
     assert cleared["cell_se_line_end_off"][-1] == 0
     # every interior tet face inside one power cell joins two of its cells
     assert got["cell_nbr_off"][-1] > 0
+
+
+def test_components_on_a_non_convex_domain():
+    """The slotted cube splits power cells, facets and edges into several
+    components; every array, the component indices included, equals the
+    oracle's on the device's own cells."""
+    cfg = W.config_slotted_cube()
+    adj = rpd.mesh_adjacency(cfg["vert3d"].shape[0], cfg["tets"])
+    nb = int((adj["f_adjs"] == 1).sum())
+    with rpd.RPD(predicate_mode=rpd.PRED_FP32_FILTER, neighbor_source=rpd.NEIGH_KNN, knn_k=64,
+                 certify=True) as r:
+        r.set_mesh(cfg["vert3d"], cfg["tets"], adj["v_adjs"], adj["e_adj6"], adj["f_adjs"],
+                   adj["f_ids"])
+        r.set_sites(cfg["sites"], cfg["flags"])
+        r.compute()
+        h, p = r.cells()
+        r.compute_power_cells(nb - 1)
+        got = r.power_cells()
+    _same(got, P.power_cells(h, p, cfg["sites"].shape[0], nb - 1))
+    assert got["cell_cc"].max() >= 1 and got["facet_cc"].max() >= 1 and got["edge_cc"].max() >= 1

@@ -96,3 +96,80 @@ def test_feature_edge_records(golden_cases):
         for k in got:
             assert np.array_equal(got[k], ends[k]), (name, k)
         assert len(want[1]) > 0 and len(want[2]) > 0 and len(ends) > 0
+
+
+def _check_groups(labels, members, adj, by_size):
+    """labels[i] of members[i] (cells of one group): the connected
+    components of the group under adj, numbered by smallest cell, or by
+    size then smallest cell."""
+    from scipy.sparse import coo_matrix
+    from scipy.sparse.csgraph import connected_components
+    cells = sorted(set(members))
+    pos = {c: i for i, c in enumerate(cells)}
+    r, c = [], []
+    for a in cells:
+        for b in adj.get(a, ()):
+            if b in pos:
+                r.append(pos[a])
+                c.append(pos[b])
+    m = coo_matrix((np.ones(len(r)), (r, c)), shape=(len(cells), len(cells)))
+    _, comp = connected_components(m, directed=False)
+    lab = {}
+    for cell, l in zip(members, labels):
+        assert lab.setdefault(cell, l) == l
+    # same partition
+    for a in cells:
+        for b in cells:
+            assert (comp[pos[a]] == comp[pos[b]]) == (lab[a] == lab[b])
+    groups = {}
+    for cell in cells:
+        groups.setdefault(lab[cell], []).append(cell)
+    order = sorted(groups.values(), key=lambda g: (len(g), g[0]) if by_size else g[0])
+    assert [lab[g[0]] for g in order] == list(range(len(groups)))
+
+
+def slotted_cells():
+    """Cells of the slotted cube (a non-convex domain) by the oracle's own
+    pipeline: kNN lists, the candidate rule, clipping."""
+    from libmat_gb300 import workloads as W
+    from oracle import oracle as O
+    cfg = W.config_slotted_cube()
+    adj = O.mesh_adjacency(cfg["vert3d"].shape[0], cfg["tets"])
+    mesh = dict(vert3d=cfg["vert3d"], tets=cfg["tets"],
+                **{k: adj[k] for k in ("v_adjs", "e_adj6", "f_adjs", "f_ids")})
+    s4f = cfg["sites"].astype(np.float32)
+    nbr, _ = O.knn(s4f, 64)
+    offs, ps = O.candidate_pairs(cfg["vert3d"].astype(np.float32), cfg["tets"], s4f, cfg["flags"], nbr)
+    h, p, _ = O.clip_cells(mesh, cfg["sites"], nbr, offs, ps)
+    return cfg, adj, h, p
+
+
+def test_power_cell_components(golden_cases):
+    cfg, madj, hs, ps = slotted_cells()
+    cases = [(name, ref_headers(golden_cases[name]), golden_cases[name]["ref_payload"],
+              golden_cases[name]["sites"].shape[0], int((golden_cases[name]["f_adjs"] == 1).sum()))
+             for name in ("cube_k64", "random_full", "dups_flags_holes", "overflow")]
+    cases.append(("slotted", hs, ps, cfg["sites"].shape[0], madj["n_boundary_faces"]))
+    split = 0
+    for name, h, payload, ns, nb in cases:
+        pc = P.power_cells(h, payload, ns, nb - 1)
+        n = len(pc["cell_cc"])
+        adj = {q: set(pc["cell_nbrs"][pc["cell_nbr_off"][q]:pc["cell_nbr_off"][q + 1]].tolist())
+               for q in range(n)}
+        for s in range(ns):
+            cs = pc["site_cells"][pc["site_cell_off"][s]:pc["site_cell_off"][s + 1]].tolist()
+            if cs:
+                _check_groups(pc["cell_cc"][cs].tolist(), cs, adj, False)
+        keys = pc["facet_keys"]
+        for k in np.unique(keys):
+            rows = np.nonzero(keys == k)[0]
+            _check_groups(pc["facet_cc"][rows].tolist(), pc["facet_cells"][rows].tolist(), adj, True)
+        e = pc["edges"]
+        if len(e):
+            _, first = np.unique(e[:, :3], axis=0, return_inverse=True)
+            for g in np.unique(first):
+                rows = np.nonzero(first == g)[0]
+                _check_groups(pc["edge_cc"][rows].tolist(), e[rows, 3].tolist(), adj, False)
+        if name == "slotted":
+            split = min(pc["cell_cc"].max(), pc["facet_cc"].max(), pc["edge_cc"].max())
+    assert split >= 1  # the non-convex domain splits cells, facets and edges
