@@ -478,7 +478,12 @@ constexpr int kPairMaxK = 128;  // longest neighbour list (rpd_config.knn_k <= 1
 // the rule in two parts: each lane tries its own tet against the first
 // kRuleFirst neighbours; the tets that survive wait in a per-warp queue
 // (kRuleQueue entries) and are finished 32 at a time, one per lane
-constexpr int kRuleFirst = 8;
+// (8: 4 to 16 were measured on the 1M-tet workload, 8 the fastest; the
+// macro only serves such sweeps)
+#ifndef RPD_RULE_FIRST
+#define RPD_RULE_FIRST 8
+#endif
+constexpr int kRuleFirst = RPD_RULE_FIRST;
 constexpr int kRuleQueue = 64;
 
 // cell range of the site's box in the tet grid (empty range for no box)
