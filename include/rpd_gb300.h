@@ -381,8 +381,28 @@ rpd_status rpd_copy_topology_to_host(struct rpd_ctx* ctx, rpd_topo_header* heade
  *                                     them.  The *_surf_v2fids lists are the
  *                                     surface records of a component's cells
  *                                     in ascending cell order.
+ *   sfg_*                             with a surface mesh set
+ *                                     (rpd_set_surface_mesh), libmat's
+ *                                     update_sphere_surf_v2fids
+ *                                     (rpd_update.cxx:342-405): per site
+ *                                     (site_sfg_off) its surface faces, each
+ *                                     once with its last surface record
+ *                                     (sfg_record), grouped over the face
+ *                                     adjacency without crossing a
+ *                                     no-cross pair; sorted by group (by
+ *                                     smallest face), then face
+ *                                     (surf_v2fid_in_groups)
  * Computes the per-cell topology first when needed. */
 rpd_status rpd_compute_power_cells(struct rpd_ctx* ctx, int max_sf_fid, float* ms);
+
+/* libmat's SurfaceMesh as update_sphere_surf_v2fids reads it: per
+ * triangle the faces across its three edges (facets.adjacent, -1 for none;
+ * must be symmetric) and the face pairs across sharp edges that a group does
+ * not cross (fe_sf_fs_pairs, n_pairs x 2).  Face ids are the surface face
+ * ids of the cells (tet faces numbered first, <= max_sf_fid).  Used by the
+ * following rpd_compute_power_cells calls; n_faces = 0 clears it. */
+rpd_status rpd_set_surface_mesh(struct rpd_ctx* ctx, const int32_t* facet_adj, int32_t n_faces,
+                                const int32_t* no_cross, int64_t n_pairs);
 
 /* libmat's TetMesh::tet_es2fe_map (<tid, lfid_min, lfid_max> -> <fe_type,
  * fe_id, fe_line_id>, src/rpd3d_base/rpd_update.cxx:77-82), one record per
@@ -436,6 +456,11 @@ typedef struct rpd_power_cells_view {
   const int32_t* cell_cc;     /* n_cells */
   const int32_t* facet_cc;    /* n_facets */
   const int32_t* edge_cc;     /* n_edges */
+  int64_t n_sfg;
+  const int64_t* site_sfg_off;  /* n_site + 1 */
+  const int32_t* sfg_group;
+  const int32_t* sfg_fid;
+  const int32_t* sfg_record;  /* index into surface_* */
 } rpd_power_cells_view;
 rpd_status rpd_get_power_cells(struct rpd_ctx* ctx, rpd_power_cells_view* view);
 

@@ -1083,6 +1083,44 @@ rpd_status rpd_set_feature_edges(rpd_ctx* c, const rpd_feature_edge* fe, int64_t
   return RPD_OK;
 }
 
+rpd_status rpd_set_surface_mesh(rpd_ctx* c, const int32_t* facet_adj, int32_t n_faces,
+                                const int32_t* no_cross, int64_t n_pairs) {
+  if (!c) return RPD_ERR_INVALID_ARGUMENT;
+  if (n_faces < 0 || n_pairs < 0 || (n_faces > 0 && !facet_adj) || (n_pairs > 0 && !no_cross))
+    return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_set_surface_mesh: bad arguments");
+  for (long long f = 0; f < n_faces; ++f)
+    for (int le = 0; le < 3; ++le) {
+      const int32_t g = facet_adj[3 * f + le];
+      if (g < -1 || g >= n_faces)
+        return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_set_surface_mesh: face id out of range");
+      if (g >= 0 && facet_adj[3 * g] != f && facet_adj[3 * g + 1] != f && facet_adj[3 * g + 2] != f)
+        return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_set_surface_mesh: adjacency not symmetric");
+    }
+  std::vector<unsigned long long> keys((size_t)n_pairs);
+  for (int64_t i = 0; i < n_pairs; ++i) {
+    const int32_t a = no_cross[2 * i], b = no_cross[2 * i + 1];
+    if (a < 0 || b < 0 || a >= n_faces || b >= n_faces)
+      return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_set_surface_mesh: pair face id out of range");
+    keys[i] = ((unsigned long long)(uint32_t)std::min(a, b) << 32) | (uint32_t)std::max(a, b);
+  }
+  std::sort(keys.begin(), keys.end());
+  keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  CK(c->sf_adj.ensure((size_t)std::max(3ll * n_faces, 3ll)), "alloc");
+  CK(c->sf_no_cross.ensure(std::max(keys.size(), (size_t)1)), "alloc");
+  if (n_faces > 0)
+    CK(cudaMemcpyAsync(c->sf_adj.ptr, facet_adj, sizeof(int32_t) * 3 * (size_t)n_faces,
+                       cudaMemcpyHostToDevice, c->stream), "H2D");
+  if (!keys.empty())
+    CK(cudaMemcpyAsync(c->sf_no_cross.ptr, keys.data(), sizeof(unsigned long long) * keys.size(),
+                       cudaMemcpyHostToDevice, c->stream), "H2D");
+  CK(cudaStreamSynchronize(c->stream), "sync");
+  c->sf_faces = n_faces;
+  c->sf_n_no_cross = (long long)keys.size();
+  c->has_power_cells = false;
+  return RPD_OK;
+}
+
 rpd_status rpd_compute_power_cells(rpd_ctx* c, int max_sf_fid, float* ms) {
   if (!c) return RPD_ERR_INVALID_ARGUMENT;
   if (!c->has_result) return fail(c, RPD_ERR_NOT_READY, "rpd_compute_power_cells: no result");
@@ -1261,6 +1299,47 @@ rpd_status rpd_compute_power_cells(rpd_ctx* c, int max_sf_fid, float* ms) {
   cp.scan_tmp = cp.gid + n_all;
   cp.err = c->pc_cc_err.ptr;
   CK(power_cell_components(cp, st), "components");
+  // surface groups (update_sphere_surf_v2fids), with a surface mesh set
+  const long long n_sg = c->sf_faces > 0 ? n_sf : 0;
+  const size_t sg_hist = radix_hist_ints(std::max(n_sg, 1ll));
+  CK(c->sfg_k.ensure((size_t)std::max(3 * n_sg, 3ll)), "alloc");
+  CK(c->sfg_v.ensure((size_t)std::max(2 * n_sg, 2ll)), "alloc");
+  CK(c->sfg_i.ensure((size_t)std::max(8 * n_sg, 8ll) + sg_hist + scan_temp_ints((long long)sg_hist) + 16),
+     "alloc");
+  CK(c->sfg_l.ensure((size_t)(n_sg + 1 + (n_site + 1) + scan64_temp(std::max(n_sg, 1ll)) + 16)), "alloc");
+  SurfaceGroupParams sg = {};
+  sg.n_sf = n_sg;
+  sg.n_site = n_site;
+  sg.site_bits = site_bits;
+  sg.cells = c->cells.ptr;
+  sg.surface_cell = p.sf_cell;
+  sg.surface_fid = p.sf_fid;
+  sg.facet_adj = c->sf_adj.ptr;
+  sg.n_faces = c->sf_faces;
+  sg.no_cross = c->sf_no_cross.ptr;
+  sg.n_no_cross = c->sf_n_no_cross;
+  const long long m = std::max(n_sg, 1ll);
+  sg.keys = c->sfg_k.ptr;
+  sg.keys_tmp = sg.keys + m;
+  sg.ekey = sg.keys_tmp + m;
+  sg.vals = c->sfg_v.ptr;
+  sg.vals_tmp = sg.vals + m;
+  sg.flag = c->sfg_i.ptr;
+  sg.erec = sg.flag + m;
+  sg.parent = sg.erec + m;
+  sg.root = sg.parent + m;
+  sg.rank = sg.root + m;
+  sg.out_group = sg.rank + m;
+  sg.out_fid = sg.out_group + m;
+  sg.out_rec = sg.out_fid + m;
+  sg.hist = sg.out_rec + m;
+  sg.hist_tmp = sg.hist + sg_hist;
+  sg.pos = c->sfg_l.ptr;
+  sg.site_off = sg.pos + (m + 1);
+  sg.scan_tmp = sg.site_off + (n_site + 1);
+  sg.err = c->pc_cc_err.ptr;
+  long long n_sfg = 0;
+  CK(surface_groups(sg, &n_sfg, st), "surface groups");
   unsigned int cc_err = 0;
   CK(cudaMemcpyAsync(&cc_err, c->pc_cc_err.ptr, sizeof(cc_err), cudaMemcpyDeviceToHost, st), "D2H");
   CK(cudaEventRecord(c->ev[kEvTopo1], st), "event");
@@ -1305,6 +1384,11 @@ rpd_status rpd_compute_power_cells(rpd_ctx* c, int max_sf_fid, float* ms) {
   v.cell_se_line_end_off = reinterpret_cast<const int64_t*>(c->pc_off.ptr + 7 * (n + 1));
   v.se_line_end = p.se_end;
   v.se_line_end_pos = p.se_end_pos;
+  v.n_sfg = n_sfg;
+  v.site_sfg_off = reinterpret_cast<const int64_t*>(sg.site_off);
+  v.sfg_group = sg.out_group;
+  v.sfg_fid = sg.out_fid;
+  v.sfg_record = sg.out_rec;
   v.cell_cc = cp.cell_cc;
   v.facet_cc = cp.facet_cc;
   v.edge_cc = cp.edge_cc;

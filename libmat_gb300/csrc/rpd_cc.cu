@@ -206,7 +206,142 @@ __global__ void cc_label_kernel(CcParams p) {
 
 unsigned blocks_for(long long n) { return (unsigned)((n + 255) / 256 > 0 ? (n + 255) / 256 : 1); }
 
+// ---- surface groups (update_sphere_surf_v2fids) ----------------------------
+
+__device__ __forceinline__ long long lower_u64(const unsigned long long* a, long long n,
+                                               unsigned long long k) {
+  long long lo = 0, hi = n;
+  while (lo < hi) {
+    const long long mid = (lo + hi) >> 1;
+    if (a[mid] < k) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// (site, face) key of every surface record, the record as value
+__global__ void sfg_keys_kernel(SurfaceGroupParams p) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= p.n_sf) return;
+  const int site = p.cells[p.surface_cell[k]].site_id;
+  p.keys[k] = ((unsigned long long)(uint32_t)site << 32) | (uint32_t)p.surface_fid[k];
+  p.vals[k] = (uint32_t)k;
+}
+
+// the last record of each (site, face): the map's last assignment (records
+// are in cell order, the sort is stable)
+__global__ void sfg_last_kernel(SurfaceGroupParams p) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < p.n_sf) p.flag[i] = (i == p.n_sf - 1 || p.keys[i + 1] != p.keys[i]) ? 1 : 0;
+}
+
+__global__ void sfg_compact_kernel(SurfaceGroupParams p) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.n_sf || !p.flag[i]) return;
+  const long long e = p.pos[i];
+  p.ekey[e] = p.keys[i];
+  p.erec[e] = (int32_t)p.vals[i];
+  p.parent[e] = (int32_t)e;
+}
+
+// joins each (site, face) with the site's entries of the faces across its
+// edges, unless the edge is sharp (a no-cross pair)
+__global__ void sfg_union_kernel(SurfaceGroupParams p, long long n_e) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n_e) return;
+  const unsigned long long key = p.ekey[e];
+  const unsigned long long site = key >> 32;
+  const long long f = (long long)(uint32_t)key;
+  if (f >= p.n_faces) return;
+  bool ok = true;
+  for (int le = 0; le < 3; ++le) {
+    const int nf = p.facet_adj[3 * f + le];
+    if (nf < 0) continue;
+    const unsigned long long lo = (unsigned long long)(f < nf ? f : nf), hi = (unsigned long long)(f < nf ? nf : f);
+    const unsigned long long pk = (lo << 32) | hi;
+    const long long c = lower_u64(p.no_cross, p.n_no_cross, pk);
+    if (c < p.n_no_cross && p.no_cross[c] == pk) continue;
+    const unsigned long long want = (site << 32) | (uint32_t)nf;
+    const long long j = lower_u64(p.ekey, n_e, want);
+    if (j < n_e && p.ekey[j] == want) ok &= uf_unite(p.parent, (int)e, (int)j);
+  }
+  if (!ok) atomicOr(p.err, 1u);
+}
+
+__global__ void sfg_roots_kernel(SurfaceGroupParams p, long long n_e) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n_e) return;
+  const int r = uf_find(p.parent, (int)e);
+  p.root[e] = r;
+  p.flag[e] = r == e ? 1 : 0;
+}
+
+// group number of each root: its prefix count among its site's roots (faces
+// ascending, so groups are ordered by smallest face)
+__global__ void sfg_rank_kernel(SurfaceGroupParams p, long long n_e) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n_e || !p.flag[e]) return;
+  const long long start = lower_u64(p.ekey, n_e, p.ekey[e] & 0xffffffff00000000ull);
+  p.rank[e] = (int32_t)(p.pos[e] - p.pos[start]);
+}
+
+// (site, group) keys for the output order; faces stay ascending in a group
+__global__ void sfg_out_keys_kernel(SurfaceGroupParams p, long long n_e) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n_e) return;
+  p.keys[e] = (p.ekey[e] & 0xffffffff00000000ull) | (uint32_t)p.rank[p.root[e]];
+  p.vals[e] = (uint32_t)e;
+}
+
+__global__ void sfg_gather_kernel(SurfaceGroupParams p, long long n_e) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_e) return;
+  const long long e = p.vals[i];
+  p.out_group[i] = (int32_t)(uint32_t)p.keys[i];
+  p.out_fid[i] = (int32_t)(uint32_t)p.ekey[e];
+  p.out_rec[i] = p.erec[e];
+}
+
 }  // namespace
+
+cudaError_t surface_groups(const SurfaceGroupParams& p, long long* n_entries, cudaStream_t st) {
+  *n_entries = 0;
+  if (p.n_sf <= 0)
+    return cudaMemsetAsync(p.site_off, 0, sizeof(long long) * (size_t)(p.n_site + 1), st);
+  if (p.n_sf > 0x7fffffffll) return cudaErrorInvalidValue;
+  const unsigned nb = blocks_for(p.n_sf);
+  sfg_keys_kernel<<<nb, 256, 0, st>>>(p);
+  note_launches(1);
+  cudaError_t e = radix_sort_pairs(p.keys, p.vals, p.n_sf, 32 + p.site_bits, p.keys_tmp, p.vals_tmp,
+                                   p.hist, p.hist_tmp, st);
+  if (e != cudaSuccess) return e;
+  sfg_last_kernel<<<nb, 256, 0, st>>>(p);
+  note_launches(1);
+  e = scan64_exclusive(p.flag, p.pos, p.n_sf, p.scan_tmp, st);
+  long long n_e = 0;
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&n_e, p.pos + p.n_sf, sizeof(n_e), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return e;
+  const unsigned ne = blocks_for(n_e);
+  sfg_compact_kernel<<<nb, 256, 0, st>>>(p);
+  sfg_union_kernel<<<ne, 256, 0, st>>>(p, n_e);
+  sfg_roots_kernel<<<ne, 256, 0, st>>>(p, n_e);
+  note_launches(3);
+  e = scan64_exclusive(p.flag, p.pos, n_e, p.scan_tmp, st);
+  if (e != cudaSuccess) return e;
+  sfg_rank_kernel<<<ne, 256, 0, st>>>(p, n_e);
+  sfg_out_keys_kernel<<<ne, 256, 0, st>>>(p, n_e);
+  note_launches(2);
+  e = radix_sort_pairs(p.keys, p.vals, n_e, 32 + p.site_bits, p.keys_tmp, p.vals_tmp, p.hist,
+                       p.hist_tmp, st);
+  if (e != cudaSuccess) return e;
+  sfg_gather_kernel<<<ne, 256, 0, st>>>(p, n_e);
+  note_launches(1);
+  e = pc_site_offsets(p.keys, n_e, p.n_site, 32, p.site_off, st);
+  *n_entries = n_e;
+  return e != cudaSuccess ? e : cudaGetLastError();
+}
 
 size_t power_cell_components_temp(long long n_total) { return scan64_temp(n_total + 1); }
 

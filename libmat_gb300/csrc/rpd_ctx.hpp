@@ -174,6 +174,15 @@ struct rpd_ctx {
   DevBuf<int32_t> pc_cc_i;      // union-find arrays and the component labels
   DevBuf<long long> pc_cc_l;    // their scans and group ranges
   DevBuf<unsigned int> pc_cc_err;
+  // surface mesh for the surface groups (rpd_set_surface_mesh) and scratch
+  DevBuf<int32_t> sf_adj;
+  DevBuf<unsigned long long> sf_no_cross;
+  int sf_faces = 0;
+  long long sf_n_no_cross = 0;
+  DevBuf<unsigned long long> sfg_k;
+  DevBuf<uint32_t> sfg_v;
+  DevBuf<int32_t> sfg_i;
+  DevBuf<long long> sfg_l;
   DevBuf<float> pc_fe_pos;
   // TetMesh::tet_es2fe_map: sorted unique keys and (type, id, line) values
   DevBuf<unsigned long long> fe_keys;

@@ -339,6 +339,31 @@ struct CcParams {
 };
 size_t power_cell_components_temp(long long n_total);
 cudaError_t power_cell_components(const CcParams& p, cudaStream_t st);
+
+// surface groups of each site (rpd_cc.cu): its surface faces (the last
+// record of each) grouped over the surface mesh's face adjacency, not across
+// no-cross pairs; output sorted by (site, group, face)
+struct SurfaceGroupParams {
+  long long n_sf;
+  int n_site, site_bits;
+  const rpd_cell_header* cells;
+  const int32_t *surface_cell, *surface_fid;
+  const int32_t* facet_adj;  // 3 per face, -1 for none
+  int n_faces;
+  const unsigned long long* no_cross;  // sorted (min << 32 | max) face pairs
+  long long n_no_cross;
+  unsigned long long *keys, *keys_tmp;  // n_sf each
+  uint32_t *vals, *vals_tmp;
+  int32_t *hist, *hist_tmp;  // radix_hist_ints(n_sf), scan_temp_ints(of that)
+  int32_t* flag;             // n_sf
+  long long *pos, *scan_tmp;  // n_sf + 1, scan64_temp(n_sf)
+  unsigned long long* ekey;   // entries (n_sf at most)
+  int32_t *erec, *parent, *root, *rank;
+  int32_t *out_group, *out_fid, *out_rec;
+  long long* site_off;  // n_site + 1
+  unsigned int* err;
+};
+cudaError_t surface_groups(const SurfaceGroupParams& p, long long* n_entries, cudaStream_t st);
 cudaError_t pc_neighbours(const PowerCellParams& p, long long n_tf, int pass, cudaStream_t st);
 cudaError_t pc_site_offsets(const unsigned long long* keys, long long n, int n_site, int shift,
                             long long* off, cudaStream_t st);

@@ -56,7 +56,7 @@ EXPORTS = [
     "rpd_compute_polygons", "rpd_get_polygons", "rpd_copy_polygons_to_host", "rpd_dist2mat",
     "rpd_compute_partial", "rpd_compute_power_cells", "rpd_get_power_cells",
     "rpd_set_feature_edges", "rpd_copy_device_to_host", "rpd_set_polygon_slice",
-    "rpd_write_polygons_bgeo",
+    "rpd_write_polygons_bgeo", "rpd_set_surface_mesh",
     "rpd_batch_create", "rpd_batch_destroy", "rpd_batch_last_error", "rpd_batch_add_mesh",
     "rpd_batch_size", "rpd_batch_set_graph", "rpd_batch_compute", "rpd_batch_autotune",
     "rpd_batch_mesh_cells", "rpd_batch_copy_mesh_cells", "rpd_batch_context",
@@ -102,7 +102,9 @@ class PowerCellsView(ctypes.Structure):
         (f, ctypes.c_void_p) for f in ("cell_ce_covered_off", "ce_covered")] + [
         ("n_se_line_end", ctypes.c_int64)] + [
         (f, ctypes.c_void_p) for f in ("cell_se_line_end_off", "se_line_end", "se_line_end_pos",
-                                       "cell_cc", "facet_cc", "edge_cc")]
+                                       "cell_cc", "facet_cc", "edge_cc")] + [
+        ("n_sfg", ctypes.c_int64)] + [
+        (f, ctypes.c_void_p) for f in ("site_sfg_off", "sfg_group", "sfg_fid", "sfg_record")]
 
 
 class Stats(ctypes.Structure):
@@ -243,6 +245,8 @@ def load(path=LIB_PATH):
     L.rpd_get_power_cells.argtypes = [vp, c.POINTER(PowerCellsView)]
     L.rpd_set_feature_edges.restype = i32
     L.rpd_set_feature_edges.argtypes = [vp, vp, i64]
+    L.rpd_set_surface_mesh.restype = i32
+    L.rpd_set_surface_mesh.argtypes = [vp, vp, i32, vp, i64]
     L.rpd_set_polygon_slice.restype = i32
     L.rpd_set_polygon_slice.argtypes = [vp, i32, vp, vp]
     L.rpd_write_polygons_bgeo.restype = i32
@@ -586,6 +590,14 @@ class RPD:
                                  np.int32).reshape(-1, 6)
         self._check(self._L.rpd_set_feature_edges(self._h, _p(r), r.shape[0]))
 
+    def set_surface_mesh(self, facet_adj, no_cross=None):
+        """libmat's SurfaceMesh for the surface groups: (n_faces, 3) face
+        adjacency (-1 for none) and (m, 2) no-cross face pairs; None clears."""
+        a = np.ascontiguousarray(np.zeros((0, 3)) if facet_adj is None else facet_adj, np.int32)
+        b = np.ascontiguousarray(np.zeros((0, 2)) if no_cross is None else no_cross, np.int32)
+        self._check(self._L.rpd_set_surface_mesh(self._h, _p(a), a.reshape(-1, 3).shape[0], _p(b),
+                                                 b.reshape(-1, 2).shape[0]))
+
     def _d2h(self, ptr, dtype, count):
         out = np.zeros(max(int(count), 1), dtype)
         if count > 0:
@@ -631,6 +643,9 @@ class RPD:
         d["cell_cc"] = self._d2h(v.cell_cc, np.int32, n)
         d["facet_cc"] = self._d2h(v.facet_cc, np.int32, v.n_facets)
         d["edge_cc"] = self._d2h(v.edge_cc, np.int32, v.n_edges)
+        d["site_sfg_off"] = self._d2h(v.site_sfg_off, np.int64, ns + 1)
+        for f in ("sfg_group", "sfg_fid", "sfg_record"):
+            d[f] = self._d2h(getattr(v, f), np.int32, v.n_sfg)
         return d
 
     def compute_partial(self, recompute):

@@ -89,9 +89,10 @@ def _cc(to_visit, neighbors):
     return out
 
 
-def power_cells(cells, payload, n_site, max_sf_fid, feature_edges=None):
+def power_cells(cells, payload, n_site, max_sf_fid, feature_edges=None, surface=None):
     """cells: emitted cells (HEADER_DTYPE, output order); feature_edges:
-    (m, 6) int records or None.  Returns the arrays of rpd_power_cells_view."""
+    (m, 6) int records or None; surface: (facet_adj (n_faces, 3), no_cross
+    pairs (m, 2)) or None.  Returns the arrays of rpd_power_cells_view."""
     fe = {}
     if feature_edges is not None:
         for r in np.asarray(feature_edges, np.int64).reshape(-1, 6):
@@ -230,6 +231,41 @@ def power_cells(cells, payload, n_site, max_sf_fid, feature_edges=None):
     out["surface_fid"] = np.array([f for q in sk for f, _ in surf[q]], np.int32)
     out["surface_pos"] = np.array([p for q in sk for _, p in surf[q]], np.float32).reshape(-1, 3)
     out["cell_surface_off"] = np.searchsorted(out["surface_cell"], np.arange(n + 1)).astype(np.int64)
+    # update_sphere_surf_v2fids (rpd_update.cxx:342-405): per sphere its
+    # surface faces (the last record of each face, cells ascending), grouped
+    # over the surface mesh's face adjacency without crossing sharp edges
+    rec_at, k = {}, 0
+    for q in sk:
+        for j in range(len(surf[q])):
+            rec_at[(q, j)] = k
+            k += 1
+    sfg = []
+    if surface is not None:
+        fadj = np.asarray(surface[0]).reshape(-1, 3)
+        no_cross = {(min(int(a), int(b)), max(int(a), int(b))) for a, b in np.asarray(surface[1]).reshape(-1, 2)}
+        for s_ in range(n_site):
+            fid2rec = {}
+            for q in by_site[s_]:
+                for j, (fid, _) in enumerate(surf.get(q, [])):
+                    fid2rec[fid] = rec_at[(q, j)]
+            fids = set(fid2rec)
+            nb = {}
+            for f in sorted(fids):
+                if f >= fadj.shape[0]:
+                    continue
+                for nf in fadj[f]:
+                    nf = int(nf)
+                    if nf < 0 or (min(f, nf), max(f, nf)) in no_cross or nf not in fids:
+                        continue
+                    nb.setdefault(f, set()).add(nf)
+            for j, comp in enumerate(_cc(fids, nb)):
+                for f in sorted(comp):
+                    sfg.append((s_, j, f, fid2rec[f]))
+    sfg = np.array(sfg, np.int64).reshape(-1, 4)
+    out["site_sfg_off"] = np.searchsorted(sfg[:, 0], np.arange(n_site + 1)).astype(np.int64)
+    out["sfg_group"] = sfg[:, 1].astype(np.int32)
+    out["sfg_fid"] = sfg[:, 2].astype(np.int32)
+    out["sfg_record"] = sfg[:, 3].astype(np.int32)
     for name, cov in (("se_covered", se_cov), ("ce_covered", ce_cov)):
         out["cell_%s_off" % name] = np.cumsum([0] + [len(x) for x in cov]).astype(np.int64)
         out[name] = np.array([r for x in cov for r in sorted(x)], np.int32).reshape(-1, 5)

@@ -137,3 +137,36 @@ def feature_edge_records(n_tet, seed, frac=0.3):
     again[:, 3] = rng.choice([1, 2], size=len(again))
     again[:, 4] += 1000
     return np.concatenate([recs, again]).astype(np.int32)
+
+
+FACE_LV = [(2, 1, 3), (0, 2, 3), (1, 0, 3), (0, 1, 2)]  # tet face f leaves out vertex f
+
+
+def surface_mesh(vert, tets, f_adjs, f_ids):
+    """libmat's SurfaceMesh inputs of the surface groups, from a tet mesh:
+    its boundary triangles (face ids 0 .. nb - 1, numbered first), per face
+    the faces across its three edges (-1 for none), and the pairs across a
+    sharp edge (normals more than ~8 degrees apart) as the no-cross pairs."""
+    f_adjs, f_ids = np.asarray(f_adjs), np.asarray(f_ids)
+    nb = int((f_adjs == 1).sum())
+    tri = np.zeros((nb, 3), np.int64)
+    for t, f in zip(*np.nonzero(f_adjs == 1)):
+        tri[f_ids[t, f]] = np.asarray(tets)[t, list(FACE_LV[f])]
+    edge_faces = {}
+    for fid in range(nb):
+        for le in range(3):
+            a, b = int(tri[fid, le]), int(tri[fid, (le + 1) % 3])
+            edge_faces.setdefault((min(a, b), max(a, b)), []).append(fid)
+    adj = -np.ones((nb, 3), np.int32)
+    for fid in range(nb):
+        for le in range(3):
+            a, b = int(tri[fid, le]), int(tri[fid, (le + 1) % 3])
+            others = [x for x in edge_faces[(min(a, b), max(a, b))] if x != fid]
+            if len(others) == 1:
+                adj[fid, le] = others[0]
+    p = np.asarray(vert)[tri]
+    nrm = np.cross(p[:, 1] - p[:, 0], p[:, 2] - p[:, 0])
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    pairs = [(f, int(g)) for f in range(nb) for g in adj[f]
+             if g > f and abs(float(nrm[f] @ nrm[g])) < 0.99]
+    return adj, np.array(pairs, np.int32).reshape(-1, 2)

@@ -7,7 +7,7 @@ import pytest
 from libmat_gb300 import rpd
 from libmat_gb300 import workloads as W
 from oracle import powercell_oracle as P
-from tests.helpers import feature_edge_records
+from tests.helpers import feature_edge_records, surface_mesh
 
 pytestmark = pytest.mark.gpu
 
@@ -83,7 +83,15 @@ def test_components_on_a_non_convex_domain():
         r.set_sites(cfg["sites"], cfg["flags"])
         r.compute()
         h, p = r.cells()
+        sadj, pairs = surface_mesh(cfg["vert3d"], cfg["tets"], adj["f_adjs"], adj["f_ids"])
+        bad = sadj.copy()  # face 0 names a face that does not name it back
+        bad[0, 0] = next(g for g in range(1, sadj.shape[0]) if 0 not in sadj[g])
+        for a, b in ((bad, pairs), (sadj, pairs + sadj.shape[0])):
+            with pytest.raises(rpd.RPDError):
+                r.set_surface_mesh(a, b)
+        r.set_surface_mesh(sadj, pairs)
         r.compute_power_cells(nb - 1)
         got = r.power_cells()
-    _same(got, P.power_cells(h, p, cfg["sites"].shape[0], nb - 1))
+    _same(got, P.power_cells(h, p, cfg["sites"].shape[0], nb - 1, surface=(sadj, pairs)))
     assert got["cell_cc"].max() >= 1 and got["facet_cc"].max() >= 1 and got["edge_cc"].max() >= 1
+    assert got["sfg_group"].max() >= 1

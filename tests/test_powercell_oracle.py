@@ -173,3 +173,33 @@ def test_power_cell_components(golden_cases):
         if name == "slotted":
             split = min(pc["cell_cc"].max(), pc["facet_cc"].max(), pc["edge_cc"].max())
     assert split >= 1  # the non-convex domain splits cells, facets and edges
+
+
+def test_surface_groups():
+    """update_sphere_surf_v2fids: per site, its surface faces once (with the
+    last record of the face), in groups that are the components of the face
+    adjacency without the sharp pairs, ordered by smallest face."""
+    from tests.helpers import surface_mesh
+    cfg, madj, h, p = slotted_cells()
+    adj, pairs = surface_mesh(cfg["vert3d"], cfg["tets"], madj["f_adjs"], madj["f_ids"])
+    assert len(pairs) > 0
+    ns, nb = cfg["sites"].shape[0], madj["n_boundary_faces"]
+    pc = P.power_cells(h, p, ns, nb - 1, surface=(adj, pairs))
+    sharp = {(min(a, b), max(a, b)) for a, b in pairs.tolist()}
+    nbrs = {f: {int(g) for g in adj[f] if g >= 0 and (min(f, g), max(f, g)) not in sharp}
+            for f in range(adj.shape[0])}
+    site_of_rec = h[h["status"] == SUCCESS]["site_id"][pc["surface_cell"]]
+    split = 0
+    for s in range(ns):
+        a, b = pc["site_sfg_off"][s], pc["site_sfg_off"][s + 1]
+        fids = pc["sfg_fid"][a:b].tolist()
+        recs = np.nonzero(site_of_rec == s)[0]
+        assert sorted(fids) == sorted(set(pc["surface_fid"][recs].tolist()))
+        for f, r in zip(fids, pc["sfg_record"][a:b]):  # the last record of the face
+            assert r == recs[pc["surface_fid"][recs] == f].max()
+        if fids:
+            _check_groups(pc["sfg_group"][a:b].tolist(), fids, nbrs, False)
+            split = max(split, int(pc["sfg_group"][a:b].max()))
+        g = pc["sfg_group"][a:b]
+        assert np.all(np.diff(g) >= 0)  # grouped, faces ascending in a group
+    assert split >= 1
