@@ -459,6 +459,10 @@ def run_ours(args):
         "tuning": tuning,
         "learned": learned,
         "reclipped": int(st.n_reclipped),
+        # cells whose whole 64-entry list left the certificate unproven: sites
+        # beyond the list may cut them (the reference's triangulation lists
+        # have none); the topology comparison above uses the same lists
+        "uncertified_cells": int(st.n_uncertified),
         "stage_ms": {"knn": st.ms_knn, "pairs": st.ms_pairs, "clip": st.ms_clip,
                      "clip_kernel": st.ms_clip_kernel, "epilogue": st.ms_epilogue,
                      "predict": st.ms_predict, "compact": st.ms_compact},

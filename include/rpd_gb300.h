@@ -102,6 +102,15 @@ typedef struct rpd_config {
 } rpd_config;
 
 /* One record per candidate (tet, site) pair; 32 bytes. */
+/* rpd_cell_header.flags: set on an emitted cell of a certified compute
+ * (config.certify, GPU-built lists) that was clipped by its site's whole
+ * list without the security-radius certificate holding: sites beyond the
+ * list may still cut it, so it can be larger than the exact restricted
+ * cell.  Lists holding all power neighbours (libmat's triangulation
+ * neighbours through rpd_set_neighbors) give exact cells; a longer knn_k
+ * flags fewer. */
+#define RPD_CELL_UNCERTIFIED 1u
+
 typedef struct rpd_cell_header {
   int32_t tet_id;
   int32_t site_id;
@@ -150,6 +159,7 @@ typedef struct rpd_stats {
   int64_t n_exact_flips;      /* RPD_PRED_EXACT: of those, exact sign !=
                                  FP64 sign (where the reference errs) */
   float ms_epilogue;          /* coordinates, volumes, hashes (in ms_clip) */
+  int64_t n_uncertified;      /* emitted cells flagged RPD_CELL_UNCERTIFIED */
 } rpd_stats;
 
 typedef struct rpd_cells_view {

@@ -502,7 +502,7 @@ static rpd_status finish_compute(rpd_ctx* c, bool knn, bool learned, rpd_stats* 
   const float cert_margin = (float)(16.0 * std::ldexp(1.0, -24) * (L + std::sqrt(D2)) + 1e-30);
   c->n_reclipped = 0;
   for (int attempt = 0; attempt < 3; ++attempt) {
-    CK(cudaMemsetAsync(c->scratch.ptr + 28, 0, 3 * sizeof(unsigned long long), st), "memset");
+    CK(cudaMemsetAsync(c->scratch.ptr + 28, 0, 4 * sizeof(unsigned long long), st), "memset");
     CK(c->payload.ensure((size_t)pcap), "alloc payload");
     CK(cudaMemsetAsync(c->scratch.ptr, 0, 4 * sizeof(unsigned long long), st), "memset");
     ClipParams p;
@@ -537,6 +537,7 @@ static rpd_status finish_compute(rpd_ctx* c, bool knn, bool learned, rpd_stats* 
     p.pair_klen = learned ? c->pair_klen.ptr : (use_pair_k ? c->user_pair_k.ptr : nullptr);
     p.lazy_cert = (learned || use_pair_k) ? 1 : 0;
     p.misses = c->scratch.ptr + 28;
+    p.uncertified = c->scratch.ptr + 31;
     p.consumed = (certify && c->want_consumed) ? c->consumed.ptr : nullptr;
     p.cert_margin = cert_margin;
     p.pair_index = nullptr;
@@ -639,6 +640,7 @@ static rpd_status finish_compute(rpd_ctx* c, bool knn, bool learned, rpd_stats* 
     stats->learned = learned ? 1 : 0;
     stats->n_fp64_uncertain = (int64_t)host_scratch[29];
     stats->n_exact_flips = (int64_t)host_scratch[30];
+    stats->n_uncertified = (int64_t)host_scratch[31];
     cudaEventElapsedTime(&stats->ms_epilogue, c->ev[kEvEpi0], c->ev[kEvClip]);
   }
   return RPD_OK;

@@ -691,6 +691,7 @@ struct Cert {
   bool lazy;          // test the certificate once, after the whole (short) list
   bool certified;
   int consumed;       // list entries taken before the certificate held
+  float R;            // eager: the cell radius bound after the last clip
 };
 
 __device__ __forceinline__ bool cert_holds(float key, float R, float margin) {
@@ -834,6 +835,7 @@ __device__ void clip_list(WarpCell& c, CellState& s, const int32_t* list, int k,
       break;
     }
   }
+  cert.R = R;
 }
 
 // ------------------------------------------------------------------------
@@ -1117,6 +1119,7 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : kClipMaxThreads, MINB > 0 ? M
   const int wid = threadIdx.x >> 5;
   WarpCell& c = reinterpret_cast<WarpCell*>(smem_raw)[wid];
   PredCount pc = {0u, 0u, p.exact_counters};
+  unsigned int n_uncert = 0;  // lane-uniform
 
   for (;;) {
     long long q = 0;
@@ -1195,6 +1198,17 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : kClipMaxThreads, MINB > 0 ? M
       }
     }
     if (p.consumed && lane == 0) p.consumed[q] = cert.consumed;
+    // a cell clipped by its whole, full list (no -1 before the end) without
+    // the certificate holding: unseen sites have keys >= the list's last, so
+    // one test against that key still certifies it; otherwise sites beyond
+    // the list may cut it and it is flagged (lists of all power neighbours,
+    // as libmat's triangulation gives, leave no such cells)
+    bool uncert = false;
+    if (CERT && s.status == kSuccess && !cert.certified && klen == p.k && cert.consumed >= p.k) {
+      const float R = cert.lazy ? cell_radius(c, s.nb_v, lane) : cert.R;
+      uncert = !cert_holds(__ldg(cert.keys + p.k - 1), R, cert.margin);
+      n_uncert += uncert ? 1u : 0u;
+    }
 
     // ---- emit
     rpd_cell_header hd;
@@ -1202,7 +1216,7 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : kClipMaxThreads, MINB > 0 ? M
     hd.site_id = sid;
     hd.status = s.status;
     hd.nb_v = hd.nb_p = hd.nb_e = 0;
-    hd.flags = 0;
+    hd.flags = uncert ? RPD_CELL_UNCERTIFIED : 0;
     hd.offset = 0;
     hd.volume = 0.0;
     if (s.status == kSuccess) {
@@ -1249,6 +1263,7 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : kClipMaxThreads, MINB > 0 ? M
   if (lane == 0) {
     atomicAdd(p.counters + 0, (unsigned long long)pc.pred);
     atomicAdd(p.counters + 1, (unsigned long long)pc.esc);
+    if (n_uncert && p.uncertified) atomicAdd(p.uncertified, (unsigned long long)n_uncert);
   }
 }
 

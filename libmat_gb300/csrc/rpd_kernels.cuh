@@ -42,6 +42,7 @@ struct ClipParams {
   unsigned long long payload_cap;
   unsigned long long* work;      // work-queue counter, zeroed before launch
   unsigned long long* counters;  // [0] predicates, [1] escalated
+  unsigned long long* uncertified;  // cells flagged RPD_CELL_UNCERTIFIED, or null
   unsigned long long* exact_counters;  // [0] FP64 sign uncertain, [1] exact != FP64, or null
   int geometry;
   // distance-ordered lists with the security-radius certificate

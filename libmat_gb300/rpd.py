@@ -25,6 +25,7 @@ STATUS_NAMES = ["triangle_overflow", "vertex_overflow", "inconsistent_boundary",
                 "security_radius_not_reached", "success", "needs_exact_predicates",
                 "no_intersection", "edge_overflow", "needs_perturb", "other"]
 SUCCESS = 4
+CELL_UNCERTIFIED = 1  # rpd_cell_header.flags: RPD_CELL_UNCERTIFIED
 
 HEADER_DTYPE = np.dtype([
     ("tet_id", "<i4"), ("site_id", "<i4"), ("status", "<i4"),
@@ -118,7 +119,8 @@ class Stats(ctypes.Structure):
                 ("n_launches", ctypes.c_int32), ("search", ctypes.c_int64 * 6),
                 ("n_reclipped", ctypes.c_int64), ("ms_predict", ctypes.c_float),
                 ("learned", ctypes.c_int32), ("n_fp64_uncertain", ctypes.c_int64),
-                ("n_exact_flips", ctypes.c_int64), ("ms_epilogue", ctypes.c_float)]
+                ("n_exact_flips", ctypes.c_int64), ("ms_epilogue", ctypes.c_float),
+                ("n_uncertified", ctypes.c_int64)]
 
     def as_dict(self):
         d = {f: getattr(self, f) for f, _ in self._fields_ if f not in ("status_counts", "search")}
