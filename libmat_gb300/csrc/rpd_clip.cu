@@ -1203,12 +1203,11 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : kClipMaxThreads, MINB > 0 ? M
     // one test against that key still certifies it; otherwise sites beyond
     // the list may cut it and it is flagged (lists of all power neighbours,
     // as libmat's triangulation gives, leave no such cells)
-    bool uncert = false;
-    if (CERT && s.status == kSuccess && !cert.certified && klen == p.k && cert.consumed >= p.k) {
-      const float R = cert.lazy ? cell_radius(c, s.nb_v, lane) : cert.R;
-      uncert = !cert_holds(__ldg(cert.keys + p.k - 1), R, cert.margin);
-      n_uncert += uncert ? 1u : 0u;
-    }
+    // (lazy mode keeps no radius: its full-list cells are flagged untested)
+    const bool uncert = CERT && s.status == kSuccess && !cert.certified && klen == p.k &&
+                        cert.consumed >= p.k &&
+                        (cert.lazy || !cert_holds(__ldg(cert.keys + p.k - 1), cert.R, cert.margin));
+    n_uncert += uncert ? 1u : 0u;
 
     // ---- emit
     rpd_cell_header hd;
