@@ -64,3 +64,16 @@ def test_slice_plane(golden_cases):
         want = O.cell_polygons(cells[keep], c["ref_payload"])
         for k in want:
             assert np.array_equal(got[k], want[k]), (name, k)
+
+
+@pytest.mark.parametrize("mode", ["triangles", "boundary"])
+def test_writer_on_other_soups_matches_reference(tmp_path, golden_cases, mode):
+    c = golden_cases["random_full"]
+    h = ref_headers(c)
+    nb = int((c["f_adjs"] == 1).sum())
+    s = O.cell_polygons(h, c["ref_payload"], triangulate=mode == "triangles",
+                        boundary_only=mode == "boundary", max_sf_fid=nb - 1)
+    ref = B.ref_bgeo_bytes(s["points"], s["poly_offsets"], s["indices"], s["poly_site"], tmp_path)
+    if ref is None:
+        pytest.skip("reference sources not present")
+    assert B.bgeo_bytes(s["points"], s["poly_offsets"], s["indices"], s["poly_site"]) == ref
