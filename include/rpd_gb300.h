@@ -29,6 +29,12 @@ extern "C" {
 
 #define RPD_GB300_ABI_VERSION 1
 
+/* Opaque handles: a context (one device, one stream) and a batch of meshes.
+ * Declared here at file scope so that every prototype below names the same
+ * type in C. */
+struct rpd_ctx;
+struct rpd_batch;
+
 typedef enum rpd_status {
   RPD_OK = 0,
   RPD_ERR_INVALID_ARGUMENT = 1,

@@ -44,3 +44,39 @@ def test_invalid_mesh_rejected():
 
     with pytest.raises(rpd.RPDError):
         rpd.mesh_adjacency(3, np.array([[0, 1, 2, 5]], np.int32))
+
+
+def test_header_is_plain_c(tmp_path):
+    """include/rpd_gb300.h compiles as C99 (a cgo / FFI binding reads it as
+    C), and the structs the ctypes mirror reads have the same size and field
+    offsets in C."""
+    import ctypes
+    import os
+    import subprocess
+    fields = {"rpd_power_cells_view": (rpd.PowerCellsView, ["n_facets", "n_edges", "surface_pos",
+                                                            "se_covered", "se_line_end_pos",
+                                                            "cell_cc", "n_sfg", "sfg_record"]),
+              "rpd_stats": (rpd.Stats, ["n_predicates", "ms_total", "search", "ms_epilogue",
+                                        "n_uncertified"])}
+    lines = ['#include "rpd_gb300.h"', "#include <stddef.h>", "#include <stdio.h>",
+             "int main(void) {"]
+    for cname, (_, names) in fields.items():
+        lines.append('  printf("%%zu\\n", sizeof(%s));' % cname)
+        for f in names:
+            lines.append('  printf("%%zu\\n", offsetof(%s, %s));' % (cname, f))
+    lines += ['  printf("%u\\n", RPD_CELL_UNCERTIFIED);',
+              '  printf("%zu\\n", sizeof(rpd_feature_edge));', "  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I" + os.path.join(ROOT, "include"),
+                        str(src), "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True,
+                                          check=True).stdout.split()]
+    want = []
+    for _, (cls, names) in fields.items():
+        want.append(ctypes.sizeof(cls))
+        want += [getattr(cls, f).offset for f in names]
+    want += [rpd.CELL_UNCERTIFIED, 24]
+    assert out == want
