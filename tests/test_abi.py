@@ -53,11 +53,11 @@ def test_header_is_plain_c(tmp_path):
     import ctypes
     import os
     import subprocess
-    fields = {"rpd_power_cells_view": (rpd.PowerCellsView, ["n_facets", "n_edges", "surface_pos",
-                                                            "se_covered", "se_line_end_pos",
-                                                            "cell_cc", "n_sfg", "sfg_record"]),
-              "rpd_stats": (rpd.Stats, ["n_predicates", "ms_total", "search", "ms_epilogue",
-                                        "n_uncertified"])}
+    mirrors = {"rpd_config": rpd.Config, "rpd_mesh_info": rpd.MeshInfo,
+               "rpd_power_cells_view": rpd.PowerCellsView, "rpd_stats": rpd.Stats,
+               "rpd_tuning": rpd.Tuning, "rpd_mlp_report": rpd.MlpReport,
+               "rpd_cells_view": rpd.CellsView}
+    fields = {c: (cls, [f[0] for f in cls._fields_]) for c, cls in mirrors.items()}
     lines = ['#include "rpd_gb300.h"', "#include <stddef.h>", "#include <stdio.h>",
              "int main(void) {"]
     for cname, (_, names) in fields.items():
