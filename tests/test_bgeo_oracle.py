@@ -77,3 +77,19 @@ def test_writer_on_other_soups_matches_reference(tmp_path, golden_cases, mode):
     if ref is None:
         pytest.skip("reference sources not present")
     assert B.bgeo_bytes(s["points"], s["poly_offsets"], s["indices"], s["poly_site"]) == ref
+
+
+def test_no_points_is_refused(tmp_path):
+    """The reference writer throws on a geometry without points; the oracle
+    raises (and rpd_write_polygons_bgeo returns an error)."""
+    empty = (np.zeros((0, 3), np.float32), np.zeros(1, np.int64), np.zeros(0, np.uint32),
+             np.zeros(0, np.int32))
+    with pytest.raises(ValueError):
+        B.bgeo_bytes(*empty)
+    try:
+        ref = B.ref_bgeo_bytes(*empty, tmp_path)
+    except RuntimeError:
+        return  # the reference refused too
+    if ref is None:
+        pytest.skip("reference sources not present")
+    raise AssertionError("the reference wrote a file without points")

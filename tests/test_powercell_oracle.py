@@ -203,3 +203,21 @@ def test_surface_groups():
         g = pc["sfg_group"][a:b]
         assert np.all(np.diff(g) >= 0)  # grouped, faces ascending in a group
     assert split >= 1
+
+
+def test_power_cells_without_cells(golden_cases):
+    """No emitted cell (every status other than success): all record arrays
+    empty, every offset array zeros, with and without the optional maps."""
+    from tests.helpers import feature_edge_records
+    c = golden_cases["cube_k64"]
+    h = ref_headers(c).copy()
+    h["status"] = 6  # no_intersection
+    ns = c["sites"].shape[0]
+    adj = -np.ones((4, 3), np.int32)
+    pc = P.power_cells(h, c["ref_payload"], ns, 0, feature_edge_records(c["tets"].shape[0], 1),
+                       surface=(adj, np.zeros((0, 2), np.int32)))
+    for k, v in pc.items():
+        if k.endswith("_off"):
+            assert not np.any(v), k
+        else:
+            assert len(v) == 0, k
