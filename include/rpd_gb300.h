@@ -104,7 +104,17 @@ typedef struct rpd_config {
                             at most 12) */
   int topology_hash;     /* 1 (default): canonical topology hash of every
                             cell (rpd_copy_topology_hashes_to_host) */
-  int reserved[3];
+  int exact_lists;       /* 1 (default; RPD_NEIGH_KNN): a site whose cell
+                            its whole list leaves uncertified (sites beyond
+                            the list may cut it) gets a longer list -- every
+                            site whose key is below the cell's radius bound,
+                            at most 512, then 4096 entries -- and those
+                            cells are clipped again, for up to three rounds,
+                            inside the same rpd_compute.  Lists complete to
+                            the radius make every cell exact; cells still
+                            uncertified after the rounds keep the flag.
+                            0: one pass, cells flagged as they come */
+  int reserved[2];
 } rpd_config;
 
 /* One record per candidate (tet, site) pair; 32 bytes. */
@@ -166,6 +176,16 @@ typedef struct rpd_stats {
                                  FP64 sign (where the reference errs) */
   float ms_epilogue;          /* coordinates, volumes, hashes (in ms_clip) */
   int64_t n_uncertified;      /* emitted cells flagged RPD_CELL_UNCERTIFIED */
+  int64_t n_extended_sites;   /* exact_lists: sites given a longer list
+                                 (summed over the rounds) */
+  int64_t n_cert_reclipped;   /* exact_lists: cells clipped again with a
+                                 longer list (summed over the rounds) */
+  float ms_extend;            /* exact_lists: device time of the rounds (in
+                                 ms_clip) */
+  int32_t n_extend_rounds;    /* rounds that found uncertified cells */
+  int32_t ext_longest;        /* longest extended list clipped */
+  float ms_extend_lists;      /* exact_lists: of ms_extend, building the
+                                 longer lists */
 } rpd_stats;
 
 typedef struct rpd_cells_view {

@@ -175,6 +175,7 @@ void rpd_config_default(rpd_config* cfg) {
   cfg->warps_per_block = 0;
   cfg->blocks_per_sm = 0;
   cfg->topology_hash = 1;
+  cfg->exact_lists = 1;
 }
 
 static bool config_valid(const rpd_config& c0) {
@@ -190,6 +191,7 @@ static bool config_valid(const rpd_config& c0) {
   if (c0.box_planes < 0 || c0.box_planes > 128) return false;
   if (c0.learned_k < 0 || c0.learned_k > 1 || (c0.learned_k && !c0.certify)) return false;
   if (c0.topology_hash < 0 || c0.topology_hash > 1) return false;
+  if (c0.exact_lists < 0 || c0.exact_lists > 1) return false;
   return true;
 }
 
@@ -230,6 +232,10 @@ void rpd_destroy(rpd_ctx* c) {
   c->site4f.release(); c->site4d.release(); c->flags.release();
   c->nbr.release(); c->nbr_dist.release(); c->site_klen.release(); c->reclip_idx.release();
   c->topo_hash.release(); c->nbr_ref_tmp.release(); c->knn_status.release(); c->nbr_keys.release();
+  c->nbr_bound.release(); c->site_need.release(); c->site_row.release(); c->ext_sites.release();
+  c->site_flag.release(); c->site_pos.release(); c->ext_idx.release(); c->ext_nbr.release();
+  c->ext_len.release();
+  c->ext_keys.release(); c->ext_bound.release(); c->ext_off.release();
   c->s_cell_of.release(); c->s_cell_count.release(); c->s_cell_start.release();
   c->s_cell_fill.release(); c->s_cell_items.release();
   c->t_cell_of.release(); c->t_cell_count.release(); c->t_cell_start.release();
@@ -449,9 +455,21 @@ rpd_status rpd_set_neighbors(rpd_ctx* c, const int32_t* nbr, int k, int layout) 
 // CSR of the pairs, clipping (+ re-clip), epilogue, compaction and the
 // statistics: the part of a compute after the candidate pairs are in
 // pair_buf / tet_count (n_pairs of them)
-static rpd_status finish_compute(rpd_ctx* c, bool knn, bool learned, rpd_stats* stats) {
+// exact lists: rounds of longer lists for the sites whose cells the pass
+// before left uncertified (list lengths of the rounds; the last round gives
+// every site, which certifies any cell)
+constexpr int kExtRounds = 3;
+constexpr int kExtK[kExtRounds - 1] = {512, 4096};
+
+static rpd_status finish_compute(rpd_ctx* c, bool knn, bool learned, rpd_stats* stats,
+                                 bool extend_ok) {
   cudaStream_t st = c->stream;
   const int n_tet = c->n_tet;
+  const int n_site = c->n_site;
+  // lists the GPU built: bounds are known, and uncertified cells can be
+  // given longer lists
+  const bool extend = extend_ok && knn && c->cfg.exact_lists != 0;
+  c->ext_valid = false;
   CK(c->tet_offsets.ensure((size_t)n_tet + 1), "alloc");
   CK(c->tet_fill.ensure(n_tet), "alloc");
   CK(c->scan_tmp.ensure(scan_temp_ints(std::max<long long>(c->n_pairs, n_tet)) + 16), "alloc");
@@ -501,8 +519,29 @@ static rpd_status finish_compute(rpd_ctx* c, bool knn, bool learned, rpd_stats* 
   }
   const float cert_margin = (float)(16.0 * std::ldexp(1.0, -24) * (L + std::sqrt(D2)) + 1e-30);
   c->n_reclipped = 0;
+  long long n_ext_sites = 0, n_cert_reclipped = 0;
+  int n_ext_rounds = 0, ext_longest = 0;
+  float ms_ext_lists = 0.f;
+  if (extend) {
+    CK(c->site_need.ensure((size_t)n_site), "alloc");
+    CK(c->site_row.ensure((size_t)n_site), "alloc");
+    CK(c->ext_sites.ensure((size_t)n_site), "alloc");
+    CK(c->site_flag.ensure((size_t)n_site), "alloc");
+    CK(c->site_pos.ensure((size_t)n_site + 1), "alloc");
+    CK(c->scan_tmp.ensure(scan_temp_ints(std::max<long long>(std::max<long long>(n_pairs, n_tet),
+                                                             n_site)) + 16), "alloc");
+  }
   for (int attempt = 0; attempt < 3; ++attempt) {
     CK(cudaMemsetAsync(c->scratch.ptr + 28, 0, 4 * sizeof(unsigned long long), st), "memset");
+    if (extend) {
+      CK(cudaMemsetAsync(c->site_need.ptr, 0, sizeof(unsigned int) * (size_t)n_site, st), "memset");
+      CK(cudaMemsetAsync(c->site_row.ptr, 0xff, sizeof(int32_t) * (size_t)n_site, st), "memset");
+      c->ext_used = 0;
+      c->ext_rows = 0;
+      n_ext_sites = n_cert_reclipped = 0;
+      n_ext_rounds = ext_longest = 0;
+      ms_ext_lists = 0.f;
+    }
     CK(c->payload.ensure((size_t)pcap), "alloc payload");
     CK(cudaMemsetAsync(c->scratch.ptr, 0, 4 * sizeof(unsigned long long), st), "memset");
     ClipParams p;
@@ -543,6 +582,14 @@ static rpd_status finish_compute(rpd_ctx* c, bool knn, bool learned, rpd_stats* 
     p.pair_index = nullptr;
     p.n_work = n_pairs;
     p.topo_hash = c->cfg.topology_hash ? c->topo_hash.ptr : nullptr;
+    p.uncertified = nullptr;  // counted at the compaction, after every round
+    p.nbr_bound = knn ? c->nbr_bound.ptr : nullptr;
+    p.site_row = nullptr;  // base lists only in the first pass
+    p.ext_nbr = nullptr;
+    p.ext_keys = nullptr;
+    p.ext_off = nullptr;
+    p.ext_len = nullptr;
+    p.ext_bound = nullptr;
     CK(cudaEventRecord(c->ev[kEvClipK0], st), "event");
     if (n_pairs > 0) CK(launch_clip_cells(p, c->cfg.predicate_mode, certify, variant, blocks, warps, st), "clip");
     CK(cudaEventRecord(c->ev[kEvClipK1], st), "event");
@@ -568,6 +615,140 @@ static rpd_status finish_compute(rpd_ctx* c, bool knn, bool learned, rpd_stats* 
         CK(launch_clip_cells(p, c->cfg.predicate_mode, certify, variant, blocks, warps, st), "reclip");
       }
     }
+    // ---- the cells the clip kernel flagged uncertified, bounded again from
+    // their records (FP64 where the FP32 bound is loose): the flag stays
+    // where the certificate still fails, and with exact lists the cell's
+    // radius goes into its site's site_need
+    CK(cudaEventRecord(c->ev[kEvExt0], st), "event");
+    // (scratch[32]: cells still flagged after a recheck, compacted into
+    // ext_idx; the selection's count is read on the device)
+    CK(c->flag_tmp.ensure((size_t)n_pairs + 1), "alloc");
+    CK(c->pos_tmp.ensure((size_t)n_pairs + 1), "alloc");
+    CK(c->reclip_idx.ensure((size_t)std::max<long long>(n_pairs, 1)), "alloc");
+    CK(c->ext_idx.ensure((size_t)std::max<long long>(n_pairs, 1)), "alloc");
+    auto recheck = [&](bool rows) -> rpd_status {
+      CK(select_uncertified(c->pair_headers.ptr, n_pairs, c->flag_tmp.ptr, c->pos_tmp.ptr,
+                            c->scan_tmp.ptr, c->reclip_idx.ptr, st), "select cells");
+      CK(cudaMemsetAsync(c->scratch.ptr + 32, 0, sizeof(unsigned long long), st), "memset");
+      RecheckParams rp;
+      rp.headers = c->pair_headers.ptr;
+      rp.idx = c->reclip_idx.ptr;
+      rp.n_dev = c->pos_tmp.ptr + n_pairs;
+      rp.payload = c->payload.ptr;
+      rp.site4f = c->site4f.ptr;
+      rp.site_row = rows ? c->site_row.ptr : nullptr;
+      rp.ext_bound = c->ext_bound.ptr;
+      rp.nbr_bound = c->nbr_bound.ptr;
+      rp.margin = cert_margin;
+      rp.site_need = extend ? c->site_need.ptr : nullptr;
+      rp.kept_idx = c->ext_idx.ptr;
+      rp.kept_count = c->scratch.ptr + 32;
+      CK(launch_recheck_cells(rp, c->num_sms, st), "recheck");
+      return RPD_OK;
+    };
+    if (knn && n_pairs > 0) {
+      rpd_status rs = recheck(false);
+      if (rs != RPD_OK) return rs;
+    }
+    // ---- exact lists: the sites of uncertified cells get every site whose
+    // key lies below the cells' radius bound (at most kExtK entries), and
+    // those cells are clipped again; a round's re-clip can leave a cell
+    // uncertified (its list was cut at kExtK), which the next round takes up
+    for (int round = 0; extend && n_pairs > 0 && round < kExtRounds; ++round) {
+      CK(select_sites(c->site_need.ptr, n_site, c->site_flag.ptr, c->site_pos.ptr, c->scan_tmp.ptr,
+                      c->ext_sites.ptr, st), "select sites");
+      int32_t n_f = 0;
+      unsigned long long n_flag = 0;
+      CK(cudaMemcpyAsync(&n_f, c->site_pos.ptr + n_site, sizeof(n_f), cudaMemcpyDeviceToHost, st), "D2H");
+      CK(cudaMemcpyAsync(&n_flag, c->scratch.ptr + 32, sizeof(n_flag), cudaMemcpyDeviceToHost, st),
+         "D2H");
+      CK(cudaStreamSynchronize(st), "extend sync");
+      if (round > 0) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c->ev[kEvExtR0], c->ev[kEvExtK]);
+        ms_ext_lists += ms;
+      }
+      if (n_f == 0 || n_flag == 0) break;
+      const bool last = round == kExtRounds - 1;
+      const int KL = last ? n_site
+                          : std::min(kExtK[round], std::min(knn_max_k(), std::max(n_site - 1, 1)));
+      const long long need = c->ext_used + (last ? (long long)n_site : (long long)n_f * KL);
+      CK(c->ext_nbr.grow_keep((size_t)need, (size_t)c->ext_used, st), "alloc ext");
+      CK(c->ext_keys.grow_keep((size_t)need, (size_t)c->ext_used, st), "alloc ext");
+      CK(c->ext_len.grow_keep((size_t)c->ext_rows + n_f, (size_t)c->ext_rows, st), "alloc ext");
+      CK(c->ext_bound.grow_keep((size_t)c->ext_rows + n_f, (size_t)c->ext_rows, st), "alloc ext");
+      CK(c->ext_off.grow_keep((size_t)c->ext_rows + n_f, (size_t)c->ext_rows, st), "alloc ext");
+      CK(cudaEventRecord(c->ev[kEvExtR0], st), "event");
+      if (last) {
+        CK(complete_rows(c->ext_sites.ptr, n_f, c->ext_rows, c->ext_used, n_site, c->site_row.ptr,
+                         c->ext_off.ptr, c->ext_len.ptr, c->ext_bound.ptr, c->ext_nbr.ptr, st),
+           "complete rows");
+      } else {
+        Grid g = make_grid(c->site_lo, c->site_hi, n_site, 2.0);
+        KnnArgs ka = {};
+        ka.site4f = c->site4f.ptr;
+        ka.n_rows = n_f;
+        ka.g = g;
+        ka.cell_start = c->s_cell_start.ptr;
+        ka.cell_items = c->s_cell_items.ptr;
+        ka.k = KL;
+        ka.w_max = c->w_max;
+        // ascending key in every mode: in site-id order the hundreds of
+        // entries would clip the cell with many sites that are not its
+        // neighbours before those that are, past the 64-plane capacity
+        ka.order_by_id = 0;
+        ka.nbr = c->ext_nbr.ptr + c->ext_used;
+        ka.keys = c->ext_keys.ptr + c->ext_used;
+        ka.subset = c->ext_sites.ptr;
+        // every key up to the radius bound of the site's uncertified cells:
+        // the certificate then holds at the end of the list, since clipping
+        // with more planes only shrinks the cells (the slack covers the
+        // rounding of the radius bounds and of the certificate's test)
+        ka.radius = c->site_need.ptr;
+        ka.bound_scale = 1.0f + 1.0f / 512.0f;
+        ka.bound_abs = 2.0f * cert_margin;
+        ka.len_out = c->ext_len.ptr + c->ext_rows;
+        ka.bound_out = c->ext_bound.ptr + c->ext_rows;
+        CK(launch_knn(ka, st), "extended lists");
+        CK(assign_rows(c->ext_sites.ptr, n_f, c->ext_rows, c->ext_used, KL, c->site_row.ptr,
+                       c->ext_off.ptr, st), "rows");
+      }
+      CK(cudaEventRecord(c->ev[kEvExtK], st), "event");
+      c->ext_used = need;
+      c->ext_rows += n_f;
+      // the still uncertified cells, clipped again with the new rows
+      CK(cudaMemsetAsync(c->site_need.ptr, 0, sizeof(unsigned int) * (size_t)n_site, st), "memset");
+      CK(cudaMemsetAsync(c->scratch.ptr + 1, 0, sizeof(unsigned long long), st), "memset");
+      ClipParams pe = p;
+      pe.site_klen = nullptr;
+      pe.pair_klen = nullptr;
+      pe.lazy_cert = 0;
+      pe.consumed = nullptr;
+      pe.pair_index = c->ext_idx.ptr;
+      pe.n_work = (long long)n_flag;
+      pe.site_row = c->site_row.ptr;
+      pe.ext_nbr = c->ext_nbr.ptr;
+      pe.ext_keys = c->ext_keys.ptr;
+      pe.ext_off = c->ext_off.ptr;
+      pe.ext_len = c->ext_len.ptr;
+      pe.ext_bound = c->ext_bound.ptr;
+      CK(launch_clip_cells(pe, c->cfg.predicate_mode, certify, variant, blocks, warps, st),
+         "reclip extended");
+      ++n_ext_rounds;
+      n_ext_sites += n_f;
+      n_cert_reclipped += (long long)n_flag;
+      ext_longest = std::max(ext_longest, KL);
+      rpd_status rs = recheck(true);
+      if (rs != RPD_OK) return rs;
+      if (round == kExtRounds - 1) {
+        CK(cudaStreamSynchronize(st), "extend sync");
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c->ev[kEvExtR0], c->ev[kEvExtK]);
+        ms_ext_lists += ms;
+      }
+    }
+    CK(cudaEventRecord(c->ev[kEvExt1], st), "event");
+    c->ext_valid = extend;
     unsigned long long cur = 0;
     CK(cudaMemcpyAsync(&cur, c->scratch.ptr, sizeof(cur), cudaMemcpyDeviceToHost, st), "D2H");
     CK(cudaStreamSynchronize(st), "clip sync");
@@ -598,8 +779,10 @@ static rpd_status finish_compute(rpd_ctx* c, bool knn, bool learned, rpd_stats* 
   CK(c->pos_tmp.ensure((size_t)n_pairs + 1), "alloc");
   CK(c->scan_tmp.ensure(scan_temp_ints(std::max<long long>(n_pairs, n_tet)) + 16), "alloc");
   CK(c->n_out.ensure(1), "alloc");
+  CK(cudaMemsetAsync(c->scratch.ptr + 31, 0, sizeof(unsigned long long), st), "memset");
   CK(compact_cells(c->pair_headers.ptr, n_pairs, c->flag_tmp.ptr, c->pos_tmp.ptr, c->scan_tmp.ptr,
-                   c->cells.ptr, c->n_out.ptr, c->scratch.ptr + 8, st), "compact");
+                   c->cells.ptr, c->n_out.ptr, c->scratch.ptr + 8, st, c->scratch.ptr + 31),
+     "compact");
   CK(cudaEventRecord(c->ev[kEvEnd], st), "event");
   unsigned long long host_scratch[32];
   long long n_cells = 0;
@@ -642,6 +825,12 @@ static rpd_status finish_compute(rpd_ctx* c, bool knn, bool learned, rpd_stats* 
     stats->n_exact_flips = (int64_t)host_scratch[30];
     stats->n_uncertified = (int64_t)host_scratch[31];
     cudaEventElapsedTime(&stats->ms_epilogue, c->ev[kEvEpi0], c->ev[kEvClip]);
+    stats->n_extended_sites = n_ext_sites;
+    stats->n_cert_reclipped = n_cert_reclipped;
+    stats->n_extend_rounds = n_ext_rounds;
+    stats->ext_longest = ext_longest;
+    stats->ms_extend_lists = ms_ext_lists;
+    cudaEventElapsedTime(&stats->ms_extend, c->ev[kEvExt0], c->ev[kEvExt1]);
   }
   return RPD_OK;
 }
@@ -661,7 +850,7 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
   CK(cudaSetDevice(c->device), "cudaSetDevice");
   cudaStream_t st = c->stream;
   const int n_site = c->n_site, n_tet = c->n_tet;
-  CK(c->scratch.ensure(32), "alloc scratch");
+  CK(c->scratch.ensure(40), "alloc scratch");
   CK(cudaMemsetAsync(c->scratch.ptr, 0, 32 * sizeof(unsigned long long), st), "memset");
   take_launches();
   CK(cudaEventRecord(c->ev[kEvStart], st), "event");
@@ -684,9 +873,11 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
     CK(grid_build_sites(c->site4f.ptr, n_site, g, c->s_cell_of.ptr, c->s_cell_count.ptr,
                         c->s_cell_start.ptr, c->s_cell_fill.ptr, c->s_cell_items.ptr,
                         c->scan_tmp.ptr, st), "site grid");
+    CK(c->nbr_bound.ensure((size_t)n_site), "alloc nbr");
     CK(launch_knn(c->site4f.ptr, n_site, g, c->s_cell_start.ptr, c->s_cell_items.ptr, c->k,
                   c->w_max, c->cfg.clip_order == RPD_ORDER_SITE_ID ? 1 : 0, c->nbr.ptr,
-                  c->nbr_keys.ptr, c->nbr_dist.ptr, c->knn_status.ptr, st), "knn");
+                  c->nbr_keys.ptr, c->nbr_dist.ptr, c->knn_status.ptr, st, 0,
+                  c->nbr_bound.ptr), "knn");
   }
   CK(cudaEventRecord(c->ev[kEvKnn], st), "event");
 
@@ -808,7 +999,7 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
     if (c->n_pairs > INT32_MAX) return fail(c, RPD_ERR_CAPACITY, "rpd_compute: more than 2^31 pairs");
     c->pair_cap_hint = std::max<long long>(c->pair_cap_hint, c->n_pairs + c->n_pairs / 8 + 1024);
   }
-  return finish_compute(c, knn, learned, stats);
+  return finish_compute(c, knn, learned, stats, true);
 }
 
 rpd_status rpd_autotune(rpd_ctx* c, int repeats, rpd_tuning* result) {
@@ -2151,6 +2342,6 @@ rpd_status rpd_cuda_fail(rpd_ctx* c, cudaError_t e, const char* where) { return 
 Grid rpd_make_grid(const double* lo, const double* hi, long long n_items, double per_cell) {
   return make_grid(lo, hi, n_items, per_cell);
 }
-rpd_status rpd_finish_compute(rpd_ctx* c, bool knn, bool learned, rpd_stats* stats) {
-  return finish_compute(c, knn, learned, stats);
+rpd_status rpd_finish_compute(rpd_ctx* c, bool knn, bool learned, rpd_stats* stats, bool extend) {
+  return finish_compute(c, knn, learned, stats, extend);
 }

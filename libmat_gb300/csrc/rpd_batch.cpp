@@ -120,13 +120,14 @@ rpd_status upload(rpd_batch* b) {
   BCK(c->nbr_keys.ensure((size_t)n_site * k), "alloc");
   BCK(c->nbr_dist.ensure((size_t)n_site * k), "alloc");
   BCK(c->knn_status.ensure((size_t)n_site), "alloc");
+  BCK(c->nbr_bound.ensure((size_t)n_site), "alloc");
   BCK(c->s_cell_of.ensure((size_t)n_site), "alloc");
   BCK(c->site_box.ensure((size_t)n_site * 2), "alloc");
   BCK(c->site_planes.ensure((size_t)n_site * kBoxPlanes), "alloc");
   BCK(c->site_nplanes.ensure((size_t)n_site), "alloc");
   BCK(c->centroid.ensure((size_t)n_tet), "alloc");
   BCK(c->tet_count.ensure((size_t)n_tet), "alloc");
-  BCK(c->scratch.ensure(32), "alloc");
+  BCK(c->scratch.ensure(40), "alloc");
   // meshes to lanes, largest first onto the least loaded lane
   std::vector<int> order(b->meshes.size());
   for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
@@ -217,7 +218,8 @@ rpd_status front_end(rpd_batch* b) {
     BCK(launch_knn(c->site4f.ptr + sb, m.n_site, m.site_grid, L.s_cell_start.ptr,
                    L.s_cell_items.ptr, k, m.w_max, c->cfg.clip_order == RPD_ORDER_SITE_ID ? 1 : 0,
                    c->nbr.ptr + (long long)sb * k, c->nbr_keys.ptr + (long long)sb * k,
-                   c->nbr_dist.ptr + (long long)sb * k, c->knn_status.ptr + sb, ls, sb),
+                   c->nbr_dist.ptr + (long long)sb * k, c->knn_status.ptr + sb, ls, sb,
+                   c->nbr_bound.ptr + sb),
         "knn");
     // candidate pairs per radius class (as rpd_compute, with this mesh's bounds)
     double diag2 = 0.0, cs = 0.0, ext = 0.0;

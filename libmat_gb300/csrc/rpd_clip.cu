@@ -661,10 +661,79 @@ __device__ __forceinline__ float vertex_radius(float4 K, float4 M, float3 S) {
   return num / (aw - ew) * (1.0f + 1e-6f);
 }
 
+// The same bound in FP64, for a vertex whose FP32 bound is loose or void
+// (|K_w| close to its error: nearly parallel planes, as at the faces of
+// sliver tets).  Products of two floats are exact in double and every 3x3
+// minor rounds at most 3 times, so each cofactor is within 4 eps of its
+// permanent (eps = 2^-53); the translation by S and the norm add a few eps.
+__device__ __noinline__ float vertex_radius_d(float4 p1, float4 p2, float4 p3, float3 S) {
+  const double x1 = p1.x, y1 = p1.y, z1 = p1.z, w1 = p1.w;
+  const double x2 = p2.x, y2 = p2.y, z2 = p2.z, w2 = p2.w;
+  const double x3 = p3.x, y3 = p3.y, z3 = p3.z, w3 = p3.w;
+  // det3 of rows (a_i, b_i, c_i) and its permanent
+  auto d3 = [](double a1, double b1, double c1, double a2, double b2, double c2, double a3,
+               double b3, double c3, double& perm) {
+    perm = fabs(a1) * (fabs(b2 * c3) + fabs(b3 * c2)) + fabs(b1) * (fabs(a2 * c3) + fabs(a3 * c2)) +
+           fabs(c1) * (fabs(a2 * b3) + fabs(a3 * b2));
+    return a1 * (b2 * c3 - b3 * c2) - b1 * (a2 * c3 - a3 * c2) + c1 * (a2 * b3 - a3 * b2);
+  };
+  double Mx, My, Mz, Mw;
+  const double Kx = -d3(y1, z1, w1, y2, z2, w2, y3, z3, w3, Mx);
+  const double Ky = d3(x1, z1, w1, x2, z2, w2, x3, z3, w3, My);
+  const double Kz = -d3(x1, y1, w1, x2, y2, w2, x3, y3, w3, Mz);
+  const double Kw = d3(x1, y1, z1, x2, y2, z2, x3, y3, z3, Mw);
+  const double eps = 1.1102230246251565e-16;
+  const double ew = 4.0 * eps * Mw;
+  const double aw = fabs(Kw);
+  if (!(aw > 2.0 * ew)) return INFINITY;
+  const double sx = S.x, sy = S.y, sz = S.z;
+  const double nx = Kx - Kw * sx, ny = Ky - Kw * sy, nz = Kz - Kw * sz;
+  const double ex = 4.0 * eps * (Mx + fabs(sx) * Mw) + 2.0 * eps * fabs(nx);
+  const double ey = 4.0 * eps * (My + fabs(sy) * Mw) + 2.0 * eps * fabs(ny);
+  const double ez = 4.0 * eps * (Mz + fabs(sz) * Mw) + 2.0 * eps * fabs(nz);
+  const double ax = fabs(nx) + ex, ay = fabs(ny) + ey, az = fabs(nz) + ez;
+  const double r = sqrt(ax * ax + ay * ay + az * az) * (1.0 + 8.0 * eps) / (aw - ew);
+  return __double2float_ru(r * (1.0 + 8.0 * eps));
+}
+
+// the radius bound of a vertex: FP32 where it is tight (its upper and lower
+// bounds within 2^-10 of each other), else FP64 -- the FP32 cofactors of
+// nearly parallel planes (the faces of sliver tets) cancel, and their error
+// terms can exceed the distance itself
+__device__ __forceinline__ float vertex_radius_p(float4 K, float4 M, float3 S, float4 p1,
+                                                 float4 p2, float4 p3) {
+  const float g = 6.0f * 5.9604645e-08f;
+  const float ew = g * M.w, aw = fabsf(K.w);
+  if (aw > 64.0f * ew) {
+    const float nx = __fmaf_rn(-K.w, S.x, K.x), ny = __fmaf_rn(-K.w, S.y, K.y),
+                nz = __fmaf_rn(-K.w, S.z, K.z);
+    const float e = g * (M.x + M.y + M.z + (fabsf(S.x) + fabsf(S.y) + fabsf(S.z)) * M.w) +
+                    2.4e-7f * (fabsf(nx) + fabsf(ny) + fabsf(nz));
+    const float n = sqrtf(nx * nx + ny * ny + nz * nz);
+    if (e < n * (1.0f / 2048.0f)) return vertex_radius(K, M, S);
+  }
+  return vertex_radius_d(p1, p2, p3, S);
+}
+
 // the cell radius: the largest of the vertices' cached bounds
 __device__ __forceinline__ float cell_radius(const WarpCell& c, int nb_v, int lane) {
   float r = 0.f;
   for (int v = lane; v < nb_v; v += 32) r = fmaxf(r, c.u.f.rad[v]);
+  for (int o = 16; o > 0; o >>= 1) r = fmaxf(r, __shfl_xor_sync(0xffffffffu, r, o));
+  return r;
+}
+
+// the same bound from the planes alone (no cached cofactors: plain FP64
+// clipping, which keeps none)
+__device__ __forceinline__ float cell_radius_fresh(const WarpCell& c, int nb_v, int lane,
+                                                   float3 S) {
+  float r = 0.f;
+  for (int v = lane; v < nb_v; v += 32) {
+    const uchar4 t = c.ver[v];
+    float4 K, M;
+    vertex_cofactors(c.pl[t.x], c.pl[t.y], c.pl[t.z], K, M);
+    r = fmaxf(r, vertex_radius(K, M, S));
+  }
   for (int o = 16; o > 0; o >>= 1) r = fmaxf(r, __shfl_xor_sync(0xffffffffu, r, o));
   return r;
 }
@@ -718,7 +787,7 @@ __device__ void clip_list(WarpCell& c, CellState& s, const int32_t* list, int k,
     uint32_t valid = __ballot_sync(0xffffffffu, j != -1);
     int count = (~valid == 0u) ? 32 : (__ffs(~valid) - 1);  // up to first -1
     float key_mine = 0.f;
-    if (CERT && lane < count) key_mine = __ldg(cert.keys + base + lane);
+    if (eager && lane < count) key_mine = __ldg(cert.keys + base + lane);
     float4 e_mine = make_float4(0.f, 0.f, 0.f, 0.f);
     if (lane < count) e_mine = make_plane(j);
     // planes already in the cell that equal this lane's plane
@@ -836,6 +905,67 @@ __device__ void clip_list(WarpCell& c, CellState& s, const int32_t* list, int k,
     }
   }
   cert.R = R;
+}
+
+// End of a cell's list without the certificate holding on the way (status
+// success).  A shortened list (learned or per-site lengths) that ran out
+// first: the cell is clipped again with its whole list
+// (kSecurityRadiusNotReached marks it).  A whole list: the sites missing from
+// it have keys >= its completeness bound, so one test against the bound can
+// still certify the cell; otherwise such a site may cut it, and the cell is
+// flagged, its radius recorded for a longer list.  Lists of all power
+// neighbours, as libmat's triangulation gives, leave no such cells.  Out of
+// line: it runs for a few cells, and keeps the hot loop's code small.
+// pointers of the list metadata finish_list reads (by value: a noinline
+// call must not take the address of the kernel's parameters or state)
+struct ListMeta {
+  const int32_t* nbr;
+  const float* keys;
+  const int32_t* site_row;
+  const int32_t* ext_len;
+  const float* ext_bound;
+  const float* nbr_bound;
+  unsigned long long* misses;
+  int k;
+};
+
+// returns 1: flagged uncertified (recheck_cells_kernel takes it up), 2: a
+// short list missed (re-clip whole), 0
+template <bool CERT, bool EXT>
+__device__ __forceinline__ int finish_list(const WarpCell& c, int nb_v, ListMeta m, int sid,
+                                          int klen, bool lazy, float R_eager, float margin,
+                                          int lane, float3 S) {
+  int full;
+  float bound;
+  const int row = EXT ? __ldg(m.site_row + sid) : -1;
+  if (row >= 0) {
+    full = __ldg(m.ext_len + row);
+    bound = __ldg(m.ext_bound + row);
+  } else {
+    full = m.k;
+    bound = m.nbr_bound ? __ldg(m.nbr_bound + sid) : INFINITY;
+  }
+  // (only base lists are shortened)
+  if (CERT && klen < full && __ldg(m.nbr + (long long)sid * m.k + klen) != -1) {
+    bool ok = false;
+    if (lazy) {
+      // one certificate test after the whole short list
+      float R = cell_radius(c, nb_v, lane);
+      ok = cert_holds(__ldg(m.keys + (long long)sid * m.k + klen), R, margin);
+    }
+    if (ok) return 0;
+    if (m.misses && lane == 0) atomicAdd(m.misses, 1ull);
+    return 2;
+  }
+  if (klen != full || !(bound < INFINITY) || (!CERT && !m.nbr_bound)) return 0;
+  // the FP32 radius bounds (cached, or from the planes): a cell they do not
+  // certify is flagged, and recheck_cells_kernel bounds it again with FP64
+  // where they are loose
+  float R;
+  if (CERT && !lazy) R = R_eager;
+  else if (CERT) R = cell_radius(c, nb_v, lane);
+  else R = cell_radius_fresh(c, nb_v, lane, S);
+  return cert_holds(bound, R, margin) ? 0 : 1;
 }
 
 // ------------------------------------------------------------------------
@@ -1111,7 +1241,9 @@ __device__ uint64_t cell_topology_hash(const Cell& c, int nb_v, int lane) {
 
 // MINB > 0 caps registers so that MINB blocks of 128 threads fit on an SM
 // (occupancy variants chosen by the autotuner)
-template <int PRED, bool CERT, int MINB>
+// EXT: sites may have extended rows (the exact-lists rounds); the first
+// pass, on base lists only, runs without that code
+template <int PRED, bool CERT, int MINB, bool EXT>
 __global__ void __launch_bounds__(MINB > 0 ? 128 : kClipMaxThreads, MINB > 0 ? MINB : 1)
     clip_cells_kernel(ClipParams p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1168,45 +1300,55 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : kClipMaxThreads, MINB > 0 ? M
       __syncwarp();
     }
 
-    // ---- clip by the site's neighbour list
+    // ---- clip by the site's neighbour list: its base row, or the extended
+    // row it was given after an earlier pass left one of its cells
+    // uncertified
     const float4* site4f = p.site4f;
     auto make_plane = [&](int j) { return bisector_f(seed, __ldg(site4f + j)); };
-    const int32_t* list = p.nbr + (long long)sid * p.k;
-    int klen = p.k;
-    if (p.site_klen) klen = min(klen, __ldg(p.site_klen + sid));
-    if (p.pair_klen) klen = min(klen, __ldg(p.pair_klen + q));
-    Cert cert;
-    cert.keys = CERT ? p.keys + (long long)sid * p.k : nullptr;
-    cert.S = make_float3(seed.x, seed.y, seed.z);
-    cert.margin = p.cert_margin;
-    cert.lazy = p.lazy_cert != 0;
-    cert.certified = false;
-    clip_list<PRED, true, CERT>(c, s, list, klen, sid, make_plane, lane, pc, cert);
-    // a shortened list that ran out before the certificate held: the cell
-    // is clipped again with the whole list (status kSecurityRadiusNotReached
-    // marks it)
-    if (CERT && s.status == kSuccess && !cert.certified && klen < p.k && __ldg(list + klen) != -1) {
-      bool ok = false;
-      if (cert.lazy) {
-        // one certificate test after the whole short list
-        float R = cell_radius(c, s.nb_v, lane);
-        ok = cert_holds(__ldg(cert.keys + klen), R, cert.margin);
-      }
-      if (!ok) {
-        if (p.misses && lane == 0) atomicAdd(p.misses, 1ull);
-        s.status = kSecurityRadiusNotReached;
+    const int32_t* list;
+    const float* keys;
+    int klen;
+    bool complete = false;  // a row of every site (id order, no keys)
+    {
+      const int row = EXT ? __ldg(p.site_row + sid) : -1;
+      if (row >= 0) {
+        const long long off = __ldg(p.ext_off + row);
+        list = p.ext_nbr + off;
+        klen = __ldg(p.ext_len + row);
+        complete = !(__ldg(p.ext_bound + row) < INFINITY);
+        keys = (p.ext_keys && !complete) ? p.ext_keys + off : nullptr;
+      } else {
+        list = p.nbr + (long long)sid * p.k;
+        keys = p.keys ? p.keys + (long long)sid * p.k : nullptr;
+        klen = p.k;
+        if (p.site_klen) klen = min(klen, __ldg(p.site_klen + sid));
+        if (p.pair_klen) klen = min(klen, __ldg(p.pair_klen + q));
       }
     }
+    Cert cert;
+    cert.keys = CERT ? keys : nullptr;
+    cert.S = make_float3(seed.x, seed.y, seed.z);
+    cert.margin = p.cert_margin;
+    cert.lazy = p.lazy_cert != 0 || complete;
+    cert.certified = false;
+    clip_list<PRED, true, CERT>(c, s, list, klen, sid, make_plane, lane, pc, cert);
+    bool uncert = false;
+    if (s.status == kSuccess && !cert.certified) {
+      ListMeta m;
+      m.nbr = p.nbr;
+      m.keys = p.keys;
+      m.site_row = p.site_row;
+      m.ext_len = p.ext_len;
+      m.ext_bound = p.ext_bound;
+      m.nbr_bound = p.nbr_bound;
+      m.misses = p.misses;
+      m.k = p.k;
+      const int r = finish_list<CERT, EXT>(c, s.nb_v, m, sid, klen, cert.lazy, cert.R, cert.margin,
+                                      lane, make_float3(seed.x, seed.y, seed.z));
+      uncert = r == 1;
+      if (r == 2) s.status = kSecurityRadiusNotReached;
+    }
     if (p.consumed && lane == 0) p.consumed[q] = cert.consumed;
-    // a cell clipped by its whole, full list (no -1 before the end) without
-    // the certificate holding: unseen sites have keys >= the list's last, so
-    // one test against that key still certifies it; otherwise sites beyond
-    // the list may cut it and it is flagged (lists of all power neighbours,
-    // as libmat's triangulation gives, leave no such cells)
-    // (lazy mode keeps no radius: its full-list cells are flagged untested)
-    const bool uncert = CERT && s.status == kSuccess && !cert.certified && klen == p.k &&
-                        cert.consumed >= p.k &&
-                        (cert.lazy || !cert_holds(__ldg(cert.keys + p.k - 1), cert.R, cert.margin));
     n_uncert += uncert ? 1u : 0u;
 
     // ---- emit
@@ -1264,6 +1406,56 @@ __global__ void __launch_bounds__(MINB > 0 ? 128 : kClipMaxThreads, MINB > 0 ? M
     atomicAdd(p.counters + 1, (unsigned long long)pc.esc);
     if (n_uncert && p.uncertified) atomicAdd(p.uncertified, (unsigned long long)n_uncert);
   }
+}
+
+// ------------------------------------------------------------------------
+// recheck of the cells flagged uncertified: the radius bound again, from
+// the emitted record's planes, FP64 for the vertices whose FP32 bound is
+// loose; a cell it certifies loses the flag, the others give their site's
+// longer list its length (site_need, the largest radius of the site's
+// flagged cells)
+// ------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) recheck_cells_kernel(RecheckParams p) {
+  const int lane = threadIdx.x & 31;
+  const long long n_warps = ((long long)gridDim.x * blockDim.x) >> 5;
+  const long long n = *p.n_dev;
+  for (long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n;
+       w += n_warps) {
+    const long long q = __ldg(p.idx + w);
+    rpd_cell_header h = p.headers[q];
+    const int sid = h.site_id;
+    const float4 seed = __ldg(p.site4f + sid);
+    const float3 S = make_float3(seed.x, seed.y, seed.z);
+    const int row = p.site_row ? __ldg(p.site_row + sid) : -1;
+    const float bound = row >= 0 ? __ldg(p.ext_bound + row) : __ldg(p.nbr_bound + sid);
+    const PayloadLayout L(h.nb_v, h.nb_p, h.nb_e);
+    const float4* pl = reinterpret_cast<const float4*>(p.payload + h.offset + L.plane);
+    const uchar4* ver = reinterpret_cast<const uchar4*>(p.payload + h.offset + L.ver);
+    float r = 0.f;
+    for (int v = lane; v < h.nb_v; v += 32) {
+      const uchar4 t = ver[v];
+      const float4 a = pl[t.x], b = pl[t.y], d = pl[t.z];
+      float4 K, M;
+      vertex_cofactors(a, b, d, K, M);
+      r = fmaxf(r, vertex_radius_p(K, M, S, a, b, d));
+    }
+    for (int o = 16; o > 0; o >>= 1) r = fmaxf(r, __shfl_xor_sync(0xffffffffu, r, o));
+    if (lane == 0) {
+      // a complete list (bound infinite) certifies any cell
+      if (!(bound < INFINITY) || cert_holds(bound, r, p.margin)) {
+        p.headers[q].flags = (uint8_t)(h.flags & ~RPD_CELL_UNCERTIFIED);
+      } else {
+        if (p.site_need) atomicMax(p.site_need + sid, __float_as_uint(r));
+        if (p.kept_idx) p.kept_idx[atomicAdd(p.kept_count, 1ull)] = (int32_t)q;
+      }
+    }
+  }
+}
+
+cudaError_t launch_recheck_cells(const RecheckParams& p, int num_sms, cudaStream_t st) {
+  recheck_cells_kernel<<<(unsigned)(num_sms * 16), 128, 0, st>>>(p);
+  note_launches(1);
+  return cudaGetLastError();
 }
 
 // ------------------------------------------------------------------------
@@ -1535,9 +1727,9 @@ template <int PRED, bool CERT, int MINB>
 static int occ_of(int warps) {
   size_t smem = sizeof(WarpCell) * warps;
   int n = 0;
-  cudaFuncSetAttribute(clip_cells_kernel<PRED, CERT, MINB>,
+  cudaFuncSetAttribute(clip_cells_kernel<PRED, CERT, MINB, false>,
                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, clip_cells_kernel<PRED, CERT, MINB>,
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, clip_cells_kernel<PRED, CERT, MINB, false>,
                                                 warps * 32, smem);
   return n > 0 ? n : 1;
 }
@@ -1572,21 +1764,32 @@ int box_blocks_per_sm(int warps) {
   return n > 0 ? n : 1;
 }
 
-template <int PRED, bool CERT, int MINB>
+template <int PRED, bool CERT, int MINB, bool EXT>
 static void launch_one(const ClipParams& p, int blocks, int warps, cudaStream_t st) {
   size_t smem = sizeof(WarpCell) * warps;
-  cudaFuncSetAttribute(clip_cells_kernel<PRED, CERT, MINB>,
+  cudaFuncSetAttribute(clip_cells_kernel<PRED, CERT, MINB, EXT>,
                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  clip_cells_kernel<PRED, CERT, MINB><<<blocks, warps * 32, smem, st>>>(p);
+  clip_cells_kernel<PRED, CERT, MINB, EXT><<<blocks, warps * 32, smem, st>>>(p);
   note_launches(1);
 }
 
+// the re-clips with extended rows (few cells) use one register budget (80:
+// six blocks of four warps per SM), whatever the first pass's variant
 template <int PRED, bool CERT>
 static void launch_variant(const ClipParams& p, int variant, int blocks, int warps,
                            cudaStream_t st) {
-  if (variant == 1) launch_one<PRED, CERT, 6>(p, blocks, 4, st);
-  else if (variant == 2) launch_one<PRED, CERT, 8>(p, blocks, 4, st);
-  else launch_one<PRED, CERT, 0>(p, blocks, warps, st);
+  if (p.site_row) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    launch_one<PRED, CERT, 6, true>(p, (sms > 0 ? sms : 1) * 6, 4, st);
+  } else if (variant == 1) {
+    launch_one<PRED, CERT, 6, false>(p, blocks, 4, st);
+  } else if (variant == 2) {
+    launch_one<PRED, CERT, 8, false>(p, blocks, 4, st);
+  } else {
+    launch_one<PRED, CERT, 0, false>(p, blocks, warps, st);
+  }
 }
 
 cudaError_t launch_clip_cells(const ClipParams& p, int pred_mode, int certify, int variant,

@@ -68,7 +68,7 @@ struct DevBuf {
 
 enum Ev {
   kEvStart, kEvKnn, kEvPairs, kEvPred0, kEvPred1, kEvClipK0, kEvClipK1, kEvEpi0, kEvClip, kEvEnd,
-  kEvTopo0, kEvTopo1, kEvCount
+  kEvTopo0, kEvTopo1, kEvExt0, kEvExt1, kEvExtR0, kEvExtK, kEvCount
 };
 
 }  // namespace rpd_host
@@ -120,6 +120,19 @@ struct rpd_ctx {
   long long n_reclipped = 0;
   DevBuf<float> nbr_keys;
   bool has_user_nbr = false;
+  // exact lists (rpd_config.exact_lists): the completeness bound of every
+  // base list, and the longer lists given to sites whose cells a pass left
+  // uncertified -- row r of the extended lists starts at ext_off[r]
+  DevBuf<float> nbr_bound;          // n_site
+  DevBuf<unsigned int> site_need;   // n_site: radius bound (float bits), 0 = none
+  DevBuf<int32_t> site_row;         // n_site: extended row, -1 = base list
+  DevBuf<int32_t> ext_sites, site_flag, site_pos, ext_idx;
+  DevBuf<int32_t> ext_nbr, ext_len;
+  DevBuf<float> ext_keys, ext_bound;
+  DevBuf<long long> ext_off;
+  long long ext_used = 0;           // entries of ext_nbr / ext_keys in use
+  int ext_rows = 0;                 // rows in use
+  bool ext_valid = false;           // site_row / ext_* describe the last compute's lists
 
   // grids
   DevBuf<int32_t> s_cell_of, s_cell_count, s_cell_start, s_cell_fill, s_cell_items;
@@ -204,6 +217,7 @@ struct rpd_ctx {
   DevBuf<int32_t> flag_tmp, pos_tmp;
   DevBuf<unsigned long long> scratch;  // [0] payload cursor [1] work [2..3] counters
                                        // [4] pair cursor [8..18] status hist
+                                       // [32] cells still uncertified
   DevBuf<long long> n_out;
   long long payload_cap_hint = 0;
 
@@ -245,7 +259,8 @@ rpd_status rpd_cuda_fail(rpd_ctx* c, cudaError_t e, const char* where);
 Grid rpd_make_grid(const double* lo, const double* hi, long long n_items, double per_cell);
 // CSR, clipping, epilogue, compaction and statistics once pair_buf /
 // tet_count hold the candidate pairs (c->n_pairs of them)
-rpd_status rpd_finish_compute(rpd_ctx* c, bool knn, bool learned, rpd_stats* stats);
+rpd_status rpd_finish_compute(rpd_ctx* c, bool knn, bool learned, rpd_stats* stats,
+                              bool extend = false);
 
 #define RPD_CK(ctx, expr, where)                                      \
   do {                                                                \

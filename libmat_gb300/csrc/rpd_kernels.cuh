@@ -57,7 +57,40 @@ struct ClipParams {
   const int32_t* pair_index;
   long long n_work;
   unsigned long long* topo_hash;  // n_pairs canonical topology hashes, or null
+  // completeness of the lists: every site missing from site s's base list
+  // has a key >= nbr_bound[s] (INFINITY: the list holds every site); null =
+  // no bound known (no cell is ever flagged uncertified)
+  const float* nbr_bound;
+  // extended lists: site s clips with row site_row[s] (>= 0) instead of its
+  // base row; the row's entries start at ext_off[row], ext_len[row] of them
+  // (-1 padded beyond), keys ascending (certified clipping), and every site
+  // not in it has a key >= ext_bound[row]
+  const int32_t* site_row;       // n_site, or null
+  const int32_t* ext_nbr;
+  const float* ext_keys;
+  const long long* ext_off;
+  const int32_t* ext_len;
+  const float* ext_bound;
 };
+
+// cells flagged RPD_CELL_UNCERTIFIED by the clip kernel, bounded again:
+// flag cleared where the certificate holds, else the radius (float bits)
+// raised into site_need[site] (optional)
+struct RecheckParams {
+  rpd_cell_header* headers;  // pair headers
+  const int32_t* idx;        // the flagged pairs, *n_dev of them
+  const int32_t* n_dev;
+  const uint8_t* payload;
+  const float4* site4f;
+  const int32_t* site_row;   // as ClipParams, or null
+  const float* ext_bound;
+  const float* nbr_bound;
+  float margin;
+  unsigned int* site_need;
+  int32_t* kept_idx;                // the pairs still flagged, in any order
+  unsigned long long* kept_count;   // their number (added to)
+};
+cudaError_t launch_recheck_cells(const RecheckParams& p, int num_sms, cudaStream_t st);
 
 // coordinates, volume and topology hash of the emitted cells (after the
 // clip passes, before compaction)
@@ -153,7 +186,33 @@ cudaError_t grid_build_tets(const float4* centroid, int n_tet, const uint8_t* cl
 cudaError_t launch_knn(const float4* site4f, int n_site, const Grid& g,
                        const int32_t* cell_start, const int32_t* cell_items, int k,
                        float w_max, int order_by_id, int32_t* nbr, float* keys,
-                       int32_t* nbr_dist, int32_t* status, cudaStream_t st, int id_offset = 0);
+                       int32_t* nbr_dist, int32_t* status, cudaStream_t st, int id_offset = 0,
+                       float* bound_out = nullptr);
+// the general form: rows for a subset of the sites, only keys up to a
+// per-site bound, longer lists (k <= knn_max_k())
+struct KnnArgs {
+  const float4* site4f;  // the mesh's sites; subset, rows and grid items index them
+  int n_rows;
+  Grid g;
+  const int32_t* cell_start;
+  const int32_t* cell_items;
+  int k;                 // row stride and longest list
+  float w_max;
+  int order_by_id;       // nbr sorted by id (else distance order)
+  int32_t* nbr;          // n_rows x k, -1 padded
+  float* keys;           // n_rows x k ascending keys (INFINITY padded), or null
+  int32_t* nbr_dist;     // n_rows x k in distance order, or null
+  int32_t* status;       // per row: 1 = every site of the grid was seen, or null
+  int id_offset;         // added to the listed ids
+  const int32_t* subset;       // row f lists site subset[f] (null: row f is site f)
+  const unsigned int* radius;  // per site, float bits R: only keys <= R * bound_scale +
+                               // bound_abs are listed (null: no bound)
+  float bound_scale, bound_abs;
+  int32_t* len_out;      // per row: entries listed, or null
+  float* bound_out;      // per row: every site not listed has a key >= this, or null
+};
+int knn_max_k();
+cudaError_t launch_knn(const KnnArgs& a, cudaStream_t st);
 
 // candidate pairs: per site, tets whose centroid lies in the site's box and
 // that pass the reference rule; appends (tet, site) and counts per tet
@@ -193,11 +252,29 @@ cudaError_t pairs_to_csr(const int2* pair_buf, long long n_pairs, int n_tet,
                          const int32_t* tet_offsets, int32_t* tet_fill, int32_t* pair_site,
                          int32_t* pair_tet, int32_t* tet_k_out, cudaStream_t st);
 
-// compaction of emitted cells (status success) in pair order
+// compaction of emitted cells (status success) in pair order; n_uncert
+// (optional) counts the emitted cells flagged RPD_CELL_UNCERTIFIED
 cudaError_t compact_cells(const rpd_cell_header* pair_headers, long long n_pairs,
                           int32_t* flag_tmp, int32_t* pos_tmp, int32_t* scan_tmp,
                           rpd_cell_header* out, long long* n_out_dev,
-                          unsigned long long* status_hist, cudaStream_t st);
+                          unsigned long long* status_hist, cudaStream_t st,
+                          unsigned long long* n_uncert = nullptr);
+// indices of the pairs whose header carries RPD_CELL_UNCERTIFIED
+cudaError_t select_uncertified(const rpd_cell_header* h, long long n, int32_t* flag_tmp,
+                               int32_t* pos_tmp, int32_t* scan_tmp, int32_t* idx_out,
+                               cudaStream_t st);
+// sites with site_need != 0, ascending (idx_out), their count at pos_tmp[n]
+cudaError_t select_sites(const unsigned int* site_need, int n, int32_t* flag_tmp,
+                         int32_t* pos_tmp, int32_t* scan_tmp, int32_t* idx_out, cudaStream_t st);
+// extended rows row0 + f (f < n) of the sites sites[f]: site_row[sites[f]] =
+// row0 + f, ext_off[row0 + f] = off0 + f * stride
+cudaError_t assign_rows(const int32_t* sites, int n, int row0, long long off0, int stride,
+                        int32_t* site_row, long long* ext_off, cudaStream_t st);
+// rows row0 + f of the sites sites[f], all on one list of every site
+// (written at ext_nbr[off..off + n_site)), bound INFINITY
+cudaError_t complete_rows(const int32_t* sites, int n, int row0, long long off, int n_site,
+                          int32_t* site_row, long long* ext_off, int32_t* ext_len,
+                          float* ext_bound, int32_t* ext_nbr, cudaStream_t st);
 
 // batches: first compacted cell of each mesh (n_mesh + 1 entries); record
 // sizes; gather of one mesh's records with mesh-local ids

@@ -303,6 +303,7 @@ __device__ void for_items(int n_cells_iter, CellAt cell_at, const int32_t* cell_
 // ------------------------------------------------------------------------
 constexpr int kKnnBuf = 1024;
 constexpr int kKnnWarps = 4;
+constexpr int kKnnLongBuf = 8192;  // long lists (k > kKnnBuf - 64): 64 KB, one warp per block
 
 __device__ __forceinline__ uint32_t order_key(float f) {
   uint32_t u = __float_as_uint(f);
@@ -349,17 +350,31 @@ __device__ __forceinline__ int next_pow2(int x) {
   return p;
 }
 
-__global__ void __launch_bounds__(kKnnWarps * 32) knn_kernel(
-    const float4* site4f, int n_site, Grid g, const int32_t* cell_start,
-    const int32_t* cell_items, int k, float w_max, int order_by_id, int32_t* nbr, float* keys,
-    int32_t* nbr_dist, int32_t* status, int id_offset) {
-  __shared__ unsigned long long sbuf[kKnnWarps][kKnnBuf];
-  __shared__ int scnt[kKnnWarps];
+// One warp per row: the k smallest (key, id) of site i = subset[row] (or
+// i = row), optionally only keys <= B (B = R_i * bound_scale + bound_abs,
+// R_i the float in radius[i]).  Rings of grid cells around the site are
+// searched until every site outside has a key above the k-th kept one (or
+// above B): keys of sites at distance >= D are >= (D^2 + w_i - w_max)/(2D).
+// Candidates collect in a per-warp buffer of BUF entries (key bits | id,
+// 64-bit) that is sorted and cut to k whenever it fills.
+template <int BUF, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) knn_kernel(KnnArgs a) {
+  extern __shared__ __align__(16) unsigned long long knn_smem[];
+  __shared__ int scnt[WARPS];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  unsigned long long* buf = sbuf[wid];
-  const int i = blockIdx.x * kKnnWarps + wid;
-  if (i >= n_site) return;
-  const float4 si = site4f[i];
+  unsigned long long* buf = knn_smem + (size_t)wid * BUF;
+  const int row = blockIdx.x * WARPS + wid;
+  if (row >= a.n_rows) return;
+  const int i = a.subset ? a.subset[row] : row;
+  const int k = a.k;
+  const Grid& g = a.g;
+  const float4 si = a.site4f[i];
+  float B = INFINITY;
+  if (a.radius) {
+    const float R = __uint_as_float(a.radius[i]);
+    B = R * a.bound_scale + a.bound_abs;
+    if (!(B < INFINITY)) B = INFINITY;  // inf or nan radius: no bound
+  }
   const int cx = clampi((int)floorf((si.x - g.lo.x) * g.inv_cell), 0, g.nx - 1);
   const int cy = clampi((int)floorf((si.y - g.lo.y) * g.inv_cell), 0, g.ny - 1);
   const int cz = clampi((int)floorf((si.z - g.lo.z) * g.inv_cell), 0, g.nz - 1);
@@ -378,24 +393,24 @@ __global__ void __launch_bounds__(kKnnWarps * 32) knn_kernel(
       if (x < 0 || y < 0 || z < 0 || x >= g.nx || y >= g.ny || z >= g.nz) return -1;
       return x + g.nx * (y + g.ny * z);
     };
-    for_items(n_cube, cell_at, cell_start, cell_items, lane, [&](int j, bool valid) {
+    for_items(n_cube, cell_at, a.cell_start, a.cell_items, lane, [&](int j, bool valid) {
       bool take = false;
       unsigned long long packed = 0;
       if (valid && j != i) {
-        float key = bisector_key(si, site4f[j]);
+        float key = bisector_key(si, a.site4f[j]);
         packed = ((unsigned long long)order_key(key) << 32) | (uint32_t)j;
-        take = packed < kth;
+        take = packed < kth && key <= B;
       }
       uint32_t m = __ballot_sync(0xffffffffu, take);
       int base = scnt[wid];
       if (take) buf[base + __popc(m & ((1u << lane) - 1u))] = packed;
       __syncwarp();
       int cnt = base + __popc(m);
-      if (cnt > kKnnBuf - 32) {
+      if (cnt > BUF - 32) {
         // sort and keep the best k
-        for (int q = cnt + lane; q < kKnnBuf; q += 32) buf[q] = ~0ull;
+        for (int q = cnt + lane; q < BUF; q += 32) buf[q] = ~0ull;
         __syncwarp();
-        warp_bitonic_sort(buf, kKnnBuf, lane);
+        warp_bitonic_sort(buf, BUF, lane);
         cnt = min(cnt, k);
         if (cnt >= k) kth = buf[k - 1];
       }
@@ -409,29 +424,37 @@ __global__ void __launch_bounds__(kKnnWarps * 32) knn_kernel(
     warp_bitonic_sort(buf, n, lane);
     cnt = min(cnt, k);
     if (lane == 0) scnt[wid] = cnt;
+    float T = B;  // keys above T are not wanted
     if (cnt >= k) {
       kth = buf[k - 1];
-      // keys of sites outside the searched block are >= f(D) with
-      // D >= r * cell, f(D) = (D^2 + wi - wmax) / (2D) increasing in D
-      float D = (float)r * g.cell;
-      if (D > 0.f) {
-        float lb = (D * D + si.w - w_max) / (2.f * D);
-        float kv = key_value((uint32_t)(kth >> 32));
-        if (kv < lb - 1e-4f * (fabsf(lb) + D)) done = 1;
-      }
+      T = fminf(T, key_value((uint32_t)(kth >> 32)));
+    }
+    // keys of sites outside the searched block are >= f(D) with
+    // D >= r * cell, f(D) = (D^2 + wi - wmax) / (2D) increasing in D
+    float D = (float)r * g.cell;
+    if (D > 0.f && T < INFINITY) {
+      float lb = (D * D + si.w - a.w_max) / (2.f * D);
+      if (T < lb - 1e-4f * (fabsf(lb) + D)) done = 1;
     }
     __syncwarp();
   }
   int cnt = scnt[wid];
-  if (status && lane == 0) status[i] = done ? 0 : 1;  // 1: exhausted grid
+  if (a.status && lane == 0) a.status[row] = done ? 0 : 1;  // 1: exhausted grid
+  if (lane == 0) {
+    if (a.len_out) a.len_out[row] = cnt;
+    // every site not listed has a key >= this: the k-th key when the list
+    // is full, else the bound (or none: all sites were seen)
+    if (a.bound_out) a.bound_out[row] = cnt >= k ? key_value((uint32_t)(buf[k - 1] >> 32)) : B;
+  }
+  const long long rb = (long long)row * k;
   // outputs in distance order
   for (int q = lane; q < k; q += 32) {
-    int32_t id = q < cnt ? (int32_t)(uint32_t)buf[q] + id_offset : -1;
-    if (keys) keys[(long long)i * k + q] = q < cnt ? key_value((uint32_t)(buf[q] >> 32)) : INFINITY;
-    if (!order_by_id) nbr[(long long)i * k + q] = id;
-    if (nbr_dist) nbr_dist[(long long)i * k + q] = id;
+    int32_t id = q < cnt ? (int32_t)(uint32_t)buf[q] + a.id_offset : -1;
+    if (a.keys) a.keys[rb + q] = q < cnt ? key_value((uint32_t)(buf[q] >> 32)) : INFINITY;
+    if (!a.order_by_id) a.nbr[rb + q] = id;
+    if (a.nbr_dist) a.nbr_dist[rb + q] = id;
   }
-  if (order_by_id) {
+  if (a.order_by_id) {
     __syncwarp();
     int n = next_pow2(max(k, 1));
     // reuse the buffer: ids as 64-bit values, padding at the end
@@ -444,21 +467,52 @@ __global__ void __launch_bounds__(kKnnWarps * 32) knn_kernel(
     __syncwarp();
     warp_bitonic_sort(buf, n, lane);
     for (int q = lane; q < k; q += 32)
-      nbr[(long long)i * k + q] = q < cnt ? (int32_t)buf[q] + id_offset : -1;
+      a.nbr[rb + q] = q < cnt ? (int32_t)buf[q] + a.id_offset : -1;
   }
+}
+
+int knn_max_k() { return kKnnLongBuf - 64; }
+
+cudaError_t launch_knn(const KnnArgs& a, cudaStream_t st) {
+  if (a.n_rows <= 0) return cudaSuccess;
+  if (a.k < 1 || a.k > knn_max_k()) return cudaErrorInvalidValue;
+  if (a.k <= kKnnBuf - 64) {
+    const size_t smem = (size_t)kKnnWarps * kKnnBuf * sizeof(unsigned long long);
+    int blocks = (a.n_rows + kKnnWarps - 1) / kKnnWarps;
+    knn_kernel<kKnnBuf, kKnnWarps><<<blocks, kKnnWarps * 32, smem, st>>>(a);
+  } else {
+    // long lists: one warp per block, kKnnLongBuf entries of shared memory
+    const size_t smem = (size_t)kKnnLongBuf * sizeof(unsigned long long);
+    // (set on every such launch: the attribute belongs to the current device)
+    cudaError_t e = cudaFuncSetAttribute(knn_kernel<kKnnLongBuf, 1>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    knn_kernel<kKnnLongBuf, 1><<<a.n_rows, 32, smem, st>>>(a);
+  }
+  note_launches(1);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_knn(const float4* site4f, int n_site, const Grid& g, const int32_t* cell_start,
                        const int32_t* cell_items, int k, float w_max, int order_by_id,
                        int32_t* nbr, float* keys, int32_t* nbr_dist, int32_t* status,
-                       cudaStream_t st, int id_offset) {
-  if (n_site <= 0) return cudaSuccess;
-  int blocks = (n_site + kKnnWarps - 1) / kKnnWarps;
-  knn_kernel<<<blocks, kKnnWarps * 32, 0, st>>>(site4f, n_site, g, cell_start, cell_items, k,
-                                               w_max, order_by_id, nbr, keys, nbr_dist, status,
-                                               id_offset);
-  note_launches(1);
-  return cudaGetLastError();
+                       cudaStream_t st, int id_offset, float* bound_out) {
+  KnnArgs a = {};
+  a.site4f = site4f;
+  a.n_rows = n_site;
+  a.g = g;
+  a.cell_start = cell_start;
+  a.cell_items = cell_items;
+  a.k = k;
+  a.w_max = w_max;
+  a.order_by_id = order_by_id;
+  a.nbr = nbr;
+  a.keys = keys;
+  a.nbr_dist = nbr_dist;
+  a.status = status;
+  a.id_offset = id_offset;
+  a.bound_out = bound_out;
+  return launch_knn(a, st);
 }
 
 // ------------------------------------------------------------------------
@@ -789,19 +843,22 @@ cudaError_t pairs_to_csr(const int2* pair_buf, long long n_pairs, int n_tet,
 // compaction
 // ------------------------------------------------------------------------
 __global__ void flag_cells_kernel(const rpd_cell_header* h, long long n, int32_t* flag,
-                                  unsigned long long* hist) {
-  __shared__ unsigned int sh[11];
-  if (threadIdx.x < 11) sh[threadIdx.x] = 0;
+                                  unsigned long long* hist, unsigned long long* n_uncert) {
+  __shared__ unsigned int sh[12];
+  if (threadIdx.x < 12) sh[threadIdx.x] = 0;
   __syncthreads();
   long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (q < n) {
-    int s = h[q].status;
+    const rpd_cell_header hq = h[q];
+    const int s = hq.status;
     flag[q] = s == kSuccess ? 1 : 0;
     int b = (s >= 0 && s <= 8) ? s : (s == kPayloadFull ? 10 : 9);
     atomicAdd(sh + b, 1u);
+    if (s == kSuccess && (hq.flags & RPD_CELL_UNCERTIFIED)) atomicAdd(sh + 11, 1u);
   }
   __syncthreads();
   if (threadIdx.x < 11 && sh[threadIdx.x]) atomicAdd(hist + threadIdx.x, (unsigned long long)sh[threadIdx.x]);
+  if (threadIdx.x == 11 && n_uncert && sh[11]) atomicAdd(n_uncert, (unsigned long long)sh[11]);
 }
 
 __global__ void gather_cells_kernel(const rpd_cell_header* h, long long n, const int32_t* pos,
@@ -813,10 +870,11 @@ __global__ void gather_cells_kernel(const rpd_cell_header* h, long long n, const
 
 cudaError_t compact_cells(const rpd_cell_header* pair_headers, long long n_pairs, int32_t* flag_tmp,
                           int32_t* pos_tmp, int32_t* scan_tmp, rpd_cell_header* out,
-                          long long* n_out_dev, unsigned long long* status_hist, cudaStream_t st) {
+                          long long* n_out_dev, unsigned long long* status_hist, cudaStream_t st,
+                          unsigned long long* n_uncert) {
   int nb = (int)((n_pairs + 255) / 256);
   if (n_pairs > 0) {
-    flag_cells_kernel<<<nb, 256, 0, st>>>(pair_headers, n_pairs, flag_tmp, status_hist);
+    flag_cells_kernel<<<nb, 256, 0, st>>>(pair_headers, n_pairs, flag_tmp, status_hist, n_uncert);
     note_launches(1);
   }
   cudaError_t err = scan_exclusive(flag_tmp, pos_tmp, n_pairs, scan_tmp, st);
@@ -852,6 +910,97 @@ cudaError_t select_pairs(const rpd_cell_header* h, long long n, int status, int3
     scatter_index_kernel<<<nb, 256, 0, st>>>(flag_tmp, pos_tmp, n, idx_out);
     note_launches(1);
   }
+  return cudaGetLastError();
+}
+
+__global__ void flag_uncert_kernel(const rpd_cell_header* h, long long n, int32_t* flag) {
+  long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < n) {
+    const rpd_cell_header hq = h[q];
+    flag[q] = (hq.status == kSuccess && (hq.flags & RPD_CELL_UNCERTIFIED)) ? 1 : 0;
+  }
+}
+
+cudaError_t select_uncertified(const rpd_cell_header* h, long long n, int32_t* flag_tmp,
+                               int32_t* pos_tmp, int32_t* scan_tmp, int32_t* idx_out,
+                               cudaStream_t st) {
+  int nb = (int)((n + 255) / 256);
+  if (n > 0) {
+    flag_uncert_kernel<<<nb, 256, 0, st>>>(h, n, flag_tmp);
+    note_launches(1);
+  }
+  cudaError_t err = scan_exclusive(flag_tmp, pos_tmp, n, scan_tmp, st);
+  if (err != cudaSuccess) return err;
+  if (n > 0) {
+    scatter_index_kernel<<<nb, 256, 0, st>>>(flag_tmp, pos_tmp, n, idx_out);
+    note_launches(1);
+  }
+  return cudaGetLastError();
+}
+
+__global__ void flag_need_kernel(const unsigned int* need, int n, int32_t* flag) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) flag[i] = need[i] != 0u ? 1 : 0;
+}
+
+cudaError_t select_sites(const unsigned int* site_need, int n, int32_t* flag_tmp,
+                         int32_t* pos_tmp, int32_t* scan_tmp, int32_t* idx_out, cudaStream_t st) {
+  int nb = (n + 255) / 256;
+  if (n > 0) {
+    flag_need_kernel<<<nb, 256, 0, st>>>(site_need, n, flag_tmp);
+    note_launches(1);
+  }
+  cudaError_t err = scan_exclusive(flag_tmp, pos_tmp, n, scan_tmp, st);
+  if (err != cudaSuccess) return err;
+  if (n > 0) {
+    scatter_index_kernel<<<nb, 256, 0, st>>>(flag_tmp, pos_tmp, n, idx_out);
+    note_launches(1);
+  }
+  return cudaGetLastError();
+}
+
+__global__ void assign_rows_kernel(const int32_t* sites, int n, int row0, long long off0,
+                                   int stride, int32_t* site_row, long long* ext_off) {
+  int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f < n) {
+    site_row[sites[f]] = row0 + f;
+    ext_off[row0 + f] = off0 + (long long)f * stride;
+  }
+}
+
+cudaError_t assign_rows(const int32_t* sites, int n, int row0, long long off0, int stride,
+                        int32_t* site_row, long long* ext_off, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  assign_rows_kernel<<<(n + 255) / 256, 256, 0, st>>>(sites, n, row0, off0, stride, site_row,
+                                                      ext_off);
+  note_launches(1);
+  return cudaGetLastError();
+}
+
+// complete rows: one shared list of every site (ids 0..n_site-1, the seed
+// itself included: its bisector is the zero plane, which clips nothing) at
+// ext_nbr[off..off + n_site), and rows row0 + f of the sites sites[f] on it
+__global__ void complete_rows_kernel(const int32_t* sites, int n, int row0, long long off,
+                                     int n_site, int32_t* site_row, long long* ext_off,
+                                     int32_t* ext_len, float* ext_bound, int32_t* ext_nbr) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n_site) ext_nbr[off + i] = i;
+  if (i < n) {
+    site_row[sites[i]] = row0 + i;
+    ext_off[row0 + i] = off;
+    ext_len[row0 + i] = n_site;
+    ext_bound[row0 + i] = INFINITY;
+  }
+}
+
+cudaError_t complete_rows(const int32_t* sites, int n, int row0, long long off, int n_site,
+                          int32_t* site_row, long long* ext_off, int32_t* ext_len,
+                          float* ext_bound, int32_t* ext_nbr, cudaStream_t st) {
+  const int m = n > n_site ? n : n_site;
+  if (m <= 0) return cudaSuccess;
+  complete_rows_kernel<<<(m + 255) / 256, 256, 0, st>>>(sites, n, row0, off, n_site, site_row,
+                                                        ext_off, ext_len, ext_bound, ext_nbr);
+  note_launches(1);
   return cudaGetLastError();
 }
 

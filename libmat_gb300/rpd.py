@@ -74,7 +74,8 @@ class Config(ctypes.Structure):
                 ("warps_per_block", ctypes.c_int), ("blocks_per_sm", ctypes.c_int),
                 ("certify", ctypes.c_int), ("clip_variant", ctypes.c_int),
                 ("learned_k", ctypes.c_int), ("box_planes", ctypes.c_int),
-                ("topology_hash", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
+                ("topology_hash", ctypes.c_int), ("exact_lists", ctypes.c_int),
+                ("reserved", ctypes.c_int * 2)]
 
 
 class MeshInfo(ctypes.Structure):
@@ -120,7 +121,10 @@ class Stats(ctypes.Structure):
                 ("n_reclipped", ctypes.c_int64), ("ms_predict", ctypes.c_float),
                 ("learned", ctypes.c_int32), ("n_fp64_uncertain", ctypes.c_int64),
                 ("n_exact_flips", ctypes.c_int64), ("ms_epilogue", ctypes.c_float),
-                ("n_uncertified", ctypes.c_int64)]
+                ("n_uncertified", ctypes.c_int64), ("n_extended_sites", ctypes.c_int64),
+                ("n_cert_reclipped", ctypes.c_int64), ("ms_extend", ctypes.c_float),
+                ("n_extend_rounds", ctypes.c_int32), ("ext_longest", ctypes.c_int32),
+                ("ms_extend_lists", ctypes.c_float)]
 
     def as_dict(self):
         d = {f: getattr(self, f) for f, _ in self._fields_ if f not in ("status_counts", "search")}
@@ -342,7 +346,7 @@ class RPD:
     def __init__(self, device=0, predicate_mode=PRED_FP32_FILTER, neighbor_source=NEIGH_KNN,
                  knn_k=64, clip_order=ORDER_SITE_ID, compute_geometry=True,
                  warps_per_block=0, blocks_per_sm=0, certify=False, clip_variant=0,
-                 learned_k=False, box_planes=0, topology_hash=True):
+                 learned_k=False, box_planes=0, topology_hash=True, exact_lists=True):
         L = load()
         cfg = Config()
         L.rpd_config_default(ctypes.byref(cfg))
@@ -359,6 +363,7 @@ class RPD:
         cfg.learned_k = 1 if learned_k else 0
         cfg.box_planes = box_planes
         cfg.topology_hash = 1 if topology_hash else 0
+        cfg.exact_lists = 1 if exact_lists else 0
         h = ctypes.c_void_p()
         s = L.rpd_create(ctypes.byref(cfg), ctypes.byref(h))
         if s != 0:

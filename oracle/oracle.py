@@ -76,6 +76,8 @@ def lib():
         L.orc_topo_bytes.argtypes = [i32, i32, i32]
         L.orc_cell_topology.restype = i64
         L.orc_cell_topology.argtypes = [i64, vp, vp, vp, vp, i64]
+        L.orc_power_neighbors.restype = i32
+        L.orc_power_neighbors.argtypes = [i32, vp, vp, i32, vp, vp, i32]
         L.orc_cell_polygons.restype = i32
         L.orc_cell_polygons.argtypes = [i64, vp, vp, i32, i32, i32, vp, vp, i64, vp, vp, i64,
                                         vp, vp, i64, vp]
@@ -155,6 +157,23 @@ def knn(site4f, k, n_threads=None):
     keys = np.empty((n, k), np.float32)
     lib().orc_knn(n, _p(site4f), k, _p(nbr), _p(keys), n_threads or nthreads())
     return nbr, keys
+
+
+def power_neighbors(site4f, lo, hi, max_nbr=96, n_threads=None):
+    """Power neighbours of every site inside the box [lo, hi] -- the stand-in
+    for libmat's regular-triangulation lists (exact signs, ascending keys
+    until no unseen site can cut the cell).  Returns (nbr [n, max_nbr] ids
+    ascending, -1 padded; count [n]: neighbours, -1 hidden, -2 / -3 the
+    clipper's capacity or max_nbr exceeded)."""
+    site4f = np.ascontiguousarray(site4f, np.float32)
+    n = site4f.shape[0]
+    region = np.ascontiguousarray(np.concatenate([np.asarray(lo, np.float64).ravel(),
+                                                  np.asarray(hi, np.float64).ravel()]))
+    nbr = np.empty((n, max_nbr), np.int32)
+    count = np.empty(n, np.int32)
+    lib().orc_power_neighbors(n, _p(site4f), _p(region), max_nbr, _p(nbr), _p(count),
+                              n_threads or nthreads())
+    return nbr, count
 
 
 def candidate_pairs(vert3f, tets, site4f, flags, nbr, n_threads=None):

@@ -1348,3 +1348,240 @@ int orc_cell_polygons(int64_t n_cells, const orc_cell_header* cells,
   }
   return 0;
 }
+
+/* ------------------------------------------------------------------ */
+/* power neighbours: the stand-in for libmat's regular-triangulation   */
+/* neighbour lists (src/rpd3d_base/triangulation.cxx:62-144, :442-558) */
+/* ------------------------------------------------------------------ */
+typedef struct {
+  double key;
+  int32_t id;
+} pn_kv;
+
+static int pn_less(const pn_kv* a, const pn_kv* b) {
+  return a->key < b->key || (a->key == b->key && a->id < b->id);
+}
+
+static int pn_cmp(const void* x, const void* y) {
+  const pn_kv* a = (const pn_kv*)x;
+  const pn_kv* b = (const pn_kv*)y;
+  return pn_less(a, b) ? -1 : (pn_less(b, a) ? 1 : 0);
+}
+
+/* v[0..n) rearranged so that its m smallest entries come first (any order) */
+static void pn_select(pn_kv* v, int64_t n, int64_t m) {
+  int64_t lo = 0, hi = n - 1;
+  while (lo < hi) {
+    pn_kv piv = v[lo + (hi - lo) / 2];
+    int64_t i = lo, j = hi;
+    while (i <= j) {
+      while (pn_less(&v[i], &piv)) ++i;
+      while (pn_less(&piv, &v[j])) --j;
+      if (i <= j) {
+        pn_kv t = v[i];
+        v[i] = v[j];
+        v[j] = t;
+        ++i;
+        --j;
+      }
+    }
+    if (m - 1 <= j) hi = j;
+    else if (m - 1 >= i) lo = i;
+    else break;
+  }
+}
+
+/* largest distance from the seed to a vertex of the cell, vertices solved
+ * in double from the float planes */
+static double pn_radius(const cell_t* c) {
+  double r = 0.0;
+  for (int v = 0; v < c->nb_v; ++v) {
+    double a[4], b[4], d[4], x[3];
+    for (int q = 0; q < 4; ++q) {
+      a[q] = c->pl[c->ver[v][0]][q];
+      b[q] = c->pl[c->ver[v][1]][q];
+      d[q] = c->pl[c->ver[v][2]][q];
+    }
+    vertex_d(a, b, d, x);
+    double dx = x[0] - c->seed[0], dy = x[1] - c->seed[1], dz = x[2] - c->seed[2];
+    double r2 = sqrt(dx * dx + dy * dy + dz * dz);
+    if (!(r2 <= r)) r = r2;  /* NaN propagates as "unbounded" */
+  }
+  return r;
+}
+
+/* drops the planes no vertex uses and rebuilds the edge list from the
+ * vertices (the clipper never deletes either): only the cell's current
+ * faces and edges stay, so a long clip sequence fits the capacities.  Edge
+ * and face adjacency counts are not kept (the neighbour lists do not use
+ * them). */
+static void pn_compact(cell_t* c) {
+  uint8_t map[ORC_MAX_P];
+  memset(map, END, sizeof(map));
+  for (int v = 0; v < c->nb_v; ++v)
+    for (int q = 0; q < 3; ++q) map[c->ver[v][q]] = 0;
+  int np = 0;
+  for (int p = 0; p < c->nb_p; ++p) {
+    if (map[p] == END && p >= 4) continue;  /* the region's faces stay at 0..3 */
+    map[p] = (uint8_t)np;
+    if (np != p) {
+      memcpy(c->pl[np], c->pl[p], sizeof(c->pl[p]));
+      c->id2[np][0] = c->id2[p][0];
+      c->id2[np][1] = c->id2[p][1];
+      c->h[np] = c->h[p];
+    }
+    ++np;
+  }
+  c->nb_p = np;
+  c->nb_e = 0;
+  for (int v = 0; v < c->nb_v; ++v) {
+    for (int q = 0; q < 3; ++q) c->ver[v][q] = map[c->ver[v][q]];
+    for (int q = 0; q < 3; ++q) {
+      int a = c->ver[v][q], b = c->ver[v][(q + 1) % 3];
+      int lo = a < b ? a : b, hi = a < b ? b : a;
+      if (find_edge(c, lo, hi) >= 0) continue;
+      c->edge[c->nb_e][0] = (uint8_t)lo;
+      c->edge[c->nb_e][1] = (uint8_t)hi;
+      c->edge[c->nb_e][2] = 1;
+      c->nb_e++;
+    }
+  }
+}
+
+int orc_power_neighbors(int n_site, const float* site4, const double* region, int max_nbr,
+                        int32_t* nbr, int32_t* count, int n_threads) {
+  /* a regular tet around the region's box: vertices c + s (+-1, +-1, +-1)
+   * with an even number of minus signs; its inradius s / sqrt(3) exceeds
+   * the box's half diagonal */
+  double c0[3], h2 = 0.0, L = 0.0;
+  for (int a = 0; a < 3; ++a) {
+    c0[a] = 0.5 * (region[a] + region[3 + a]);
+    h2 += 0.25 * (region[3 + a] - region[a]) * (region[3 + a] - region[a]);
+    L = fmax(L, fmax(fabs(region[a]), fabs(region[3 + a])));
+  }
+  const double s = sqrt(h2) * sqrt(3.0) * 1.05 + 1.0;
+  static const double sg[4][3] = {{1, 1, 1}, {1, -1, -1}, {-1, 1, -1}, {-1, -1, 1}};
+  float tv3[12];
+  for (int v = 0; v < 4; ++v)
+    for (int a = 0; a < 3; ++a) tv3[3 * v + a] = (float)(c0[a] + s * sg[v][a]);
+  int32_t tv[4] = {0, 1, 2, 3};
+  const int32_t vad[4] = {1, 1, 1, 1}, fa[4] = {1, 1, 1, 1}, fi[4] = {-1, -1, -1, -1};
+  const uint8_t e6[6] = {1, 1, 1, 1, 1, 1};
+  {
+    /* inward normals need a positively oriented tet: the centre must lie on
+     * the inner side of face 0 */
+    cell_t t;
+    cell_init(&t, tv3, tv, vad, e6, fa, fi);
+    if ((double)t.pl[0][0] * c0[0] + (double)t.pl[0][1] * c0[1] + (double)t.pl[0][2] * c0[2] +
+            (double)t.pl[0][3] < 0.0) {
+      tv[0] = 1;
+      tv[1] = 0;
+    }
+  }
+  /* rounding of the float bisector planes against the exact keys, and of
+   * the radius: a site whose key exceeds R + margin cannot cut the cell */
+  const double margin = 1e-5 * (L + 2.0 * sqrt(h2)) + 1e-12;
+  int bad = 0;
+#ifdef _OPENMP
+  if (n_threads > 0) omp_set_num_threads(n_threads);
+#pragma omp parallel reduction(+ : bad)
+#endif
+  {
+    pn_kv* kv = (pn_kv*)malloc(sizeof(pn_kv) * (size_t)(n_site > 0 ? n_site : 1));
+    cell_t* c = (cell_t*)malloc(sizeof(cell_t));
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 16)
+#endif
+    for (int i = 0; i < n_site; ++i) {
+      const float* si = site4 + 4 * (int64_t)i;
+      int64_t m = 0;
+      int hidden = 0;
+      for (int j = 0; j < n_site; ++j) {
+        if (j == i) continue;
+        const float* sj = site4 + 4 * (int64_t)j;
+        double dx = (double)sj[0] - si[0], dy = (double)sj[1] - si[1], dz = (double)sj[2] - si[2];
+        double d2 = dx * dx + dy * dy + dz * dz;
+        if (d2 == 0.0) {
+          if ((double)sj[3] > (double)si[3]) hidden = 1;
+          continue;
+        }
+        kv[m].key = (d2 - (double)sj[3] + (double)si[3]) / (2.0 * sqrt(d2));
+        kv[m].id = j;
+        ++m;
+      }
+      int32_t* row = nbr + (int64_t)i * max_nbr;
+      for (int r = 0; r < max_nbr; ++r) row[r] = -1;
+      if (hidden) {
+        count[i] = -1;
+        continue;
+      }
+      c->pred_mode = 2;
+      c->n_pred = c->n_esc = c->n_unc = c->n_flip = 0;
+      c->seed_id = i;
+      memcpy(c->seed, si, sizeof(float) * 4);
+      cell_init(c, tv3, tv, vad, e6, fa, fi);
+      double R = pn_radius(c);
+      int64_t sorted = 0, pos = 0;
+      int certified = 0;
+      while (pos < m && c->status == ORC_SUCCESS) {
+        if (pos == sorted) {
+          /* next chunk of the smallest keys */
+          int64_t want = sorted == 0 ? 256 : (m - sorted);
+          if (want > m - sorted) want = m - sorted;
+          pn_select(kv + sorted, m - sorted, want);
+          qsort(kv + sorted, (size_t)want, sizeof(pn_kv), pn_cmp);
+          sorted += want;
+        }
+        if (kv[pos].key * (1.0 - 1e-9) - margin > R) {
+          certified = 1;
+          break;
+        }
+        if (c->nb_p > ORC_MAX_P - 8 || c->nb_e > ORC_MAX_E - 48) pn_compact(c);
+        int nb_p0 = c->nb_p;
+        clip_by_site(c, site4, kv[pos].id);
+        if (c->status == ORC_SUCCESS && c->nb_p > nb_p0) R = pn_radius(c);
+        ++pos;
+      }
+      (void)certified;
+      if (c->status == ORC_NO_INTERSECTION) {
+        count[i] = -1;
+        continue;
+      }
+      if (c->status != ORC_SUCCESS) {
+        count[i] = -2;
+        ++bad;
+        continue;
+      }
+      /* the sites of the bisector planes (4..) that carry a vertex */
+      uint8_t used[ORC_MAX_P];
+      memset(used, 0, sizeof(used));
+      for (int v = 0; v < c->nb_v; ++v)
+        for (int q = 0; q < 3; ++q) used[c->ver[v][q]] = 1;
+      int n = 0;
+      int32_t ids[ORC_MAX_P];
+      for (int p = 4; p < c->nb_p; ++p) {
+        if (!used[p]) continue;
+        ids[n++] = c->id2[p][0] == i ? c->id2[p][1] : c->id2[p][0];
+      }
+      for (int a = 1; a < n; ++a) {
+        int32_t x = ids[a];
+        int b = a - 1;
+        while (b >= 0 && ids[b] > x) {
+          ids[b + 1] = ids[b];
+          --b;
+        }
+        ids[b + 1] = x;
+      }
+      if (n > max_nbr) {
+        count[i] = -3;
+        ++bad;
+        continue;
+      }
+      for (int r = 0; r < n; ++r) row[r] = ids[r];
+      count[i] = n;
+    }
+    free(c);
+    free(kv);
+  }
+  return bad;
+}

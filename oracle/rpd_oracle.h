@@ -155,6 +155,20 @@ int orc_cell_polygons(int64_t n_cells, const orc_cell_header* cells,
                       int32_t* poly_site, int32_t* poly_adj_site, int64_t max_polys,
                       int64_t* counts);
 
+/* ---- power neighbours, the stand-in for libmat's regular-triangulation
+ * neighbour lists (CGAL, src/rpd3d_base/triangulation.cxx:62-144,
+ * :442-558): site j is a neighbour of site i when its float bisector plane
+ * is a face of i's power cell inside `region` (lo[3], hi[3]).  The cell is a
+ * tet enclosing the region clipped by the clipper above in exact-sign mode
+ * (pred_mode 2) with every other site in ascending key order, until the next
+ * key exceeds the cell's radius (vertices solved in double) by a margin
+ * covering the rounding of the float planes.  Rows of max_nbr ids,
+ * ascending, -1 padded; count[i] = neighbours, -1 for an empty cell (a
+ * hidden sphere), -2 for a cell beyond the clipper's capacities, -3 for
+ * more than max_nbr neighbours.  Returns the number of -2 / -3 sites. */
+int orc_power_neighbors(int n_site, const float* site4, const double* region, int max_nbr,
+                        int32_t* nbr, int32_t* count, int n_threads);
+
 /* ---- single predicates, exposed for filter tests */
 double orc_det4x4_ref(const float* p1, const float* p2, const float* p3,
                       const float* e);

@@ -22,7 +22,10 @@ def meshes():
 
 
 def single(cfg, **kw):
+    # the batch clips with the GPU lists as built (one pass, uncertified
+    # cells flagged): the single-mesh run the same way
     a = cfg["adj"]
+    kw.setdefault("exact_lists", False)
     with rpd.RPD(neighbor_source=rpd.NEIGH_KNN, knn_k=64, **kw) as r:
         r.set_mesh(cfg["vert3d"], cfg["tets"], a["v_adjs"], a["e_adj6"], a["f_adjs"], a["f_ids"])
         r.set_sites(cfg["sites"], cfg["flags"])

@@ -16,8 +16,9 @@ pytestmark = pytest.mark.gpu
 
 
 def run(cfg, adj, pred, certify=False):
+    # the reference's algorithm on the GPU's 64-entry lists (no longer lists)
     with rpd.RPD(predicate_mode=pred, neighbor_source=rpd.NEIGH_KNN, knn_k=64,
-                 certify=certify) as r:
+                 certify=certify, exact_lists=False) as r:
         r.set_mesh(cfg["vert3d"], cfg["tets"], adj["v_adjs"], adj["e_adj6"], adj["f_adjs"],
                    adj["f_ids"])
         r.set_sites(cfg["sites"], cfg["flags"])

@@ -13,8 +13,9 @@ pytestmark = pytest.mark.gpu
 
 
 def _engine(cfg, adj):
+    # one pass: the recomputed set below is derived from the 64-entry lists
     r = rpd.RPD(predicate_mode=rpd.PRED_FP32_FILTER, neighbor_source=rpd.NEIGH_KNN, knn_k=64,
-                certify=True, topology_hash=False)
+                certify=True, topology_hash=False, exact_lists=False)
     r.set_mesh(cfg["vert3d"], cfg["tets"], adj["v_adjs"], adj["e_adj6"], adj["f_adjs"], adj["f_ids"])
     return r
 
