@@ -183,15 +183,29 @@ def clip_algorithmic_bytes(cfg, n_pairs, k, topo_bytes):
     return mesh + sites + 8 * k * ns + 8 * n_pairs + 32 * n_pairs + topo_bytes
 
 
-def cpu_sample_run(cfg, adj, nbr, n_tets, seed=0, n_threads=None):
+# DRAM traffic of one clip launch per candidate pair: ncu
+# dram__bytes_read.sum + dram__bytes_write.sum of clip_cells_kernel on the
+# 206k-tet ellipsoid (the same workload family, scaled by the launch's pairs:
+# its traffic grows with them), and smsp__issue_active of the same capture;
+# the capture and its command are summarised in
+# profiles/clip_cells_kernel_ellipsoid_200k.md
+CLIP_DRAM_BYTES_PER_PAIR = 304.4
+CLIP_ISSUE_ACTIVE = 0.802
+
+
+def sample_tets(n_tet, n, seed):
+    rng = np.random.default_rng(seed)
+    return np.sort(rng.choice(n_tet, size=min(n, n_tet), replace=False))
+
+
+def cpu_sample_run(cfg, adj, nbr, n_tets, seed=0, n_threads=None, clip_nbr=None):
     """The oracle on n_tets random tets: the reference's candidate rule over
-    all sites (brute force, as the reference) + clipping with FP64
-    predicates.  Returns (cells, seconds, pairs)."""
+    all sites with the lists nbr (brute force, as the reference) + clipping
+    with FP64 predicates, with the lists clip_nbr (default nbr).  Returns
+    (cells, seconds, pairs, details)."""
     from oracle import oracle as O
 
-    rng = np.random.default_rng(seed)
-    sub = np.sort(rng.choice(cfg["tets"].shape[0], size=min(n_tets, cfg["tets"].shape[0]),
-                             replace=False))
+    sub = sample_tets(cfg["tets"].shape[0], n_tets, seed)
     tets = cfg["tets"][sub]
     mesh = dict(vert3d=cfg["vert3d"], tets=tets, v_adjs=adj["v_adjs"],
                 e_adj6=adj["e_adj6"][sub], f_adjs=adj["f_adjs"][sub], f_ids=adj["f_ids"][sub])
@@ -199,9 +213,110 @@ def cpu_sample_run(cfg, adj, nbr, n_tets, seed=0, n_threads=None):
     offs, ps = O.candidate_pairs(cfg["vert3d"].astype(np.float32), tets,
                                  cfg["sites"].astype(np.float32), cfg["flags"], nbr,
                                  n_threads=n_threads)
-    h, p, _ = O.clip_cells(mesh, cfg["sites"], nbr, offs, ps, pred_mode=0, n_threads=n_threads)
+    h, p, _ = O.clip_cells(mesh, cfg["sites"], nbr if clip_nbr is None else clip_nbr, offs, ps,
+                           pred_mode=0, n_threads=n_threads)
     dt = time.perf_counter() - t0
-    return int((h["status"] == 4).sum()), dt, int(offs[-1])
+    return int((h["status"] == 4).sum()), dt, int(offs[-1]), dict(sub=sub, offs=offs, ps=ps, h=h,
+                                                                  p=p)
+
+
+def parity_vs_oracle(cfg, adj, base_nbr, final_nbr, gpu_offs, gpu_ps, gpu_ph, gpu_hash, gpu_p,
+                     n_tets, seed=0):
+    """The fast path's cells on a sample of tets against the oracle's (the
+    reference's algorithm, FP64 predicates) with the same lists: the
+    candidate pairs by the reference rule on the base lists, and every cell
+    clipped with the list the GPU finally used for its site (its exact-lists
+    extension where it got one).  Pairs and statuses compared one for one,
+    emitted cells by their canonical topology (the certified path clips in
+    ascending key and records fewer dead planes), FP64 vertices (as sorted
+    rows) and volumes against the oracle's FP64 reconstruction.  Returns
+    (report, cells, seconds)."""
+    from oracle import oracle as O
+
+    c, dt, npairs, d = cpu_sample_run(cfg, adj, base_nbr, n_tets, seed=seed, clip_nbr=final_nbr)
+    sub, offs, ps, oh, op = d["sub"], d["offs"], d["ps"], d["h"], d["p"]
+    # the GPU's pairs of the sampled tets, in the same CSR order
+    idx = np.concatenate([np.arange(gpu_offs[t], gpu_offs[t + 1]) for t in sub]).astype(np.int64)
+    pairs_equal = bool(np.array_equal(np.diff(offs), np.diff(gpu_offs)[sub]) and
+                       np.array_equal(ps, gpu_ps[idx]))
+    rep = {"sample_tets": int(len(sub)), "pairs": int(npairs), "pairs_equal": pairs_equal}
+    if not pairs_equal:
+        return rep, c, dt
+    gh = gpu_ph[idx]
+    rep["status_differing"] = int((gh["status"] != oh["status"]).sum())
+    ok = (gh["status"] == 4) & (oh["status"] == 4)
+    ohash = O.topology_hashes(oh, op)
+    rep["cells_compared"] = int(ok.sum())
+    rep["cells_topology_differing"] = int((ohash[ok] != gpu_hash[idx][ok]).sum())
+    vmax = vsq = 0.0
+    vn = 0
+    wmax = wsq = 0.0
+    nw = 0
+    for j in np.flatnonzero(ok):
+        q = idx[j]
+        a = _xyz(gpu_p, gpu_ph, q)
+        b = _xyz(op, oh, j)
+        if a.shape != b.shape:
+            continue
+        a = a[np.lexsort(a.T[::-1])]
+        b = b[np.lexsort(b.T[::-1])]
+        dv = np.abs(a - b) / 1000.0  # relative to the coordinate scale (libmat's [0, 1000])
+        vmax = max(vmax, float(dv.max()))
+        vsq += float((dv * dv).sum())
+        vn += dv.size
+        rv = abs(gh["volume"][j] - oh["volume"][j]) / max(abs(oh["volume"][j]), 1e-30)
+        wmax = max(wmax, rv)
+        wsq += rv * rv
+        nw += 1
+    rep.update({"vertex_max_rel": vmax, "vertex_rms_rel": (vsq / max(vn, 1)) ** 0.5,
+                "volume_max_rel": wmax, "volume_rms_rel": (wsq / max(nw, 1)) ** 0.5})
+    return rep, c, dt
+
+
+def true_rpd_check(cfg, adj, rpd, fast_ph, fast_hash):
+    """The fast path's cells against the exact restricted power diagram: the
+    oracle's power neighbours of every site (the stand-in for libmat's
+    regular triangulation, exact signs) clipped by the engine's reference
+    path (user lists in site-id order, as libmat runs them; hidden spheres
+    unflagged, as libmat's is_rt_valid).  Cells compared by (tet, site) and
+    canonical topology."""
+    from oracle import oracle as O
+
+    t0 = time.perf_counter()
+    s4 = cfg["sites"].astype(np.float32)
+    v = cfg["vert3d"]
+    nbr, cnt = O.power_neighbors(s4, v.min(0), v.max(0), max_nbr=128)
+    pn_s = time.perf_counter() - t0
+    k = max(int(cnt.max()), 1)
+    flags = cfg["flags"].copy()
+    flags[cnt < 0] = 0
+    with rpd.RPD(predicate_mode=rpd.PRED_FP32_FILTER, neighbor_source=rpd.NEIGH_USER,
+                 topology_hash=True) as r:
+        r.set_mesh(cfg["vert3d"], cfg["tets"], adj["v_adjs"], adj["e_adj6"], adj["f_adjs"],
+                   adj["f_ids"])
+        r.set_sites(cfg["sites"], flags)
+        r.set_neighbors(np.ascontiguousarray(nbr[:, :k]))
+        r.compute()
+        ph = r.pair_headers()
+        hs = r.topology_hashes()
+
+    def keyed(h, hh):
+        ok = h["status"] == rpd.SUCCESS
+        key = (h["tet_id"][ok].astype(np.int64) << 32) | h["site_id"][ok].astype(np.int64)
+        o = np.argsort(key)
+        return key[o], hh[ok][o]
+
+    ka, ha = keyed(fast_ph, fast_hash)
+    kb, hb = keyed(ph, hs)
+    common, ia, ib = np.intersect1d(ka, kb, assume_unique=True, return_indices=True)
+    n_topo = int((ha[ia] != hb[ib]).sum())
+    return {"cells": int(len(ka)), "reference_cells": int(len(kb)),
+            "cells_missing": int(len(kb) - len(common)), "cells_extra": int(len(ka) - len(common)),
+            "cells_topology_differing": n_topo,
+            "true_rpd_differing": int(len(kb) - len(common) + len(ka) - len(common) + n_topo),
+            "hidden_sites": int((cnt == -1).sum()), "capacity_sites": int((cnt < -1).sum()),
+            "power_neighbours_mean": float(cnt[cnt >= 0].mean()),
+            "power_neighbours_s": round(pn_s, 2)}
 
 
 def run_reference(args):
@@ -225,7 +340,7 @@ def run_reference(args):
     cells = 0
     secs = 0.0
     for s in range(args.steps):
-        c, dt, _ = cpu_sample_run(cfg, adj, nbr, sample, seed=s)
+        c, dt, _, _ = cpu_sample_run(cfg, adj, nbr, sample, seed=s)
         cells += c
         secs += dt
     v = cells / secs
@@ -302,10 +417,10 @@ def run_ours(args):
                    adj["f_ids"])
         r.set_sites(cfg["sites"], cfg["flags"])
 
-    def engine(pred, certify):
+    def engine(pred, certify, k=None):
         r = rpd.RPD(device=local if world > 1 else 0, predicate_mode=pred,
-                    neighbor_source=rpd.NEIGH_KNN, knn_k=args.k, clip_order=rpd.ORDER_SITE_ID,
-                    certify=certify)
+                    neighbor_source=rpd.NEIGH_KNN, knn_k=k or args.k,
+                    clip_order=rpd.ORDER_SITE_ID, certify=certify)
         load(r)
         return r
 
@@ -351,6 +466,7 @@ def run_ours(args):
     fast_ph = fast.pair_headers()
     fast_hash = fast.topology_hashes()
     fast_h, fast_p = fast.cells()
+    final_lists = fast.site_lists_padded(ns)
     # ---- per-cell topology of the emitted cells (what libmat's consumers
     # rebuild on the host: active planes and edges, face cycles, Euler
     # numbers), on the device; reported beside the step, not inside it
@@ -384,7 +500,8 @@ def run_ours(args):
 
     # ---- plain FP64 path: whole list in site-id order, FP64 determinant on
     # every predicate
-    plain = engine(rpd.PRED_FP64, False)
+    # (the same base lists as the fast path: its tuned k)
+    plain = engine(rpd.PRED_FP64, False, k=fast.config().knn_k)
     plain_tuning = plain.autotune(repeats=1).as_dict() if not args.no_tune else None
     plain.configure(topology_hash=0)
     pms, pcells, pst = timed(plain, max(1, args.steps // 2), 1)
@@ -411,28 +528,33 @@ def run_ours(args):
     xyz_bytes = 24 * int(fast_ph["nb_v"][ok].astype(np.int64).sum())
     alg = clip_algorithmic_bytes(cfg, st.n_pairs, st.knn_k, st.payload_bytes - xyz_bytes)
     achieved = alg / (st.ms_clip_kernel / 1000.0) / 1e9
-    # DRAM bytes of one clip launch, from the ncu capture summarised in
-    # profiles/ (per pair on a smaller case of the same workload family,
-    # scaled by this launch's pairs: traffic grows with the pairs)
-    traffic = None
-    issue = None
-    tfile = os.path.join(ROOT, "profiles", "clip_cells_kernel_ellipsoid_200k.md")
-    if os.path.exists(tfile):
-        for ln in open(tfile):
-            if ln.startswith("traffic_bytes_per_pair:"):
-                traffic = float(ln.split(":")[1]) * st.n_pairs
-            if ln.startswith("issue_active_frac:"):
-                issue = float(ln.split(":")[1])
+    traffic = CLIP_DRAM_BYTES_PER_PAIR * st.n_pairs
 
-    cpu = None
+    cpu = parity = true_rpd = None
     if rank == 0 and not args.no_cpu:
         from oracle import oracle as O
 
-        nbr = fast.neighbor_lists(ns)
-        c, dt, _ = cpu_sample_run(cfg, adj, nbr, args.cpu_sample)
+        # the oracle (test infrastructure) as the checker, and as the CPU
+        # baseline on the same sample.  Base lists as built (site-id order,
+        # -1 padded) for the candidate rule; the sites without an extension
+        # clip with them in that order, the others with their extended list
+        # in ascending key (as the plain FP64 path does)
+        base = fast.neighbor_lists(ns)
+        kb = base.shape[1]
+        clip_lists = np.full((ns, max(kb, final_lists.shape[1])), -1, np.int32)
+        clip_lists[:, :final_lists.shape[1]] = final_lists
+        is_base = (final_lists >= 0).sum(axis=1) <= kb
+        clip_lists[is_base] = -1
+        clip_lists[is_base, :kb] = base[is_base]
+        offs_g, ps_g = fast.pairs(nt)
+        parity, c, dt = parity_vs_oracle(cfg, adj, base, clip_lists, offs_g, ps_g, fast_ph,
+                                         fast_hash, fast_p, args.cpu_sample)
         cpu = {"value": c / dt, "unit": UNIT, "cores": O.nthreads(), "kind": "port",
                "sample": "%d random tets: reference candidate rule over all sites + clipping "
-                         "(FP64 predicates), oracle on all host threads" % args.cpu_sample}
+                         "with FP64 predicates and the GPU's final lists, oracle on all host "
+                         "threads" % args.cpu_sample}
+        if not args.no_true_rpd:
+            true_rpd = true_rpd_check(cfg, adj, rpd, fast_ph, fast_hash)
     fast.close()
     if rank != 0:
         return
@@ -444,7 +566,10 @@ def run_ours(args):
         "config": {"workload": name, "n_tet": nt, "n_vert": nv, "n_site": ns, "knn_k": st.knn_k,
                    "n_pairs": st.n_pairs, "n_cells": st.n_cells,
                    "predicates": "fp32 filter, fp64 det when undecided",
-                   "neighbours": "gpu kNN, k smallest power-bisector distances",
+                   "neighbours": "gpu kNN base lists (the k smallest power-bisector "
+                                 "distances, k autotuned) + exact-lists rounds (sites of "
+                                 "uncertified cells get every site whose key lies below the "
+                                 "cells' radius bound; those cells are clipped again)",
                    "clipping": "ascending bisector distance, security-radius certificate",
                    "learned_k": used_learned, "l2": "flushed between steps (256 MB write)",
                    "parallelism": "replicas" if world > 1 else "single gpu",
@@ -459,13 +584,19 @@ def run_ours(args):
         "tuning": tuning,
         "learned": learned,
         "reclipped": int(st.n_reclipped),
-        # cells whose whole 64-entry list left the certificate unproven: sites
-        # beyond the list may cut them (the reference's triangulation lists
-        # have none); the topology comparison above uses the same lists
+        # emitted cells whose certificate failed after the rounds (sites
+        # beyond their list might cut them); 0 = every cell is exact
         "uncertified_cells": int(st.n_uncertified),
+        "exact_lists": {"extended_sites": int(st.n_extended_sites),
+                        "cells_reclipped": int(st.n_cert_reclipped),
+                        "rounds": int(st.n_extend_rounds), "longest": int(st.ext_longest),
+                        "ms": st.ms_extend, "ms_lists": st.ms_extend_lists},
+        "parity_vs_oracle": parity,
+        "true_rpd": true_rpd,
         "stage_ms": {"knn": st.ms_knn, "pairs": st.ms_pairs, "clip": st.ms_clip,
                      "clip_kernel": st.ms_clip_kernel, "epilogue": st.ms_epilogue,
-                     "predict": st.ms_predict, "compact": st.ms_compact},
+                     "exact_lists": st.ms_extend, "predict": st.ms_predict,
+                     "compact": st.ms_compact},
         "predicates": {"evaluated": st.n_predicates, "escalated_fp64": st.n_escalated,
                        "escalation_rate": st.n_escalated / max(st.n_predicates, 1)},
         "status_counts": {rpd.STATUS_NAMES[i]: int(st.status_counts[i]) for i in range(10)
@@ -478,8 +609,8 @@ def run_ours(args):
                      "peak_source": peak_src,
                      "algorithmic_bytes": alg,
                      # the bound that applies: instruction issue (ncu
-                     # smsp__issue_active of the same kernel, the profile above)
-                     "issue_active_frac": issue},
+                     # smsp__issue_active of the same kernel)
+                     "issue_active_frac": CLIP_ISSUE_ACTIVE},
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
     }
@@ -802,6 +933,8 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=20000)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner")
+    ap.add_argument("--no-true-rpd", action="store_true",
+                    help="skip the comparison with the power-neighbour lists")
     ap.add_argument("--no-learned", action="store_true", help="skip training the k-predictor")
     ap.add_argument("--force-learned", action="store_true",
                     help="time the learned lengths even if the autotuner prefers others")

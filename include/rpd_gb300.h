@@ -269,6 +269,10 @@ typedef struct rpd_tuning {
   float ms_clip_best;  /* clip stage of the chosen configuration */
   float ms_clip_first; /* clip stage of the first candidate (defaults) */
   int learned_k;       /* 1: the k-predictor's lengths won (rpd_config.learned_k set) */
+  int knn_k;           /* GPU-built lists with exact_lists: the base list
+                          length (64, 96 or 128) of the fastest whole
+                          compute -- the cells do not depend on it */
+  float ms_total_best; /* the whole compute with the chosen configuration */
 } rpd_tuning;
 rpd_status rpd_autotune(struct rpd_ctx* ctx, int repeats, rpd_tuning* result);
 
@@ -591,6 +595,17 @@ rpd_status rpd_copy_polygons_to_host(struct rpd_ctx* ctx, float* points, int64_t
  * copied to the host.  k_out receives k. */
 rpd_status rpd_copy_neighbors_to_host(struct rpd_ctx* ctx, int32_t* nbr,
                                       int64_t capacity, int* k_out);
+
+/* Every site's list as the last rpd_compute clipped its cells with, as a
+ * CSR on the host: the extended list of a site that the exact-lists rounds
+ * gave one (every site whose key lies below its cells' radius bound, in
+ * ascending key; or every site, in id order), else its base list in clip
+ * order (ascending key when certified, else as built), holes (-1) dropped.
+ * An extended list holds the base list, so the cells of such a site that
+ * the base list already certified are its cells too.  offsets: n_site + 1
+ * entries; with ids NULL only n_total (the entries) is returned. */
+rpd_status rpd_copy_site_lists_to_host(struct rpd_ctx* ctx, int64_t* offsets, int32_t* ids,
+                                       int64_t capacity, int64_t* n_total);
 
 /* The candidate pairs of the last rpd_compute as a per-tet CSR (host). */
 rpd_status rpd_copy_pairs_to_host(struct rpd_ctx* ctx, int32_t* tet_offsets,

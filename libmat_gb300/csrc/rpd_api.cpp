@@ -1088,6 +1088,37 @@ rpd_status rpd_autotune(rpd_ctx* c, int repeats, rpd_tuning* result) {
   } else {
     c->has_site_klen = false;
   }
+  // base list length of GPU-built exact lists: longer base lists cost the
+  // kNN and the pair rule more, and leave fewer cells to the longer-list
+  // rounds; the cells are the same, so the whole compute decides
+  float best_total = INFINITY;
+  if (c->cfg.neighbor_source == RPD_NEIGH_KNN && c->cfg.certify && c->cfg.exact_lists) {
+    const int k0 = c->cfg.knn_k;
+    const int ks[4] = {k0, 64, 96, 128};
+    int best_k = k0;
+    for (int i = 0; i < 4; ++i) {
+      if (i > 0 && ks[i] == k0) continue;
+      c->cfg.knn_k = ks[i];
+      std::vector<float> t;
+      for (int r = 0; r < repeats + 1; ++r) {
+        rpd_stats st;
+        rpd_status s = rpd_compute(c, &st);
+        if (s != RPD_OK) {
+          c->cfg.knn_k = k0;
+          return s;
+        }
+        if (r > 0) t.push_back(st.ms_total);
+      }
+      std::sort(t.begin(), t.end());
+      const float med = t[t.size() / 2];
+      ++tried;
+      if (med < best_total) {
+        best_total = med;
+        best_k = ks[i];
+      }
+    }
+    c->cfg.knn_k = best_k;
+  }
   c->has_result = false;
   if (result) {
     result->warps_per_block = best_c.warps;
@@ -1097,6 +1128,8 @@ rpd_status rpd_autotune(rpd_ctx* c, int repeats, rpd_tuning* result) {
     result->n_candidates = tried;
     result->ms_clip_best = best;
     result->ms_clip_first = first;
+    result->knn_k = c->cfg.knn_k;
+    result->ms_total_best = best_total;
   }
   return RPD_OK;
 }
@@ -1989,6 +2022,56 @@ rpd_status rpd_copy_neighbors_to_host(rpd_ctx* c, int32_t* nbr, int64_t capacity
   CK(cudaSetDevice(c->device), "cudaSetDevice");
   CK(cudaMemcpyAsync(nbr, c->nbr.ptr, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost, c->stream), "D2H");
   CK(cudaStreamSynchronize(c->stream), "sync");
+  return RPD_OK;
+}
+
+rpd_status rpd_copy_site_lists_to_host(rpd_ctx* c, int64_t* offsets, int32_t* ids,
+                                       int64_t capacity, int64_t* n_total) {
+  if (!c || !n_total) return RPD_ERR_INVALID_ARGUMENT;
+  if (!c->has_result) return fail(c, RPD_ERR_NOT_READY, "rpd_copy_site_lists_to_host: no compute yet");
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  cudaStream_t st = c->stream;
+  const int n_site = c->n_site, k = c->k;
+  // the base lists in clip order: certified clipping reads the key-ordered
+  // copy (GPU-built lists only)
+  const bool knn = c->cfg.neighbor_source == RPD_NEIGH_KNN;
+  const int32_t* base = (knn && c->cfg.certify) ? c->nbr_dist.ptr : c->nbr.ptr;
+  std::vector<int32_t> nb((size_t)n_site * k), row((size_t)n_site, -1);
+  CK(cudaMemcpyAsync(nb.data(), base, sizeof(int32_t) * nb.size(), cudaMemcpyDeviceToHost, st), "D2H");
+  std::vector<long long> eoff;
+  std::vector<int32_t> elen, enbr;
+  if (c->ext_valid && c->ext_rows > 0) {
+    eoff.resize((size_t)c->ext_rows);
+    elen.resize((size_t)c->ext_rows);
+    enbr.resize((size_t)c->ext_used);
+    CK(cudaMemcpyAsync(row.data(), c->site_row.ptr, sizeof(int32_t) * (size_t)n_site,
+                       cudaMemcpyDeviceToHost, st), "D2H");
+    CK(cudaMemcpyAsync(eoff.data(), c->ext_off.ptr, sizeof(long long) * eoff.size(),
+                       cudaMemcpyDeviceToHost, st), "D2H");
+    CK(cudaMemcpyAsync(elen.data(), c->ext_len.ptr, sizeof(int32_t) * elen.size(),
+                       cudaMemcpyDeviceToHost, st), "D2H");
+    CK(cudaMemcpyAsync(enbr.data(), c->ext_nbr.ptr, sizeof(int32_t) * enbr.size(),
+                       cudaMemcpyDeviceToHost, st), "D2H");
+  }
+  CK(cudaStreamSynchronize(st), "sync");
+  long long pos = 0;
+  for (int i = 0; i < n_site; ++i) {
+    if (offsets) offsets[i] = pos;
+    const int r = row[(size_t)i];
+    const int32_t* L = r >= 0 ? enbr.data() + eoff[(size_t)r] : nb.data() + (size_t)i * k;
+    const int n = r >= 0 ? elen[(size_t)r] : k;
+    for (int q = 0; q < n; ++q) {
+      const int32_t j = L[q];
+      if (j < 0 || j == i) continue;  // holes, and the seed in a complete row
+      if (ids) {
+        if (pos >= capacity) return fail(c, RPD_ERR_CAPACITY, "rpd_copy_site_lists_to_host: buffer too small");
+        ids[pos] = j;
+      }
+      ++pos;
+    }
+  }
+  if (offsets) offsets[n_site] = pos;
+  *n_total = pos;
   return RPD_OK;
 }
 

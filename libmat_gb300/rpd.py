@@ -47,6 +47,7 @@ EXPORTS = [
     "rpd_destroy", "rpd_last_error", "rpd_set_mesh", "rpd_set_sites", "rpd_set_neighbors",
     "rpd_compute", "rpd_get_cells", "rpd_copy_cells_to_host", "rpd_copy_neighbors_to_host",
     "rpd_copy_pairs_to_host", "rpd_copy_pair_headers_to_host", "rpd_build_mesh_adjacency",
+    "rpd_copy_site_lists_to_host",
     "rpd_host_alloc", "rpd_host_free", "rpd_compact_cells_noalloc", "rpd_set_site_k",
     "rpd_copy_topology_hashes_to_host", "rpd_autotune",
     "rpd_mlp_collect", "rpd_mlp_clear_samples", "rpd_mlp_train", "rpd_mlp_enable",
@@ -137,7 +138,8 @@ class Tuning(ctypes.Structure):
     _fields_ = [("warps_per_block", ctypes.c_int), ("clip_variant", ctypes.c_int),
                 ("k_bucket", ctypes.c_int), ("n_candidates", ctypes.c_int),
                 ("ms_clip_best", ctypes.c_float), ("ms_clip_first", ctypes.c_float),
-                ("learned_k", ctypes.c_int)]
+                ("learned_k", ctypes.c_int), ("knn_k", ctypes.c_int),
+                ("ms_total_best", ctypes.c_float)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -200,6 +202,8 @@ def load(path=LIB_PATH):
     L.rpd_copy_cells_to_host.argtypes = [vp, vp, i64, vp, i64, c.POINTER(i64), c.POINTER(i64)]
     L.rpd_copy_neighbors_to_host.restype = i32
     L.rpd_copy_neighbors_to_host.argtypes = [vp, vp, i64, c.POINTER(i32)]
+    L.rpd_copy_site_lists_to_host.restype = i32
+    L.rpd_copy_site_lists_to_host.argtypes = [vp, vp, vp, i64, c.POINTER(i64)]
     L.rpd_copy_pairs_to_host.restype = i32
     L.rpd_copy_pairs_to_host.argtypes = [vp, vp, vp, i64, c.POINTER(i64)]
     L.rpd_copy_pair_headers_to_host.restype = i32
@@ -745,6 +749,29 @@ class RPD:
         out = np.zeros((n_site, k), np.int32)
         kk = ctypes.c_int()
         self._check(self._L.rpd_copy_neighbors_to_host(self._h, _p(out), out.size, ctypes.byref(kk)))
+        return out
+
+    def site_lists(self, n_site):
+        """Every site's list as the last compute clipped its cells with (CSR:
+        offsets [n_site + 1] int64, ids)."""
+        n = ctypes.c_int64()
+        self._check(self._L.rpd_copy_site_lists_to_host(self._h, None, None, 0, ctypes.byref(n)))
+        offs = np.zeros(n_site + 1, np.int64)
+        ids = np.zeros(max(n.value, 1), np.int32)
+        self._check(self._L.rpd_copy_site_lists_to_host(self._h, _p(offs), _p(ids), ids.size,
+                                                        ctypes.byref(n)))
+        return offs, ids[:n.value]
+
+    def site_lists_padded(self, n_site):
+        """The same lists as an [n_site, longest] matrix, -1 padded (the
+        oracle's list layout)."""
+        offs, ids = self.site_lists(n_site)
+        lens = np.diff(offs)
+        k = max(int(lens.max()) if n_site else 1, 1)
+        out = np.full((n_site, k), -1, np.int32)
+        rows = np.repeat(np.arange(n_site), lens)
+        cols = np.arange(ids.size) - np.repeat(offs[:-1], lens)
+        out[rows, cols] = ids
         return out
 
     def pairs(self, n_tet):

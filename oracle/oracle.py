@@ -76,6 +76,8 @@ def lib():
         L.orc_topo_bytes.argtypes = [i32, i32, i32]
         L.orc_cell_topology.restype = i64
         L.orc_cell_topology.argtypes = [i64, vp, vp, vp, vp, i64]
+        L.orc_topology_hashes.restype = None
+        L.orc_topology_hashes.argtypes = [i64, vp, vp, vp]
         L.orc_power_neighbors.restype = i32
         L.orc_power_neighbors.argtypes = [i32, vp, vp, i32, vp, vp, i32]
         L.orc_cell_polygons.restype = i32
@@ -157,6 +159,15 @@ def knn(site4f, k, n_threads=None):
     keys = np.empty((n, k), np.float32)
     lib().orc_knn(n, _p(site4f), k, _p(nbr), _p(keys), n_threads or nthreads())
     return nbr, keys
+
+
+def topology_hashes(headers, payload):
+    """Canonical topology hash of every record (0 where not emitted)."""
+    headers = np.ascontiguousarray(headers)
+    payload = np.ascontiguousarray(payload, np.uint8)
+    out = np.zeros(len(headers), np.uint64)
+    lib().orc_topology_hashes(len(headers), _p(headers), _p(payload), _p(out))
+    return out
 
 
 def power_neighbors(site4f, lo, hi, max_nbr=96, n_threads=None):

@@ -1585,3 +1585,47 @@ int orc_power_neighbors(int n_site, const float* site4, const double* region, in
   }
   return bad;
 }
+
+/* ------------------------------------------------------------------ */
+/* canonical topology hash of emitted cells: the sum over vertices of  */
+/* a splitmix64 chain over the sorted face keys (id2) of the vertex's  */
+/* three planes and its #adj -- independent of plane and vertex order */
+/* ------------------------------------------------------------------ */
+static uint64_t orc_mix64(uint64_t z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+void orc_topology_hashes(int64_t n, const orc_cell_header* h, const uint8_t* payload,
+                         uint64_t* out) {
+  for (int64_t q = 0; q < n; ++q) {
+    out[q] = 0;
+    if (h[q].status != ORC_SUCCESS) continue;
+    const int nb_v = h[q].nb_v, nb_p = h[q].nb_p;
+    const uint8_t* rec = payload + h[q].offset;
+    const int32_t* id2 = (const int32_t*)(rec + 16 * (size_t)nb_p);
+    const uint8_t* ver = rec + 16 * (size_t)nb_p + al16(8 * (size_t)nb_p);
+    uint64_t sum = 0;
+    for (int v = 0; v < nb_v; ++v) {
+      uint64_t k[3];
+      for (int a = 0; a < 3; ++a) {
+        const int p = ver[4 * v + a];
+        k[a] = ((uint64_t)(uint32_t)id2[2 * p] << 32) | (uint32_t)id2[2 * p + 1];
+      }
+      for (int a = 1; a < 3; ++a)
+        for (int b = a; b > 0 && k[b - 1] > k[b]; --b) {
+          uint64_t t = k[b];
+          k[b] = k[b - 1];
+          k[b - 1] = t;
+        }
+      uint64_t hv = orc_mix64(k[0]);
+      hv = orc_mix64(hv ^ k[1]);
+      hv = orc_mix64(hv ^ k[2]);
+      hv = orc_mix64(hv ^ (uint64_t)ver[4 * v + 3]);
+      sum += hv;
+    }
+    out[q] = sum;
+  }
+}

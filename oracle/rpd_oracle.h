@@ -169,6 +169,14 @@ int orc_cell_polygons(int64_t n_cells, const orc_cell_header* cells,
 int orc_power_neighbors(int n_site, const float* site4, const double* region, int max_nbr,
                         int32_t* nbr, int32_t* count, int n_threads);
 
+/* ---- canonical topology hash of each record (0 for cells not emitted):
+ * the sum over vertices of splitmix64 (Steele et al. 2014) chained over the
+ * sorted face keys (id2 as int32 pairs) of the vertex's three planes and
+ * its #adj -- independent of the order of planes and vertices, so cells
+ * clipped in different orders compare by their active faces */
+void orc_topology_hashes(int64_t n, const orc_cell_header* h, const uint8_t* payload,
+                         uint64_t* out);
+
 /* ---- single predicates, exposed for filter tests */
 double orc_det4x4_ref(const float* p1, const float* p2, const float* p3,
                       const float* e);

@@ -131,3 +131,27 @@ def test_filter_is_sound_on_near_degenerate_planes():
             d = O.det4x4_ref(p[0], p[1], p[2], e)
             assert (d > 0) == (s > 0)
     assert decided > 1000
+
+
+def test_topology_hash_matches_the_python_definition():
+    """The oracle's canonical topology hash (used by the benchmark's parity
+    check) equals the definition in tests/helpers.py, which the engine's
+    hashes are tested against."""
+    from tests.helpers import topology_hash
+
+    cfg = W.config_small_cube(n=6, n_site=150, seed=3)
+    adj = O.mesh_adjacency(cfg["vert3d"].shape[0], cfg["tets"])
+    nbr, _ = O.knn(cfg["sites"].astype(np.float32), 32)
+    nbr = np.sort(nbr, axis=1)
+    offs, ps = O.candidate_pairs(cfg["vert3d"].astype(np.float32), cfg["tets"],
+                                 cfg["sites"].astype(np.float32), cfg["flags"], nbr)
+    mesh = dict(vert3d=cfg["vert3d"], tets=cfg["tets"],
+                **{k: adj[k] for k in ("v_adjs", "e_adj6", "f_adjs", "f_ids")})
+    h, p, _ = O.clip_cells(mesh, cfg["sites"], nbr, offs, ps)
+    hs = O.topology_hashes(h, p)
+    ok = np.flatnonzero(h["status"] == O.SUCCESS)
+    assert len(ok) > 1000
+    for q in ok[::7]:
+        assert int(hs[q]) == topology_hash(p, h["offset"][q], h["nb_v"][q], h["nb_p"][q],
+                                           h["nb_e"][q])
+    assert np.all(hs[h["status"] != O.SUCCESS] == 0)
