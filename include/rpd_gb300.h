@@ -625,9 +625,13 @@ rpd_status rpd_copy_pairs_to_host(struct rpd_ctx* ctx, int32_t* tet_offsets,
  * array inside the library (reserved on each GPU that loads it until exit),
  * so n_pairs is limited to 2^25; larger inputs return RPD_ERR_CAPACITY.  The
  * first call on a device looks up that array's address (call it once before
- * any stream capture).  Calls share the array: calls that overlap on the GPU
- * race and must be serialised by the caller.  Asynchronous on `stream`
- * (a cudaStream_t, NULL = default stream). */
+ * any stream capture); the address is kept per device ordinal, so calls must
+ * run in the device's primary context and not after a cudaDeviceReset in
+ * the same process.  Calls share the array: calls that overlap on the GPU
+ * race and must be serialised by the caller.  A launch that fails returns
+ * RPD_ERR_CUDA; an error the caller left pending is neither reported nor
+ * cleared.  Asynchronous on `stream` (a cudaStream_t, NULL = default
+ * stream). */
 rpd_status rpd_compact_cells_noalloc(const rpd_cell_header* pair_headers, int64_t n_pairs,
                                      rpd_cell_header* cells_out, int64_t* n_cells_out,
                                      uint64_t* status_counts, void* stream);

@@ -784,7 +784,7 @@ static rpd_status finish_compute(rpd_ctx* c, bool knn, bool learned, rpd_stats* 
                    c->cells.ptr, c->n_out.ptr, c->scratch.ptr + 8, st, c->scratch.ptr + 31),
      "compact");
   CK(cudaEventRecord(c->ev[kEvEnd], st), "event");
-  unsigned long long host_scratch[32];
+  unsigned long long host_scratch[40];
   long long n_cells = 0;
   CK(cudaMemcpyAsync(host_scratch, c->scratch.ptr, sizeof(host_scratch), cudaMemcpyDeviceToHost, st), "D2H");
   CK(cudaMemcpyAsync(&n_cells, c->n_out.ptr, sizeof(n_cells), cudaMemcpyDeviceToHost, st), "D2H");

@@ -18,7 +18,15 @@
 //
 // Set-up: the first call on a device (the device current at the call) looks
 // up the array's device address with cudaGetSymbolAddress; make that first
-// call before any stream capture.  The address is cached per device.
+// call before any stream capture.  The address is cached per device
+// ordinal: calls must run in the device's primary context (the one the CUDA
+// runtime uses), and the cached address is not looked up again after
+// cudaDeviceReset, so do not call this entry point after a reset in the
+// same process.
+//
+// Errors: the launches' own configuration errors are returned as
+// RPD_ERR_CUDA; an error the caller left pending before the call is neither
+// reported nor cleared.
 //
 // Every call reuses the same array, which keeps the last call's contents; a
 // call overwrites every count it reads.  Two calls whose kernels overlap on
@@ -31,6 +39,7 @@
 #include <mutex>
 
 #include "rpd_common.cuh"
+#include "rpd_scan.cuh"
 
 namespace {
 
@@ -44,34 +53,7 @@ static __device__ __align__(256) int32_t g_compact_scratch[kScratchInts];
 std::mutex g_setup_mutex;
 int32_t* g_scratch_ptr[kMaxDevices] = {};
 
-__device__ __forceinline__ int warp_scan_incl(int v, int lane) {
-  for (int o = 1; o < 32; o <<= 1) {
-    int t = __shfl_up_sync(0xffffffffu, v, o);
-    if (lane >= o) v += t;
-  }
-  return v;
-}
-
-// exclusive block scan of one flag per thread; total in *total
-__device__ int block_scan_flags(int v, int* total) {
-  __shared__ int wsum[32];
-  __shared__ int wtot;
-  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  int incl = warp_scan_incl(v, lane);
-  if (lane == 31) wsum[wid] = incl;
-  __syncthreads();
-  if (wid == 0) {
-    int x = lane < (int)(blockDim.x >> 5) ? wsum[lane] : 0;
-    int xi = warp_scan_incl(x, lane);
-    wsum[lane] = xi - x;
-    if (lane == 31) wtot = xi;
-  }
-  __syncthreads();
-  int r = incl - v + wsum[wid];
-  if (total) *total = wtot;
-  __syncthreads();
-  return r;
-}
+static_assert(kBlock == 1024, "the block scans below assume 32 full warps per block");
 
 __global__ void na_zero(unsigned long long* hist) {
   if (hist && threadIdx.x < 11) hist[threadIdx.x] = 0ull;
@@ -91,7 +73,7 @@ __global__ void na_count(const rpd_cell_header* h, long long n, int32_t* counts,
     atomicAdd(sh + b, 1u);
   }
   int tot;
-  block_scan_flags(f, &tot);
+  rpd::block_excl_scan<int>(f, &tot);
   if (threadIdx.x == 0) counts[blockIdx.x] = tot;
   if (hist && threadIdx.x < 11 && sh[threadIdx.x])
     atomicAdd(hist + threadIdx.x, (unsigned long long)sh[threadIdx.x]);
@@ -104,7 +86,7 @@ __global__ void na_scan_counts(int32_t* counts, int nb) {
     int i = base + threadIdx.x;
     int v = i < nb ? counts[i] : 0;
     int tot;
-    int ex = block_scan_flags(v, &tot);
+    int ex = rpd::block_excl_scan<int>(v, &tot);
     if (i < nb) counts[i] = ex + carry;
     carry += tot;
   }
@@ -115,7 +97,7 @@ __global__ void na_scatter(const rpd_cell_header* h, long long n, const int32_t*
                            rpd_cell_header* out, int64_t* n_out) {
   long long q = (long long)blockIdx.x * kBlock + threadIdx.x;
   int f = (q < n && h[q].status == rpd::kSuccess) ? 1 : 0;
-  int pos = block_scan_flags(f, nullptr) + offs[blockIdx.x];
+  int pos = rpd::block_excl_scan<int>(f, nullptr) + offs[blockIdx.x];
   if (f) out[pos] = h[q];
   if (blockIdx.x == 0 && threadIdx.x == 0) *n_out = offs[nb];
 }
@@ -149,11 +131,25 @@ extern "C" rpd_status rpd_compact_cells_noalloc(const rpd_cell_header* pair_head
   }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   unsigned long long* hist = reinterpret_cast<unsigned long long*>(status_counts);
-  const int nb = (int)((n_pairs + kBlock - 1) / kBlock);
-  na_zero<<<1, 32, 0, st>>>(hist);
-  if (nb > 0) na_count<<<nb, kBlock, 0, st>>>(pair_headers, n_pairs, scratch, hist);
-  na_scan_counts<<<1, kBlock, 0, st>>>(scratch, nb);
-  na_scatter<<<nb > 0 ? nb : 1, kBlock, 0, st>>>(pair_headers, n_pairs, scratch, nb, cells_out,
-                                                 n_cells_out);
-  return cudaGetLastError() == cudaSuccess ? RPD_OK : RPD_ERR_CUDA;
+  int nb = (int)((n_pairs + kBlock - 1) / kBlock);
+  // each launch's own status (cudaLaunchKernel returns it): a launch that
+  // fails is reported without consulting the thread's last-error state
+  void* a_zero[] = {&hist};
+  if (cudaLaunchKernel((const void*)na_zero, dim3(1), dim3(32), a_zero, 0, st) != cudaSuccess)
+    return RPD_ERR_CUDA;
+  if (nb > 0) {
+    void* a_count[] = {&pair_headers, &n_pairs, &scratch, &hist};
+    if (cudaLaunchKernel((const void*)na_count, dim3(nb), dim3(kBlock), a_count, 0, st) !=
+        cudaSuccess)
+      return RPD_ERR_CUDA;
+  }
+  void* a_scan[] = {&scratch, &nb};
+  if (cudaLaunchKernel((const void*)na_scan_counts, dim3(1), dim3(kBlock), a_scan, 0, st) !=
+      cudaSuccess)
+    return RPD_ERR_CUDA;
+  void* a_scatter[] = {&pair_headers, &n_pairs, &scratch, &nb, &cells_out, &n_cells_out};
+  if (cudaLaunchKernel((const void*)na_scatter, dim3(nb > 0 ? nb : 1), dim3(kBlock), a_scatter,
+                       0, st) != cudaSuccess)
+    return RPD_ERR_CUDA;
+  return RPD_OK;
 }

@@ -26,6 +26,7 @@
 
 #include "rpd_common.cuh"
 #include "rpd_kernels.cuh"
+#include "rpd_scan.cuh"
 
 namespace rpd {
 
@@ -44,42 +45,11 @@ constexpr int kScanBlock = 1024;
 
 size_t scan_temp_ints(long long n) { return (size_t)((n + kScanBlock - 1) / kScanBlock) + 1; }
 
-__device__ __forceinline__ int warp_incl_scan(int v, int lane) {
-  for (int o = 1; o < 32; o <<= 1) {
-    int t = __shfl_up_sync(0xffffffffu, v, o);
-    if (lane >= o) v += t;
-  }
-  return v;
-}
-
-// block-wide exclusive scan of one value per thread; returns the exclusive
-// prefix and writes the block total to *total
-__device__ int block_excl_scan(int v, int* total) {
-  __shared__ int wsum[32];
-  __shared__ int wtot;
-  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  int incl = warp_incl_scan(v, lane);
-  if (lane == 31) wsum[wid] = incl;
-  __syncthreads();
-  if (wid == 0) {
-    int nw = blockDim.x >> 5;
-    int x = lane < nw ? wsum[lane] : 0;
-    int xi = warp_incl_scan(x, lane);
-    if (lane < nw) wsum[lane] = xi - x;
-    if (lane == 31) wtot = xi;
-  }
-  __syncthreads();
-  int res = incl - v + wsum[wid];
-  if (total) *total = wtot;
-  __syncthreads();
-  return res;
-}
-
 __global__ void scan_reduce_kernel(const int32_t* in, long long n, int32_t* block_sums) {
   long long i = (long long)blockIdx.x * kScanBlock + threadIdx.x;
   int v = i < n ? in[i] : 0;
   int tot;
-  block_excl_scan(v, &tot);
+  block_excl_scan<int>(v, &tot);
   if (threadIdx.x == 0) block_sums[blockIdx.x] = tot;
 }
 
@@ -89,7 +59,7 @@ __global__ void scan_blocksums_kernel(int32_t* sums, int nb) {
     int i = base + threadIdx.x;
     int v = i < nb ? sums[i] : 0;
     int tot;
-    int ex = block_excl_scan(v, &tot);
+    int ex = block_excl_scan<int>(v, &tot);
     if (i < nb) sums[i] = ex + carry;
     carry += tot;
   }
@@ -100,7 +70,7 @@ __global__ void scan_apply_kernel(const int32_t* in, long long n, const int32_t*
                                   int nb, int32_t* out) {
   long long i = (long long)blockIdx.x * kScanBlock + threadIdx.x;
   int v = i < n ? in[i] : 0;
-  int ex = block_excl_scan(v, nullptr);
+  int ex = block_excl_scan<int>(v, nullptr);
   if (i < n) out[i] = ex + block_sums[blockIdx.x];
   if (blockIdx.x == 0 && threadIdx.x == 0) out[n] = block_sums[nb];
 }
@@ -277,7 +247,7 @@ __device__ void for_items(int n_cells_iter, CellAt cell_at, const int32_t* cell_
       b = cell_start[cell];
       cnt = cell_start[cell + 1] - b;
     }
-    int incl = warp_incl_scan(cnt, lane);
+    int incl = warp_incl_scan<int>(cnt, lane);
     int total = __shfl_sync(0xffffffffu, incl, 31);
     int excl = incl - cnt;
     for (int ib = 0; ib < total; ib += 32) {

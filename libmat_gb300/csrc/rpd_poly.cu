@@ -35,6 +35,7 @@
 #include "rpd_common.cuh"
 #include "rpd_hostfloat.cuh"
 #include "rpd_kernels.cuh"
+#include "rpd_scan.cuh"
 
 namespace rpd {
 
@@ -42,40 +43,10 @@ namespace {
 
 constexpr int kScan64 = 1024;
 
-__device__ __forceinline__ long long warp_incl_scan64(long long v, int lane) {
-  for (int o = 1; o < 32; o <<= 1) {
-    const long long t = __shfl_up_sync(0xffffffffu, v, o);
-    if (lane >= o) v += t;
-  }
-  return v;
-}
-
-// block-wide exclusive scan; *total receives the block's sum
-__device__ long long block_excl_scan64(long long v, long long* total) {
-  __shared__ long long wsum[32];
-  __shared__ long long wtot;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const long long incl = warp_incl_scan64(v, lane);
-  if (lane == 31) wsum[wid] = incl;
-  __syncthreads();
-  if (wid == 0) {
-    const int nw = blockDim.x >> 5;
-    const long long x = lane < nw ? wsum[lane] : 0;
-    const long long xi = warp_incl_scan64(x, lane);
-    if (lane < nw) wsum[lane] = xi - x;
-    if (lane == 31) wtot = xi;
-  }
-  __syncthreads();
-  const long long res = incl - v + wsum[wid];
-  if (total) *total = wtot;
-  __syncthreads();
-  return res;
-}
-
 __global__ void scan64_reduce_kernel(const int32_t* in, long long n, long long* sums) {
   const long long i = (long long)blockIdx.x * kScan64 + threadIdx.x;
   long long tot;
-  block_excl_scan64(i < n ? in[i] : 0, &tot);
+  block_excl_scan<long long>(i < n ? in[i] : 0, &tot);
   if (threadIdx.x == 0) sums[blockIdx.x] = tot;
 }
 
@@ -84,7 +55,7 @@ __global__ void scan64_blocksums_kernel(long long* sums, int nb) {
   for (int base = 0; base < nb; base += kScan64) {
     const int i = base + threadIdx.x;
     long long tot;
-    const long long ex = block_excl_scan64(i < nb ? sums[i] : 0, &tot);
+    const long long ex = block_excl_scan<long long>(i < nb ? sums[i] : 0, &tot);
     if (i < nb) sums[i] = ex + carry;
     carry += tot;
   }
@@ -94,7 +65,7 @@ __global__ void scan64_blocksums_kernel(long long* sums, int nb) {
 __global__ void scan64_apply_kernel(const int32_t* in, long long n, const long long* sums, int nb,
                                     long long* out) {
   const long long i = (long long)blockIdx.x * kScan64 + threadIdx.x;
-  const long long ex = block_excl_scan64(i < n ? in[i] : 0, nullptr);
+  const long long ex = block_excl_scan<long long>(i < n ? in[i] : 0, nullptr);
   if (i < n) out[i] = ex + sums[blockIdx.x];
   if (blockIdx.x == 0 && threadIdx.x == 0) out[n] = sums[nb];
 }

@@ -106,8 +106,34 @@ def build_ref_bgeo(force=False):
     return out
 
 
+def build_ref_dist2mat(force=False):
+    """Returns the path of _ref/librefd2m.so -- the reference's own dist2mat
+    distance functions (src/dist2mat/dist2mat.cu) behind
+    ref_dist2mat_driver.cu, compiled by nvcc for the host -- or None without
+    reference sources (or without nvcc)."""
+    src_dir = os.path.join(REF_ROOT, "src", "dist2mat")
+    src = os.path.join(src_dir, "dist2mat.cu")
+    if not os.path.exists(src):
+        return None
+    import shutil
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        return None
+    outdir = os.path.join(HERE, "_ref")
+    os.makedirs(outdir, exist_ok=True)
+    out = os.path.join(outdir, "librefd2m.so")
+    drv = os.path.join(HERE, "ref_dist2mat_driver.cu")
+    if force or _stale(out, [drv, src]):
+        _run([nvcc, "-O2", "-shared", "-std=c++17", "-w",
+              "-gencode", "arch=compute_103a,code=sm_103a",
+              "-Xcompiler", "-fPIC,-ffp-contract=off",
+              "-I" + os.path.join(REF_ROOT, "include"), "-I" + src_dir, drv, "-o", out])
+    return out
+
+
 if __name__ == "__main__":
     print(build_oracle(force="-f" in sys.argv))
     print(build_ref(force="-f" in sys.argv))
     print(build_ref_topo(force="-f" in sys.argv))
     print(build_ref_bgeo(force="-f" in sys.argv))
+    print(build_ref_dist2mat(force="-f" in sys.argv))

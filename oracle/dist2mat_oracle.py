@@ -33,6 +33,13 @@ def sphere_d(p, s):
     return np.sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]) - s[3]
 
 
+def _sq(x):
+    """The reference's powf(x, 2.f): the square rounded once (glibc's powf
+    and the device's restatement agree on it; numpy's float32 ** 2 does not
+    always)."""
+    return x * x
+
+
 def _dot(a, b):
     return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]
 
@@ -93,16 +100,16 @@ def slab_d(p, m1, m2, m3):
         t2 = f((np.float64(B * D) - 2.0 * np.float64(A) * np.float64(E)) / np.float64(den))
     elif R1 != 0.0 and R2 == 0.0:
         H2, K2 = -B / (2.0 * C), -E / (2.0 * C)
-        W1 = (2.0 * A + B * H2) ** 2 - 4.0 * R1 * R1 * (A + B * H2 + C * H2 * H2)
+        W1 = _sq(2.0 * A + B * H2) - 4.0 * R1 * R1 * (A + B * H2 + C * H2 * H2)
         W2 = 2.0 * (2.0 * A + B * H2) * (B * K2 + D) - 4.0 * R1 * R1 * (B * K2 + 2.0 * C * H2 * K2 + D + E * H2)
-        W3 = (B * K2 + D) ** 2 - 4.0 * R1 * R1 * (C * K2 * K2 + E * K2 + F)
+        W3 = _sq(B * K2 + D) - 4.0 * R1 * R1 * (C * K2 * K2 + E * K2 + F)
         r = _roots(W1, W2, W3)
         t1, t2 = _pick(p, m1, m2, m3, (r[0], H2 * r[0] + K2), (r[1], H2 * r[1] + K2))
     elif R1 == 0.0 and R2 != 0.0:
         H1, K1 = -B / (2.0 * A), -D / (2.0 * A)
-        W1 = (2.0 * C + B * H1) ** 2 - 4.0 * R2 * R2 * (C + B * H1 + A * H1 * H1)
+        W1 = _sq(2.0 * C + B * H1) - 4.0 * R2 * R2 * (C + B * H1 + A * H1 * H1)
         W2 = 2.0 * (2.0 * C + B * H1) * (B * K1 + E) - 4.0 * R2 * R2 * (B * K1 + 2.0 * A * H1 * K1 + E + D * H1)
-        W3 = (B * K1 + E) ** 2 - 4.0 * R2 * R2 * (A * K1 * K1 + D * K1 + F)
+        W3 = _sq(B * K1 + E) - 4.0 * R2 * R2 * (A * K1 * K1 + D * K1 + F)
         r = _roots(W1, W2, W3)
         t1, t2 = _pick(p, m1, m2, m3, (H1 * r[0] + K1, r[0]), (H1 * r[1] + K1, r[1]))
     else:
@@ -111,21 +118,21 @@ def slab_d(p, m1, m2, m3):
             t2 = -L3 / L2
             W1 = 4.0 * A * A - 4.0 * R1 * R1 * A
             W2 = 4.0 * A * (B * t2 + D) - 4.0 * R1 * R1 * (B * t2 + D)
-            W3 = (B * t2 + D) ** 2 - (C * t2 * t2 + E * t2 + F)
+            W3 = _sq(B * t2 + D) - (C * t2 * t2 + E * t2 + F)
             r = _roots(W1, W2, W3)
             t1, _ = _pick(p, m1, m2, m3, (r[0], t2), (r[1], t2))
         elif L1 != 0.0 and L2 == 0.0:
             t1 = L3 / L1
             W1 = 4.0 * C * C - 4.0 * R2 * R2 * C
             W2 = 4.0 * C * (B * t1 + E) - 4.0 * R2 * R2 * (B * t1 + E)
-            W3 = (B * t1 + E) ** 2 - (A * t1 * t1 + D * t1 + F)
+            W3 = _sq(B * t1 + E) - (A * t1 * t1 + D * t1 + F)
             r = _roots(W1, W2, W3)
             _, t2 = _pick(p, m1, m2, m3, (t1, r[0]), (t1, r[1]))
         else:
             H3, K3 = L2 / L1, L3 / L1
-            W1 = (2.0 * C + B * H3) ** 2 - 4.0 * R2 * R2 * (A * H3 * H3 + B * H3 + C)
+            W1 = _sq(2.0 * C + B * H3) - 4.0 * R2 * R2 * (A * H3 * H3 + B * H3 + C)
             W2 = 2.0 * (2.0 * C + B * H3) * (B * K3 + E) - 4.0 * R2 * R2 * (2.0 * A * H3 * K3 + B * K3 + D * H3 + E)
-            W3 = (B * K3 + E) ** 2 - 4.0 * R2 * R2 * (A * K3 * K3 + D * K3 + F)
+            W3 = _sq(B * K3 + E) - 4.0 * R2 * R2 * (A * K3 * K3 + D * K3 + F)
             r = _roots(W1, W2, W3)
             t1, t2 = _pick(p, m1, m2, m3, (H3 * r[0] + K3, r[0]), (H3 * r[1] + K3, r[1]))
     if t1 + t2 < 1.0 and 0.0 <= t1 <= 1.0 and 0.0 <= t2 <= 1.0:

@@ -104,6 +104,36 @@ def ref_lib():
     return _ref
 
 
+_refd2m = None
+
+
+def ref_dist2mat(spheres, samples, offsets, counts, prims):
+    """The reference's own dist2mat distance functions (src/dist2mat/
+    dist2mat.cu:5-193, compiled for the CPU) with the kernel's selection
+    rule: (dist float32, closest int32) per sample, or None where the
+    reference sources (or nvcc) are absent."""
+    global _refd2m
+    if _refd2m is None:
+        path = _build.build_ref_dist2mat()
+        if path is None:
+            return None
+        L = ctypes.CDLL(path)
+        vp, i32 = ctypes.c_void_p, ctypes.c_int
+        L.refd2m_eval.restype = None
+        L.refd2m_eval.argtypes = [i32, vp, vp, vp, vp, vp, vp, vp]
+        _refd2m = L
+    smp = np.ascontiguousarray(samples, np.float32).reshape(-1, 3)
+    sph = np.ascontiguousarray(spheres, np.float32).reshape(-1, 4)
+    pr = np.ascontiguousarray(prims, np.int32).reshape(-1, 3)
+    off = np.ascontiguousarray(offsets, np.uint32)
+    cnt = np.ascontiguousarray(counts, np.uint32)
+    dist = np.empty(smp.shape[0], np.float32)
+    closest = np.empty(smp.shape[0], np.int32)
+    _refd2m.refd2m_eval(smp.shape[0], _p(smp), _p(sph), _p(pr), _p(off), _p(cnt), _p(dist),
+                        _p(closest))
+    return dist, closest
+
+
 def ref_topo_lib():
     """The reference's own ConvexCellHost topology on the CPU, or None."""
     global _reftopo

@@ -1448,11 +1448,116 @@ static void pn_compact(cell_t* c) {
   }
 }
 
+/* one region tet: 4 float vertices, positively oriented (the clipper's
+ * face planes point inwards) */
+typedef struct {
+  float v[12];
+} pn_tet;
+
+static void pn_orient(pn_tet* t) {
+  /* the centroid must lie on the inner side of the clipper's first face
+   * plane; otherwise two vertices swap */
+  const int32_t tv[4] = {0, 1, 2, 3};
+  const int32_t vad[4] = {1, 1, 1, 1}, fa[4] = {1, 1, 1, 1}, fi[4] = {-1, -1, -1, -1};
+  const uint8_t e6[6] = {1, 1, 1, 1, 1, 1};
+  cell_t c;
+  cell_init(&c, t->v, tv, vad, e6, fa, fi);
+  double cen[3] = {0, 0, 0};
+  for (int v = 0; v < 4; ++v)
+    for (int k = 0; k < 3; ++k) cen[k] += 0.25 * t->v[3 * v + k];
+  if ((double)c.pl[0][0] * cen[0] + (double)c.pl[0][1] * cen[1] + (double)c.pl[0][2] * cen[2] +
+          (double)c.pl[0][3] < 0.0) {
+    for (int k = 0; k < 3; ++k) {
+      const float x = t->v[k];
+      t->v[k] = t->v[3 + k];
+      t->v[3 + k] = x;
+    }
+  }
+}
+
+/* the 8 tets of the midpoint subdivision: 4 at the corners, 4 around the
+ * octahedron's diagonal m02-m13 */
+static void pn_split(const pn_tet* t, pn_tet out[8]) {
+  float m[4][4][3];
+  for (int a = 0; a < 4; ++a)
+    for (int b = 0; b < 4; ++b)
+      for (int k = 0; k < 3; ++k)
+        m[a][b][k] = (float)(0.5 * ((double)t->v[3 * a + k] + (double)t->v[3 * b + k]));
+  static const int ix[8][4][2] = {
+      {{0, 0}, {0, 1}, {0, 2}, {0, 3}}, {{0, 1}, {1, 1}, {1, 2}, {1, 3}},
+      {{0, 2}, {1, 2}, {2, 2}, {2, 3}}, {{0, 3}, {1, 3}, {2, 3}, {3, 3}},
+      {{0, 2}, {1, 3}, {0, 1}, {0, 3}}, {{0, 2}, {1, 3}, {0, 3}, {2, 3}},
+      {{0, 2}, {1, 3}, {2, 3}, {1, 2}}, {{0, 2}, {1, 3}, {1, 2}, {0, 1}}};
+  for (int q = 0; q < 8; ++q) {
+    for (int v = 0; v < 4; ++v)
+      for (int k = 0; k < 3; ++k) out[q].v[3 * v + k] = m[ix[q][v][0]][ix[q][v][1]][k];
+    pn_orient(&out[q]);
+  }
+}
+
+static int pn_meets_box(const pn_tet* t, const double* box) {
+  for (int k = 0; k < 3; ++k) {
+    double lo = t->v[k], hi = t->v[k];
+    for (int v = 1; v < 4; ++v) {
+      lo = fmin(lo, t->v[3 * v + k]);
+      hi = fmax(hi, t->v[3 * v + k]);
+    }
+    if (hi < box[k] || lo > box[3 + k]) return 0;
+  }
+  return 1;
+}
+
+/* clips region tet t by the sites in ascending key (kv[0..m), sorted on
+ * demand in chunks) until the next key exceeds the cell's radius; marks the
+ * sites of the final cell's bisector faces in `hit`.  Returns the cell's
+ * status. */
+static int pn_clip_region(cell_t* c, const pn_tet* t, const float* site4, int i, pn_kv* kv,
+                          int64_t m, int64_t* sorted, double margin, uint8_t* hit) {
+  const int32_t tv[4] = {0, 1, 2, 3};
+  const int32_t vad[4] = {1, 1, 1, 1}, fa[4] = {1, 1, 1, 1}, fi[4] = {-1, -1, -1, -1};
+  const uint8_t e6[6] = {1, 1, 1, 1, 1, 1};
+  c->pred_mode = 2;
+  c->n_pred = c->n_esc = c->n_unc = c->n_flip = 0;
+  c->seed_id = i;
+  memcpy(c->seed, site4 + 4 * (int64_t)i, sizeof(float) * 4);
+  cell_init(c, t->v, tv, vad, e6, fa, fi);
+  double R = pn_radius(c);
+  int64_t pos = 0;
+  while (pos < m && c->status == ORC_SUCCESS) {
+    if (pos == *sorted) {
+      /* next chunk of the smallest keys */
+      int64_t want = *sorted == 0 ? 256 : (m - *sorted);
+      if (want > m - *sorted) want = m - *sorted;
+      pn_select(kv + *sorted, m - *sorted, want);
+      qsort(kv + *sorted, (size_t)want, sizeof(pn_kv), pn_cmp);
+      *sorted += want;
+    }
+    if (kv[pos].key * (1.0 - 1e-9) - margin > R) break;
+    if (c->nb_p > ORC_MAX_P - 8 || c->nb_e > ORC_MAX_E - 48) pn_compact(c);
+    const int nb_p0 = c->nb_p;
+    clip_by_site(c, site4, kv[pos].id);
+    if (c->status == ORC_SUCCESS && c->nb_p > nb_p0) R = pn_radius(c);
+    ++pos;
+  }
+  if (c->status != ORC_SUCCESS) return c->status;
+  uint8_t used[ORC_MAX_P];
+  memset(used, 0, sizeof(used));
+  for (int v = 0; v < c->nb_v; ++v)
+    for (int q = 0; q < 3; ++q) used[c->ver[v][q]] = 1;
+  for (int p = 4; p < c->nb_p; ++p)
+    if (used[p]) hit[c->id2[p][0] == i ? c->id2[p][1] : c->id2[p][0]] = 1;
+  return ORC_SUCCESS;
+}
+
 int orc_power_neighbors(int n_site, const float* site4, const double* region, int max_nbr,
                         int32_t* nbr, int32_t* count, int n_threads) {
   /* a regular tet around the region's box: vertices c + s (+-1, +-1, +-1)
    * with an even number of minus signs; its inradius s / sqrt(3) exceeds
-   * the box's half diagonal */
+   * the box's half diagonal.  A cell beyond the clipper's capacities (a
+   * large power cell with many faces) is computed again on the 8 tets of
+   * the region's midpoint subdivision (those that meet the box), recursively:
+   * a face of the cell inside the box lies in one of them, so the union of
+   * their neighbours is the cell's. */
   double c0[3], h2 = 0.0, L = 0.0;
   for (int a = 0; a < 3; ++a) {
     c0[a] = 0.5 * (region[a] + region[3 + a]);
@@ -1461,26 +1566,14 @@ int orc_power_neighbors(int n_site, const float* site4, const double* region, in
   }
   const double s = sqrt(h2) * sqrt(3.0) * 1.05 + 1.0;
   static const double sg[4][3] = {{1, 1, 1}, {1, -1, -1}, {-1, 1, -1}, {-1, -1, 1}};
-  float tv3[12];
+  pn_tet root;
   for (int v = 0; v < 4; ++v)
-    for (int a = 0; a < 3; ++a) tv3[3 * v + a] = (float)(c0[a] + s * sg[v][a]);
-  int32_t tv[4] = {0, 1, 2, 3};
-  const int32_t vad[4] = {1, 1, 1, 1}, fa[4] = {1, 1, 1, 1}, fi[4] = {-1, -1, -1, -1};
-  const uint8_t e6[6] = {1, 1, 1, 1, 1, 1};
-  {
-    /* inward normals need a positively oriented tet: the centre must lie on
-     * the inner side of face 0 */
-    cell_t t;
-    cell_init(&t, tv3, tv, vad, e6, fa, fi);
-    if ((double)t.pl[0][0] * c0[0] + (double)t.pl[0][1] * c0[1] + (double)t.pl[0][2] * c0[2] +
-            (double)t.pl[0][3] < 0.0) {
-      tv[0] = 1;
-      tv[1] = 0;
-    }
-  }
+    for (int a = 0; a < 3; ++a) root.v[3 * v + a] = (float)(c0[a] + s * sg[v][a]);
+  pn_orient(&root);
   /* rounding of the float bisector planes against the exact keys, and of
    * the radius: a site whose key exceeds R + margin cannot cut the cell */
   const double margin = 1e-5 * (L + 2.0 * sqrt(h2)) + 1e-12;
+  enum { kMaxDepth = 7, kStack = 8 * kMaxDepth + 1 };
   int bad = 0;
 #ifdef _OPENMP
   if (n_threads > 0) omp_set_num_threads(n_threads);
@@ -1488,7 +1581,10 @@ int orc_power_neighbors(int n_site, const float* site4, const double* region, in
 #endif
   {
     pn_kv* kv = (pn_kv*)malloc(sizeof(pn_kv) * (size_t)(n_site > 0 ? n_site : 1));
+    uint8_t* hit = (uint8_t*)calloc((size_t)(n_site > 0 ? n_site : 1), 1);
     cell_t* c = (cell_t*)malloc(sizeof(cell_t));
+    pn_tet stack[kStack];
+    int depth_of[kStack];
 #ifdef _OPENMP
 #pragma omp for schedule(dynamic, 16)
 #endif
@@ -1515,72 +1611,70 @@ int orc_power_neighbors(int n_site, const float* site4, const double* region, in
         count[i] = -1;
         continue;
       }
-      c->pred_mode = 2;
-      c->n_pred = c->n_esc = c->n_unc = c->n_flip = 0;
-      c->seed_id = i;
-      memcpy(c->seed, si, sizeof(float) * 4);
-      cell_init(c, tv3, tv, vad, e6, fa, fi);
-      double R = pn_radius(c);
-      int64_t sorted = 0, pos = 0;
-      int certified = 0;
-      while (pos < m && c->status == ORC_SUCCESS) {
-        if (pos == sorted) {
-          /* next chunk of the smallest keys */
-          int64_t want = sorted == 0 ? 256 : (m - sorted);
-          if (want > m - sorted) want = m - sorted;
-          pn_select(kv + sorted, m - sorted, want);
-          qsort(kv + sorted, (size_t)want, sizeof(pn_kv), pn_cmp);
-          sorted += want;
+      int64_t sorted = 0;
+      int nonempty = 0, failed = 0, top = 0;
+      stack[top] = root;
+      depth_of[top++] = 0;
+      while (top > 0 && !failed) {
+        const pn_tet t = stack[--top];
+        const int depth = depth_of[top];
+        const int st = pn_clip_region(c, &t, site4, i, kv, m, &sorted, margin, hit);
+        if (st == ORC_SUCCESS) {
+          nonempty = 1;
+        } else if (st != ORC_NO_INTERSECTION) {
+          if (depth >= kMaxDepth) {
+            failed = 1;
+            break;
+          }
+          pn_tet sub[8];
+          pn_split(&t, sub);
+          for (int q = 0; q < 8; ++q) {
+            if (!pn_meets_box(&sub[q], region)) continue;
+            stack[top] = sub[q];
+            depth_of[top++] = depth + 1;
+          }
         }
-        if (kv[pos].key * (1.0 - 1e-9) - margin > R) {
-          certified = 1;
-          break;
-        }
-        if (c->nb_p > ORC_MAX_P - 8 || c->nb_e > ORC_MAX_E - 48) pn_compact(c);
-        int nb_p0 = c->nb_p;
-        clip_by_site(c, site4, kv[pos].id);
-        if (c->status == ORC_SUCCESS && c->nb_p > nb_p0) R = pn_radius(c);
-        ++pos;
       }
-      (void)certified;
-      if (c->status == ORC_NO_INTERSECTION) {
+      /* the marked sites (all among the clipped, kv[0..sorted)), and the
+       * marks cleared */
+      int n = 0, over = 0;
+      for (int64_t q = 0; q < sorted; ++q) {
+        const int j = kv[q].id;
+        if (!hit[j]) continue;
+        hit[j] = 0;
+        if (n < max_nbr) row[n] = j;
+        else over = 1;
+        ++n;
+      }
+      if (failed) {
+        count[i] = -2;
+        ++bad;
+        for (int r = 0; r < max_nbr; ++r) row[r] = -1;
+        continue;
+      }
+      if (over) {
+        count[i] = -3;
+        ++bad;
+        for (int r = 0; r < max_nbr; ++r) row[r] = -1;
+        continue;
+      }
+      if (!nonempty) {
         count[i] = -1;
         continue;
       }
-      if (c->status != ORC_SUCCESS) {
-        count[i] = -2;
-        ++bad;
-        continue;
-      }
-      /* the sites of the bisector planes (4..) that carry a vertex */
-      uint8_t used[ORC_MAX_P];
-      memset(used, 0, sizeof(used));
-      for (int v = 0; v < c->nb_v; ++v)
-        for (int q = 0; q < 3; ++q) used[c->ver[v][q]] = 1;
-      int n = 0;
-      int32_t ids[ORC_MAX_P];
-      for (int p = 4; p < c->nb_p; ++p) {
-        if (!used[p]) continue;
-        ids[n++] = c->id2[p][0] == i ? c->id2[p][1] : c->id2[p][0];
-      }
       for (int a = 1; a < n; ++a) {
-        int32_t x = ids[a];
+        int32_t x = row[a];
         int b = a - 1;
-        while (b >= 0 && ids[b] > x) {
-          ids[b + 1] = ids[b];
+        while (b >= 0 && row[b] > x) {
+          row[b + 1] = row[b];
           --b;
         }
-        ids[b + 1] = x;
+        row[b + 1] = x;
       }
-      if (n > max_nbr) {
-        count[i] = -3;
-        ++bad;
-        continue;
-      }
-      for (int r = 0; r < n; ++r) row[r] = ids[r];
       count[i] = n;
     }
     free(c);
+    free(hit);
     free(kv);
   }
   return bad;

@@ -170,3 +170,32 @@ def surface_mesh(vert, tets, f_adjs, f_ids):
     pairs = [(f, int(g)) for f in range(nb) for g in adj[f]
              if g > f and abs(float(nrm[f] @ nrm[g])) < 0.99]
     return adj, np.array(pairs, np.int32).reshape(-1, 2)
+
+
+def dist2mat_workload(seed, n_sph=300, n_smp=400, max_prims=80, radius_levels=0):
+    """dist2mat inputs: random medial spheres in the unit cube, samples near
+    them, per sample a list of spheres, cones and slabs over nearby spheres
+    (no sphere of a primitive inside another)."""
+    rng = np.random.default_rng(seed)
+    c = rng.uniform(0, 1, (n_sph, 3))
+    r = rng.uniform(0.01, 0.05, n_sph)
+    if radius_levels:  # few distinct radii: the slab's and cone's equal-radius branches
+        r = np.round(r * radius_levels / 0.05) * (0.05 / radius_levels)
+    sph = np.c_[c, r].astype(np.float32)
+    smp = (c[rng.integers(0, n_sph, n_smp)] + rng.normal(0, 0.05, (n_smp, 3))).astype(np.float32)
+    offs, cnts, prims = [], [], []
+    for s in range(n_smp):
+        near = np.argsort(np.linalg.norm(c - smp[s], axis=1))[:12]
+        n = int(rng.integers(0, max_prims + 1)) if s % 17 else 0
+        offs.append(len(prims))
+        cnts.append(n)
+        for _ in range(n):
+            kind = rng.integers(0, 3)
+            while True:
+                a, b, cc = rng.choice(near, 3, replace=False)
+                ok = all(abs(r[u] - r[v]) < 0.9 * np.linalg.norm(c[u] - c[v])
+                         for u, v in ((a, b), (a, cc), (b, cc)))
+                if ok:
+                    break
+            prims.append([-1, -1, a] if kind == 0 else ([-1, a, b] if kind == 1 else [a, b, cc]))
+    return sph, smp, np.array(offs, np.uint32), np.array(cnts, np.uint32), np.array(prims, np.int32)

@@ -7,35 +7,9 @@ import pytest
 
 from libmat_gb300 import rpd
 from oracle import dist2mat_oracle as D
+from tests.helpers import dist2mat_workload as workload
 
 pytestmark = pytest.mark.gpu
-
-
-def workload(seed, n_sph=300, n_smp=400, max_prims=80):
-    """Random medial spheres in the unit cube, samples near them, per sample
-    a list of spheres, cones and slabs over nearby spheres (no sphere of a
-    primitive inside another)."""
-    rng = np.random.default_rng(seed)
-    c = rng.uniform(0, 1, (n_sph, 3))
-    r = rng.uniform(0.01, 0.05, n_sph)
-    sph = np.c_[c, r].astype(np.float32)
-    smp = (c[rng.integers(0, n_sph, n_smp)] + rng.normal(0, 0.05, (n_smp, 3))).astype(np.float32)
-    offs, cnts, prims = [], [], []
-    for s in range(n_smp):
-        near = np.argsort(np.linalg.norm(c - smp[s], axis=1))[:12]
-        n = int(rng.integers(0, max_prims + 1)) if s % 17 else 0
-        offs.append(len(prims))
-        cnts.append(n)
-        for _ in range(n):
-            kind = rng.integers(0, 3)
-            while True:
-                a, b, cc = rng.choice(near, 3, replace=False)
-                ok = all(abs(r[u] - r[v]) < 0.9 * np.linalg.norm(c[u] - c[v])
-                         for u, v in ((a, b), (a, cc), (b, cc)))
-                if ok:
-                    break
-            prims.append([-1, -1, a] if kind == 0 else ([-1, a, b] if kind == 1 else [a, b, cc]))
-    return sph, smp, np.array(offs, np.uint32), np.array(cnts, np.uint32), np.array(prims, np.int32)
 
 
 @pytest.mark.parametrize("seed", [0, 1])
@@ -48,12 +22,11 @@ def test_dist2mat_matches_oracle(seed):
     empty = cnts == 0
     assert np.all(dist[empty] == 1e16) and np.all(closest[empty] == -1)
     ne = ~empty
-    # the same float32 expressions, one rounding per operation: bit for bit
-    # on nearly every sample (a few slabs that cancel differ in the last
-    # bits), and the same primitive
+    # the same float32 expressions, one rounding per operation (the oracle
+    # pinned to the reference's own functions): bit for bit, and the same
+    # primitive
     f32 = fd.astype(np.float32)
-    assert np.mean(dist[ne] == f32[ne]) > 0.99
-    assert np.all(np.abs(dist[ne] - f32[ne]) <= 2e-5 * np.maximum(np.abs(f32[ne]), 1e-2))
+    assert np.array_equal(dist[ne], f32[ne])
     assert np.array_equal(closest[ne], fi[ne])
     # against float64: within float error except where the float closed form
     # cancels (ill-conditioned slabs; the reference's float kernel shares
@@ -109,3 +82,20 @@ def test_device_pointers_match_host():
                                vp(dist), vp(cl), 1)
         assert st == 0
     assert np.array_equal(dist.cpu().numpy(), dist_h) and np.array_equal(cl.cpu().numpy(), cl_h)
+
+
+def test_dist2mat_equals_reference_golden_vectors():
+    """The device against the reference's own distance functions (golden
+    vectors made by the reference compiled for the CPU,
+    tests/golden/make_golden_dist2mat.py): bit for bit."""
+    import os
+
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                             "dist2mat_ref.npz"))
+    for name in sorted({k.split("_")[0] for k in g.files}):
+        c = {k[len(name) + 1:]: g[k] for k in g.files if k.startswith(name + "_")}
+        with rpd.RPD() as r:
+            dist, closest = r.dist2mat(c["spheres"], c["samples"], c["offsets"], c["counts"],
+                                       c["prims"])
+        assert np.array_equal(dist, c["dist"]), name
+        assert np.array_equal(closest, c["closest"]), name

@@ -54,6 +54,28 @@ def test_noalloc_compaction_matches_rpd_compute():
             got = out[: n * 32].cpu().numpy().view(rpd.HEADER_DTYPE)
             assert got.tobytes() == want.tobytes(), call
             assert np.array_equal(hist.cpu().numpy()[:10], want_status), call
+            assert int(hist[10].item()) == 0, call  # no payload-full cells, as rpd_compute
+        # without the status histogram: the same compacted records
+        out.fill_(0xAB)
+        torch.cuda.synchronize()
+        s = L.rpd_compact_cells_noalloc(ctypes.c_void_p(view.pair_headers), n_pairs,
+                                        ctypes.c_void_p(out.data_ptr()),
+                                        ctypes.c_void_p(n_out.data_ptr()), None,
+                                        ctypes.c_void_p(stream))
+        assert s == 0
+        torch.cuda.synchronize()
+        assert int(n_out.item()) == len(want)
+        assert out[: len(want) * 32].cpu().numpy().tobytes() == want.tobytes()
+        # no pairs: no cells, an all-zero histogram (the array still holds the
+        # previous call's counts)
+        n_out.fill_(-1)
+        hist.fill_(7)
+        s = L.rpd_compact_cells_noalloc(None, 0, None, ctypes.c_void_p(n_out.data_ptr()),
+                                        ctypes.c_void_p(hist.data_ptr()), ctypes.c_void_p(stream))
+        assert s == 0
+        torch.cuda.synchronize()
+        assert int(n_out.item()) == 0
+        assert not hist.cpu().numpy().any()
         # beyond the fixed array: rejected before any launch
         s = L.rpd_compact_cells_noalloc(ctypes.c_void_p(view.pair_headers), (1 << 25) + 1,
                                         ctypes.c_void_p(out.data_ptr()),
