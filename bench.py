@@ -185,12 +185,12 @@ def clip_algorithmic_bytes(cfg, n_pairs, k, topo_bytes):
 
 # DRAM traffic of one clip launch per candidate pair: ncu
 # dram__bytes_read.sum + dram__bytes_write.sum of clip_cells_kernel on the
-# 206k-tet ellipsoid (the same workload family, scaled by the launch's pairs:
+# 200k-tet ellipsoid (the same workload family, scaled by the launch's pairs:
 # its traffic grows with them), and smsp__issue_active of the same capture;
 # the capture and its command are summarised in
 # profiles/clip_cells_kernel_ellipsoid_200k.md
-CLIP_DRAM_BYTES_PER_PAIR = 304.4
-CLIP_ISSUE_ACTIVE = 0.802
+CLIP_DRAM_BYTES_PER_PAIR = 308.0
+CLIP_ISSUE_ACTIVE = 0.783
 
 
 def sample_tets(n_tet, n, seed):
