@@ -14,13 +14,29 @@
   (src/IO/IO_CUDA/io_utils.cpp) behind ref_bgeo_driver.cpp, through
   ref_io_shim/ (CUDA's vector structs, an empty json header), same
   condition.
+* ``_ref/librefd2m.so`` -- the reference's own dist2mat distance functions
+  (src/dist2mat/dist2mat.cu) behind ref_dist2mat_driver.cu, same condition.
+
+The reference sources are found through $RPD_REFERENCE_ROOT or, without it,
+as a checkout named ``reference`` beside this repository.
 """
 import os
 import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = os.environ.get("RPD_REFERENCE_ROOT", "/root/reference")
+
+
+def _reference_root():
+    """The libmat source checkout: $RPD_REFERENCE_ROOT, else a checkout named
+    ``reference`` beside this repository; "" (every _ref build skips) when
+    neither holds libmat's sources."""
+    env = os.environ.get("RPD_REFERENCE_ROOT")
+    cand = env if env else os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
+    return cand if os.path.isfile(os.path.join(cand, "src", "rpd3d", "convex_cell.cu")) else ""
+
+
+REF_ROOT = _reference_root()
 
 
 def _run(cmd):
@@ -48,6 +64,8 @@ def build_oracle(force=False):
 
 def build_ref(force=False):
     """Returns the path of _ref/libref.so, or None without reference sources."""
+    if not REF_ROOT:
+        return None
     kernel = os.path.join(REF_ROOT, "src", "rpd3d", "convex_cell.cu")
     if not os.path.exists(kernel):
         return None
@@ -71,6 +89,8 @@ def build_ref_topo(force=False):
     """Returns the path of _ref/libreftopo.so -- the reference's own
     ConvexCellHost topology (src/rpd3d_base/voronoi_defs.cxx) behind
     ref_topo_driver.cpp -- or None without reference sources."""
+    if not REF_ROOT:
+        return None
     defs = os.path.join(REF_ROOT, "src", "rpd3d_base", "voronoi_defs.cxx")
     if not os.path.exists(defs):
         return None
@@ -91,6 +111,8 @@ def build_ref_bgeo(force=False):
     """Returns the path of _ref/librefbgeo.so -- the reference's own Houdini
     geometry writer behind ref_bgeo_driver.cpp -- or None without reference
     sources."""
+    if not REF_ROOT:
+        return None
     io_dir = os.path.join(REF_ROOT, "src", "IO", "IO_CUDA")
     src = os.path.join(io_dir, "io_utils.cpp")
     if not os.path.exists(src):
@@ -111,6 +133,8 @@ def build_ref_dist2mat(force=False):
     distance functions (src/dist2mat/dist2mat.cu) behind
     ref_dist2mat_driver.cu, compiled by nvcc for the host -- or None without
     reference sources (or without nvcc)."""
+    if not REF_ROOT:
+        return None
     src_dir = os.path.join(REF_ROOT, "src", "dist2mat")
     src = os.path.join(src_dir, "dist2mat.cu")
     if not os.path.exists(src):
