@@ -14,6 +14,10 @@
   (src/IO/IO_CUDA/io_utils.cpp) behind ref_bgeo_driver.cpp, through
   ref_io_shim/ (CUDA's vector structs, an empty json header), same
   condition.
+* ``_ref/librefpc.so`` -- the reference's own power-cell construction
+  (src/rpd3d_base/rpd_update.cxx:1-521, fed to the compiler on its standard
+  input) behind ref_powercell_driver.cpp, through ref_pc_shim/ (PowerCell,
+  a surface mesh from arrays), same condition.
 * ``_ref/librefd2m.so`` -- the reference's own dist2mat distance functions
   (src/dist2mat/dist2mat.cu) behind ref_dist2mat_driver.cu, same condition.
 
@@ -107,6 +111,51 @@ def build_ref_topo(force=False):
     return out
 
 
+# rpd_update.cxx up to the end of update_pc_edge_cc_info: get_all_voro_info,
+# its helpers, the surface groups and the component updates; the rest of the
+# file needs the sphere model and geogram
+_PC_LAST_LINE = 521
+
+
+def build_ref_powercell(force=False):
+    """Returns the path of _ref/librefpc.so -- the reference's own power-cell
+    construction (src/rpd3d_base/rpd_update.cxx:1-521, read into the
+    compiler's standard input, never copied) behind ref_powercell_driver.cpp
+    with ref_pc_shim/ -- or None without reference sources or when those
+    lines do not end where update_pc_edge_cc_info does."""
+    if not REF_ROOT:
+        return None
+    base = os.path.join(REF_ROOT, "src", "rpd3d_base")
+    upd = os.path.join(base, "rpd_update.cxx")
+    defs = os.path.join(base, "voronoi_defs.cxx")
+    if not (os.path.exists(upd) and os.path.exists(defs)):
+        return None
+    outdir = os.path.join(HERE, "_ref")
+    os.makedirs(outdir, exist_ok=True)
+    out = os.path.join(outdir, "librefpc.so")
+    drv = os.path.join(HERE, "ref_powercell_driver.cpp")
+    shim = os.path.join(HERE, "ref_pc_shim")
+    deps = [drv, upd, defs, os.path.join(HERE, "rpd_oracle.h"),
+            os.path.join(shim, "medial_sphere.h"), os.path.join(shim, "input_types.h")]
+    if force or _stale(out, deps):
+        with open(upd) as f:
+            lines = f.readlines()
+        head = "".join(lines[:_PC_LAST_LINE])
+        tail = "".join(lines[_PC_LAST_LINE:_PC_LAST_LINE + 3])
+        if ("void update_pc_edge_cc_info(PowerCell& pcell)" not in head
+                or "update_sphere_type_based_on_pcells" not in tail
+                or not lines[_PC_LAST_LINE - 1].startswith("}")):
+            return None
+        cmd = ["g++", "-O2", "-fPIC", "-shared", "-std=c++17", "-DNDEBUG",
+               "-ffp-contract=off", "-w", "-pthread", "-I" + shim,
+               "-I" + os.path.join(REF_ROOT, "include"), "-I" + base,
+               drv, defs, "-x", "c++", "-", "-o", out]
+        r = subprocess.run(cmd, input=head, capture_output=True, text=True, cwd=outdir)
+        if r.returncode != 0:
+            raise RuntimeError("build failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
+    return out
+
+
 def build_ref_bgeo(force=False):
     """Returns the path of _ref/librefbgeo.so -- the reference's own Houdini
     geometry writer behind ref_bgeo_driver.cpp -- or None without reference
@@ -159,5 +208,6 @@ if __name__ == "__main__":
     print(build_oracle(force="-f" in sys.argv))
     print(build_ref(force="-f" in sys.argv))
     print(build_ref_topo(force="-f" in sys.argv))
+    print(build_ref_powercell(force="-f" in sys.argv))
     print(build_ref_bgeo(force="-f" in sys.argv))
     print(build_ref_dist2mat(force="-f" in sys.argv))

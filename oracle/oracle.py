@@ -375,6 +375,114 @@ def ref_cell_topology(cells, payload, n_threads=None):
     return th[:n], out[:used]
 
 
+_refpc = None
+
+# the arrays of ref_pc_get, in its order: (name, dtype, columns)
+REF_PC_ARRAYS = [("site_cells", np.int32, 1), ("nbr_cell", np.int32, 1), ("nbr", np.int32, 1),
+                 ("tfid_cell", np.int32, 1), ("tfid", np.int32, 1), ("facet_keys", np.int64, 1),
+                 ("facet_cells", np.int32, 1), ("facet_cc", np.int32, 1), ("cell_cc", np.int32, 1),
+                 ("edges", np.int32, 7), ("edge_cc", np.int32, 1), ("vertex_cell", np.int32, 1),
+                 ("vertex_lvid", np.int32, 1), ("vertex_ids", np.int32, 3),
+                 ("vertex_pos", np.float32, 3), ("vertex_sfid", np.int32, 1),
+                 ("surface_cell", np.int32, 1), ("surface_fid", np.int32, 1),
+                 ("surface_pos", np.float32, 3), ("sfg", np.int32, 4), ("se_covered", np.int32, 5),
+                 ("ce_covered", np.int32, 5), ("se_line_end", np.int32, 4),
+                 ("se_line_end_pos", np.float32, 3)]
+
+
+def ref_power_cells(cells, payload, n_site, max_sf_fid, feature_edges=None, surface=None):
+    """libmat's own get_all_voro_info and the per-sphere component updates
+    (src/rpd3d_base/rpd_update.cxx:1-521 compiled for the CPU,
+    ref_powercell_driver.cpp) on the emitted cells of `cells`, as the arrays
+    of powercell_oracle.power_cells (same arguments), plus "n_failed"
+    (spheres whose construction threw) and "n_mismatch" (maps that disagree
+    with each other); None without the reference sources."""
+    global _refpc
+    if _refpc is None:
+        path = _build.build_ref_powercell()
+        if path is None:
+            return None
+        L = ctypes.CDLL(path)
+        vp, i32, i64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64
+        L.ref_pc_run.restype = vp
+        L.ref_pc_run.argtypes = [i64, vp, vp, i32, i32, i64, vp, i32, vp, i64, vp]
+        L.ref_pc_get.restype = i64
+        L.ref_pc_get.argtypes = [vp, i32, vp, i64]
+        L.ref_pc_free.restype = None
+        L.ref_pc_free.argtypes = [vp]
+        _refpc = L
+    L = _refpc
+    h = np.ascontiguousarray(cells)
+    payload = np.ascontiguousarray(payload, np.uint8)
+    fe = np.ascontiguousarray(np.zeros((0, 6)) if feature_edges is None else feature_edges,
+                              np.int32).reshape(-1, 6)
+    if surface is not None:
+        adj = np.ascontiguousarray(surface[0], np.int32).reshape(-1, 3)
+        nc = np.ascontiguousarray(surface[1], np.int32).reshape(-1, 2)
+    else:
+        adj, nc = None, np.zeros((0, 2), np.int32)
+    handle = L.ref_pc_run(h.shape[0], _p(h), _p(payload), int(n_site), int(max_sf_fid),
+                          fe.shape[0], _p(fe), 0 if adj is None else adj.shape[0],
+                          None if adj is None else _p(adj), nc.shape[0], _p(nc))
+    try:
+        raw = {}
+        for i, (name, dt, cols) in enumerate(REF_PC_ARRAYS):
+            n = L.ref_pc_get(handle, i, None, 0)
+            a = np.zeros(max(n, 1), dt)
+            L.ref_pc_get(handle, i, _p(a), a.size)
+            raw[name] = a[:n].reshape(-1, cols) if cols > 1 else a[:n]
+        n_failed = int(L.ref_pc_get(handle, 24, None, 0))
+        n_mismatch = int(L.ref_pc_get(handle, 25, None, 0))
+    finally:
+        L.ref_pc_free(handle)
+    n = int((h["status"] == SUCCESS).sum())
+    site = h[h["status"] == SUCCESS]["site_id"].astype(np.int64)
+
+    def csr(rows, vals, count, dtype):
+        rows = np.asarray(rows, np.int64)
+        off = np.searchsorted(rows, np.arange(count + 1)).astype(np.int64)
+        return off, np.asarray(vals, dtype)
+
+    out = {}
+    out["site_cell_off"] = np.searchsorted(site[raw["site_cells"]] if n else np.zeros(0, np.int64),
+                                           np.arange(n_site + 1)).astype(np.int64)
+    out["site_cells"] = raw["site_cells"].astype(np.uint32)
+    out["cell_nbr_off"], out["cell_nbrs"] = csr(raw["nbr_cell"], raw["nbr"], n, np.int32)
+    out["cell_tfid_off"], out["cell_tfids"] = csr(raw["tfid_cell"], raw["tfid"], n, np.int32)
+    out["facet_keys"] = raw["facet_keys"].astype(np.uint64)
+    out["facet_cells"] = raw["facet_cells"].astype(np.uint32)
+    out["cell_cc"] = raw["cell_cc"]
+    out["facet_cc"] = raw["facet_cc"]
+    out["edge_cc"] = raw["edge_cc"]
+    out["site_facet_off"] = np.searchsorted(raw["facet_keys"] >> 32,
+                                            np.arange(n_site + 1)).astype(np.int64)
+    out["edges"] = raw["edges"].reshape(-1, 7)
+    out["site_edge_off"] = np.searchsorted(out["edges"][:, 0], np.arange(n_site + 1)).astype(np.int64)
+    for k in ("vertex_cell", "vertex_lvid", "vertex_sfid"):
+        out[k] = raw[k]
+    out["vertex_ids"] = raw["vertex_ids"].reshape(-1, 3)
+    out["vertex_pos"] = raw["vertex_pos"].reshape(-1, 3)
+    out["cell_vertex_off"] = np.searchsorted(raw["vertex_cell"], np.arange(n + 1)).astype(np.int64)
+    out["surface_cell"] = raw["surface_cell"]
+    out["surface_fid"] = raw["surface_fid"]
+    out["surface_pos"] = raw["surface_pos"].reshape(-1, 3)
+    out["cell_surface_off"] = np.searchsorted(raw["surface_cell"], np.arange(n + 1)).astype(np.int64)
+    sfg = raw["sfg"].reshape(-1, 4)
+    out["site_sfg_off"] = np.searchsorted(sfg[:, 0], np.arange(n_site + 1)).astype(np.int64)
+    out["sfg_group"], out["sfg_fid"], out["sfg_record"] = sfg[:, 1], sfg[:, 2], sfg[:, 3]
+    for name in ("se_covered", "ce_covered"):
+        rows = raw[name].reshape(-1, 5)
+        out["cell_%s_off" % name] = np.searchsorted(rows[:, 0], np.arange(n + 1)).astype(np.int64)
+        out[name] = rows
+    out["se_line_end"] = raw["se_line_end"].reshape(-1, 4)
+    out["se_line_end_pos"] = raw["se_line_end_pos"].reshape(-1, 3)
+    out["cell_se_line_end_off"] = np.searchsorted(out["se_line_end"][:, 0],
+                                                  np.arange(n + 1)).astype(np.int64)
+    out["n_failed"] = n_failed
+    out["n_mismatch"] = n_mismatch
+    return out
+
+
 def topo_bytes(nb_v, nb_p, nb_e):
     return int(lib().orc_topo_bytes(int(nb_v), int(nb_p), int(nb_e)))
 

@@ -126,3 +126,33 @@ def test_learned_requires_predictor():
             r.compute()
         r.mlp_enable(False)
         r.compute()
+
+
+def test_repass_counts_with_and_without_the_network(trained):
+    """Both re-passes, with the network and without it, on one unseen mesh
+    with exact lists: the network's misses (cells whose predicted length did
+    not certify, clipped again with the whole list) are its only extra
+    re-pass; the cells left uncertified by their whole base list -- and so
+    the exact-lists re-clip -- are the same set either way, as are the
+    emitted cells."""
+    p, m, _, _ = trained
+    cfg = W.config_ellipsoid(target_tets=40000, n_site=2000, seed=35)
+    runs = {}
+    for net in (False, True):
+        with engine(cfg, knn_k=32, certify=True, learned_k=net, exact_lists=True) as r:
+            if net:
+                r.mlp_set_params(p, m)
+            st = r.compute()
+            runs[net] = (st, r.pair_headers(), r.topology_hashes())
+    (s0, h0, t0), (s1, h1, t1) = runs[False], runs[True]
+    assert s0.learned == 0 and s1.learned == 1
+    assert s0.n_uncertified == 0 and s1.n_uncertified == 0
+    # without the network there is no first-pass re-clip
+    assert s0.n_reclipped == 0
+    assert 0 < s1.n_reclipped <= 0.08 * s1.n_pairs
+    # the exact-lists re-pass does real work at k = 32 and is the same
+    assert s0.n_cert_reclipped > 0
+    assert s1.n_cert_reclipped == s0.n_cert_reclipped
+    assert s1.n_extended_sites == s0.n_extended_sites
+    assert np.array_equal(h0["status"], h1["status"])
+    assert np.array_equal(t0, t1)
