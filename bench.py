@@ -15,7 +15,9 @@ device-resident mesh and sites to device-resident compact cells.
           set-up: 200k labelled cells of two meshes with other seeds)
   plain   the plain FP64 path: FP64 determinant on every predicate
   e2e     the fast path through the C ABI with host buffers: mesh + sites
-          host->device, compute, every cell device->host, per step
+          host->device, compute, every cell device->host, per step; two
+          contexts in turn, one step's copy back overlapping the next
+          step's upload and compute ("serial": one context, blocking copy)
   cpu_baseline / --impl reference: the oracle (CPU restatement of the
           reference's clipper and candidate rule, all host cores) on a
           bounded sample of the same workload's tets
@@ -160,14 +162,19 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def flush_l2():
-    """Writes 256 MB (> 129 MB L2) on the device between timed steps."""
+def flush_l2(device_sync=True):
+    """Writes 256 MB (> 129 MB L2) on the device between timed steps; waits
+    for the whole device, or (device_sync=False) only for the write itself,
+    so that copies in flight on the engines' streams keep running."""
     import torch
 
     if not hasattr(flush_l2, "buf"):
         flush_l2.buf = torch.empty(64 << 20, dtype=torch.int32, device="cuda")
     flush_l2.buf.fill_(1)
-    torch.cuda.synchronize()
+    if device_sync:
+        torch.cuda.synchronize()
+    else:
+        torch.cuda.current_stream().synchronize()
 
 
 def clip_algorithmic_bytes(cfg, n_pairs, k, topo_bytes):
@@ -871,9 +878,14 @@ def _sample_topology_equal(h1, p1, h2, p2, n=20000):
 
 
 def _e2e(args, cfg, adj, rpd, tuned):
-    """The same metric through the C ABI with host buffers (page-locked):
-    per step rpd_set_mesh + rpd_set_sites (host->device), rpd_compute, and
-    rpd_copy_cells_to_host (device->host of every cell)."""
+    """The same metric through the C ABI with host buffers (page-locked): per
+    step rpd_set_mesh + rpd_set_sites (host->device), rpd_compute, and the
+    device->host copy of every cell.  Two contexts take the steps in turn:
+    step i's copy back (rpd_copy_cells_to_host_async) runs on the copy engine
+    while step i + 1 computes on the other context, and the timed region
+    ends when the last step's cells have landed.  No L2 flush between the
+    steps: each step writes 1.7 GB of cells (> 129 MB L2).  "serial" is one
+    context with the blocking copy (rpd_copy_cells_to_host)."""
     nt, nv, ns = cfg["tets"].shape[0], cfg["vert3d"].shape[0], cfg["sites"].shape[0]
     pins = {}
 
@@ -891,48 +903,118 @@ def _e2e(args, cfg, adj, rpd, tuned):
     fi = pin("fi", adj["f_ids"])
     s = pin("s", cfg["sites"])
     fl = pin("fl", cfg["flags"])
-    r = rpd.RPD(predicate_mode=rpd.PRED_FP32_FILTER, neighbor_source=rpd.NEIGH_KNN,
-                knn_k=args.k, clip_order=rpd.ORDER_SITE_ID, certify=True)
-    # the fast engine's tuned configuration and trained predictor
-    tc = tuned.config()
-    tc.topology_hash = 0
-    r.set_config(tc)
-    try:
-        params, margin = tuned.mlp_params()
-        r.mlp_set_params(params, margin)
-    except rpd.RPDError:
-        pass
-    r.set_mesh(v, t, va, e6, fa, fi)
-    r.set_sites(s, fl)
-    st = r.compute()
-    hbuf = rpd.PinnedArray((int(st.n_cells * 1.1) + 1024,), rpd.HEADER_DTYPE)
-    pbuf = rpd.PinnedArray((int(st.payload_bytes * 1.1) + (1 << 20),), np.uint8)
     h2d = (v.nbytes + t.nbytes + va.nbytes + e6.nbytes + fa.nbytes + fi.nbytes + s.nbytes +
            fl.nbytes)
-    for _ in range(args.warmup):
-        r.set_mesh(v, t, va, e6, fa, fi)
-        r.set_sites(s, fl)
-        r.compute()
-        r.cells(hbuf.array, pbuf.array)
-    cells, d2h, secs = 0, 0, 0.0
-    for _ in range(args.steps):
-        flush_l2()
-        t0 = time.perf_counter()
+
+    def engine():
+        r = rpd.RPD(predicate_mode=rpd.PRED_FP32_FILTER, neighbor_source=rpd.NEIGH_KNN,
+                    knn_k=args.k, clip_order=rpd.ORDER_SITE_ID, certify=True)
+        # the fast engine's tuned configuration and trained predictor
+        tc = tuned.config()
+        tc.topology_hash = 0
+        r.set_config(tc)
+        try:
+            params, margin = tuned.mlp_params()
+            r.mlp_set_params(params, margin)
+        except rpd.RPDError:
+            pass
         r.set_mesh(v, t, va, e6, fa, fi)
         r.set_sites(s, fl)
         st = r.compute()
-        h, p = r.cells(hbuf.array, pbuf.array)
-        secs += time.perf_counter() - t0
-        cells += st.n_cells
-        d2h += h.nbytes + p.nbytes
-    r.close()
+        hbuf = rpd.PinnedArray((int(st.n_cells * 1.1) + 1024,), rpd.HEADER_DTYPE)
+        pbuf = rpd.PinnedArray((int(st.payload_bytes * 1.1) + (1 << 20),), np.uint8)
+        return r, hbuf, pbuf
+
+    def upload_compute(r):
+        r.set_mesh(v, t, va, e6, fa, fi)
+        r.set_sites(s, fl)
+        return r.compute()
+
+    engines = [engine(), engine()]
+    # ---- serial: one context, blocking copy
+    r0, hb0, pb0 = engines[0]
+    for _ in range(args.warmup):
+        upload_compute(r0)
+        r0.cells(hb0.array, pb0.array)
+    serial_secs, serial_cells = 0.0, 0
+    parts = np.zeros(3)
+    for _ in range(args.steps):
+        flush_l2()
+        t0 = time.perf_counter()
+        r0.set_mesh(v, t, va, e6, fa, fi)
+        r0.set_sites(s, fl)
+        t1 = time.perf_counter()
+        st = r0.compute()
+        t2 = time.perf_counter()
+        h, p = r0.cells(hb0.array, pb0.array)
+        t3 = time.perf_counter()
+        parts += (t1 - t0, t2 - t1, t3 - t2)
+        serial_secs += t3 - t0
+        serial_cells += st.n_cells
+    copy_bytes = h.nbytes + p.nbytes
+    # ---- pipelined: two contexts in turn.  Step i uploads on its context,
+    # then step i - 1's copy back is queued on the other one, then step i
+    # computes: the bulk copy overlaps the compute only, never the upload
+    # (both would share the host link)
+    d2h = [0]
+    pparts = np.zeros(4)  # upload, compute (host wall), compute (device), queue copy
+
+    def run(first, n):
+        cells, prev = 0, None
+        for i in range(first, first + n):
+            r, hb, pb = engines[i % 2]
+            t0 = time.perf_counter()
+            r.set_mesh(v, t, va, e6, fa, fi)
+            r.set_sites(s, fl)
+            t1 = time.perf_counter()
+            if prev is not None:
+                pr, phb, ppb = prev
+                h, p = pr.cells_async(phb.array, ppb.array)
+                d2h[0] += h.nbytes + p.nbytes
+            t2 = time.perf_counter()
+            st = r.compute()
+            t3 = time.perf_counter()
+            pparts[:] += (t1 - t0, t3 - t2, st.ms_total / 1000.0, t2 - t1)
+            cells += st.n_cells
+            prev = engines[i % 2]
+        pr, phb, ppb = prev
+        h, p = pr.cells_async(phb.array, ppb.array)
+        d2h[0] += h.nbytes + p.nbytes
+        return cells
+
+    run(0, args.warmup)
+    for r, _, _ in engines:
+        r.synchronize()
+    flush_l2()
+    d2h[0] = 0
+    pparts[:] = 0
+    t0 = time.perf_counter()
+    cells = run(args.warmup, args.steps)
+    t_end = time.perf_counter()
+    for r, _, _ in engines:
+        r.synchronize()
+    secs = time.perf_counter() - t0
+    tail_ms = 1000 * (time.perf_counter() - t_end)
+    for r, hb, pb in engines:
+        r.close()
+        hb.free()
+        pb.free()
     for pa in pins.values():
         pa.free()
-    hbuf.free()
-    pbuf.free()
     return {"value": cells / secs, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-            "d2h_bytes_per_step": int(d2h // args.steps),
-            "ms_per_step": 1000 * secs / args.steps}
+            "d2h_bytes_per_step": int(d2h[0] // args.steps),
+            "ms_per_step": 1000 * secs / args.steps, "pipelined": "2 contexts in turn",
+            "l2": "not flushed between pipelined steps: each writes 1.7 GB of cells (> 129 MB)",
+            "parts_ms": {"upload": 1000 * pparts[0] / args.steps,
+                         "compute_wall": 1000 * pparts[1] / args.steps,
+                         "compute_device": 1000 * pparts[2] / args.steps,
+                         "queue_copy": 1000 * pparts[3] / args.steps, "last_copy_wait": tail_ms},
+            "serial": {"value": serial_cells / serial_secs,
+                       "ms_per_step": 1000 * serial_secs / args.steps,
+                       "upload_ms": 1000 * parts[0] / args.steps,
+                       "compute_ms": 1000 * parts[1] / args.steps,
+                       "copy_ms": 1000 * parts[2] / args.steps,
+                       "copy_gbps": copy_bytes / (parts[2] / args.steps) / 1e9}}
 
 
 def main():

@@ -290,6 +290,20 @@ rpd_status rpd_copy_cells_to_host(struct rpd_ctx* ctx, rpd_cell_header* headers,
                                   int64_t payload_capacity, int64_t* n_cells,
                                   int64_t* payload_bytes);
 
+/* The same copies queued on the context's stream without waiting for them
+ * (same arguments and checks; sizes are returned at once).  The buffers must
+ * be page-locked (rpd_host_alloc) and stay untouched until
+ * rpd_synchronize(ctx), or the context's next call that waits on its stream,
+ * returns.  Two contexts used in turn overlap one mesh's device->host copy
+ * with the next mesh's upload and compute. */
+rpd_status rpd_copy_cells_to_host_async(struct rpd_ctx* ctx, rpd_cell_header* headers,
+                                        int64_t max_cells, void* payload,
+                                        int64_t payload_capacity, int64_t* n_cells,
+                                        int64_t* payload_bytes);
+
+/* Waits until everything queued on the context's stream has finished. */
+rpd_status rpd_synchronize(struct rpd_ctx* ctx);
+
 /* The headers of every candidate pair of the last rpd_compute (dropped
  * cells included, with their failure status), in (tet, site) order. */
 rpd_status rpd_copy_pair_headers_to_host(struct rpd_ctx* ctx, rpd_cell_header* headers,
@@ -754,8 +768,9 @@ rpd_status rpd_batch_copy_mesh_cells(struct rpd_batch* batch, int mesh, rpd_cell
  * call rpd_set_mesh / rpd_set_sites / rpd_compute on it. */
 struct rpd_ctx* rpd_batch_context(struct rpd_batch* batch);
 
-/* Page-locked host buffers for fast host<->device copies (cudaMallocHost);
- * NULL on failure. */
+/* Page-locked host buffers for fast host<->device copies (cudaMallocHost),
+ * every page written once (zeros) before they are returned; NULL on
+ * failure. */
 void* rpd_host_alloc(size_t bytes);
 void rpd_host_free(void* p);
 

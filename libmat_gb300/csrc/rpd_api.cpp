@@ -41,6 +41,42 @@ rpd_status cuda_fail(rpd_ctx* c, cudaError_t e, const char* where) {
               std::string(where) + ": " + cudaGetErrorString(e));
 }
 
+// The small device->host reads of set-up and compute (counts, sizes,
+// statistics).  add() queues a one-block kernel that stores the bytes into
+// the context's page-locked, device-mapped staging memory, in stream order
+// like cudaMemcpyAsync; wait() synchronizes the stream and hands them to
+// their destinations.  The copy engines are not involved, so another
+// context's bulk copy of its cells (queued on an engine) holds none of
+// them up.
+struct SmallReads {
+  rpd_ctx* c;
+  cudaStream_t st;
+  struct Read {
+    void* dst;
+    size_t off, n;
+  } r[8];
+  int nr = 0;
+  size_t used = 0;
+  SmallReads(rpd_ctx* ctx, cudaStream_t s) : c(ctx), st(s) {}
+  cudaError_t add(void* dst, const void* src, size_t n) {
+    const size_t off = (used + 15) & ~(size_t)15;
+    if (nr == 8 || off + n > rpd_ctx::kStageBytes) return cudaErrorInvalidValue;
+    const cudaError_t e = launch_stage_bytes(src, c->stage_dev + off, n, st);
+    if (e != cudaSuccess) return e;
+    r[nr++] = {dst, off, n};
+    used = off + n;
+    return cudaSuccess;
+  }
+  cudaError_t wait() {
+    const cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return e;
+    for (int i = 0; i < nr; ++i) std::memcpy(r[i].dst, c->stage_host + r[i].off, r[i].n);
+    nr = 0;
+    used = 0;
+    return cudaSuccess;
+  }
+};
+
 #define CK(expr, where)                          \
   do {                                           \
     cudaError_t _e = (expr);                     \
@@ -219,6 +255,18 @@ rpd_status rpd_create(const rpd_config* cfg, rpd_ctx** out) {
   }
   for (int i = 0; i < kEvCount; ++i) cudaEventCreate(&c->ev[i]);
   cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device);
+  void* stage = nullptr;
+  if (cudaHostAlloc(&stage, rpd_ctx::kStageBytes, cudaHostAllocMapped) != cudaSuccess ||
+      cudaHostGetDevicePointer((void**)&c->stage_dev, stage, 0) != cudaSuccess) {
+    cudaGetLastError();
+    if (stage) cudaFreeHost(stage);
+    cudaStreamDestroy(c->stream);
+    for (int i = 0; i < kEvCount; ++i)
+      if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+    delete c;
+    return RPD_ERR_CUDA;
+  }
+  c->stage_host = static_cast<uint8_t*>(stage);
   *out = c;
   return RPD_OK;
 }
@@ -249,6 +297,7 @@ void rpd_destroy(rpd_ctx* c) {
   for (int i = 0; i < kEvCount; ++i)
     if (c->ev[i]) cudaEventDestroy(c->ev[i]);
   if (c->stream) cudaStreamDestroy(c->stream);
+  if (c->stage_host) cudaFreeHost(c->stage_host);
   delete c;
 }
 
@@ -327,8 +376,9 @@ rpd_status rpd_set_mesh(rpd_ctx* c, const double* xyz, int n_vert, const int32_t
   CK(mesh_prep_geometry(c->vert3d.ptr, n_vert, c->tets.ptr, c->f_adjs.ptr, n_tet, c->vert3f.ptr,
                         c->vert2.ptr, c->tet_rad.ptr, c->bmark.ptr, c->prep.ptr, st), "prep");
   MeshPrepOut po;
-  CK(cudaMemcpyAsync(&po, c->prep.ptr, sizeof(po), cudaMemcpyDeviceToHost, st), "D2H");
-  CK(cudaStreamSynchronize(st), "set_mesh sync");
+  SmallReads rd(c, st);
+  CK(rd.add(&po, c->prep.ptr, sizeof(po)), "D2H");
+  CK(rd.wait(), "set_mesh sync");
   if (po.bad & 1u) return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_set_mesh: non-finite vertex");
   if (po.bad & 2u) return fail(c, RPD_ERR_INVALID_ARGUMENT, "rpd_set_mesh: vertex id out of range");
   const double rmax = key_to_double(po.rmax_key);
@@ -336,9 +386,8 @@ rpd_status rpd_set_mesh(rpd_ctx* c, const double* xyz, int n_vert, const int32_t
   // its histogram bin), and the rest
   std::vector<int32_t> hist(kRadiusBins);
   CK(mesh_prep_histogram(c->tet_rad.ptr, n_tet, rmax, c->prep_hist.ptr, st), "histogram");
-  CK(cudaMemcpyAsync(hist.data(), c->prep_hist.ptr, sizeof(int32_t) * kRadiusBins,
-                     cudaMemcpyDeviceToHost, st), "D2H");
-  CK(cudaStreamSynchronize(st), "set_mesh sync");
+  CK(rd.add(hist.data(), c->prep_hist.ptr, sizeof(int32_t) * kRadiusBins), "D2H");
+  CK(rd.wait(), "set_mesh sync");
   const long long want = std::min<long long>(n_tet, (long long)std::ceil(0.995 * (double)n_tet));
   long long acc = 0;
   int bin = kRadiusBins - 1;
@@ -352,8 +401,8 @@ rpd_status rpd_set_mesh(rpd_ctx* c, const double* xyz, int n_vert, const int32_t
   const double r0 = rmax * (double)(bin + 1) / (double)kRadiusBins;
   CK(mesh_prep_classify(c->tet_rad.ptr, n_tet, r0, c->tet_class.ptr, c->prep.ptr, st), "classes");
   CK(launch_tet_face_planes(c->vert3d.ptr, c->tets.ptr, n_tet, c->face2.ptr, st), "face planes");
-  CK(cudaMemcpyAsync(&po, c->prep.ptr, sizeof(po), cudaMemcpyDeviceToHost, st), "D2H");
-  CK(cudaStreamSynchronize(st), "set_mesh sync");
+  CK(rd.add(&po, c->prep.ptr, sizeof(po)), "D2H");
+  CK(rd.wait(), "set_mesh sync");
   for (int k = 0; k < rpd_ctx::kClasses; ++k) {
     c->class_count[k] = k < 2 ? po.class_count[k] : 0;
     c->class_radius[k] = k < 2 && po.class_count[k] > 0 ? key_to_double(po.class_rmax_key[k]) : 0.0;
@@ -602,8 +651,9 @@ static rpd_status finish_compute(rpd_ctx* c, bool knn, bool learned, rpd_stats* 
       CK(select_pairs(c->pair_headers.ptr, n_pairs, kSecurityRadiusNotReached, c->flag_tmp.ptr,
                       c->pos_tmp.ptr, c->scan_tmp.ptr, c->reclip_idx.ptr, st), "select");
       int32_t n_re = 0;
-      CK(cudaMemcpyAsync(&n_re, c->pos_tmp.ptr + n_pairs, sizeof(n_re), cudaMemcpyDeviceToHost, st), "D2H");
-      CK(cudaStreamSynchronize(st), "reclip sync");
+      SmallReads rd(c, st);
+      CK(rd.add(&n_re, c->pos_tmp.ptr + n_pairs, sizeof(n_re)), "D2H");
+      CK(rd.wait(), "reclip sync");
       c->n_reclipped = n_re;
       if (n_re > 0) {
         CK(cudaMemsetAsync(c->scratch.ptr + 1, 0, sizeof(unsigned long long), st), "memset");
@@ -659,10 +709,10 @@ static rpd_status finish_compute(rpd_ctx* c, bool knn, bool learned, rpd_stats* 
                       c->ext_sites.ptr, st), "select sites");
       int32_t n_f = 0;
       unsigned long long n_flag = 0;
-      CK(cudaMemcpyAsync(&n_f, c->site_pos.ptr + n_site, sizeof(n_f), cudaMemcpyDeviceToHost, st), "D2H");
-      CK(cudaMemcpyAsync(&n_flag, c->scratch.ptr + 32, sizeof(n_flag), cudaMemcpyDeviceToHost, st),
-         "D2H");
-      CK(cudaStreamSynchronize(st), "extend sync");
+      SmallReads rd(c, st);
+      CK(rd.add(&n_f, c->site_pos.ptr + n_site, sizeof(n_f)), "D2H");
+      CK(rd.add(&n_flag, c->scratch.ptr + 32, sizeof(n_flag)), "D2H");
+      CK(rd.wait(), "extend sync");
       if (round > 0) {
         float ms = 0.f;
         cudaEventElapsedTime(&ms, c->ev[kEvExtR0], c->ev[kEvExtK]);
@@ -750,8 +800,9 @@ static rpd_status finish_compute(rpd_ctx* c, bool knn, bool learned, rpd_stats* 
     CK(cudaEventRecord(c->ev[kEvExt1], st), "event");
     c->ext_valid = extend;
     unsigned long long cur = 0;
-    CK(cudaMemcpyAsync(&cur, c->scratch.ptr, sizeof(cur), cudaMemcpyDeviceToHost, st), "D2H");
-    CK(cudaStreamSynchronize(st), "clip sync");
+    SmallReads rd(c, st);
+    CK(rd.add(&cur, c->scratch.ptr, sizeof(cur)), "D2H");
+    CK(rd.wait(), "clip sync");
     c->payload_bytes = (long long)cur;
     if ((long long)cur <= (long long)c->payload.cap) break;
     pcap = (long long)cur + (long long)cur / 8 + (1 << 20);
@@ -786,9 +837,12 @@ static rpd_status finish_compute(rpd_ctx* c, bool knn, bool learned, rpd_stats* 
   CK(cudaEventRecord(c->ev[kEvEnd], st), "event");
   unsigned long long host_scratch[40];
   long long n_cells = 0;
-  CK(cudaMemcpyAsync(host_scratch, c->scratch.ptr, sizeof(host_scratch), cudaMemcpyDeviceToHost, st), "D2H");
-  CK(cudaMemcpyAsync(&n_cells, c->n_out.ptr, sizeof(n_cells), cudaMemcpyDeviceToHost, st), "D2H");
-  CK(cudaStreamSynchronize(st), "compute sync");
+  {
+    SmallReads rd(c, st);
+    CK(rd.add(host_scratch, c->scratch.ptr, sizeof(host_scratch)), "D2H");
+    CK(rd.add(&n_cells, c->n_out.ptr, sizeof(n_cells)), "D2H");
+    CK(rd.wait(), "compute sync");
+  }
   c->n_cells = n_cells;
   c->tet_k = (int)reinterpret_cast<int32_t*>(host_scratch + 5)[0];
   c->has_result = true;
@@ -989,8 +1043,9 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
                         c->scratch.ptr + 27, c->num_sms, st), "pairs");
       }
       unsigned long long np = 0;
-      CK(cudaMemcpyAsync(&np, c->scratch.ptr + 4, sizeof(np), cudaMemcpyDeviceToHost, st), "D2H");
-      CK(cudaStreamSynchronize(st), "pairs sync");
+      SmallReads rd(c, st);
+      CK(rd.add(&np, c->scratch.ptr + 4, sizeof(np)), "D2H");
+      CK(rd.wait(), "pairs sync");
       c->n_pairs = (long long)np;
       if ((long long)np <= (long long)c->pair_buf.cap) break;
       cap = (long long)np + (long long)np / 8 + 1024;
@@ -1149,6 +1204,22 @@ rpd_status rpd_get_cells(rpd_ctx* c, rpd_cells_view* v) {
 rpd_status rpd_copy_cells_to_host(rpd_ctx* c, rpd_cell_header* headers, int64_t max_cells,
                                   void* payload, int64_t payload_capacity, int64_t* n_cells,
                                   int64_t* payload_bytes) {
+  const rpd_status s = rpd_copy_cells_to_host_async(c, headers, max_cells, payload,
+                                                    payload_capacity, n_cells, payload_bytes);
+  if (s != RPD_OK || (!headers && !payload)) return s;
+  return rpd_synchronize(c);
+}
+
+rpd_status rpd_synchronize(rpd_ctx* c) {
+  if (!c) return RPD_ERR_INVALID_ARGUMENT;
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  CK(cudaStreamSynchronize(c->stream), "sync");
+  return RPD_OK;
+}
+
+rpd_status rpd_copy_cells_to_host_async(rpd_ctx* c, rpd_cell_header* headers, int64_t max_cells,
+                                        void* payload, int64_t payload_capacity,
+                                        int64_t* n_cells, int64_t* payload_bytes) {
   if (!c) return RPD_ERR_INVALID_ARGUMENT;
   if (!c->has_result) return fail(c, RPD_ERR_NOT_READY, "rpd_copy_cells_to_host: no result");
   if (n_cells) *n_cells = c->n_cells;
@@ -1164,7 +1235,6 @@ rpd_status rpd_copy_cells_to_host(rpd_ctx* c, rpd_cell_header* headers, int64_t 
   if (payload && c->payload_bytes > 0)
     CK(cudaMemcpyAsync(payload, c->payload.ptr, (size_t)c->payload_bytes, cudaMemcpyDeviceToHost, st),
        "D2H payload");
-  CK(cudaStreamSynchronize(st), "copy sync");
   return RPD_OK;
 }
 
@@ -2411,6 +2481,9 @@ void* rpd_host_alloc(size_t bytes) {
     cudaGetLastError();
     return nullptr;
   }
+  // every page written once here: the first device->host copies into
+  // pages never touched from the host ran at about 40 % of the link rate
+  std::memset(p, 0, bytes);
   return p;
 }
 

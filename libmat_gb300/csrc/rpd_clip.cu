@@ -768,6 +768,226 @@ __device__ __forceinline__ bool cert_holds(float key, float R, float margin) {
 }
 
 // ------------------------------------------------------------------------
+// one clip of the cell kernel, by the whole warp
+// ------------------------------------------------------------------------
+// The reference's update (convex_cell.cu:618-774) is sequential: the
+// swap-to-tail partition of the conflicting vertices, the walk around the
+// cavity, then one edge and one vertex per boundary plane.  The warp
+// computes the same result:
+//  * partition: the swap-to-tail loop is a fixed permutation of the
+//    conflict bits.  With n vertices, C the conflicting slots, n' = n - |C|
+//    and T the surviving slots in [n', n):
+//      a slot v < n' outside C keeps its vertex;
+//      the j-th slot of C below n' takes the j-th highest slot of T;
+//      tail slot p >= n' takes the lowest slot of C if p = n - 1, the
+//      vertex of slot p + 1 if that slot conflicts, and otherwise the
+//      (rho + 1)-th lowest slot of C, rho the slots of T above p;
+//    each lane gathers its slot (cells of up to 32 vertices; lane 0 runs
+//    the loop itself for larger ones);
+//  * boundary: the cavity of one removed vertex is its triangle; otherwise
+//    lane 0 walks it (compute_boundary) and lists its planes in order;
+//  * lane k makes edge k and vertex k along the boundary, with the vertex's
+//    cofactors and radius bound, and the status is the one the sequential
+//    loop stops with: the first vertex with a zero determinant needs
+//    perturbation unless a triangle overflow comes strictly before it.
+
+// position of the j-th (1-based) lowest set bit of m (m has at least j)
+__device__ __forceinline__ int select_bit(uint32_t m, int j) {
+  int pos = 0;
+#pragma unroll
+  for (int w = 16; w > 0; w >>= 1) {
+    const int c = __popc(m & ((1u << w) - 1u));
+    if (c < j) {
+      j -= c;
+      m >>= w;
+      pos += w;
+    }
+  }
+  return pos;
+}
+
+// the swap-to-tail partition run by one thread (cells of more than 32
+// vertices); returns the survivors' count
+template <bool COF, bool RAD>
+__device__ __noinline__ int partition_serial(WarpCell& c, int nb_v, uint32_t m0, uint32_t m1,
+                                             uint32_t m2) {
+  int i = 0;
+  while (i < nb_v) {
+    const uint32_t wi = i < 32 ? m0 : (i < 64 ? m1 : m2);
+    if ((wi >> (i & 31)) & 1u) {
+      nb_v--;
+      const uchar4 tv = c.ver[i];
+      c.ver[i] = c.ver[nb_v];
+      c.ver[nb_v] = tv;
+      if (COF) {
+        const float4 k = c.u.f.K[i];
+        c.u.f.K[i] = c.u.f.K[nb_v];
+        c.u.f.K[nb_v] = k;
+        const float4 mm = c.u.f.M[i];
+        c.u.f.M[i] = c.u.f.M[nb_v];
+        c.u.f.M[nb_v] = mm;
+      }
+      if (RAD) {
+        const float r = c.u.f.rad[i];
+        c.u.f.rad[i] = c.u.f.rad[nb_v];
+        c.u.f.rad[nb_v] = r;
+      }
+      const uint32_t wn = nb_v < 32 ? m0 : (nb_v < 64 ? m1 : m2);
+      const uint32_t bit = 1u << (i & 31);
+      const uint32_t nw = ((wn >> (nb_v & 31)) & 1u) ? (wi | bit) : (wi & ~bit);
+      if (i < 32) m0 = nw;
+      else if (i < 64) m1 = nw;
+      else m2 = nw;
+    } else {
+      i++;
+    }
+  }
+  return nb_v;
+}
+
+// Adds plane e with id2 `id` as plane s.nb_p and clips the cell by it; the
+// conflicting vertex slots are in mask[3] (warp-uniform).  All lanes.
+template <bool COF, bool RAD>
+__device__ __forceinline__ void clip_full(WarpCell& c, CellState& s, const uint32_t* mask,
+                                          float4 e, int2 id, int lane, float3 S) {
+  const int cur = s.nb_p;
+  if (lane == 0) {
+    c.pl[cur] = e;
+    c.h[cur] = 1;
+    c.id2[cur] = id;
+  }
+  s.nb_p = cur + 1;
+  const int n = s.nb_v;
+  int n2;
+  if (n <= 32) {
+    const uint32_t valid = n == 32 ? ~0u : ((1u << n) - 1u);
+    const uint32_t C = mask[0] & valid;
+    n2 = n - __popc(C);  // at most n - 1: the plane conflicts somewhere
+    const uint32_t low = (1u << n2) - 1u;
+    const uint32_t T = ~C & valid & ~low;
+    const int v = lane;
+    int src = v;
+    if (v < n2) {
+      if ((C >> v) & 1u) {
+        const int j = __popc(C & ((1u << v) - 1u)) + 1;
+        src = select_bit(T, __popc(T) - j + 1);
+      }
+    } else if (v == n - 1) {
+      src = __ffs(C) - 1;
+    } else if (v < n) {
+      if ((C >> (v + 1)) & 1u) src = v + 1;
+      else src = select_bit(C, __popc(T >> (v + 1)) + 1);
+    }
+    const bool move = v < n && src != v;
+    uchar4 t;
+    float4 K, M;
+    float rd = 0.f;
+    if (move) {
+      t = c.ver[src];
+      if (COF && v < n2) {
+        K = c.u.f.K[src];
+        M = c.u.f.M[src];
+        if (RAD) rd = c.u.f.rad[src];
+      }
+    }
+    __syncwarp();
+    if (move) {
+      c.ver[v] = t;
+      if (COF && v < n2) {
+        c.u.f.K[v] = K;
+        c.u.f.M[v] = M;
+        if (RAD) c.u.f.rad[v] = rd;
+      }
+    }
+  } else {
+    if (lane == 0) n2 = partition_serial<COF, RAD>(c, n, mask[0], mask[1], mask[2]);
+    n2 = __shfl_sync(0xffffffffu, n2, 0);
+  }
+  __syncwarp();
+  s.nb_v = n2;
+  s.kept = n2;
+  if (n2 == 0) {
+    s.status = kNoIntersection;
+    return;
+  }
+  const int nb_r = n - n2;
+  int len = 3;
+  uchar4 tr = make_uchar4(0, 0, 0, 0);
+  if (nb_r == 1) {
+    // the cavity is the removed vertex's triangle, its planes in order
+    tr = c.ver[n2];
+  } else {
+    if (lane < kMaxP / 4) reinterpret_cast<uint32_t*>(c.bnext)[lane] = 0xffffffffu;
+    __syncwarp();
+    int st = s.status, L = 0;
+    if (lane == 0) {
+      int first, r = nb_r;
+      compute_boundary(c, n2, r, first, st);
+      if (st == kSuccess && first != kEnd) {
+        // the boundary holds at most nb_p - 1 planes
+        int cir = first;
+        do {
+          c.perm[L++] = (uint8_t)cir;
+          cir = c.bnext[cir];
+        } while (cir != first && L < kMaxP);
+        if (cir != first) st = kInconsistentBoundary;
+      }
+    }
+    st = __shfl_sync(0xffffffffu, st, 0);
+    len = __shfl_sync(0xffffffffu, L, 0);
+    s.status = st;
+    if (st != kSuccess || len == 0) return;
+  }
+  __syncwarp();  // tr and the boundary are read before new vertices land
+  if (s.nb_e + len > kMaxE) {
+    s.status = kEdgeOverflow;
+    return;
+  }
+  const uint8_t hcur = c.h[cur];
+  const int nb_e = s.nb_e;
+  int zero_k = kMaxP;  // first boundary vertex whose three planes are dependent
+  for (int k = lane; k < len; k += 32) {
+    int cir, nx;
+    if (nb_r == 1) {
+      cir = k == 0 ? tr.x : (k == 1 ? tr.y : tr.z);
+      nx = k == 0 ? tr.y : (k == 1 ? tr.z : tr.x);
+    } else {
+      cir = c.perm[k];
+      nx = c.perm[k + 1 == len ? 0 : k + 1];
+    }
+    const float4 pcir = c.pl[cir], pnx = c.pl[nx];
+    const uint8_t hcir = c.h[cir], hnx = c.h[nx];
+    // cur > cir: the new plane has the largest index
+    c.edge[nb_e + k] = make_uchar4((uint8_t)cir, (uint8_t)cur, hcur > hcir ? hcur : hcir, 0);
+    // the largest count of the vertex's three edges (edge_adj)
+    uint8_t adj = hcur > hcir ? hcur : hcir;
+    if (hnx > adj) adj = hnx;
+    if (cir < 4 && nx < 4) {
+      const uint8_t te = c.edge[cTetEdgeSlot[cir][nx]].z;
+      if (te > adj) adj = te;
+    }
+    const int slot = n2 + k;
+    if (slot + 1 < kMaxT) {
+      c.ver[slot] = make_uchar4((uint8_t)cur, (uint8_t)cir, (uint8_t)nx, adj);
+      if (COF) {
+        float4 K, M;
+        vertex_cofactors(e, pcir, pnx, K, M);
+        c.u.f.K[slot] = K;
+        c.u.f.M[slot] = M;
+        if (RAD) c.u.f.rad[slot] = vertex_radius(K, M, S);
+      }
+    }
+    if (det3x3_f(e, pcir, pnx) == 0.f && k < zero_k) zero_k = k;
+  }
+  for (int o = 16; o > 0; o >>= 1) zero_k = min(zero_k, __shfl_xor_sync(0xffffffffu, zero_k, o));
+  const int k_of = max(kMaxT - 1 - n2, 0);  // first vertex that would overflow
+  if (zero_k < len && zero_k <= k_of) s.status = kNeedsPerturb;
+  else if (k_of < len) s.status = kTriangleOverflow;
+  s.nb_e = nb_e + len;
+  s.nb_v = n2 + len;
+}
+
+// ------------------------------------------------------------------------
 // the neighbour loop shared by the cell kernel and the box kernel
 // ------------------------------------------------------------------------
 // make_plane(j) builds the plane of list entry j (bisector, or offset
@@ -848,6 +1068,18 @@ __device__ void clip_list(WarpCell& c, CellState& s, const int32_t* list, int k,
       // the plane of list entry `hit` clips: write it and update topology
       float4 e = shfl4(e_mine, hit);
       int jn = __shfl_sync(0xffffffffu, j, hit);
+      if (FULL) {
+        clip_full<kCof, CERT>(c, s, mask, e,
+                              make_int2(seed_id < jn ? seed_id : jn, seed_id < jn ? jn : seed_id),
+                              lane, cert.S);
+        __syncwarp();
+        if (eager && s.status == kSuccess) R = cell_radius(c, s.nb_v, lane);
+        if (plane_eq(e_mine, e)) dup_mine |= 1ull << (s.nb_p - 1);
+        any_dup = __any_sync(0xffffffffu, dup_mine != 0ull);
+        if (s.status != kSuccess) break;
+        r = hit + 1;
+        continue;
+      }
       if (lane < kMaxP / 4) reinterpret_cast<uint32_t*>(c.bnext)[lane] = 0xffffffffu;
       if (kCof && !FULL)
         for (int v = lane; v < s.nb_v; v += 32) c.perm[v] = (uint8_t)v;

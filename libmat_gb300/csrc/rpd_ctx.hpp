@@ -82,6 +82,12 @@ struct rpd_ctx {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[kEvCount] = {};
   std::string err;
+  // page-locked, device-mapped staging for the small device->host reads of
+  // set-up and compute (SmallReads): stores from a kernel, not the copy
+  // engines, so another context's bulk copy does not hold them up
+  static constexpr size_t kStageBytes = 64 << 10;
+  uint8_t* stage_host = nullptr;
+  uint8_t* stage_dev = nullptr;
 
   // mesh
   int n_vert = 0, n_tet = 0;

@@ -473,6 +473,9 @@ struct MeshPrepOut {
 };
 double key_to_double(unsigned long long k);
 cudaError_t mesh_prep_init(MeshPrepOut* out, cudaStream_t st);
+// copies n bytes from device memory to dst (device-mapped host memory) with
+// one block of stores, in stream order
+cudaError_t launch_stage_bytes(const void* src, void* dst, size_t n, cudaStream_t st);
 // float and double-float vertices, box, id check, FP64 tet radii, volume,
 // boundary vertex marks (bmark may be null)
 cudaError_t mesh_prep_geometry(const double* xyz, int n_vert, const int4* tets,

@@ -246,4 +246,16 @@ cudaError_t boundary_list(const uint8_t* bmark, const float* vert3f, int n_vert,
   return cudaGetLastError();
 }
 
+__global__ void stage_bytes_kernel(const uint8_t* __restrict__ src, uint8_t* dst, int n) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
+}
+
+cudaError_t launch_stage_bytes(const void* src, void* dst, size_t n, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  stage_bytes_kernel<<<1, 256, 0, st>>>(static_cast<const uint8_t*>(src),
+                                       static_cast<uint8_t*>(dst), (int)n);
+  note_launches(1);
+  return cudaGetLastError();
+}
+
 }  // namespace rpd

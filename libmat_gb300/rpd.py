@@ -45,7 +45,8 @@ TOPO_OPEN_FACE = 2
 EXPORTS = [
     "rpd_status_string", "rpd_config_default", "rpd_payload_bytes", "rpd_create",
     "rpd_destroy", "rpd_last_error", "rpd_set_mesh", "rpd_set_sites", "rpd_set_neighbors",
-    "rpd_compute", "rpd_get_cells", "rpd_copy_cells_to_host", "rpd_copy_neighbors_to_host",
+    "rpd_compute", "rpd_get_cells", "rpd_copy_cells_to_host", "rpd_copy_cells_to_host_async",
+    "rpd_synchronize", "rpd_copy_neighbors_to_host",
     "rpd_copy_pairs_to_host", "rpd_copy_pair_headers_to_host", "rpd_build_mesh_adjacency",
     "rpd_copy_site_lists_to_host",
     "rpd_host_alloc", "rpd_host_free", "rpd_compact_cells_noalloc", "rpd_set_site_k",
@@ -200,6 +201,11 @@ def load(path=LIB_PATH):
     L.rpd_get_cells.argtypes = [vp, c.POINTER(CellsView)]
     L.rpd_copy_cells_to_host.restype = i32
     L.rpd_copy_cells_to_host.argtypes = [vp, vp, i64, vp, i64, c.POINTER(i64), c.POINTER(i64)]
+    L.rpd_copy_cells_to_host_async.restype = i32
+    L.rpd_copy_cells_to_host_async.argtypes = [vp, vp, i64, vp, i64, c.POINTER(i64),
+                                               c.POINTER(i64)]
+    L.rpd_synchronize.restype = i32
+    L.rpd_synchronize.argtypes = [vp]
     L.rpd_copy_neighbors_to_host.restype = i32
     L.rpd_copy_neighbors_to_host.argtypes = [vp, vp, i64, c.POINTER(i32)]
     L.rpd_copy_site_lists_to_host.restype = i32
@@ -564,6 +570,20 @@ class RPD:
         self._check(self._L.rpd_copy_cells_to_host(self._h, _p(h), h.shape[0], _p(p), p.nbytes,
                                                    ctypes.byref(n), ctypes.byref(b)))
         return h[:n.value], p[:b.value]
+
+    def cells_async(self, headers_out, payload_out):
+        """Queues the copy of the emitted cells into page-locked arrays
+        (PinnedArray) and returns their (headers, payload) views at once;
+        they hold the cells after synchronize()."""
+        n = ctypes.c_int64()
+        b = ctypes.c_int64()
+        self._check(self._L.rpd_copy_cells_to_host_async(
+            self._h, _p(headers_out), headers_out.shape[0], _p(payload_out), payload_out.nbytes,
+            ctypes.byref(n), ctypes.byref(b)))
+        return headers_out[:n.value], payload_out[:b.value]
+
+    def synchronize(self):
+        self._check(self._L.rpd_synchronize(self._h))
 
     def compute_topology(self):
         """Per-cell topology of the emitted cells on the device (active
