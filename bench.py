@@ -196,8 +196,9 @@ def clip_algorithmic_bytes(cfg, n_pairs, k, topo_bytes):
 # its traffic grows with them), and smsp__issue_active of the same capture;
 # the capture and its command are summarised in
 # profiles/clip_cells_kernel_ellipsoid_200k.md
-CLIP_DRAM_BYTES_PER_PAIR = 308.0
-CLIP_ISSUE_ACTIVE = 0.783
+CLIP_DRAM_BYTES_PER_PAIR = 320.9
+CLIP_ISSUE_ACTIVE = 0.695
+CLIP_THREADS_PER_INST = 16.27
 
 
 def sample_tets(n_tet, n, seed):
@@ -635,9 +636,11 @@ def run_ours(args):
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                      "peak_source": peak_src,
                      "algorithmic_bytes": alg,
-                     # the bound that applies: instruction issue (ncu
-                     # smsp__issue_active of the same kernel)
-                     "issue_active_frac": CLIP_ISSUE_ACTIVE},
+                     # what bounds it instead: instruction issue and
+                     # latency (ncu smsp__issue_active and threads per
+                     # executed instruction of the same kernel)
+                     "issue_active_frac": CLIP_ISSUE_ACTIVE,
+                     "threads_per_inst": CLIP_THREADS_PER_INST},
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
     }
