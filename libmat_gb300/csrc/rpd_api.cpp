@@ -976,12 +976,13 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
         Grid tg = make_grid(c->mesh_lo, c->mesh_hi, c->class_count[cl], 4.0);
         long long nc = (long long)tg.nx * tg.ny * tg.nz;
         CK(c->t_cell_count.ensure(nc), "alloc");
+        CK(c->t_cell_rmax.ensure(nc), "alloc");
         CK(c->t_cell_start.ensure(nc + 1), "alloc");
         CK(c->t_cell_fill.ensure(nc), "alloc");
         CK(c->scan_tmp.ensure(scan_temp_ints(std::max<long long>(nc, n_tet)) + 16), "alloc");
         CK(grid_build_tets(c->centroid.ptr, n_tet, c->tet_class.ptr, cl, tg, c->t_cell_of.ptr,
                            c->t_cell_count.ptr, c->t_cell_start.ptr, c->t_cell_fill.ptr,
-                           c->t_cell_items.ptr, c->scan_tmp.ptr, st), "tet grid");
+                           c->t_cell_items.ptr, c->scan_tmp.ptr, st, c->t_cell_rmax.ptr), "tet grid");
         // per-site boxes: every tet of this class that passes the rule has
         // its centroid in the site's cell pushed out by the class radius
         const double R = c->class_radius[cl] * (1.0 + 1e-5) + 1e-6 * cs;
@@ -1021,6 +1022,7 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
         pp.tg = tg;
         pp.tcell_start = c->t_cell_start.ptr;
         pp.tcell_items = c->t_cell_items.ptr;
+        pp.tcell_rmax = c->t_cell_rmax.ptr;
         pp.site4f = c->site4f.ptr;
         pp.flags = c->flags.ptr;
         pp.nbr = c->nbr.ptr;
@@ -1028,6 +1030,7 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
         pp.k = c->k;
         pp.n_site = n_site;
         pp.site_box = c->site_box.ptr;
+        pp.offset_r = bp.offset_r;
         pp.site_planes = c->site_planes.ptr;
         pp.site_nplanes = c->site_nplanes.ptr;
         pp.coord_scale = (float)cs;

@@ -44,6 +44,7 @@ struct FrontLane {
   cudaEvent_t done = nullptr;
   DevBuf<int32_t> s_cell_count, s_cell_start, s_cell_fill, s_cell_items;
   DevBuf<int32_t> t_cell_of, t_cell_count, t_cell_start, t_cell_fill, t_cell_items;
+  DevBuf<float> t_cell_rmax;
   DevBuf<int32_t> scan_tmp, pair_ntasks, pair_taskoff;
   DevBuf<unsigned long long> work;  // the pair kernel's task counter
   std::vector<int> meshes;           // meshes of this lane
@@ -166,6 +167,7 @@ rpd_status upload(rpd_batch* b) {
     BCK(L.t_cell_of.ensure((size_t)max_tet), "alloc");
     BCK(L.t_cell_items.ensure((size_t)max_tet), "alloc");
     BCK(L.t_cell_count.ensure((size_t)max_tc), "alloc");
+    BCK(L.t_cell_rmax.ensure((size_t)max_tc), "alloc");
     BCK(L.t_cell_start.ensure((size_t)max_tc + 1), "alloc");
     BCK(L.t_cell_fill.ensure((size_t)max_tc), "alloc");
     const long long scan_n = std::max(std::max(max_sc, max_tc), std::max(max_site, max_tet)) + 1;
@@ -236,7 +238,8 @@ rpd_status front_end(rpd_batch* b) {
       const Grid& tg = m.tet_grid[cl];
       BCK(grid_build_tets(c->centroid.ptr + tb, m.n_tet, c->tet_class.ptr + tb, cl, tg,
                           L.t_cell_of.ptr, L.t_cell_count.ptr, L.t_cell_start.ptr,
-                          L.t_cell_fill.ptr, L.t_cell_items.ptr, L.scan_tmp.ptr, ls),
+                          L.t_cell_fill.ptr, L.t_cell_items.ptr, L.scan_tmp.ptr, ls,
+                          L.t_cell_rmax.ptr),
           "tet grid");
       const double R = m.class_radius[cl] * (1.0 + 1e-5) + 1e-6 * cs;
       BoxParams bp;
@@ -272,6 +275,7 @@ rpd_status front_end(rpd_batch* b) {
       pp.tg = tg;
       pp.tcell_start = L.t_cell_start.ptr;
       pp.tcell_items = L.t_cell_items.ptr;
+      pp.tcell_rmax = L.t_cell_rmax.ptr;
       pp.site4f = c->site4f.ptr;
       pp.flags = c->flags.ptr;
       pp.nbr = c->nbr.ptr + (long long)sb * k;
@@ -279,6 +283,7 @@ rpd_status front_end(rpd_batch* b) {
       pp.k = k;
       pp.n_site = m.n_site;
       pp.site_box = c->site_box.ptr + 2ll * sb;
+      pp.offset_r = bp.offset_r;
       pp.site_planes = c->site_planes.ptr + (long long)sb * kBoxPlanes;
       pp.site_nplanes = c->site_nplanes.ptr + sb;
       pp.coord_scale = (float)cs;

@@ -60,6 +60,7 @@ struct __align__(16) WarpCell {
   uint8_t h[kMaxP];
   uint8_t bnext[kMaxP];
   uint8_t perm[kMaxT];  // during a clip: the slot each surviving vertex came from
+  float4 cand[32];      // the planes of the list chunk being tested, one per lane
 };
 
 struct CellState {
@@ -1008,12 +1009,19 @@ __device__ void clip_list(WarpCell& c, CellState& s, const int32_t* list, int k,
     int count = (~valid == 0u) ? 32 : (__ffs(~valid) - 1);  // up to first -1
     float key_mine = 0.f;
     if (eager && lane < count) key_mine = __ldg(cert.keys + base + lane);
-    float4 e_mine = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (lane < count) e_mine = make_plane(j);
-    // planes already in the cell that equal this lane's plane
+    // the lane's plane goes to shared memory (the tests read it from there;
+    // no register holds it through the chunk), with the planes already in
+    // the cell that equal it
     uint64_t dup_mine = 0;
-    for (int p = 0; p < s.nb_p; ++p)
-      if (plane_eq(e_mine, c.pl[p])) dup_mine |= 1ull << p;
+    {
+      float4 e_mine = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (lane < count) e_mine = make_plane(j);
+      __syncwarp();  // the previous chunk's planes are no longer read
+      c.cand[lane] = e_mine;
+      for (int p = 0; p < s.nb_p; ++p)
+        if (plane_eq(e_mine, c.pl[p])) dup_mine |= 1ull << p;
+    }
+    __syncwarp();
     bool any_dup = __any_sync(0xffffffffu, dup_mine != 0ull);
     int r = 0;
     while (r < count) {
@@ -1036,7 +1044,7 @@ __device__ void clip_list(WarpCell& c, CellState& s, const int32_t* list, int k,
         int V = 1 << lgV;
         int pi = lane >> lgV, vi = lane & (V - 1);
         int pidx = r + pi;
-        float4 e = shfl4(e_mine, pidx & 31);
+        const float4 e = c.cand[pidx & 31];
         uint64_t dup = any_dup ? shfl64(dup_mine, pidx & 31) : 0ull;
         bool cf = false;
         if (pidx < count && vi < s.nb_v) cf = in_conflict<PRED>(c, vi, e, dup, pc);
@@ -1049,7 +1057,7 @@ __device__ void clip_list(WarpCell& c, CellState& s, const int32_t* list, int k,
         mask[0] = (V == 32) ? m : ((m >> (pf << lgV)) & ((1u << V) - 1u));
         hit = r + pf;
       } else {
-        float4 e = shfl4(e_mine, r);
+        const float4 e = c.cand[r];
         uint64_t dup = any_dup ? shfl64(dup_mine, r) : 0ull;
         bool any = false;
         for (int w = 0; w < 3; ++w) {
@@ -1066,7 +1074,7 @@ __device__ void clip_list(WarpCell& c, CellState& s, const int32_t* list, int k,
         hit = r;
       }
       // the plane of list entry `hit` clips: write it and update topology
-      float4 e = shfl4(e_mine, hit);
+      const float4 e = c.cand[hit];
       int jn = __shfl_sync(0xffffffffu, j, hit);
       if (FULL) {
         clip_full<kCof, CERT>(c, s, mask, e,
@@ -1074,7 +1082,7 @@ __device__ void clip_list(WarpCell& c, CellState& s, const int32_t* list, int k,
                               lane, cert.S);
         __syncwarp();
         if (eager && s.status == kSuccess) R = cell_radius(c, s.nb_v, lane);
-        if (plane_eq(e_mine, e)) dup_mine |= 1ull << (s.nb_p - 1);
+        if (plane_eq(c.cand[lane], e)) dup_mine |= 1ull << (s.nb_p - 1);
         any_dup = __any_sync(0xffffffffu, dup_mine != 0ull);
         if (s.status != kSuccess) break;
         r = hit + 1;
@@ -1126,7 +1134,7 @@ __device__ void clip_list(WarpCell& c, CellState& s, const int32_t* list, int k,
       __syncwarp();
       if (eager && s.status == kSuccess) R = cell_radius(c, s.nb_v, lane);
       // later planes of this chunk identical to the new one
-      if (plane_eq(e_mine, e)) dup_mine |= 1ull << (s.nb_p - 1);
+      if (plane_eq(c.cand[lane], e)) dup_mine |= 1ull << (s.nb_p - 1);
       any_dup = __any_sync(0xffffffffu, dup_mine != 0ull);
       if (s.status != kSuccess) break;
       r = hit + 1;

@@ -143,6 +143,7 @@ struct rpd_ctx {
   // grids
   DevBuf<int32_t> s_cell_of, s_cell_count, s_cell_start, s_cell_fill, s_cell_items;
   DevBuf<int32_t> t_cell_of, t_cell_count, t_cell_start, t_cell_fill, t_cell_items;
+  DevBuf<float> t_cell_rmax;
   DevBuf<float4> centroid, site_box, site_planes, tet_xyz;
   DevBuf<uchar4> tet_vadj;
   DevBuf<int32_t> site_nplanes, pair_ntasks, pair_taskoff;

@@ -175,11 +175,12 @@ cudaError_t grid_build_sites(const float4* pts, int n, const Grid& g, int32_t* c
 cudaError_t tet_centroids(const float* vert3f, const int4* tets, int n_tet, float4* centroid,
                           cudaStream_t st, float4* tet_xyz = nullptr,
                           const int32_t* v_adjs = nullptr, uchar4* tet_vadj = nullptr);
-// bins the tets of radius class `want` (all tets when cls is null) by centroid
+// bins the tets of radius class `want` (all tets when cls is null) by centroid;
+// cell_rmax (optional) gets the largest tet radius (centroid.w) of each cell
 cudaError_t grid_build_tets(const float4* centroid, int n_tet, const uint8_t* cls, int want,
                             const Grid& g, int32_t* cell_of, int32_t* cell_count,
                             int32_t* cell_start, int32_t* cell_fill, int32_t* cell_items,
-                            int32_t* scan_tmp, cudaStream_t st);
+                            int32_t* scan_tmp, cudaStream_t st, float* cell_rmax = nullptr);
 
 // k smallest power-bisector distances per site (ties by id); lists in
 // distance order or sorted by id
@@ -226,6 +227,7 @@ struct PairParams {
   Grid tg;
   const int32_t* tcell_start;
   const int32_t* tcell_items;
+  const float* tcell_rmax;  // largest tet radius of each tet-grid cell (may be null)
   const float4* site4f;   // all sites
   const uint32_t* flags;  // all sites
   const int32_t* nbr;     // this mesh's rows
@@ -241,6 +243,10 @@ struct PairParams {
   long long pair_cap;
   int32_t* tet_count;
   unsigned long long* diag;  // search counters (see rpd_stats::search)
+  // the radius the site planes were pushed out by (the tet class's largest
+  // tet radius, rounded up): each centroid test takes back what its own
+  // tet's radius does not need
+  float offset_r;
 };
 // n_tasks, task_off: n_site and n_site + 1 ints; work: one counter
 cudaError_t launch_pairs(const PairParams& p, int32_t* n_tasks, int32_t* task_off,

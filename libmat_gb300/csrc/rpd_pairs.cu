@@ -103,7 +103,8 @@ __device__ __forceinline__ int cell_index(const Grid& g, float x, float y, float
 }
 
 __global__ void bin_points_kernel(const float4* pts, int n, Grid g, int32_t* cell_of,
-                                  int32_t* cell_count, const uint8_t* cls, int want) {
+                                  int32_t* cell_count, const uint8_t* cls, int want,
+                                  float* cell_rmax) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   if (cls && cls[i] != want) {
@@ -114,6 +115,8 @@ __global__ void bin_points_kernel(const float4* pts, int n, Grid g, int32_t* cel
   int c = cell_index(g, p.x, p.y, p.z);
   cell_of[i] = c;
   atomicAdd(cell_count + c, 1);
+  // radii are >= 0: their bit patterns order as the floats do
+  if (cell_rmax) atomicMax(reinterpret_cast<unsigned int*>(cell_rmax) + c, __float_as_uint(p.w));
 }
 
 __global__ void fill_cells_kernel(int n, const int32_t* cell_of, const int32_t* cell_start,
@@ -163,7 +166,8 @@ cudaError_t grid_build_sites(const float4* pts, int n, const Grid& g, int32_t* c
   long long n_cells = (long long)g.nx * g.ny * g.nz;
   cudaMemsetAsync(cell_count, 0, sizeof(int32_t) * n_cells, st);
   if (n > 0) {
-    bin_points_kernel<<<(n + 255) / 256, 256, 0, st>>>(pts, n, g, cell_of, cell_count, nullptr, 0);
+    bin_points_kernel<<<(n + 255) / 256, 256, 0, st>>>(pts, n, g, cell_of, cell_count, nullptr, 0,
+                                                      nullptr);
     note_launches(1);
   }
   return grid_finish(n, g, cell_of, cell_count, cell_start, cell_fill, cell_items, scan_tmp, st);
@@ -218,12 +222,13 @@ cudaError_t tet_centroids(const float* vert3f, const int4* tets, int n_tet, floa
 cudaError_t grid_build_tets(const float4* centroid, int n_tet, const uint8_t* cls, int want,
                             const Grid& g, int32_t* cell_of, int32_t* cell_count,
                             int32_t* cell_start, int32_t* cell_fill, int32_t* cell_items,
-                            int32_t* scan_tmp, cudaStream_t st) {
+                            int32_t* scan_tmp, cudaStream_t st, float* cell_rmax) {
   long long n_cells = (long long)g.nx * g.ny * g.nz;
   cudaMemsetAsync(cell_count, 0, sizeof(int32_t) * n_cells, st);
+  if (cell_rmax) cudaMemsetAsync(cell_rmax, 0, sizeof(float) * n_cells, st);
   if (n_tet > 0) {
     bin_points_kernel<<<(n_tet + 255) / 256, 256, 0, st>>>(centroid, n_tet, g, cell_of, cell_count,
-                                                          cls, want);
+                                                          cls, want, cell_rmax);
     note_launches(1);
   }
   return grid_finish(n_tet, g, cell_of, cell_count, cell_start, cell_fill, cell_items, scan_tmp,
@@ -550,6 +555,7 @@ __global__ void __launch_bounds__(kPairWarps * 32) pairs_kernel(PairParams p,
                                                                 const int32_t* task_off,
                                                                 unsigned long long* work) {
   __shared__ float4 spl[kPairWarps][kBoxPlanes];
+  __shared__ float spn[kPairWarps][kBoxPlanes];  // |normal| of each plane, rounded down
   __shared__ float4 snb[kPairWarps][kPairMaxK];  // the site's neighbours (rule order)
   // queued tets: vertices (12 floats), power distances to the site (4), id
   __shared__ float sq_v[kPairWarps][16][kRuleQueue];
@@ -582,11 +588,17 @@ __global__ void __launch_bounds__(kPairWarps * 32) pairs_kernel(PairParams p,
     // exact planes accept
     const int npl = p.site_nplanes[i];
     float4* pl = spl[wid];
+    float* pn = spn[wid];
     __syncwarp();
     for (int q = lane; q < npl; q += 32) {
       float4 e = p.site_planes[(long long)i * kBoxPlanes + q];
       float tol = 4e-6f * ((fabsf(e.x) + fabsf(e.y) + fabsf(e.z)) * p.coord_scale + fabsf(e.w));
       pl[q] = make_float4(e.x, e.y, e.z, e.w + tol);
+      // bisectors only: the region's box planes (axis-aligned, the mesh box
+      // and its margin) were not pushed out (an axis-aligned bisector is
+      // left as it is too, which only accepts more)
+      const int n_zero = (e.x == 0.f) + (e.y == 0.f) + (e.z == 0.f);
+      pn[q] = n_zero >= 2 ? 0.f : sqrtf(e.x * e.x + e.y * e.y + e.z * e.z) * (1.0f - 1e-5f);
     }
     __syncwarp();
     const float4 si = p.site4f[p.site_base + i];
@@ -624,8 +636,24 @@ __global__ void __launch_bounds__(kPairWarps * 32) pairs_kernel(PairParams p,
                      hc * (fabsf(e.x) + fabsf(e.y) + fabsf(e.z));
         if (best < 0.f) return -1;
       }
+      const int cell = x + g.nx * (y + g.ny * z);
+      // again with the cell's largest tet radius in place of the class's
+      // (the centroid test below, applied to the best centroid in the cell)
+      if (p.tcell_rmax) {
+        const float shrink =
+            fmaxf(p.offset_r - (__ldg(p.tcell_rmax + cell) * (1.0f + 1e-5f) + 1e-6f * p.coord_scale),
+                  0.f);
+        if (shrink > 0.f) {
+          for (int q = 0; q < npl; ++q) {
+            float4 e = pl[q];
+            float best = e.x * cxm + e.y * cym + e.z * czm + e.w +
+                         hc * (fabsf(e.x) + fabsf(e.y) + fabsf(e.z)) - shrink * pn[q];
+            if (best < 0.f) return -1;
+          }
+        }
+      }
       ++n_keep;
-      return x + g.nx * (y + g.ny * z);
+      return cell;
     };
     // a tet that passed the rule becomes a pair
     auto emit = [&](bool pass, int t) {
@@ -685,9 +713,16 @@ __global__ void __launch_bounds__(kPairWarps * 32) pairs_kernel(PairParams p,
         float4 c = p.centroid[t];
         bool in = c.x >= blo.x && c.x <= bhi.x && c.y >= blo.y && c.y <= bhi.y &&
                   c.z >= blo.z && c.z <= bhi.z;
+        // A tet passes the rule for neighbour m only if a vertex lies on the
+        // site's side of their bisector, so its centroid lies within the
+        // tet's own radius of it: the planes were pushed out by the class's
+        // largest radius, and each test takes back (R - r_t) |n|, r_t the
+        // tet's radius (c.w, a float square root) rounded up and |n| rounded
+        // down so that the test only ever accepts more than the exact one
+        const float shrink = fmaxf(p.offset_r - (c.w * (1.0f + 1e-5f) + 1e-6f * p.coord_scale), 0.f);
         for (int q = 0; q < npl && in; ++q) {
           float4 e = pl[q];
-          in = e.x * c.x + e.y * c.y + e.z * c.z + e.w >= 0.f;
+          in = e.x * c.x + e.y * c.y + e.z * c.z + e.w - shrink * pn[q] >= 0.f;
         }
         if (in) {
           ++n_in;
