@@ -1031,6 +1031,9 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
         pp.n_site = n_site;
         pp.site_box = c->site_box.ptr;
         pp.offset_r = bp.offset_r;
+        pp.rule_keys = knn ? c->nbr_keys.ptr : nullptr;
+        pp.accept_margin = (float)(16.0 * u * (cs + std::sqrt(diag2)));
+        pp.accept_err = 1.01f * bp.offset_e;
         pp.site_planes = c->site_planes.ptr;
         pp.site_nplanes = c->site_nplanes.ptr;
         pp.coord_scale = (float)cs;

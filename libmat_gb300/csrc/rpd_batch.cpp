@@ -284,6 +284,7 @@ rpd_status front_end(rpd_batch* b) {
       pp.n_site = m.n_site;
       pp.site_box = c->site_box.ptr + 2ll * sb;
       pp.offset_r = bp.offset_r;
+      pp.rule_keys = nullptr;  // (the rule checks every neighbour)
       pp.site_planes = c->site_planes.ptr + (long long)sb * kBoxPlanes;
       pp.site_nplanes = c->site_nplanes.ptr + sb;
       pp.coord_scale = (float)cs;

@@ -247,6 +247,12 @@ struct PairParams {
   // tet radius, rounded up): each centroid test takes back what its own
   // tet's radius does not need
   float offset_r;
+  // keys of the rule's (distance-ordered) lists, or null; with them a tet
+  // whose nearest vertex lies within the key of neighbour r (less the
+  // margins) passes the rule for r and every later neighbour at once
+  const float* rule_keys;
+  float accept_margin;  // absolute rounding of a key (as the certificate's)
+  float accept_err;     // bound on the float error of pd_m(v) - pd_i(v)
 };
 // n_tasks, task_off: n_site and n_site + 1 ints; work: one counter
 cudaError_t launch_pairs(const PairParams& p, int32_t* n_tasks, int32_t* task_off,

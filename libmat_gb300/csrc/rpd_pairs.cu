@@ -560,6 +560,10 @@ __global__ void __launch_bounds__(kPairWarps * 32) pairs_kernel(PairParams p,
   // queued tets: vertices (12 floats), power distances to the site (4), id
   __shared__ float sq_v[kPairWarps][16][kRuleQueue];
   __shared__ int sq_t[kPairWarps][kRuleQueue];
+  // every 8th neighbour r: its key and the smallest site distance |c_m - c_i|
+  // (rounded down) of the neighbours from r on
+  __shared__ float schk_key[kPairWarps][kPairMaxK / 8];
+  __shared__ float schk_d[kPairWarps][kPairMaxK / 8];
   const int lane = threadIdx.x & 31;
   const int wid = threadIdx.x >> 5;
   const long long n_tasks = task_off[p.n_site];
@@ -614,6 +618,34 @@ __global__ void __launch_bounds__(kPairWarps * 32) pairs_kernel(PairParams p,
       nb[r] = m < 0 ? make_float4(0.f, 0.f, 0.f, -INFINITY) : __ldg(p.site4f + m);
     }
     __syncwarp();
+    // the acceptance checkpoints (distance-ordered lists with keys only)
+    const bool acc_ok = p.rule_keys != nullptr && k_staged == p.k;
+    if (acc_ok) {
+      float carry = INFINITY;
+      for (int w = (k_staged - 1) >> 5; w >= 0; --w) {
+        const int r = lane + 32 * w;
+        float d = INFINITY;  // a hole never rejects
+        if (r < k_staged) {
+          const float4 m = nb[r];
+          if (m.w != -INFINITY) {
+            const float dx = m.x - si.x, dy = m.y - si.y, dz = m.z - si.z;
+            d = sqrtf(dx * dx + dy * dy + dz * dz) * (1.0f - 1e-6f);
+          }
+        }
+        // suffix minimum: lane l gets the minimum over lanes >= l
+        for (int o = 1; o < 32; o <<= 1) {
+          const float t = __shfl_down_sync(0xffffffffu, d, o);
+          if (lane + o < 32) d = fminf(d, t);
+        }
+        d = fminf(d, carry);
+        carry = __shfl_sync(0xffffffffu, d, 0);
+        if (r < k_staged && (r & 7) == 0) {
+          schk_d[wid][r >> 3] = d;
+          schk_key[wid][r >> 3] = __ldg(p.rule_keys + (long long)i * p.k + r);
+        }
+      }
+      __syncwarp();
+    }
     // neighbour r of the rule order (staged, or read for long user lists)
     auto rule_site = [&](int r) -> float4 {
       if (r < k_staged) return nb[r];
@@ -687,7 +719,23 @@ __global__ void __launch_bounds__(kPairWarps * 32) pairs_kernel(PairParams p,
         }
         t = qt[lane];
         pass = true;
+        // distance from the site to the tet's nearest vertex, rounded up
+        float m2 = INFINITY;
+        for (int a = 0; a < 4; ++a) {
+          const float dx = v[a].x - si.x, dy = v[a].y - si.y, dz = v[a].z - si.z;
+          m2 = fminf(m2, dx * dx + dy * dy + dz * dz);
+        }
+        const float d_up = sqrtf(m2) * (1.0f + 1e-6f);
         for (int r = kRuleFirst; r < p.k && pass; ++r) {
+          // pd_m(v) - pd_i(v) = 2 |c_m - c_i| (key_m - (v - c_i).u_m) for the
+          // unit direction u_m to m: a vertex within key_m of the site,
+          // by more than the float error of the two power distances, has
+          // pd_m(v) > pd_i(v) as evaluated; keys ascend along the list
+          if (acc_ok && (r & 7) == 0) {
+            const float g = schk_key[wid][r >> 3] * (1.0f - 64.0f * 5.9604645e-08f) -
+                            p.accept_margin - d_up;
+            if (g > 0.f && 2.0f * schk_d[wid][r >> 3] * g > p.accept_err) break;
+          }
           const float4 sm = rule_site(r);
           bool hit = false;
           for (int a = 0; a < 4; ++a) hit |= pow_dist(sm, v[a]) > pdi[a];
