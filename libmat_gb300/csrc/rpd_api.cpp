@@ -460,6 +460,7 @@ rpd_status rpd_set_sites(rpd_ctx* c, const double* xyzw, int n_site, const uint3
     c->cells_for_mesh = false;  // site ids of the previous cells no longer apply
   }
   c->n_site = n_site;
+  c->has_site_range = false;  // (a batch sets its meshes' ranges after this)
   for (int a = 0; a < 3; ++a) {
     c->site_lo[a] = lo[a];
     c->site_hi[a] = hi[a];
@@ -731,7 +732,8 @@ static rpd_status finish_compute(rpd_ctx* c, bool knn, bool learned, rpd_stats* 
       CK(cudaEventRecord(c->ev[kEvExtR0], st), "event");
       if (last) {
         CK(complete_rows(c->ext_sites.ptr, n_f, c->ext_rows, c->ext_used, n_site, c->site_row.ptr,
-                         c->ext_off.ptr, c->ext_len.ptr, c->ext_bound.ptr, c->ext_nbr.ptr, st),
+                         c->ext_off.ptr, c->ext_len.ptr, c->ext_bound.ptr, c->ext_nbr.ptr, st,
+                         c->has_site_range ? c->site_range.ptr : nullptr),
            "complete rows");
       } else {
         Grid g = make_grid(c->site_lo, c->site_hi, n_site, 2.0);
@@ -741,6 +743,7 @@ static rpd_status finish_compute(rpd_ctx* c, bool knn, bool learned, rpd_stats* 
         ka.g = g;
         ka.cell_start = c->s_cell_start.ptr;
         ka.cell_items = c->s_cell_items.ptr;
+        ka.site_range = c->has_site_range ? c->site_range.ptr : nullptr;
         ka.k = KL;
         ka.w_max = c->w_max;
         // ascending key in every mode: in site-id order the hundreds of

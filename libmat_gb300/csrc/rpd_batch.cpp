@@ -115,6 +115,18 @@ rpd_status upload(rpd_batch* b) {
   // radius classes per mesh (the context's are over all tets)
   BCK(cudaMemcpy(c->tet_class.ptr, b->tet_class.data(), b->tet_class.size(), cudaMemcpyHostToDevice),
       "H2D classes");
+  // each site's lists hold only its own mesh's sites (the exact-lists rounds
+  // search one grid of every site)
+  {
+    std::vector<int2> range((size_t)n_site);
+    for (const BatchMesh& m : b->meshes)
+      for (int i = 0; i < m.n_site; ++i)
+        range[(size_t)(m.site_base + i)] = make_int2(m.site_base, m.site_base + m.n_site);
+    BCK(c->site_range.ensure((size_t)n_site), "alloc");
+    BCK(cudaMemcpy(c->site_range.ptr, range.data(), sizeof(int2) * range.size(),
+                   cudaMemcpyHostToDevice), "H2D ranges");
+    c->has_site_range = true;
+  }
   const int k = c->cfg.knn_k;
   c->k = k;
   BCK(c->nbr.ensure((size_t)n_site * k), "alloc");
@@ -502,7 +514,23 @@ rpd_status rpd_batch_compute(rpd_batch* b, rpd_stats* stats) {
   }
   if (c->n_pairs > INT32_MAX) return bfail(b, RPD_ERR_CAPACITY, "rpd_batch_compute: more than 2^31 pairs");
   c->pair_cap_hint = std::max<long long>(c->pair_cap_hint, c->n_pairs + c->n_pairs / 8 + 1024);
-  rpd_status s = rpd_finish_compute(c, true, false, stats);
+  // exact lists: the rounds search one grid of every site of the batch, each
+  // site restricted to its mesh's ids
+  const bool exact = c->cfg.exact_lists != 0;
+  if (exact) {
+    const int n_site = c->n_site;
+    const Grid g = rpd_make_grid(c->site_lo, c->site_hi, n_site, 2.0);
+    const long long nc = (long long)g.nx * g.ny * g.nz;
+    BCK(c->s_cell_count.ensure((size_t)nc), "alloc");
+    BCK(c->s_cell_start.ensure((size_t)nc + 1), "alloc");
+    BCK(c->s_cell_fill.ensure((size_t)nc), "alloc");
+    BCK(c->s_cell_items.ensure((size_t)n_site), "alloc");
+    BCK(c->scan_tmp.ensure(scan_temp_ints(std::max<long long>(nc, n_site)) + 16), "alloc");
+    BCK(grid_build_sites(c->site4f.ptr, n_site, g, c->s_cell_of.ptr, c->s_cell_count.ptr,
+                         c->s_cell_start.ptr, c->s_cell_fill.ptr, c->s_cell_items.ptr,
+                         c->scan_tmp.ptr, st), "site grid");
+  }
+  rpd_status s = rpd_finish_compute(c, true, false, stats, exact);
   c->cells_for_mesh = false;  // a batch's cells are not one mesh's (no partial update)
   if (s != RPD_OK) return bfail(b, s, rpd_last_error(c));
   // first compacted cell of every mesh

@@ -126,6 +126,10 @@ struct rpd_ctx {
   long long n_reclipped = 0;
   DevBuf<float> nbr_keys;
   bool has_user_nbr = false;
+  // per site: the ids its lists may hold (a batch: its mesh's sites); the
+  // exact-lists rounds search the whole-context site grid with it
+  DevBuf<int2> site_range;
+  bool has_site_range = false;
   // exact lists (rpd_config.exact_lists): the completeness bound of every
   // base list, and the longer lists given to sites whose cells a pass left
   // uncertified -- row r of the extended lists starts at ext_off[r]

@@ -211,6 +211,9 @@ struct KnnArgs {
   float bound_scale, bound_abs;
   int32_t* len_out;      // per row: entries listed, or null
   float* bound_out;      // per row: every site not listed has a key >= this, or null
+  // per site: the ids [x, y) it may list (its mesh's sites in a batch), or
+  // null for every site
+  const int2* site_range;
 };
 int knn_max_k();
 cudaError_t launch_knn(const KnnArgs& a, cudaStream_t st);
@@ -284,9 +287,11 @@ cudaError_t assign_rows(const int32_t* sites, int n, int row0, long long off0, i
                         int32_t* site_row, long long* ext_off, cudaStream_t st);
 // rows row0 + f of the sites sites[f], all on one list of every site
 // (written at ext_nbr[off..off + n_site)), bound INFINITY
+// (site_range: each row takes only its site's range of the shared list)
 cudaError_t complete_rows(const int32_t* sites, int n, int row0, long long off, int n_site,
                           int32_t* site_row, long long* ext_off, int32_t* ext_len,
-                          float* ext_bound, int32_t* ext_nbr, cudaStream_t st);
+                          float* ext_bound, int32_t* ext_nbr, cudaStream_t st,
+                          const int2* site_range = nullptr);
 
 // batches: first compacted cell of each mesh (n_mesh + 1 entries); record
 // sizes; gather of one mesh's records with mesh-local ids

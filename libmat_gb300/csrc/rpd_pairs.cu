@@ -344,6 +344,7 @@ __global__ void __launch_bounds__(WARPS * 32) knn_kernel(KnnArgs a) {
   const int k = a.k;
   const Grid& g = a.g;
   const float4 si = a.site4f[i];
+  const int2 rng = a.site_range ? a.site_range[i] : make_int2(0, 0x7fffffff);
   float B = INFINITY;
   if (a.radius) {
     const float R = __uint_as_float(a.radius[i]);
@@ -371,7 +372,7 @@ __global__ void __launch_bounds__(WARPS * 32) knn_kernel(KnnArgs a) {
     for_items(n_cube, cell_at, a.cell_start, a.cell_items, lane, [&](int j, bool valid) {
       bool take = false;
       unsigned long long packed = 0;
-      if (valid && j != i) {
+      if (valid && j != i && j >= rng.x && j < rng.y) {
         float key = bisector_key(si, a.site4f[j]);
         packed = ((unsigned long long)order_key(key) << 32) | (uint32_t)j;
         take = packed < kth && key <= B;
@@ -1035,24 +1036,29 @@ cudaError_t assign_rows(const int32_t* sites, int n, int row0, long long off0, i
 // ext_nbr[off..off + n_site), and rows row0 + f of the sites sites[f] on it
 __global__ void complete_rows_kernel(const int32_t* sites, int n, int row0, long long off,
                                      int n_site, int32_t* site_row, long long* ext_off,
-                                     int32_t* ext_len, float* ext_bound, int32_t* ext_nbr) {
+                                     int32_t* ext_len, float* ext_bound, int32_t* ext_nbr,
+                                     const int2* site_range) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n_site) ext_nbr[off + i] = i;
   if (i < n) {
-    site_row[sites[i]] = row0 + i;
-    ext_off[row0 + i] = off;
-    ext_len[row0 + i] = n_site;
+    const int s = sites[i];
+    const int2 r = site_range ? site_range[s] : make_int2(0, n_site);
+    site_row[s] = row0 + i;
+    ext_off[row0 + i] = off + r.x;
+    ext_len[row0 + i] = r.y - r.x;
     ext_bound[row0 + i] = INFINITY;
   }
 }
 
 cudaError_t complete_rows(const int32_t* sites, int n, int row0, long long off, int n_site,
                           int32_t* site_row, long long* ext_off, int32_t* ext_len,
-                          float* ext_bound, int32_t* ext_nbr, cudaStream_t st) {
+                          float* ext_bound, int32_t* ext_nbr, cudaStream_t st,
+                          const int2* site_range) {
   const int m = n > n_site ? n : n_site;
   if (m <= 0) return cudaSuccess;
   complete_rows_kernel<<<(m + 255) / 256, 256, 0, st>>>(sites, n, row0, off, n_site, site_row,
-                                                        ext_off, ext_len, ext_bound, ext_nbr);
+                                                        ext_off, ext_len, ext_bound, ext_nbr,
+                                                        site_range);
   note_launches(1);
   return cudaGetLastError();
 }

@@ -809,7 +809,7 @@ class Batch:
 
     def __init__(self, device=0, predicate_mode=PRED_FP32_FILTER, knn_k=64,
                  clip_order=ORDER_SITE_ID, compute_geometry=True, certify=False, clip_variant=0,
-                 topology_hash=True, use_graph=True):
+                 topology_hash=True, use_graph=True, exact_lists=True):
         L = load()
         cfg = Config()
         L.rpd_config_default(ctypes.byref(cfg))
@@ -822,6 +822,7 @@ class Batch:
         cfg.certify = 1 if certify else 0
         cfg.clip_variant = clip_variant
         cfg.topology_hash = 1 if topology_hash else 0
+        cfg.exact_lists = 1 if exact_lists else 0
         h = ctypes.c_void_p()
         s = L.rpd_batch_create(ctypes.byref(cfg), ctypes.byref(h))
         if s != 0:

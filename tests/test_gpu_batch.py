@@ -7,7 +7,7 @@ import pytest
 
 from libmat_gb300 import rpd
 from libmat_gb300 import workloads as W
-from tests.helpers import compare_cells, xyz_of
+from tests.helpers import compare_cells, topology_hash, xyz_of
 
 pytestmark = pytest.mark.gpu
 
@@ -51,7 +51,7 @@ def same_cells(h1, p1, h2, p2):
 def test_batch_equals_single_mesh_runs(certify):
     ms = meshes()
     kw = dict(predicate_mode=rpd.PRED_FP32_FILTER, certify=certify)
-    with rpd.Batch(**kw) as b:
+    with rpd.Batch(exact_lists=False, **kw) as b:
         for cfg in ms:
             a = cfg["adj"]
             b.add_mesh(cfg["vert3d"], cfg["tets"], a["v_adjs"], a["e_adj6"], a["f_adjs"],
@@ -68,6 +68,46 @@ def test_batch_equals_single_mesh_runs(certify):
         assert same_cells(gh, gp, *again[m]), m
         total += sst.n_cells
     assert st.n_cells == total == st2.n_cells
+
+
+def canonical(h, p):
+    """(tet << 32 | site, canonical topology hash) of emitted cells, sorted;
+    the hash is computed here from the records, whose plane ids are the
+    mesh's own (rpd_batch_copy_mesh_cells maps them back)."""
+    key = (h["tet_id"].astype(np.int64) << 32) | h["site_id"].astype(np.int64)
+    hs = np.array([topology_hash(p, h["offset"][q], h["nb_v"][q], h["nb_p"][q], h["nb_e"][q])
+                   for q in range(len(h))], np.uint64)
+    order = np.argsort(key)
+    return key[order], hs[order]
+
+
+def test_exact_batch_equals_exact_single_mesh_runs():
+    """Exact lists in a batch: the rounds search one grid of every site of
+    the batch, each site restricted to its own mesh's sites.  With short
+    base lists the rounds do real work; every mesh's cells then equal (by
+    (tet, site) and canonical topology) those of an exact single-mesh run."""
+    ms = meshes()
+    kw = dict(predicate_mode=rpd.PRED_FP32_FILTER, certify=True, knn_k=16)
+    with rpd.Batch(exact_lists=True, **kw) as b:
+        for cfg in ms:
+            a = cfg["adj"]
+            b.add_mesh(cfg["vert3d"], cfg["tets"], a["v_adjs"], a["e_adj6"], a["f_adjs"],
+                       a["f_ids"], cfg["sites"], cfg["flags"])
+        st = b.compute()
+        got = [canonical(*b.mesh_cells(m)) for m in range(len(ms))]
+    assert st.n_uncertified == 0
+    assert st.n_extended_sites > 0 and st.n_cert_reclipped > 0
+    for m, cfg in enumerate(ms):
+        a = cfg["adj"]
+        with rpd.RPD(neighbor_source=rpd.NEIGH_KNN, exact_lists=True, **kw) as r:
+            r.set_mesh(cfg["vert3d"], cfg["tets"], a["v_adjs"], a["e_adj6"], a["f_adjs"],
+                       a["f_ids"])
+            r.set_sites(cfg["sites"], cfg["flags"])
+            sst = r.compute()
+            want = canonical(*r.cells())
+        assert sst.n_uncertified == 0
+        assert np.array_equal(got[m][0], want[0]), m
+        assert np.array_equal(got[m][1], want[1]), m
 
 
 def test_batch_without_graph_and_tuned():
