@@ -709,7 +709,8 @@ def run_batch(args):
     0.04]) in one batch: the per-mesh front end replayed from a CUDA graph,
     one persistent clip launch for all meshes, autotuned.  Beside it: the
     same batch with the front end launched directly, a loop of single-mesh
-    computes, and the plain FP64 batch (topology reference)."""
+    computes, and the plain FP64 batch (topology reference).  Exact lists
+    are on in every form (the cells are the exact restricted cells)."""
     from libmat_gb300 import rpd
     from libmat_gb300 import workloads as W
 
@@ -749,7 +750,12 @@ def run_batch(args):
     out["batch_graph"] = {"cells_per_s": v, "ms_per_step": m_, "n_launches": int(st.n_launches),
                           "stage_ms": {"front_end": st.ms_knn, "pairs_csr": st.ms_pairs,
                                        "clip": st.ms_clip, "clip_kernel": st.ms_clip_kernel,
-                                       "epilogue": st.ms_epilogue, "compact": st.ms_compact}}
+                                       "epilogue": st.ms_epilogue, "compact": st.ms_compact,
+                                       "exact_lists": st.ms_extend},
+                          "uncertified_cells": int(st.n_uncertified),
+                          "exact_lists": {"extended_sites": int(st.n_extended_sites),
+                                          "cells_reclipped": int(st.n_cert_reclipped),
+                                          "rounds": int(st.n_extend_rounds)}}
     n_cells, n_pairs = int(st.n_cells), int(st.n_pairs)
     fast.configure(topology_hash=1)
     fast.compute()

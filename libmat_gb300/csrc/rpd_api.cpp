@@ -736,7 +736,8 @@ static rpd_status finish_compute(rpd_ctx* c, bool knn, bool learned, rpd_stats* 
                          c->has_site_range ? c->site_range.ptr : nullptr),
            "complete rows");
       } else {
-        Grid g = make_grid(c->site_lo, c->site_hi, n_site, 2.0);
+        Grid g = c->has_site_range ? make_grid(c->grid_lo, c->grid_hi, n_site, 2.0)
+                                   : make_grid(c->site_lo, c->site_hi, n_site, 2.0);
         KnnArgs ka = {};
         ka.site4f = c->site4f.ptr;
         ka.n_rows = n_f;
@@ -744,6 +745,7 @@ static rpd_status finish_compute(rpd_ctx* c, bool knn, bool learned, rpd_stats* 
         ka.cell_start = c->s_cell_start.ptr;
         ka.cell_items = c->s_cell_items.ptr;
         ka.site_range = c->has_site_range ? c->site_range.ptr : nullptr;
+        ka.grid_pos = c->has_site_range ? c->site_gridpos.ptr : nullptr;
         ka.k = KL;
         ka.w_max = c->w_max;
         // ascending key in every mode: in site-id order the hundreds of

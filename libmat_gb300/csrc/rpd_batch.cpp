@@ -117,14 +117,44 @@ rpd_status upload(rpd_batch* b) {
       "H2D classes");
   // each site's lists hold only its own mesh's sites (the exact-lists rounds
   // search one grid of every site)
+  // (and, for that grid, each mesh moved to a slot of its own: meshes that
+  // overlap in space would otherwise fill every grid cell with sites of the
+  // others)
   {
     std::vector<int2> range((size_t)n_site);
+    double ext[3] = {0, 0, 0};
     for (const BatchMesh& m : b->meshes)
-      for (int i = 0; i < m.n_site; ++i)
-        range[(size_t)(m.site_base + i)] = make_int2(m.site_base, m.site_base + m.n_site);
+      for (int a = 0; a < 3; ++a) ext[a] = std::max(ext[a], m.site_hi[a] - m.site_lo[a]);
+    const int nm = (int)b->meshes.size();
+    int side = 1;
+    while ((long long)side * side * side < nm) ++side;
+    double stride[3];
+    for (int a = 0; a < 3; ++a) stride[a] = ext[a] * (1.0 + 1e-3) + 1e-6 * (ext[a] + 1.0);
+    std::vector<float4> gpos((size_t)n_site);
+    for (int mi = 0; mi < nm; ++mi) {
+      const BatchMesh& m = b->meshes[(size_t)mi];
+      const int slot[3] = {mi % side, (mi / side) % side, mi / (side * side)};
+      double off[3];
+      for (int a = 0; a < 3; ++a) off[a] = slot[a] * stride[a] - m.site_lo[a];
+      for (int i = 0; i < m.n_site; ++i) {
+        const size_t s = (size_t)(m.site_base + i);
+        range[s] = make_int2(m.site_base, m.site_base + m.n_site);
+        const double* x = &b->sites[4 * s];
+        gpos[s] = make_float4((float)(x[0] + off[0]), (float)(x[1] + off[1]),
+                              (float)(x[2] + off[2]), (float)x[3]);
+      }
+    }
+    for (int a = 0; a < 3; ++a) {
+      c->grid_lo[a] = 0.0;
+      c->grid_hi[a] = stride[a] * (a == 0 ? side : (a == 1 ? std::min(side, (nm + side - 1) / side)
+                                                          : (nm + side * side - 1) / (side * side)));
+    }
     BCK(c->site_range.ensure((size_t)n_site), "alloc");
     BCK(cudaMemcpy(c->site_range.ptr, range.data(), sizeof(int2) * range.size(),
                    cudaMemcpyHostToDevice), "H2D ranges");
+    BCK(c->site_gridpos.ensure((size_t)n_site), "alloc");
+    BCK(cudaMemcpy(c->site_gridpos.ptr, gpos.data(), sizeof(float4) * gpos.size(),
+                   cudaMemcpyHostToDevice), "H2D grid positions");
     c->has_site_range = true;
   }
   const int k = c->cfg.knn_k;
@@ -519,14 +549,14 @@ rpd_status rpd_batch_compute(rpd_batch* b, rpd_stats* stats) {
   const bool exact = c->cfg.exact_lists != 0;
   if (exact) {
     const int n_site = c->n_site;
-    const Grid g = rpd_make_grid(c->site_lo, c->site_hi, n_site, 2.0);
+    const Grid g = rpd_make_grid(c->grid_lo, c->grid_hi, n_site, 2.0);
     const long long nc = (long long)g.nx * g.ny * g.nz;
     BCK(c->s_cell_count.ensure((size_t)nc), "alloc");
     BCK(c->s_cell_start.ensure((size_t)nc + 1), "alloc");
     BCK(c->s_cell_fill.ensure((size_t)nc), "alloc");
     BCK(c->s_cell_items.ensure((size_t)n_site), "alloc");
     BCK(c->scan_tmp.ensure(scan_temp_ints(std::max<long long>(nc, n_site)) + 16), "alloc");
-    BCK(grid_build_sites(c->site4f.ptr, n_site, g, c->s_cell_of.ptr, c->s_cell_count.ptr,
+    BCK(grid_build_sites(c->site_gridpos.ptr, n_site, g, c->s_cell_of.ptr, c->s_cell_count.ptr,
                          c->s_cell_start.ptr, c->s_cell_fill.ptr, c->s_cell_items.ptr,
                          c->scan_tmp.ptr, st), "site grid");
   }

@@ -130,6 +130,10 @@ struct rpd_ctx {
   // exact-lists rounds search the whole-context site grid with it
   DevBuf<int2> site_range;
   bool has_site_range = false;
+  // per site: its place in the exact-lists rounds' site grid (a batch: its
+  // mesh moved to a slot of its own), over [grid_lo, grid_hi]
+  DevBuf<float4> site_gridpos;
+  double grid_lo[3] = {0, 0, 0}, grid_hi[3] = {0, 0, 0};
   // exact lists (rpd_config.exact_lists): the completeness bound of every
   // base list, and the longer lists given to sites whose cells a pass left
   // uncertified -- row r of the extended lists starts at ext_off[r]

@@ -214,6 +214,11 @@ struct KnnArgs {
   // per site: the ids [x, y) it may list (its mesh's sites in a batch), or
   // null for every site
   const int2* site_range;
+  // per site: where the grid holds it, or null (its position).  A batch
+  // moves each mesh to a slot of its own in the grid's space; keys use the
+  // real positions, and a mesh moves as a whole, so distances within it
+  // are kept
+  const float4* grid_pos;
 };
 int knn_max_k();
 cudaError_t launch_knn(const KnnArgs& a, cudaStream_t st);

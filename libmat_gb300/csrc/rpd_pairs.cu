@@ -351,9 +351,10 @@ __global__ void __launch_bounds__(WARPS * 32) knn_kernel(KnnArgs a) {
     B = R * a.bound_scale + a.bound_abs;
     if (!(B < INFINITY)) B = INFINITY;  // inf or nan radius: no bound
   }
-  const int cx = clampi((int)floorf((si.x - g.lo.x) * g.inv_cell), 0, g.nx - 1);
-  const int cy = clampi((int)floorf((si.y - g.lo.y) * g.inv_cell), 0, g.ny - 1);
-  const int cz = clampi((int)floorf((si.z - g.lo.z) * g.inv_cell), 0, g.nz - 1);
+  const float4 gp = a.grid_pos ? a.grid_pos[i] : si;
+  const int cx = clampi((int)floorf((gp.x - g.lo.x) * g.inv_cell), 0, g.nx - 1);
+  const int cy = clampi((int)floorf((gp.y - g.lo.y) * g.inv_cell), 0, g.ny - 1);
+  const int cz = clampi((int)floorf((gp.z - g.lo.z) * g.inv_cell), 0, g.nz - 1);
   const int rmax = max(max(max(cx, g.nx - 1 - cx), max(cy, g.ny - 1 - cy)), max(cz, g.nz - 1 - cz));
   if (lane == 0) scnt[wid] = 0;
   __syncwarp();
