@@ -978,7 +978,7 @@ rpd_status rpd_compute(rpd_ctx* c, rpd_stats* stats) {
       CK(cudaMemsetAsync(c->scratch.ptr + 20, 0, 6 * sizeof(unsigned long long), st), "memset");
       for (int cl = 0; cl < rpd_ctx::kClasses; ++cl) {
         if (c->class_count[cl] == 0) continue;
-        Grid tg = make_grid(c->mesh_lo, c->mesh_hi, c->class_count[cl], 4.0);
+        Grid tg = make_grid(c->mesh_lo, c->mesh_hi, c->class_count[cl], kTetsPerCell);
         long long nc = (long long)tg.nx * tg.ny * tg.nz;
         CK(c->t_cell_count.ensure(nc), "alloc");
         CK(c->t_cell_rmax.ensure(nc), "alloc");

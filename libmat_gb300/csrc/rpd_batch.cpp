@@ -195,7 +195,7 @@ rpd_status upload(rpd_batch* b) {
       max_sc = std::max<long long>(max_sc, (long long)m.site_grid.nx * m.site_grid.ny * m.site_grid.nz);
       for (int cl = 0; cl < 2; ++cl) {
         if (m.class_count[cl] == 0) continue;
-        m.tet_grid[cl] = rpd_make_grid(m.mesh_lo, m.mesh_hi, m.class_count[cl], 4.0);
+        m.tet_grid[cl] = rpd_make_grid(m.mesh_lo, m.mesh_hi, m.class_count[cl], kTetsPerCell);
         const Grid& g = m.tet_grid[cl];
         max_tc = std::max<long long>(max_tc, (long long)g.nx * g.ny * g.nz);
       }
