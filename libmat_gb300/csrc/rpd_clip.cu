@@ -474,25 +474,23 @@ __device__ __forceinline__ uint8_t edge_adj(const WarpCell& c, int a, int b) {
 }
 
 // Adds plane e (already written to slot nb_p by the caller) and applies the
-// clip whose conflicting vertex slots are in mask[3].  Lane 0 only.
-// FULL: reference bookkeeping (edges, adjacency counts, perturb check);
-// otherwise only the polytope (box clipping for the candidate filter).
-template <bool FULL>
-__device__ void apply_clip(WarpCell& c, CellState& s, const uint32_t* mask_in) {
+// clip whose conflicting vertex slots are in mask[3], by lane 0, for the box
+// kernel: only the polytope (no edges, adjacency counts or perturbation
+// check; the cell kernel's update is clip_full, by the whole warp).
+__device__ void apply_clip_box(WarpCell& c, CellState& s, const uint32_t* mask_in) {
   // conflict bits of vertex slots 0..95 in registers (32-bit words)
   uint32_t m0 = mask_in[0], m1 = mask_in[1], m2 = mask_in[2];
   const int cur = s.nb_p;
   s.nb_p++;
-  // conflict partition, exactly the reference's swap-to-tail loop.  Only the
-  // dual triangles move here; perm records where each slot's vertex came
-  // from, and the warp moves the cofactors afterwards (the conflict bit of
-  // a slot at or past the shrinking end is never read again)
+  // conflict partition, the reference's swap-to-tail loop.  Only the dual
+  // triangles move here; perm records where each slot's vertex came from,
+  // and the warp moves the cofactors afterwards (the conflict bit of a slot
+  // at or past the shrinking end is never read again)
   int nb_v = s.nb_v, nb_r = 0, i = 0;
   while (i < nb_v) {
-    // box kernel: the next conflicting slot from i on (the loop would step
-    // over the others one at a time; bits at or past nb_v are stale and end
-    // it).  Measured slower in the cell kernel, faster in the box kernel.
-    if (!FULL) {
+    // the next conflicting slot from i on (bits at or past nb_v are stale
+    // and end the loop)
+    {
       uint32_t w = i < 32 ? m0 : (i < 64 ? m1 : m2);
       w &= ~0u << (i & 31);
       int base = i & ~31;
@@ -510,21 +508,9 @@ __device__ void apply_clip(WarpCell& c, CellState& s, const uint32_t* mask_in) {
       const uchar4 tv = c.ver[i];
       c.ver[i] = c.ver[nb_v];
       c.ver[nb_v] = tv;
-      if (FULL) {  // cell kernel: the cofactors move with the triangle
-        const float4 k = c.u.f.K[i];
-        c.u.f.K[i] = c.u.f.K[nb_v];
-        c.u.f.K[nb_v] = k;
-        const float4 mm = c.u.f.M[i];
-        c.u.f.M[i] = c.u.f.M[nb_v];
-        c.u.f.M[nb_v] = mm;
-        const float r = c.u.f.rad[i];
-        c.u.f.rad[i] = c.u.f.rad[nb_v];
-        c.u.f.rad[nb_v] = r;
-      } else {  // box kernel: the warp moves them afterwards (perm)
-        const uint8_t pv = c.perm[i];
-        c.perm[i] = c.perm[nb_v];
-        c.perm[nb_v] = pv;
-      }
+      const uint8_t pv = c.perm[i];
+      c.perm[i] = c.perm[nb_v];
+      c.perm[nb_v] = pv;
       const uint32_t wn = nb_v < 32 ? m0 : (nb_v < 64 ? m1 : m2);
       const uint32_t bit = 1u << (i & 31);
       const uint32_t nw = ((wn >> (nb_v & 31)) & 1u) ? (wi | bit) : (wi & ~bit);
@@ -556,54 +542,17 @@ __device__ void apply_clip(WarpCell& c, CellState& s, const uint32_t* mask_in) {
   }
   if (s.status != kSuccess) return;
   if (first == kEnd) return;
-  const uint8_t hcur = c.h[cur];
-  if (FULL) {
-    int cir = first;
-    do {
-      if (s.nb_e >= kMaxE) {
-        s.status = kEdgeOverflow;
-        return;
-      }
-      // cur > cir: the new plane has the largest index
-      const uint8_t hb = c.h[cir];
-      c.edge[s.nb_e] = make_uchar4((uint8_t)cir, (uint8_t)cur, hcur > hb ? hcur : hb, 0);
-      s.nb_e++;
-      cir = c.bnext[cir];
-    } while (cir != first);
-  }
-  // new vertices around the cavity boundary; the planes and face counts of
-  // consecutive boundary planes carry over from one step to the next
-  const float4 pcur = c.pl[cur];
+  // new vertices around the cavity boundary
   int cir = first;
-  float4 pcir = c.pl[cir];
-  uint8_t hcir = c.h[cir];
   do {
     const int nx = c.bnext[cir];
-    const float4 pnx = c.pl[nx];
-    const uint8_t hnx = c.h[nx];
     if (s.nb_v + 1 >= kMaxT) {
       s.status = kTriangleOverflow;
-    } else {
-      uint8_t adj = 0;
-      if (FULL) {
-        // max of the counts of the vertex's three edges (edge_adj): the two
-        // edges on the new plane have max(h_cur, h_other); the third is a
-        // tet edge (its own count) when both its planes are tet faces
-        adj = hcur > hcir ? hcur : hcir;
-        if (hnx > adj) adj = hnx;
-        if (cir < 4 && nx < 4) {
-          const uint8_t te = c.edge[cTetEdgeSlot[cir][nx]].z;
-          if (te > adj) adj = te;
-        }
-      }
-      c.ver[s.nb_v] = make_uchar4((uint8_t)cur, (uint8_t)cir, (uint8_t)nx, adj);
-      s.nb_v++;
+      return;
     }
-    if (FULL && det3x3_f(pcur, pcir, pnx) == 0.f) s.status = kNeedsPerturb;
-    if (s.status != kSuccess) return;
+    c.ver[s.nb_v] = make_uchar4((uint8_t)cur, (uint8_t)cir, (uint8_t)nx, 0);
+    s.nb_v++;
     cir = nx;
-    pcir = pnx;
-    hcir = hnx;
   } while (cir != first);
 }
 
@@ -629,11 +578,6 @@ __device__ __forceinline__ uint64_t shfl64(uint64_t v, int src) {
   return ((uint64_t)hi << 32) | lo;
 }
 
-// ------------------------------------------------------------------------
-// the neighbour loop shared by the cell kernel and the box kernel
-// ------------------------------------------------------------------------
-// make_plane(j) builds the plane of list entry j (bisector, or offset
-// bisector for the box kernel).
 // ------------------------------------------------------------------------
 // security-radius certificate (lists in ascending bisector distance)
 // ------------------------------------------------------------------------
@@ -1097,7 +1041,7 @@ __device__ void clip_list(WarpCell& c, CellState& s, const int32_t* list, int k,
         c.pl[cur] = e;
         c.h[cur] = 1;
         c.id2[cur] = make_int2(seed_id < jn ? seed_id : jn, seed_id < jn ? jn : seed_id);
-        apply_clip<FULL>(c, s, mask);
+        apply_clip_box(c, s, mask);
       }
       __syncwarp();
       broadcast_state(s);
