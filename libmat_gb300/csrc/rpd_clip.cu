@@ -395,21 +395,8 @@ __device__ __forceinline__ bool in_conflict(const WarpCell& c, int vi, float4 e,
 }
 
 // ------------------------------------------------------------------------
-// sequential topology update, run by lane 0 (convex_cell.cu:618-774)
+// topology update (convex_cell.cu:618-774)
 // ------------------------------------------------------------------------
-__device__ __forceinline__ bool getbit(const uint32_t* m, int i) {
-  return (m[i >> 5] >> (i & 31)) & 1u;
-}
-__device__ __forceinline__ void putbit(uint32_t* m, int i, bool b) {
-  uint32_t bit = 1u << (i & 31);
-  m[i >> 5] = b ? (m[i >> 5] | bit) : (m[i >> 5] & ~bit);
-}
-
-
-__device__ __forceinline__ uint8_t tri_plane(const uchar4& t, int e) {
-  return e == 0 ? t.x : (e == 1 ? t.y : t.z);
-}
-
 // cavity boundary as a circular list over plane ids (convex_cell.cu:618-678)
 // (bnext must be all kEnd on entry; the warp clears it before lane 0 runs)
 __device__ void compute_boundary(WarpCell& c, int nb_v, int& nb_r, int& first,
@@ -457,20 +444,6 @@ __device__ void compute_boundary(WarpCell& c, int nb_v, int& nb_r, int& first,
     t = nb_v;
     nb_r--;
   }
-}
-
-// #adjacent cells of the edge between planes a and b.  The reference looks
-// the edge up in the cell's edge list (find_edge_id, convex_cell.cu:511-522)
-// and reads its count; that count is fixed when the edge is created: the
-// tet's own count for the six initial edges (both planes are tet faces,
-// convex_cell.cu:193-211) and max(h_a, h_b) for every edge made by new_edge
-// (:604-616).  Two existing planes never become adjacent later (a clip only
-// adds adjacencies to the new plane), so every edge queried by new_vertex
-// exists exactly once and its count follows from the two plane ids.
-__device__ __forceinline__ uint8_t edge_adj(const WarpCell& c, int a, int b) {
-  if (a < 4 && b < 4) return c.edge[cTetEdgeSlot[a][b]].z;
-  uint8_t ha = c.h[a], hb = c.h[b];
-  return ha > hb ? ha : hb;
 }
 
 // Adds plane e (already written to slot nb_p by the caller) and applies the
@@ -562,14 +535,6 @@ __device__ __forceinline__ void broadcast_state(CellState& s) {
   s.nb_e = __shfl_sync(0xffffffffu, s.nb_e, 0);
   s.status = __shfl_sync(0xffffffffu, s.status, 0);
   s.kept = __shfl_sync(0xffffffffu, s.kept, 0);
-}
-
-__device__ __forceinline__ float4 shfl4(float4 v, int src) {
-  v.x = __shfl_sync(0xffffffffu, v.x, src);
-  v.y = __shfl_sync(0xffffffffu, v.y, src);
-  v.z = __shfl_sync(0xffffffffu, v.z, src);
-  v.w = __shfl_sync(0xffffffffu, v.w, src);
-  return v;
 }
 
 __device__ __forceinline__ uint64_t shfl64(uint64_t v, int src) {
@@ -904,7 +869,12 @@ __device__ __forceinline__ void clip_full(WarpCell& c, CellState& s, const uint3
     const uint8_t hcir = c.h[cir], hnx = c.h[nx];
     // cur > cir: the new plane has the largest index
     c.edge[nb_e + k] = make_uchar4((uint8_t)cir, (uint8_t)cur, hcur > hcir ? hcur : hcir, 0);
-    // the largest count of the vertex's three edges (edge_adj)
+    // the largest count of the vertex's three edges.  The reference looks
+    // each edge up in the cell's edge list (find_edge_id,
+    // convex_cell.cu:511-522); an edge's count is fixed when it is made: the
+    // tet's own count for the six initial edges (convex_cell.cu:193-211),
+    // max(h_a, h_b) for every edge made by new_edge (:604-616), and two
+    // existing planes never become adjacent later
     uint8_t adj = hcur > hcir ? hcur : hcir;
     if (hnx > adj) adj = hnx;
     if (cir < 4 && nx < 4) {

@@ -572,6 +572,8 @@ __global__ void __launch_bounds__(kPairWarps * 32) pairs_kernel(PairParams p,
   // queued tets: vertices (12 floats), power distances to the site (4), id
   __shared__ float sq_v[kPairWarps][16][kRuleQueue];
   __shared__ int sq_t[kPairWarps][kRuleQueue];
+  // tets whose centroid passed, waiting for the rule's first part
+  __shared__ int sa_t[kPairWarps][kRuleQueue];
   // every 8th neighbour r: its key and the smallest site distance |c_m - c_i|
   // (rounded down) of the neighbours from r on
   __shared__ float schk_key[kPairWarps][kPairMaxK / 8];
@@ -764,53 +766,43 @@ __global__ void __launch_bounds__(kPairWarps * 32) pairs_kernel(PairParams p,
       __syncwarp();
       qn = rest;
     };
-    for_items(n_iter, cell_at, p.tcell_start, p.tcell_items, lane, [&](int t, bool valid) {
+    // the first n tets of the centroid queue, one per lane: their vertices,
+    // power distances and the rule's first kRuleFirst neighbours; survivors
+    // join the drain's queue (qn <= 31 before, so there is room for 32)
+    int* qa_t = sa_t[wid];
+    int qa = 0;  // tets in the centroid queue (warp-uniform)
+    auto first_part = [&](int n) {
       bool pass = false, survive = false;
       float3 v[4] = {};
       float pdi[4] = {};
-      if (valid) {
-        ++n_items;
-        float4 c = p.centroid[t];
-        bool in = c.x >= blo.x && c.x <= bhi.x && c.y >= blo.y && c.y <= bhi.y &&
-                  c.z >= blo.z && c.z <= bhi.z;
-        // A tet passes the rule for neighbour m only if a vertex lies on the
-        // site's side of their bisector, so its centroid lies within the
-        // tet's own radius of it: the planes were pushed out by the class's
-        // largest radius, and each test takes back (R - r_t) |n|, r_t the
-        // tet's radius (c.w, a float square root) rounded up and |n| rounded
-        // down so that the test only ever accepts more than the exact one
-        const float shrink = fmaxf(p.offset_r - (c.w * (1.0f + 1e-5f) + 1e-6f * p.coord_scale), 0.f);
-        for (int q = 0; q < npl && in; ++q) {
-          float4 e = pl[q];
-          in = e.x * c.x + e.y * c.y + e.z * c.z + e.w - shrink * pn[q] >= 0.f;
+      int t = -1;
+      if (lane < n) {
+        t = qa_t[lane];
+        const float4 q0 = __ldg(p.tet_xyz + 3ll * t), q1 = __ldg(p.tet_xyz + 3ll * t + 1),
+                     q2 = __ldg(p.tet_xyz + 3ll * t + 2);
+        v[0] = make_float3(q0.x, q0.y, q0.z);
+        v[1] = make_float3(q0.w, q1.x, q1.y);
+        v[2] = make_float3(q1.z, q1.w, q2.x);
+        v[3] = make_float3(q2.y, q2.z, q2.w);
+        for (int a = 0; a < 4; ++a) pdi[a] = pow_dist(si, v[a]);
+        // voronoi.cu:154-193 (holes, -1, never reject: voronoi.cu:171):
+        // a candidate iff every neighbour m has a tet vertex where
+        // pd_m > pd_i; the order of the neighbours does not matter
+        pass = true;
+        for (int r = 0; r < min(p.k, kRuleFirst) && pass; ++r) {
+          const float4 sm = rule_site(r);
+          bool hit = false;
+          for (int a = 0; a < 4; ++a) hit |= pow_dist(sm, v[a]) > pdi[a];
+          pass = hit;
         }
-        if (in) {
-          ++n_in;
-          const float4 q0 = __ldg(p.tet_xyz + 3ll * t), q1 = __ldg(p.tet_xyz + 3ll * t + 1),
-                       q2 = __ldg(p.tet_xyz + 3ll * t + 2);
-          v[0] = make_float3(q0.x, q0.y, q0.z);
-          v[1] = make_float3(q0.w, q1.x, q1.y);
-          v[2] = make_float3(q1.z, q1.w, q2.x);
-          v[3] = make_float3(q2.y, q2.z, q2.w);
-          for (int a = 0; a < 4; ++a) pdi[a] = pow_dist(si, v[a]);
-          // voronoi.cu:154-193 (holes, -1, never reject: voronoi.cu:171):
-          // a candidate iff every neighbour m has a tet vertex where
-          // pd_m > pd_i; the order of the neighbours does not matter
-          pass = true;
-          for (int r = 0; r < min(p.k, kRuleFirst) && pass; ++r) {
-            const float4 sm = rule_site(r);
-            bool hit = false;
-            for (int a = 0; a < 4; ++a) hit |= pow_dist(sm, v[a]) > pdi[a];
-            pass = hit;
-          }
-          if (pass && p.k > kRuleFirst) {
-            survive = true;
-            pass = false;
-          }
+        if (pass && p.k > kRuleFirst) {
+          survive = true;
+          pass = false;
         }
       }
-      // (the whole warp from here) survivors join the queue: qn <= 31
-      // before, so there is room for 32 more
+      __syncwarp();  // every lane has read its entry
+      const int rest = qa - n;  // < 32: sources n.., targets 0.. do not overlap
+      if (lane < rest) qa_t[lane] = qa_t[n + lane];
       const uint32_t sv = __ballot_sync(0xffffffffu, survive);
       if (survive) {
         const int pos = qn + __popc(sv & ((1u << lane) - 1u));
@@ -825,8 +817,39 @@ __global__ void __launch_bounds__(kPairWarps * 32) pairs_kernel(PairParams p,
       qn += __popc(sv);
       emit(pass, t);
       __syncwarp();
+      qa = rest;
       if (qn >= 32) drain(32);
+    };
+    for_items(n_iter, cell_at, p.tcell_start, p.tcell_items, lane, [&](int t, bool valid) {
+      bool in = false;
+      if (valid) {
+        ++n_items;
+        float4 c = p.centroid[t];
+        in = c.x >= blo.x && c.x <= bhi.x && c.y >= blo.y && c.y <= bhi.y && c.z >= blo.z &&
+             c.z <= bhi.z;
+        // A tet passes the rule for neighbour m only if a vertex lies on the
+        // site's side of their bisector, so its centroid lies within the
+        // tet's own radius of it: the planes were pushed out by the class's
+        // largest radius, and each test takes back (R - r_t) |n|, r_t the
+        // tet's radius (c.w, a float square root) rounded up and |n| rounded
+        // down so that the test only ever accepts more than the exact one
+        const float shrink = fmaxf(p.offset_r - (c.w * (1.0f + 1e-5f) + 1e-6f * p.coord_scale), 0.f);
+        for (int q = 0; q < npl && in; ++q) {
+          float4 e = pl[q];
+          in = e.x * c.x + e.y * c.y + e.z * c.z + e.w - shrink * pn[q] >= 0.f;
+        }
+        if (in) ++n_in;
+      }
+      // (the whole warp from here) the tets that passed join the centroid
+      // queue: qa <= 31 before, so there is room for 32 more; the rule's
+      // first part then runs on full warps
+      const uint32_t ia = __ballot_sync(0xffffffffu, in);
+      if (in) qa_t[qa + __popc(ia & ((1u << lane) - 1u))] = t;
+      qa += __popc(ia);
+      __syncwarp();
+      if (qa >= 32) first_part(32);
     });
+    if (qa > 0) first_part(qa);
     if (qn > 0) drain(qn);
   }
   if (p.diag) {
