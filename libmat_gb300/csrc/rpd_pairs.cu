@@ -676,10 +676,12 @@ __global__ void __launch_bounds__(kPairWarps * 32) pairs_kernel(PairParams p,
       float cxm = g.lo.x + ((float)x + 0.5f) * g.cell;
       float cym = g.lo.y + ((float)y + 0.5f) * g.cell;
       float czm = g.lo.z + ((float)z + 0.5f) * g.cell;
+      // (the culling tests use FMA: one rounding per term, well inside the
+      // planes' loosening; the rule itself keeps the reference's order)
       for (int q = 0; q < npl; ++q) {
         float4 e = pl[q];
-        float best = e.x * cxm + e.y * cym + e.z * czm + e.w +
-                     hc * (fabsf(e.x) + fabsf(e.y) + fabsf(e.z));
+        float best = __fmaf_rn(e.x, cxm, __fmaf_rn(e.y, cym, __fmaf_rn(e.z, czm,
+                     __fmaf_rn(hc, fabsf(e.x) + fabsf(e.y) + fabsf(e.z), e.w))));
         if (best < 0.f) return -1;
       }
       const int cell = x + g.nx * (y + g.ny * z);
@@ -692,8 +694,9 @@ __global__ void __launch_bounds__(kPairWarps * 32) pairs_kernel(PairParams p,
         if (shrink > 0.f) {
           for (int q = 0; q < npl; ++q) {
             float4 e = pl[q];
-            float best = e.x * cxm + e.y * cym + e.z * czm + e.w +
-                         hc * (fabsf(e.x) + fabsf(e.y) + fabsf(e.z)) - shrink * pn[q];
+            float best = __fmaf_rn(e.x, cxm, __fmaf_rn(e.y, cym, __fmaf_rn(e.z, czm,
+                         __fmaf_rn(hc, fabsf(e.x) + fabsf(e.y) + fabsf(e.z),
+                                   __fmaf_rn(-shrink, pn[q], e.w)))));
             if (best < 0.f) return -1;
           }
         }
@@ -836,7 +839,8 @@ __global__ void __launch_bounds__(kPairWarps * 32) pairs_kernel(PairParams p,
         const float shrink = fmaxf(p.offset_r - (c.w * (1.0f + 1e-5f) + 1e-6f * p.coord_scale), 0.f);
         for (int q = 0; q < npl && in; ++q) {
           float4 e = pl[q];
-          in = e.x * c.x + e.y * c.y + e.z * c.z + e.w - shrink * pn[q] >= 0.f;
+          in = __fmaf_rn(e.x, c.x, __fmaf_rn(e.y, c.y, __fmaf_rn(e.z, c.z,
+               __fmaf_rn(-shrink, pn[q], e.w)))) >= 0.f;
         }
         if (in) ++n_in;
       }
