@@ -618,6 +618,13 @@ __global__ void __launch_bounds__(kPairWarps * 32) pairs_kernel(PairParams p,
       const int n_zero = (e.x == 0.f) + (e.y == 0.f) + (e.z == 0.f);
       pn[q] = n_zero >= 2 ? 0.f : sqrtf(e.x * e.x + e.y * e.y + e.z * e.z) * (1.0f - 1e-5f);
     }
+    // the tests take the planes two at a time: an odd count gets a plane
+    // that every point passes (kBoxPlanes is even, so the slot exists)
+    static_assert(kBoxPlanes % 2 == 0, "plane pairs");
+    if (lane == 0 && (npl & 1)) {
+      pl[npl] = make_float4(0.f, 0.f, 0.f, 1.f);
+      pn[npl] = 0.f;
+    }
     __syncwarp();
     const float4 si = p.site4f[p.site_base + i];
     const Grid& g = p.tg;
@@ -678,12 +685,12 @@ __global__ void __launch_bounds__(kPairWarps * 32) pairs_kernel(PairParams p,
       float czm = g.lo.z + ((float)z + 0.5f) * g.cell;
       // (the culling tests use FMA: one rounding per term, well inside the
       // planes' loosening; the rule itself keeps the reference's order)
-      for (int q = 0; q < npl; ++q) {
-        float4 e = pl[q];
-        float best = __fmaf_rn(e.x, cxm, __fmaf_rn(e.y, cym, __fmaf_rn(e.z, czm,
-                     __fmaf_rn(hc, fabsf(e.x) + fabsf(e.y) + fabsf(e.z), e.w))));
-        if (best < 0.f) return -1;
-      }
+      auto box_max = [&](float4 e, float off) {
+        return __fmaf_rn(e.x, cxm, __fmaf_rn(e.y, cym, __fmaf_rn(e.z, czm,
+               __fmaf_rn(hc, fabsf(e.x) + fabsf(e.y) + fabsf(e.z), e.w - off))));
+      };
+      for (int q = 0; q < npl; q += 2)
+        if ((box_max(pl[q], 0.f) < 0.f) | (box_max(pl[q + 1], 0.f) < 0.f)) return -1;
       const int cell = x + g.nx * (y + g.ny * z);
       // again with the cell's largest tet radius in place of the class's
       // (the centroid test below, applied to the best centroid in the cell)
@@ -692,13 +699,9 @@ __global__ void __launch_bounds__(kPairWarps * 32) pairs_kernel(PairParams p,
             fmaxf(p.offset_r - (__ldg(p.tcell_rmax + cell) * (1.0f + 1e-5f) + 1e-6f * p.coord_scale),
                   0.f);
         if (shrink > 0.f) {
-          for (int q = 0; q < npl; ++q) {
-            float4 e = pl[q];
-            float best = __fmaf_rn(e.x, cxm, __fmaf_rn(e.y, cym, __fmaf_rn(e.z, czm,
-                         __fmaf_rn(hc, fabsf(e.x) + fabsf(e.y) + fabsf(e.z),
-                                   __fmaf_rn(-shrink, pn[q], e.w)))));
-            if (best < 0.f) return -1;
-          }
+          for (int q = 0; q < npl; q += 2)
+            if ((box_max(pl[q], shrink * pn[q]) < 0.f) | (box_max(pl[q + 1], shrink * pn[q + 1]) < 0.f))
+              return -1;
         }
       }
       ++n_keep;
@@ -837,11 +840,12 @@ __global__ void __launch_bounds__(kPairWarps * 32) pairs_kernel(PairParams p,
         // tet's radius (c.w, a float square root) rounded up and |n| rounded
         // down so that the test only ever accepts more than the exact one
         const float shrink = fmaxf(p.offset_r - (c.w * (1.0f + 1e-5f) + 1e-6f * p.coord_scale), 0.f);
-        for (int q = 0; q < npl && in; ++q) {
-          float4 e = pl[q];
-          in = __fmaf_rn(e.x, c.x, __fmaf_rn(e.y, c.y, __fmaf_rn(e.z, c.z,
-               __fmaf_rn(-shrink, pn[q], e.w)))) >= 0.f;
-        }
+        auto side = [&](int q) {
+          const float4 e = pl[q];
+          return __fmaf_rn(e.x, c.x, __fmaf_rn(e.y, c.y, __fmaf_rn(e.z, c.z,
+                 __fmaf_rn(-shrink, pn[q], e.w))));
+        };
+        for (int q = 0; q < npl && in; q += 2) in = (side(q) >= 0.f) & (side(q + 1) >= 0.f);
         if (in) ++n_in;
       }
       // (the whole warp from here) the tets that passed join the centroid
