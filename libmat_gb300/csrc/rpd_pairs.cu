@@ -525,6 +525,9 @@ constexpr int kPairMaxK = 128;  // longest neighbour list (rpd_config.knn_k <= 1
 #define RPD_RULE_FIRST 8
 #endif
 constexpr int kRuleFirst = RPD_RULE_FIRST;
+// (even: the drain steps two neighbours at a time from kRuleFirst, and its
+// acceptance checkpoints sit at multiples of 8)
+static_assert(kRuleFirst % 2 == 0, "kRuleFirst even");
 constexpr int kRuleQueue = 64;
 
 // cell range of the site's box in the tet grid (empty range for no box)
@@ -746,7 +749,7 @@ __global__ void __launch_bounds__(kPairWarps * 32) pairs_kernel(PairParams p,
           m2 = fminf(m2, dx * dx + dy * dy + dz * dz);
         }
         const float d_up = sqrtf(m2) * (1.0f + 1e-6f);
-        for (int r = kRuleFirst; r < p.k && pass; ++r) {
+        for (int r = kRuleFirst; r < p.k && pass; r += 2) {
           // pd_m(v) - pd_i(v) = 2 |c_m - c_i| (key_m - (v - c_i).u_m) for the
           // unit direction u_m to m: a vertex within key_m of the site,
           // by more than the float error of the two power distances, has
@@ -756,10 +759,16 @@ __global__ void __launch_bounds__(kPairWarps * 32) pairs_kernel(PairParams p,
                             p.accept_margin - d_up;
             if (g > 0.f && 2.0f * schk_d[wid][r >> 3] * g > p.accept_err) break;
           }
-          const float4 sm = rule_site(r);
-          bool hit = false;
-          for (int a = 0; a < 4; ++a) hit |= pow_dist(sm, v[a]) > pdi[a];
-          pass = hit;
+          // two neighbours per step (independent chains; the rule is an AND,
+          // so testing one past a failure changes nothing)
+          const float4 sm0 = rule_site(r);
+          const float4 sm1 = r + 1 < p.k ? rule_site(r + 1) : sm0;
+          bool hit0 = false, hit1 = false;
+          for (int a = 0; a < 4; ++a) {
+            hit0 |= pow_dist(sm0, v[a]) > pdi[a];
+            hit1 |= pow_dist(sm1, v[a]) > pdi[a];
+          }
+          pass = hit0 & hit1;
         }
       }
       emit(pass, t);
@@ -795,11 +804,16 @@ __global__ void __launch_bounds__(kPairWarps * 32) pairs_kernel(PairParams p,
         // a candidate iff every neighbour m has a tet vertex where
         // pd_m > pd_i; the order of the neighbours does not matter
         pass = true;
-        for (int r = 0; r < min(p.k, kRuleFirst) && pass; ++r) {
-          const float4 sm = rule_site(r);
-          bool hit = false;
-          for (int a = 0; a < 4; ++a) hit |= pow_dist(sm, v[a]) > pdi[a];
-          pass = hit;
+        const int r_end = min(p.k, kRuleFirst);
+        for (int r = 0; r < r_end && pass; r += 2) {
+          const float4 sm0 = rule_site(r);
+          const float4 sm1 = r + 1 < r_end ? rule_site(r + 1) : sm0;
+          bool hit0 = false, hit1 = false;
+          for (int a = 0; a < 4; ++a) {
+            hit0 |= pow_dist(sm0, v[a]) > pdi[a];
+            hit1 |= pow_dist(sm1, v[a]) > pdi[a];
+          }
+          pass = hit0 & hit1;
         }
         if (pass && p.k > kRuleFirst) {
           survive = true;
