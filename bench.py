@@ -964,29 +964,51 @@ def _e2e(args, cfg, adj, rpd, tuned):
     copy_bytes = h.nbytes + p.nbytes
     # ---- pipelined: two contexts, each driven by its own host thread (the
     # library's calls on one context never wait for another's).  Each step
-    # uploads, computes and queues its copy back; one context's copy and its
-    # host round trips overlap the other context's kernels
+    # uploads (after its context's previous copy has landed), computes and
+    # queues its copy back.  The computes take turns in step order: two
+    # contexts' kernels on one GPU time-slice rather than run side by side,
+    # so a step's upload and the previous step's copy back run while the
+    # other context computes
     import threading
 
     def run(first, n, timed):
-        out = [[0, 0, np.zeros(3)], [0, 0, np.zeros(3)]]  # cells, d2h bytes, parts
+        out = [[0, 0, np.zeros(4)], [0, 0, np.zeros(4)]]  # cells, d2h bytes, parts
         go = threading.Barrier(3)
+        turn = threading.Condition()
+        nxt = [first]  # the step whose compute goes next
+        errors = []
 
         def worker(e):
             r, hb, pb = engines[e]
-            go.wait()
-            for i in range(first + e, first + n, 2):
-                t0 = time.perf_counter()
-                r.set_mesh(v, t, va, e6, fa, fi)
-                r.set_sites(s, fl)
-                t1 = time.perf_counter()
-                st = r.compute()
-                t2 = time.perf_counter()
-                h, p = r.cells_async(hb.array, pb.array)
-                out[e][0] += st.n_cells
-                out[e][1] += h.nbytes + p.nbytes
-                out[e][2] += (t1 - t0, t2 - t1, st.ms_total / 1000.0)
-            r.synchronize()
+            try:
+                go.wait()
+                for i in range(first + e, first + n, 2):
+                    t0 = time.perf_counter()
+                    r.set_mesh(v, t, va, e6, fa, fi)
+                    r.set_sites(s, fl)
+                    t1 = time.perf_counter()
+                    with turn:
+                        if not turn.wait_for(lambda: nxt[0] == i or errors, timeout=300):
+                            raise RuntimeError("pipelined e2e: no turn for step %d" % i)
+                        if errors:
+                            return
+                    t2 = time.perf_counter()
+                    try:
+                        st = r.compute()
+                    finally:
+                        with turn:
+                            nxt[0] = i + 1
+                            turn.notify_all()
+                    t3 = time.perf_counter()
+                    h, p = r.cells_async(hb.array, pb.array)
+                    out[e][0] += st.n_cells
+                    out[e][1] += h.nbytes + p.nbytes
+                    out[e][2] += (t1 - t0, t2 - t1, t3 - t2, st.ms_total / 1000.0)
+                r.synchronize()
+            except BaseException as ex:  # the other worker stops at its next turn
+                with turn:
+                    errors.append(ex)
+                    turn.notify_all()
 
         ths = [threading.Thread(target=worker, args=(e,)) for e in (0, 1)]
         for th in ths:
@@ -995,14 +1017,20 @@ def _e2e(args, cfg, adj, rpd, tuned):
         t0 = time.perf_counter()
         for th in ths:
             th.join()
+        if errors:
+            raise errors[0]
         return time.perf_counter() - t0, out
 
     run(0, max(2, args.warmup), False)
     flush_l2()
-    secs, out = run(args.warmup, args.steps, True)
+    # a pipeline fills (the first upload) and drains (the last copy back)
+    # outside any overlap: at least 16 steps, so that these two ends weigh
+    # little against the steady state
+    n_pipe = max(args.steps, 16)
+    secs, out = run(args.warmup, n_pipe, True)
     cells = out[0][0] + out[1][0]
     d2h_total = out[0][1] + out[1][1]
-    pparts = out[0][2] + out[1][2]
+    pparts = (out[0][2] + out[1][2]) / n_pipe
     for r, hb, pb in engines:
         r.close()
         hb.free()
@@ -1010,13 +1038,12 @@ def _e2e(args, cfg, adj, rpd, tuned):
     for pa in pins.values():
         pa.free()
     return {"value": cells / secs, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-            "d2h_bytes_per_step": int(d2h_total // args.steps),
-            "ms_per_step": 1000 * secs / args.steps,
-            "pipelined": "2 contexts, one host thread each",
+            "d2h_bytes_per_step": int(d2h_total // n_pipe),
+            "ms_per_step": 1000 * secs / n_pipe, "steps": n_pipe,
+            "pipelined": "2 contexts, one host thread each, computes in turn",
             "l2": "not flushed between pipelined steps: each writes 1.7 GB of cells (> 129 MB)",
-            "parts_ms": {"upload": 1000 * pparts[0] / args.steps,
-                         "compute_wall": 1000 * pparts[1] / args.steps,
-                         "compute_device": 1000 * pparts[2] / args.steps},
+            "parts_ms": {"upload": 1000 * pparts[0], "wait_turn": 1000 * pparts[1],
+                         "compute_wall": 1000 * pparts[2], "compute_device": 1000 * pparts[3]},
             "serial": {"value": serial_cells / serial_secs,
                        "ms_per_step": 1000 * serial_secs / args.steps,
                        "upload_ms": 1000 * parts[0] / args.steps,
