@@ -964,11 +964,11 @@ def _e2e(args, cfg, adj, rpd, tuned):
     copy_bytes = h.nbytes + p.nbytes
     # ---- pipelined: two contexts, each driven by its own host thread (the
     # library's calls on one context never wait for another's).  Each step
-    # uploads (after its context's previous copy has landed), computes and
-    # queues its copy back.  The computes take turns in step order: two
-    # contexts' kernels on one GPU time-slice rather than run side by side,
-    # so a step's upload and the previous step's copy back run while the
-    # other context computes
+    # uploads, computes and queues its copy back.  Upload and compute take
+    # turns in step order: two contexts' kernels on one GPU time-slice rather
+    # than run side by side (rpd_set_mesh launches the mesh's preparation
+    # kernels too), so a step's copy back runs while the other context
+    # uploads and computes
     import threading
 
     def run(first, n, timed):
@@ -984,16 +984,16 @@ def _e2e(args, cfg, adj, rpd, tuned):
                 go.wait()
                 for i in range(first + e, first + n, 2):
                     t0 = time.perf_counter()
-                    r.set_mesh(v, t, va, e6, fa, fi)
-                    r.set_sites(s, fl)
-                    t1 = time.perf_counter()
                     with turn:
                         if not turn.wait_for(lambda: nxt[0] == i or errors, timeout=300):
                             raise RuntimeError("pipelined e2e: no turn for step %d" % i)
                         if errors:
                             return
-                    t2 = time.perf_counter()
+                    t1 = time.perf_counter()
                     try:
+                        r.set_mesh(v, t, va, e6, fa, fi)
+                        r.set_sites(s, fl)
+                        t2 = time.perf_counter()
                         st = r.compute()
                     finally:
                         with turn:
@@ -1040,9 +1040,9 @@ def _e2e(args, cfg, adj, rpd, tuned):
     return {"value": cells / secs, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
             "d2h_bytes_per_step": int(d2h_total // n_pipe),
             "ms_per_step": 1000 * secs / n_pipe, "steps": n_pipe,
-            "pipelined": "2 contexts, one host thread each, computes in turn",
+            "pipelined": "2 contexts, one host thread each, upload + compute in turn",
             "l2": "not flushed between pipelined steps: each writes 1.7 GB of cells (> 129 MB)",
-            "parts_ms": {"upload": 1000 * pparts[0], "wait_turn": 1000 * pparts[1],
+            "parts_ms": {"wait_turn": 1000 * pparts[0], "upload": 1000 * pparts[1],
                          "compute_wall": 1000 * pparts[2], "compute_device": 1000 * pparts[3]},
             "serial": {"value": serial_cells / serial_secs,
                        "ms_per_step": 1000 * serial_secs / args.steps,
