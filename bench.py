@@ -886,14 +886,72 @@ def _sample_topology_equal(h1, p1, h2, p2, n=20000):
     return True
 
 
+def pipelined_steps(first, n, upload, compute, copy_back, finish, n_ctx=2, timeout=300.0):
+    """Steps first .. first + n - 1 on n_ctx contexts, step i on context
+    (i - first) % n_ctx, each context driven by its own host thread.
+    upload(e) and compute(e) of the steps take turns in step order (two
+    contexts' kernels on one GPU time-slice rather than run side by side);
+    copy_back(e, compute's result) queues the step's copy back and returns
+    at once, so the copy runs while the next steps upload and compute;
+    finish(e) after a context's last step waits for its copies.  Returns the
+    wall time from the threads' start to the last finish and, per step,
+    (seconds waiting for the turn, uploading, computing, copy_back's value).
+    The first error of any thread stops the others at their next turn and is
+    raised here."""
+    go = threading.Barrier(n_ctx + 1)
+    turn = threading.Condition()
+    nxt = [first]  # the step whose turn it is
+    errors = []
+    records = {}
+
+    def worker(e):
+        try:
+            go.wait()
+            for i in range(first + e, first + n, n_ctx):
+                t0 = time.perf_counter()
+                with turn:
+                    if not turn.wait_for(lambda: nxt[0] == i or bool(errors), timeout=timeout):
+                        raise RuntimeError("pipelined steps: no turn for step %d" % i)
+                    if errors:
+                        return
+                t1 = time.perf_counter()
+                try:
+                    upload(e)
+                    t2 = time.perf_counter()
+                    res = compute(e)
+                finally:
+                    with turn:
+                        nxt[0] = i + 1
+                        turn.notify_all()
+                t3 = time.perf_counter()
+                records[i] = (t1 - t0, t2 - t1, t3 - t2, copy_back(e, res))
+            finish(e)
+        except BaseException as ex:
+            with turn:
+                errors.append(ex)
+                turn.notify_all()
+
+    ths = [threading.Thread(target=worker, args=(e,)) for e in range(n_ctx)]
+    for th in ths:
+        th.start()
+    go.wait()
+    t0 = time.perf_counter()
+    for th in ths:
+        th.join()
+    if errors:
+        raise errors[0]
+    return time.perf_counter() - t0, [records[i] for i in sorted(records)]
+
+
 def _e2e(args, cfg, adj, rpd, tuned):
     """The same metric through the C ABI with host buffers (page-locked): per
     step rpd_set_mesh + rpd_set_sites (host->device), rpd_compute, and the
     device->host copy of every cell.  Two contexts take the steps in turn,
-    each driven by its own host thread: a step's copy back
+    each driven by its own host thread, uploads and computes one after the
+    other (pipelined_steps): a step's copy back
     (rpd_copy_cells_to_host_async) and its host round trips overlap the
-    other context's kernels, and the timed region ends when the last step's
-    cells have landed.  No L2 flush between the steps: each step writes 1.7
+    other context's upload and kernels, and the timed region ends when the
+    last step's cells have landed.  No L2 flush between the steps: each step writes 1.7
     GB of cells (> 129 MB L2).  "serial" is one context with the blocking
     copy (rpd_copy_cells_to_host)."""
     nt, nv, ns = cfg["tets"].shape[0], cfg["vert3d"].shape[0], cfg["sites"].shape[0]
@@ -962,75 +1020,32 @@ def _e2e(args, cfg, adj, rpd, tuned):
         serial_secs += t3 - t0
         serial_cells += st.n_cells
     copy_bytes = h.nbytes + p.nbytes
-    # ---- pipelined: two contexts, each driven by its own host thread (the
-    # library's calls on one context never wait for another's).  Each step
-    # uploads, computes and queues its copy back.  Upload and compute take
-    # turns in step order: two contexts' kernels on one GPU time-slice rather
-    # than run side by side (rpd_set_mesh launches the mesh's preparation
-    # kernels too), so a step's copy back runs while the other context
-    # uploads and computes
-    import threading
+    # ---- pipelined (pipelined_steps): two contexts, one host thread each;
+    # a step's copy back runs while the other context uploads and computes
+    def run(first, n):
+        def upload(e):
+            r = engines[e][0]
+            r.set_mesh(v, t, va, e6, fa, fi)
+            r.set_sites(s, fl)
 
-    def run(first, n, timed):
-        out = [[0, 0, np.zeros(4)], [0, 0, np.zeros(4)]]  # cells, d2h bytes, parts
-        go = threading.Barrier(3)
-        turn = threading.Condition()
-        nxt = [first]  # the step whose compute goes next
-        errors = []
-
-        def worker(e):
+        def copy_back(e, st):
             r, hb, pb = engines[e]
-            try:
-                go.wait()
-                for i in range(first + e, first + n, 2):
-                    t0 = time.perf_counter()
-                    with turn:
-                        if not turn.wait_for(lambda: nxt[0] == i or errors, timeout=300):
-                            raise RuntimeError("pipelined e2e: no turn for step %d" % i)
-                        if errors:
-                            return
-                    t1 = time.perf_counter()
-                    try:
-                        r.set_mesh(v, t, va, e6, fa, fi)
-                        r.set_sites(s, fl)
-                        t2 = time.perf_counter()
-                        st = r.compute()
-                    finally:
-                        with turn:
-                            nxt[0] = i + 1
-                            turn.notify_all()
-                    t3 = time.perf_counter()
-                    h, p = r.cells_async(hb.array, pb.array)
-                    out[e][0] += st.n_cells
-                    out[e][1] += h.nbytes + p.nbytes
-                    out[e][2] += (t1 - t0, t2 - t1, t3 - t2, st.ms_total / 1000.0)
-                r.synchronize()
-            except BaseException as ex:  # the other worker stops at its next turn
-                with turn:
-                    errors.append(ex)
-                    turn.notify_all()
+            h, p = r.cells_async(hb.array, pb.array)
+            return st.n_cells, h.nbytes + p.nbytes, st.ms_total / 1000.0
 
-        ths = [threading.Thread(target=worker, args=(e,)) for e in (0, 1)]
-        for th in ths:
-            th.start()
-        go.wait()
-        t0 = time.perf_counter()
-        for th in ths:
-            th.join()
-        if errors:
-            raise errors[0]
-        return time.perf_counter() - t0, out
+        return pipelined_steps(first, n, upload, lambda e: engines[e][0].compute(), copy_back,
+                               lambda e: engines[e][0].synchronize())
 
-    run(0, max(2, args.warmup), False)
+    run(0, max(2, args.warmup))
     flush_l2()
     # a pipeline fills (the first upload) and drains (the last copy back)
     # outside any overlap: at least 16 steps, so that these two ends weigh
     # little against the steady state
     n_pipe = max(args.steps, 16)
-    secs, out = run(args.warmup, n_pipe, True)
-    cells = out[0][0] + out[1][0]
-    d2h_total = out[0][1] + out[1][1]
-    pparts = (out[0][2] + out[1][2]) / n_pipe
+    secs, recs = run(args.warmup, n_pipe)
+    cells = sum(rec[3][0] for rec in recs)
+    d2h_total = sum(rec[3][1] for rec in recs)
+    pparts = np.array([[rec[0], rec[1], rec[2], rec[3][2]] for rec in recs]).mean(axis=0)
     for r, hb, pb in engines:
         r.close()
         hb.free()
