@@ -516,11 +516,13 @@ __device__ __forceinline__ float pow_dist(float4 s, float3 v) {
 
 constexpr int kPairWarps = 4;
 constexpr int kPairMaxK = 128;  // longest neighbour list (rpd_config.knn_k <= 128)
-// the rule in two parts: each lane tries its own tet against the first
-// kRuleFirst neighbours; the tets that survive wait in a per-warp queue
-// (kRuleQueue entries) and are finished 32 at a time, one per lane
-// (8: 4 to 16 were measured on the 1M-tet workload, 8 the fastest; the
-// macro only serves such sweeps)
+// a tet goes through three stages, each on full warps: the centroid test
+// (one tet per lane); the tets that pass wait in a per-warp queue and try
+// the rule's first kRuleFirst neighbours 32 at a time; the tets that survive
+// those wait in a second queue and are finished 32 at a time against the
+// rest of the list (queues of kRuleQueue entries).  kRuleFirst: 4 to 16 were
+// measured on the 1M-tet workload, 8 the fastest; the macro only serves such
+// sweeps
 #ifndef RPD_RULE_FIRST
 #define RPD_RULE_FIRST 8
 #endif
